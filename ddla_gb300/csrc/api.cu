@@ -1,0 +1,620 @@
+// C ABI of libddla_gb300: handles, workspaces, host staging and the extern "C"
+// entry points declared in include/ddla_gb300.h.
+//
+// Host-pointer entry points replace DDLA's P/Invoke calls into BLIS
+// (DDLA/BLAS/Native/3m.cs:12-162) and its factorization classes
+// (DDLA/Factorizations/LU.cs, Cholesky.cs, LDLT.cs).  They validate arguments
+// the way DDLA's checked wrappers do (DDLA/BLAS/3m.cs:10-315: empty problems
+// return early, mismatched shapes are rejected), stage the strided host views
+// into device buffers, run the device implementation on the calling thread's
+// handle and copy results back before returning.
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+namespace ddla {
+
+std::atomic<int64_t> g_launches{0};
+static thread_local std::string t_error;
+void set_error(const std::string &msg) { t_error = msg; }
+
+int workspace(ddla_handle h, int slot, size_t bytes, void **out) {
+    Workspace &w = h->ws[slot];
+    if (w.bytes < bytes) {
+        if (w.ptr) {
+            cudaStreamSynchronize(h->stream);
+            cudaFree(w.ptr);
+            w.ptr = nullptr;
+            w.bytes = 0;
+        }
+        size_t want = bytes + bytes / 8 + 256;
+        if (cudaMalloc(&w.ptr, want) != cudaSuccess) {
+            cudaGetLastError();
+            set_error("device workspace allocation of " + std::to_string(want) + " bytes failed");
+            return DDLA_ERR_NOMEM;
+        }
+        w.bytes = want;
+    }
+    *out = w.ptr;
+    return 0;
+}
+
+int pinned(ddla_handle h, size_t bytes, void **out) {
+    if (h->pinned_bytes < bytes) {
+        if (h->pinned) {
+            cudaStreamSynchronize(h->stream);
+            cudaFreeHost(h->pinned);
+        }
+        h->pinned = nullptr;
+        h->pinned_bytes = 0;
+        if (cudaMallocHost(&h->pinned, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            set_error("pinned host allocation failed");
+            return DDLA_ERR_NOMEM;
+        }
+        h->pinned_bytes = bytes;
+    }
+    *out = h->pinned;
+    return 0;
+}
+
+int reset_info(ddla_handle h) {
+    static const int init[INFO_COUNT] = {INT32_MAX, 0, 0, 0};
+    DDLA_CUDA(cudaMemcpyAsync(h->d_info, init, sizeof(init), cudaMemcpyHostToDevice, h->stream));
+    return 0;
+}
+
+int read_info(ddla_handle h, int *pivot) {
+    int v[INFO_COUNT];
+    DDLA_CUDA(cudaMemcpyAsync(v, h->d_info, sizeof(v), cudaMemcpyDeviceToHost, h->stream));
+    DDLA_CUDA(cudaStreamSynchronize(h->stream));
+    *pivot = (v[INFO_PIVOT] == INT32_MAX) ? 0 : v[INFO_PIVOT];
+    if (v[INFO_TIMEOUT]) {
+        set_error("a bounded device-side wait gave up");
+        return DDLA_ERR_TIMEOUT;
+    }
+    return 0;
+}
+
+static int handle_init(ddla_handle h, void *stream) {
+    DDLA_CUDA(cudaGetDevice(&h->device));
+    cudaDeviceProp prop;
+    DDLA_CUDA(cudaGetDeviceProperties(&prop, h->device));
+    if (prop.major < 10) {
+        set_error(std::string("device ") + prop.name + " is not a Blackwell (sm_10x) GPU");
+        return DDLA_ERR_NO_DEVICE;
+    }
+    h->sm_count = prop.multiProcessorCount;
+    h->smem_optin = prop.sharedMemPerBlockOptin;
+    if (stream) {
+        h->stream = (cudaStream_t)stream;
+        h->own_stream = false;
+    } else {
+        DDLA_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+        h->own_stream = true;
+    }
+    DDLA_CUDA(cudaMalloc(&h->d_info, sizeof(int) * INFO_COUNT));
+    DDLA_CUDA(cudaEventCreate(&h->ev0));
+    DDLA_CUDA(cudaEventCreate(&h->ev1));
+    return reset_info(h);
+}
+
+static void handle_free(ddla_handle h) {
+    if (!h) return;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    for (auto &w : h->ws)
+        if (w.ptr) cudaFree(w.ptr);
+    if (h->pinned) cudaFreeHost(h->pinned);
+    if (h->d_info) cudaFree(h->d_info);
+    if (h->ev0) cudaEventDestroy(h->ev0);
+    if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+}
+
+int default_handle(ddla_handle *out) {
+    static thread_local ddla_handle t_handle = nullptr;
+    if (!t_handle) {
+        ddla_handle h = new ddla_handle_s();
+        int rc = handle_init(h, nullptr);
+        if (rc) {
+            handle_free(h);
+            return rc;
+        }
+        t_handle = h;
+    }
+    *out = t_handle;
+    return 0;
+}
+
+// ------------------------------------------------------------------ staging
+// A host view staged into a device buffer; the device copy keeps the host
+// orientation when one stride is 1 (2-D copies), else is packed row-major.
+struct Staged {
+    double *d = nullptr;
+    View<double> view{};
+};
+
+static bool rowwise(i64 rows, i64 cols, i64 rs, i64 cs) { return cs == 1 && (rows <= 1 || rs >= cols); }
+static bool colwise(i64 rows, i64 cols, i64 rs, i64 cs) { return rs == 1 && (cols <= 1 || cs >= rows); }
+
+static int stage_in(ddla_handle h, int slot, const double *hp, i64 rows, i64 cols, i64 rs, i64 cs, bool copy,
+                    Staged *out) {
+    size_t bytes = sizeof(double) * (size_t)(rows * cols > 0 ? rows * cols : 1);
+    void *d;
+    DDLA_TRY(workspace(h, slot, bytes, &d));
+    out->d = (double *)d;
+    if (rows == 0 || cols == 0) {
+        out->view = View<double>{out->d, rows, cols, cols, 1};
+        return 0;
+    }
+    if (rowwise(rows, cols, rs, cs)) {
+        out->view = View<double>{out->d, rows, cols, cols, 1};
+        if (copy)
+            DDLA_CUDA(cudaMemcpy2DAsync(out->d, cols * 8, hp, (rows > 1 ? rs : cols) * 8, cols * 8, rows,
+                                        cudaMemcpyHostToDevice, h->stream));
+    } else if (colwise(rows, cols, rs, cs)) {
+        out->view = View<double>{out->d, rows, cols, 1, rows};
+        if (copy)
+            DDLA_CUDA(cudaMemcpy2DAsync(out->d, rows * 8, hp, (cols > 1 ? cs : rows) * 8, rows * 8, cols,
+                                        cudaMemcpyHostToDevice, h->stream));
+    } else {
+        out->view = View<double>{out->d, rows, cols, cols, 1};
+        if (copy) {
+            void *pin;
+            DDLA_TRY(pinned(h, bytes, &pin));
+            DDLA_CUDA(cudaStreamSynchronize(h->stream));
+            double *pp = (double *)pin;
+            for (i64 i = 0; i < rows; i++)
+                for (i64 j = 0; j < cols; j++) pp[i * cols + j] = hp[i * rs + j * cs];
+            DDLA_CUDA(cudaMemcpyAsync(out->d, pp, bytes, cudaMemcpyHostToDevice, h->stream));
+            DDLA_CUDA(cudaStreamSynchronize(h->stream));
+        }
+    }
+    return 0;
+}
+
+// Copies the device view back to the host view; `tri` limits the copy to one
+// triangle (DDLA_LOWER / DDLA_UPPER incl. diagonal) so the other triangle of
+// the caller's array is never touched.
+static int stage_out(ddla_handle h, const Staged &s, double *hp, i64 rows, i64 cols, i64 rs, i64 cs,
+                     int tri = DDLA_DENSE) {
+    if (rows == 0 || cols == 0) return 0;
+    const View<double> &v = s.view;
+    if (tri == DDLA_DENSE && rowwise(rows, cols, rs, cs) && v.cs == 1) {
+        DDLA_CUDA(cudaMemcpy2DAsync(hp, (rows > 1 ? rs : cols) * 8, v.p, cols * 8, cols * 8, rows,
+                                    cudaMemcpyDeviceToHost, h->stream));
+        DDLA_CUDA(cudaStreamSynchronize(h->stream));
+        return 0;
+    }
+    if (tri == DDLA_DENSE && colwise(rows, cols, rs, cs) && v.rs == 1) {
+        DDLA_CUDA(cudaMemcpy2DAsync(hp, (cols > 1 ? cs : rows) * 8, v.p, rows * 8, rows * 8, cols,
+                                    cudaMemcpyDeviceToHost, h->stream));
+        DDLA_CUDA(cudaStreamSynchronize(h->stream));
+        return 0;
+    }
+    size_t bytes = sizeof(double) * (size_t)(rows * cols);
+    void *pin;
+    DDLA_TRY(pinned(h, bytes, &pin));
+    DDLA_CUDA(cudaMemcpyAsync(pin, v.p, bytes, cudaMemcpyDeviceToHost, h->stream));
+    DDLA_CUDA(cudaStreamSynchronize(h->stream));
+    const double *pp = (const double *)pin;
+    for (i64 i = 0; i < rows; i++)
+        for (i64 j = 0; j < cols; j++) {
+            if (tri == DDLA_LOWER && j > i) continue;
+            if (tri == DDLA_UPPER && j < i) continue;
+            hp[i * rs + j * cs] = pp[i * v.rs + j * v.cs];
+        }
+    return 0;
+}
+
+static View<const double> cv(const View<double> &v) { return View<const double>{v.p, v.rows, v.cols, v.rs, v.cs}; }
+
+template <typename T>
+int gemm_any(ddla_handle h, int prec, i64 m, i64 n, i64 k, T alpha, View<const T> A, View<const T> B, T beta,
+             View<T> C, int uplo);
+
+template <>
+int gemm_any<double>(ddla_handle h, int prec, i64 m, i64 n, i64 k, double alpha, View<const double> A,
+                     View<const double> B, double beta, View<double> C, int uplo) {
+    (void)prec;
+    return gemm_f64(h->stream, m, n, k, alpha, A, B, beta, C, uplo);
+}
+
+int gemm_tc(ddla_handle h, int prec, i64 m, i64 n, i64 k, float alpha, View<const float> A, View<const float> B,
+            float beta, View<float> C, int uplo);
+
+template <>
+int gemm_any<float>(ddla_handle h, int prec, i64 m, i64 n, i64 k, float alpha, View<const float> A,
+                    View<const float> B, float beta, View<float> C, int uplo) {
+    if (prec == DDLA_PREC_TF32X3 || prec == DDLA_PREC_BF16X3)
+        return gemm_tc(h, prec, m, n, k, alpha, A, B, beta, C, uplo);
+    return gemm_f32(h->stream, m, n, k, alpha, A, B, beta, C, uplo);
+}
+
+}  // namespace ddla
+
+using namespace ddla;
+
+// ------------------------------------------------------------------ argument checks
+#define CHECK_ARG(cond, pos)                                                         \
+    do {                                                                             \
+        if (!(cond)) {                                                               \
+            set_error(std::string("invalid argument ") + std::to_string(pos) + ": " #cond); \
+            return -(pos);                                                           \
+        }                                                                            \
+    } while (0)
+
+static bool valid_trans(int t) { return t == DDLA_NO_TRANSPOSE || t == DDLA_TRANSPOSE || t == DDLA_CONJ_NO_TRANSPOSE || t == DDLA_CONJ_TRANSPOSE; }
+static bool is_trans(int t) { return (t & DDLA_TRANSPOSE) != 0; }
+static bool valid_tri(int u) { return u == DDLA_LOWER || u == DDLA_UPPER; }
+
+#define GET_HANDLE(h)                  \
+    ddla_handle h;                     \
+    do {                               \
+        int rc_ = default_handle(&h);  \
+        if (rc_) return rc_;           \
+    } while (0)
+
+extern "C" {
+
+const char *ddla_last_error(void) { return t_error.c_str(); }
+const char *ddla_version(void) { return "ddla_gb300 0.1 (sm_103a)"; }
+int64_t ddla_kernel_launches(void) { return g_launches.load(); }
+
+int ddla_handle_create(ddla_handle *h, void *stream) {
+    CHECK_ARG(h != nullptr, 1);
+    ddla_handle x = new ddla_handle_s();
+    int rc = handle_init(x, stream);
+    if (rc) {
+        handle_free(x);
+        return rc;
+    }
+    *h = x;
+    return 0;
+}
+
+int ddla_handle_destroy(ddla_handle h) {
+    handle_free(h);
+    return 0;
+}
+
+int ddla_handle_sync(ddla_handle h) {
+    DDLA_CUDA(cudaStreamSynchronize(h->stream));
+    return 0;
+}
+
+// ------------------------------------------------------------------ level 3, device
+int ddla_dev_dgemm(ddla_handle h, int32_t ta, int32_t tb, ddla_dim_t m, ddla_dim_t n, ddla_dim_t k, double alpha,
+                   const double *a, ddla_inc_t rsa, ddla_inc_t csa, const double *b, ddla_inc_t rsb,
+                   ddla_inc_t csb, double beta, double *c, ddla_inc_t rsc, ddla_inc_t csc) {
+    CHECK_ARG(valid_trans(ta), 2);
+    CHECK_ARG(valid_trans(tb), 3);
+    CHECK_ARG(m >= 0, 4);
+    CHECK_ARG(n >= 0, 5);
+    CHECK_ARG(k >= 0, 6);
+    if (m == 0 || n == 0) return 0;
+    View<const double> A{a, is_trans(ta) ? k : m, is_trans(ta) ? m : k, rsa, csa};
+    View<const double> B{b, is_trans(tb) ? n : k, is_trans(tb) ? k : n, rsb, csb};
+    if (is_trans(ta)) A = A.t();
+    if (is_trans(tb)) B = B.t();
+    return gemm_f64(h->stream, m, n, k, alpha, A, B, beta, View<double>{c, m, n, rsc, csc});
+}
+
+int ddla_dev_dgemmt(ddla_handle h, int32_t uplo, int32_t ta, int32_t tb, ddla_dim_t m, ddla_dim_t k, double alpha,
+                    const double *a, ddla_inc_t rsa, ddla_inc_t csa, const double *b, ddla_inc_t rsb,
+                    ddla_inc_t csb, double beta, double *c, ddla_inc_t rsc, ddla_inc_t csc) {
+    CHECK_ARG(valid_tri(uplo), 2);
+    CHECK_ARG(valid_trans(ta), 3);
+    CHECK_ARG(valid_trans(tb), 4);
+    CHECK_ARG(m >= 0, 5);
+    CHECK_ARG(k >= 0, 6);
+    if (m == 0) return 0;
+    View<const double> A{a, is_trans(ta) ? k : m, is_trans(ta) ? m : k, rsa, csa};
+    View<const double> B{b, is_trans(tb) ? m : k, is_trans(tb) ? k : m, rsb, csb};
+    if (is_trans(ta)) A = A.t();
+    if (is_trans(tb)) B = B.t();
+    return gemm_f64(h->stream, m, m, k, alpha, A, B, beta, View<double>{c, m, m, rsc, csc}, uplo);
+}
+
+int ddla_dev_dtrsm(ddla_handle h, int32_t side, int32_t uplo, int32_t ta, int32_t diag, ddla_dim_t m, ddla_dim_t n,
+                   double alpha, const double *a, ddla_inc_t rsa, ddla_inc_t csa, double *b, ddla_inc_t rsb,
+                   ddla_inc_t csb) {
+    CHECK_ARG(side == DDLA_LEFT || side == DDLA_RIGHT, 2);
+    CHECK_ARG(valid_tri(uplo), 3);
+    CHECK_ARG(valid_trans(ta), 4);
+    CHECK_ARG(diag == DDLA_UNIT_DIAG || diag == DDLA_NONUNIT_DIAG, 5);
+    CHECK_ARG(m >= 0, 6);
+    CHECK_ARG(n >= 0, 7);
+    if (m == 0 || n == 0) return 0;
+    i64 na = side == DDLA_LEFT ? m : n;
+    return trsm<double>(h, side, uplo, ta, diag, m, n, alpha, View<const double>{a, na, na, rsa, csa},
+                        View<double>{b, m, n, rsb, csb});
+}
+
+// ------------------------------------------------------------------ level 3, host
+int ddla_dgemm(int32_t ta, int32_t tb, ddla_dim_t m, ddla_dim_t n, ddla_dim_t k, const double *alpha,
+               const double *a, ddla_inc_t rsa, ddla_inc_t csa, const double *b, ddla_inc_t rsb, ddla_inc_t csb,
+               const double *beta, double *c, ddla_inc_t rsc, ddla_inc_t csc) {
+    CHECK_ARG(valid_trans(ta), 1);
+    CHECK_ARG(valid_trans(tb), 2);
+    CHECK_ARG(m >= 0, 3);
+    CHECK_ARG(n >= 0, 4);
+    CHECK_ARG(k >= 0, 5);
+    CHECK_ARG(alpha != nullptr, 6);
+    CHECK_ARG(beta != nullptr, 13);
+    if (m == 0 || n == 0) return 0;
+    GET_HANDLE(h);
+    i64 ar = is_trans(ta) ? k : m, ac = is_trans(ta) ? m : k;
+    i64 br = is_trans(tb) ? n : k, bc = is_trans(tb) ? k : n;
+    Staged sa, sb, sc;
+    DDLA_TRY(stage_in(h, WS_A, a, ar, ac, rsa, csa, k > 0, &sa));
+    DDLA_TRY(stage_in(h, WS_B, b, br, bc, rsb, csb, k > 0, &sb));
+    DDLA_TRY(stage_in(h, WS_C, c, m, n, rsc, csc, *beta != 0.0, &sc));
+    View<const double> A = cv(sa.view), B = cv(sb.view);
+    if (is_trans(ta)) A = A.t();
+    if (is_trans(tb)) B = B.t();
+    DDLA_TRY(gemm_f64(h->stream, m, n, k, *alpha, A, B, *beta, sc.view));
+    return stage_out(h, sc, c, m, n, rsc, csc);
+}
+
+int ddla_dgemmt(int32_t uplo, int32_t ta, int32_t tb, ddla_dim_t m, ddla_dim_t k, const double *alpha,
+                const double *a, ddla_inc_t rsa, ddla_inc_t csa, const double *b, ddla_inc_t rsb, ddla_inc_t csb,
+                const double *beta, double *c, ddla_inc_t rsc, ddla_inc_t csc) {
+    CHECK_ARG(valid_tri(uplo), 1);
+    CHECK_ARG(valid_trans(ta), 2);
+    CHECK_ARG(valid_trans(tb), 3);
+    CHECK_ARG(m >= 0, 4);
+    CHECK_ARG(k >= 0, 5);
+    CHECK_ARG(alpha != nullptr, 6);
+    CHECK_ARG(beta != nullptr, 13);
+    if (m == 0) return 0;
+    GET_HANDLE(h);
+    i64 ar = is_trans(ta) ? k : m, ac = is_trans(ta) ? m : k;
+    i64 br = is_trans(tb) ? m : k, bc = is_trans(tb) ? k : m;
+    Staged sa, sb, sc;
+    DDLA_TRY(stage_in(h, WS_A, a, ar, ac, rsa, csa, k > 0, &sa));
+    DDLA_TRY(stage_in(h, WS_B, b, br, bc, rsb, csb, k > 0, &sb));
+    DDLA_TRY(stage_in(h, WS_C, c, m, m, rsc, csc, *beta != 0.0, &sc));
+    View<const double> A = cv(sa.view), B = cv(sb.view);
+    if (is_trans(ta)) A = A.t();
+    if (is_trans(tb)) B = B.t();
+    DDLA_TRY(gemm_f64(h->stream, m, m, k, *alpha, A, B, *beta, sc.view, uplo));
+    return stage_out(h, sc, c, m, m, rsc, csc, uplo);
+}
+
+int ddla_dsyrk(int32_t uplo, int32_t ta, ddla_dim_t m, ddla_dim_t k, const double *alpha, const double *a,
+               ddla_inc_t rsa, ddla_inc_t csa, const double *beta, double *c, ddla_inc_t rsc, ddla_inc_t csc) {
+    CHECK_ARG(valid_tri(uplo), 1);
+    CHECK_ARG(valid_trans(ta), 2);
+    CHECK_ARG(m >= 0, 3);
+    CHECK_ARG(k >= 0, 4);
+    CHECK_ARG(alpha != nullptr, 5);
+    CHECK_ARG(beta != nullptr, 9);
+    if (m == 0) return 0;
+    GET_HANDLE(h);
+    i64 ar = is_trans(ta) ? k : m, ac = is_trans(ta) ? m : k;
+    Staged sa, sc;
+    DDLA_TRY(stage_in(h, WS_A, a, ar, ac, rsa, csa, k > 0, &sa));
+    DDLA_TRY(stage_in(h, WS_C, c, m, m, rsc, csc, *beta != 0.0, &sc));
+    View<const double> A = cv(sa.view);
+    if (is_trans(ta)) A = A.t();
+    DDLA_TRY(gemm_f64(h->stream, m, m, k, *alpha, A, A.t(), *beta, sc.view, uplo));
+    return stage_out(h, sc, c, m, m, rsc, csc, uplo);
+}
+
+int ddla_dtrsm(int32_t side, int32_t uplo, int32_t ta, int32_t diag, ddla_dim_t m, ddla_dim_t n,
+               const double *alpha, const double *a, ddla_inc_t rsa, ddla_inc_t csa, double *b, ddla_inc_t rsb,
+               ddla_inc_t csb) {
+    CHECK_ARG(side == DDLA_LEFT || side == DDLA_RIGHT, 1);
+    CHECK_ARG(valid_tri(uplo), 2);
+    CHECK_ARG(valid_trans(ta), 3);
+    CHECK_ARG(diag == DDLA_UNIT_DIAG || diag == DDLA_NONUNIT_DIAG, 4);
+    CHECK_ARG(m >= 0, 5);
+    CHECK_ARG(n >= 0, 6);
+    CHECK_ARG(alpha != nullptr, 7);
+    if (m == 0 || n == 0) return 0;
+    GET_HANDLE(h);
+    i64 na = side == DDLA_LEFT ? m : n;
+    Staged sa, sb;
+    DDLA_TRY(stage_in(h, WS_A, a, na, na, rsa, csa, true, &sa));
+    DDLA_TRY(stage_in(h, WS_B, b, m, n, rsb, csb, true, &sb));
+    DDLA_TRY(trsm<double>(h, side, uplo, ta, diag, m, n, *alpha, cv(sa.view), sb.view));
+    return stage_out(h, sb, b, m, n, rsb, csb);
+}
+
+// ------------------------------------------------------------------ factorizations, device
+int ddla_dev_dgetrf(ddla_handle h, ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t csa, int32_t *piv,
+                    const ddla_opts *opts) {
+    CHECK_ARG(n >= 0, 2);
+    CHECK_ARG(piv != nullptr || n == 0, 6);
+    if (n == 0) return 0;
+    DDLA_TRY(reset_info(h));
+    DDLA_TRY(getrf<double>(h, n, View<double>{a, n, n, rsa, csa}, piv, DDLA_PREC_FP64, opts ? opts->nb : 0));
+    int info;
+    DDLA_TRY(read_info(h, &info));
+    return info;
+}
+
+int ddla_dev_dgetrs(ddla_handle h, int32_t trans, ddla_dim_t n, ddla_dim_t nrhs, const double *lu, ddla_inc_t rsa,
+                    ddla_inc_t csa, const int32_t *piv, double *b, ddla_inc_t rsb, ddla_inc_t csb) {
+    CHECK_ARG(n >= 0, 3);
+    CHECK_ARG(nrhs >= 0, 4);
+    if (n == 0 || nrhs == 0) return 0;
+    return getrs<double>(h, trans, n, nrhs, View<const double>{lu, n, n, rsa, csa}, piv,
+                         View<double>{b, n, nrhs, rsb, csb});
+}
+
+int ddla_dev_dpotrf(ddla_handle h, int32_t uplo, ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t csa,
+                    const ddla_opts *opts) {
+    CHECK_ARG(valid_tri(uplo), 2);
+    CHECK_ARG(n >= 0, 3);
+    if (n == 0) return 0;
+    DDLA_TRY(reset_info(h));
+    DDLA_TRY(potrf<double>(h, uplo, n, View<double>{a, n, n, rsa, csa}, DDLA_PREC_FP64, opts ? opts->nb : 0));
+    int info;
+    DDLA_TRY(read_info(h, &info));
+    return info;
+}
+
+int ddla_dev_dpotrs(ddla_handle h, int32_t uplo, ddla_dim_t n, ddla_dim_t nrhs, const double *a, ddla_inc_t rsa,
+                    ddla_inc_t csa, double *b, ddla_inc_t rsb, ddla_inc_t csb) {
+    CHECK_ARG(valid_tri(uplo), 2);
+    if (n == 0 || nrhs == 0) return 0;
+    return potrs<double>(h, uplo, n, nrhs, View<const double>{a, n, n, rsa, csa}, View<double>{b, n, nrhs, rsb, csb});
+}
+
+int ddla_dev_dldlt(ddla_handle h, int32_t uplo, ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t csa,
+                   const ddla_opts *opts) {
+    CHECK_ARG(valid_tri(uplo), 2);
+    CHECK_ARG(n >= 0, 3);
+    if (n == 0) return 0;
+    DDLA_TRY(reset_info(h));
+    DDLA_TRY(ldlt<double>(h, uplo, n, View<double>{a, n, n, rsa, csa}, DDLA_PREC_FP64, opts ? opts->nb : 0));
+    int info;
+    DDLA_TRY(read_info(h, &info));
+    return info;
+}
+
+int ddla_dev_dldlts(ddla_handle h, int32_t uplo, ddla_dim_t n, ddla_dim_t nrhs, const double *a, ddla_inc_t rsa,
+                    ddla_inc_t csa, double *b, ddla_inc_t rsb, ddla_inc_t csb) {
+    CHECK_ARG(valid_tri(uplo), 2);
+    if (n == 0 || nrhs == 0) return 0;
+    DDLA_TRY(reset_info(h));
+    DDLA_TRY(ldlts<double>(h, uplo, n, nrhs, View<const double>{a, n, n, rsa, csa},
+                           View<double>{b, n, nrhs, rsb, csb}));
+    int info;
+    DDLA_TRY(read_info(h, &info));
+    return info;
+}
+
+// ------------------------------------------------------------------ factorizations, host
+int ddla_dgetrf(ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t csa, int32_t *piv, const ddla_opts *opts) {
+    CHECK_ARG(n >= 0, 1);
+    CHECK_ARG(piv != nullptr || n == 0, 5);
+    if (n == 0) return 0;
+    GET_HANDLE(h);
+    Staged sa;
+    DDLA_TRY(stage_in(h, WS_A, a, n, n, rsa, csa, true, &sa));
+    int32_t *dp;
+    DDLA_TRY(workspace(h, WS_X, sizeof(int32_t) * (size_t)n, (void **)&dp));
+    DDLA_TRY(reset_info(h));
+    DDLA_TRY(getrf<double>(h, n, sa.view, dp, DDLA_PREC_FP64, opts ? opts->nb : 0));
+    int info;
+    DDLA_TRY(read_info(h, &info));
+    DDLA_CUDA(cudaMemcpyAsync(piv, dp, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost, h->stream));
+    DDLA_TRY(stage_out(h, sa, a, n, n, rsa, csa));
+    return info;
+}
+
+int ddla_dgetrs(int32_t trans, ddla_dim_t n, ddla_dim_t nrhs, const double *lu, ddla_inc_t rsa, ddla_inc_t csa,
+                const int32_t *piv, double *b, ddla_inc_t rsb, ddla_inc_t csb) {
+    CHECK_ARG(n >= 0, 2);
+    CHECK_ARG(nrhs >= 0, 3);
+    CHECK_ARG(piv != nullptr || n == 0, 7);
+    if (n == 0 || nrhs == 0) return 0;
+    GET_HANDLE(h);
+    Staged sa, sb;
+    DDLA_TRY(stage_in(h, WS_A, lu, n, n, rsa, csa, true, &sa));
+    DDLA_TRY(stage_in(h, WS_B, b, n, nrhs, rsb, csb, true, &sb));
+    int32_t *dp;
+    DDLA_TRY(workspace(h, WS_X, sizeof(int32_t) * (size_t)n, (void **)&dp));
+    DDLA_CUDA(cudaMemcpyAsync(dp, piv, sizeof(int32_t) * (size_t)n, cudaMemcpyHostToDevice, h->stream));
+    DDLA_TRY(getrs<double>(h, trans, n, nrhs, cv(sa.view), dp, sb.view));
+    return stage_out(h, sb, b, n, nrhs, rsb, csb);
+}
+
+int ddla_dgetrf_nopiv(ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t csa, const ddla_opts *opts) {
+    CHECK_ARG(n >= 0, 1);
+    if (n == 0) return 0;
+    GET_HANDLE(h);
+    Staged sa;
+    DDLA_TRY(stage_in(h, WS_A, a, n, n, rsa, csa, true, &sa));
+    DDLA_TRY(reset_info(h));
+    DDLA_TRY(getrf_nopiv<double>(h, n, sa.view, DDLA_PREC_FP64, opts ? opts->nb : 0));
+    int info;
+    DDLA_TRY(read_info(h, &info));
+    DDLA_TRY(stage_out(h, sa, a, n, n, rsa, csa));
+    return info;
+}
+
+int ddla_dgetrs_nopiv(int32_t trans, ddla_dim_t n, ddla_dim_t nrhs, const double *lu, ddla_inc_t rsa,
+                      ddla_inc_t csa, double *b, ddla_inc_t rsb, ddla_inc_t csb) {
+    CHECK_ARG(n >= 0, 2);
+    CHECK_ARG(nrhs >= 0, 3);
+    if (n == 0 || nrhs == 0) return 0;
+    GET_HANDLE(h);
+    Staged sa, sb;
+    DDLA_TRY(stage_in(h, WS_A, lu, n, n, rsa, csa, true, &sa));
+    DDLA_TRY(stage_in(h, WS_B, b, n, nrhs, rsb, csb, true, &sb));
+    DDLA_TRY(getrs_nopiv<double>(h, trans, n, nrhs, cv(sa.view), sb.view));
+    return stage_out(h, sb, b, n, nrhs, rsb, csb);
+}
+
+int ddla_dpotrf(int32_t uplo, ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t csa, const ddla_opts *opts) {
+    CHECK_ARG(valid_tri(uplo), 1);
+    CHECK_ARG(n >= 0, 2);
+    if (n == 0) return 0;
+    GET_HANDLE(h);
+    Staged sa;
+    DDLA_TRY(stage_in(h, WS_A, a, n, n, rsa, csa, true, &sa));
+    DDLA_TRY(reset_info(h));
+    DDLA_TRY(potrf<double>(h, uplo, n, sa.view, DDLA_PREC_FP64, opts ? opts->nb : 0));
+    int info;
+    DDLA_TRY(read_info(h, &info));
+    DDLA_TRY(stage_out(h, sa, a, n, n, rsa, csa, uplo));
+    return info;
+}
+
+int ddla_dpotrs(int32_t uplo, ddla_dim_t n, ddla_dim_t nrhs, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
+                double *b, ddla_inc_t rsb, ddla_inc_t csb) {
+    CHECK_ARG(valid_tri(uplo), 1);
+    CHECK_ARG(n >= 0, 2);
+    CHECK_ARG(nrhs >= 0, 3);
+    if (n == 0 || nrhs == 0) return 0;
+    GET_HANDLE(h);
+    Staged sa, sb;
+    DDLA_TRY(stage_in(h, WS_A, a, n, n, rsa, csa, true, &sa));
+    DDLA_TRY(stage_in(h, WS_B, b, n, nrhs, rsb, csb, true, &sb));
+    DDLA_TRY(potrs<double>(h, uplo, n, nrhs, cv(sa.view), sb.view));
+    return stage_out(h, sb, b, n, nrhs, rsb, csb);
+}
+
+int ddla_dldlt(int32_t uplo, ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t csa, const ddla_opts *opts) {
+    CHECK_ARG(valid_tri(uplo), 1);
+    CHECK_ARG(n >= 0, 2);
+    if (n == 0) return 0;
+    GET_HANDLE(h);
+    Staged sa;
+    DDLA_TRY(stage_in(h, WS_A, a, n, n, rsa, csa, true, &sa));
+    DDLA_TRY(reset_info(h));
+    DDLA_TRY(ldlt<double>(h, uplo, n, sa.view, DDLA_PREC_FP64, opts ? opts->nb : 0));
+    int info;
+    DDLA_TRY(read_info(h, &info));
+    DDLA_TRY(stage_out(h, sa, a, n, n, rsa, csa, uplo));
+    return info;
+}
+
+int ddla_dldlts(int32_t uplo, ddla_dim_t n, ddla_dim_t nrhs, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
+                double *b, ddla_inc_t rsb, ddla_inc_t csb) {
+    CHECK_ARG(valid_tri(uplo), 1);
+    CHECK_ARG(n >= 0, 2);
+    CHECK_ARG(nrhs >= 0, 3);
+    if (n == 0 || nrhs == 0) return 0;
+    GET_HANDLE(h);
+    Staged sa, sb;
+    DDLA_TRY(stage_in(h, WS_A, a, n, n, rsa, csa, true, &sa));
+    DDLA_TRY(stage_in(h, WS_B, b, n, nrhs, rsb, csb, true, &sb));
+    DDLA_TRY(reset_info(h));
+    DDLA_TRY(ldlts<double>(h, uplo, n, nrhs, cv(sa.view), sb.view));
+    int info;
+    DDLA_TRY(read_info(h, &info));
+    if (info) return info;
+    return stage_out(h, sb, b, n, nrhs, rsb, csb);
+}
+
+}  // extern "C"

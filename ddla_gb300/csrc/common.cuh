@@ -1,0 +1,153 @@
+// Internal definitions shared by the CUDA translation units of libddla_gb300.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <atomic>
+#include <string>
+
+#include "../../include/ddla_gb300.h"
+
+namespace ddla {
+
+typedef int64_t i64;
+
+// ------------------------------------------------------------------ status
+// Thread-local last error message and a process-wide kernel launch counter.
+void set_error(const std::string &msg);
+extern std::atomic<int64_t> g_launches;
+inline void count_launch(int64_t n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+struct Status {
+    int code = 0;
+};
+
+#define DDLA_CUDA(expr)                                                                          \
+    do {                                                                                         \
+        cudaError_t e_ = (expr);                                                                 \
+        if (e_ != cudaSuccess) {                                                                 \
+            ::ddla::set_error(std::string("CUDA error ") + cudaGetErrorString(e_) + " at " +      \
+                              __FILE__ + ":" + std::to_string(__LINE__) + " in " #expr);         \
+            return DDLA_ERR_CUDA;                                                                \
+        }                                                                                        \
+    } while (0)
+
+#define DDLA_LAUNCHED()                                                                          \
+    do {                                                                                         \
+        ::ddla::count_launch();                                                                  \
+        cudaError_t e_ = cudaGetLastError();                                                     \
+        if (e_ != cudaSuccess) {                                                                 \
+            ::ddla::set_error(std::string("kernel launch failed: ") + cudaGetErrorString(e_) +   \
+                              " at " + __FILE__ + ":" + std::to_string(__LINE__));               \
+            return DDLA_ERR_CUDA;                                                                \
+        }                                                                                        \
+    } while (0)
+
+#define DDLA_TRY(expr)                   \
+    do {                                 \
+        int s_ = (expr);                 \
+        if (s_ != 0) return s_;          \
+    } while (0)
+
+// ------------------------------------------------------------------ views
+// Strided matrix view in elements, DDLA's MatrixView layout.
+template <typename T>
+struct View {
+    T *p;
+    i64 rows, cols, rs, cs;
+    __host__ __device__ T &at(i64 i, i64 j) const { return p[i * rs + j * cs]; }
+    __host__ __device__ View t() const { return View{p, cols, rows, cs, rs}; }
+    __host__ __device__ View sub(i64 i, i64 ni, i64 j, i64 nj) const {
+        return View{p + i * rs + j * cs, ni, nj, rs, cs};
+    }
+};
+
+inline int flip_uplo(int u) { return u == DDLA_LOWER ? DDLA_UPPER : (u == DDLA_UPPER ? DDLA_LOWER : u); }
+
+// ------------------------------------------------------------------ handle
+struct Workspace {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+};
+
+}  // namespace ddla
+
+struct ddla_handle_s {
+    int device = 0;
+    int sm_count = 0;
+    int max_cluster = 8;         // largest cluster size the panel kernel may use
+    size_t smem_optin = 0;       // max dynamic shared memory per block
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    // Growable device scratch areas (indexed by purpose).
+    ddla::Workspace ws[8];
+    // Pinned host staging for host-pointer calls.
+    void *pinned = nullptr;
+    size_t pinned_bytes = 0;
+    int *d_info = nullptr;       // device status words (info, timeout flags)
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+namespace ddla {
+
+enum WsSlot { WS_A = 0, WS_B = 1, WS_C = 2, WS_TMP = 3, WS_PIV = 4, WS_F32 = 5, WS_X = 6, WS_MISC = 7 };
+
+// Returns a device buffer of at least `bytes` from slot `slot` (grown on demand).
+int workspace(ddla_handle h, int slot, size_t bytes, void **out);
+int pinned(ddla_handle h, size_t bytes, void **out);
+// The calling thread's default handle (created on first use).
+int default_handle(ddla_handle *out);
+
+// Device status words in h->d_info.
+enum InfoSlot { INFO_PIVOT = 0, INFO_TIMEOUT = 1, INFO_COUNT = 4 };
+int reset_info(ddla_handle h);
+// Reads the device info words (synchronizes the stream).  Returns the first
+// failing pivot (1-based, 0 = none) in *pivot; DDLA_ERR_TIMEOUT if a bounded
+// wait gave up.
+int read_info(ddla_handle h, int *pivot);
+
+// ------------------------------------------------------------------ kernels
+// GEMM: C = alpha*A*B + beta*C on device views (A m x k, B k x n, C m x n).
+// uplo = DDLA_DENSE for a full C, DDLA_LOWER / DDLA_UPPER for GEMMT (only that
+// triangle of C is written; tiles outside it are skipped).
+// batch > 1 runs `batch` independent products with element offsets
+// sa/sb/sc between consecutive problems.
+int gemm_f64(cudaStream_t s, i64 m, i64 n, i64 k, double alpha, View<const double> A, View<const double> B,
+             double beta, View<double> C, int uplo = DDLA_DENSE, i64 batch = 1, i64 sa = 0, i64 sb = 0, i64 sc = 0);
+int gemm_f32(cudaStream_t s, i64 m, i64 n, i64 k, float alpha, View<const float> A, View<const float> B,
+             float beta, View<float> C, int uplo = DDLA_DENSE);
+
+// Triangular solve, B <- op(A)^-1 alpha B (left) or alpha B op(A)^-1 (right).
+template <typename T>
+int trsm(ddla_handle h, int side, int uplo, int trans, int diag, i64 m, i64 n, T alpha, View<const T> A, View<T> B);
+
+// Precision-dispatching GEMM used by the factorization drivers.
+template <typename T>
+int gemm_any(ddla_handle h, int prec, i64 m, i64 n, i64 k, T alpha, View<const T> A, View<const T> B, T beta,
+             View<T> C, int uplo = DDLA_DENSE);
+
+// Factorization drivers (device data, row/col strides arbitrary).
+template <typename T>
+int getrf(ddla_handle h, i64 n, View<T> A, int32_t *d_piv, int prec, int nb);
+template <typename T>
+int getrs(ddla_handle h, int trans, i64 n, i64 nrhs, View<const T> LU, const int32_t *d_piv, View<T> B);
+template <typename T>
+int getrf_nopiv(ddla_handle h, i64 n, View<T> A, int prec, int nb);
+template <typename T>
+int getrs_nopiv(ddla_handle h, int trans, i64 n, i64 nrhs, View<const T> LU, View<T> B);
+template <typename T>
+int potrf(ddla_handle h, int uplo, i64 n, View<T> A, int prec, int nb);
+template <typename T>
+int potrs(ddla_handle h, int uplo, i64 n, i64 nrhs, View<const T> A, View<T> B);
+template <typename T>
+int ldlt(ddla_handle h, int uplo, i64 n, View<T> A, int prec, int nb);
+template <typename T>
+int ldlts(ddla_handle h, int uplo, i64 n, i64 nrhs, View<const T> A, View<T> B);
+
+// Row interchanges of rows [0, npiv) of X with relative pivots (forward or
+// backward), applied to every column of X.
+template <typename T>
+int laswp(cudaStream_t s, View<T> X, const int32_t *d_piv, i64 npiv, bool forward);
+
+}  // namespace ddla

@@ -1,0 +1,332 @@
+// Blocked right-looking factorizations and their solves on device data.
+//
+//   getrf   LU with partial pivoting   DDLA/Factorizations/LU.cs:251-342
+//   getrf_nopiv  LU without pivoting   LU.cs:133-203
+//   potrf   Cholesky (lower / upper)   DDLA/Factorizations/Cholesky.cs:52-208
+//   ldlt    unpivoted LDL^T            DDLA/Factorizations/LDLT.cs:56-265
+//
+// Each step factors a diagonal block (or, for LU, a whole column panel) with a
+// single-kernel on-chip factorization, solves the off-diagonal block with
+// TRSM and updates the trailing matrix with one GEMM / GEMMT in the requested
+// precision.  Failure statuses (1-based pivot index) are accumulated on the
+// device with atomicMin and read once at the end.
+#include <climits>
+
+#include "common.cuh"
+
+namespace ddla {
+
+template <typename T>
+int panel_width_for(ddla_handle h, i64 m);
+template <typename T>
+int panel_lu(ddla_handle h, View<T> X, i64 pc, int w, int32_t *d_piv, i64 row_base, int *d_info);
+template <typename T>
+int apply_perm(ddla_handle h, View<T> B, const int32_t *d_piv, i64 n, bool forward);
+
+namespace {
+
+constexpr int DIAG_MAX = 128;
+constexpr int DIAG_THREADS = 1024;
+
+enum DiagKind { DK_CHOL = 0, DK_LDLT = 1, DK_LU_NOPIV = 2 };
+
+// Unblocked factorization of one bs x bs diagonal block held in shared memory.
+//   DK_CHOL: lower Cholesky of the lower triangle (Cholesky.cs:127-140): a
+//            finite pivot <= 0 fails (Sqrt, :228-236), a non-finite square
+//            root fails (managed InvScaled, DDLA/BLAS/Managed/1v.cs:283-292).
+//   DK_LDLT: lower LDL^T (LDLT.cs:141-158): pivots 0..bs-2 must be non-zero
+//            and finite.
+//   DK_LU_NOPIV: LU without pivoting (LU.cs:188-203): pivots 0..bs-2 non-zero.
+// `upper` factors the transposed view (A = U^T U, U^T D U), which yields the
+// upper-triangle results of DDLA's upper variants.
+template <typename T>
+__global__ void __launch_bounds__(DIAG_THREADS)
+    k_diag(T *A, i64 rs, i64 cs, int bs, int kind, int *info, i64 row_base) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *S = (T *)smem_raw;
+    const int LD = bs + 1;
+    const int tid = threadIdx.x;
+    __shared__ int s_fail;
+    for (int e = tid; e < bs * bs; e += DIAG_THREADS) {
+        int i = e / bs, j = e % bs;
+        S[i * LD + j] = A[i * rs + j * cs];
+    }
+    if (tid == 0) s_fail = 0;
+    __syncthreads();
+    const int last = (kind == DK_CHOL) ? bs : bs - 1;
+    for (int i = 0; i < last; i++) {
+        T piv = S[i * LD + i];
+        bool fail = false;
+        if (kind == DK_CHOL) {
+            if (isfinite((double)piv) && piv <= T(0)) fail = true;
+            else {
+                piv = sqrt(piv);
+                if (!isfinite((double)piv) || piv == T(0)) fail = true;
+            }
+        } else {
+            if (piv == T(0) || (kind == DK_LDLT && !isfinite((double)piv))) fail = true;
+        }
+        if (fail) {
+            if (tid == 0) { atomicMin(info, (int)(row_base + i + 1)); s_fail = 1; }
+            break;
+        }
+        __syncthreads();
+        if (tid == 0 && kind == DK_CHOL) S[i * LD + i] = piv;
+        const T rinv = T(1) / piv;
+        // scale column i below the diagonal
+        for (int r = i + 1 + tid; r < bs; r += DIAG_THREADS) S[r * LD + i] *= rinv;
+        __syncthreads();
+        // trailing update
+        const int nr = bs - i - 1;
+        if (kind == DK_LU_NOPIV) {
+            for (int e = tid; e < nr * nr; e += DIAG_THREADS) {
+                int r = i + 1 + e / nr, c = i + 1 + e % nr;
+                S[r * LD + c] = fma(S[r * LD + i], -S[i * LD + c], S[r * LD + c]);
+            }
+        } else {
+            const T alpha = (kind == DK_CHOL) ? T(-1) : -piv;
+            for (int e = tid; e < nr * nr; e += DIAG_THREADS) {
+                int r = i + 1 + e / nr, c = i + 1 + e % nr;
+                if (c > r) continue;
+                T sc = alpha * S[r * LD + i];
+                S[r * LD + c] = fma(S[c * LD + i], sc, S[r * LD + c]);
+            }
+        }
+        __syncthreads();
+    }
+    __syncthreads();
+    for (int e = tid; e < bs * bs; e += DIAG_THREADS) {
+        int i = e / bs, j = e % bs;
+        if (kind != DK_LU_NOPIV && j > i) continue;  // only the factored triangle
+        A[i * rs + j * cs] = S[i * LD + j];
+    }
+}
+
+// Scale columns j of X (m x b) by 1/d_j where d_j = D(j,j); rows == false
+// scales columns, rows == true scales rows of X (b x m) by 1/d_i.  Zero or
+// non-finite d fails (managed InvScaled).
+template <typename T>
+__global__ void k_scale_by_diag(T *X, i64 rs, i64 cs, i64 m, int b, const T *D, i64 drs, i64 dcs, bool rows,
+                                int *info, i64 row_base) {
+    i64 tot = m * b;
+    for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < tot; e += (i64)gridDim.x * blockDim.x) {
+        i64 r = e / b;
+        int j = (int)(e % b);
+        T d = D[j * drs + j * dcs];
+        if (d == T(0) || !isfinite((double)d)) {
+            if (r == 0) atomicMin(info, (int)(row_base + j + 1));
+            continue;
+        }
+        T *p = rows ? &X[(i64)j * rs + r * cs] : &X[r * rs + (i64)j * cs];
+        *p *= T(1) / d;
+    }
+}
+
+template <typename T>
+__global__ void k_copy(const T *X, i64 rs, i64 cs, i64 m, i64 n, T *Y, i64 ld) {
+    i64 tot = m * n;
+    for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < tot; e += (i64)gridDim.x * blockDim.x) {
+        i64 i = e / n, j = e % n;
+        Y[i * ld + j] = X[i * rs + j * cs];
+    }
+}
+
+template <typename T>
+int diag_kernel(ddla_handle h, View<T> A11, int bs, int kind, i64 row_base) {
+    size_t smem = sizeof(T) * (size_t)bs * (bs + 1);
+    static bool attr_set[2] = {false, false};
+    if (!attr_set[sizeof(T) == 8]) {
+        DDLA_CUDA(cudaFuncSetAttribute(k_diag<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->smem_optin));
+        attr_set[sizeof(T) == 8] = true;
+    }
+    k_diag<T><<<1, DIAG_THREADS, smem, h->stream>>>(A11.p, A11.rs, A11.cs, bs, kind, h->d_info + INFO_PIVOT,
+                                                   row_base);
+    DDLA_LAUNCHED();
+    return 0;
+}
+
+int grid_for(i64 tot) { return (int)((tot + 255) / 256 < 8192 ? ((tot + 255) / 256 > 0 ? (tot + 255) / 256 : 1) : 8192); }
+
+template <typename T>
+int prec_of(int prec) {
+    return sizeof(T) == 8 ? DDLA_PREC_FP64 : (prec == DDLA_PREC_FP64 ? DDLA_PREC_FP32 : prec);
+}
+
+int pick_nb(int nb, int dflt) { return nb > 0 ? (nb > DIAG_MAX ? DIAG_MAX : nb) : dflt; }
+
+}  // namespace
+
+// ------------------------------------------------------------------ LU (pivoted)
+template <typename T>
+int getrf(ddla_handle h, i64 n, View<T> A, int32_t *d_piv, int prec, int nb) {
+    if (n == 0) return 0;
+    prec = prec_of<T>(prec);
+    int w = panel_width_for<T>(h, n);
+    if (w == 0) w = 8;
+    if (nb > 0 && nb < w) w = nb < 8 ? 8 : nb;
+    for (i64 j0 = 0; j0 < n; j0 += w) {
+        int b = (int)(n - j0 < w ? n - j0 : w);
+        View<T> rowsX = A.sub(j0, n - j0, 0, n);
+        DDLA_TRY(panel_lu<T>(h, rowsX, j0, b, d_piv + j0, j0, h->d_info + INFO_PIVOT));
+        i64 r = n - j0 - b;
+        if (r > 0) {
+            View<const T> A11{A.p + j0 * A.rs + j0 * A.cs, b, b, A.rs, A.cs};
+            View<T> A12 = A.sub(j0, b, j0 + b, r);
+            DDLA_TRY(trsm<T>(h, DDLA_LEFT, DDLA_LOWER, DDLA_NO_TRANSPOSE, DDLA_UNIT_DIAG, b, r, T(1), A11, A12));
+            View<const T> A21{A.p + (j0 + b) * A.rs + j0 * A.cs, r, b, A.rs, A.cs};
+            View<const T> cA12{A12.p, b, r, A12.rs, A12.cs};
+            DDLA_TRY(gemm_any<T>(h, prec, r, r, b, T(-1), A21, cA12, T(1), A.sub(j0 + b, r, j0 + b, r)));
+        }
+    }
+    return 0;
+}
+
+template <typename T>
+int getrs(ddla_handle h, int trans, i64 n, i64 nrhs, View<const T> LU, const int32_t *d_piv, View<T> B) {
+    if (n == 0 || nrhs == 0) return 0;
+    if (!trans) {
+        DDLA_TRY(apply_perm<T>(h, B, d_piv, n, true));
+        DDLA_TRY(trsm<T>(h, DDLA_LEFT, DDLA_LOWER, DDLA_NO_TRANSPOSE, DDLA_UNIT_DIAG, n, nrhs, T(1), LU, B));
+        DDLA_TRY(trsm<T>(h, DDLA_LEFT, DDLA_UPPER, DDLA_NO_TRANSPOSE, DDLA_NONUNIT_DIAG, n, nrhs, T(1), LU, B));
+    } else {
+        DDLA_TRY(trsm<T>(h, DDLA_LEFT, DDLA_UPPER, DDLA_TRANSPOSE, DDLA_NONUNIT_DIAG, n, nrhs, T(1), LU, B));
+        DDLA_TRY(trsm<T>(h, DDLA_LEFT, DDLA_LOWER, DDLA_TRANSPOSE, DDLA_UNIT_DIAG, n, nrhs, T(1), LU, B));
+        DDLA_TRY(apply_perm<T>(h, B, d_piv, n, false));
+    }
+    return 0;
+}
+
+// ------------------------------------------------------------------ LU (no pivoting)
+template <typename T>
+int getrf_nopiv(ddla_handle h, i64 n, View<T> A, int prec, int nb) {
+    if (n == 0) return 0;
+    prec = prec_of<T>(prec);
+    nb = pick_nb(nb, DIAG_MAX);
+    if (n <= nb) return diag_kernel<T>(h, A, (int)n, DK_LU_NOPIV, 0);
+    for (i64 j0 = 0; j0 < n; j0 += nb) {
+        int b = (int)(n - j0 < nb ? n - j0 : nb);
+        i64 r = n - j0 - b;
+        View<T> A11 = A.sub(j0, b, j0, b);
+        // every diagonal of a non-final block is tested (LU.cs:181 then the
+        // next block's unblocked step); the final block leaves its last one.
+        DDLA_TRY(diag_kernel<T>(h, A11, b, DK_LU_NOPIV, j0));
+        if (r > 0) {
+            View<const T> cA11{A11.p, b, b, A11.rs, A11.cs};
+            View<T> A12 = A.sub(j0, b, j0 + b, r), A21 = A.sub(j0 + b, r, j0, b);
+            DDLA_TRY(trsm<T>(h, DDLA_LEFT, DDLA_LOWER, DDLA_NO_TRANSPOSE, DDLA_UNIT_DIAG, b, r, T(1), cA11, A12));
+            DDLA_TRY(trsm<T>(h, DDLA_RIGHT, DDLA_UPPER, DDLA_NO_TRANSPOSE, DDLA_NONUNIT_DIAG, r, b, T(1), cA11, A21));
+            View<const T> cA21{A21.p, r, b, A21.rs, A21.cs}, cA12{A12.p, b, r, A12.rs, A12.cs};
+            DDLA_TRY(gemm_any<T>(h, prec, r, r, b, T(-1), cA21, cA12, T(1), A.sub(j0 + b, r, j0 + b, r)));
+        }
+    }
+    return 0;
+}
+
+template <typename T>
+int getrs_nopiv(ddla_handle h, int trans, i64 n, i64 nrhs, View<const T> LU, View<T> B) {
+    if (n == 0 || nrhs == 0) return 0;
+    if (!trans) {
+        DDLA_TRY(trsm<T>(h, DDLA_LEFT, DDLA_LOWER, DDLA_NO_TRANSPOSE, DDLA_UNIT_DIAG, n, nrhs, T(1), LU, B));
+        DDLA_TRY(trsm<T>(h, DDLA_LEFT, DDLA_UPPER, DDLA_NO_TRANSPOSE, DDLA_NONUNIT_DIAG, n, nrhs, T(1), LU, B));
+    } else {
+        DDLA_TRY(trsm<T>(h, DDLA_LEFT, DDLA_UPPER, DDLA_TRANSPOSE, DDLA_NONUNIT_DIAG, n, nrhs, T(1), LU, B));
+        DDLA_TRY(trsm<T>(h, DDLA_LEFT, DDLA_LOWER, DDLA_TRANSPOSE, DDLA_UNIT_DIAG, n, nrhs, T(1), LU, B));
+    }
+    return 0;
+}
+
+// ------------------------------------------------------------------ Cholesky
+template <typename T>
+int potrf(ddla_handle h, int uplo, i64 n, View<T> A, int prec, int nb) {
+    if (n == 0) return 0;
+    prec = prec_of<T>(prec);
+    nb = pick_nb(nb, DIAG_MAX);
+    // The upper factorization is the lower one of the transposed view.
+    View<T> L = (uplo == DDLA_UPPER) ? A.t() : A;
+    for (i64 j0 = 0; j0 < n; j0 += nb) {
+        int b = (int)(n - j0 < nb ? n - j0 : nb);
+        i64 r = n - j0 - b;
+        View<T> L11 = L.sub(j0, b, j0, b);
+        DDLA_TRY(diag_kernel<T>(h, L11, b, DK_CHOL, j0));
+        if (r > 0) {
+            View<const T> cL11{L11.p, b, b, L11.rs, L11.cs};
+            View<T> L21 = L.sub(j0 + b, r, j0, b);
+            DDLA_TRY(trsm<T>(h, DDLA_RIGHT, DDLA_LOWER, DDLA_TRANSPOSE, DDLA_NONUNIT_DIAG, r, b, T(1), cL11, L21));
+            View<const T> cL21{L21.p, r, b, L21.rs, L21.cs};
+            DDLA_TRY(gemm_any<T>(h, prec, r, r, b, T(-1), cL21, cL21.t(), T(1), L.sub(j0 + b, r, j0 + b, r),
+                                 DDLA_LOWER));
+        }
+    }
+    return 0;
+}
+
+template <typename T>
+int potrs(ddla_handle h, int uplo, i64 n, i64 nrhs, View<const T> A, View<T> B) {
+    if (n == 0 || nrhs == 0) return 0;
+    View<const T> L = (uplo == DDLA_UPPER) ? A.t() : A;
+    DDLA_TRY(trsm<T>(h, DDLA_LEFT, DDLA_LOWER, DDLA_NO_TRANSPOSE, DDLA_NONUNIT_DIAG, n, nrhs, T(1), L, B));
+    DDLA_TRY(trsm<T>(h, DDLA_LEFT, DDLA_UPPER, DDLA_NO_TRANSPOSE, DDLA_NONUNIT_DIAG, n, nrhs, T(1), L.t(), B));
+    return 0;
+}
+
+// ------------------------------------------------------------------ LDL^T
+template <typename T>
+int ldlt(ddla_handle h, int uplo, i64 n, View<T> A, int prec, int nb) {
+    if (n == 0) return 0;
+    prec = prec_of<T>(prec);
+    nb = pick_nb(nb, DIAG_MAX);
+    View<T> L = (uplo == DDLA_UPPER) ? A.t() : A;
+    T *Y = nullptr;
+    if (n > nb) DDLA_TRY(workspace(h, WS_TMP, sizeof(T) * (size_t)(n - nb) * nb, (void **)&Y));
+    for (i64 j0 = 0; j0 < n; j0 += nb) {
+        int b = (int)(n - j0 < nb ? n - j0 : nb);
+        i64 r = n - j0 - b;
+        View<T> L11 = L.sub(j0, b, j0, b);
+        DDLA_TRY(diag_kernel<T>(h, L11, b, DK_LDLT, j0));
+        if (r > 0) {
+            View<const T> cL11{L11.p, b, b, L11.rs, L11.cs};
+            View<T> L21 = L.sub(j0 + b, r, j0, b);
+            // A21 <- A21 L11^-T (unit), LDLT.cs:185-187
+            DDLA_TRY(trsm<T>(h, DDLA_RIGHT, DDLA_LOWER, DDLA_TRANSPOSE, DDLA_UNIT_DIAG, r, b, T(1), cL11, L21));
+            // Y21 = A21 (= L21 D), LDLT.cs:188-189
+            k_copy<T><<<grid_for(r * b), 256, 0, h->stream>>>(L21.p, L21.rs, L21.cs, r, b, Y, b);
+            DDLA_LAUNCHED();
+            // A21[:, j] /= d_j, LDLT.cs:190-191
+            k_scale_by_diag<T><<<grid_for(r * b), 256, 0, h->stream>>>(L21.p, L21.rs, L21.cs, r, b, L11.p, L11.rs,
+                                                                      L11.cs, false, h->d_info + INFO_PIVOT, j0);
+            DDLA_LAUNCHED();
+            // A22 -= Y21 A21^T on the lower triangle, LDLT.cs:192-193
+            View<const T> cY{Y, r, b, b, 1}, cL21{L21.p, r, b, L21.rs, L21.cs};
+            DDLA_TRY(gemm_any<T>(h, prec, r, r, b, T(-1), cY, cL21.t(), T(1), L.sub(j0 + b, r, j0 + b, r),
+                                 DDLA_LOWER));
+        }
+    }
+    return 0;
+}
+
+template <typename T>
+int ldlts(ddla_handle h, int uplo, i64 n, i64 nrhs, View<const T> A, View<T> B) {
+    if (n == 0 || nrhs == 0) return 0;
+    View<const T> L = (uplo == DDLA_UPPER) ? A.t() : A;
+    DDLA_TRY(trsm<T>(h, DDLA_LEFT, DDLA_LOWER, DDLA_NO_TRANSPOSE, DDLA_UNIT_DIAG, n, nrhs, T(1), L, B));
+    // X.row(i) /= a_ii, LDLT.cs:274-275
+    k_scale_by_diag<T><<<grid_for(n * nrhs), 256, 0, h->stream>>>(B.p, B.cs, B.rs, nrhs, (int)n, A.p, A.rs, A.cs,
+                                                                 false, h->d_info + INFO_PIVOT, 0);
+    DDLA_LAUNCHED();
+    DDLA_TRY(trsm<T>(h, DDLA_LEFT, DDLA_UPPER, DDLA_NO_TRANSPOSE, DDLA_UNIT_DIAG, n, nrhs, T(1), L.t(), B));
+    return 0;
+}
+
+#define INST(T)                                                                                     \
+    template int getrf<T>(ddla_handle, i64, View<T>, int32_t *, int, int);                          \
+    template int getrs<T>(ddla_handle, int, i64, i64, View<const T>, const int32_t *, View<T>);     \
+    template int getrf_nopiv<T>(ddla_handle, i64, View<T>, int, int);                               \
+    template int getrs_nopiv<T>(ddla_handle, int, i64, i64, View<const T>, View<T>);                \
+    template int potrf<T>(ddla_handle, int, i64, View<T>, int, int);                                \
+    template int potrs<T>(ddla_handle, int, i64, i64, View<const T>, View<T>);                      \
+    template int ldlt<T>(ddla_handle, int, i64, View<T>, int, int);                                 \
+    template int ldlts<T>(ddla_handle, int, i64, i64, View<const T>, View<T>);
+INST(double)
+INST(float)
+
+}  // namespace ddla

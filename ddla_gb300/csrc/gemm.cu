@@ -1,0 +1,281 @@
+// GEMM kernels of libddla_gb300.
+//
+// FP64: DMMA (mma.sync.aligned.m8n8k4 .f64) on shared-memory tiles.  On GB300
+// FP64 runs at ~1/70 of the FP32 CUDA-core rate (DMMA and DFMA both measure
+// ~1.05 TFLOP/s), so an FP64 GEMM is compute-bound at any reasonable tile; the
+// kernel reads operands through arbitrary element strides (DDLA views) and
+// spends its effort on keeping every SM's DMMA pipe busy (tile shape chosen
+// for an even split of tiles over the 152 SMs).
+//
+// FP32: CUDA-core FFMA, 128x128 tiles, 8x8 outputs per thread, double-buffered
+// shared memory.  Used by the FP32-factorization (mixed) paths when the
+// tensor-core variant is not selected.
+//
+// Both compute C = alpha*A*B + beta*C (BLIS semantics: beta == 0 never reads C)
+// and optionally only the lower or upper triangle of C (GEMMT / SYRK), skipping
+// tiles that do not intersect it (DDLA's GEMMTMacroKernel computes and masks
+// them, DDLA/BLAS/Managed/3m/MacroKernel.cs:158-216).
+#include "common.cuh"
+
+namespace ddla {
+
+// ------------------------------------------------------------------ FP64
+namespace {
+
+constexpr int BK64 = 16;
+
+template <int BM, int BN, int WM, int WN>
+__global__ void __launch_bounds__(WM *WN * 32)
+    k_gemm_f64(i64 m, i64 n, i64 k, double alpha, const double *__restrict__ A, i64 rsa, i64 csa,
+               const double *__restrict__ B, i64 rsb, i64 csb, double beta, double *C, i64 rsc, i64 csc,
+               int uplo, i64 sa, i64 sb, i64 sc) {
+    constexpr int NT = WM * WN * 32;
+    constexpr int TWM = BM / WM, TWN = BN / WN;  // warp tile
+    constexpr int FM = TWM / 8, FN = TWN / 8;   // 8x8 fragments per warp
+    constexpr int PAD = 8;
+    __shared__ double As[BK64][BM + PAD];
+    __shared__ double Bs[BK64][BN + PAD];
+
+    const i64 bz = blockIdx.z;
+    A += bz * sa;
+    B += bz * sb;
+    C += bz * sc;
+    const i64 m0 = (i64)blockIdx.y * BM, n0 = (i64)blockIdx.x * BN;
+    if (uplo == DDLA_LOWER && n0 > m0 + BM - 1) return;
+    if (uplo == DDLA_UPPER && m0 > n0 + BN - 1) return;
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int wm = warp / WN, wn = warp % WN;
+    double acc[FM][FN][2];
+#pragma unroll
+    for (int i = 0; i < FM; i++)
+#pragma unroll
+        for (int j = 0; j < FN; j++) acc[i][j][0] = acc[i][j][1] = 0.0;
+
+    const bool a_kfast = (csa == 1);  // K contiguous in A
+    const bool b_nfast = (csb == 1);  // N contiguous in B
+    for (i64 k0 = 0; k0 < k; k0 += BK64) {
+        // A tile BM x BK
+        for (int e = tid; e < BM * BK64; e += NT) {
+            int r, kk;
+            if (a_kfast) { kk = e % BK64; r = e / BK64; } else { r = e % BM; kk = e / BM; }
+            i64 gr = m0 + r, gk = k0 + kk;
+            As[kk][r] = (gr < m && gk < k) ? A[gr * rsa + gk * csa] : 0.0;
+        }
+        // B tile BK x BN
+        for (int e = tid; e < BN * BK64; e += NT) {
+            int c, kk;
+            if (b_nfast) { c = e % BN; kk = e / BN; } else { kk = e % BK64; c = e / BK64; }
+            i64 gc = n0 + c, gk = k0 + kk;
+            Bs[kk][c] = (gc < n && gk < k) ? B[gk * rsb + gc * csb] : 0.0;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int ks = 0; ks < BK64; ks += 4) {
+            double af[FM], bf[FN];
+#pragma unroll
+            for (int i = 0; i < FM; i++) af[i] = As[ks + (lane & 3)][wm * TWM + i * 8 + (lane >> 2)];
+#pragma unroll
+            for (int j = 0; j < FN; j++) bf[j] = Bs[ks + (lane & 3)][wn * TWN + j * 8 + (lane >> 2)];
+#pragma unroll
+            for (int i = 0; i < FM; i++)
+#pragma unroll
+                for (int j = 0; j < FN; j++)
+                    asm volatile(
+                        "mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};\n"
+                        : "+d"(acc[i][j][0]), "+d"(acc[i][j][1])
+                        : "d"(af[i]), "d"(bf[j]));
+        }
+        __syncthreads();
+    }
+    // Epilogue: fragment element (row lane/4, cols 2*(lane%4)+{0,1}).
+#pragma unroll
+    for (int i = 0; i < FM; i++)
+#pragma unroll
+        for (int j = 0; j < FN; j++)
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                i64 gr = m0 + wm * TWM + i * 8 + (lane >> 2);
+                i64 gc = n0 + wn * TWN + j * 8 + 2 * (lane & 3) + h;
+                if (gr >= m || gc >= n) continue;
+                if (uplo == DDLA_LOWER && gc > gr) continue;
+                if (uplo == DDLA_UPPER && gc < gr) continue;
+                double *cp = C + gr * rsc + gc * csc;
+                double v = alpha * acc[i][j][h];
+                *cp = (beta == 0.0) ? v : fma(beta, *cp, v);
+            }
+}
+
+template <int BM, int BN, int WM, int WN>
+int launch_f64(cudaStream_t s, i64 m, i64 n, i64 k, double alpha, View<const double> A, View<const double> B,
+               double beta, View<double> C, int uplo, i64 batch, i64 sa, i64 sb, i64 sc) {
+    i64 gx = (n + BN - 1) / BN, gy = (m + BM - 1) / BM;
+    if (gy > 65535) { set_error("gemm_f64: m too large for one launch"); return DDLA_ERR_UNSUPPORTED; }
+    for (i64 b0 = 0; b0 < batch; b0 += 65535) {
+        i64 nb = batch - b0 < 65535 ? batch - b0 : 65535;
+        dim3 grid((unsigned)gx, (unsigned)gy, (unsigned)nb);
+        k_gemm_f64<BM, BN, WM, WN><<<grid, WM * WN * 32, 0, s>>>(
+            m, n, k, alpha, A.p + b0 * sa, A.rs, A.cs, B.p + b0 * sb, B.rs, B.cs, beta, C.p + b0 * sc, C.rs, C.cs,
+            uplo, sa, sb, sc);
+        DDLA_LAUNCHED();
+    }
+    return 0;
+}
+
+int g_sms = 0;
+int sm_count() {
+    if (!g_sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+        if (g_sms <= 0) g_sms = 152;
+    }
+    return g_sms;
+}
+
+// Fraction of SM slots busy in the last wave when `tiles` equal tiles are
+// spread over the SMs.
+double balance(i64 tiles, int sms) {
+    i64 waves = (tiles + sms - 1) / sms;
+    return (double)tiles / (double)(waves * sms);
+}
+
+}  // namespace
+
+int gemm_f64(cudaStream_t s, i64 m, i64 n, i64 k, double alpha, View<const double> A, View<const double> B,
+             double beta, View<double> C, int uplo, i64 batch, i64 sa, i64 sb, i64 sc) {
+    if (m <= 0 || n <= 0 || batch <= 0) return 0;
+    if (k <= 0 || alpha == 0.0) {
+        // C = beta*C on the requested part: reuse the kernel with k = 0.
+        k = 0;
+    }
+    if (n <= 16)
+        return launch_f64<128, 16, 4, 1>(s, m, n, k, alpha, A, B, beta, C, uplo, batch, sa, sb, sc);
+    int sms = sm_count();
+    i64 t64 = ((m + 63) / 64) * ((n + 63) / 64) * batch;
+    i64 t32 = ((m + 31) / 32) * ((n + 63) / 64) * batch;
+    i64 t3232 = ((m + 31) / 32) * ((n + 31) / 32) * batch;
+    double b64 = balance(t64, sms), b32 = balance(t32, sms), b3232 = balance(t3232, sms);
+    if (t64 >= 8 * sms || (b64 >= 0.9 && b64 >= b32 - 0.02))
+        return launch_f64<64, 64, 2, 2>(s, m, n, k, alpha, A, B, beta, C, uplo, batch, sa, sb, sc);
+    if (b32 >= 0.9 || b32 >= b3232 - 0.02)
+        return launch_f64<32, 64, 2, 2>(s, m, n, k, alpha, A, B, beta, C, uplo, batch, sa, sb, sc);
+    return launch_f64<32, 32, 2, 2>(s, m, n, k, alpha, A, B, beta, C, uplo, batch, sa, sb, sc);
+}
+
+// ------------------------------------------------------------------ FP32
+namespace {
+
+constexpr int SBM = 128, SBN = 128, SBK = 8;
+
+// C = alpha*A*B + beta*C, 256 threads, each thread an 8x8 block split in two
+// 4-row and two 4-column halves (rows ty*4 and 64+ty*4, cols tx*4 and 64+tx*4)
+// so shared-memory reads are conflict-free float4 broadcasts.
+__global__ void __launch_bounds__(256)
+    k_sgemm(i64 m, i64 n, i64 k, float alpha, const float *__restrict__ A, i64 rsa, i64 csa,
+            const float *__restrict__ B, i64 rsb, i64 csb, float beta, float *C, i64 rsc, i64 csc, int uplo) {
+    __shared__ __align__(16) float As[2][SBK][SBM];
+    __shared__ __align__(16) float Bs[2][SBK][SBN];
+    const i64 m0 = (i64)blockIdx.y * SBM, n0 = (i64)blockIdx.x * SBN;
+    if (uplo == DDLA_LOWER && n0 > m0 + SBM - 1) return;
+    if (uplo == DDLA_UPPER && m0 > n0 + SBN - 1) return;
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+
+    // Loader mapping: A tile 128x8 = 1024 elements, 4 per thread.
+    //   K-contiguous A: thread -> row tid/2, k (tid&1)*4 .. +3
+    //   otherwise:      thread -> k tid/32, rows (tid&31)*4 .. +3
+    // B tile 8x128: N-contiguous: k tid/32, cols (tid&31)*4..+3; else col tid/2, k (tid&1)*4..
+    const bool a_k = (csa == 1), b_n = (csb == 1);
+    float ra[4], rb[4];
+    auto load = [&](i64 k0) {
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            int r, kk;
+            if (a_k) { r = tid >> 1; kk = (tid & 1) * 4 + e; } else { kk = tid >> 5; r = (tid & 31) * 4 + e; }
+            i64 gr = m0 + r, gk = k0 + kk;
+            ra[e] = (gr < m && gk < k) ? A[gr * rsa + gk * csa] : 0.f;
+            int c;
+            if (b_n) { kk = tid >> 5; c = (tid & 31) * 4 + e; } else { c = tid >> 1; kk = (tid & 1) * 4 + e; }
+            i64 gc = n0 + c;
+            gk = k0 + kk;
+            rb[e] = (gc < n && gk < k) ? B[gk * rsb + gc * csb] : 0.f;
+        }
+    };
+    auto store = [&](int buf) {
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            int r, kk;
+            if (a_k) { r = tid >> 1; kk = (tid & 1) * 4 + e; } else { kk = tid >> 5; r = (tid & 31) * 4 + e; }
+            As[buf][kk][r] = ra[e];
+            int c;
+            if (b_n) { kk = tid >> 5; c = (tid & 31) * 4 + e; } else { c = tid >> 1; kk = (tid & 1) * 4 + e; }
+            Bs[buf][kk][c] = rb[e];
+        }
+    };
+
+    float acc[8][8];
+#pragma unroll
+    for (int i = 0; i < 8; i++)
+#pragma unroll
+        for (int j = 0; j < 8; j++) acc[i][j] = 0.f;
+
+    int buf = 0;
+    if (k > 0) {
+        load(0);
+        store(0);
+    }
+    __syncthreads();
+    for (i64 k0 = 0; k0 < k; k0 += SBK) {
+        bool more = k0 + SBK < k;
+        if (more) load(k0 + SBK);
+#pragma unroll
+        for (int kk = 0; kk < SBK; kk++) {
+            float4 a0 = *reinterpret_cast<const float4 *>(&As[buf][kk][ty * 4]);
+            float4 a1 = *reinterpret_cast<const float4 *>(&As[buf][kk][64 + ty * 4]);
+            float4 b0 = *reinterpret_cast<const float4 *>(&Bs[buf][kk][tx * 4]);
+            float4 b1 = *reinterpret_cast<const float4 *>(&Bs[buf][kk][64 + tx * 4]);
+            float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+            float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+            for (int i = 0; i < 8; i++)
+#pragma unroll
+                for (int j = 0; j < 8; j++) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
+        }
+        if (more) {
+            store(buf ^ 1);
+            __syncthreads();
+            buf ^= 1;
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        i64 gr = m0 + (i < 4 ? ty * 4 + i : 64 + ty * 4 + i - 4);
+        if (gr >= m) continue;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            i64 gc = n0 + (j < 4 ? tx * 4 + j : 64 + tx * 4 + j - 4);
+            if (gc >= n) continue;
+            if (uplo == DDLA_LOWER && gc > gr) continue;
+            if (uplo == DDLA_UPPER && gc < gr) continue;
+            float *cp = C + gr * rsc + gc * csc;
+            float v = alpha * acc[i][j];
+            *cp = (beta == 0.f) ? v : fmaf(beta, *cp, v);
+        }
+    }
+}
+
+}  // namespace
+
+int gemm_f32(cudaStream_t s, i64 m, i64 n, i64 k, float alpha, View<const float> A, View<const float> B,
+             float beta, View<float> C, int uplo) {
+    if (m <= 0 || n <= 0) return 0;
+    if (k < 0 || alpha == 0.f) k = 0;
+    i64 gx = (n + SBN - 1) / SBN, gy = (m + SBM - 1) / SBM;
+    if (gy > 65535) { set_error("gemm_f32: m too large"); return DDLA_ERR_UNSUPPORTED; }
+    k_sgemm<<<dim3((unsigned)gx, (unsigned)gy), 256, 0, s>>>(m, n, k, alpha, A.p, A.rs, A.cs, B.p, B.rs, B.cs,
+                                                            beta, C.p, C.rs, C.cs, uplo);
+    DDLA_LAUNCHED();
+    return 0;
+}
+
+}  // namespace ddla

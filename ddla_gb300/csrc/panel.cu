@@ -1,0 +1,507 @@
+// LU panel factorization with partial pivoting and the row interchanges.
+//
+// The panel (m rows x w <= 64 columns) is factored by ONE thread-block cluster
+// (up to 16 CTAs).  Each CTA keeps a contiguous slice of the panel rows in
+// shared memory for the whole factorization, so no panel data goes back to
+// HBM between columns.  Per column j:
+//   1. each CTA finds the first largest |a(r,j)| among its rows r >= j
+//      (NaN compares smaller than everything, like bli_damaxv as DDLA
+//      documents it, DDLA/BLAS/1v.cs:29-42);
+//   2. it stores (value, row) into every CTA's candidate table (DSMEM) and a
+//      copy of its candidate row, plus row j if it owns it, in local
+//      double-buffered slots;
+//   3. one cluster barrier;
+//   4. every CTA picks the same winner (largest value, lowest row on ties),
+//      reads the pivot row from the winner's shared memory, and the owners of
+//      rows j and p swap them (whole panel rows, LU.cs:367-374);
+//   5. rows below j are scaled by 1/pivot (InvScal, a zero pivot stops the
+//      factorization and reports it, DDLA/BLAS/1v.cs:97-103) and rank-1
+//      updated (GeR(-1), LU.cs:357-360).
+// The published slots are double-buffered on the column parity, so one
+// cluster barrier per column orders all cross-CTA traffic: a slot written in
+// column j+2 was last read in column j, before its reader reached the barrier
+// of column j+1.
+//
+// Every row carries its origin (row index at panel start), so the interchange
+// of the rest of the matrix is a gather of the touched rows (at most 2w),
+// applied by k_laswp_list in parallel over columns.
+#include <cooperative_groups.h>
+
+#include <climits>
+
+#include "common.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace ddla {
+
+constexpr int PANEL_WMAX = 64;
+constexpr int PANEL_THREADS = 512;
+constexpr int PANEL_MAXCS = 16;
+
+template <typename T>
+struct PanelArgs {
+    T *P;
+    i64 rs, cs;
+    int m, w, rows_per;
+    int32_t *piv;
+    int *info;
+    i64 row_base;
+    int *touch_count, *touch_rows, *touch_src;
+};
+
+struct PanelSmem {
+    size_t rows, origin, cand_row, jrow, urow, prow, cand_val, cand_idx, orgs, red, total;
+};
+
+template <typename T>
+__host__ __device__ inline PanelSmem panel_smem_layout(int rows_per, int w) {
+    PanelSmem L;
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+        size_t at = o;
+        o = (o + bytes + 15) & ~(size_t)15;
+        return at;
+    };
+    L.rows = take(sizeof(T) * (size_t)rows_per * (w + 1));
+    L.origin = take(sizeof(int) * (size_t)rows_per);
+    L.cand_row = take(sizeof(T) * 2 * w);
+    L.jrow = take(sizeof(T) * 2 * w);
+    L.urow = take(sizeof(T) * w);
+    L.prow = take(sizeof(T) * w);
+    L.cand_val = take(sizeof(double) * 2 * PANEL_MAXCS);
+    L.cand_idx = take(sizeof(int) * 2 * PANEL_MAXCS);
+    L.orgs = take(sizeof(int) * 4);
+    L.red = take((sizeof(double) + sizeof(int)) * (PANEL_THREADS / 32) + 16);
+    L.total = o;
+    return L;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(PANEL_THREADS) k_panel_lu(PanelArgs<T> a) {
+    cg::cluster_group cluster = cg::this_cluster();
+    const int CS = (int)cluster.num_blocks();
+    const int rank = (int)cluster.block_rank();
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    constexpr int NW = PANEL_THREADS / 32;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int w = a.w, WP = w + 1, rp = a.rows_per;
+    const PanelSmem L = panel_smem_layout<T>(rp, w);
+    T *rows = (T *)(smem + L.rows);
+    int *origin = (int *)(smem + L.origin);
+    T *cand_row = (T *)(smem + L.cand_row);
+    T *jrow = (T *)(smem + L.jrow);
+    T *urow = (T *)(smem + L.urow);
+    T *prow = (T *)(smem + L.prow);
+    double *cand_val = (double *)(smem + L.cand_val);
+    int *cand_idx = (int *)(smem + L.cand_idx);
+    int *orgs = (int *)(smem + L.orgs);  // [0..1] my candidate origin, [2..3] row-j origin
+    double *red_v = (double *)(smem + L.red);
+    int *red_i = (int *)(red_v + NW);
+    __shared__ int s_best;
+
+    const int base = rank * rp;
+    int nloc = a.m - base;
+    nloc = nloc < 0 ? 0 : (nloc > rp ? rp : nloc);
+
+    if (rank == 0 && tid == 0) *a.touch_count = 0;
+    for (int e = tid; e < nloc * w; e += PANEL_THREADS) {
+        int l = e / w, c = e % w;
+        rows[l * WP + c] = a.P[(i64)(base + l) * a.rs + (i64)c * a.cs];
+    }
+    for (int l = tid; l < nloc; l += PANEL_THREADS) origin[l] = base + l;
+    __syncthreads();
+
+    const int kmax = a.m < w ? a.m : w;
+    for (int j = 0; j < kmax; j++) {
+        const int buf = j & 1;
+        // 1. local first-max of |column j| over rows g >= j
+        double bv = -1.0;
+        int bi = INT_MAX;
+        int l0 = j - base;
+        if (l0 < 0) l0 = 0;
+        for (int l = l0 + tid; l < nloc; l += PANEL_THREADS) {
+            double v = fabs((double)rows[l * WP + j]);
+            if (v > bv) { bv = v; bi = base + l; }
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            double ov = __shfl_down_sync(0xffffffffu, bv, off);
+            int oi = __shfl_down_sync(0xffffffffu, bi, off);
+            if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
+        }
+        if (lane == 0) { red_v[warp] = bv; red_i[warp] = bi; }
+        __syncthreads();
+        if (tid == 0) {
+            for (int q = 1; q < NW; q++)
+                if (red_v[q] > bv || (red_v[q] == bv && red_i[q] < bi)) { bv = red_v[q]; bi = red_i[q]; }
+            s_best = bi;
+            for (int r2 = 0; r2 < CS; r2++) {
+                double *cv = cluster.map_shared_rank(cand_val, r2);
+                int *ci = cluster.map_shared_rank(cand_idx, r2);
+                cv[buf * PANEL_MAXCS + rank] = bv;
+                ci[buf * PANEL_MAXCS + rank] = bi;
+            }
+        }
+        __syncthreads();
+        // 2. publish my candidate row and, if I own it, row j
+        {
+            int mine = s_best;
+            if (mine != INT_MAX) {
+                int lb = mine - base;
+                for (int c = tid; c < w; c += PANEL_THREADS) cand_row[buf * w + c] = rows[lb * WP + c];
+                if (tid == 0) orgs[buf] = origin[lb];
+            }
+            if (j >= base && j < base + nloc) {
+                int lj = j - base;
+                for (int c = tid; c < w; c += PANEL_THREADS) jrow[buf * w + c] = rows[lj * WP + c];
+                if (tid == 0) orgs[2 + buf] = origin[lj];
+            }
+        }
+        cluster.sync();
+        // 3. winner (identical in every CTA)
+        double wv = -1.0;
+        int wi = INT_MAX;
+        for (int r2 = 0; r2 < CS; r2++) {
+            double v = cand_val[buf * PANEL_MAXCS + r2];
+            int i = cand_idx[buf * PANEL_MAXCS + r2];
+            if (v > wv || (v == wv && i < wi)) { wv = v; wi = i; }
+        }
+        const int oj = j / rp;
+        const int p = (wi == INT_MAX) ? j : wi;
+        const int op = p / rp;
+        if (rank == 0 && tid == 0) a.piv[j] = p - j;
+        // 4. fetch the pivot row (winner's candidate row) and, for the owner of
+        //    p, the old row j
+        {
+            const T *src = (wi == INT_MAX) ? cluster.map_shared_rank(jrow + buf * w, oj)
+                                           : cluster.map_shared_rank(cand_row + buf * w, op);
+            for (int c = tid; c < w; c += PANEL_THREADS) urow[c] = src[c];
+            if (op == rank && p != j) {
+                const T *js = cluster.map_shared_rank(jrow + buf * w, oj);
+                for (int c = tid; c < w; c += PANEL_THREADS) prow[c] = js[c];
+            }
+        }
+        int urow_org = 0, jorg = 0;
+        if (tid == 0) {
+            urow_org = (wi == INT_MAX) ? *cluster.map_shared_rank(orgs + 2 + buf, oj)
+                                       : *cluster.map_shared_rank(orgs + buf, op);
+            jorg = *cluster.map_shared_rank(orgs + 2 + buf, oj);
+        }
+        __syncthreads();
+        // 5. swap rows j and p
+        if (p != j) {
+            if (oj == rank) {
+                int lj = j - base;
+                for (int c = tid; c < w; c += PANEL_THREADS) rows[lj * WP + c] = urow[c];
+                if (tid == 0) origin[lj] = urow_org;
+            }
+            if (op == rank) {
+                int lp = p - base;
+                for (int c = tid; c < w; c += PANEL_THREADS) rows[lp * WP + c] = prow[c];
+                if (tid == 0) origin[lp] = jorg;
+            }
+        }
+        __syncthreads();
+        // 6. scale and rank-1 update of rows g > j, one thread per row
+        const T ujj = urow[j];
+        if (ujj == T(0)) {
+            if (rank == 0 && tid == 0) atomicMin(a.info, (int)(a.row_base + j + 1));
+            break;
+        }
+        const T rinv = T(1) / ujj;
+        int ls = j + 1 - base;
+        if (ls < 0) ls = 0;
+        for (int l = ls + tid; l < nloc; l += PANEL_THREADS) {
+            T *row = rows + l * WP;
+            T lv = row[j] * rinv;
+            row[j] = lv;
+            for (int c = j + 1; c < w; c++) row[c] = fma(lv, -urow[c], row[c]);
+        }
+        __syncthreads();
+    }
+    // All DSMEM traffic must finish before any CTA of the cluster exits.
+    cluster.sync();
+    for (int e = tid; e < nloc * w; e += PANEL_THREADS) {
+        int l = e / w, c = e % w;
+        a.P[(i64)(base + l) * a.rs + (i64)c * a.cs] = rows[l * WP + c];
+    }
+    for (int l = tid; l < nloc; l += PANEL_THREADS) {
+        if (origin[l] != base + l) {
+            int k = atomicAdd(a.touch_count, 1);
+            a.touch_rows[k] = base + l;
+            a.touch_src[k] = origin[l];
+        }
+    }
+}
+
+// Fallback for panels that do not fit in one cluster's shared memory: one CTA
+// factors the panel in global memory (same arithmetic, same pivot rule).
+template <typename T>
+__global__ void __launch_bounds__(1024) k_panel_lu_global(PanelArgs<T> a, int *origin) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    __shared__ double red_v[32];
+    __shared__ int red_i[32];
+    __shared__ int s_p;
+    for (int g = tid; g < a.m; g += 1024) origin[g] = g;
+    if (tid == 0) *a.touch_count = 0;
+    __syncthreads();
+    auto at = [&](i64 r, i64 c) -> T & { return a.P[r * a.rs + c * a.cs]; };
+    const int kmax = a.m < a.w ? a.m : a.w;
+    for (int j = 0; j < kmax; j++) {
+        double bv = -1.0;
+        int bi = INT_MAX;
+        for (int g = j + tid; g < a.m; g += 1024) {
+            double v = fabs((double)at(g, j));
+            if (v > bv) { bv = v; bi = g; }
+        }
+        for (int off = 16; off > 0; off >>= 1) {
+            double ov = __shfl_down_sync(0xffffffffu, bv, off);
+            int oi = __shfl_down_sync(0xffffffffu, bi, off);
+            if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
+        }
+        if (lane == 0) { red_v[warp] = bv; red_i[warp] = bi; }
+        __syncthreads();
+        if (tid == 0) {
+            for (int q = 1; q < 32; q++)
+                if (red_v[q] > bv || (red_v[q] == bv && red_i[q] < bi)) { bv = red_v[q]; bi = red_i[q]; }
+            int p = bi == INT_MAX ? j : bi;
+            s_p = p;
+            a.piv[j] = p - j;
+            if (p != j) { int t = origin[j]; origin[j] = origin[p]; origin[p] = t; }
+        }
+        __syncthreads();
+        const int p = s_p;
+        if (p != j)
+            for (int c = tid; c < a.w; c += 1024) { T t = at(j, c); at(j, c) = at(p, c); at(p, c) = t; }
+        __syncthreads();
+        const T ujj = at(j, j);
+        if (ujj == T(0)) {
+            if (tid == 0) atomicMin(a.info, (int)(a.row_base + j + 1));
+            break;
+        }
+        const T rinv = T(1) / ujj;
+        for (int g = j + 1 + tid; g < a.m; g += 1024) {
+            T lv = at(g, j) * rinv;
+            at(g, j) = lv;
+            for (int c = j + 1; c < a.w; c++) at(g, c) = fma(lv, -at(j, c), at(g, c));
+        }
+        __syncthreads();
+    }
+    __syncthreads();
+    for (int g = tid; g < a.m; g += 1024)
+        if (origin[g] != g) {
+            int k = atomicAdd(a.touch_count, 1);
+            a.touch_rows[k] = g;
+            a.touch_src[k] = origin[g];
+        }
+}
+
+// Gather-then-scatter of the touched rows for the columns outside the panel:
+// columns c' in [0, ncols) map to c' (c' < skip0) or c' + skipw.
+constexpr int LASWP_MAXT = 2 * PANEL_WMAX;
+template <typename T>
+__global__ void __launch_bounds__(256)
+    k_laswp_list(T *X, i64 rs, i64 cs, i64 ncols, i64 skip0, i64 skipw, const int *count, const int *rows,
+                 const int *src) {
+    __shared__ T tmp[LASWP_MAXT][32];
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    i64 cc = (i64)blockIdx.x * 32 + lane;
+    const int cnt = *count;
+    const bool ok = cc < ncols;
+    i64 c = cc < skip0 ? cc : cc + skipw;
+    for (int t = wp; t < cnt; t += 8)
+        if (ok) tmp[t][lane] = X[(i64)src[t] * rs + c * cs];
+    __syncthreads();
+    for (int t = wp; t < cnt; t += 8)
+        if (ok) X[(i64)rows[t] * rs + c * cs] = tmp[t][lane];
+}
+
+// Relative pivots -> permutation (perm[k] = source row of row k after the
+// forward interchanges), one thread, permutation held in shared memory.
+__global__ void k_piv_to_perm_smem(const int32_t *piv, i64 n, int *perm) {
+    extern __shared__ int sp[];
+    for (i64 i = threadIdx.x; i < n; i += blockDim.x) sp[i] = (int)i;
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (i64 i = 0; i < n; i++) {
+            i64 t = i + piv[i];
+            if (t != i) { int x = sp[i]; sp[i] = sp[t]; sp[t] = x; }
+        }
+    __syncthreads();
+    for (i64 i = threadIdx.x; i < n; i += blockDim.x) perm[i] = sp[i];
+}
+__global__ void k_piv_to_perm_global(const int32_t *piv, i64 n, int *perm) {
+    for (i64 i = 0; i < n; i++) perm[i] = (int)i;
+    for (i64 i = 0; i < n; i++) {
+        i64 t = i + piv[i];
+        if (t != i) { int x = perm[i]; perm[i] = perm[t]; perm[t] = x; }
+    }
+}
+
+// forward: Y[k] = X[perm[k]];  backward: Y[perm[k]] = X[k].  Y contiguous.
+template <typename T>
+__global__ void k_permute_rows(const T *X, i64 rs, i64 cs, i64 n, i64 ncol, const int *perm, bool forward, T *Y) {
+    i64 tot = n * ncol;
+    for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < tot; e += (i64)gridDim.x * blockDim.x) {
+        i64 k = e / ncol, c = e % ncol;
+        if (forward) Y[k * ncol + c] = X[(i64)perm[k] * rs + c * cs];
+        else Y[(i64)perm[k] * ncol + c] = X[k * rs + c * cs];
+    }
+}
+template <typename T>
+__global__ void k_copy_back(const T *Y, i64 n, i64 ncol, T *X, i64 rs, i64 cs) {
+    i64 tot = n * ncol;
+    for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < tot; e += (i64)gridDim.x * blockDim.x) {
+        i64 k = e / ncol, c = e % ncol;
+        X[k * rs + c * cs] = Y[e];
+    }
+}
+
+// ------------------------------------------------------------------ host side
+
+namespace {
+int g_max_cluster[2] = {0, 0};  // [double, float]
+
+template <typename T>
+int max_cluster(ddla_handle h) {
+    int &mc = g_max_cluster[sizeof(T) == 8 ? 0 : 1];
+    if (mc) return mc;
+    DDLA_CUDA(cudaFuncSetAttribute(k_panel_lu<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    DDLA_CUDA(cudaFuncSetAttribute(k_panel_lu<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)h->smem_optin));
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(PANEL_MAXCS);
+    cfg.blockDim = dim3(PANEL_THREADS);
+    cfg.dynamicSmemBytes = h->smem_optin;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = PANEL_MAXCS;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int cs = 0;
+    if (cudaOccupancyMaxPotentialClusterSize(&cs, (const void *)k_panel_lu<T>, &cfg) != cudaSuccess || cs < 1) {
+        cudaGetLastError();
+        cs = 8;
+    }
+    int p2 = 1;
+    while (p2 * 2 <= cs && p2 * 2 <= PANEL_MAXCS) p2 *= 2;
+    mc = p2;
+    return mc;
+}
+}  // namespace
+
+// Widest panel (power of two, <= 64) whose m rows fit in one cluster.
+template <typename T>
+int panel_width_for(ddla_handle h, i64 m) {
+    int cs = max_cluster<T>(h);
+    if (cs <= 0) return 0;
+    for (int w = PANEL_WMAX; w >= 8; w /= 2) {
+        i64 rp = (m + cs - 1) / cs;
+        if (panel_smem_layout<T>((int)rp, w).total <= h->smem_optin) return w;
+    }
+    return 0;
+}
+
+// Factor the m x w panel at P (relative pivots into d_piv[0..w)), then apply
+// the interchanges to the other columns of the full rows: X is the m-row
+// block containing the panel at column offset pc, with ncols columns.
+template <typename T>
+int panel_lu(ddla_handle h, View<T> X, i64 pc, int w, int32_t *d_piv, i64 row_base, int *d_info) {
+    cudaStream_t s = h->stream;
+    const i64 m = X.rows;
+    int *tbuf;
+    DDLA_TRY(workspace(h, WS_PIV, sizeof(int) * (size_t)(1 + 2 * LASWP_MAXT + m), (void **)&tbuf));
+    int *tcount = tbuf, *trows = tbuf + 1, *tsrc = tbuf + 1 + LASWP_MAXT, *origin = tbuf + 1 + 2 * LASWP_MAXT;
+    PanelArgs<T> a;
+    a.P = X.p + pc * X.cs;
+    a.rs = X.rs;
+    a.cs = X.cs;
+    a.m = (int)m;
+    a.w = w;
+    a.piv = d_piv;
+    a.info = d_info;
+    a.row_base = row_base;
+    a.touch_count = tcount;
+    a.touch_rows = trows;
+    a.touch_src = tsrc;
+    int cs = max_cluster<T>(h);
+    // smallest cluster that holds the rows with at most 512 rows per CTA
+    int use = 1;
+    while (use < cs && ((m + use - 1) / use > 512 ||
+                        panel_smem_layout<T>((int)((m + use - 1) / use), w).total > h->smem_optin))
+        use *= 2;
+    i64 rp = (m + use - 1) / use;
+    size_t smem = panel_smem_layout<T>((int)rp, w).total;
+    if (w <= PANEL_WMAX && smem <= h->smem_optin) {
+        a.rows_per = (int)rp;
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(use);
+        cfg.blockDim = dim3(PANEL_THREADS);
+        cfg.dynamicSmemBytes = smem;
+        cfg.stream = s;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = use;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        DDLA_CUDA(cudaLaunchKernelEx(&cfg, k_panel_lu<T>, a));
+        DDLA_LAUNCHED();
+    } else {
+        if (w > PANEL_WMAX) { set_error("panel_lu: panel wider than 64"); return DDLA_ERR_UNSUPPORTED; }
+        a.rows_per = (int)m;
+        k_panel_lu_global<T><<<1, 1024, 0, s>>>(a, origin);
+        DDLA_LAUNCHED();
+    }
+    i64 other = X.cols - w;
+    if (other > 0) {
+        unsigned grid = (unsigned)((other + 31) / 32);
+        k_laswp_list<T><<<grid, 256, 0, s>>>(X.p, X.rs, X.cs, other, pc, w, tcount, trows, tsrc);
+        DDLA_LAUNCHED();
+    }
+    return 0;
+}
+
+template <typename T>
+int apply_perm(ddla_handle h, View<T> B, const int32_t *d_piv, i64 n, bool forward) {
+    if (n == 0 || B.cols == 0) return 0;
+    cudaStream_t s = h->stream;
+    int *perm;
+    T *tmp;
+    DDLA_TRY(workspace(h, WS_MISC, sizeof(int) * (size_t)n, (void **)&perm));
+    DDLA_TRY(workspace(h, WS_TMP, sizeof(T) * (size_t)n * B.cols, (void **)&tmp));
+    size_t sm = sizeof(int) * (size_t)n;
+    if (sm <= h->smem_optin) {
+        DDLA_CUDA(cudaFuncSetAttribute(k_piv_to_perm_smem, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)h->smem_optin));
+        k_piv_to_perm_smem<<<1, 256, sm, s>>>(d_piv, n, perm);
+    } else {
+        k_piv_to_perm_global<<<1, 1, 0, s>>>(d_piv, n, perm);
+    }
+    DDLA_LAUNCHED();
+    i64 tot = n * B.cols;
+    int blocks = (int)((tot + 255) / 256 < 8192 ? (tot + 255) / 256 : 8192);
+    k_permute_rows<T><<<blocks, 256, 0, s>>>(B.p, B.rs, B.cs, n, B.cols, perm, forward, tmp);
+    DDLA_LAUNCHED();
+    k_copy_back<T><<<blocks, 256, 0, s>>>(tmp, n, B.cols, B.p, B.rs, B.cs);
+    DDLA_LAUNCHED();
+    return 0;
+}
+
+template <typename T>
+int laswp(cudaStream_t, View<T>, const int32_t *, i64, bool) {
+    return DDLA_ERR_UNSUPPORTED;
+}
+
+template int panel_width_for<double>(ddla_handle, i64);
+template int panel_width_for<float>(ddla_handle, i64);
+template int panel_lu<double>(ddla_handle, View<double>, i64, int, int32_t *, i64, int *);
+template int panel_lu<float>(ddla_handle, View<float>, i64, int, int32_t *, i64, int *);
+template int apply_perm<double>(ddla_handle, View<double>, const int32_t *, i64, bool);
+template int apply_perm<float>(ddla_handle, View<float>, const int32_t *, i64, bool);
+
+}  // namespace ddla

@@ -1,0 +1,381 @@
+// Mixed-precision solves: LU / Cholesky in FP32 storage (trailing updates on
+// FP32 CUDA cores or 3xTF32 / 3xBF16 tcgen05 tensor cores), then classical
+// iterative refinement with everything that decides accuracy in FP64 on the
+// GPU: the residual r = b - A x, the solution update x += d, and the
+// backward-error test
+//     max_j ||b_j - A x_j||_inf / (||A||_inf ||x_j||_inf + ||b_j||_inf) <= tol.
+// Only the correction solve (A d = r with the FP32 factors) runs in FP32.
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+
+namespace ddla {
+
+template <typename T>
+int getrf(ddla_handle h, i64 n, View<T> A, int32_t *d_piv, int prec, int nb);
+
+namespace {
+
+constexpr int MAX_RHS = 16;
+
+__global__ void k_d2s(const double *X, i64 n, float *Y) {
+    for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < n; e += (i64)gridDim.x * blockDim.x)
+        Y[e] = (float)X[e];
+}
+__global__ void k_s2d_add(const float *D, i64 n, double *X) {
+    for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < n; e += (i64)gridDim.x * blockDim.x)
+        X[e] += (double)D[e];
+}
+__global__ void k_s2d(const float *D, i64 n, double *X) {
+    for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < n; e += (i64)gridDim.x * blockDim.x)
+        X[e] = (double)D[e];
+}
+
+// r = b - A x for row-major A (n x n, lda), X/B/R n x nrhs row-major; one warp
+// per row.  Also writes |r| row maxima per column into rowmax (for the norm).
+template <int NR>
+__global__ void __launch_bounds__(256)
+    k_residual(i64 n, const double *__restrict__ A, i64 lda, const double *__restrict__ X,
+               const double *__restrict__ B, double *R) {
+    const int lane = threadIdx.x & 31;
+    const i64 row = (blockIdx.x * (i64)blockDim.x + threadIdx.x) >> 5;
+    if (row >= n) return;
+    double acc[NR];
+#pragma unroll
+    for (int c = 0; c < NR; c++) acc[c] = 0.0;
+    const double *ar = A + row * lda;
+    for (i64 j = lane; j < n; j += 32) {
+        double a = ar[j];
+#pragma unroll
+        for (int c = 0; c < NR; c++) acc[c] = fma(a, X[j * NR + c], acc[c]);
+    }
+#pragma unroll
+    for (int c = 0; c < NR; c++) {
+        double v = acc[c];
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+        acc[c] = v;
+    }
+    if (lane == 0)
+#pragma unroll
+        for (int c = 0; c < NR; c++) R[row * NR + c] = B[row * NR + c] - acc[c];
+}
+
+// Column-wise max |X[:, c]| over rows (atomicMax on the bit pattern of the
+// non-negative double).
+__global__ void k_colmax_abs(const double *X, i64 n, int nr, unsigned long long *out) {
+    for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < n * nr; e += (i64)gridDim.x * blockDim.x) {
+        double v = fabs(X[e]);
+        if (v == v) atomicMax(&out[e % nr], (unsigned long long)__double_as_longlong(v));
+    }
+}
+
+// ||A||_inf = max_i sum_j |a_ij| (row-major), one warp per row.
+__global__ void k_norm_inf(i64 n, const double *A, i64 lda, unsigned long long *out) {
+    const int lane = threadIdx.x & 31;
+    const i64 row = (blockIdx.x * (i64)blockDim.x + threadIdx.x) >> 5;
+    if (row >= n) return;
+    double s = 0.0;
+    for (i64 j = lane; j < n; j += 32) s += fabs(A[row * lda + j]);
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+    if (lane == 0) atomicMax(out, (unsigned long long)__double_as_longlong(s));
+}
+
+// Max |x - xr| and |xr| per column.
+__global__ void k_fwd_err(const double *X, const double *XR, i64 n, int nr, unsigned long long *out) {
+    for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < n * nr; e += (i64)gridDim.x * blockDim.x) {
+        double d = fabs(X[e] - XR[e]), r = fabs(XR[e]);
+        atomicMax(&out[0], (unsigned long long)__double_as_longlong(d));
+        atomicMax(&out[1], (unsigned long long)__double_as_longlong(r));
+    }
+}
+
+int grid1(i64 tot) {
+    i64 g = (tot + 255) / 256;
+    return (int)(g < 1 ? 1 : (g > 16384 ? 16384 : g));
+}
+
+template <int NR>
+int residual_nr(cudaStream_t s, i64 n, const double *A, const double *X, const double *B, double *R) {
+    unsigned grid = (unsigned)((n * 32 + 255) / 256);
+    k_residual<NR><<<grid, 256, 0, s>>>(n, A, n, X, B, R);
+    DDLA_LAUNCHED();
+    return 0;
+}
+
+int residual(cudaStream_t s, i64 n, int nr, const double *A, const double *X, const double *B, double *R) {
+    switch (nr) {
+        case 1: return residual_nr<1>(s, n, A, X, B, R);
+        case 2: return residual_nr<2>(s, n, A, X, B, R);
+        case 4: return residual_nr<4>(s, n, A, X, B, R);
+        case 8: return residual_nr<8>(s, n, A, X, B, R);
+        case 16: return residual_nr<16>(s, n, A, X, B, R);
+        default: break;
+    }
+    // generic width: FP64 GEMM on the DMMA path (R = B - A X)
+    DDLA_CUDA(cudaMemcpyAsync(R, B, sizeof(double) * n * nr, cudaMemcpyDeviceToDevice, s));
+    return gemm_f64(s, n, nr, n, -1.0, View<const double>{A, n, n, n, 1}, View<const double>{X, n, nr, nr, 1}, 1.0,
+                    View<double>{R, n, nr, nr, 1});
+}
+
+double u64d(unsigned long long v) { return __builtin_bit_cast(double, v); }
+
+}  // namespace
+
+// Shared refinement loop.  `solve32(d)` overwrites the FP32 right-hand side d
+// (n x nr) with the correction.
+template <typename F>
+int refine(ddla_handle h, i64 n, int nr, const double *A, const double *B, double *X, const double *x_ref,
+           const ddla_opts *opts, ddla_solve_report *rep, F solve32, float *d32, double *R,
+           unsigned long long *norms) {
+    cudaStream_t s = h->stream;
+    const int max_iter = (opts && opts->max_iter) ? opts->max_iter : 30;
+    const double tol = (opts && opts->tol > 0) ? opts->tol : 1e-14;
+    const i64 tot = n * nr;
+    // norms[0] = ||A||_inf, [1..nr] = ||b_j||, [1+nr .. 1+2nr) = ||x_j||, [1+2nr .. 1+3nr) = ||r_j||
+    DDLA_CUDA(cudaMemsetAsync(norms, 0, sizeof(unsigned long long) * (1 + 3 * MAX_RHS + 2), s));
+    k_norm_inf<<<(unsigned)((n * 32 + 255) / 256), 256, 0, s>>>(n, A, n, norms);
+    DDLA_LAUNCHED();
+    k_colmax_abs<<<grid1(tot), 256, 0, s>>>(B, n, nr, norms + 1);
+    DDLA_LAUNCHED();
+    // x0 = LU \ b
+    k_d2s<<<grid1(tot), 256, 0, s>>>(B, tot, d32);
+    DDLA_LAUNCHED();
+    DDLA_TRY(solve32(d32));
+    k_s2d<<<grid1(tot), 256, 0, s>>>(d32, tot, X);
+    DDLA_LAUNCHED();
+    int it = 0;
+    double berr = INFINITY;
+    const int iters = max_iter < 0 ? 0 : max_iter;
+    std::vector<unsigned long long> hn(1 + 3 * MAX_RHS);
+    for (;;) {
+        DDLA_TRY(residual(s, n, nr, A, X, B, R));
+        DDLA_CUDA(cudaMemsetAsync(norms + 1 + nr, 0, sizeof(unsigned long long) * 2 * nr, s));
+        k_colmax_abs<<<grid1(tot), 256, 0, s>>>(X, n, nr, norms + 1 + nr);
+        DDLA_LAUNCHED();
+        k_colmax_abs<<<grid1(tot), 256, 0, s>>>(R, n, nr, norms + 1 + 2 * nr);
+        DDLA_LAUNCHED();
+        DDLA_CUDA(cudaMemcpyAsync(hn.data(), norms, sizeof(unsigned long long) * (1 + 3 * nr),
+                                  cudaMemcpyDeviceToHost, s));
+        DDLA_CUDA(cudaStreamSynchronize(s));
+        double an = u64d(hn[0]);
+        berr = 0.0;
+        for (int c = 0; c < nr; c++) {
+            double bn = u64d(hn[1 + c]), xn = u64d(hn[1 + nr + c]), rn = u64d(hn[1 + 2 * nr + c]);
+            double den = an * xn + bn;
+            double e = den > 0 ? rn / den : (rn > 0 ? INFINITY : 0.0);
+            if (!(e <= berr)) berr = e;  // NaN propagates
+        }
+        if (berr <= tol || it >= iters) break;
+        k_d2s<<<grid1(tot), 256, 0, s>>>(R, tot, d32);
+        DDLA_LAUNCHED();
+        DDLA_TRY(solve32(d32));
+        k_s2d_add<<<grid1(tot), 256, 0, s>>>(d32, tot, X);
+        DDLA_LAUNCHED();
+        it++;
+    }
+    rep->iterations = it;
+    rep->backward_error = berr;
+    rep->converged = berr <= tol;
+    rep->forward_error = -1.0;
+    if (x_ref) {
+        DDLA_CUDA(cudaMemsetAsync(norms + 1 + 3 * MAX_RHS, 0, 2 * sizeof(unsigned long long), s));
+        k_fwd_err<<<grid1(tot), 256, 0, s>>>(X, x_ref, n, nr, norms + 1 + 3 * MAX_RHS);
+        DDLA_LAUNCHED();
+        unsigned long long fe[2];
+        DDLA_CUDA(cudaMemcpyAsync(fe, norms + 1 + 3 * MAX_RHS, sizeof(fe), cudaMemcpyDeviceToHost, s));
+        DDLA_CUDA(cudaStreamSynchronize(s));
+        double rn = u64d(fe[1]);
+        rep->forward_error = rn > 0 ? u64d(fe[0]) / rn : u64d(fe[0]);
+    }
+    if (!rep->converged) {
+        set_error("iterative refinement did not reach the backward-error tolerance");
+        return DDLA_ERR_NOT_CONVERGED;
+    }
+    return 0;
+}
+
+int mixed_lu(ddla_handle h, i64 n, i64 nrhs, const double *A, const double *B, double *X, const double *x_ref,
+             const ddla_opts *opts, ddla_solve_report *rep) {
+    cudaStream_t s = h->stream;
+    const int prec = (opts && opts->precision) ? opts->precision : DDLA_PREC_FP32;
+    const int nb = opts ? opts->nb : 0;
+    *rep = ddla_solve_report{};
+    rep->precision = prec;
+    rep->pivots_agree = -1;
+    if (nrhs > MAX_RHS) {
+        set_error("mixed solve: at most 16 right-hand sides per call");
+        return DDLA_ERR_UNSUPPORTED;
+    }
+    const int nr = (int)nrhs;
+    float *A32, *d32;
+    double *R;
+    int32_t *piv;
+    unsigned long long *norms;
+    DDLA_TRY(workspace(h, WS_F32, sizeof(float) * (size_t)n * n, (void **)&A32));
+    DDLA_TRY(workspace(h, WS_B, sizeof(float) * (size_t)n * nr + 256, (void **)&d32));
+    DDLA_TRY(workspace(h, WS_C, sizeof(double) * (size_t)n * nr, (void **)&R));
+    DDLA_TRY(workspace(h, WS_X, sizeof(int32_t) * (size_t)n, (void **)&piv));
+    DDLA_TRY(workspace(h, WS_A, sizeof(unsigned long long) * (2 + 3 * MAX_RHS + 2), (void **)&norms));
+    DDLA_TRY(reset_info(h));
+    DDLA_CUDA(cudaEventRecord(h->ev0, s));
+    k_d2s<<<grid1(n * n), 256, 0, s>>>(A, n * n, A32);
+    DDLA_LAUNCHED();
+    DDLA_TRY(getrf<float>(h, n, View<float>{A32, n, n, n, 1}, piv, prec, nb));
+    DDLA_CUDA(cudaEventRecord(h->ev1, s));
+    int info;
+    DDLA_TRY(read_info(h, &info));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+    rep->factor_ms = ms;
+    rep->info = info;
+    if (info) return info;
+    auto solve32 = [&](float *d) {
+        return getrs<float>(h, 0, n, nr, View<const float>{A32, n, n, n, 1}, piv, View<float>{d, n, nr, nr, 1});
+    };
+    DDLA_CUDA(cudaEventRecord(h->ev0, s));
+    int rc = refine(h, n, nr, A, B, X, x_ref, opts, rep, solve32, d32, R, norms);
+    DDLA_CUDA(cudaEventRecord(h->ev1, s));
+    DDLA_CUDA(cudaEventSynchronize(h->ev1));
+    cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+    rep->refine_ms = ms;
+    return rc;
+}
+
+int mixed_chol(ddla_handle h, int uplo, i64 n, i64 nrhs, const double *A, const double *B, double *X,
+               const double *x_ref, const ddla_opts *opts, ddla_solve_report *rep) {
+    cudaStream_t s = h->stream;
+    const int prec = (opts && opts->precision) ? opts->precision : DDLA_PREC_FP32;
+    const int nb = opts ? opts->nb : 0;
+    *rep = ddla_solve_report{};
+    rep->precision = prec;
+    rep->pivots_agree = -1;
+    if (nrhs > MAX_RHS) {
+        set_error("mixed solve: at most 16 right-hand sides per call");
+        return DDLA_ERR_UNSUPPORTED;
+    }
+    const int nr = (int)nrhs;
+    float *A32, *d32;
+    double *R;
+    unsigned long long *norms;
+    DDLA_TRY(workspace(h, WS_F32, sizeof(float) * (size_t)n * n, (void **)&A32));
+    DDLA_TRY(workspace(h, WS_B, sizeof(float) * (size_t)n * nr + 256, (void **)&d32));
+    DDLA_TRY(workspace(h, WS_C, sizeof(double) * (size_t)n * nr, (void **)&R));
+    DDLA_TRY(workspace(h, WS_A, sizeof(unsigned long long) * (2 + 3 * MAX_RHS + 2), (void **)&norms));
+    DDLA_TRY(reset_info(h));
+    DDLA_CUDA(cudaEventRecord(h->ev0, s));
+    k_d2s<<<grid1(n * n), 256, 0, s>>>(A, n * n, A32);
+    DDLA_LAUNCHED();
+    DDLA_TRY(potrf<float>(h, uplo, n, View<float>{A32, n, n, n, 1}, prec, nb));
+    DDLA_CUDA(cudaEventRecord(h->ev1, s));
+    int info;
+    DDLA_TRY(read_info(h, &info));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+    rep->factor_ms = ms;
+    rep->info = info;
+    if (info) return info;
+    auto solve32 = [&](float *d) {
+        return potrs<float>(h, uplo, n, nr, View<const float>{A32, n, n, n, 1}, View<float>{d, n, nr, nr, 1});
+    };
+    DDLA_CUDA(cudaEventRecord(h->ev0, s));
+    int rc = refine(h, n, nr, A, B, X, x_ref, opts, rep, solve32, d32, R, norms);
+    DDLA_CUDA(cudaEventRecord(h->ev1, s));
+    DDLA_CUDA(cudaEventSynchronize(h->ev1));
+    cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+    rep->refine_ms = ms;
+    return rc;
+}
+
+}  // namespace ddla
+
+using namespace ddla;
+
+extern "C" {
+
+int ddla_dev_dgesv_mixed(ddla_handle h, ddla_dim_t n, ddla_dim_t nrhs, const double *a, const double *b, double *x,
+                         const double *x_ref, const ddla_opts *opts, ddla_solve_report *report) {
+    if (n < 0) return -2;
+    if (nrhs < 0) return -3;
+    if (!report) return -9;
+    if (n == 0 || nrhs == 0) { *report = ddla_solve_report{}; return 0; }
+    return mixed_lu(h, n, nrhs, a, b, x, x_ref, opts, report);
+}
+
+int ddla_dev_dposv_mixed(ddla_handle h, int32_t uplo, ddla_dim_t n, ddla_dim_t nrhs, const double *a,
+                         const double *b, double *x, const double *x_ref, const ddla_opts *opts,
+                         ddla_solve_report *report) {
+    if (uplo != DDLA_LOWER && uplo != DDLA_UPPER) return -2;
+    if (n < 0) return -3;
+    if (nrhs < 0) return -4;
+    if (!report) return -10;
+    if (n == 0 || nrhs == 0) { *report = ddla_solve_report{}; return 0; }
+    return mixed_chol(h, uplo, n, nrhs, a, b, x, x_ref, opts, report);
+}
+
+// Host-pointer variants: A (n x n) and B (n x nrhs) are arbitrary strided host
+// views; X receives the solution.
+static int host_mixed(bool chol, int32_t uplo, ddla_dim_t n, ddla_dim_t nrhs, const double *a, ddla_inc_t rsa,
+                      ddla_inc_t csa, const double *b, ddla_inc_t rsb, ddla_inc_t csb, double *x, ddla_inc_t rsx,
+                      ddla_inc_t csx, const double *x_ref, const ddla_opts *opts, ddla_solve_report *report) {
+    if (n < 0) return -1;
+    if (nrhs < 0 || nrhs > 16) return -2;
+    if (!report) return -15;
+    if (n == 0 || nrhs == 0) { *report = ddla_solve_report{}; return 0; }
+    ddla_handle h;
+    DDLA_TRY(default_handle(&h));
+    cudaStream_t s = h->stream;
+    // dense row-major device copies (the mixed kernels assume them)
+    double *dA, *dB, *dX, *dR = nullptr;
+    size_t nn = (size_t)n * n, nb = (size_t)n * nrhs;
+    DDLA_CUDA(cudaMallocAsync(&dA, nn * 8, s));
+    DDLA_CUDA(cudaMallocAsync(&dB, nb * 8, s));
+    DDLA_CUDA(cudaMallocAsync(&dX, nb * 8, s));
+    if (x_ref) DDLA_CUDA(cudaMallocAsync(&dR, nb * 8, s));
+    auto pack_in = [&](const double *hp, i64 r, i64 c, i64 rs, i64 cs, double *d) -> int {
+        if (cs == 1 && (r <= 1 || rs >= c)) {
+            DDLA_CUDA(cudaMemcpy2DAsync(d, c * 8, hp, (r > 1 ? rs : c) * 8, c * 8, r, cudaMemcpyHostToDevice, s));
+        } else {
+            std::vector<double> tmp((size_t)(r * c));
+            for (i64 i = 0; i < r; i++)
+                for (i64 j = 0; j < c; j++) tmp[i * c + j] = hp[i * rs + j * cs];
+            DDLA_CUDA(cudaMemcpyAsync(d, tmp.data(), tmp.size() * 8, cudaMemcpyHostToDevice, s));
+            DDLA_CUDA(cudaStreamSynchronize(s));
+        }
+        return 0;
+    };
+    int rc = pack_in(a, n, n, rsa, csa, dA);
+    if (!rc) rc = pack_in(b, n, nrhs, rsb, csb, dB);
+    if (!rc && x_ref) rc = pack_in(x_ref, n, nrhs, nrhs, 1, dR);
+    if (!rc) rc = chol ? mixed_chol(h, uplo, n, nrhs, dA, dB, dX, dR, opts, report)
+                       : mixed_lu(h, n, nrhs, dA, dB, dX, dR, opts, report);
+    if (rc == 0 || rc == DDLA_ERR_NOT_CONVERGED) {
+        std::vector<double> tmp(nb);
+        if (cudaMemcpyAsync(tmp.data(), dX, nb * 8, cudaMemcpyDeviceToHost, s) == cudaSuccess &&
+            cudaStreamSynchronize(s) == cudaSuccess) {
+            for (i64 i = 0; i < n; i++)
+                for (i64 j = 0; j < nrhs; j++) x[i * rsx + j * csx] = tmp[i * nrhs + j];
+        }
+    }
+    cudaFreeAsync(dA, s);
+    cudaFreeAsync(dB, s);
+    cudaFreeAsync(dX, s);
+    if (dR) cudaFreeAsync(dR, s);
+    cudaStreamSynchronize(s);
+    return rc;
+}
+
+int ddla_dgesv_mixed(ddla_dim_t n, ddla_dim_t nrhs, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
+                     const double *b, ddla_inc_t rsb, ddla_inc_t csb, double *x, ddla_inc_t rsx, ddla_inc_t csx,
+                     const double *x_ref, const ddla_opts *opts, ddla_solve_report *report) {
+    return host_mixed(false, 0, n, nrhs, a, rsa, csa, b, rsb, csb, x, rsx, csx, x_ref, opts, report);
+}
+
+int ddla_dposv_mixed(int32_t uplo, ddla_dim_t n, ddla_dim_t nrhs, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
+                     const double *b, ddla_inc_t rsb, ddla_inc_t csb, double *x, ddla_inc_t rsx, ddla_inc_t csx,
+                     const double *x_ref, const ddla_opts *opts, ddla_solve_report *report) {
+    if (uplo != DDLA_LOWER && uplo != DDLA_UPPER) return -1;
+    return host_mixed(true, uplo, n, nrhs, a, rsa, csa, b, rsb, csb, x, rsx, csx, x_ref, opts, report);
+}
+
+}  // extern "C"

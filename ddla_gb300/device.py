@@ -1,0 +1,88 @@
+"""Device-resident calls (ddla_dev_* entry points) on torch CUDA tensors.
+
+torch is used only for device memory and streams; every computation is a call
+into libddla_gb300.so.
+"""
+import ctypes as C
+
+from . import _lib
+from ._lib import Opts, SolveReport, check, lib
+
+
+def _p(t):
+    return C.c_void_p(t.data_ptr())
+
+
+def _st(t):
+    return t.stride(0), t.stride(1)
+
+
+class Handle:
+    """ddla_handle bound to a CUDA stream (torch.cuda.Stream or None)."""
+
+    def __init__(self, stream=None):
+        self.h = C.c_void_p()
+        s = None if stream is None else C.c_void_p(stream.cuda_stream)
+        check(lib().ddla_handle_create(C.byref(self.h), s), "handle_create")
+
+    def close(self):
+        if self.h:
+            lib().ddla_handle_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def sync(self):
+        check(lib().ddla_handle_sync(self.h), "handle_sync")
+
+    def gemm(self, alpha, A, B, beta, Cm, ta=0, tb=0):
+        m, n = Cm.shape
+        k = A.shape[0] if ta else A.shape[1]
+        check(lib().ddla_dev_dgemm(self.h, ta, tb, m, n, k, alpha, _p(A), *_st(A), _p(B), *_st(B), beta, _p(Cm),
+                                   *_st(Cm)), "dev_dgemm")
+
+    def gemmt(self, uplo, alpha, A, B, beta, Cm, ta=0, tb=0):
+        m = Cm.shape[0]
+        k = A.shape[0] if ta else A.shape[1]
+        check(lib().ddla_dev_dgemmt(self.h, uplo, ta, tb, m, k, alpha, _p(A), *_st(A), _p(B), *_st(B), beta,
+                                    _p(Cm), *_st(Cm)), "dev_dgemmt")
+
+    def trsm(self, side, uplo, ta, diag, alpha, A, B):
+        m, n = B.shape
+        check(lib().ddla_dev_dtrsm(self.h, side, uplo, ta, diag, m, n, alpha, _p(A), *_st(A), _p(B), *_st(B)),
+              "dev_dtrsm")
+
+    def getrf(self, A, piv, nb=0):
+        o = Opts()
+        o.nb = nb
+        return lib().ddla_dev_dgetrf(self.h, A.shape[0], _p(A), *_st(A), _p(piv), C.byref(o))
+
+    def getrs(self, LU, piv, B, trans=0):
+        check(lib().ddla_dev_dgetrs(self.h, trans, LU.shape[0], B.shape[1], _p(LU), *_st(LU), _p(piv), _p(B),
+                                    *_st(B)), "dev_dgetrs")
+
+    def potrf(self, uplo, A, nb=0):
+        o = Opts()
+        o.nb = nb
+        return lib().ddla_dev_dpotrf(self.h, uplo, A.shape[0], _p(A), *_st(A), C.byref(o))
+
+    def potrs(self, uplo, A, B):
+        check(lib().ddla_dev_dpotrs(self.h, uplo, A.shape[0], B.shape[1], _p(A), *_st(A), _p(B), *_st(B)),
+              "dev_dpotrs")
+
+    def gesv_mixed(self, A, B, X, x_ref=None, precision=_lib.PREC_FP32, tol=0.0, max_iter=0, nb=0, spd=False,
+                   uplo=_lib.LOWER):
+        o = Opts()
+        o.precision, o.tol, o.max_iter, o.nb = precision, tol, max_iter, nb
+        rep = SolveReport()
+        xr = C.c_void_p(0) if x_ref is None else _p(x_ref)
+        n, nrhs = B.shape
+        if spd:
+            rc = lib().ddla_dev_dposv_mixed(self.h, uplo, n, nrhs, _p(A), _p(B), _p(X), xr, C.byref(o), C.byref(rep))
+        else:
+            rc = lib().ddla_dev_dgesv_mixed(self.h, n, nrhs, _p(A), _p(B), _p(X), xr, C.byref(o), C.byref(rep))
+        return rc, rep.as_dict()
+
+
+def measure_peaks():
+    f64, f32 = C.c_double(), C.c_double()
+    check(lib().ddla_measure_peaks(C.byref(f64), C.byref(f32)), "measure_peaks")
+    return f64.value, f32.value

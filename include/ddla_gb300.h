@@ -1,0 +1,223 @@
+/*
+ * ddla_gb300.h -- C ABI of the GB300 (sm_103a) implementation of DDLA's dense
+ * hot path: BLIS-shaped FP64 level-3 calls, the blocked LU / Cholesky / LDL^T
+ * factorizations and solves, mixed-precision solves with FP64 iterative
+ * refinement, batched small factorizations and two-operand einsum.
+ *
+ * Every entry point is `extern "C"`, takes plain pointers, sizes and element
+ * strides, and returns an int32 status:
+ *     0                 success
+ *     < 0 (> -1000)     -(position of the first invalid argument), 1-based
+ *     > 0               1-based index of the first failing pivot (singular LU
+ *                       pivot, non-positive Cholesky pivot, zero LDL^T pivot);
+ *                       DDLA throws LinalgException / ArgumentException there
+ *     DDLA_ERR_*        runtime errors (CUDA, timeout, no convergence, memory)
+ * A human-readable message for the last failure of the calling thread is
+ * available from ddla_last_error().
+ *
+ * Matrices follow DDLA's MatrixView (DDLA/Core/MatrixView.cs:22-31): a pointer
+ * to the head element plus a row stride and a column stride, in elements.
+ * Either stride may be 1; a transposed view swaps them.  Flag values are the
+ * BLIS values DDLA's enums carry (DDLA/Misc/Flags/*.cs).  dim/inc types are
+ * 64-bit (DDLA/Alias.cs:1-3); alpha and beta are passed by pointer like the
+ * `in double` of DDLA's P/Invoke declarations.
+ *
+ * Host-pointer entry points (ddla_d*) are synchronous drop-ins for the BLIS
+ * calls DDLA makes through P/Invoke: data is copied to the device, computed
+ * there and copied back before return; the caller's arrays are not retained.
+ * Device entry points (ddla_dev_*) take device pointers and a handle whose
+ * stream they are enqueued on; they return once enqueued unless stated.
+ * All entry points are thread-safe: host-pointer calls use a per-thread handle.
+ */
+#ifndef DDLA_GB300_H
+#define DDLA_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int64_t ddla_dim_t;
+typedef int64_t ddla_inc_t;
+
+/* TransType, DDLA/Misc/Flags/TransType.cs:3-9 */
+enum { DDLA_NO_TRANSPOSE = 0, DDLA_TRANSPOSE = 8, DDLA_CONJ_NO_TRANSPOSE = 16, DDLA_CONJ_TRANSPOSE = 24 };
+/* UpLo, DDLA/Misc/Flags/UpLo.cs:3-9 */
+enum { DDLA_ZEROS = 0x00, DDLA_LOWER = 0xC0, DDLA_UPPER = 0x60, DDLA_DENSE = 0xE0 };
+/* DiagType, DDLA/Misc/Flags/DiagType.cs */
+enum { DDLA_NONUNIT_DIAG = 0x000, DDLA_UNIT_DIAG = 0x100 };
+/* SideType, DDLA/Misc/Flags/SideType.cs */
+enum { DDLA_LEFT = 0, DDLA_RIGHT = 1 };
+
+/* runtime status codes (all below -1000 so they never collide with argument
+ * positions) */
+enum {
+    DDLA_OK = 0,
+    DDLA_ERR_CUDA = -1001,          /* a CUDA runtime call failed */
+    DDLA_ERR_NOMEM = -1002,         /* device or pinned allocation failed */
+    DDLA_ERR_TIMEOUT = -1003,       /* a bounded device-side wait gave up */
+    DDLA_ERR_NOT_CONVERGED = -1004, /* iterative refinement hit max_iter */
+    DDLA_ERR_UNSUPPORTED = -1005,   /* valid request this build does not cover */
+    DDLA_ERR_NO_DEVICE = -1006      /* no usable sm_103 device */
+};
+
+/* Precision of the O(n^3) work in the mixed solvers. */
+enum {
+    DDLA_PREC_FP64 = 0,      /* plain FP64 factorization (DMMA) */
+    DDLA_PREC_FP32 = 1,      /* FP32 factorization, FP32 CUDA-core GEMM updates */
+    DDLA_PREC_TF32X3 = 2,    /* FP32 factorization, 3xTF32 tcgen05 tensor-core GEMM updates */
+    DDLA_PREC_BF16X3 = 3     /* FP32 factorization, 3xBF16 tcgen05 tensor-core GEMM updates */
+};
+
+/* Options of the factorization / mixed-solver calls.  Zero-initialised means
+ * defaults.  (DDLA keeps these as mutable statics: LU.PLUBlockSize,
+ * Cholesky.BlockSize, LDLT.BlockSize = 128, DDLA/Factorizations/LU.cs:131,235,
+ * Cholesky.cs:125, LDLT.cs:139.) */
+typedef struct ddla_opts {
+    int32_t precision;     /* DDLA_PREC_*, default TF32X3 for the mixed solvers */
+    int32_t nb;            /* outer block size; 0 = automatic */
+    int32_t max_iter;      /* refinement iterations; 0 = default 30; <0 = none */
+    int32_t reserved;
+    double tol;            /* target relative backward error; 0 = 1e-14 */
+} ddla_opts;
+
+/* Result record of a mixed-precision solve. */
+typedef struct ddla_solve_report {
+    int32_t iterations;        /* refinement steps taken */
+    int32_t converged;         /* 1 when backward_error <= tol */
+    int32_t precision;         /* precision actually used for the factorization */
+    int32_t info;              /* factorization status (0 or failing pivot) */
+    double backward_error;     /* max_j ||b_j - A x_j||_inf / (||A||_inf ||x_j||_inf + ||b_j||_inf) */
+    double forward_error;      /* ||x - x_ref||_inf / ||x_ref||_inf when x_ref was given, else -1 */
+    double factor_ms;          /* device time of the factorization */
+    double refine_ms;          /* device time of the refinement loop */
+    int32_t pivots_agree;      /* LU: pivots equal to an FP64 partial-pivoting run, -1 = not measured */
+    int32_t reserved;
+} ddla_solve_report;
+
+/* ---------------------------------------------------------------- runtime */
+
+/* Message describing the calling thread's last failure ("" if none). */
+const char *ddla_last_error(void);
+/* Library version string. */
+const char *ddla_version(void);
+/* Number of kernels this library has launched in this process (all threads). */
+int64_t ddla_kernel_launches(void);
+
+typedef struct ddla_handle_s *ddla_handle;
+/* Create a handle bound to the current device and a stream (cudaStream_t cast
+ * to void*; NULL = a new non-blocking stream owned by the handle). */
+int ddla_handle_create(ddla_handle *h, void *stream);
+int ddla_handle_destroy(ddla_handle h);
+int ddla_handle_sync(ddla_handle h);
+
+/* Measure this GPU's FP64 DMMA and FP32 FFMA throughput (TFLOP/s) with
+ * bounded register-resident loops (no memory traffic). */
+int ddla_measure_peaks(double *fp64_tflops, double *fp32_tflops);
+
+/* ------------------------------------------------ BLIS-shaped level 3 (host) */
+
+/* C = beta*C + alpha*op(A)*op(B).  Replaces bli_dgemm,
+ * DDLA/BLAS/Native/3m.cs:12-24 (wrapper DDLA/BLAS/3m.cs:10-31). */
+int ddla_dgemm(int32_t transa, int32_t transb, ddla_dim_t m, ddla_dim_t n, ddla_dim_t k,
+               const double *alpha, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
+               const double *b, ddla_inc_t rsb, ddla_inc_t csb,
+               const double *beta, double *c, ddla_inc_t rsc, ddla_inc_t csc);
+
+/* Triangle of C (uploc) = beta*C + alpha*op(A)*op(B), C m x m.  Replaces
+ * bli_dgemmt, DDLA/BLAS/Native/3m.cs:26-38 (wrapper DDLA/BLAS/3m.cs:44-70). */
+int ddla_dgemmt(int32_t uploc, int32_t transa, int32_t transb, ddla_dim_t m, ddla_dim_t k,
+                const double *alpha, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
+                const double *b, ddla_inc_t rsb, ddla_inc_t csb,
+                const double *beta, double *c, ddla_inc_t rsc, ddla_inc_t csc);
+
+/* Triangle of C = beta*C + alpha*op(A)*op(A)^T.  Replaces bli_dsyrk,
+ * DDLA/BLAS/Native/3m.cs:96-106 (wrapper DDLA/BLAS/3m.cs:118-138). */
+int ddla_dsyrk(int32_t uploc, int32_t transa, ddla_dim_t m, ddla_dim_t k,
+               const double *alpha, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
+               const double *beta, double *c, ddla_inc_t rsc, ddla_inc_t csc);
+
+/* Left: solve op(A) X = alpha B; Right: X op(A) = alpha B; B <- X.  Replaces
+ * bli_dtrsm, DDLA/BLAS/Native/3m.cs:151-162 (wrapper DDLA/BLAS/3m.cs:287-305). */
+int ddla_dtrsm(int32_t side, int32_t uploa, int32_t transa, int32_t diaga, ddla_dim_t m, ddla_dim_t n,
+               const double *alpha, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
+               double *b, ddla_inc_t rsb, ddla_inc_t csb);
+
+/* ------------------------------------------------ factorizations (host) */
+
+/* In-place LU with partial pivoting; piv[i] is RELATIVE (row i swapped with
+ * row i + piv[i]) exactly as LU.PLUDecompose, DDLA/Factorizations/LU.cs:251-264. */
+int ddla_dgetrf(ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t csa, int32_t *piv, const ddla_opts *opts);
+/* Solve with the factors of ddla_dgetrf (trans != 0: A^T X = B).
+ * LU.PLUSolve, LU.cs:266-287, 431-465. */
+int ddla_dgetrs(int32_t trans, ddla_dim_t n, ddla_dim_t nrhs, const double *lu, ddla_inc_t rsa, ddla_inc_t csa,
+                const int32_t *piv, double *b, ddla_inc_t rsb, ddla_inc_t csb);
+/* In-place LU without pivoting, LU.LUDecompose, LU.cs:133-142, 169-203. */
+int ddla_dgetrf_nopiv(ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t csa, const ddla_opts *opts);
+/* LU.LUSolve, LU.cs:144-167, 205-231. */
+int ddla_dgetrs_nopiv(int32_t trans, ddla_dim_t n, ddla_dim_t nrhs, const double *lu, ddla_inc_t rsa, ddla_inc_t csa,
+                      double *b, ddla_inc_t rsb, ddla_inc_t csb);
+/* In-place Cholesky of the uplo triangle, Cholesky.CholDecompose,
+ * DDLA/Factorizations/Cholesky.cs:52-69. */
+int ddla_dpotrf(int32_t uplo, ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t csa, const ddla_opts *opts);
+/* Cholesky.CholeskySolve, Cholesky.cs:102-123, 210-226. */
+int ddla_dpotrs(int32_t uplo, ddla_dim_t n, ddla_dim_t nrhs, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
+                double *b, ddla_inc_t rsb, ddla_inc_t csb);
+/* In-place unpivoted LDL^T, LDLT.LDLTDecompose, DDLA/Factorizations/LDLT.cs:56-73. */
+int ddla_dldlt(int32_t uplo, ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t csa, const ddla_opts *opts);
+/* LDLT.LDLTSolve, LDLT.cs:105-126, 267-295. */
+int ddla_dldlts(int32_t uplo, ddla_dim_t n, ddla_dim_t nrhs, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
+                double *b, ddla_inc_t rsb, ddla_inc_t csb);
+
+/* Mixed-precision solves: factor in opts->precision, refine in FP64 until the
+ * relative backward error is <= opts->tol.  A and B are read only; X receives
+ * the solution.  x_ref (may be NULL) is an oracle solution for the forward
+ * error.  No reference counterpart: DDLA's LU(A).Solve / Cholesky(A).Solve
+ * (LU.cs:64-100, Cholesky.cs:71-88) are FP64-only. */
+int ddla_dgesv_mixed(ddla_dim_t n, ddla_dim_t nrhs, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
+                     const double *b, ddla_inc_t rsb, ddla_inc_t csb, double *x, ddla_inc_t rsx, ddla_inc_t csx,
+                     const double *x_ref, const ddla_opts *opts, ddla_solve_report *report);
+int ddla_dposv_mixed(int32_t uplo, ddla_dim_t n, ddla_dim_t nrhs, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
+                     const double *b, ddla_inc_t rsb, ddla_inc_t csb, double *x, ddla_inc_t rsx, ddla_inc_t csx,
+                     const double *x_ref, const ddla_opts *opts, ddla_solve_report *report);
+
+/* ------------------------------------------------ device-resident variants */
+/* Same semantics as the host calls; pointers are device pointers; work is
+ * enqueued on the handle's stream.  Factorization statuses > 0 are produced
+ * on the device: these calls synchronize the stream to return them. */
+int ddla_dev_dgemm(ddla_handle h, int32_t transa, int32_t transb, ddla_dim_t m, ddla_dim_t n, ddla_dim_t k,
+                   double alpha, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
+                   const double *b, ddla_inc_t rsb, ddla_inc_t csb,
+                   double beta, double *c, ddla_inc_t rsc, ddla_inc_t csc);
+int ddla_dev_dgemmt(ddla_handle h, int32_t uploc, int32_t transa, int32_t transb, ddla_dim_t m, ddla_dim_t k,
+                    double alpha, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
+                    const double *b, ddla_inc_t rsb, ddla_inc_t csb,
+                    double beta, double *c, ddla_inc_t rsc, ddla_inc_t csc);
+int ddla_dev_dtrsm(ddla_handle h, int32_t side, int32_t uploa, int32_t transa, int32_t diaga, ddla_dim_t m,
+                   ddla_dim_t n, double alpha, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
+                   double *b, ddla_inc_t rsb, ddla_inc_t csb);
+int ddla_dev_dgetrf(ddla_handle h, ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t csa, int32_t *piv,
+                    const ddla_opts *opts);
+int ddla_dev_dgetrs(ddla_handle h, int32_t trans, ddla_dim_t n, ddla_dim_t nrhs, const double *lu, ddla_inc_t rsa,
+                    ddla_inc_t csa, const int32_t *piv, double *b, ddla_inc_t rsb, ddla_inc_t csb);
+int ddla_dev_dpotrf(ddla_handle h, int32_t uplo, ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t csa,
+                    const ddla_opts *opts);
+int ddla_dev_dpotrs(ddla_handle h, int32_t uplo, ddla_dim_t n, ddla_dim_t nrhs, const double *a, ddla_inc_t rsa,
+                    ddla_inc_t csa, double *b, ddla_inc_t rsb, ddla_inc_t csb);
+int ddla_dev_dldlt(ddla_handle h, int32_t uplo, ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t csa,
+                   const ddla_opts *opts);
+int ddla_dev_dldlts(ddla_handle h, int32_t uplo, ddla_dim_t n, ddla_dim_t nrhs, const double *a, ddla_inc_t rsa,
+                    ddla_inc_t csa, double *b, ddla_inc_t rsb, ddla_inc_t csb);
+/* Mixed solves on device data (A, B row-major contiguous n x n, n x nrhs;
+ * X n x nrhs row-major).  Synchronous (returns the report). */
+int ddla_dev_dgesv_mixed(ddla_handle h, ddla_dim_t n, ddla_dim_t nrhs, const double *a, const double *b, double *x,
+                         const double *x_ref, const ddla_opts *opts, ddla_solve_report *report);
+int ddla_dev_dposv_mixed(ddla_handle h, int32_t uplo, ddla_dim_t n, ddla_dim_t nrhs, const double *a,
+                         const double *b, double *x, const double *x_ref, const ddla_opts *opts,
+                         ddla_solve_report *report);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DDLA_GB300_H */

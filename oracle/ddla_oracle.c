@@ -1,0 +1,839 @@
+/*
+ * ddla_oracle.c -- TEST INFRASTRUCTURE ONLY.
+ *
+ * CPU restatement of DDLA's FP64 dense hot path, used as the parity oracle by
+ * tests/, by __graft_entry__.smoke() and by bench.py's CPU-baseline leg.  It is
+ * never linked into, loaded by, or called from the product library
+ * (ddla_gb300/), which must fail loudly when its CUDA build is missing.
+ *
+ * Parity status: UNPINNED.  DDLA (C#/.NET) cannot be built or run here (no .NET
+ * runtime; its micro-kernel needs x86 AVX2; its factorizations P/Invoke a
+ * closed Windows BLIS DLL) and it ships no golden vectors.  This file is pinned
+ * instead against (a) the property checks of DDLA's own tests at their sizes and
+ * tolerances and (b) an independent LAPACK (scipy) on the same inputs -- see
+ * tests/test_oracle.py.
+ *
+ * Every routine cites the reference file:line it restates (paths relative to
+ * the DDLA repository root).  BLIS routines that DDLA delegates to (gemm, trsm,
+ * syrk, ger, amaxv, scalv) follow BLIS's documented typed-API semantics, with
+ * the blocking structure of DDLA's managed provider where one exists.
+ *
+ * Conventions: a matrix is (pointer to head element, rows, cols, row stride,
+ * column stride) in elements, exactly like DDLA's MatrixView
+ * (DDLA/Core/MatrixView.cs:22-31); transposition swaps rows/cols and strides
+ * (DDLA/Core/MatrixView.cs:481).  Flag values are BLIS's
+ * (DDLA/Misc/Flags/*.cs).  Status: 0 ok, >0 = 1-based index of the failing
+ * pivot (DDLA throws LinalgException / ArgumentException there), <0 = bad
+ * argument.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+typedef int64_t i64;
+
+enum { TR_NO = 0, TR_T = 8 };            /* TransType  DDLA/Misc/Flags/TransType.cs:3-9 */
+enum { UL_LOWER = 0xC0, UL_UPPER = 0x60, UL_DENSE = 0xE0 }; /* UpLo DDLA/Misc/Flags/UpLo.cs:3-9 */
+enum { DG_NONUNIT = 0, DG_UNIT = 0x100 }; /* DiagType DDLA/Misc/Flags/DiagType.cs */
+enum { SD_LEFT = 0, SD_RIGHT = 1 };        /* SideType DDLA/Misc/Flags/SideType.cs */
+
+/* GEMMKernel blocking constants, DDLA/Einsum/GEMMKernel.cs:11-21 */
+#define MC 510
+#define NC 512
+#define KC 144
+#define MR 6
+#define NR 8
+#define KR 6
+/* Block sizes of the factorizations: LU.cs:131,235, Cholesky.cs:125, LDLT.cs:139 */
+#define NB 128
+
+typedef struct { double *p; i64 r, c, rs, cs; } mat;
+
+static inline double *AT(mat A, i64 i, i64 j) { return A.p + i * A.rs + j * A.cs; }
+static inline mat mk(double *p, i64 r, i64 c, i64 rs, i64 cs) { mat m = {p, r, c, rs, cs}; return m; }
+static inline mat tr(mat A) { mat m = {A.p, A.c, A.r, A.cs, A.rs}; return m; }
+static inline mat sub(mat A, i64 i, i64 ni, i64 j, i64 nj) {
+    mat m = {A.p + i * A.rs + j * A.cs, ni, nj, A.rs, A.cs}; return m;
+}
+static inline int flip_uplo(int u) { return u == UL_LOWER ? UL_UPPER : (u == UL_UPPER ? UL_LOWER : u); }
+static inline i64 align_up(i64 x, i64 a) { return (x + a - 1) / a * a; }
+
+static int g_threads = 1;
+void orc_set_threads(int n) { g_threads = n < 1 ? 1 : n; }
+int orc_get_threads(void) { return g_threads; }
+int orc_has_openmp(void) {
+#ifdef _OPENMP
+    return 1;
+#else
+    return 0;
+#endif
+}
+
+/* ------------------------------------------------------------------------ */
+/* Level-1/2 primitives                                                      */
+/* ------------------------------------------------------------------------ */
+
+/* Scal on a matrix (triangle): alpha==0 sets zero, alpha!=1 multiplies.
+ * DDLA/BLAS/Managed/1m.cs:251-300, DDLA/BLAS/Managed/1v.cs:294-300. */
+static void scal_m(int uplo, double alpha, mat A) {
+    if (alpha == 1.0) return;
+    for (i64 i = 0; i < A.r; i++) {
+        i64 j0 = 0, j1 = A.c;
+        if (uplo == UL_LOWER) j1 = i + 1 < A.c ? i + 1 : A.c;
+        if (uplo == UL_UPPER) j0 = i;
+        for (i64 j = j0; j < j1; j++) {
+            double *x = AT(A, i, j);
+            *x = (alpha == 0.0) ? 0.0 : *x * alpha;
+        }
+    }
+}
+
+/* bli_damaxv as documented by DDLA (DDLA/BLAS/1v.cs:29-42): index of the first
+ * element of largest |x|; NaN compares smaller than every other value; an
+ * empty vector gives 0. */
+i64 orc_damax(i64 n, const double *x, i64 inc) {
+    i64 best = 0;
+    double bv = -1.0;
+    for (i64 i = 0; i < n; i++) {
+        double v = fabs(x[i * inc]);
+        if (v > bv) { bv = v; best = i; }
+    }
+    return best;
+}
+
+static void swap_rows(mat A, i64 i, i64 j) {   /* MatrixView.SwapRow, Managed/1v.cs:324-328 */
+    if (i == j) return;
+    for (i64 c = 0; c < A.c; c++) { double t = *AT(A, i, c); *AT(A, i, c) = *AT(A, j, c); *AT(A, j, c) = t; }
+}
+
+/* A += alpha * x * y^T (bli_dger, DDLA/BLAS/2m.cs:35-49): column-wise axpy with
+ * the scalar alpha*y[j], fused multiply-add. */
+static void ger(double alpha, const double *x, i64 incx, const double *y, i64 incy, mat A) {
+    for (i64 j = 0; j < A.c; j++) {
+        double s = alpha * y[j * incy];
+        for (i64 i = 0; i < A.r; i++) *AT(A, i, j) = fma(x[i * incx], s, *AT(A, i, j));
+    }
+}
+
+/* Symmetric rank-1 on one triangle: A += alpha*x*x^T (managed SyR,
+ * DDLA/BLAS/Managed/2m.cs:381-421: row i gets fma(x[j], alpha*x[i], A[i][j])). */
+static void syr(int uplo, double alpha, const double *x, i64 incx, mat A) {
+    for (i64 i = 0; i < A.r; i++) {
+        double s = alpha * x[i * incx];
+        i64 j0 = uplo == UL_LOWER ? 0 : i, j1 = uplo == UL_LOWER ? i + 1 : A.c;
+        for (i64 j = j0; j < j1; j++) *AT(A, i, j) = fma(x[j * incx], s, *AT(A, i, j));
+    }
+}
+
+/* x *= 1/alpha (InvScal: native DDLA/BLAS/1v.cs:97-103 rejects alpha==0; the
+ * managed one DDLA/BLAS/Managed/1v.cs:283-292 also rejects non-finite alpha
+ * and skips alpha==1).  Returns 0 or -1 when DDLA would throw. */
+static int invscal(double alpha, double *x, i64 n, i64 inc, int managed) {
+    if (alpha == 0.0) return -1;
+    if (managed && !isfinite(alpha)) return -1;
+    if (managed && alpha == 1.0) return 0;
+    double s = 1.0 / alpha;
+    for (i64 i = 0; i < n; i++) x[i * inc] *= s;
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* GEMM: DDLA's managed BLIS-style 5-loop algorithm                          */
+/* ------------------------------------------------------------------------ */
+
+/* 6x8 micro-kernel, DDLA/Einsum/GEMMKernel.cs:36-233: for each k (ascending) one
+ * fused multiply-add per output element into a fresh accumulator; output tile
+ * stored row-major. */
+static void micro(i64 kc, const double *a, const double *b, double *c) {
+    double acc[MR][NR];
+    for (int r = 0; r < MR; r++) for (int s = 0; s < NR; s++) acc[r][s] = 0.0;
+    for (i64 k = 0; k < kc; k++) {
+        const double *ak = a + k * MR, *bk = b + k * NR;
+        for (int r = 0; r < MR; r++) {
+            double av = ak[r];
+            for (int s = 0; s < NR; s++) acc[r][s] = fma(av, bk[s], acc[r][s]);
+        }
+    }
+    for (int r = 0; r < MR; r++) for (int s = 0; s < NR; s++) c[r * NR + s] = acc[r][s];
+}
+
+/* GEPack, DDLA/BLAS/Managed/3m/Packing.cs:30-101: panels of `blk` rows, each
+ * stored [col][row] with zero padding of the ragged last panel. */
+static void pack(mat S, double *buf, int blk) {
+    i64 np = align_up(S.r, blk) / blk;
+    for (i64 pi = 0; pi < np; pi++) {
+        double *dst = buf + pi * S.c * blk;
+        i64 r0 = pi * blk, ar = S.r - r0 < blk ? S.r - r0 : blk;
+        for (i64 col = 0; col < S.c; col++)
+            for (int r = 0; r < blk; r++) *dst++ = r < ar ? *AT(S, r0 + r, col) : 0.0;
+    }
+}
+
+/* Macro kernel, DDLA/BLAS/Managed/3m/MacroKernel.cs:69-96 (GEMM) and :147-216
+ * (GEMMT masks).  tri: 0 = full tile add via fused axpy (Managed/1m.cs:86-158),
+ * UL_LOWER/UL_UPPER = masked scalar add alpha*t + c (MacroKernel.cs:177-211). */
+static void macro(i64 mc, i64 nc, i64 kc, double alpha, const double *bufA, const double *bufB,
+                  mat C, int tri, i64 diag0) {
+    i64 ip = align_up(mc, MR) / MR;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(g_threads) if (g_threads > 1 && ip >= 8)
+#endif
+    for (i64 i = 0; i < ip; i++) {
+        double t[MR * NR];
+        i64 amr = mc - i * MR < MR ? mc - i * MR : MR;
+        for (i64 j = 0; j < align_up(nc, NR); j += NR) {
+            i64 anr = nc - j < NR ? nc - j : NR;
+            mat Ct = sub(C, i * MR, amr, j, anr);
+            if (tri == 0) {
+                micro(kc, bufA + i * kc * MR, bufB + j * kc, t);
+                for (i64 r = 0; r < amr; r++)
+                    for (i64 s = 0; s < anr; s++) *AT(Ct, r, s) = fma(t[r * NR + s], alpha, *AT(Ct, r, s));
+            } else {
+                i64 diag = diag0 + i * MR - j;
+                if (tri == UL_UPPER && diag >= anr) continue;
+                if (tri == UL_LOWER && diag <= -amr) continue;
+                micro(kc, bufA + i * kc * MR, bufB + j * kc, t);
+                for (i64 r = 0; r < amr; r++) {
+                    i64 s0 = 0, s1 = anr;
+                    if (tri == UL_UPPER) { s0 = r + diag; if (s0 > anr) s0 = anr; if (s0 < 0) s0 = 0; }
+                    else { s1 = r + diag + 1; if (s1 < 0) s1 = 0; if (s1 > anr) s1 = anr; }
+                    for (i64 s = s0; s < s1; s++) *AT(Ct, r, s) = alpha * t[r * NR + s] + *AT(Ct, r, s);
+                }
+            }
+        }
+    }
+}
+
+/* GeMMInner / GeMMT loops, DDLA/BLAS/Managed/3m/GeMM.cs:14-73 and
+ * DDLA/BLAS/Managed/3m.cs:75-130.  C is already beta-scaled. */
+static void gemm_core(double alpha, mat A, mat B, mat C, int tri) {
+    i64 m = C.r, n = C.c, k = A.c;
+    if (C.cs < C.rs) {              /* prefer row-major C: solve the transposed problem */
+        mat T = A; A = tr(B); B = tr(T); C = tr(C);
+        m = C.r; n = C.c;
+        if (tri) tri = flip_uplo(tri);
+    }
+    if (m == 0 || n == 0 || k == 0) return;
+    i64 mce = MC < align_up(m, MR) ? MC : align_up(m, MR);
+    i64 nce = NC < align_up(n, NR) ? NC : align_up(n, NR);
+    double *bufA = (double *)malloc(sizeof(double) * mce * KC);
+    double *bufB = (double *)malloc(sizeof(double) * KC * nce);
+    for (i64 ic = 0; ic < m; ic += MC) {
+        i64 mc = m - ic < MC ? m - ic : MC;
+        for (i64 pc = 0; pc < k; pc += KC) {
+            i64 kc = k - pc < KC ? k - pc : KC;
+            pack(sub(A, ic, mc, pc, kc), bufA, MR);
+            for (i64 jc = 0; jc < n; jc += NC) {
+                i64 nc = n - jc < NC ? n - jc : NC;
+                pack(tr(sub(B, pc, kc, jc, nc)), bufB, NR);
+                macro(mc, nc, kc, alpha, bufA, bufB, sub(C, ic, mc, jc, nc), tri, ic - jc);
+            }
+        }
+    }
+    free(bufA); free(bufB);
+}
+
+/* C = beta*C + alpha*op(A)*op(B); DDLA/BLAS/Managed/3m.cs:13-39 (beta first). */
+void orc_dgemm(int ta, int tb, i64 m, i64 n, i64 k, double alpha,
+               const double *a, i64 rsa, i64 csa, const double *b, i64 rsb, i64 csb,
+               double beta, double *c, i64 rsc, i64 csc) {
+    mat A = mk((double *)a, ta == TR_T ? k : m, ta == TR_T ? m : k, rsa, csa);
+    mat B = mk((double *)b, tb == TR_T ? n : k, tb == TR_T ? k : n, rsb, csb);
+    if (ta == TR_T) A = tr(A);
+    if (tb == TR_T) B = tr(B);
+    mat C = mk(c, m, n, rsc, csc);
+    if (m == 0 || n == 0) return;
+    scal_m(UL_DENSE, beta, C);
+    if (k == 0) return;
+    gemm_core(alpha, A, B, C, 0);
+}
+
+/* C(uplo triangle) = beta*C + alpha*op(A)*op(B); DDLA/BLAS/Managed/3m.cs:51-131. */
+void orc_dgemmt(int uplo, int ta, int tb, i64 m, i64 k, double alpha,
+                const double *a, i64 rsa, i64 csa, const double *b, i64 rsb, i64 csb,
+                double beta, double *c, i64 rsc, i64 csc) {
+    mat A = mk((double *)a, ta == TR_T ? k : m, ta == TR_T ? m : k, rsa, csa);
+    mat B = mk((double *)b, tb == TR_T ? m : k, tb == TR_T ? k : m, rsb, csb);
+    if (ta == TR_T) A = tr(A);
+    if (tb == TR_T) B = tr(B);
+    mat C = mk(c, m, m, rsc, csc);
+    if (m == 0) return;
+    scal_m(uplo, beta, C);
+    if (k == 0) return;
+    gemm_core(alpha, A, B, C, uplo);
+}
+
+/* SYRK as GEMMT(A, A^T), DDLA/BLAS/Managed/3m.cs:200-216. */
+void orc_dsyrk(int uplo, int ta, i64 m, i64 k, double alpha, const double *a, i64 rsa, i64 csa,
+               double beta, double *c, i64 rsc, i64 csc) {
+    mat A = mk((double *)a, ta == TR_T ? k : m, ta == TR_T ? m : k, rsa, csa);
+    if (ta == TR_T) A = tr(A);
+    mat C = mk(c, m, m, rsc, csc);
+    if (m == 0) return;
+    scal_m(uplo, beta, C);
+    if (k == 0) return;
+    gemm_core(alpha, A, tr(A), C, uplo);
+}
+
+/* ------------------------------------------------------------------------ */
+/* TRSM / TRSV                                                              */
+/* ------------------------------------------------------------------------ */
+
+/* Triangular solve with one vector, column-oriented (DDLA/BLAS/Managed/2m.cs:625-865). */
+static void trsv(int uplo, int unit, mat A, double *x, i64 inc) {
+    i64 n = A.r;
+    if (uplo == UL_LOWER) {
+        for (i64 j = 0; j < n; j++) {
+            if (!unit) x[j * inc] /= *AT(A, j, j);
+            double xj = -x[j * inc];
+            for (i64 i = j + 1; i < n; i++) x[i * inc] = fma(*AT(A, i, j), xj, x[i * inc]);
+        }
+    } else {
+        for (i64 j = n - 1; j >= 0; j--) {
+            if (!unit) x[j * inc] /= *AT(A, j, j);
+            double xj = -x[j * inc];
+            for (i64 i = 0; i < j; i++) x[i * inc] = fma(*AT(A, i, j), xj, x[i * inc]);
+        }
+    }
+}
+
+/* Left solve tri(A)*X = B in KC-row blocks: GEMM update of the block from the
+ * solved part, then a TRSV per column (DDLA/BLAS/Managed/3m/TrSM.cs:62-122). */
+static void trsm_left(int uplo, int unit, mat A, mat B) {
+    i64 m = B.r;
+    if (uplo == UL_LOWER) {
+        for (i64 i0 = 0; i0 < m; i0 += KC) {
+            i64 b = m - i0 < KC ? m - i0 : KC;
+            if (i0 > 0) gemm_core(-1.0, sub(A, i0, b, 0, i0), sub(B, 0, i0, 0, B.c), sub(B, i0, b, 0, B.c), 0);
+            mat A11 = sub(A, i0, b, i0, b);
+            for (i64 j = 0; j < B.c; j++) trsv(UL_LOWER, unit, A11, AT(B, i0, j), B.rs);
+        }
+    } else {
+        for (i64 i1 = m; i1 > 0; i1 -= KC) {
+            i64 b = i1 < KC ? i1 : KC, i0 = i1 - b;
+            if (i1 < m) gemm_core(-1.0, sub(A, i0, b, i1, m - i1), sub(B, i1, m - i1, 0, B.c), sub(B, i0, b, 0, B.c), 0);
+            mat A11 = sub(A, i0, b, i0, b);
+            for (i64 j = 0; j < B.c; j++) trsv(UL_UPPER, unit, A11, AT(B, i0, j), B.rs);
+        }
+    }
+}
+
+/* bli_dtrsm semantics (DDLA/BLAS/3m.cs:276-305): Left solves op(A)*X = alpha*B,
+ * Right solves X*op(A) = alpha*B, B overwritten.  alpha is applied first
+ * (DDLA/BLAS/Managed/3m.cs:434).  A right solve is the left solve of the
+ * transposed system. */
+void orc_dtrsm(int side, int uplo, int ta, int diag, i64 m, i64 n, double alpha,
+               const double *a, i64 rsa, i64 csa, double *b, i64 rsb, i64 csb) {
+    i64 na = side == SD_LEFT ? m : n;
+    mat A = mk((double *)a, na, na, rsa, csa);
+    mat B = mk(b, m, n, rsb, csb);
+    if (m == 0 || n == 0) return;
+    scal_m(UL_DENSE, alpha, B);
+    if (ta == TR_T) { A = tr(A); uplo = flip_uplo(uplo); }
+    if (side == SD_RIGHT) { A = tr(A); uplo = flip_uplo(uplo); B = tr(B); }
+    trsm_left(uplo, diag == DG_UNIT, A, B);
+}
+
+/* ------------------------------------------------------------------------ */
+/* LU with partial pivoting, DDLA/Factorizations/LU.cs                      */
+/* ------------------------------------------------------------------------ */
+
+/* PLUDecUnblock, LU.cs:344-374: per column AMax (relative pivot), swap whole
+ * panel rows, InvScal (native: throws on 0), GeR(-1).  `row0` is the global
+ * index of the panel's first row for the status code. */
+static int plu_unblock(mat A, int *piv, i64 row0) {
+    i64 len = A.r < A.c ? A.r : A.c;
+    for (i64 i = 0; i < len; i++) {
+        i64 ip = orc_damax(A.r - i, AT(A, i, i), A.rs);
+        piv[i] = (int)ip;
+        if (ip != 0) swap_rows(sub(A, i, A.r - i, 0, A.c), 0, ip);
+        double a11 = *AT(A, i, i);
+        if (invscal(a11, AT(A, i + 1, i), A.r - i - 1, A.rs, 0)) return (int)(row0 + i + 1);
+        ger(-1.0, AT(A, i + 1, i), A.rs, AT(A, i, i + 1), A.cs, sub(A, i + 1, A.r - i - 1, i + 1, A.c - i - 1));
+    }
+    return 0;
+}
+
+/* ApplyPivInternel (Left), LU.cs:376-404: forward applies swaps i <-> i+p[i]
+ * in increasing i, backward in decreasing i. */
+static void apply_piv(mat X, const int *piv, i64 np, int forward) {
+    if (X.r == 0 || X.c == 0) return;
+    if (forward) { for (i64 i = 0; i < np; i++) if (piv[i] > 0) swap_rows(X, i, i + piv[i]); }
+    else { for (i64 i = np - 1; i >= 0; i--) if (piv[i] > 0) swap_rows(X, i, i + piv[i]); }
+}
+
+/* PLUDecompose / PLUDecBlock, LU.cs:251-264, 289-342 (blocked iff n >= 128). */
+int orc_dgetrf(i64 n, double *a, i64 rs, i64 cs, int *piv) {
+    mat A = mk(a, n, n, rs, cs);
+    if (n < NB) return plu_unblock(A, piv, 0);
+    for (i64 j0 = 0; j0 < n; j0 += NB) {
+        i64 b = n - j0 < NB ? n - j0 : NB;
+        int info = plu_unblock(sub(A, j0, n - j0, j0, b), piv + j0, j0);
+        if (info) return info;
+        apply_piv(sub(A, j0, n - j0, 0, j0), piv + j0, b, 1);
+        apply_piv(sub(A, j0, n - j0, j0 + b, n - j0 - b), piv + j0, b, 1);
+        i64 r = n - j0 - b;
+        if (r > 0) {
+            mat A11 = sub(A, j0, b, j0, b), A12 = sub(A, j0, b, j0 + b, r);
+            trsm_left(UL_LOWER, 1, A11, A12);
+            gemm_core(-1.0, sub(A, j0 + b, r, j0, b), A12, sub(A, j0 + b, r, j0 + b, r), 0);
+        }
+    }
+    return 0;
+}
+
+/* PLUSolveInternel, LU.cs:431-465. */
+void orc_dgetrs(int trans, i64 n, i64 nrhs, const double *a, i64 rs, i64 cs, const int *piv,
+                double *b, i64 rsb, i64 csb) {
+    if (n == 0 || nrhs == 0) return;
+    mat B = mk(b, n, nrhs, rsb, csb);
+    if (!trans) {
+        apply_piv(B, piv, n, 1);
+        orc_dtrsm(SD_LEFT, UL_LOWER, TR_NO, DG_UNIT, n, nrhs, 1.0, a, rs, cs, b, rsb, csb);
+        orc_dtrsm(SD_LEFT, UL_UPPER, TR_NO, DG_NONUNIT, n, nrhs, 1.0, a, rs, cs, b, rsb, csb);
+    } else {
+        orc_dtrsm(SD_LEFT, UL_UPPER, TR_T, DG_NONUNIT, n, nrhs, 1.0, a, rs, cs, b, rsb, csb);
+        orc_dtrsm(SD_LEFT, UL_LOWER, TR_T, DG_UNIT, n, nrhs, 1.0, a, rs, cs, b, rsb, csb);
+        apply_piv(B, piv, n, 0);
+    }
+}
+
+/* LU without pivoting: LUDecUnblock LU.cs:188-203 (pivots 0..n-2 checked),
+ * LUDecBlock LU.cs:169-186 (blocked iff n > 128). */
+static int lu_unblock(mat A, i64 row0) {
+    i64 len = A.r < A.c ? A.r : A.c;
+    for (i64 i = 0; i + 1 < len; i++) {
+        if (invscal(*AT(A, i, i), AT(A, i + 1, i), A.r - i - 1, A.rs, 0)) return (int)(row0 + i + 1);
+        ger(-1.0, AT(A, i + 1, i), A.rs, AT(A, i, i + 1), A.cs, sub(A, i + 1, A.r - i - 1, i + 1, A.c - i - 1));
+    }
+    return 0;
+}
+
+int orc_dgetrf_nopiv(i64 n, double *a, i64 rs, i64 cs) {
+    mat A = mk(a, n, n, rs, cs);
+    if (n <= NB) return lu_unblock(A, 0);
+    for (i64 j0 = 0; j0 < n; j0 += NB) {
+        i64 b = n - j0 < NB ? n - j0 : NB, r = n - j0 - b;
+        mat A11 = sub(A, j0, b, j0, b);
+        int info = lu_unblock(A11, j0);
+        if (info) return info;
+        if (r > 0) {
+            mat A12 = sub(A, j0, b, j0 + b, r), A21 = sub(A, j0 + b, r, j0, b);
+            trsm_left(UL_LOWER, 1, A11, A12);
+            trsm_left(UL_LOWER, 0, tr(A11), tr(A21));       /* X * U11 = A21 */
+            gemm_core(-1.0, A21, A12, sub(A, j0 + b, r, j0 + b, r), 0);
+        }
+    }
+    return 0;
+}
+
+/* LUSolveInternal, LU.cs:205-231 for trans == 0.  For trans != 0 this solves
+ * A^T X = B (U^T first, then L^T); DDLA's code applies the two transposed
+ * solves in the opposite order. */
+void orc_dgetrs_nopiv(int trans, i64 n, i64 nrhs, const double *a, i64 rs, i64 cs,
+                      double *b, i64 rsb, i64 csb) {
+    if (n == 0 || nrhs == 0) return;
+    if (!trans) {
+        orc_dtrsm(SD_LEFT, UL_LOWER, TR_NO, DG_UNIT, n, nrhs, 1.0, a, rs, cs, b, rsb, csb);
+        orc_dtrsm(SD_LEFT, UL_UPPER, TR_NO, DG_NONUNIT, n, nrhs, 1.0, a, rs, cs, b, rsb, csb);
+    } else {
+        orc_dtrsm(SD_LEFT, UL_UPPER, TR_T, DG_NONUNIT, n, nrhs, 1.0, a, rs, cs, b, rsb, csb);
+        orc_dtrsm(SD_LEFT, UL_LOWER, TR_T, DG_UNIT, n, nrhs, 1.0, a, rs, cs, b, rsb, csb);
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Cholesky, DDLA/Factorizations/Cholesky.cs                                */
+/* ------------------------------------------------------------------------ */
+
+/* CholeskyLowerUnblock, Cholesky.cs:127-140 with Sqrt :228-236 (finite <= 0
+ * throws) and managed InvScaled (non-finite throws). */
+static int chol_lower_unblock(mat A, i64 row0) {
+    for (i64 i = 0; i < A.r; i++) {
+        double *a11 = AT(A, i, i);
+        if (isfinite(*a11) && *a11 <= 0) return (int)(row0 + i + 1);
+        *a11 = sqrt(*a11);
+        if (invscal(*a11, AT(A, i + 1, i), A.r - i - 1, A.rs, 1)) return (int)(row0 + i + 1);
+        syr(UL_LOWER, -1.0, AT(A, i + 1, i), A.rs, sub(A, i + 1, A.r - i - 1, i + 1, A.r - i - 1));
+    }
+    return 0;
+}
+
+/* CholeskyUpperUnblock, Cholesky.cs:162-186: dot-product form, no <=0 check
+ * (sqrt of a negative gives NaN which the managed InvScaled then rejects). */
+static int chol_upper_unblock(mat A, i64 row0) {
+    i64 n = A.r;
+    for (i64 i = 0; i < n; i++) {
+        double *a11 = AT(A, i, i);
+        double d = 0.0;
+        for (i64 p = 0; p < i; p++) d = fma(*AT(A, p, i), *AT(A, p, i), d);
+        *a11 -= d;
+        *a11 = sqrt(*a11);
+        /* a12 -= A02^T a01 */
+        for (i64 j = i + 1; j < n; j++) {
+            double s = 0.0;
+            for (i64 p = 0; p < i; p++) s = fma(*AT(A, p, j), *AT(A, p, i), s);
+            *AT(A, i, j) -= s;
+        }
+        if (invscal(*a11, AT(A, i, i + 1), n - i - 1, A.cs, 1)) return (int)(row0 + i + 1);
+    }
+    return 0;
+}
+
+int orc_dpotrf(int uplo, i64 n, double *a, i64 rs, i64 cs) {
+    mat A = mk(a, n, n, rs, cs);
+    if (n <= NB) return uplo == UL_LOWER ? chol_lower_unblock(A, 0) : chol_upper_unblock(A, 0);
+    for (i64 j0 = 0; j0 < n; j0 += NB) {
+        i64 b = n - j0 < NB ? n - j0 : NB, r = n - j0 - b;
+        mat A11 = sub(A, j0, b, j0, b);
+        if (uplo == UL_LOWER) {
+            /* CholeskyLowerBlock, Cholesky.cs:142-160 */
+            int info = chol_lower_unblock(A11, j0);
+            if (info) return info;
+            if (r > 0) {
+                mat A21 = sub(A, j0 + b, r, j0, b);
+                trsm_left(UL_LOWER, 0, A11, tr(A21));       /* A21 * L11^-T: L11 X^T = A21^T */
+                gemm_core(-1.0, A21, tr(A21), sub(A, j0 + b, r, j0 + b, r), UL_LOWER);
+            }
+        } else {
+            /* CholeskyUpperBlock, Cholesky.cs:188-208 */
+            int info = chol_upper_unblock(A11, j0);
+            if (info) return info;
+            if (r > 0) {
+                mat A12 = sub(A, j0, b, j0 + b, r);
+                trsm_left(UL_LOWER, 0, tr(A11), A12);         /* U11^T X = A12 */
+                gemm_core(-1.0, tr(A12), A12, sub(A, j0 + b, r, j0 + b, r), UL_UPPER);
+            }
+        }
+    }
+    return 0;
+}
+
+/* CholeskySolveUncheck, Cholesky.cs:210-226. */
+void orc_dpotrs(int uplo, i64 n, i64 nrhs, const double *a, i64 rs, i64 cs, double *b, i64 rsb, i64 csb) {
+    if (n == 0 || nrhs == 0) return;
+    if (uplo == UL_LOWER) {
+        orc_dtrsm(SD_LEFT, UL_LOWER, TR_NO, DG_NONUNIT, n, nrhs, 1.0, a, rs, cs, b, rsb, csb);
+        orc_dtrsm(SD_LEFT, UL_UPPER, TR_NO, DG_NONUNIT, n, nrhs, 1.0, a, cs, rs, b, rsb, csb);
+    } else {
+        orc_dtrsm(SD_LEFT, UL_LOWER, TR_NO, DG_NONUNIT, n, nrhs, 1.0, a, cs, rs, b, rsb, csb);
+        orc_dtrsm(SD_LEFT, UL_UPPER, TR_NO, DG_NONUNIT, n, nrhs, 1.0, a, rs, cs, b, rsb, csb);
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* LDL^T without pivoting, DDLA/Factorizations/LDLT.cs                      */
+/* ------------------------------------------------------------------------ */
+
+/* LDLTLowerUnblock LT.cs:141-158 / LDLTUpperUnblock :204-221: only the first
+ * n-1 diagonals are tested against zero. */
+static int ldlt_unblock(int uplo, mat A, i64 row0) {
+    i64 n = A.r;
+    for (i64 i = 0; i + 1 < n; i++) {
+        double a11 = *AT(A, i, i);
+        if (a11 == 0) return (int)(row0 + i + 1);
+        mat A22 = sub(A, i + 1, n - i - 1, i + 1, n - i - 1);
+        if (uplo == UL_LOWER) {
+            if (invscal(a11, AT(A, i + 1, i), n - i - 1, A.rs, 1)) return (int)(row0 + i + 1);
+            syr(UL_LOWER, -a11, AT(A, i + 1, i), A.rs, A22);
+        } else {
+            if (invscal(a11, AT(A, i, i + 1), n - i - 1, A.cs, 0)) return (int)(row0 + i + 1);
+            syr(UL_UPPER, -a11, AT(A, i, i + 1), A.cs, A22);
+        }
+    }
+    return 0;
+}
+
+/* LDLTLowerBlock LDLT.cs:160-202 / LDLTUpperBlock :223-265 (blocked iff n > 128). */
+int orc_dldlt(int uplo, i64 n, double *a, i64 rs, i64 cs) {
+    mat A = mk(a, n, n, rs, cs);
+    if (n <= NB) return ldlt_unblock(uplo, A, 0);
+    double *work = (double *)malloc(sizeof(double) * (size_t)(n - NB) * NB);
+    int info = 0;
+    for (i64 j0 = 0; j0 < n && !info; j0 += NB) {
+        i64 b = n - j0 < NB ? n - j0 : NB, r = n - j0 - b;
+        mat A11 = sub(A, j0, b, j0, b);
+        info = ldlt_unblock(uplo, A11, j0);
+        if (info || r == 0) break;
+        if (uplo == UL_LOWER) {
+            mat A21 = sub(A, j0 + b, r, j0, b);
+            trsm_left(UL_LOWER, 1, A11, tr(A21));         /* A21 * L11^-T, unit */
+            mat Y = mk(work, r, b, b, 1);
+            for (i64 i = 0; i < r; i++) for (i64 j = 0; j < b; j++) *AT(Y, i, j) = *AT(A21, i, j);
+            for (i64 j = 0; j < b && !info; j++)
+                if (invscal(*AT(A11, j, j), AT(A21, 0, j), r, A21.rs, 1)) info = (int)(j0 + j + 1);
+            if (!info) gemm_core(-1.0, Y, tr(A21), sub(A, j0 + b, r, j0 + b, r), UL_LOWER);
+        } else {
+            mat A12 = sub(A, j0, b, j0 + b, r);
+            trsm_left(UL_LOWER, 1, tr(A11), A12);           /* U11^T X = A12, unit */
+            mat Y = mk(work, b, r, r, 1);
+            for (i64 i = 0; i < b; i++) for (i64 j = 0; j < r; j++) *AT(Y, i, j) = *AT(A12, i, j);
+            for (i64 i = 0; i < b && !info; i++)
+                if (invscal(*AT(A11, i, i), AT(A12, i, 0), r, A12.cs, 1)) info = (int)(j0 + i + 1);
+            if (!info) gemm_core(-1.0, tr(A12), Y, sub(A, j0 + b, r, j0 + b, r), UL_UPPER);
+        }
+    }
+    free(work);
+    return info;
+}
+
+/* LDLTSolveUncheck, LDLT.cs:267-295. */
+int orc_dldlts(int uplo, i64 n, i64 nrhs, const double *a, i64 rs, i64 cs, double *b, i64 rsb, i64 csb) {
+    if (n == 0 || nrhs == 0) return 0;
+    i64 lrs = uplo == UL_LOWER ? rs : cs, lcs = uplo == UL_LOWER ? cs : rs;   /* L view */
+    orc_dtrsm(SD_LEFT, UL_LOWER, TR_NO, DG_UNIT, n, nrhs, 1.0, a, lrs, lcs, b, rsb, csb);
+    for (i64 i = 0; i < n; i++)
+        if (invscal(a[i * rs + i * cs], b + i * rsb, nrhs, csb, 1)) return (int)(i + 1);
+    orc_dtrsm(SD_LEFT, UL_UPPER, TR_NO, DG_UNIT, n, nrhs, 1.0, a, lcs, lrs, b, rsb, csb);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Einsum: MArray.Contract index analysis + block-scatter GEMM               */
+/* ------------------------------------------------------------------------ */
+
+#define ORC_MAXMODE 16
+typedef struct { i64 len, sa, sb, sc; } orc_mode;   /* TripleIndice */
+typedef struct {
+    int nbatch, nm, nn, nk, swapped;
+    orc_mode batch[3 * ORC_MAXMODE];
+    orc_mode m[ORC_MAXMODE];   /* len, sa (operand-A stride), sc */
+    orc_mode n[ORC_MAXMODE];   /* len, sb (operand-B stride), sc */
+    orc_mode k[ORC_MAXMODE];   /* len, sa, sb */
+} orc_contract_desc;
+
+typedef struct { char sym; i64 len, s1, s2, s3; int used; } ent;
+
+/* IndiceUtils.Diagonal, DDLA/Utilities/IndiceUtils.cs:18-48: a repeated
+ * symbol becomes one mode whose stride is the sum of the strides. */
+static int diagonal(const char *sym, int rank, const i64 *len, const i64 *str, ent *out, int *cnt) {
+    *cnt = 0;
+    if ((int)strlen(sym) != rank) return -1;
+    for (int i = 0; i < rank; i++) {
+        int f = -1;
+        for (int j = 0; j < *cnt; j++) if (out[j].sym == sym[i]) f = j;
+        if (f >= 0) {
+            if (out[f].len != len[i]) return -1;
+            out[f].s1 += str[i];
+        } else {
+            ent e = {sym[i], len[i], str[i], 0, 0, 0};
+            out[(*cnt)++] = e;
+        }
+    }
+    return 0;
+}
+
+/* IndiceUtils.Fold for two-stride modes, IndiceUtils.cs:186-244: an outer mode
+ * whose strides equal (len*stride) of an inner mode absorbs it. */
+static void fold2(orc_mode *v, int *cnt, int first, int second) {
+    /* first/second: which stride fields are the pair (0 = sa, 1 = sb, 2 = sc) */
+    int changed = 1;
+    while (changed) {
+        changed = 0;
+        for (int o = 0; o < *cnt && !changed; o++)
+            for (int in = 0; in < *cnt && !changed; in++) {
+                if (o == in) continue;
+                i64 so[3] = {v[o].sa, v[o].sb, v[o].sc}, si[3] = {v[in].sa, v[in].sb, v[in].sc};
+                if (so[first] == v[in].len * si[first] && so[second] == v[in].len * si[second]) {
+                    v[o].len *= v[in].len;
+                    v[o].sa = v[in].sa; v[o].sb = v[in].sb; v[o].sc = v[in].sc;
+                    for (int t = in; t + 1 < *cnt; t++) v[t] = v[t + 1];
+                    (*cnt)--;
+                    changed = 1;
+                }
+            }
+    }
+}
+
+static void sort_desc(orc_mode *v, int cnt, int field) {
+    for (int i = 1; i < cnt; i++) {     /* stable insertion sort */
+        orc_mode x = v[i];
+        i64 kx = field == 0 ? x.sa : field == 1 ? x.sb : x.sc;
+        int j = i - 1;
+        while (j >= 0) {
+            i64 kj = field == 0 ? v[j].sa : field == 1 ? v[j].sb : v[j].sc;
+            if (kj >= kx) break;
+            v[j + 1] = v[j]; j--;
+        }
+        v[j + 1] = x;
+    }
+}
+
+/* MArray.Contract(result, expr, alpha, left, right) index analysis,
+ * DDLA/Einsum/MArray.Contract.cs:48-125 with IndiceUtils.Divide
+ * (IndiceUtils.cs:73-125).  Modes of length 1 are dropped as in :175-180. */
+int orc_contract_plan(const char *expr, int ra, const i64 *la, const i64 *sa,
+                      int rb, const i64 *lb, const i64 *sb, int rc, const i64 *lc, const i64 *sc,
+                      orc_contract_desc *d) {
+    char sA[ORC_MAXMODE + 1], sB[ORC_MAXMODE + 1], sC[ORC_MAXMODE + 1];
+    int ns = 0, which = 0;
+    char *dst[3] = {sA, sB, sC};
+    for (const char *p = expr; *p; p++) {
+        if (*p == ' ') continue;
+        if (*p == ',') { if (which != 0) return -1; dst[which][ns] = 0; which = 1; ns = 0; continue; }
+        if (*p == '-' && p[1] == '>') { if (which != 1) return -1; dst[which][ns] = 0; which = 2; ns = 0; p++; continue; }
+        if (ns >= ORC_MAXMODE) return -1;
+        dst[which][ns++] = *p;
+    }
+    if (which != 2) return -1;
+    dst[2][ns] = 0;
+    ent A[ORC_MAXMODE], B[ORC_MAXMODE], C[ORC_MAXMODE];
+    int na, nb, nc;
+    if (diagonal(sA, ra, la, sa, A, &na) || diagonal(sB, rb, lb, sb, B, &nb) || diagonal(sC, rc, lc, sc, C, &nc)) return -2;
+    memset(d, 0, sizeof(*d));
+    orc_mode abc[ORC_MAXMODE], cc[ORC_MAXMODE], ao[ORC_MAXMODE], bo[ORC_MAXMODE];
+    int nabc = 0, ncc = 0, nao = 0, nbo = 0;
+    for (int i = 0; i < na; i++) A[i].used = A[i].len <= 1;
+    for (int i = 0; i < nb; i++) B[i].used = B[i].len <= 1;
+    for (int i = 0; i < nc; i++) C[i].used = C[i].len <= 1;
+    for (int ic = 0; ic < nc; ic++) {
+        if (C[ic].used) continue;
+        int fa = -1, fb = -1;
+        for (int i = 0; i < na; i++) if (!A[i].used && A[i].sym == C[ic].sym) fa = i;
+        for (int i = 0; i < nb; i++) if (!B[i].used && B[i].sym == C[ic].sym) fb = i;
+        if (fa >= 0 && A[fa].len != C[ic].len) return -2;
+        if (fb >= 0 && B[fb].len != C[ic].len) return -2;
+        orc_mode md = {C[ic].len, fa >= 0 ? A[fa].s1 : 0, fb >= 0 ? B[fb].s1 : 0, C[ic].s1};
+        if (fa >= 0 && fb >= 0) abc[nabc++] = md;
+        else if (fa >= 0) d->m[d->nm++] = md;
+        else if (fb >= 0) d->n[d->nn++] = md;
+        else cc[ncc++] = md;
+        if (fa >= 0) A[fa].used = 1;
+        if (fb >= 0) B[fb].used = 1;
+        C[ic].used = 1;
+    }
+    for (int i = 0; i < na; i++) {
+        if (A[i].used) continue;
+        int fb = -1;
+        for (int j = 0; j < nb; j++) if (!B[j].used && B[j].sym == A[i].sym) fb = j;
+        if (fb >= 0) {
+            if (B[fb].len != A[i].len) return -2;
+            orc_mode md = {A[i].len, A[i].s1, B[fb].s1, 0};
+            d->k[d->nk++] = md; B[fb].used = 1;
+        } else { orc_mode md = {A[i].len, A[i].s1, 0, 0}; ao[nao++] = md; }
+        A[i].used = 1;
+    }
+    for (int j = 0; j < nb; j++) if (!B[j].used) { orc_mode md = {B[j].len, 0, B[j].s1, 0}; bo[nbo++] = md; }
+    /* batch order: ABC by descending C stride, then C-only, A-only, B-only (Contract.cs:68-89) */
+    sort_desc(abc, nabc, 2); sort_desc(cc, ncc, 2); sort_desc(ao, nao, 0); sort_desc(bo, nbo, 1);
+    for (int i = 0; i < nabc; i++) d->batch[d->nbatch++] = abc[i];
+    for (int i = 0; i < ncc; i++) d->batch[d->nbatch++] = cc[i];
+    for (int i = 0; i < nao; i++) d->batch[d->nbatch++] = ao[i];
+    for (int i = 0; i < nbo; i++) d->batch[d->nbatch++] = bo[i];
+    /* Fold + sort (Contract.cs:91-99): M by (sa, sc) sorted on C stride, N by
+     * (sb, sc) on C stride, K by (sa, sb) on A stride. */
+    fold2(d->m, &d->nm, 0, 2); sort_desc(d->m, d->nm, 2);
+    fold2(d->n, &d->nn, 1, 2); sort_desc(d->n, d->nn, 2);
+    fold2(d->k, &d->nk, 0, 1); sort_desc(d->k, d->nk, 0);
+    if (d->nm == 0) { orc_mode u = {1, 1, 1, 1}; d->m[d->nm++] = u; }
+    if (d->nn == 0) { orc_mode u = {1, 1, 1, 1}; d->n[d->nn++] = u; }
+    if (d->nk == 0) { orc_mode u = {1, 1, 1, 1}; d->k[d->nk++] = u; }
+    /* Operand swap when N's innermost C stride is 1 (Contract.cs:101-121). */
+    if (d->n[d->nn - 1].sc == 1) {
+        d->swapped = 1;
+        orc_mode tmp[ORC_MAXMODE];
+        int t = d->nm;
+        memcpy(tmp, d->m, sizeof(tmp));
+        memcpy(d->m, d->n, sizeof(tmp)); d->nm = d->nn;
+        memcpy(d->n, tmp, sizeof(tmp)); d->nn = t;
+        for (int i = 0; i < d->nm; i++) { i64 s = d->m[i].sb; d->m[i].sb = 0; d->m[i].sa = s; }
+        for (int i = 0; i < d->nn; i++) { i64 s = d->n[i].sa; d->n[i].sa = 0; d->n[i].sb = s; }
+        for (int i = 0; i < d->nk; i++) { i64 s = d->k[i].sa; d->k[i].sa = d->k[i].sb; d->k[i].sb = s; }
+        for (int i = 0; i < d->nbatch; i++) { i64 s = d->batch[i].sa; d->batch[i].sa = d->batch[i].sb; d->batch[i].sb = s; }
+    }
+    return 0;
+}
+
+static i64 total_len(const orc_mode *v, int cnt) { i64 t = 1; for (int i = 0; i < cnt; i++) t *= v[i].len; return t; }
+
+/* Offsets of every flattened index of a mode list (BlockScatterMatrix scatter
+ * vectors, DDLA/Einsum/BlockScatterMatrix.cs:205-324); the last mode varies
+ * fastest. */
+static void scatter(const orc_mode *v, int cnt, int field, i64 *out) {
+    i64 tot = total_len(v, cnt);
+    for (i64 f = 0; f < tot; f++) {
+        i64 rem = f, off = 0;
+        for (int i = cnt - 1; i >= 0; i--) {
+            i64 idx = rem % v[i].len; rem /= v[i].len;
+            i64 s = field == 0 ? v[i].sa : field == 1 ? v[i].sb : v[i].sc;
+            off += idx * s;
+        }
+        out[f] = off;
+    }
+}
+
+/* BlockScatterContract_Silent, DDLA/Einsum/MArray.Contract.cs:313-405: for each
+ * batch index, C[m,n] += alpha * sum_k A[m,k] B[k,n] with the MC/KC/NC
+ * blocking, K padded to KR with zeros, the 6x8 micro-kernel and a fused
+ * C += alpha*tile (BSMBlock.UnpackAxpy, DDLA/Einsum/BSMBlock.cs:195-305).
+ * Operands are (A, B) after the plan's optional swap. */
+void orc_contract_exec(const orc_contract_desc *d, double alpha, const double *a, const double *b, double *c) {
+    if (alpha == 0.0) return;
+    if (d->swapped) { const double *t = a; a = b; b = t; }
+    i64 m = total_len(d->m, d->nm), n = total_len(d->n, d->nn), k = total_len(d->k, d->nk);
+    i64 *rA = malloc(sizeof(i64) * m), *rC = malloc(sizeof(i64) * m);
+    i64 *cB = malloc(sizeof(i64) * n), *cC = malloc(sizeof(i64) * n);
+    i64 *kA = malloc(sizeof(i64) * k), *kB = malloc(sizeof(i64) * k);
+    scatter(d->m, d->nm, 0, rA); scatter(d->m, d->nm, 2, rC);
+    scatter(d->n, d->nn, 1, cB); scatter(d->n, d->nn, 2, cC);
+    scatter(d->k, d->nk, 0, kA); scatter(d->k, d->nk, 1, kB);
+    i64 nbt = total_len(d->batch, d->nbatch);
+    i64 kmax = align_up(k < KC ? k : KC, KR);
+    double *bufA = malloc(sizeof(double) * align_up(m < MC ? m : MC, MR) * kmax);
+    double *bufB = malloc(sizeof(double) * align_up(n < NC ? n : NC, NR) * kmax);
+    for (i64 bt = 0; bt < nbt; bt++) {
+        i64 rem = bt, oa = 0, ob = 0, oc = 0;
+        for (int i = d->nbatch - 1; i >= 0; i--) {
+            i64 idx = rem % d->batch[i].len; rem /= d->batch[i].len;
+            oa += idx * d->batch[i].sa; ob += idx * d->batch[i].sb; oc += idx * d->batch[i].sc;
+        }
+        for (i64 i0 = 0; i0 < m; i0 += MC) {
+            i64 ic = m - i0 < MC ? m - i0 : MC;
+            for (i64 q = 0; q < k; q += KC) {
+                i64 qc = k - q < KC ? k - q : KC, qa = align_up(qc, KR);
+                for (i64 p = 0; p < align_up(ic, MR) / MR; p++)
+                    for (i64 kk = 0; kk < qa; kk++)
+                        for (int r = 0; r < MR; r++) {
+                            i64 row = i0 + p * MR + r;
+                            bufA[(p * qa + kk) * MR + r] = (row < i0 + ic && kk < qc) ? a[oa + rA[row] + kA[q + kk]] : 0.0;
+                        }
+                for (i64 j0 = 0; j0 < n; j0 += NC) {
+                    i64 jc = n - j0 < NC ? n - j0 : NC;
+                    for (i64 p = 0; p < align_up(jc, NR) / NR; p++)
+                        for (i64 kk = 0; kk < qa; kk++)
+                            for (int s = 0; s < NR; s++) {
+                                i64 col = j0 + p * NR + s;
+                                bufB[(p * qa + kk) * NR + s] = (col < j0 + jc && kk < qc) ? b[ob + kB[q + kk] + cB[col]] : 0.0;
+                            }
+                    i64 ip = align_up(ic, MR) / MR;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(g_threads) if (g_threads > 1 && ip >= 8)
+#endif
+                    for (i64 p = 0; p < ip; p++) {
+                        double t[MR * NR];
+                        for (i64 s0 = 0; s0 < align_up(jc, NR); s0 += NR) {
+                            micro(qa, bufA + p * qa * MR, bufB + (s0 / NR) * qa * NR, t);
+                            for (int r = 0; r < MR; r++) {
+                                i64 row = i0 + p * MR + r;
+                                if (row >= i0 + ic) break;
+                                for (int s = 0; s < NR; s++) {
+                                    i64 col = j0 + s0 + s;
+                                    if (col >= j0 + jc) break;
+                                    double *cp = c + oc + rC[row] + cC[col];
+                                    *cp = fma(t[r * NR + s], alpha, *cp);
+                                }
+                            }
+                        }
+                    }
+                }
+            }
+        }
+    }
+    free(rA); free(rC); free(cB); free(cC); free(kA); free(kB); free(bufA); free(bufB);
+}
+
+int orc_contract_desc_size(void) { return (int)sizeof(orc_contract_desc); }

@@ -1,0 +1,189 @@
+"""ctypes front end of the oracle (TEST INFRASTRUCTURE ONLY).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
+this module; the product library never does.  Each function takes numpy
+float64 arrays (any strides: element strides are passed through exactly like
+DDLA's MatrixView RowStride/ColStride) and mirrors the C entry points of
+ddla_oracle.c, which restate DDLA's algorithms (see the citations there).
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+
+TRANS_NO, TRANS_T = 0, 8
+LOWER, UPPER, DENSE = 0xC0, 0x60, 0xE0
+NONUNIT, UNIT = 0, 0x100
+LEFT, RIGHT = 0, 1
+
+_i64 = C.c_int64
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+class ContractDesc(C.Structure):
+    class Mode(C.Structure):
+        _fields_ = [("len", _i64), ("sa", _i64), ("sb", _i64), ("sc", _i64)]
+
+    _fields_ = [("nbatch", C.c_int), ("nm", C.c_int), ("nn", C.c_int), ("nk", C.c_int),
+                ("swapped", C.c_int),
+                ("batch", Mode * 48), ("m", Mode * 16), ("n", Mode * 16), ("k", Mode * 16)]
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        _lib = C.CDLL(path)
+        L = _lib
+        L.orc_damax.restype = _i64
+        L.orc_damax.argtypes = [_i64, _dp, _i64]
+        for name in ("orc_dgetrf",):
+            getattr(L, name).argtypes = [_i64, _dp, _i64, _i64, _ip]
+        L.orc_dgetrf_nopiv.argtypes = [_i64, _dp, _i64, _i64]
+        L.orc_dpotrf.argtypes = [C.c_int, _i64, _dp, _i64, _i64]
+        L.orc_dldlt.argtypes = [C.c_int, _i64, _dp, _i64, _i64]
+        L.orc_dgetrs.argtypes = [C.c_int, _i64, _i64, _dp, _i64, _i64, _ip, _dp, _i64, _i64]
+        L.orc_dgetrs.restype = None
+        L.orc_dgetrs_nopiv.argtypes = [C.c_int, _i64, _i64, _dp, _i64, _i64, _dp, _i64, _i64]
+        L.orc_dgetrs_nopiv.restype = None
+        L.orc_dpotrs.argtypes = [C.c_int, _i64, _i64, _dp, _i64, _i64, _dp, _i64, _i64]
+        L.orc_dpotrs.restype = None
+        L.orc_dldlts.argtypes = [C.c_int, _i64, _i64, _dp, _i64, _i64, _dp, _i64, _i64]
+        L.orc_dgemm.argtypes = [C.c_int, C.c_int, _i64, _i64, _i64, C.c_double, _dp, _i64, _i64,
+                                _dp, _i64, _i64, C.c_double, _dp, _i64, _i64]
+        L.orc_dgemm.restype = None
+        L.orc_dgemmt.argtypes = [C.c_int, C.c_int, C.c_int, _i64, _i64, C.c_double, _dp, _i64, _i64,
+                                 _dp, _i64, _i64, C.c_double, _dp, _i64, _i64]
+        L.orc_dgemmt.restype = None
+        L.orc_dsyrk.argtypes = [C.c_int, C.c_int, _i64, _i64, C.c_double, _dp, _i64, _i64,
+                                C.c_double, _dp, _i64, _i64]
+        L.orc_dsyrk.restype = None
+        L.orc_dtrsm.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, _i64, _i64, C.c_double,
+                                _dp, _i64, _i64, _dp, _i64, _i64]
+        L.orc_dtrsm.restype = None
+        L.orc_set_threads.argtypes = [C.c_int]
+        L.orc_contract_plan.argtypes = [C.c_char_p, C.c_int, C.POINTER(_i64), C.POINTER(_i64),
+                                        C.c_int, C.POINTER(_i64), C.POINTER(_i64),
+                                        C.c_int, C.POINTER(_i64), C.POINTER(_i64),
+                                        C.POINTER(ContractDesc)]
+        L.orc_contract_exec.argtypes = [C.POINTER(ContractDesc), C.c_double, _dp, _dp, _dp]
+        L.orc_contract_exec.restype = None
+        assert L.orc_contract_desc_size() == C.sizeof(ContractDesc)
+    return _lib
+
+
+def set_threads(n):
+    lib().orc_set_threads(int(n))
+
+
+def has_openmp():
+    return bool(lib().orc_has_openmp())
+
+
+def _ptr(x):
+    assert x.dtype == np.float64
+    return x.ctypes.data_as(_dp)
+
+
+def _st(x):
+    """Element strides (row, col) of a 2-D float64 array view."""
+    return x.strides[0] // 8, x.strides[1] // 8
+
+
+def damax(x):
+    return int(lib().orc_damax(x.shape[0], _ptr(x), x.strides[0] // 8))
+
+
+def dgemm(alpha, A, B, beta, Cm, ta=TRANS_NO, tb=TRANS_NO):
+    m, n = Cm.shape
+    k = A.shape[0] if ta == TRANS_T else A.shape[1]
+    lib().orc_dgemm(ta, tb, m, n, k, alpha, _ptr(A), *_st(A), _ptr(B), *_st(B), beta, _ptr(Cm), *_st(Cm))
+
+
+def dgemmt(uplo, alpha, A, B, beta, Cm, ta=TRANS_NO, tb=TRANS_NO):
+    m = Cm.shape[0]
+    k = A.shape[0] if ta == TRANS_T else A.shape[1]
+    lib().orc_dgemmt(uplo, ta, tb, m, k, alpha, _ptr(A), *_st(A), _ptr(B), *_st(B), beta, _ptr(Cm), *_st(Cm))
+
+
+def dsyrk(uplo, alpha, A, beta, Cm, ta=TRANS_NO):
+    m = Cm.shape[0]
+    k = A.shape[0] if ta == TRANS_T else A.shape[1]
+    lib().orc_dsyrk(uplo, ta, m, k, alpha, _ptr(A), *_st(A), beta, _ptr(Cm), *_st(Cm))
+
+
+def dtrsm(side, uplo, ta, diag, alpha, A, B):
+    m, n = B.shape
+    lib().orc_dtrsm(side, uplo, ta, diag, m, n, alpha, _ptr(A), *_st(A), _ptr(B), *_st(B))
+
+
+def dgetrf(A):
+    """In-place PLU of A; returns (info, relative pivots int32[n])."""
+    n = A.shape[0]
+    piv = np.zeros(max(n, 1), dtype=np.int32)
+    info = lib().orc_dgetrf(n, _ptr(A), *_st(A), piv.ctypes.data_as(_ip))
+    return info, piv[:n]
+
+
+def dgetrs(LU, piv, B, trans=0):
+    piv = np.ascontiguousarray(piv, dtype=np.int32)
+    lib().orc_dgetrs(trans, LU.shape[0], B.shape[1], _ptr(LU), *_st(LU), piv.ctypes.data_as(_ip), _ptr(B), *_st(B))
+
+
+def dgetrf_nopiv(A):
+    return lib().orc_dgetrf_nopiv(A.shape[0], _ptr(A), *_st(A))
+
+
+def dgetrs_nopiv(LU, B, trans=0):
+    lib().orc_dgetrs_nopiv(trans, LU.shape[0], B.shape[1], _ptr(LU), *_st(LU), _ptr(B), *_st(B))
+
+
+def dpotrf(uplo, A):
+    return lib().orc_dpotrf(uplo, A.shape[0], _ptr(A), *_st(A))
+
+
+def dpotrs(uplo, Lf, B):
+    lib().orc_dpotrs(uplo, Lf.shape[0], B.shape[1], _ptr(Lf), *_st(Lf), _ptr(B), *_st(B))
+
+
+def dldlt(uplo, A):
+    return lib().orc_dldlt(uplo, A.shape[0], _ptr(A), *_st(A))
+
+
+def dldlts(uplo, F, B):
+    return lib().orc_dldlts(uplo, F.shape[0], B.shape[1], _ptr(F), *_st(F), _ptr(B), *_st(B))
+
+
+def _arr(v):
+    return (_i64 * max(len(v), 1))(*v)
+
+
+def contract_plan(expr, A, B, Cm):
+    d = ContractDesc()
+    sa = [s // 8 for s in A.strides]
+    sb = [s // 8 for s in B.strides]
+    sc = [s // 8 for s in Cm.strides]
+    rc = lib().orc_contract_plan(expr.encode(), A.ndim, _arr(A.shape), _arr(sa), B.ndim, _arr(B.shape), _arr(sb),
+                                 Cm.ndim, _arr(Cm.shape), _arr(sc), C.byref(d))
+    if rc != 0:
+        raise ValueError(f"contract plan failed ({rc}) for {expr!r}")
+    return d
+
+
+def contract(expr, alpha, A, B, Cm):
+    """Cm += alpha * contraction(A, B) in place (MArray.Contract(result, ...))."""
+    d = contract_plan(expr, A, B, Cm)
+    lib().orc_contract_exec(C.byref(d), alpha, _ptr(A), _ptr(B), _ptr(Cm))
+    return d
+
+
+def plan_dict(d):
+    def modes(arr, cnt):
+        return [(arr[i].len, arr[i].sa, arr[i].sb, arr[i].sc) for i in range(cnt)]
+    return {"batch": modes(d.batch, d.nbatch), "m": modes(d.m, d.nm), "n": modes(d.n, d.nn),
+            "k": modes(d.k, d.nk), "swapped": d.swapped}

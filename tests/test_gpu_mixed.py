@@ -1,0 +1,43 @@
+"""Mixed-precision solves: FP32 factorization + FP64 refinement reach the
+FP64 backward-error target and agree with the FP64 oracle solution."""
+import numpy as np
+import pytest
+
+from helpers import berr, rng, spd
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("n,nrhs", [(100, 1), (1024, 1), (2048, 4), (3000, 16)])
+def test_mixed_lu_reaches_fp64(ddla, orc, n, nrhs):
+    r = rng(n)
+    A = r.standard_normal((n, n))
+    B = r.standard_normal((n, nrhs))
+    F = A.copy()
+    info, piv = orc.dgetrf(F)
+    Xo = B.copy()
+    orc.dgetrs(F, piv, Xo)
+    X, rep = ddla.solve_mixed(A, B, precision=ddla.PREC_FP32, x_ref=Xo)
+    assert rep["converged"] == 1
+    assert rep["backward_error"] <= 1e-14
+    assert berr(A, X, B) <= 1e-14
+    assert rep["forward_error"] <= 1e-10
+
+
+@pytest.mark.parametrize("n,nrhs", [(500, 16), (2048, 16)])
+def test_mixed_cholesky(ddla, orc, n, nrhs):
+    r = rng(n + 1)
+    A = spd(r, n)
+    B = r.standard_normal((n, nrhs))
+    X, rep = ddla.solve_mixed(A, B, spd=True, precision=ddla.PREC_FP32)
+    assert rep["converged"] == 1 and rep["backward_error"] <= 1e-14
+    assert berr(A, X, B) <= 1e-14
+
+
+def test_mixed_no_refinement_reports_not_converged(ddla):
+    r = rng(1)
+    A = r.standard_normal((300, 300))
+    B = r.standard_normal((300, 1))
+    with pytest.raises(ddla.DDLAError) as e:
+        ddla.solve_mixed(A, B, precision=ddla.PREC_FP32, max_iter=-1)
+    assert e.value.code == -1004

@@ -1,0 +1,256 @@
+"""CPU pinning of the oracle (no GPU).
+
+DDLA ships no golden vectors and cannot run here (C#/.NET, x86-only kernel,
+closed Windows BLIS), so the oracle is pinned by (a) DDLA's own property tests
+at their sizes and tolerances (Tests/TestFlame/*.cs,
+Tests/TestEinsum/TestSimpleBSMTC.cs, Tests/TestManagedBlas/Level3m/*.cs) and
+(b) an independent LAPACK/BLAS (scipy/numpy) on the same inputs, including the
+exact partial-pivoting sequence.
+"""
+import numpy as np
+import pytest
+import scipy.linalg as sl
+
+from helpers import apply_piv, berr, make_lmat, make_umat, norms, rel_max, rng, spd, uniform
+
+TINY, SMALL, MEDIUM, LARGE = 4, 64, 256, 1024
+
+
+@pytest.mark.parametrize("m,n,k", [(1, 1, 1), (7, 9, 5), (6, 8, 144), (130, 200, 300), (513, 600, 145)])
+def test_gemm_matches_numpy(orc, m, n, k):
+    # DDLA Tests/TestManagedBlas/Level3m/TestGeMM.cs:40-55: alpha=2, beta=1.2, abs tol 1e-10
+    r = rng(10 + m)
+    A, B, C0 = uniform(r, (m, k)), uniform(r, (k, n)), uniform(r, (m, n))
+    Cm = C0.copy()
+    orc.dgemm(2.0, A, B, 1.2, Cm)
+    assert np.max(np.abs(Cm - (1.2 * C0 + 2.0 * A @ B))) < 1e-10
+
+
+@pytest.mark.parametrize("layout", ["row", "col", "strided"])
+def test_gemm_layouts(orc, layout):
+    r = rng(3)
+    m, n, k = 70, 90, 50
+    def mk(shape):
+        x = uniform(r, shape)
+        if layout == "col":
+            return np.asfortranarray(x)
+        if layout == "strided":   # colStride = 4 (Tests/CreateUtils.cs)
+            big = np.zeros((shape[0], shape[1] * 4))
+            big[:, ::4] = x
+            return big[:, ::4]
+        return x
+    A, B, Cm = mk((k, m)), mk((n, k)), mk((m, n))
+    ref = 0.5 * Cm + 2.0 * A.T @ B.T
+    orc.dgemm(2.0, A, B, 0.5, Cm, ta=orc.TRANS_T, tb=orc.TRANS_T)
+    assert np.max(np.abs(Cm - ref)) < 1e-12
+
+
+def test_gemm_beta_zero_ignores_nan(orc):
+    A, B = np.ones((3, 2)), np.ones((2, 4))
+    Cm = np.full((3, 4), np.nan)
+    orc.dgemm(1.0, A, B, 0.0, Cm)
+    assert np.all(Cm == 2.0)
+
+
+@pytest.mark.parametrize("uplo", ["L", "U"])
+def test_gemmt_syrk(orc, uplo):
+    # TestGeMMT.cs:94-112 / TestSyRk.cs:74-92
+    r = rng(4)
+    u = orc.LOWER if uplo == "L" else orc.UPPER
+    tri = np.tril if uplo == "L" else np.triu
+    anti = (lambda x: np.triu(x, 1)) if uplo == "L" else (lambda x: np.tril(x, -1))
+    A, B, C0 = uniform(r, (300, 70)), uniform(r, (70, 300)), uniform(r, (300, 300))
+    Cm = C0.copy()
+    orc.dgemmt(u, 2.0, A, B, 1.2, Cm)
+    assert np.max(np.abs(tri(Cm) - tri(1.2 * C0 + 2 * A @ B))) < 1e-10
+    assert np.array_equal(anti(Cm), anti(C0))
+    Cm = C0.copy()
+    orc.dsyrk(u, -1.0, A, 1.0, Cm)
+    assert np.max(np.abs(tri(Cm) - tri(C0 - A @ A.T))) < 1e-10
+
+
+@pytest.mark.parametrize("side", [0, 1])
+@pytest.mark.parametrize("uplo", [0xC0, 0x60])
+@pytest.mark.parametrize("trans", [0, 8])
+@pytest.mark.parametrize("diag", [0, 0x100])
+def test_trsm(orc, side, uplo, trans, diag):
+    # TestTrSM.cs:105-127: diagonal shifted by 2, alpha 1.2, tol 1e-8
+    r = rng(5)
+    m, n = 300, 170
+    na = m if side == 0 else n
+    A = uniform(r, (na, na)) / na + 2 * np.eye(na)
+    T = np.tril(A) if uplo == 0xC0 else np.triu(A)
+    if diag:
+        np.fill_diagonal(T, 1.0)
+    opT = T.T if trans else T
+    B = uniform(r, (m, n))
+    X = B.copy()
+    orc.dtrsm(side, uplo, trans, diag, 1.2, A, X)
+    res = opT @ X - 1.2 * B if side == 0 else X @ opT - 1.2 * B
+    assert np.max(np.abs(res)) < 1e-8
+
+
+def test_damax_first_max_and_nan(orc):
+    assert orc.damax(np.array([1.0, -3.0, 3.0, 2.0])) == 1
+    assert orc.damax(np.array([np.nan, 0.5, -0.5])) == 1
+    assert orc.damax(np.array([np.nan, np.nan])) == 0
+    assert orc.damax(np.zeros(0)) == 0
+
+
+@pytest.mark.parametrize("n", [TINY, SMALL, 127, 128, 129, MEDIUM])
+def test_plu_property_and_lapack_pivots(orc, n):
+    # TestPLU.cs:79-116: A = L*U from random unit-L/U, ||P*A - L*U|| < 1e-8, 20 repetitions
+    r = rng(100 + n)
+    for _ in range(5):
+        A = make_lmat(r.random((n, n))) @ make_umat(r.random((n, n)))
+        F = A.copy()
+        info, piv = orc.dgetrf(F)
+        assert info == 0
+        L, U = make_lmat(F), make_umat(F)
+        for v in norms(apply_piv(A, piv) - L @ U):
+            assert v < 1e-8
+    # independent LAPACK: identical partial-pivoting sequence on N(0,1) inputs
+    # (the L*U inputs above are exponentially ill-conditioned, so their late
+    # pivots are decided by rounding noise)
+    for _ in range(5):
+        A = r.standard_normal((n, n))
+        F = A.copy()
+        info, piv = orc.dgetrf(F)
+        lu, sp = sl.lu_factor(A)
+        assert np.array_equal(piv, sp - np.arange(n))
+        assert rel_max(F, lu) < 1e-10
+
+
+def test_plu_large_spd_and_solver(orc):
+    # TestPLU.cs:22-73 (RandomSPD(1024), tol 1e-6; solver with X = I)
+    r = rng(7)
+    n = LARGE
+    G = r.random((n, n))
+    A = G @ G.T + n * np.eye(n)
+    F = A.copy()
+    info, piv = orc.dgetrf(F)
+    assert info == 0
+    for v in norms(apply_piv(A, piv) - make_lmat(F) @ make_umat(F)):
+        assert v < 1e-6
+    A = r.random((n, n))
+    X = A.copy()
+    info, piv = orc.dgetrf(X)
+    B = A @ np.eye(n)
+    orc.dgetrs(X, piv, B)
+    for v in norms(B - np.eye(n)):
+        assert v < 1e-6
+
+
+@pytest.mark.parametrize("n", [TINY, SMALL, MEDIUM])
+def test_lu_nopiv_property(orc, n):
+    # TestLU.cs:31-63: tol 1e-6
+    r = rng(200 + n)
+    A = make_lmat(r.random((n, n))) @ make_umat(r.random((n, n)) + n * np.eye(n))
+    F = A.copy()
+    assert orc.dgetrf_nopiv(F) == 0
+    for v in norms(A - make_lmat(F) @ make_umat(F)):
+        assert v < 1e-6
+    b = r.random((n, 3))
+    x = b.copy()
+    orc.dgetrs_nopiv(F, x)
+    assert berr(A, x, b) < 1e-14
+    x = b.copy()
+    orc.dgetrs_nopiv(F, x, trans=1)
+    assert berr(A.T, x, b) < 1e-14
+
+
+@pytest.mark.parametrize("n", [TINY, SMALL, MEDIUM])
+@pytest.mark.parametrize("uplo", ["L", "U"])
+def test_cholesky_property(orc, n, uplo):
+    # TestChol.cs:26-96: A = L*L^T (random L), tol 1e-10
+    r = rng(300 + n)
+    L0 = r.random((n, n))
+    A = L0 @ L0.T if uplo == "L" else L0.T @ L0
+    A += n * np.eye(n) * 1e-3
+    F = A.copy()
+    u = orc.LOWER if uplo == "L" else orc.UPPER
+    assert orc.dpotrf(u, F) == 0
+    if uplo == "L":
+        Lf = np.tril(F)
+        res = A - Lf @ Lf.T
+    else:
+        Uf = np.triu(F)
+        res = A - Uf.T @ Uf
+    for v in norms(res):
+        assert v < 1e-10 * max(1.0, np.abs(A).max())
+    ref = np.linalg.cholesky(A)
+    got = np.tril(F) if uplo == "L" else np.triu(F).T
+    assert rel_max(got, ref) < 1e-12
+
+
+@pytest.mark.parametrize("uplo", ["L", "U"])
+def test_cholesky_solver(orc, uplo):
+    # TestChol.cs:101-162: U*U^T + sqrt(n) I, 256 RHS, tol 1e-8
+    r = rng(9)
+    n = 300
+    U = r.random((n, n))
+    A = U @ U.T + np.sqrt(n) * np.eye(n)
+    X = r.random((n, 64))
+    B = A @ X
+    F = A.copy()
+    u = orc.LOWER if uplo == "L" else orc.UPPER
+    assert orc.dpotrf(u, F) == 0
+    orc.dpotrs(u, F, B)
+    for v in norms(B - X):
+        assert v < 1e-8
+
+
+@pytest.mark.parametrize("n", [TINY, SMALL, MEDIUM])
+@pytest.mark.parametrize("uplo", ["L", "U"])
+def test_ldlt_property(orc, n, uplo):
+    r = rng(400 + n)
+    A = spd(r, n)
+    F = A.copy()
+    u = orc.LOWER if uplo == "L" else orc.UPPER
+    assert orc.dldlt(u, F) == 0
+    D = np.diag(np.diag(F))
+    L = make_lmat(F) if uplo == "L" else make_lmat(F.T)
+    for v in norms(A - L @ D @ L.T):
+        assert v < 1e-10
+    b = r.random((n, 4))
+    x = b.copy()
+    assert orc.dldlts(u, F, x) == 0
+    assert berr(A, x, b) < 1e-14
+
+
+def test_failures_report_pivot_index(orc):
+    A = np.eye(5)
+    A[2, 2] = -1.0
+    assert orc.dpotrf(orc.LOWER, A.copy()) == 3
+    S = np.eye(4)
+    S[:, 1] = 0.0          # singular: column 1 is zero below the diagonal too
+    info, _ = orc.dgetrf(S.copy())
+    assert info == 2
+    Z = np.eye(4)
+    Z[1, 1] = 0.0
+    assert orc.dldlt(orc.LOWER, Z.copy()) == 2
+
+
+@pytest.mark.parametrize("expr,sa,sb", [
+    ("mnk,nktc->mct", (5, 7, 9), (7, 9, 4, 3)),      # Tests/TestEinsum/TestSimpleBSMTC.cs:10-51
+    ("mk,kn->mn", (37, 29), (29, 23)),
+    ("bik,bkj->bij", (6, 20, 21), (6, 21, 22)),
+    ("abcd,cdef->abef", (4, 5, 6, 7), (6, 7, 3, 2)),
+    ("ij,jk->ki", (11, 13), (13, 17)),
+    ("aij,ajk->ik", (3, 8, 9), (3, 9, 10)),           # batch mode summed (A-B shared, not in C)
+])
+def test_contract_vs_einsum(orc, expr, sa, sb):
+    r = rng(11)
+    A, B = uniform(r, sa), uniform(r, sb)
+    ref = np.einsum(expr.replace(" ", ""), A, B)
+    Cm = np.zeros(ref.shape)
+    orc.contract(expr, 1.0, A, B, Cm)
+    assert np.max(np.abs(Cm - ref)) < 1e-10
+
+
+def test_contract_plan_folds_to_single_gemm(orc):
+    A, B = np.zeros((8, 8, 8, 8)), np.zeros((8, 8, 8, 8))
+    Cm = np.zeros((8, 8, 8, 8))
+    d = orc.plan_dict(orc.contract_plan("abcd,cdef->abef", A, B, Cm))
+    assert len(d["m"]) == 1 and len(d["n"]) == 1 and len(d["k"]) == 1 and d["batch"] == []
+    assert d["m"][0][0] == 64 and d["n"][0][0] == 64 and d["k"][0][0] == 64
