@@ -1,0 +1,313 @@
+"""Benchmark: mixed-precision LU solve with FP64 iterative refinement on one GB300.
+
+Workload (the configuration the headline metric is quoted on): A n x n with
+i.i.d. N(0,1) entries, n = 8192, one right-hand side b ~ N(0,1); LU with
+partial pivoting in FP32 storage with trailing updates in the selected
+precision, then FP64 refinement on the GPU until the relative backward error
+max ||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf) <= 1e-14.
+
+A step = one complete solve (FP64 -> FP32 conversion, factorization, initial
+solve, refinement loop) from the FP64 A and b resident in HBM.  The credited
+work is the algorithmic LU+solve count 2/3 n^3 + 2 n^2 flops (refinement flops
+are not credited).  A step only counts if it reaches the tolerance.
+
+  value   device throughput, inputs resident, CUDA events on the solve stream
+  e2e     the same through the host C ABI (ddla_dgesv_mixed) with pinned host
+          buffers: host->device copy of A and b, solve, device->host copy of x
+  roofline  the dominant kernel class, timed per launch with CUDA events
+  cpu_baseline  the oracle (C restatement of DDLA's managed LU + solve) on the
+          host cores, bounded sample
+
+--impl reference times that CPU restatement as the reference arm.
+--gpus N (torchrun, one rank per GPU) runs N independent replicas: the solve
+does not shard across devices.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_DEFAULT = 8192
+SEED = 0xDD1A0002
+TOL = 1e-14
+METRIC = "Solve GFLOP/s at FP64-level residual: mixed+refined vs plain FP64, 1 GB300"
+UNIT = "GFLOP/s"
+
+
+def lu_flops(n, nrhs=1):
+    return 2.0 / 3.0 * n ** 3 + 2.0 * n ** 2 * nrhs
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi sampler running while the timed region runs."""
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def cpu_sample(n, threads, reps=1):
+    """Oracle LU + solve (DDLA's managed algorithm restated in C) on n x n."""
+    import numpy as np
+    from oracle import oracle
+    oracle.set_threads(threads)
+    r = np.random.default_rng(SEED)
+    A = r.standard_normal((n, n))
+    b = r.standard_normal((n, 1))
+    best = None
+    for _ in range(reps):
+        F = A.copy()
+        x = b.copy()
+        t = time.perf_counter()
+        info, piv = oracle.dgetrf(F)
+        oracle.dgetrs(F, piv, x)
+        dt = time.perf_counter() - t
+        assert info == 0
+        best = dt if best is None else min(best, dt)
+    return lu_flops(n) / best / 1e9, best
+
+
+def reference_arm(args):
+    rank, world, _ = dist_env()
+    if world > 1 and rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    n = args.cpu_n
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, dt = cpu_sample(n, cores)
+        if i >= args.warmup:
+            vals.append(v)
+    value = statistics.median(vals)
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic N(0,1), seeded",
+           "config": {"workload": f"LU (partial pivoting) + solve, n={n} sample of n={args.n}, 1 RHS, FP64, CPU",
+                      "n": n},
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                            "sample": f"oracle dgetrf+dgetrs (C restatement of DDLA managed LU) n={n}, "
+                                      f"{cores} OpenMP threads, one solve per step"},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--precision", default="auto", choices=["auto", "fp32", "tf32x3", "bf16x3", "fp64"])
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-n", type=int, default=4096)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return reference_arm(args)
+
+    import numpy as np
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+
+    import ddla_gb300 as D
+    from ddla_gb300 import device as dv
+    from ddla_gb300 import build as bld
+    bld.build()
+    L = D.lib()
+
+    prec_map = {"fp32": D.PREC_FP32, "tf32x3": D.PREC_TF32X3, "bf16x3": D.PREC_BF16X3, "fp64": D.PREC_FP64}
+    prec_name = args.precision if args.precision != "auto" else os.environ.get("DDLA_BENCH_PREC", "fp32")
+    prec = prec_map[prec_name]
+    n = args.n
+    stream = torch.cuda.Stream()
+    h = dv.Handle(stream)
+    g = torch.Generator(device="cuda").manual_seed(SEED + rank)
+    A = torch.randn(n, n, dtype=torch.float64, device="cuda", generator=g)
+    b = torch.randn(n, 1, dtype=torch.float64, device="cuda", generator=g)
+    X = torch.zeros(n, 1, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+
+    def step():
+        rc, rep = h.gesv_mixed(A, b, X, precision=prec, tol=TOL)
+        if rc != 0 or not rep["converged"]:
+            raise RuntimeError(f"solve failed rc={rc} rep={rep} err={D._lib.last_error()}")
+        return rep
+
+    for _ in range(args.warmup):
+        step()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    clocks = ClockSampler(local)
+    L.ddla_timing_enable(1)
+    launches0 = D.kernel_launches()
+    barrier()
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    reps = [step() for _ in range(args.steps)]
+    e1.record(stream)
+    barrier()
+    clk = clocks.stop()
+    launches = D.kernel_launches() - launches0
+    ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = lu_flops(n) * world / (ms * 1e-3) / 1e9
+
+    # dominant kernel class from the per-launch CUDA-event records of the timed region
+    classes = {0: "trailing_update_gemm", 1: "lu_panel", 2: "trsm", 3: "laswp", 4: "refinement"}
+    per = {}
+    for cls in classes:
+        t_ms, cnt, fl, by = C.c_double(), C.c_int64(), C.c_double(), C.c_double()
+        L.ddla_timing_read(cls, C.byref(t_ms), C.byref(cnt), C.byref(fl), C.byref(by))
+        per[classes[cls]] = {"ms_per_step": t_ms.value / args.steps, "launches": cnt.value, "flops": fl.value,
+                             "bytes": by.value}
+    L.ddla_timing_enable(0)
+    f64_peak, f32_peak = dv.measure_peaks()
+    upd = per["trailing_update_gemm"]
+    dom = max(per, key=lambda k: per[k]["ms_per_step"])
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    if prec in (D.PREC_TF32X3, D.PREC_BF16X3):
+        bound, peak, peak_src = "tensor", peaks.get("bf16_tflops", 1900.0), "MEASURED_PEAKS.json bf16_tflops (burst)"
+    elif prec == D.PREC_FP64:
+        bound, peak, peak_src = "tensor", f64_peak, "live DMMA probe (ddla_measure_peaks)"
+    else:
+        bound, peak, peak_src = "fp32-cuda-core", f32_peak, "live FFMA probe (ddla_measure_peaks)"
+    upd_ms_launch = upd["ms_per_step"] * args.steps / max(upd["launches"], 1)
+    upd_flops_launch = upd["flops"] / max(upd["launches"], 1)
+    achieved = upd_flops_launch / (upd_ms_launch * 1e-3) / 1e12 if upd["launches"] else 0.0
+    roofline = {"bound": bound, "kernel": "trailing_update_gemm", "achieved": achieved, "peak": peak,
+                "unit": "TFLOP/s", "frac": achieved / peak if peak else None, "traffic": None,
+                "peak_source": peak_src, "dominant_class": dom,
+                "classes_ms_per_step": {k: round(v["ms_per_step"], 4) for k, v in per.items()},
+                "note": "achieved = algorithmic 2*m*n*k per trailing-update launch / its CUDA-event duration"}
+
+    # end-to-end through the host C ABI with pinned host buffers
+    e2e = None
+    if not args.no_e2e and rank == 0:
+        Ah = A.cpu().pin_memory()
+        bh = b.cpu().pin_memory()
+        xh = torch.zeros(n, 1, dtype=torch.float64).pin_memory()
+        opts = D._lib.Opts()
+        opts.precision, opts.tol = prec, TOL
+        rep = D._lib.SolveReport()
+
+        def e2e_step():
+            rc = L.ddla_dgesv_mixed(n, 1, C.c_void_p(Ah.data_ptr()), n, 1, C.c_void_p(bh.data_ptr()), 1, 1,
+                                    C.c_void_p(xh.data_ptr()), 1, 1, None, C.byref(opts), C.byref(rep))
+            if rc != 0:
+                raise RuntimeError(f"e2e solve failed {rc}: {D._lib.last_error()}")
+        for _ in range(2):
+            e2e_step()
+        k2 = max(3, min(args.steps, 5))
+        t = time.perf_counter()
+        for _ in range(k2):
+            e2e_step()
+        dt = (time.perf_counter() - t) / k2
+        e2e = {"value": lu_flops(n) / dt / 1e9, "unit": UNIT, "ms_per_step": dt * 1e3,
+               "h2d_bytes_per_step": n * n * 8 + n * 8, "d2h_bytes_per_step": n * 8,
+               "api": "ddla_dgesv_mixed (host pointers)"}
+
+    cpu = None
+    if not args.no_cpu and rank == 0 and world == 1:
+        threads = max(1, (os.cpu_count() or 2) // 2)
+        v, dt = cpu_sample(args.cpu_n, threads)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"oracle dgetrf+dgetrs (C restatement of DDLA managed LU) n={args.cpu_n}, one solve, "
+                         f"{dt:.2f} s, ProcessorCount/2 threads like ParallelHelperEX"}
+
+    if rank == 0:
+        last = reps[-1]
+        out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f32-factor+f64-refine" if prec != D.PREC_FP64 else "f64",
+               "data": "synthetic N(0,1), seeded, inputs 512 MB > L2 (no flush needed)",
+               "config": {"workload": f"LU (partial pivoting) + solve, n={n}, 1 RHS, mixed {prec_name} factor + "
+                                      f"FP64 iterative refinement to backward error <= {TOL:g}",
+                          "n": n, "nrhs": 1, "precision": prec_name, "tol": TOL, "parallelism": f"replicas{world}",
+                          "l2": "inputs larger than L2"},
+               "backward_error": last["backward_error"], "refine_iterations": last["iterations"],
+               "factor_ms": last["factor_ms"], "refine_ms": last["refine_ms"],
+               "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+               "clocks": clk, "peaks_live": {"fp64_tflops": f64_peak, "fp32_tflops": f32_peak}}
+        print(json.dumps(out))
+    h.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -43,6 +43,15 @@ int workspace(ddla_handle h, int slot, size_t bytes, void **out) {
     return 0;
 }
 
+int max_dyn_smem(const void *fn, size_t optin, size_t *avail) {
+    cudaFuncAttributes fa;
+    DDLA_CUDA(cudaFuncGetAttributes(&fa, fn));
+    size_t lim = optin > fa.sharedSizeBytes ? optin - fa.sharedSizeBytes : 0;
+    DDLA_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lim));
+    *avail = lim;
+    return 0;
+}
+
 int pinned(ddla_handle h, size_t bytes, void **out) {
     if (h->pinned_bytes < bytes) {
         if (h->pinned) {

@@ -27,6 +27,7 @@ struct Status {
     do {                                                                                         \
         cudaError_t e_ = (expr);                                                                 \
         if (e_ != cudaSuccess) {                                                                 \
+            cudaGetLastError();                                                                  \
             ::ddla::set_error(std::string("CUDA error ") + cudaGetErrorString(e_) + " at " +      \
                               __FILE__ + ":" + std::to_string(__LINE__) + " in " #expr);         \
             return DDLA_ERR_CUDA;                                                                \
@@ -92,6 +93,10 @@ struct ddla_handle_s {
 namespace ddla {
 
 enum WsSlot { WS_A = 0, WS_B = 1, WS_C = 2, WS_TMP = 3, WS_PIV = 4, WS_F32 = 5, WS_X = 6, WS_MISC = 7 };
+
+// Raises the kernel's dynamic shared-memory limit to everything the device
+// allows beside its static shared memory; returns that limit in *avail.
+int max_dyn_smem(const void *fn, size_t optin, size_t *avail);
 
 // Returns a device buffer of at least `bytes` from slot `slot` (grown on demand).
 int workspace(ddla_handle h, int slot, size_t bytes, void **out);

@@ -13,6 +13,7 @@
 #include <climits>
 
 #include "common.cuh"
+#include "timing.cuh"
 
 namespace ddla {
 
@@ -134,10 +135,11 @@ __global__ void k_copy(const T *X, i64 rs, i64 cs, i64 m, i64 n, T *Y, i64 ld) {
 template <typename T>
 int diag_kernel(ddla_handle h, View<T> A11, int bs, int kind, i64 row_base) {
     size_t smem = sizeof(T) * (size_t)bs * (bs + 1);
-    static bool attr_set[2] = {false, false};
-    if (!attr_set[sizeof(T) == 8]) {
-        DDLA_CUDA(cudaFuncSetAttribute(k_diag<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->smem_optin));
-        attr_set[sizeof(T) == 8] = true;
+    static size_t avail[2] = {0, 0};
+    if (!avail[sizeof(T) == 8]) DDLA_TRY(max_dyn_smem((const void *)k_diag<T>, h->smem_optin, &avail[sizeof(T) == 8]));
+    if (smem > avail[sizeof(T) == 8]) {
+        set_error("diagonal block does not fit in shared memory");
+        return DDLA_ERR_UNSUPPORTED;
     }
     k_diag<T><<<1, DIAG_THREADS, smem, h->stream>>>(A11.p, A11.rs, A11.cs, bs, kind, h->d_info + INFO_PIVOT,
                                                    row_base);
@@ -167,14 +169,21 @@ int getrf(ddla_handle h, i64 n, View<T> A, int32_t *d_piv, int prec, int nb) {
     for (i64 j0 = 0; j0 < n; j0 += w) {
         int b = (int)(n - j0 < w ? n - j0 : w);
         View<T> rowsX = A.sub(j0, n - j0, 0, n);
-        DDLA_TRY(panel_lu<T>(h, rowsX, j0, b, d_piv + j0, j0, h->d_info + INFO_PIVOT));
+        {
+            Timed t(h->stream, TC_PANEL, 2.0 * b * b * ((n - j0) - b / 3.0), 2.0 * sizeof(T) * (n - j0) * (double)n);
+            DDLA_TRY(panel_lu<T>(h, rowsX, j0, b, d_piv + j0, j0, h->d_info + INFO_PIVOT));
+        }
         i64 r = n - j0 - b;
         if (r > 0) {
             View<const T> A11{A.p + j0 * A.rs + j0 * A.cs, b, b, A.rs, A.cs};
             View<T> A12 = A.sub(j0, b, j0 + b, r);
-            DDLA_TRY(trsm<T>(h, DDLA_LEFT, DDLA_LOWER, DDLA_NO_TRANSPOSE, DDLA_UNIT_DIAG, b, r, T(1), A11, A12));
+            {
+                Timed t(h->stream, TC_TRSM, (double)b * b * r, sizeof(T) * (2.0 * b * r + b * b));
+                DDLA_TRY(trsm<T>(h, DDLA_LEFT, DDLA_LOWER, DDLA_NO_TRANSPOSE, DDLA_UNIT_DIAG, b, r, T(1), A11, A12));
+            }
             View<const T> A21{A.p + (j0 + b) * A.rs + j0 * A.cs, r, b, A.rs, A.cs};
             View<const T> cA12{A12.p, b, r, A12.rs, A12.cs};
+            Timed t(h->stream, TC_UPDATE, 2.0 * r * r * b, sizeof(T) * (2.0 * r * r + 2.0 * r * b));
             DDLA_TRY(gemm_any<T>(h, prec, r, r, b, T(-1), A21, cA12, T(1), A.sub(j0 + b, r, j0 + b, r)));
         }
     }
@@ -253,6 +262,7 @@ int potrf(ddla_handle h, int uplo, i64 n, View<T> A, int prec, int nb) {
             View<T> L21 = L.sub(j0 + b, r, j0, b);
             DDLA_TRY(trsm<T>(h, DDLA_RIGHT, DDLA_LOWER, DDLA_TRANSPOSE, DDLA_NONUNIT_DIAG, r, b, T(1), cL11, L21));
             View<const T> cL21{L21.p, r, b, L21.rs, L21.cs};
+            Timed t(h->stream, TC_UPDATE, 1.0 * r * (r + 1) * b, sizeof(T) * (1.0 * r * (r + 1) + r * b));
             DDLA_TRY(gemm_any<T>(h, prec, r, r, b, T(-1), cL21, cL21.t(), T(1), L.sub(j0 + b, r, j0 + b, r),
                                  DDLA_LOWER));
         }

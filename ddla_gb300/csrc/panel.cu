@@ -361,19 +361,21 @@ __global__ void k_copy_back(const T *Y, i64 n, i64 ncol, T *X, i64 rs, i64 cs) {
 // ------------------------------------------------------------------ host side
 
 namespace {
-int g_max_cluster[2] = {0, 0};  // [double, float]
+int g_max_cluster[2] = {0, 0};      // [double, float]
+size_t g_panel_smem[2] = {0, 0};    // dynamic shared memory available to k_panel_lu<T>
 
 template <typename T>
 int max_cluster(ddla_handle h) {
     int &mc = g_max_cluster[sizeof(T) == 8 ? 0 : 1];
     if (mc) return mc;
     DDLA_CUDA(cudaFuncSetAttribute(k_panel_lu<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-    DDLA_CUDA(cudaFuncSetAttribute(k_panel_lu<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)h->smem_optin));
+    size_t avail = 0;
+    DDLA_TRY(max_dyn_smem((const void *)k_panel_lu<T>, h->smem_optin, &avail));
+    g_panel_smem[sizeof(T) == 8 ? 0 : 1] = avail;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(PANEL_MAXCS);
     cfg.blockDim = dim3(PANEL_THREADS);
-    cfg.dynamicSmemBytes = h->smem_optin;
+    cfg.dynamicSmemBytes = avail;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
     attr[0].val.clusterDim.x = PANEL_MAXCS;
@@ -391,6 +393,8 @@ int max_cluster(ddla_handle h) {
     mc = p2;
     return mc;
 }
+template <typename T>
+size_t panel_smem_avail() { return g_panel_smem[sizeof(T) == 8 ? 0 : 1]; }
 }  // namespace
 
 // Widest panel (power of two, <= 64) whose m rows fit in one cluster.
@@ -400,7 +404,7 @@ int panel_width_for(ddla_handle h, i64 m) {
     if (cs <= 0) return 0;
     for (int w = PANEL_WMAX; w >= 8; w /= 2) {
         i64 rp = (m + cs - 1) / cs;
-        if (panel_smem_layout<T>((int)rp, w).total <= h->smem_optin) return w;
+        if (panel_smem_layout<T>((int)rp, w).total <= panel_smem_avail<T>()) return w;
     }
     return 0;
 }
@@ -428,14 +432,16 @@ int panel_lu(ddla_handle h, View<T> X, i64 pc, int w, int32_t *d_piv, i64 row_ba
     a.touch_rows = trows;
     a.touch_src = tsrc;
     int cs = max_cluster<T>(h);
+    if (cs <= 0) return cs < 0 ? cs : DDLA_ERR_UNSUPPORTED;
+    const size_t avail = panel_smem_avail<T>();
     // smallest cluster that holds the rows with at most 512 rows per CTA
     int use = 1;
     while (use < cs && ((m + use - 1) / use > 512 ||
-                        panel_smem_layout<T>((int)((m + use - 1) / use), w).total > h->smem_optin))
+                        panel_smem_layout<T>((int)((m + use - 1) / use), w).total > avail))
         use *= 2;
     i64 rp = (m + use - 1) / use;
     size_t smem = panel_smem_layout<T>((int)rp, w).total;
-    if (w <= PANEL_WMAX && smem <= h->smem_optin) {
+    if (w <= PANEL_WMAX && smem <= avail) {
         a.rows_per = (int)rp;
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(use);
@@ -475,9 +481,9 @@ int apply_perm(ddla_handle h, View<T> B, const int32_t *d_piv, i64 n, bool forwa
     DDLA_TRY(workspace(h, WS_MISC, sizeof(int) * (size_t)n, (void **)&perm));
     DDLA_TRY(workspace(h, WS_TMP, sizeof(T) * (size_t)n * B.cols, (void **)&tmp));
     size_t sm = sizeof(int) * (size_t)n;
-    if (sm <= h->smem_optin) {
-        DDLA_CUDA(cudaFuncSetAttribute(k_piv_to_perm_smem, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)h->smem_optin));
+    size_t avail = 0;
+    DDLA_TRY(max_dyn_smem((const void *)k_piv_to_perm_smem, h->smem_optin, &avail));
+    if (sm <= avail) {
         k_piv_to_perm_smem<<<1, 256, sm, s>>>(d_piv, n, perm);
     } else {
         k_piv_to_perm_global<<<1, 1, 0, s>>>(d_piv, n, perm);
