@@ -82,7 +82,7 @@ struct ddla_handle_s {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     // Growable device scratch areas (indexed by purpose).
-    ddla::Workspace ws[8];
+    ddla::Workspace ws[16];
     // Pinned host staging for host-pointer calls.
     void *pinned = nullptr;
     size_t pinned_bytes = 0;
@@ -92,7 +92,18 @@ struct ddla_handle_s {
 
 namespace ddla {
 
-enum WsSlot { WS_A = 0, WS_B = 1, WS_C = 2, WS_TMP = 3, WS_PIV = 4, WS_F32 = 5, WS_X = 6, WS_MISC = 7 };
+// Scratch slots.  A slot may be reallocated by its next user, so a buffer
+// must not be held across a call that uses the same slot:
+//   WS_A/B/C   host staging of operands, mixed-solver vectors
+//   WS_TMP     TRSM copies, row-permutation temporaries
+//   WS_PIV     LU panel touched-row lists      WS_F32  FP32 factor copy
+//   WS_X       device pivots                   WS_MISC TRSV flags, permutations
+//   WS_TRI     inverted diagonal blocks        WS_Y    LDL^T Y block
+//   WS_PERM    row permutation kept by getrf   WS_TC   tensor-core split operands
+enum WsSlot {
+    WS_A = 0, WS_B = 1, WS_C = 2, WS_TMP = 3, WS_PIV = 4, WS_F32 = 5, WS_X = 6, WS_MISC = 7,
+    WS_TRI = 8, WS_Y = 9, WS_PERM = 10, WS_TC = 11, WS_TC2 = 12
+};
 
 // Raises the kernel's dynamic shared-memory limit to everything the device
 // allows beside its static shared memory; returns that limit in *avail.
@@ -133,8 +144,13 @@ int gemm_any(ddla_handle h, int prec, i64 m, i64 n, i64 k, T alpha, View<const T
              View<T> C, int uplo = DDLA_DENSE);
 
 // Factorization drivers (device data, row/col strides arbitrary).
+// d_perm (optional, n ints): receives the row permutation of the
+// factorization (row k of P*A is row d_perm[k] of A).
 template <typename T>
-int getrf(ddla_handle h, i64 n, View<T> A, int32_t *d_piv, int prec, int nb);
+int getrf(ddla_handle h, i64 n, View<T> A, int32_t *d_piv, int prec, int nb, int *d_perm = nullptr);
+// Solve with the factors and the permutation vector of getrf.
+template <typename T>
+int getrs_perm(ddla_handle h, i64 n, i64 nrhs, View<const T> LU, const int *d_perm, View<T> B);
 template <typename T>
 int getrs(ddla_handle h, int trans, i64 n, i64 nrhs, View<const T> LU, const int32_t *d_piv, View<T> B);
 template <typename T>
@@ -150,9 +166,14 @@ int ldlt(ddla_handle h, int uplo, i64 n, View<T> A, int prec, int nb);
 template <typename T>
 int ldlts(ddla_handle h, int uplo, i64 n, i64 nrhs, View<const T> A, View<T> B);
 
-// Row interchanges of rows [0, npiv) of X with relative pivots (forward or
-// backward), applied to every column of X.
+// Triangular-solve building blocks (trsm.cu): inverses of the 64 x 64
+// diagonal blocks, and the chained whole-system solve for <= 16 columns.
 template <typename T>
-int laswp(cudaStream_t s, View<T> X, const int32_t *d_piv, i64 npiv, bool forward);
+int tri_inverse(ddla_handle h, bool lower, bool unit, View<const T> A, i64 n, T *inv);
+template <typename T>
+int trsv_apply(ddla_handle h, bool lower, View<const T> A, i64 n, const T *inv, T *X, i64 ldx, int nr);
+// Rows of B reordered by a permutation (forward: row k <- row perm[k]).
+template <typename T>
+int permute_rows(ddla_handle h, View<T> B, const int *perm, i64 n, bool forward);
 
 }  // namespace ddla

@@ -20,7 +20,7 @@ namespace ddla {
 template <typename T>
 int panel_width_for(ddla_handle h, i64 m);
 template <typename T>
-int panel_lu(ddla_handle h, View<T> X, i64 pc, int w, int32_t *d_piv, i64 row_base, int *d_info);
+int panel_lu(ddla_handle h, View<T> X, i64 pc, int w, int32_t *d_piv, i64 row_base, int *d_info, int *perm);
 template <typename T>
 int apply_perm(ddla_handle h, View<T> B, const int32_t *d_piv, i64 n, bool forward);
 
@@ -159,10 +159,18 @@ int pick_nb(int nb, int dflt) { return nb > 0 ? (nb > DIAG_MAX ? DIAG_MAX : nb) 
 }  // namespace
 
 // ------------------------------------------------------------------ LU (pivoted)
+__global__ void k_iota(int *p, i64 n) {
+    for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < n; e += (i64)gridDim.x * blockDim.x) p[e] = (int)e;
+}
+
 template <typename T>
-int getrf(ddla_handle h, i64 n, View<T> A, int32_t *d_piv, int prec, int nb) {
+int getrf(ddla_handle h, i64 n, View<T> A, int32_t *d_piv, int prec, int nb, int *d_perm) {
     if (n == 0) return 0;
     prec = prec_of<T>(prec);
+    if (d_perm) {
+        k_iota<<<grid_for(n), 256, 0, h->stream>>>(d_perm, n);
+        DDLA_LAUNCHED();
+    }
     int w = panel_width_for<T>(h, n);
     if (w == 0) w = 8;
     if (nb > 0 && nb < w) w = nb < 8 ? 8 : nb;
@@ -171,7 +179,8 @@ int getrf(ddla_handle h, i64 n, View<T> A, int32_t *d_piv, int prec, int nb) {
         View<T> rowsX = A.sub(j0, n - j0, 0, n);
         {
             Timed t(h->stream, TC_PANEL, 2.0 * b * b * ((n - j0) - b / 3.0), 2.0 * sizeof(T) * (n - j0) * (double)n);
-            DDLA_TRY(panel_lu<T>(h, rowsX, j0, b, d_piv + j0, j0, h->d_info + INFO_PIVOT));
+            DDLA_TRY(panel_lu<T>(h, rowsX, j0, b, d_piv + j0, j0, h->d_info + INFO_PIVOT,
+                                 d_perm ? d_perm + j0 : nullptr));
         }
         i64 r = n - j0 - b;
         if (r > 0) {
@@ -202,6 +211,15 @@ int getrs(ddla_handle h, int trans, i64 n, i64 nrhs, View<const T> LU, const int
         DDLA_TRY(trsm<T>(h, DDLA_LEFT, DDLA_LOWER, DDLA_TRANSPOSE, DDLA_UNIT_DIAG, n, nrhs, T(1), LU, B));
         DDLA_TRY(apply_perm<T>(h, B, d_piv, n, false));
     }
+    return 0;
+}
+
+template <typename T>
+int getrs_perm(ddla_handle h, i64 n, i64 nrhs, View<const T> LU, const int *d_perm, View<T> B) {
+    if (n == 0 || nrhs == 0) return 0;
+    DDLA_TRY(permute_rows<T>(h, B, d_perm, n, true));
+    DDLA_TRY(trsm<T>(h, DDLA_LEFT, DDLA_LOWER, DDLA_NO_TRANSPOSE, DDLA_UNIT_DIAG, n, nrhs, T(1), LU, B));
+    DDLA_TRY(trsm<T>(h, DDLA_LEFT, DDLA_UPPER, DDLA_NO_TRANSPOSE, DDLA_NONUNIT_DIAG, n, nrhs, T(1), LU, B));
     return 0;
 }
 
@@ -287,7 +305,7 @@ int ldlt(ddla_handle h, int uplo, i64 n, View<T> A, int prec, int nb) {
     nb = pick_nb(nb, DIAG_MAX);
     View<T> L = (uplo == DDLA_UPPER) ? A.t() : A;
     T *Y = nullptr;
-    if (n > nb) DDLA_TRY(workspace(h, WS_TMP, sizeof(T) * (size_t)(n - nb) * nb, (void **)&Y));
+    if (n > nb) DDLA_TRY(workspace(h, WS_Y, sizeof(T) * (size_t)(n - nb) * nb, (void **)&Y));
     for (i64 j0 = 0; j0 < n; j0 += nb) {
         int b = (int)(n - j0 < nb ? n - j0 : nb);
         i64 r = n - j0 - b;
@@ -328,7 +346,8 @@ int ldlts(ddla_handle h, int uplo, i64 n, i64 nrhs, View<const T> A, View<T> B) 
 }
 
 #define INST(T)                                                                                     \
-    template int getrf<T>(ddla_handle, i64, View<T>, int32_t *, int, int);                          \
+    template int getrf<T>(ddla_handle, i64, View<T>, int32_t *, int, int, int *);                   \
+    template int getrs_perm<T>(ddla_handle, i64, i64, View<const T>, const int *, View<T>);        \
     template int getrs<T>(ddla_handle, int, i64, i64, View<const T>, const int32_t *, View<T>);     \
     template int getrf_nopiv<T>(ddla_handle, i64, View<T>, int, int);                               \
     template int getrs_nopiv<T>(ddla_handle, int, i64, i64, View<const T>, View<T>);                \

@@ -51,7 +51,7 @@ struct PanelArgs {
 };
 
 struct PanelSmem {
-    size_t rows, origin, cand_row, jrow, urow, prow, cand_val, cand_idx, orgs, red, total;
+    size_t rows, origin, ucur, cand_val, cand_idx, cand_org, cand_rows, jrow, jorg, red, total;
 };
 
 template <typename T>
@@ -65,44 +65,77 @@ __host__ __device__ inline PanelSmem panel_smem_layout(int rows_per, int w) {
     };
     L.rows = take(sizeof(T) * (size_t)rows_per * (w + 1));
     L.origin = take(sizeof(int) * (size_t)rows_per);
-    L.cand_row = take(sizeof(T) * 2 * w);
-    L.jrow = take(sizeof(T) * 2 * w);
-    L.urow = take(sizeof(T) * w);
-    L.prow = take(sizeof(T) * w);
+    L.ucur = take(sizeof(T) * w);
     L.cand_val = take(sizeof(double) * 2 * PANEL_MAXCS);
     L.cand_idx = take(sizeof(int) * 2 * PANEL_MAXCS);
-    L.orgs = take(sizeof(int) * 4);
+    L.cand_org = take(sizeof(int) * 2 * PANEL_MAXCS);
+    L.cand_rows = take(sizeof(T) * 2 * PANEL_MAXCS * w);
+    L.jrow = take(sizeof(T) * 2 * w);
+    L.jorg = take(sizeof(int) * 2);
     L.red = take((sizeof(double) + sizeof(int)) * (PANEL_THREADS / 32) + 16);
     L.total = o;
     return L;
 }
 
+// Block-wide first-max reduction of (value, row) pairs; result in s_val/s_idx.
+__device__ __forceinline__ void block_argmax(double bv, int bi, double *red_v, int *red_i, double *s_val,
+                                             int *s_idx) {
+    constexpr int NW = PANEL_THREADS / 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        double ov = __shfl_down_sync(0xffffffffu, bv, off);
+        int oi = __shfl_down_sync(0xffffffffu, bi, off);
+        if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
+    }
+    if (lane == 0) { red_v[warp] = bv; red_i[warp] = bi; }
+    __syncthreads();
+    if (warp == 0) {
+        bv = lane < NW ? red_v[lane] : -1.0;
+        bi = lane < NW ? red_i[lane] : INT_MAX;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            double ov = __shfl_down_sync(0xffffffffu, bv, off);
+            int oi = __shfl_down_sync(0xffffffffu, bi, off);
+            if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
+        }
+        if (lane == 0) { *s_val = bv; *s_idx = bi; }
+    }
+    __syncthreads();
+}
+
+// Panel factorization, one cluster (see the file comment).  Per column the
+// critical path is: winner -> swap -> scale + update of the next column and
+// its local argmax -> finish the two rows that will be published -> push
+// candidates to every CTA (DSMEM stores) -> barrier arrive.  The rank-1 update
+// of the remaining columns runs between the barrier's arrive and wait.
 template <typename T>
 __global__ void __launch_bounds__(PANEL_THREADS) k_panel_lu(PanelArgs<T> a) {
     cg::cluster_group cluster = cg::this_cluster();
     const int CS = (int)cluster.num_blocks();
     const int rank = (int)cluster.block_rank();
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    constexpr int NW = PANEL_THREADS / 32;
+    const int tid = threadIdx.x;
     extern __shared__ __align__(16) unsigned char smem[];
     const int w = a.w, WP = w + 1, rp = a.rows_per;
     const PanelSmem L = panel_smem_layout<T>(rp, w);
     T *rows = (T *)(smem + L.rows);
     int *origin = (int *)(smem + L.origin);
-    T *cand_row = (T *)(smem + L.cand_row);
-    T *jrow = (T *)(smem + L.jrow);
-    T *urow = (T *)(smem + L.urow);
-    T *prow = (T *)(smem + L.prow);
+    T *ucur = (T *)(smem + L.ucur);
     double *cand_val = (double *)(smem + L.cand_val);
     int *cand_idx = (int *)(smem + L.cand_idx);
-    int *orgs = (int *)(smem + L.orgs);  // [0..1] my candidate origin, [2..3] row-j origin
+    int *cand_org = (int *)(smem + L.cand_org);
+    T *cand_rows = (T *)(smem + L.cand_rows);
+    T *jrow = (T *)(smem + L.jrow);
+    int *jorg = (int *)(smem + L.jorg);
     double *red_v = (double *)(smem + L.red);
-    int *red_i = (int *)(red_v + NW);
+    int *red_i = (int *)(red_v + PANEL_THREADS / 32);
+    __shared__ double s_bval;
     __shared__ int s_best;
 
     const int base = rank * rp;
     int nloc = a.m - base;
     nloc = nloc < 0 ? 0 : (nloc > rp ? rp : nloc);
+    auto owns = [&](int g) { return g >= base && g < base + nloc; };
 
     if (rank == 0 && tid == 0) *a.touch_count = 0;
     for (int e = tid; e < nloc * w; e += PANEL_THREADS) {
@@ -112,113 +145,127 @@ __global__ void __launch_bounds__(PANEL_THREADS) k_panel_lu(PanelArgs<T> a) {
     for (int l = tid; l < nloc; l += PANEL_THREADS) origin[l] = base + l;
     __syncthreads();
 
+    // Publish (value, row index, row, origin) of my candidate for column jn,
+    // and row jn itself if I own it, into buffer jn&1 of every CTA.
+    auto push = [&](int jn) {
+        const int nbf = jn & 1;
+        const int cb = s_best;
+        if (tid < CS) {
+            cluster.map_shared_rank(cand_val, tid)[nbf * PANEL_MAXCS + rank] = s_bval;
+            cluster.map_shared_rank(cand_idx, tid)[nbf * PANEL_MAXCS + rank] = cb;
+            cluster.map_shared_rank(cand_org, tid)[nbf * PANEL_MAXCS + rank] = cb != INT_MAX ? origin[cb - base] : 0;
+            if (owns(jn)) cluster.map_shared_rank(jorg, tid)[nbf] = origin[jn - base];
+        }
+        if (cb != INT_MAX) {
+            const T *src = rows + (cb - base) * WP;
+            for (int e = tid; e < CS * w; e += PANEL_THREADS) {
+                int r2 = e / w, c = e % w;
+                cluster.map_shared_rank(cand_rows, r2)[(nbf * PANEL_MAXCS + rank) * w + c] = src[c];
+            }
+        }
+        if (owns(jn)) {
+            const T *src = rows + (jn - base) * WP;
+            for (int e = tid; e < CS * w; e += PANEL_THREADS) {
+                int r2 = e / w, c = e % w;
+                cluster.map_shared_rank(jrow, r2)[nbf * w + c] = src[c];
+            }
+        }
+    };
+
     const int kmax = a.m < w ? a.m : w;
-    for (int j = 0; j < kmax; j++) {
-        const int buf = j & 1;
-        // 1. local first-max of |column j| over rows g >= j
+    {
         double bv = -1.0;
         int bi = INT_MAX;
-        int l0 = j - base;
-        if (l0 < 0) l0 = 0;
-        for (int l = l0 + tid; l < nloc; l += PANEL_THREADS) {
-            double v = fabs((double)rows[l * WP + j]);
+        for (int l = tid; l < nloc; l += PANEL_THREADS) {
+            double v = fabs((double)rows[l * WP]);
             if (v > bv) { bv = v; bi = base + l; }
         }
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            double ov = __shfl_down_sync(0xffffffffu, bv, off);
-            int oi = __shfl_down_sync(0xffffffffu, bi, off);
-            if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
-        }
-        if (lane == 0) { red_v[warp] = bv; red_i[warp] = bi; }
-        __syncthreads();
-        if (tid == 0) {
-            for (int q = 1; q < NW; q++)
-                if (red_v[q] > bv || (red_v[q] == bv && red_i[q] < bi)) { bv = red_v[q]; bi = red_i[q]; }
-            s_best = bi;
-            for (int r2 = 0; r2 < CS; r2++) {
-                double *cv = cluster.map_shared_rank(cand_val, r2);
-                int *ci = cluster.map_shared_rank(cand_idx, r2);
-                cv[buf * PANEL_MAXCS + rank] = bv;
-                ci[buf * PANEL_MAXCS + rank] = bi;
-            }
-        }
-        __syncthreads();
-        // 2. publish my candidate row and, if I own it, row j
-        {
-            int mine = s_best;
-            if (mine != INT_MAX) {
-                int lb = mine - base;
-                for (int c = tid; c < w; c += PANEL_THREADS) cand_row[buf * w + c] = rows[lb * WP + c];
-                if (tid == 0) orgs[buf] = origin[lb];
-            }
-            if (j >= base && j < base + nloc) {
-                int lj = j - base;
-                for (int c = tid; c < w; c += PANEL_THREADS) jrow[buf * w + c] = rows[lj * WP + c];
-                if (tid == 0) orgs[2 + buf] = origin[lj];
-            }
-        }
+        block_argmax(bv, bi, red_v, red_i, &s_bval, &s_best);
+        push(0);
         cluster.sync();
-        // 3. winner (identical in every CTA)
+    }
+
+    for (int j = 0; j < kmax; j++) {
+        const int buf = j & 1;
+        // winner (identical in every CTA, from local copies)
         double wv = -1.0;
-        int wi = INT_MAX;
+        int wi = INT_MAX, wr = 0;
         for (int r2 = 0; r2 < CS; r2++) {
             double v = cand_val[buf * PANEL_MAXCS + r2];
             int i = cand_idx[buf * PANEL_MAXCS + r2];
-            if (v > wv || (v == wv && i < wi)) { wv = v; wi = i; }
+            if (v > wv || (v == wv && i < wi)) { wv = v; wi = i; wr = r2; }
         }
-        const int oj = j / rp;
-        const int p = (wi == INT_MAX) ? j : wi;
-        const int op = p / rp;
+        const bool none = (wi == INT_MAX);
+        const int p = none ? j : wi;
+        const T *usrc = none ? jrow + buf * w : cand_rows + (buf * PANEL_MAXCS + wr) * w;
+        const int uorg = none ? jorg[buf] : cand_org[buf * PANEL_MAXCS + wr];
+        for (int c = tid; c < w; c += PANEL_THREADS) ucur[c] = usrc[c];
         if (rank == 0 && tid == 0) a.piv[j] = p - j;
-        // 4. fetch the pivot row (winner's candidate row) and, for the owner of
-        //    p, the old row j
-        {
-            const T *src = (wi == INT_MAX) ? cluster.map_shared_rank(jrow + buf * w, oj)
-                                           : cluster.map_shared_rank(cand_row + buf * w, op);
-            for (int c = tid; c < w; c += PANEL_THREADS) urow[c] = src[c];
-            if (op == rank && p != j) {
-                const T *js = cluster.map_shared_rank(jrow + buf * w, oj);
-                for (int c = tid; c < w; c += PANEL_THREADS) prow[c] = js[c];
-            }
-        }
-        int urow_org = 0, jorg = 0;
-        if (tid == 0) {
-            urow_org = (wi == INT_MAX) ? *cluster.map_shared_rank(orgs + 2 + buf, oj)
-                                       : *cluster.map_shared_rank(orgs + buf, op);
-            jorg = *cluster.map_shared_rank(orgs + 2 + buf, oj);
-        }
         __syncthreads();
-        // 5. swap rows j and p
         if (p != j) {
-            if (oj == rank) {
-                int lj = j - base;
-                for (int c = tid; c < w; c += PANEL_THREADS) rows[lj * WP + c] = urow[c];
-                if (tid == 0) origin[lj] = urow_org;
+            if (owns(j)) {
+                for (int c = tid; c < w; c += PANEL_THREADS) rows[(j - base) * WP + c] = ucur[c];
+                if (tid == 0) origin[j - base] = uorg;
             }
-            if (op == rank) {
-                int lp = p - base;
-                for (int c = tid; c < w; c += PANEL_THREADS) rows[lp * WP + c] = prow[c];
-                if (tid == 0) origin[lp] = jorg;
+            if (owns(p)) {
+                for (int c = tid; c < w; c += PANEL_THREADS) rows[(p - base) * WP + c] = jrow[buf * w + c];
+                if (tid == 0) origin[p - base] = jorg[buf];
             }
         }
         __syncthreads();
-        // 6. scale and rank-1 update of rows g > j, one thread per row
-        const T ujj = urow[j];
+        const T ujj = ucur[j];
         if (ujj == T(0)) {
             if (rank == 0 && tid == 0) atomicMin(a.info, (int)(a.row_base + j + 1));
             break;
         }
         const T rinv = T(1) / ujj;
+        const bool more = j + 1 < kmax;
         int ls = j + 1 - base;
         if (ls < 0) ls = 0;
+        // scale column j, update column j+1 and find its local first max
+        double bv = -1.0;
+        int bi = INT_MAX;
+        const T u1 = (j + 1 < w) ? ucur[j + 1] : T(0);
         for (int l = ls + tid; l < nloc; l += PANEL_THREADS) {
             T *row = rows + l * WP;
             T lv = row[j] * rinv;
             row[j] = lv;
-            for (int c = j + 1; c < w; c++) row[c] = fma(lv, -urow[c], row[c]);
+            if (j + 1 < w) {
+                T v = fma(lv, -u1, row[j + 1]);
+                row[j + 1] = v;
+                double av = fabs((double)v);
+                if (av > bv) { bv = av; bi = base + l; }
+            }
+        }
+        int cb = INT_MAX;
+        if (more) {
+            block_argmax(bv, bi, red_v, red_i, &s_bval, &s_best);
+            cb = s_best;
+            // finish the rows that get published: the candidate and row j+1
+            for (int c = j + 2 + tid; c < w; c += PANEL_THREADS) {
+                if (cb != INT_MAX) {
+                    T *row = rows + (cb - base) * WP;
+                    row[c] = fma(row[j], -ucur[c], row[c]);
+                }
+                if (owns(j + 1) && j + 1 != cb) {
+                    T *row = rows + (j + 1 - base) * WP;
+                    row[c] = fma(row[j], -ucur[c], row[c]);
+                }
+            }
+            __syncthreads();
+            push(j + 1);
+            cluster.barrier_arrive();
+        }
+        // rank-1 update of the remaining columns (overlaps the barrier)
+        for (int l = ls + tid; l < nloc; l += PANEL_THREADS) {
+            const int g = base + l;
+            if (more && (g == cb || g == j + 1)) continue;
+            T *row = rows + l * WP;
+            const T lv = row[j];
+            for (int c = j + 2; c < w; c++) row[c] = fma(lv, -ucur[c], row[c]);
         }
         __syncthreads();
+        if (more) cluster.barrier_wait();
     }
     // All DSMEM traffic must finish before any CTA of the cluster exits.
     cluster.sync();
@@ -413,7 +460,7 @@ int panel_width_for(ddla_handle h, i64 m) {
 // the interchanges to the other columns of the full rows: X is the m-row
 // block containing the panel at column offset pc, with ncols columns.
 template <typename T>
-int panel_lu(ddla_handle h, View<T> X, i64 pc, int w, int32_t *d_piv, i64 row_base, int *d_info) {
+int panel_lu(ddla_handle h, View<T> X, i64 pc, int w, int32_t *d_piv, i64 row_base, int *d_info, int *perm) {
     cudaStream_t s = h->stream;
     const i64 m = X.rows;
     int *tbuf;
@@ -469,6 +516,28 @@ int panel_lu(ddla_handle h, View<T> X, i64 pc, int w, int32_t *d_piv, i64 row_ba
         k_laswp_list<T><<<grid, 256, 0, s>>>(X.p, X.rs, X.cs, other, pc, w, tcount, trows, tsrc);
         DDLA_LAUNCHED();
     }
+    if (perm) {
+        // the permutation vector rides along as one more column
+        k_laswp_list<int><<<1, 256, 0, s>>>(perm, 1, 0, 1, 1, 0, tcount, trows, tsrc);
+        DDLA_LAUNCHED();
+    }
+    return 0;
+}
+
+// Y[k] = X[perm[k]] for the rows of B (forward) using a precomputed
+// permutation.
+template <typename T>
+int permute_rows(ddla_handle h, View<T> B, const int *perm, i64 n, bool forward) {
+    if (n == 0 || B.cols == 0) return 0;
+    cudaStream_t s = h->stream;
+    T *tmp;
+    DDLA_TRY(workspace(h, WS_TMP, sizeof(T) * (size_t)n * B.cols, (void **)&tmp));
+    i64 tot = n * B.cols;
+    int blocks = (int)((tot + 255) / 256 < 8192 ? (tot + 255) / 256 : 8192);
+    k_permute_rows<T><<<blocks, 256, 0, s>>>(B.p, B.rs, B.cs, n, B.cols, perm, forward, tmp);
+    DDLA_LAUNCHED();
+    k_copy_back<T><<<blocks, 256, 0, s>>>(tmp, n, B.cols, B.p, B.rs, B.cs);
+    DDLA_LAUNCHED();
     return 0;
 }
 
@@ -498,15 +567,12 @@ int apply_perm(ddla_handle h, View<T> B, const int32_t *d_piv, i64 n, bool forwa
     return 0;
 }
 
-template <typename T>
-int laswp(cudaStream_t, View<T>, const int32_t *, i64, bool) {
-    return DDLA_ERR_UNSUPPORTED;
-}
-
 template int panel_width_for<double>(ddla_handle, i64);
 template int panel_width_for<float>(ddla_handle, i64);
-template int panel_lu<double>(ddla_handle, View<double>, i64, int, int32_t *, i64, int *);
-template int panel_lu<float>(ddla_handle, View<float>, i64, int, int32_t *, i64, int *);
+template int panel_lu<double>(ddla_handle, View<double>, i64, int, int32_t *, i64, int *, int *);
+template int panel_lu<float>(ddla_handle, View<float>, i64, int, int32_t *, i64, int *, int *);
+template int permute_rows<double>(ddla_handle, View<double>, const int *, i64, bool);
+template int permute_rows<float>(ddla_handle, View<float>, const int *, i64, bool);
 template int apply_perm<double>(ddla_handle, View<double>, const int32_t *, i64, bool);
 template int apply_perm<float>(ddla_handle, View<float>, const int32_t *, i64, bool);
 

@@ -12,8 +12,6 @@
 
 namespace ddla {
 
-template <typename T>
-int getrf(ddla_handle h, i64 n, View<T> A, int32_t *d_piv, int prec, int nb);
 
 namespace {
 
@@ -211,7 +209,9 @@ int mixed_lu(ddla_handle h, i64 n, i64 nrhs, const double *A, const double *B, d
     float *A32, *d32;
     double *R;
     int32_t *piv;
+    int *perm;
     unsigned long long *norms;
+    DDLA_TRY(workspace(h, WS_PERM, sizeof(int) * (size_t)n, (void **)&perm));
     DDLA_TRY(workspace(h, WS_F32, sizeof(float) * (size_t)n * n, (void **)&A32));
     DDLA_TRY(workspace(h, WS_B, sizeof(float) * (size_t)n * nr + 256, (void **)&d32));
     DDLA_TRY(workspace(h, WS_C, sizeof(double) * (size_t)n * nr, (void **)&R));
@@ -221,7 +221,7 @@ int mixed_lu(ddla_handle h, i64 n, i64 nrhs, const double *A, const double *B, d
     DDLA_CUDA(cudaEventRecord(h->ev0, s));
     k_d2s<<<grid1(n * n), 256, 0, s>>>(A, n * n, A32);
     DDLA_LAUNCHED();
-    DDLA_TRY(getrf<float>(h, n, View<float>{A32, n, n, n, 1}, piv, prec, nb));
+    DDLA_TRY(getrf<float>(h, n, View<float>{A32, n, n, n, 1}, piv, prec, nb, perm));
     DDLA_CUDA(cudaEventRecord(h->ev1, s));
     int info;
     DDLA_TRY(read_info(h, &info));
@@ -231,7 +231,7 @@ int mixed_lu(ddla_handle h, i64 n, i64 nrhs, const double *A, const double *B, d
     rep->info = info;
     if (info) return info;
     auto solve32 = [&](float *d) {
-        return getrs<float>(h, 0, n, nr, View<const float>{A32, n, n, n, 1}, piv, View<float>{d, n, nr, nr, 1});
+        return getrs_perm<float>(h, n, nr, View<const float>{A32, n, n, n, 1}, perm, View<float>{d, n, nr, nr, 1});
     };
     DDLA_CUDA(cudaEventRecord(h->ev0, s));
     int rc = refine(h, n, nr, A, B, X, x_ref, opts, rep, solve32, d32, R, norms);

@@ -1,23 +1,28 @@
-// Triangular solve with many right-hand sides (BLIS trsm semantics).
+// Triangular solves (BLIS trsm semantics) built on inverted diagonal blocks.
 //
-// The problem is first normalised to a left solve with a non-transposed
-// triangle (a right solve X*op(A) = B is the left solve op(A)^T X^T = B^T; a
-// transposed triangle is the other triangle of the transposed view), then
-// solved in blocks of TB rows: a diagonal-block kernel (one thread per
-// right-hand-side column, triangle and columns in shared memory) followed by
-// a GEMM update of the remaining rows, forward for lower and backward for
-// upper triangles -- the block structure of DDLA's managed TrSM
-// (DDLA/BLAS/Managed/3m/TrSM.cs:62-122, blocks of KC rows, GEMM + TRSV).
+// The problem is normalised to a left solve tri(A) X = alpha B with a
+// non-transposed view (a right solve X op(A) = B is op(A)^T X^T = B^T; a
+// transposed triangle is the other triangle of the transposed view).  The
+// triangle is split into TB x TB diagonal blocks whose inverses are formed
+// once (k_tri_inv, one CTA per block).  Then:
+//   * few right-hand sides (<= 16): ONE kernel (k_trsv_chain) solves the whole
+//     system.  Each CTA owns a block row; it takes its block in ticket order
+//     (so every block it waits for is already running or done), subtracts
+//     L_ij x_j as each x_j is published (flag per block, bounded spin), then
+//     multiplies by inv(L_ii) and publishes x_i.  The off-diagonal tiles are
+//     loaded before the wait, so HBM latency overlaps the dependency chain.
+//   * many right-hand sides: per diagonal block X1 = inv(A11) B1 and the GEMM
+//     update B2 -= A21 X1 (DDLA's managed TrSM has the same block structure
+//     with a TRSV per column, DDLA/BLAS/Managed/3m/TrSM.cs:62-122).
 #include "common.cuh"
+#include "timing.cuh"
 
 namespace ddla {
 namespace {
 
-constexpr int TB = 64;   // rows per diagonal block
-// right-hand-side columns per CTA (one thread each); keeps the triangle plus
-// the column block within 48 KB of static shared memory
-template <typename T>
-constexpr int cw() { return sizeof(T) == 8 ? 32 : 64; }
+constexpr int TB = 64;
+constexpr int CHAIN_THREADS = 256;
+constexpr long long SPIN_LIMIT = 1LL << 24;
 
 template <typename T>
 __global__ void k_scale(T alpha, T *B, i64 m, i64 n, i64 rs, i64 cs) {
@@ -29,55 +34,156 @@ __global__ void k_scale(T alpha, T *B, i64 m, i64 n, i64 rs, i64 cs) {
     }
 }
 
-// Solve tri(A11) X = B1 for a bs x bs triangle (bs <= TB), columns split over
-// CTAs, one thread per column, four partial sums per dot product.
 template <typename T>
-__global__ void __launch_bounds__(cw<T>())
-    k_trsm_diag(int bs, i64 n, const T *__restrict__ A, i64 rsa, i64 csa, T *B, i64 rsb, i64 csb, int lower,
-                int unit) {
-    constexpr int CW = cw<T>();
-    __shared__ T L[TB][TB];
-    __shared__ T X[TB][CW];
-    const int t = threadIdx.x;
-    const i64 c = (i64)blockIdx.x * CW + t;
-    for (int e = t; e < bs * bs; e += CW) {
-        int i = e / bs, j = e % bs;
-        L[i][j] = A[i * rsa + j * csa];
+__global__ void k_copy2d(const T *X, i64 rs, i64 cs, i64 m, i64 n, T *Y, i64 yrs, i64 ycs) {
+    i64 tot = m * n;
+    for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < tot; e += (i64)gridDim.x * blockDim.x) {
+        i64 i = e / n, j = e % n;
+        Y[i * yrs + j * ycs] = X[i * rs + j * cs];
     }
-    if (c < n)
-        for (int i = 0; i < bs; i++) X[i][t] = B[i * rsb + c * csb];
+}
+
+// Inverse of each TB x TB diagonal block of tri(A) (lower/upper, unit or not),
+// stored row-major per block, zero outside the triangle.  One thread per
+// column of the identity; forward (lower) or backward (upper) substitution.
+template <typename T>
+__global__ void __launch_bounds__(TB) k_tri_inv(const T *A, i64 rs, i64 cs, i64 n, int lower, int unit, T *inv) {
+    __shared__ T L[TB][TB + 1];
+    __shared__ T Y[TB][TB + 1];
+    const int b = blockIdx.x, c = threadIdx.x;
+    const i64 r0 = (i64)b * TB;
+    const int bs = (int)(n - r0 < TB ? n - r0 : TB);
+    for (int i = 0; i < TB; i++) {
+        L[i][c] = (i < bs && c < bs) ? A[(r0 + i) * rs + (r0 + c) * cs] : T(0);
+        Y[i][c] = T(0);
+    }
     __syncthreads();
-    if (c >= n) return;
-    if (lower) {
-        for (int i = 0; i < bs; i++) {
-            T s0 = X[i][t], s1 = 0, s2 = 0, s3 = 0;
-            int p = 0;
-            for (; p + 3 < i; p += 4) {
-                s0 -= L[i][p] * X[p][t];
-                s1 -= L[i][p + 1] * X[p + 1][t];
-                s2 -= L[i][p + 2] * X[p + 2][t];
-                s3 -= L[i][p + 3] * X[p + 3][t];
+    if (c < bs) {
+        if (lower) {
+            for (int r = c; r < bs; r++) {
+                T s = (r == c) ? T(1) : T(0);
+                for (int k = c; k < r; k++) s -= L[r][k] * Y[k][c];
+                Y[r][c] = unit ? s : s / L[r][r];
             }
-            for (; p < i; p++) s0 -= L[i][p] * X[p][t];
-            T s = (s0 + s1) + (s2 + s3);
-            X[i][t] = unit ? s : s / L[i][i];
-        }
-    } else {
-        for (int i = bs - 1; i >= 0; i--) {
-            T s0 = X[i][t], s1 = 0, s2 = 0, s3 = 0;
-            int p = i + 1;
-            for (; p + 3 < bs; p += 4) {
-                s0 -= L[i][p] * X[p][t];
-                s1 -= L[i][p + 1] * X[p + 1][t];
-                s2 -= L[i][p + 2] * X[p + 2][t];
-                s3 -= L[i][p + 3] * X[p + 3][t];
+        } else {
+            for (int r = c; r >= 0; r--) {
+                T s = (r == c) ? T(1) : T(0);
+                for (int k = r + 1; k <= c; k++) s -= L[r][k] * Y[k][c];
+                Y[r][c] = unit ? s : s / L[r][r];
             }
-            for (; p < bs; p++) s0 -= L[i][p] * X[p][t];
-            T s = (s0 + s1) + (s2 + s3);
-            X[i][t] = unit ? s : s / L[i][i];
         }
     }
-    for (int i = 0; i < bs; i++) B[i * rsb + c * csb] = X[i][t];
+    __syncthreads();
+    T *out = inv + (i64)b * TB * TB;
+    for (int i = 0; i < TB; i++) out[i * TB + c] = Y[i][c];
+}
+
+__device__ __forceinline__ int ld_acquire(const int *p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release(int *p, int v) {
+    asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Whole-system solve with <= NR right-hand sides, X row-major n x ldx.
+// Thread t works on block row r = t/4, k-quarter q = t%4 (16 columns of the
+// tile), reduces its partial dot products over the 4 threads of the row.
+template <typename T, int NR>
+__global__ void __launch_bounds__(CHAIN_THREADS)
+    k_trsv_chain(i64 n, int nblk, const T *__restrict__ A, i64 rs, i64 cs, int lower, const T *__restrict__ inv,
+                 T *X, i64 ldx, int nr, int *flags, int *ticket, int *err) {
+    __shared__ T s_acc[TB][NR];
+    __shared__ T s_x[TB][NR];
+    __shared__ int s_blk, s_abort;
+    const int t = threadIdx.x, r = t >> 2, q = t & 3;
+    if (t == 0) {
+        s_blk = atomicAdd(ticket, 1);
+        s_abort = 0;
+    }
+    __syncthreads();
+    const int logical = s_blk;
+    const int blk = lower ? logical : nblk - 1 - logical;
+    const i64 r0 = (i64)blk * TB;
+    const int rows = (int)(n - r0 < TB ? n - r0 : TB);
+    for (int e = t; e < TB * NR; e += CHAIN_THREADS) {
+        int i = e / NR, c = e % NR;
+        s_acc[i][c] = (i < rows && c < nr) ? X[(r0 + i) * ldx + c] : T(0);
+    }
+    __syncthreads();
+    for (int d = 0; d < logical; d++) {
+        const int j = lower ? d : nblk - 1 - d;
+        const i64 c0 = (i64)j * TB;
+        const int cols = (int)(n - c0 < TB ? n - c0 : TB);
+        // tile row r, columns q*16 .. q*16+15 (loaded before waiting)
+        T a[16];
+#pragma unroll
+        for (int k = 0; k < 16; k++) {
+            int cc = q * 16 + k;
+            a[k] = (r < rows && cc < cols) ? A[(r0 + r) * rs + (c0 + cc) * cs] : T(0);
+        }
+        if (t == 0) {
+            long long it = 0;
+            while (ld_acquire(flags + j) == 0) {
+                if (++it > SPIN_LIMIT) {
+                    atomicExch(err, 1);
+                    s_abort = 1;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __syncthreads();
+        if (s_abort) return;
+        for (int e = t; e < TB * NR; e += CHAIN_THREADS) {
+            int i = e / NR, c = e % NR;
+            s_x[i][c] = (i < cols && c < nr) ? __ldcg(&X[(c0 + i) * ldx + c]) : T(0);
+        }
+        __syncthreads();
+        T p[NR];
+#pragma unroll
+        for (int c = 0; c < NR; c++) p[c] = T(0);
+#pragma unroll
+        for (int k = 0; k < 16; k++)
+#pragma unroll
+            for (int c = 0; c < NR; c++) p[c] += a[k] * s_x[q * 16 + k][c];
+#pragma unroll
+        for (int c = 0; c < NR; c++) {
+            p[c] += __shfl_xor_sync(0xffffffffu, p[c], 1);
+            p[c] += __shfl_xor_sync(0xffffffffu, p[c], 2);
+        }
+        if (q == 0)
+#pragma unroll
+            for (int c = 0; c < NR; c++) s_acc[r][c] -= p[c];
+        __syncthreads();
+    }
+    // x_blk = inv(A_blk,blk) * acc
+    {
+        const T *iv = inv + (i64)blk * TB * TB;
+        T a[16];
+#pragma unroll
+        for (int k = 0; k < 16; k++) a[k] = iv[r * TB + q * 16 + k];
+        T p[NR];
+#pragma unroll
+        for (int c = 0; c < NR; c++) p[c] = T(0);
+#pragma unroll
+        for (int k = 0; k < 16; k++)
+#pragma unroll
+            for (int c = 0; c < NR; c++) p[c] += a[k] * s_acc[q * 16 + k][c];
+#pragma unroll
+        for (int c = 0; c < NR; c++) {
+            p[c] += __shfl_xor_sync(0xffffffffu, p[c], 1);
+            p[c] += __shfl_xor_sync(0xffffffffu, p[c], 2);
+        }
+        if (q == 0 && r < rows)
+            for (int c = 0; c < nr; c++) X[(r0 + r) * ldx + c] = p[c];
+    }
+    __syncthreads();
+    if (t == 0) {
+        __threadfence();
+        st_release(flags + blk, 1);
+    }
 }
 
 template <typename T>
@@ -91,12 +197,20 @@ int scale(cudaStream_t s, T alpha, View<T> B) {
 }
 
 template <typename T>
-int diag_solve(cudaStream_t s, int bs, View<const T> A11, View<T> B1, bool lower, bool unit) {
-    i64 n = B1.cols;
-    constexpr int CW = cw<T>();
-    unsigned grid = (unsigned)((n + CW - 1) / CW);
-    k_trsm_diag<T><<<grid, CW, 0, s>>>(bs, n, A11.p, A11.rs, A11.cs, B1.p, B1.rs, B1.cs, lower ? 1 : 0,
-                                       unit ? 1 : 0);
+int copy2d(cudaStream_t s, View<const T> X, View<T> Y) {
+    i64 tot = X.rows * X.cols;
+    if (tot == 0) return 0;
+    int blocks = (int)((tot + 255) / 256 < 8192 ? (tot + 255) / 256 : 8192);
+    k_copy2d<T><<<blocks, 256, 0, s>>>(X.p, X.rs, X.cs, X.rows, X.cols, Y.p, Y.rs, Y.cs);
+    DDLA_LAUNCHED();
+    return 0;
+}
+
+template <typename T, int NR>
+int chain(ddla_handle h, i64 n, int nblk, View<const T> A, bool lower, const T *inv, T *X, i64 ldx, int nr,
+          int *flags) {
+    k_trsv_chain<T, NR><<<nblk, CHAIN_THREADS, 0, h->stream>>>(n, nblk, A.p, A.rs, A.cs, lower ? 1 : 0, inv, X, ldx,
+                                                              nr, flags, flags + nblk, h->d_info + INFO_TIMEOUT);
     DDLA_LAUNCHED();
     return 0;
 }
@@ -106,6 +220,33 @@ int diag_solve(cudaStream_t s, int bs, View<const T> A11, View<T> B1, bool lower
 template <typename T>
 int gemm_any(ddla_handle h, int prec, i64 m, i64 n, i64 k, T alpha, View<const T> A, View<const T> B, T beta,
              View<T> C, int uplo);
+
+// Inverses of the diagonal blocks of tri(A) (n x n) into inv (ceil(n/TB) *
+// TB * TB elements).
+template <typename T>
+int tri_inverse(ddla_handle h, bool lower, bool unit, View<const T> A, i64 n, T *inv) {
+    int nblk = (int)((n + TB - 1) / TB);
+    k_tri_inv<T><<<nblk, TB, 0, h->stream>>>(A.p, A.rs, A.cs, n, lower ? 1 : 0, unit ? 1 : 0, inv);
+    DDLA_LAUNCHED();
+    return 0;
+}
+
+// Solve tri(A) X = X in place for X row-major (n x nr, leading dim ldx),
+// nr <= 16, with the precomputed diagonal-block inverses.
+template <typename T>
+int trsv_apply(ddla_handle h, bool lower, View<const T> A, i64 n, const T *inv, T *X, i64 ldx, int nr) {
+    int nblk = (int)((n + TB - 1) / TB);
+    int *flags;
+    DDLA_TRY(workspace(h, WS_MISC, sizeof(int) * (size_t)(nblk + 1), (void **)&flags));
+    DDLA_CUDA(cudaMemsetAsync(flags, 0, sizeof(int) * (size_t)(nblk + 1), h->stream));
+    if (nr <= 1) return chain<T, 1>(h, n, nblk, A, lower, inv, X, ldx, nr, flags);
+    if (nr <= 2) return chain<T, 2>(h, n, nblk, A, lower, inv, X, ldx, nr, flags);
+    if (nr <= 4) return chain<T, 4>(h, n, nblk, A, lower, inv, X, ldx, nr, flags);
+    if (nr <= 8) return chain<T, 8>(h, n, nblk, A, lower, inv, X, ldx, nr, flags);
+    if (nr <= 16) return chain<T, 16>(h, n, nblk, A, lower, inv, X, ldx, nr, flags);
+    set_error("trsv_apply: more than 16 right-hand sides");
+    return DDLA_ERR_UNSUPPORTED;
+}
 
 template <typename T>
 int trsm(ddla_handle h, int side, int uplo, int trans, int diag, i64 m, i64 n, T alpha, View<const T> A,
@@ -125,29 +266,40 @@ int trsm(ddla_handle h, int side, int uplo, int trans, int diag, i64 m, i64 n, T
         m = n;
         n = t;
     }
-    const bool unit = (diag == DDLA_UNIT_DIAG);
+    const bool lower = (uplo == DDLA_LOWER), unit = (diag == DDLA_UNIT_DIAG);
     const int prec = sizeof(T) == 8 ? DDLA_PREC_FP64 : DDLA_PREC_FP32;
-    if (uplo == DDLA_LOWER) {
-        for (i64 i0 = 0; i0 < m; i0 += TB) {
-            int bs = (int)(m - i0 < TB ? m - i0 : TB);
-            DDLA_TRY(diag_solve<T>(s, bs, A.sub(i0, bs, i0, bs), B.sub(i0, bs, 0, n), true, unit));
+    const int nblk = (int)((m + TB - 1) / TB);
+    T *inv, *tmp;
+    DDLA_TRY(workspace(h, WS_TRI, sizeof(T) * (size_t)nblk * TB * TB, (void **)&inv));
+    DDLA_TRY(tri_inverse<T>(h, lower, unit, A, m, inv));
+    if (n <= 16) {
+        // few right-hand sides: one chained kernel over a contiguous copy
+        DDLA_TRY(workspace(h, WS_TMP, sizeof(T) * (size_t)m * n, (void **)&tmp));
+        View<T> X{tmp, m, n, n, 1};
+        DDLA_TRY(copy2d<T>(s, View<const T>{B.p, m, n, B.rs, B.cs}, X));
+        DDLA_TRY(trsv_apply<T>(h, lower, A, m, inv, tmp, n, (int)n));
+        return copy2d<T>(s, View<const T>{tmp, m, n, n, 1}, B);
+    }
+    DDLA_TRY(workspace(h, WS_TMP, sizeof(T) * (size_t)TB * n, (void **)&tmp));
+    View<T> Tm{tmp, TB, n, n, 1};
+    for (int bi = 0; bi < nblk; bi++) {
+        const int b = lower ? bi : nblk - 1 - bi;
+        const i64 i0 = (i64)b * TB;
+        const int bs = (int)(m - i0 < TB ? m - i0 : TB);
+        View<T> B1 = B.sub(i0, bs, 0, n);
+        View<T> T1 = Tm.sub(0, bs, 0, n);
+        DDLA_TRY(copy2d<T>(s, View<const T>{B1.p, bs, n, B1.rs, B1.cs}, T1));
+        View<const T> IV{inv + (i64)b * TB * TB, bs, bs, TB, 1};
+        DDLA_TRY(gemm_any<T>(h, prec, bs, n, bs, T(1), IV, View<const T>{tmp, bs, n, n, 1}, T(0), B1, DDLA_DENSE));
+        View<const T> X1{B1.p, bs, n, B1.rs, B1.cs};
+        if (lower) {
             i64 r = m - i0 - bs;
-            if (r > 0) {
-                View<const T> B1{B.p + i0 * B.rs, bs, n, B.rs, B.cs};
-                DDLA_TRY(gemm_any<T>(h, prec, r, n, bs, T(-1), A.sub(i0 + bs, r, i0, bs), B1, T(1),
+            if (r > 0)
+                DDLA_TRY(gemm_any<T>(h, prec, r, n, bs, T(-1), A.sub(i0 + bs, r, i0, bs), X1, T(1),
                                      B.sub(i0 + bs, r, 0, n), DDLA_DENSE));
-            }
-        }
-    } else {
-        for (i64 i1 = m; i1 > 0; i1 -= TB) {
-            int bs = (int)(i1 < TB ? i1 : TB);
-            i64 i0 = i1 - bs;
-            DDLA_TRY(diag_solve<T>(s, bs, A.sub(i0, bs, i0, bs), B.sub(i0, bs, 0, n), false, unit));
-            if (i0 > 0) {
-                View<const T> B1{B.p + i0 * B.rs, bs, n, B.rs, B.cs};
-                DDLA_TRY(gemm_any<T>(h, prec, i0, n, bs, T(-1), A.sub(0, i0, i0, bs), B1, T(1), B.sub(0, i0, 0, n),
-                                     DDLA_DENSE));
-            }
+        } else if (i0 > 0) {
+            DDLA_TRY(gemm_any<T>(h, prec, i0, n, bs, T(-1), A.sub(0, i0, i0, bs), X1, T(1), B.sub(0, i0, 0, n),
+                                 DDLA_DENSE));
         }
     }
     return 0;
@@ -155,5 +307,9 @@ int trsm(ddla_handle h, int side, int uplo, int trans, int diag, i64 m, i64 n, T
 
 template int trsm<double>(ddla_handle, int, int, int, int, i64, i64, double, View<const double>, View<double>);
 template int trsm<float>(ddla_handle, int, int, int, int, i64, i64, float, View<const float>, View<float>);
+template int tri_inverse<double>(ddla_handle, bool, bool, View<const double>, i64, double *);
+template int tri_inverse<float>(ddla_handle, bool, bool, View<const float>, i64, float *);
+template int trsv_apply<double>(ddla_handle, bool, View<const double>, i64, const double *, double *, i64, int);
+template int trsv_apply<float>(ddla_handle, bool, View<const float>, i64, const float *, float *, i64, int);
 
 }  // namespace ddla
