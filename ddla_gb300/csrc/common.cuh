@@ -109,6 +109,9 @@ enum WsSlot {
 // allows beside its static shared memory; returns that limit in *avail.
 int max_dyn_smem(const void *fn, size_t optin, size_t *avail);
 
+// Tuning parameter lookup (tune.cu); dflt when the key was never set.
+int64_t tune_get(const char *key, int64_t dflt);
+
 // Returns a device buffer of at least `bytes` from slot `slot` (grown on demand).
 int workspace(ddla_handle h, int slot, size_t bytes, void **out);
 int pinned(ddla_handle h, size_t bytes, void **out);

@@ -59,13 +59,13 @@ __global__ void __launch_bounds__(DIAG_THREADS)
         T piv = S[i * LD + i];
         bool fail = false;
         if (kind == DK_CHOL) {
-            if (isfinite((double)piv) && piv <= T(0)) fail = true;
+            if (isfinite(piv) && piv <= T(0)) fail = true;
             else {
                 piv = sqrt(piv);
-                if (!isfinite((double)piv) || piv == T(0)) fail = true;
+                if (!isfinite(piv) || piv == T(0)) fail = true;
             }
         } else {
-            if (piv == T(0) || (kind == DK_LDLT && !isfinite((double)piv))) fail = true;
+            if (piv == T(0) || (kind == DK_LDLT && !isfinite(piv))) fail = true;
         }
         if (fail) {
             if (tid == 0) { atomicMin(info, (int)(row_base + i + 1)); s_fail = 1; }
@@ -114,7 +114,7 @@ __global__ void k_scale_by_diag(T *X, i64 rs, i64 cs, i64 m, int b, const T *D, 
         i64 r = e / b;
         int j = (int)(e % b);
         T d = D[j * drs + j * dcs];
-        if (d == T(0) || !isfinite((double)d)) {
+        if (d == T(0) || !isfinite(d)) {
             if (r == 0) atomicMin(info, (int)(row_base + j + 1));
             continue;
         }
@@ -173,6 +173,7 @@ int getrf(ddla_handle h, i64 n, View<T> A, int32_t *d_piv, int prec, int nb, int
     }
     int w = panel_width_for<T>(h, n);
     if (w == 0) w = 8;
+    if (nb <= 0) nb = (int)tune_get("lu.nb", 0);
     if (nb > 0 && nb < w) w = nb < 8 ? 8 : nb;
     for (i64 j0 = 0; j0 < n; j0 += w) {
         int b = (int)(n - j0 < w ? n - j0 : w);

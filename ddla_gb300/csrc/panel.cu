@@ -50,6 +50,23 @@ struct PanelArgs {
     int *touch_count, *touch_rows, *touch_src;
 };
 
+// Pivot search keys: |x| as an unsigned integer bit pattern plus one, NaN as
+// 0.  For non-negative IEEE values the integer order is the value order, so
+// "largest key, lowest row on ties" is bli_damaxv's first-max rule with NaN
+// below every number -- and it runs on the integer pipe (on GB300 even a
+// double compare goes through the 1/64-rate FP64 pipe).
+template <typename T> struct KeyT;
+template <> struct KeyT<float> { typedef unsigned int type; };
+template <> struct KeyT<double> { typedef unsigned long long type; };
+__device__ __forceinline__ unsigned int amax_key(float v) {
+    unsigned int u = __float_as_uint(v) & 0x7fffffffu;
+    return u > 0x7f800000u ? 0u : u + 1u;
+}
+__device__ __forceinline__ unsigned long long amax_key(double v) {
+    unsigned long long u = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+    return u > 0x7ff0000000000000ull ? 0ull : u + 1ull;
+}
+
 struct PanelSmem {
     size_t rows, origin, ucur, cand_val, cand_idx, cand_org, cand_rows, jrow, jorg, red, total;
 };
@@ -66,36 +83,36 @@ __host__ __device__ inline PanelSmem panel_smem_layout(int rows_per, int w) {
     L.rows = take(sizeof(T) * (size_t)rows_per * (w + 1));
     L.origin = take(sizeof(int) * (size_t)rows_per);
     L.ucur = take(sizeof(T) * w);
-    L.cand_val = take(sizeof(double) * 2 * PANEL_MAXCS);
+    L.cand_val = take(sizeof(typename KeyT<T>::type) * 2 * PANEL_MAXCS);
     L.cand_idx = take(sizeof(int) * 2 * PANEL_MAXCS);
     L.cand_org = take(sizeof(int) * 2 * PANEL_MAXCS);
     L.cand_rows = take(sizeof(T) * 2 * PANEL_MAXCS * w);
     L.jrow = take(sizeof(T) * 2 * w);
     L.jorg = take(sizeof(int) * 2);
-    L.red = take((sizeof(double) + sizeof(int)) * (PANEL_THREADS / 32) + 16);
+    L.red = take((sizeof(typename KeyT<T>::type) + sizeof(int)) * (PANEL_THREADS / 32) + 16);
     L.total = o;
     return L;
 }
 
-// Block-wide first-max reduction of (value, row) pairs; result in s_val/s_idx.
-__device__ __forceinline__ void block_argmax(double bv, int bi, double *red_v, int *red_i, double *s_val,
-                                             int *s_idx) {
+// Block-wide first-max reduction of (key, row) pairs; result in s_val/s_idx.
+template <typename K>
+__device__ __forceinline__ void block_argmax(K bv, int bi, K *red_v, int *red_i, K *s_val, int *s_idx) {
     constexpr int NW = PANEL_THREADS / 32;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
-        double ov = __shfl_down_sync(0xffffffffu, bv, off);
+        K ov = __shfl_down_sync(0xffffffffu, bv, off);
         int oi = __shfl_down_sync(0xffffffffu, bi, off);
         if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
     }
     if (lane == 0) { red_v[warp] = bv; red_i[warp] = bi; }
     __syncthreads();
     if (warp == 0) {
-        bv = lane < NW ? red_v[lane] : -1.0;
+        bv = lane < NW ? red_v[lane] : K(0);
         bi = lane < NW ? red_i[lane] : INT_MAX;
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) {
-            double ov = __shfl_down_sync(0xffffffffu, bv, off);
+            K ov = __shfl_down_sync(0xffffffffu, bv, off);
             int oi = __shfl_down_sync(0xffffffffu, bi, off);
             if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
         }
@@ -120,16 +137,17 @@ __global__ void __launch_bounds__(PANEL_THREADS) k_panel_lu(PanelArgs<T> a) {
     const PanelSmem L = panel_smem_layout<T>(rp, w);
     T *rows = (T *)(smem + L.rows);
     int *origin = (int *)(smem + L.origin);
+    typedef typename KeyT<T>::type K;
     T *ucur = (T *)(smem + L.ucur);
-    double *cand_val = (double *)(smem + L.cand_val);
+    K *cand_val = (K *)(smem + L.cand_val);
     int *cand_idx = (int *)(smem + L.cand_idx);
     int *cand_org = (int *)(smem + L.cand_org);
     T *cand_rows = (T *)(smem + L.cand_rows);
     T *jrow = (T *)(smem + L.jrow);
     int *jorg = (int *)(smem + L.jorg);
-    double *red_v = (double *)(smem + L.red);
+    K *red_v = (K *)(smem + L.red);
     int *red_i = (int *)(red_v + PANEL_THREADS / 32);
-    __shared__ double s_bval;
+    __shared__ K s_bval;
     __shared__ int s_best;
 
     const int base = rank * rp;
@@ -174,13 +192,13 @@ __global__ void __launch_bounds__(PANEL_THREADS) k_panel_lu(PanelArgs<T> a) {
 
     const int kmax = a.m < w ? a.m : w;
     {
-        double bv = -1.0;
+        K bv = 0;
         int bi = INT_MAX;
         for (int l = tid; l < nloc; l += PANEL_THREADS) {
-            double v = fabs((double)rows[l * WP]);
-            if (v > bv) { bv = v; bi = base + l; }
+            K v = amax_key(rows[l * WP]);
+            if (v > bv || bi == INT_MAX) { bv = v; bi = base + l; }
         }
-        block_argmax(bv, bi, red_v, red_i, &s_bval, &s_best);
+        block_argmax<K>(bv, bi, red_v, red_i, &s_bval, &s_best);
         push(0);
         cluster.sync();
     }
@@ -188,10 +206,10 @@ __global__ void __launch_bounds__(PANEL_THREADS) k_panel_lu(PanelArgs<T> a) {
     for (int j = 0; j < kmax; j++) {
         const int buf = j & 1;
         // winner (identical in every CTA, from local copies)
-        double wv = -1.0;
+        K wv = 0;
         int wi = INT_MAX, wr = 0;
         for (int r2 = 0; r2 < CS; r2++) {
-            double v = cand_val[buf * PANEL_MAXCS + r2];
+            K v = cand_val[buf * PANEL_MAXCS + r2];
             int i = cand_idx[buf * PANEL_MAXCS + r2];
             if (v > wv || (v == wv && i < wi)) { wv = v; wi = i; wr = r2; }
         }
@@ -223,7 +241,7 @@ __global__ void __launch_bounds__(PANEL_THREADS) k_panel_lu(PanelArgs<T> a) {
         int ls = j + 1 - base;
         if (ls < 0) ls = 0;
         // scale column j, update column j+1 and find its local first max
-        double bv = -1.0;
+        K bv = 0;
         int bi = INT_MAX;
         const T u1 = (j + 1 < w) ? ucur[j + 1] : T(0);
         for (int l = ls + tid; l < nloc; l += PANEL_THREADS) {
@@ -233,13 +251,13 @@ __global__ void __launch_bounds__(PANEL_THREADS) k_panel_lu(PanelArgs<T> a) {
             if (j + 1 < w) {
                 T v = fma(lv, -u1, row[j + 1]);
                 row[j + 1] = v;
-                double av = fabs((double)v);
-                if (av > bv) { bv = av; bi = base + l; }
+                K av = amax_key(v);
+                if (av > bv || bi == INT_MAX) { bv = av; bi = base + l; }
             }
         }
         int cb = INT_MAX;
         if (more) {
-            block_argmax(bv, bi, red_v, red_i, &s_bval, &s_best);
+            block_argmax<K>(bv, bi, red_v, red_i, &s_bval, &s_best);
             cb = s_best;
             // finish the rows that get published: the candidate and row j+1
             for (int c = j + 2 + tid; c < w; c += PANEL_THREADS) {
@@ -286,8 +304,9 @@ __global__ void __launch_bounds__(PANEL_THREADS) k_panel_lu(PanelArgs<T> a) {
 // factors the panel in global memory (same arithmetic, same pivot rule).
 template <typename T>
 __global__ void __launch_bounds__(1024) k_panel_lu_global(PanelArgs<T> a, int *origin) {
+    typedef typename KeyT<T>::type K;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    __shared__ double red_v[32];
+    __shared__ K red_v[32];
     __shared__ int red_i[32];
     __shared__ int s_p;
     for (int g = tid; g < a.m; g += 1024) origin[g] = g;
@@ -296,14 +315,14 @@ __global__ void __launch_bounds__(1024) k_panel_lu_global(PanelArgs<T> a, int *o
     auto at = [&](i64 r, i64 c) -> T & { return a.P[r * a.rs + c * a.cs]; };
     const int kmax = a.m < a.w ? a.m : a.w;
     for (int j = 0; j < kmax; j++) {
-        double bv = -1.0;
+        K bv = 0;
         int bi = INT_MAX;
         for (int g = j + tid; g < a.m; g += 1024) {
-            double v = fabs((double)at(g, j));
-            if (v > bv) { bv = v; bi = g; }
+            K v = amax_key(at(g, j));
+            if (v > bv || bi == INT_MAX) { bv = v; bi = g; }
         }
         for (int off = 16; off > 0; off >>= 1) {
-            double ov = __shfl_down_sync(0xffffffffu, bv, off);
+            K ov = __shfl_down_sync(0xffffffffu, bv, off);
             int oi = __shfl_down_sync(0xffffffffu, bi, off);
             if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
         }
@@ -480,6 +499,8 @@ int panel_lu(ddla_handle h, View<T> X, i64 pc, int w, int32_t *d_piv, i64 row_ba
     a.touch_src = tsrc;
     int cs = max_cluster<T>(h);
     if (cs <= 0) return cs < 0 ? cs : DDLA_ERR_UNSUPPORTED;
+    const int64_t want = tune_get("panel.cluster", 0);
+    if (want > 0 && want < cs) cs = (int)want;
     const size_t avail = panel_smem_avail<T>();
     // smallest cluster that holds the rows with at most 512 rows per CTA
     int use = 1;

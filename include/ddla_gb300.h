@@ -124,6 +124,13 @@ int ddla_measure_peaks(double *fp64_tflops, double *fp32_tflops);
 int ddla_timing_enable(int on);
 int ddla_timing_read(int cls, double *total_ms, int64_t *launches, double *flops, double *bytes);
 
+/* Tuning parameters (no DDLA counterpart; DDLA hard-codes its blocking in
+ * GEMMKernel, DDLA/Einsum/GEMMKernel.cs:11-21, and LU/Cholesky/LDLT.BlockSize).
+ * Keys: "lu.nb" (LU panel width), "panel.cluster" (CTAs per panel cluster),
+ * "chol.nb", "ldlt.nb", "batched.*".  value == INT64_MIN removes a key. */
+int ddla_tune_set(const char *key, int64_t value);
+int64_t ddla_tune_get(const char *key, int64_t dflt);
+
 /* ------------------------------------------------ BLIS-shaped level 3 (host) */
 
 /* C = beta*C + alpha*op(A)*op(B).  Replaces bli_dgemm,
