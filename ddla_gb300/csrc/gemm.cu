@@ -28,7 +28,7 @@ template <int BM, int BN, int WM, int WN>
 __global__ void __launch_bounds__(WM *WN * 32)
     k_gemm_f64(i64 m, i64 n, i64 k, double alpha, const double *__restrict__ A, i64 rsa, i64 csa,
                const double *__restrict__ B, i64 rsb, i64 csb, double beta, double *C, i64 rsc, i64 csc,
-               int uplo, i64 sa, i64 sb, i64 sc) {
+               int uplo, i64 sa, i64 sb, i64 sc, const i64 *__restrict__ boff) {
     constexpr int NT = WM * WN * 32;
     constexpr int TWM = BM / WM, TWN = BN / WN;  // warp tile
     constexpr int FM = TWM / 8, FN = TWN / 8;   // 8x8 fragments per warp
@@ -37,9 +37,15 @@ __global__ void __launch_bounds__(WM *WN * 32)
     __shared__ double Bs[BK64][BN + PAD];
 
     const i64 bz = blockIdx.z;
-    A += bz * sa;
-    B += bz * sb;
-    C += bz * sc;
+    if (boff) {
+        A += boff[3 * bz];
+        B += boff[3 * bz + 1];
+        C += boff[3 * bz + 2];
+    } else {
+        A += bz * sa;
+        B += bz * sb;
+        C += bz * sc;
+    }
     const i64 m0 = (i64)blockIdx.y * BM, n0 = (i64)blockIdx.x * BN;
     if (uplo == DDLA_LOWER && n0 > m0 + BM - 1) return;
     if (uplo == DDLA_UPPER && m0 > n0 + BN - 1) return;
@@ -108,15 +114,15 @@ __global__ void __launch_bounds__(WM *WN * 32)
 
 template <int BM, int BN, int WM, int WN>
 int launch_f64(cudaStream_t s, i64 m, i64 n, i64 k, double alpha, View<const double> A, View<const double> B,
-               double beta, View<double> C, int uplo, i64 batch, i64 sa, i64 sb, i64 sc) {
+               double beta, View<double> C, int uplo, i64 batch, i64 sa, i64 sb, i64 sc, const i64 *boff) {
     i64 gx = (n + BN - 1) / BN, gy = (m + BM - 1) / BM;
     if (gy > 65535) { set_error("gemm_f64: m too large for one launch"); return DDLA_ERR_UNSUPPORTED; }
     for (i64 b0 = 0; b0 < batch; b0 += 65535) {
         i64 nb = batch - b0 < 65535 ? batch - b0 : 65535;
         dim3 grid((unsigned)gx, (unsigned)gy, (unsigned)nb);
         k_gemm_f64<BM, BN, WM, WN><<<grid, WM * WN * 32, 0, s>>>(
-            m, n, k, alpha, A.p + b0 * sa, A.rs, A.cs, B.p + b0 * sb, B.rs, B.cs, beta, C.p + b0 * sc, C.rs, C.cs,
-            uplo, sa, sb, sc);
+            m, n, k, alpha, A.p + (boff ? 0 : b0 * sa), A.rs, A.cs, B.p + (boff ? 0 : b0 * sb), B.rs, B.cs, beta,
+            C.p + (boff ? 0 : b0 * sc), C.rs, C.cs, uplo, sa, sb, sc, boff ? boff + 3 * b0 : nullptr);
         DDLA_LAUNCHED();
     }
     return 0;
@@ -142,25 +148,38 @@ double balance(i64 tiles, int sms) {
 
 }  // namespace
 
-int gemm_f64(cudaStream_t s, i64 m, i64 n, i64 k, double alpha, View<const double> A, View<const double> B,
-             double beta, View<double> C, int uplo, i64 batch, i64 sa, i64 sb, i64 sc) {
+static int gemm_f64_any(cudaStream_t s, i64 m, i64 n, i64 k, double alpha, View<const double> A,
+                        View<const double> B, double beta, View<double> C, int uplo, i64 batch, i64 sa, i64 sb, i64 sc,
+                        const i64 *boff) {
     if (m <= 0 || n <= 0 || batch <= 0) return 0;
     if (k <= 0 || alpha == 0.0) {
         // C = beta*C on the requested part: reuse the kernel with k = 0.
         k = 0;
     }
     if (n <= 16)
-        return launch_f64<128, 16, 4, 1>(s, m, n, k, alpha, A, B, beta, C, uplo, batch, sa, sb, sc);
+        return launch_f64<128, 16, 4, 1>(s, m, n, k, alpha, A, B, beta, C, uplo, batch, sa, sb, sc, boff);
     int sms = sm_count();
     i64 t64 = ((m + 63) / 64) * ((n + 63) / 64) * batch;
     i64 t32 = ((m + 31) / 32) * ((n + 63) / 64) * batch;
     i64 t3232 = ((m + 31) / 32) * ((n + 31) / 32) * batch;
     double b64 = balance(t64, sms), b32 = balance(t32, sms), b3232 = balance(t3232, sms);
     if (t64 >= 8 * sms || (b64 >= 0.9 && b64 >= b32 - 0.02))
-        return launch_f64<64, 64, 2, 2>(s, m, n, k, alpha, A, B, beta, C, uplo, batch, sa, sb, sc);
+        return launch_f64<64, 64, 2, 2>(s, m, n, k, alpha, A, B, beta, C, uplo, batch, sa, sb, sc, boff);
     if (b32 >= 0.9 || b32 >= b3232 - 0.02)
-        return launch_f64<32, 64, 2, 2>(s, m, n, k, alpha, A, B, beta, C, uplo, batch, sa, sb, sc);
-    return launch_f64<32, 32, 2, 2>(s, m, n, k, alpha, A, B, beta, C, uplo, batch, sa, sb, sc);
+        return launch_f64<32, 64, 2, 2>(s, m, n, k, alpha, A, B, beta, C, uplo, batch, sa, sb, sc, boff);
+    return launch_f64<32, 32, 2, 2>(s, m, n, k, alpha, A, B, beta, C, uplo, batch, sa, sb, sc, boff);
+}
+
+int gemm_f64(cudaStream_t s, i64 m, i64 n, i64 k, double alpha, View<const double> A, View<const double> B,
+             double beta, View<double> C, int uplo, i64 batch, i64 sa, i64 sb, i64 sc) {
+    return gemm_f64_any(s, m, n, k, alpha, A, B, beta, C, uplo, batch, sa, sb, sc, nullptr);
+}
+
+// Batched GEMM whose problem z starts at element offsets d_offsets[3z..3z+2]
+// of A, B and C (batch index tables of an einsum).
+int gemm_f64_offsets(cudaStream_t s, i64 m, i64 n, i64 k, double alpha, View<const double> A,
+                     View<const double> B, double beta, View<double> C, i64 batch, const i64 *d_offsets) {
+    return gemm_f64_any(s, m, n, k, alpha, A, B, beta, C, DDLA_DENSE, batch, 0, 0, 0, d_offsets);
 }
 
 // ------------------------------------------------------------------ FP32

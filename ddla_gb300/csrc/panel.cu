@@ -205,13 +205,18 @@ __global__ void __launch_bounds__(PANEL_THREADS) k_panel_lu(PanelArgs<T> a) {
 
     for (int j = 0; j < kmax; j++) {
         const int buf = j & 1;
-        // winner (identical in every CTA, from local copies)
-        K wv = 0;
-        int wi = INT_MAX, wr = 0;
-        for (int r2 = 0; r2 < CS; r2++) {
-            K v = cand_val[buf * PANEL_MAXCS + r2];
-            int i = cand_idx[buf * PANEL_MAXCS + r2];
-            if (v > wv || (v == wv && i < wi)) { wv = v; wi = i; wr = r2; }
+        // winner (identical in every CTA, from local copies): lanes 0..CS-1
+        // each read one candidate, then a butterfly over the warp
+        const int lane = tid & 31;
+        K wv = lane < CS ? cand_val[buf * PANEL_MAXCS + lane] : K(0);
+        int wi = lane < CS ? cand_idx[buf * PANEL_MAXCS + lane] : INT_MAX;
+        int wr = lane;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            K ov = __shfl_xor_sync(0xffffffffu, wv, off);
+            int oi = __shfl_xor_sync(0xffffffffu, wi, off);
+            int orr = __shfl_xor_sync(0xffffffffu, wr, off);
+            if (oi != INT_MAX && (wi == INT_MAX || ov > wv || (ov == wv && oi < wi))) { wv = ov; wi = oi; wr = orr; }
         }
         const bool none = (wi == INT_MAX);
         const int p = none ? j : wi;
@@ -461,6 +466,7 @@ int max_cluster(ddla_handle h) {
 }
 template <typename T>
 size_t panel_smem_avail() { return g_panel_smem[sizeof(T) == 8 ? 0 : 1]; }
+
 }  // namespace
 
 // Widest panel (power of two, <= 64) whose m rows fit in one cluster.

@@ -12,4 +12,11 @@ int gemm_tc(ddla_handle h, int prec, i64 m, i64 n, i64 k, float alpha, View<cons
     return DDLA_ERR_UNSUPPORTED;
 }
 
+int gemm_ozaki(ddla_handle h, i64 m, i64 n, i64 k, double alpha, View<const double> A, View<const double> B,
+               double beta, View<double> C, int prec) {
+    (void)h; (void)m; (void)n; (void)k; (void)alpha; (void)A; (void)B; (void)beta; (void)C; (void)prec;
+    set_error("split-precision FP64 GEMM not available in this build");
+    return DDLA_ERR_UNSUPPORTED;
+}
+
 }  // namespace ddla

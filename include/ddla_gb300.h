@@ -67,7 +67,8 @@ enum {
     DDLA_PREC_FP64 = 0,      /* plain FP64 factorization (DMMA) */
     DDLA_PREC_FP32 = 1,      /* FP32 factorization, FP32 CUDA-core GEMM updates */
     DDLA_PREC_TF32X3 = 2,    /* FP32 factorization, 3xTF32 tcgen05 tensor-core GEMM updates */
-    DDLA_PREC_BF16X3 = 3     /* FP32 factorization, 3xBF16 tcgen05 tensor-core GEMM updates */
+    DDLA_PREC_BF16X3 = 3,    /* FP32 factorization, 3xBF16 tcgen05 tensor-core GEMM updates */
+    DDLA_PREC_OZAKI = 4      /* FP64-accurate GEMM from split BF16 tensor-core products */
 };
 
 /* Options of the factorization / mixed-solver calls.  Zero-initialised means
@@ -231,6 +232,42 @@ int ddla_dev_dgesv_mixed(ddla_handle h, ddla_dim_t n, ddla_dim_t nrhs, const dou
 int ddla_dev_dposv_mixed(ddla_handle h, int32_t uplo, ddla_dim_t n, ddla_dim_t nrhs, const double *a,
                          const double *b, double *x, const double *x_ref, const ddla_opts *opts,
                          ddla_solve_report *report);
+
+/* ------------------------------------------------ einsum (two operands) */
+
+/* One mode of a contraction: length and element strides in A, B, C (0 when
+ * the mode does not occur in that operand). */
+typedef struct ddla_contract_mode {
+    int64_t len, sa, sb, sc;
+} ddla_contract_mode;
+
+/* Lowered contraction: batch modes, then the M (A,C), N (B,C) and K (A,B)
+ * mode lists after folding; `swapped` means the operand roles were exchanged
+ * (A's strides are in `sb`).  Produced by ddla_contract_plan. */
+typedef struct ddla_contract_desc {
+    int32_t nbatch, nm, nn, nk, swapped, reserved;
+    ddla_contract_mode batch[48];
+    ddla_contract_mode m[16];
+    ddla_contract_mode n[16];
+    ddla_contract_mode k[16];
+} ddla_contract_desc;
+
+/* Index analysis of MArray.Contract(result, "ab,bc->ac", alpha, left, right)
+ * (DDLA/Einsum/MArray.Contract.cs:48-125; IndiceUtils.Diagonal / Divide / Fold,
+ * DDLA/Utilities/IndiceUtils.cs:18-245): ranks, lengths and element strides of
+ * the three tensors. */
+int ddla_contract_plan(const char *expr, int32_t rank_a, const int64_t *len_a, const int64_t *str_a, int32_t rank_b,
+                       const int64_t *len_b, const int64_t *str_b, int32_t rank_c, const int64_t *len_c,
+                       const int64_t *str_c, ddla_contract_desc *out);
+/* C += alpha * contraction(A, B) on device data (MArray.Contract's
+ * accumulating overload, MArray.Contract.cs:48-50).  precision: DDLA_PREC_FP64
+ * (DMMA) or DDLA_PREC_OZAKI (FP64-accurate split BF16 tensor-core products). */
+int ddla_dev_contract(ddla_handle h, const ddla_contract_desc *d, double alpha, const double *a, const double *b,
+                      double *c, int32_t precision);
+/* Same on host arrays: a/b/c point at the element with all indices 0 and
+ * na/nb/nc are the element counts spanned by each tensor. */
+int ddla_contract(const ddla_contract_desc *d, double alpha, const double *a, int64_t na, const double *b,
+                  int64_t nb, double *c, int64_t nc, int32_t precision);
 
 #ifdef __cplusplus
 }
