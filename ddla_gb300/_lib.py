@@ -133,7 +133,13 @@ def lib():
 
 
 def exported_names():
-    return list(_SIGS)
+    """C entry points bound by this package (here and in einsum.py / batched.py)."""
+    import re
+    names = set(_SIGS)
+    for mod in ("einsum.py", "batched.py"):
+        src = open(os.path.join(HERE, mod)).read()
+        names |= set(re.findall(r"L\.(ddla_[a-z0-9_]+)\.argtypes", src))
+    return sorted(names)
 
 
 def last_error():

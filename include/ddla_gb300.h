@@ -233,6 +233,28 @@ int ddla_dev_dposv_mixed(ddla_handle h, int32_t uplo, ddla_dim_t n, ddla_dim_t n
                          const double *b, double *x, const double *x_ref, const ddla_opts *opts,
                          ddla_solve_report *report);
 
+/* ------------------------------------------------ batched small factorizations */
+
+/* Plan for `count` square row-major matrices of uneven size (1 <= n[i] <= 1024,
+ * host array), each factored and solved with one right-hand side in ONE
+ * persistent kernel launch captured into a CUDA graph (no DDLA counterpart:
+ * DDLA factors one matrix per LU / Cholesky object).  kind[i]: 0 = LU with
+ * partial pivoting (LU.PLUDecompose), 1 = LU without pivoting
+ * (LU.LUDecompose), 2 = lower Cholesky (Cholesky.CholDecompose).
+ * Device buffers, packed in item order: d_a holds the matrices back to back
+ * (sum n^2 doubles; plain mode overwrites them with the factors), d_b / d_x /
+ * d_piv the vectors (sum n each), d_info / d_iters one int per item (failing
+ * pivot or 0; refinement steps or -1 when not converged).  mixed != 0 factors
+ * in FP32 and refines in FP64 to opts->tol (default 1e-14). */
+int ddla_batched_plan_create(ddla_handle h, int64_t count, const int32_t *n, const int32_t *kind, int32_t mixed,
+                             double *d_a, const double *d_b, double *d_x, int32_t *d_piv, int32_t *d_info,
+                             int32_t *d_iters, const ddla_opts *opts, void **plan);
+/* Replay the plan's graph on the handle's stream (asynchronous). */
+int ddla_batched_plan_exec(void *plan);
+/* Algorithmic flops of one execution, persistent grid size, shared memory. */
+int ddla_batched_plan_info(void *plan, double *flops, int32_t *grid, int64_t *smem_bytes);
+int ddla_batched_plan_destroy(void *plan);
+
 /* ------------------------------------------------ einsum (two operands) */
 
 /* One mode of a contraction: length and element strides in A, B, C (0 when
