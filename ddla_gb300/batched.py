@@ -78,6 +78,8 @@ class BatchedSolver:
             self.a.copy_(self.a0)
 
     def run(self):
+        # inputs were written on torch's stream; the plan runs on the handle's
+        self.torch.cuda.current_stream().synchronize()
         check(_declare().ddla_batched_plan_exec(self.plan), "batched_plan_exec")
 
     def info_tuple(self):
@@ -86,6 +88,7 @@ class BatchedSolver:
         return fl.value, grid.value, sm.value
 
     def results(self):
+        self.h.sync()
         a = self.a.cpu().numpy()
         x = self.x.cpu().numpy()
         piv = self.piv.cpu().numpy()
