@@ -69,6 +69,8 @@ _SIGS = {
     "ddla_handle_destroy": (C.c_int, [_h]),
     "ddla_handle_sync": (C.c_int, [_h]),
     "ddla_measure_peaks": (C.c_int, [C.POINTER(_d), C.POINTER(_d)]),
+    "ddla_dev_sgemm_tc": (C.c_int, [_h, _i32, _i64, _i64, _i64, C.c_float, _pd, _i64, _i64, _pd, _i64, _i64,
+                                    C.c_float, _pd, _i64, _i64]),
     "ddla_tune_set": (C.c_int, [C.c_char_p, _i64]),
     "ddla_tune_get": (_i64, [C.c_char_p, _i64]),
     "ddla_timing_enable": (C.c_int, [C.c_int]),

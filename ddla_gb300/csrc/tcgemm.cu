@@ -1,15 +1,267 @@
-// Tensor-core (tcgen05) FP32-emulating GEMMs for the mixed-precision
-// factorizations: 3xTF32 and 3xBF16 split products with FP32 accumulation in
-// TMEM.
+// Tensor-core (tcgen05) GEMMs with FP32 accumulation in TMEM.
+//
+// gemm_tc: C = alpha * A * B + beta * C for FP32 operands with FP32-level
+// accuracy from split products on the 5th-generation tensor cores:
+//   3xTF32  x = hi + lo with hi = tf32(x), lo = tf32(x - hi);
+//           A*B ~ hi*hi + hi*lo + lo*hi   (kind::tf32)
+// The split is done on the fly while the operand tiles are staged into shared
+// memory in the canonical K-major core-matrix layout (8 rows x 16 bytes per
+// core matrix, no swizzle).  One elected thread issues the tcgen05.mma chain
+// for a 128 x 64 output tile; the FP32 accumulator lives in TMEM (64 columns)
+// and is read back with tcgen05.ld for the alpha/beta epilogue.  Every
+// mbarrier wait is bounded: on timeout the kernel records the error, waits
+// (bounded) for its own MMAs and frees its TMEM.
+//
+// gemm_ozaki: FP64 GEMM with FP64-level accuracy from BF16 slice products on
+// the same kind of kernel (see the comment at its definition).
+#include <cstdint>
+
 #include "common.cuh"
 
 namespace ddla {
+namespace {
+
+constexpr int TM = 128;          // tile rows (TMEM lanes)
+constexpr int TN = 64;           // tile columns (TMEM columns)
+constexpr int TK = 64;           // K elements staged per chunk
+constexpr int TC_THREADS = 256;
+constexpr long long TC_SPIN = 1LL << 24;
+
+// bytes of one staged operand tile (rows x TK fp32)
+constexpr int A_BYTES = TM * TK * 4;
+constexpr int B_BYTES = TN * TK * 4;
+constexpr int LBO = 128;                 // next 16-byte K chunk: next core matrix
+constexpr int SBO = (TK / 4) * 128;      // next 8-row group
+
+__device__ __forceinline__ unsigned su32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+// byte offset of element (r, k) of a K-major fp32 tile in core-matrix layout
+__device__ __forceinline__ int cm_off(int r, int k) {
+    return (r >> 3) * SBO + (k >> 2) * LBO + (r & 7) * 16 + (k & 3) * 4;
+}
+
+__device__ __forceinline__ float tf32_round(float x) {
+    unsigned u = __float_as_uint(x);
+    if ((u & 0x7f800000u) == 0x7f800000u) return x;   // inf / nan unchanged
+    u = (u + 0x1000u) & 0xffffe000u;
+    return __uint_as_float(u);
+}
+
+// smem matrix descriptor: start, LBO, SBO (16-byte units), version 1, no swizzle
+__device__ __forceinline__ uint64_t sdesc(unsigned addr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((addr & 0x3ffff) >> 4);
+    d |= (uint64_t)(LBO >> 4) << 16;
+    d |= (uint64_t)(SBO >> 4) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+
+// instruction descriptor: D f32, A/B format `fmt` (tf32 = 2, bf16 = 1), both
+// K-major, N = TN, M = TM
+__host__ __device__ constexpr uint32_t idesc(uint32_t fmt) {
+    return (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(TN >> 3) << 17) | ((uint32_t)(TM >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_tf32(unsigned tmem, uint64_t a, uint64_t b, uint32_t id, int acc) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+        "l"(a), "l"(b), "r"(id), "r"(acc)
+        : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(unsigned mbar, unsigned phase) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(mbar), "r"(phase)
+        : "memory");
+    return ok != 0;
+}
+
+struct TcArgs {
+    int64_t m, n, k;
+    float alpha, beta;
+    const float *A;
+    int64_t rsa, csa;
+    const float *B;
+    int64_t rsb, csb;
+    float *C;
+    int64_t rsc, csc;
+    int uplo;
+    int *err;
+};
+
+__global__ void __launch_bounds__(TC_THREADS) k_tc_tf32x3(TcArgs g) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned char *Ah = smem, *Al = smem + A_BYTES, *Bh = smem + 2 * A_BYTES, *Bl = Bh + B_BYTES;
+    __shared__ __align__(8) unsigned long long mbar;
+    __shared__ unsigned tmem_slot;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int64_t m0 = (int64_t)blockIdx.y * TM, n0 = (int64_t)blockIdx.x * TN;
+    if (g.uplo == DDLA_LOWER && n0 > m0 + TM - 1) return;
+    if (g.uplo == DDLA_UPPER && m0 > n0 + TN - 1) return;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(&tmem_slot)),
+                     "r"(TN)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&mbar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const unsigned tmem = tmem_slot;
+    const uint32_t id = idesc(2);
+    unsigned phase = 0;
+    bool failed = false;
+    const bool a_vec = (g.csa == 1) && ((g.rsa & 3) == 0) && ((((uintptr_t)g.A) & 15) == 0);
+
+    for (int64_t k0 = 0; k0 < g.k; k0 += TK) {
+        // stage A (TM x TK): 16-byte chunks of a row
+        for (int e = tid; e < TM * (TK / 4); e += TC_THREADS) {
+            const int r = e / (TK / 4), c = e % (TK / 4);
+            const int64_t gr = m0 + r, gk = k0 + 4 * c;
+            float v[4];
+            if (a_vec && gr < g.m && gk + 3 < g.k) {
+                float4 q = *reinterpret_cast<const float4 *>(g.A + gr * g.rsa + gk);
+                v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+            } else {
+#pragma unroll
+                for (int t = 0; t < 4; t++)
+                    v[t] = (gr < g.m && gk + t < g.k) ? g.A[gr * g.rsa + (gk + t) * g.csa] : 0.f;
+            }
+            float4 hi, lo;
+            float *ph = &hi.x, *pl = &lo.x;
+#pragma unroll
+            for (int t = 0; t < 4; t++) {
+                ph[t] = tf32_round(v[t]);
+                pl[t] = tf32_round(v[t] - ph[t]);
+            }
+            *reinterpret_cast<float4 *>(Ah + cm_off(r, 4 * c)) = hi;
+            *reinterpret_cast<float4 *>(Al + cm_off(r, 4 * c)) = lo;
+        }
+        // stage B as N-rows x K (B is K x N in memory): element (n, k) = B[k][n]
+        for (int e = tid; e < TN * TK; e += TC_THREADS) {
+            const int kk = e / TN, nn = e % TN;
+            const int64_t gk = k0 + kk, gn = n0 + nn;
+            const float v = (gk < g.k && gn < g.n) ? g.B[gk * g.rsb + gn * g.csb] : 0.f;
+            const float h = tf32_round(v);
+            *reinterpret_cast<float *>(Bh + cm_off(nn, kk)) = h;
+            *reinterpret_cast<float *>(Bl + cm_off(nn, kk)) = tf32_round(v - h);
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            for (int s = 0; s < TK / 8; s++) {
+                const unsigned off_a = s * 2 * LBO, off_b = s * 2 * LBO;
+                const uint64_t ah = sdesc(su32(Ah) + off_a), al = sdesc(su32(Al) + off_a);
+                const uint64_t bh = sdesc(su32(Bh) + off_b), bl = sdesc(su32(Bl) + off_b);
+                const int first = (k0 == 0 && s == 0) ? 0 : 1;
+                mma_tf32(tmem, ah, bh, id, first);
+                mma_tf32(tmem, ah, bl, id, 1);
+                mma_tf32(tmem, al, bh, id, 1);
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             su32(&mbar))
+                         : "memory");
+        }
+        // wait for the MMAs (bounded) before the tiles are overwritten / read
+        bool ok = false;
+        for (long long it = 0; it < TC_SPIN; it++)
+            if (mbar_try(su32(&mbar), phase)) { ok = true; break; }
+        phase ^= 1u;
+        if (__syncthreads_or(!ok)) {   // uniform across the CTA
+            failed = true;
+            if (tid == 0) atomicExch(g.err, 1);
+            break;
+        }
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (!failed && g.k > 0) {
+        // epilogue: warp w reads TMEM lanes 32*(w%4).., columns 32*(w/4)..
+        const int q = warp & 3, h = warp >> 2;
+        uint32_t d[32];
+        const unsigned taddr = tmem + ((unsigned)(32 * q) << 16) + (unsigned)(32 * h);
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+            "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+            : "=r"(d[0]), "=r"(d[1]), "=r"(d[2]), "=r"(d[3]), "=r"(d[4]), "=r"(d[5]), "=r"(d[6]), "=r"(d[7]),
+              "=r"(d[8]), "=r"(d[9]), "=r"(d[10]), "=r"(d[11]), "=r"(d[12]), "=r"(d[13]), "=r"(d[14]),
+              "=r"(d[15]), "=r"(d[16]), "=r"(d[17]), "=r"(d[18]), "=r"(d[19]), "=r"(d[20]), "=r"(d[21]),
+              "=r"(d[22]), "=r"(d[23]), "=r"(d[24]), "=r"(d[25]), "=r"(d[26]), "=r"(d[27]), "=r"(d[28]),
+              "=r"(d[29]), "=r"(d[30]), "=r"(d[31])
+            : "r"(taddr)
+            : "memory");
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        const int64_t gr = m0 + 32 * q + lane;
+        if (gr < g.m) {
+#pragma unroll
+            for (int j = 0; j < 32; j++) {
+                const int64_t gc = n0 + 32 * h + j;
+                if (gc >= g.n) break;
+                if (g.uplo == DDLA_LOWER && gc > gr) continue;
+                if (g.uplo == DDLA_UPPER && gc < gr) continue;
+                float *cp = g.C + gr * g.rsc + gc * g.csc;
+                const float v = g.alpha * __uint_as_float(d[j]);
+                *cp = (g.beta == 0.f) ? v : fmaf(g.beta, *cp, v);
+            }
+        }
+    } else if (g.k <= 0) {
+        // C = beta * C
+        for (int e = tid; e < TM * TN; e += TC_THREADS) {
+            const int64_t gr = m0 + e / TN, gc = n0 + e % TN;
+            if (gr >= g.m || gc >= g.n) continue;
+            if (g.uplo == DDLA_LOWER && gc > gr) continue;
+            if (g.uplo == DDLA_UPPER && gc < gr) continue;
+            float *cp = g.C + gr * g.rsc + gc * g.csc;
+            *cp = (g.beta == 0.f) ? 0.f : g.beta * *cp;
+        }
+    }
+    if (failed) {
+        // our MMAs may still run: wait (bounded) before giving TMEM back
+        for (long long it = 0; it < TC_SPIN; it++)
+            if (mbar_try(su32(&mbar), phase ^ 1u)) break;
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TN) : "memory");
+    }
+}
+
+constexpr size_t TC_SMEM = 2 * A_BYTES + 2 * B_BYTES;
+
+}  // namespace
 
 int gemm_tc(ddla_handle h, int prec, i64 m, i64 n, i64 k, float alpha, View<const float> A, View<const float> B,
             float beta, View<float> C, int uplo) {
-    (void)h; (void)prec; (void)m; (void)n; (void)k; (void)alpha; (void)A; (void)B; (void)beta; (void)C; (void)uplo;
-    set_error("tensor-core split-precision GEMM not available in this build");
-    return DDLA_ERR_UNSUPPORTED;
+    if (m <= 0 || n <= 0) return 0;
+    if (prec != DDLA_PREC_TF32X3) {
+        set_error("gemm_tc: only the 3xTF32 split is implemented");
+        return DDLA_ERR_UNSUPPORTED;
+    }
+    static size_t avail = 0;
+    if (!avail) DDLA_TRY(max_dyn_smem((const void *)k_tc_tf32x3, h->smem_optin, &avail));
+    if (TC_SMEM > avail) {
+        set_error("gemm_tc: not enough shared memory");
+        return DDLA_ERR_UNSUPPORTED;
+    }
+    i64 gx = (n + TN - 1) / TN, gy = (m + TM - 1) / TM;
+    if (gy > 65535) { set_error("gemm_tc: m too large"); return DDLA_ERR_UNSUPPORTED; }
+    TcArgs a{m, n, alpha == 0.f ? 0 : k, alpha, beta, A.p, A.rs, A.cs, B.p, B.rs, B.cs, C.p, C.rs, C.cs, uplo,
+             h->d_info + INFO_TIMEOUT};
+    k_tc_tf32x3<<<dim3((unsigned)gx, (unsigned)gy), TC_THREADS, TC_SMEM, h->stream>>>(a);
+    DDLA_LAUNCHED();
+    return 0;
 }
 
 int gemm_ozaki(ddla_handle h, i64 m, i64 n, i64 k, double alpha, View<const double> A, View<const double> B,
@@ -20,3 +272,21 @@ int gemm_ozaki(ddla_handle h, i64 m, i64 n, i64 k, double alpha, View<const doub
 }
 
 }  // namespace ddla
+
+using namespace ddla;
+
+// FP32 GEMM through the tensor-core path on device data (testing and tuning
+// entry point; the mixed factorizations call the same kernel internally).
+extern "C" int ddla_dev_sgemm_tc(ddla_handle h, int32_t precision, int64_t m, int64_t n, int64_t k, float alpha,
+                                 const float *a, int64_t rsa, int64_t csa, const float *b, int64_t rsb, int64_t csb,
+                                 float beta, float *c, int64_t rsc, int64_t csc) {
+    if (!h) return -1;
+    if (m < 0) return -3;
+    if (n < 0) return -4;
+    if (k < 0) return -5;
+    if (precision == DDLA_PREC_FP32)
+        return gemm_f32(h->stream, m, n, k, alpha, View<const float>{a, m, k, rsa, csa},
+                        View<const float>{b, k, n, rsb, csb}, beta, View<float>{c, m, n, rsc, csc});
+    return gemm_tc(h, precision, m, n, k, alpha, View<const float>{a, m, k, rsa, csa},
+                   View<const float>{b, k, n, rsb, csb}, beta, View<float>{c, m, n, rsc, csc}, DDLA_DENSE);
+}

@@ -233,6 +233,14 @@ int ddla_dev_dposv_mixed(ddla_handle h, int32_t uplo, ddla_dim_t n, ddla_dim_t n
                          const double *b, double *x, const double *x_ref, const ddla_opts *opts,
                          ddla_solve_report *report);
 
+/* FP32 GEMM C = alpha*A*B + beta*C on device data in the precision the mixed
+ * factorizations use for their trailing updates: DDLA_PREC_FP32 (CUDA-core
+ * FFMA) or DDLA_PREC_TF32X3 (tcgen05 tensor cores, 3xTF32 split products,
+ * FP32 accumulation in TMEM).  No DDLA counterpart (DDLA is FP64 only). */
+int ddla_dev_sgemm_tc(ddla_handle h, int32_t precision, int64_t m, int64_t n, int64_t k, float alpha, const float *a,
+                      int64_t rsa, int64_t csa, const float *b, int64_t rsb, int64_t csb, float beta, float *c,
+                      int64_t rsc, int64_t csc);
+
 /* ------------------------------------------------ batched small factorizations */
 
 /* Plan for `count` square row-major matrices of uneven size (1 <= n[i] <= 1024,

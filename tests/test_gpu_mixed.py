@@ -8,8 +8,9 @@ from helpers import berr, rng, spd
 pytestmark = pytest.mark.gpu
 
 
+@pytest.mark.parametrize("prec", ["fp32", "tf32x3"])
 @pytest.mark.parametrize("n,nrhs", [(100, 1), (1024, 1), (2048, 4), (3000, 16)])
-def test_mixed_lu_reaches_fp64(ddla, orc, n, nrhs):
+def test_mixed_lu_reaches_fp64(ddla, orc, n, nrhs, prec):
     r = rng(n)
     A = r.standard_normal((n, n))
     B = r.standard_normal((n, nrhs))
@@ -17,19 +18,20 @@ def test_mixed_lu_reaches_fp64(ddla, orc, n, nrhs):
     info, piv = orc.dgetrf(F)
     Xo = B.copy()
     orc.dgetrs(F, piv, Xo)
-    X, rep = ddla.solve_mixed(A, B, precision=ddla.PREC_FP32, x_ref=Xo)
+    X, rep = ddla.solve_mixed(A, B, precision=getattr(ddla, "PREC_" + prec.upper()), x_ref=Xo)
     assert rep["converged"] == 1
     assert rep["backward_error"] <= 1e-14
     assert berr(A, X, B) <= 1e-14
     assert rep["forward_error"] <= 1e-10
 
 
+@pytest.mark.parametrize("prec", ["fp32", "tf32x3"])
 @pytest.mark.parametrize("n,nrhs", [(500, 16), (2048, 16)])
-def test_mixed_cholesky(ddla, orc, n, nrhs):
+def test_mixed_cholesky(ddla, orc, n, nrhs, prec):
     r = rng(n + 1)
     A = spd(r, n)
     B = r.standard_normal((n, nrhs))
-    X, rep = ddla.solve_mixed(A, B, spd=True, precision=ddla.PREC_FP32)
+    X, rep = ddla.solve_mixed(A, B, spd=True, precision=getattr(ddla, "PREC_" + prec.upper()))
     assert rep["converged"] == 1 and rep["backward_error"] <= 1e-14
     assert berr(A, X, B) <= 1e-14
 

@@ -1,0 +1,48 @@
+"""GPU: the tcgen05 3xTF32 GEMM (trailing updates of the mixed factorizations)
+against an FP64 reference.  3xTF32 products carry ~2^-21 relative error per
+term; the bar is max|C - C_ref| <= 2e-5 * (|alpha| |A| |B| + |beta| |C|)
+elementwise-normalised, i.e. FP32-level accuracy."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [(128, 64, 64), (300, 200, 64), (129, 65, 8), (257, 130, 100), (64, 64, 1), (1000, 1000, 64),
+          (512, 768, 256), (33, 17, 64)]
+
+
+def _run(ddla, prec, m, n, k, alpha, beta, seed):
+    import torch
+    from ddla_gb300 import device
+    g = torch.Generator().manual_seed(seed)
+    A = torch.rand(m, k, generator=g, dtype=torch.float64) * 2 - 1
+    B = torch.rand(k, n, generator=g, dtype=torch.float64) * 2 - 1
+    Cm = torch.rand(m, n, generator=g, dtype=torch.float64) * 2 - 1
+    ref = (alpha * A.numpy() @ B.numpy() + beta * Cm.numpy())
+    scale = abs(alpha) * (np.abs(A.numpy()) @ np.abs(B.numpy())) + abs(beta) * np.abs(Cm.numpy())
+    a, b, c = A.float().cuda(), B.float().cuda(), Cm.float().cuda()
+    h = device.Handle(torch.cuda.current_stream())
+    rc = ddla.lib().ddla_dev_sgemm_tc(h.h, prec, m, n, k, alpha, C.c_void_p(a.data_ptr()), k, 1,
+                                      C.c_void_p(b.data_ptr()), n, 1, beta, C.c_void_p(c.data_ptr()), n, 1)
+    ddla._lib.check(rc, "sgemm_tc")
+    h.sync()
+    out = c.double().cpu().numpy()
+    h.close()
+    return np.max(np.abs(out - ref) / scale)
+
+
+@pytest.mark.parametrize("m,n,k", SHAPES)
+def test_tf32x3_accuracy(ddla, m, n, k):
+    err = _run(ddla, ddla.PREC_TF32X3, m, n, k, -1.0, 1.0, m * 7 + n)
+    assert err <= 2e-5, err
+
+
+def test_tf32x3_alpha_beta(ddla):
+    assert _run(ddla, ddla.PREC_TF32X3, 200, 100, 64, 0.5, 0.0, 3) <= 2e-5
+    assert _run(ddla, ddla.PREC_TF32X3, 200, 100, 64, 2.0, -0.5, 4) <= 2e-5
+
+
+def test_fp32_reference_path(ddla):
+    assert _run(ddla, ddla.PREC_FP32, 300, 200, 64, -1.0, 1.0, 5) <= 2e-6
