@@ -121,6 +121,12 @@ static void handle_free(ddla_handle h) {
     if (h->d_info) cudaFree(h->d_info);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->side) {
+        cudaStreamSynchronize(h->side);
+        cudaStreamDestroy(h->side);
+    }
+    if (h->ev_ready) cudaEventDestroy(h->ev_ready);
+    if (h->ev_panel) cudaEventDestroy(h->ev_panel);
     if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
     delete h;
 }

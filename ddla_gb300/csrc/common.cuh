@@ -88,6 +88,10 @@ struct ddla_handle_s {
     size_t pinned_bytes = 0;
     int *d_info = nullptr;       // device status words (info, timeout flags)
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // look-ahead: high-priority side stream for the next panel, and the
+    // events ordering it against the main stream (created on first use)
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_ready = nullptr, ev_panel = nullptr;
 };
 
 namespace ddla {

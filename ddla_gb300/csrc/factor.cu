@@ -20,7 +20,9 @@ namespace ddla {
 template <typename T>
 int panel_width_for(ddla_handle h, i64 m);
 template <typename T>
-int panel_lu(ddla_handle h, View<T> X, i64 pc, int w, int32_t *d_piv, i64 row_base, int *d_info, int *perm);
+int panel_factor(ddla_handle h, cudaStream_t s, View<T> X, i64 pc, int w, int32_t *d_piv, i64 row_base, int *d_info);
+template <typename T>
+int panel_swap_rest(ddla_handle h, View<T> X, i64 pc, int w, int *perm);
 template <typename T>
 int apply_perm(ddla_handle h, View<T> B, const int32_t *d_piv, i64 n, bool forward);
 
@@ -167,34 +169,75 @@ template <typename T>
 int getrf(ddla_handle h, i64 n, View<T> A, int32_t *d_piv, int prec, int nb, int *d_perm) {
     if (n == 0) return 0;
     prec = prec_of<T>(prec);
+    cudaStream_t s = h->stream;
     if (d_perm) {
-        k_iota<<<grid_for(n), 256, 0, h->stream>>>(d_perm, n);
+        k_iota<<<grid_for(n), 256, 0, s>>>(d_perm, n);
         DDLA_LAUNCHED();
     }
     int w = panel_width_for<T>(h, n);
     if (w == 0) w = 8;
     if (nb <= 0) nb = (int)tune_get("lu.nb", 0);
     if (nb > 0 && nb < w) w = nb < 8 ? 8 : nb;
+    // Look-ahead of depth one: after panel k's interchanges and U12 solve, the
+    // columns of panel k+1 are updated first and panel k+1 is factored on a
+    // high-priority side stream while the main stream updates the rest of the
+    // trailing matrix.  The panel touches only its own columns; its row
+    // interchanges on the other columns are applied on the main stream after
+    // the big update (panel_swap_rest), so the two streams never overlap in
+    // memory.
+    const bool ahead = tune_get("lu.lookahead", 1) != 0 && n > 2 * (i64)w;
+    if (ahead && !h->side) {
+        int lo = 0, hi = 0;
+        DDLA_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+        DDLA_CUDA(cudaStreamCreateWithPriority(&h->side, cudaStreamNonBlocking, hi));
+        DDLA_CUDA(cudaEventCreateWithFlags(&h->ev_ready, cudaEventDisableTiming));
+        DDLA_CUDA(cudaEventCreateWithFlags(&h->ev_panel, cudaEventDisableTiming));
+    }
+    auto panel = [&](cudaStream_t st, i64 j0, int b) -> int {
+        Timed t(st, TC_PANEL, 2.0 * b * b * ((n - j0) - b / 3.0), 2.0 * sizeof(T) * (n - j0) * (double)b);
+        return panel_factor<T>(h, st, A.sub(j0, n - j0, 0, n), j0, b, d_piv + j0, j0, h->d_info + INFO_PIVOT);
+    };
+    DDLA_TRY(panel(s, 0, (int)(n < w ? n : w)));
     for (i64 j0 = 0; j0 < n; j0 += w) {
-        int b = (int)(n - j0 < w ? n - j0 : w);
-        View<T> rowsX = A.sub(j0, n - j0, 0, n);
+        const int b = (int)(n - j0 < w ? n - j0 : w);
+        DDLA_TRY(panel_swap_rest<T>(h, A.sub(j0, n - j0, 0, n), j0, b, d_perm ? d_perm + j0 : nullptr));
+        const i64 r = n - j0 - b;
+        if (r <= 0) break;
+        View<const T> A11{A.p + j0 * A.rs + j0 * A.cs, b, b, A.rs, A.cs};
+        View<T> A12 = A.sub(j0, b, j0 + b, r);
         {
-            Timed t(h->stream, TC_PANEL, 2.0 * b * b * ((n - j0) - b / 3.0), 2.0 * sizeof(T) * (n - j0) * (double)n);
-            DDLA_TRY(panel_lu<T>(h, rowsX, j0, b, d_piv + j0, j0, h->d_info + INFO_PIVOT,
-                                 d_perm ? d_perm + j0 : nullptr));
+            Timed t(s, TC_TRSM, (double)b * b * r, sizeof(T) * (2.0 * b * r + b * b));
+            DDLA_TRY(trsm<T>(h, DDLA_LEFT, DDLA_LOWER, DDLA_NO_TRANSPOSE, DDLA_UNIT_DIAG, b, r, T(1), A11, A12));
         }
-        i64 r = n - j0 - b;
-        if (r > 0) {
-            View<const T> A11{A.p + j0 * A.rs + j0 * A.cs, b, b, A.rs, A.cs};
-            View<T> A12 = A.sub(j0, b, j0 + b, r);
+        View<const T> A21{A.p + (j0 + b) * A.rs + j0 * A.cs, r, b, A.rs, A.cs};
+        const i64 j1 = j0 + b;
+        const int b1 = (int)(r < w ? r : w);
+        if (ahead) {
+            // next panel's columns first
             {
-                Timed t(h->stream, TC_TRSM, (double)b * b * r, sizeof(T) * (2.0 * b * r + b * b));
-                DDLA_TRY(trsm<T>(h, DDLA_LEFT, DDLA_LOWER, DDLA_NO_TRANSPOSE, DDLA_UNIT_DIAG, b, r, T(1), A11, A12));
+                Timed t(s, TC_UPDATE, 2.0 * r * b1 * b, sizeof(T) * (2.0 * r * b1 + r * b + b * b1));
+                DDLA_TRY(gemm_any<T>(h, prec, r, b1, b, T(-1), A21, View<const T>{A12.p, b, b1, A12.rs, A12.cs}, T(1),
+                                     A.sub(j1, r, j1, b1)));
             }
-            View<const T> A21{A.p + (j0 + b) * A.rs + j0 * A.cs, r, b, A.rs, A.cs};
-            View<const T> cA12{A12.p, b, r, A12.rs, A12.cs};
-            Timed t(h->stream, TC_UPDATE, 2.0 * r * r * b, sizeof(T) * (2.0 * r * r + 2.0 * r * b));
-            DDLA_TRY(gemm_any<T>(h, prec, r, r, b, T(-1), A21, cA12, T(1), A.sub(j0 + b, r, j0 + b, r)));
+            DDLA_CUDA(cudaEventRecord(h->ev_ready, s));
+            DDLA_CUDA(cudaStreamWaitEvent(h->side, h->ev_ready, 0));
+            DDLA_TRY(panel(h->side, j1, b1));
+            DDLA_CUDA(cudaEventRecord(h->ev_panel, h->side));
+            const i64 rest = r - b1;
+            if (rest > 0) {
+                Timed t(s, TC_UPDATE, 2.0 * r * rest * b, sizeof(T) * (2.0 * r * rest + r * b + b * rest));
+                DDLA_TRY(gemm_any<T>(h, prec, r, rest, b, T(-1), A21,
+                                     View<const T>{A12.p + b1 * A12.cs, b, rest, A12.rs, A12.cs}, T(1),
+                                     A.sub(j1, r, j1 + b1, rest)));
+            }
+            DDLA_CUDA(cudaStreamWaitEvent(s, h->ev_panel, 0));
+        } else {
+            {
+                View<const T> cA12{A12.p, b, r, A12.rs, A12.cs};
+                Timed t(s, TC_UPDATE, 2.0 * r * r * b, sizeof(T) * (2.0 * r * r + 2.0 * r * b));
+                DDLA_TRY(gemm_any<T>(h, prec, r, r, b, T(-1), A21, cA12, T(1), A.sub(j1, r, j1, r)));
+            }
+            DDLA_TRY(panel(s, j1, b1));
         }
     }
     return 0;

@@ -481,12 +481,12 @@ int panel_width_for(ddla_handle h, i64 m) {
     return 0;
 }
 
-// Factor the m x w panel at P (relative pivots into d_piv[0..w)), then apply
-// the interchanges to the other columns of the full rows: X is the m-row
-// block containing the panel at column offset pc, with ncols columns.
+// Factor the m x w panel at column pc of X (the m-row block of full rows) on
+// stream s: relative pivots into d_piv[0..w) and the touched-row list into
+// the WS_PIV scratch, which panel_swap_rest consumes.
 template <typename T>
-int panel_lu(ddla_handle h, View<T> X, i64 pc, int w, int32_t *d_piv, i64 row_base, int *d_info, int *perm) {
-    cudaStream_t s = h->stream;
+int panel_factor(ddla_handle h, cudaStream_t s, View<T> X, i64 pc, int w, int32_t *d_piv, i64 row_base,
+                 int *d_info) {
     const i64 m = X.rows;
     int *tbuf;
     DDLA_TRY(workspace(h, WS_PIV, sizeof(int) * (size_t)(1 + 2 * LASWP_MAXT + m), (void **)&tbuf));
@@ -537,6 +537,17 @@ int panel_lu(ddla_handle h, View<T> X, i64 pc, int w, int32_t *d_piv, i64 row_ba
         k_panel_lu_global<T><<<1, 1024, 0, s>>>(a, origin);
         DDLA_LAUNCHED();
     }
+    return 0;
+}
+
+// Apply the interchanges of the last panel_factor to the other columns of the
+// rows of X (and to the permutation vector), on the handle's stream.
+template <typename T>
+int panel_swap_rest(ddla_handle h, View<T> X, i64 pc, int w, int *perm) {
+    cudaStream_t s = h->stream;
+    int *tbuf;
+    DDLA_TRY(workspace(h, WS_PIV, sizeof(int) * (size_t)(1 + 2 * LASWP_MAXT + X.rows), (void **)&tbuf));
+    int *tcount = tbuf, *trows = tbuf + 1, *tsrc = tbuf + 1 + LASWP_MAXT;
     i64 other = X.cols - w;
     if (other > 0) {
         unsigned grid = (unsigned)((other + 31) / 32);
@@ -596,8 +607,10 @@ int apply_perm(ddla_handle h, View<T> B, const int32_t *d_piv, i64 n, bool forwa
 
 template int panel_width_for<double>(ddla_handle, i64);
 template int panel_width_for<float>(ddla_handle, i64);
-template int panel_lu<double>(ddla_handle, View<double>, i64, int, int32_t *, i64, int *, int *);
-template int panel_lu<float>(ddla_handle, View<float>, i64, int, int32_t *, i64, int *, int *);
+template int panel_factor<double>(ddla_handle, cudaStream_t, View<double>, i64, int, int32_t *, i64, int *);
+template int panel_factor<float>(ddla_handle, cudaStream_t, View<float>, i64, int, int32_t *, i64, int *);
+template int panel_swap_rest<double>(ddla_handle, View<double>, i64, int, int *);
+template int panel_swap_rest<float>(ddla_handle, View<float>, i64, int, int *);
 template int permute_rows<double>(ddla_handle, View<double>, const int *, i64, bool);
 template int permute_rows<float>(ddla_handle, View<float>, const int *, i64, bool);
 template int apply_perm<double>(ddla_handle, View<double>, const int32_t *, i64, bool);

@@ -201,16 +201,47 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_tf32x3(TcArgs g) {
             : "r"(taddr)
             : "memory");
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        const int64_t gr = m0 + 32 * q + lane;
-        if (gr < g.m) {
+        // stage the tile row-major in the (now idle) operand buffer, then update
+        // C with coalesced accesses: a warp covers 128 consecutive bytes of a row
+        constexpr int SLD = TN + 4;
+        float *stage = reinterpret_cast<float *>(smem);
+        {
+            float *row = stage + (32 * q + lane) * SLD + 32 * h;
 #pragma unroll
-            for (int j = 0; j < 32; j++) {
-                const int64_t gc = n0 + 32 * h + j;
-                if (gc >= g.n) break;
+            for (int j = 0; j < 32; j += 4)
+                *reinterpret_cast<float4 *>(row + j) =
+                    make_float4(__uint_as_float(d[j]), __uint_as_float(d[j + 1]), __uint_as_float(d[j + 2]),
+                                __uint_as_float(d[j + 3]));
+        }
+        __syncthreads();
+        const bool c_vec = (g.csc == 1) && ((g.rsc & 3) == 0) && ((((uintptr_t)g.C) & 15) == 0) &&
+                           (n0 + TN <= g.n) && g.uplo == DDLA_DENSE;
+        if (c_vec) {
+            for (int e = tid; e < TM * (TN / 4); e += TC_THREADS) {
+                const int r = e / (TN / 4), c4 = (e % (TN / 4)) * 4;
+                const int64_t gr = m0 + r;
+                if (gr >= g.m) continue;
+                float4 acc = *reinterpret_cast<const float4 *>(stage + r * SLD + c4);
+                float4 *cp = reinterpret_cast<float4 *>(g.C + gr * g.rsc + n0 + c4);
+                float4 o;
+                if (g.beta == 0.f) {
+                    o = make_float4(g.alpha * acc.x, g.alpha * acc.y, g.alpha * acc.z, g.alpha * acc.w);
+                } else {
+                    float4 cv = *cp;
+                    o = make_float4(fmaf(g.beta, cv.x, g.alpha * acc.x), fmaf(g.beta, cv.y, g.alpha * acc.y),
+                                    fmaf(g.beta, cv.z, g.alpha * acc.z), fmaf(g.beta, cv.w, g.alpha * acc.w));
+                }
+                *cp = o;
+            }
+        } else {
+            for (int e = tid; e < TM * TN; e += TC_THREADS) {
+                const int r = e / TN, c = e % TN;
+                const int64_t gr = m0 + r, gc = n0 + c;
+                if (gr >= g.m || gc >= g.n) continue;
                 if (g.uplo == DDLA_LOWER && gc > gr) continue;
                 if (g.uplo == DDLA_UPPER && gc < gr) continue;
                 float *cp = g.C + gr * g.rsc + gc * g.csc;
-                const float v = g.alpha * __uint_as_float(d[j]);
+                const float v = g.alpha * stage[r * SLD + c];
                 *cp = (g.beta == 0.f) ? v : fmaf(g.beta, *cp, v);
             }
         }
