@@ -71,6 +71,7 @@ _SIGS = {
     "ddla_measure_peaks": (C.c_int, [C.POINTER(_d), C.POINTER(_d)]),
     "ddla_dev_sgemm_tc": (C.c_int, [_h, _i32, _i64, _i64, _i64, C.c_float, _pd, _i64, _i64, _pd, _i64, _i64,
                                     C.c_float, _pd, _i64, _i64]),
+    "ddla_dev_dtrsv_noalloc": (C.c_int, [C.c_void_p, _i32, _i32, _i32, _i64, _i64, _pd, _i64, _i64, _pd, _i64]),
     "ddla_tune_set": (C.c_int, [C.c_char_p, _i64]),
     "ddla_tune_get": (_i64, [C.c_char_p, _i64]),
     "ddla_timing_enable": (C.c_int, [C.c_int]),

@@ -14,6 +14,9 @@
 //   * many right-hand sides: per diagonal block X1 = inv(A11) B1 and the GEMM
 //     update B2 -= A21 X1 (DDLA's managed TrSM has the same block structure
 //     with a TRSV per column, DDLA/BLAS/Managed/3m/TrSM.cs:62-122).
+#include <mutex>
+#include <string>
+
 #include "common.cuh"
 #include "timing.cuh"
 
@@ -313,3 +316,99 @@ template int trsv_apply<double>(ddla_handle, bool, View<const double>, i64, cons
 template int trsv_apply<float>(ddla_handle, bool, View<const float>, i64, const float *, float *, i64, int);
 
 }  // namespace ddla
+
+// ------------------------------------------------------------------ allocation-free solve
+//
+// ddla_dev_dtrsv_noalloc: the chained triangular solve above for callers that
+// cannot allocate device memory (for example code that must not call
+// cudaMalloc while other work is in flight, or that runs under an allocator it
+// does not own).  All of its scratch -- the inverted 64 x 64 diagonal blocks
+// and the per-block flags -- lives in ONE file-scope device array of fixed
+// size, which every GPU that loads this library keeps for the life of the
+// process.  That caps n at DDLA_NOALLOC_MAX_N and the right-hand sides at 16.
+namespace ddla {
+namespace {
+
+constexpr int NOALLOC_MAX_N = 2048;
+constexpr int NOALLOC_MAX_RHS = 16;
+constexpr int NOALLOC_NBLK = NOALLOC_MAX_N / TB;
+constexpr size_t NOALLOC_INV_BYTES = sizeof(double) * (size_t)NOALLOC_NBLK * TB * TB;   // 1 MiB
+constexpr size_t NOALLOC_WORDS = NOALLOC_NBLK + 2;   // flags[nblk], ticket, error
+constexpr size_t NOALLOC_BYTES = NOALLOC_INV_BYTES + 256;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
+
+std::mutex g_noalloc_mu;
+void *g_noalloc_ptr[64] = {};   // device address of g_noalloc_scratch, per device ordinal
+
+}  // namespace
+
+}  // namespace ddla
+
+using namespace ddla;
+
+extern "C" int ddla_dev_dtrsv_noalloc(void *stream, int32_t uplo, int32_t trans, int32_t diag, int64_t n,
+                                      int64_t nrhs, const double *a, int64_t rsa, int64_t csa, double *x,
+                                      int64_t ldx) {
+    if (uplo != DDLA_LOWER && uplo != DDLA_UPPER) { set_error("uplo must be DDLA_LOWER or DDLA_UPPER"); return -2; }
+    if (trans != DDLA_NO_TRANSPOSE && trans != DDLA_TRANSPOSE) { set_error("trans must be 0 or 8"); return -3; }
+    if (diag != DDLA_UNIT_DIAG && diag != DDLA_NONUNIT_DIAG) { set_error("diag must be 0 or 0x100"); return -4; }
+    if (n < 0 || n > NOALLOC_MAX_N) {
+        set_error("ddla_dev_dtrsv_noalloc: n = " + std::to_string(n) + " exceeds the fixed scratch limit of " +
+                  std::to_string(NOALLOC_MAX_N));
+        return -5;
+    }
+    if (nrhs < 0 || nrhs > NOALLOC_MAX_RHS) {
+        set_error("ddla_dev_dtrsv_noalloc: nrhs = " + std::to_string(nrhs) + " exceeds the limit of " +
+                  std::to_string(NOALLOC_MAX_RHS));
+        return -6;
+    }
+    if (ldx < (nrhs > 0 ? nrhs : 1)) { set_error("ldx must be >= nrhs"); return -11; }
+    if (n == 0 || nrhs == 0) return 0;
+    int dev = 0;
+    DDLA_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) { set_error("device ordinal out of range"); return DDLA_ERR_UNSUPPORTED; }
+    void *base;
+    {
+        // one-time set-up per device, with that device current: the host-side
+        // name g_noalloc_scratch is not a device address; ask the runtime for it
+        std::lock_guard<std::mutex> g(g_noalloc_mu);
+        if (!g_noalloc_ptr[dev]) DDLA_CUDA(cudaGetSymbolAddress(&g_noalloc_ptr[dev], g_noalloc_scratch));
+        base = g_noalloc_ptr[dev];
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    double *inv = (double *)base;
+    int *words = (int *)((unsigned char *)base + NOALLOC_INV_BYTES);
+    const int nblk = (int)((n + TB - 1) / TB);
+    int *flags = words, *ticket = words + nblk, *err = words + NOALLOC_NBLK + 1;
+    // the array keeps the previous call's contents: the flags, the ticket and
+    // the error word must start at zero
+    DDLA_CUDA(cudaMemsetAsync(words, 0, sizeof(int) * NOALLOC_WORDS, s));
+    View<const double> A{a, n, n, rsa, csa};
+    bool lower = (uplo == DDLA_LOWER);
+    if (trans == DDLA_TRANSPOSE) {
+        A = A.t();
+        lower = !lower;
+    }
+    k_tri_inv<double><<<nblk, TB, 0, s>>>(A.p, A.rs, A.cs, n, lower ? 1 : 0, diag == DDLA_UNIT_DIAG ? 1 : 0, inv);
+    DDLA_LAUNCHED();
+    const int nr = (int)nrhs;
+#define NOALLOC_CHAIN(NRV)                                                                                      \
+    k_trsv_chain<double, NRV><<<nblk, CHAIN_THREADS, 0, s>>>(n, nblk, A.p, A.rs, A.cs, lower ? 1 : 0, inv, x, ldx, \
+                                                             nr, flags, ticket, err)
+    if (nr <= 1) NOALLOC_CHAIN(1);
+    else if (nr <= 2) NOALLOC_CHAIN(2);
+    else if (nr <= 4) NOALLOC_CHAIN(4);
+    else if (nr <= 8) NOALLOC_CHAIN(8);
+    else NOALLOC_CHAIN(16);
+#undef NOALLOC_CHAIN
+    DDLA_LAUNCHED();
+    int herr = 0;
+    DDLA_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    DDLA_CUDA(cudaStreamSynchronize(s));
+    if (herr) {
+        set_error("ddla_dev_dtrsv_noalloc: a bounded wait of the chained solve gave up");
+        return DDLA_ERR_TIMEOUT;
+    }
+    return 0;
+}

@@ -241,6 +241,29 @@ int ddla_dev_sgemm_tc(ddla_handle h, int32_t precision, int64_t m, int64_t n, in
                       int64_t rsa, int64_t csa, const float *b, int64_t rsb, int64_t csb, float beta, float *c,
                       int64_t rsc, int64_t csc);
 
+/* Allocation-free triangular solve (no counterpart in the reference; DDLA has
+ * no GPU code).  Solves op(tri(A)) X = X in place for n <= DDLA_NOALLOC_MAX_N
+ * and nrhs <= DDLA_NOALLOC_MAX_RHS, X row-major on the device with leading
+ * dimension ldx, A a device view (rsa, csa), on `stream` (cudaStream_t cast to
+ * void*; NULL = legacy default stream).  It is for callers that must not
+ * allocate device memory -- for example a real-time loop that may not block
+ * on cudaMalloc, or an application whose memory is owned by its own pool
+ * allocator: every other device entry point grows a handle workspace on
+ * first use, this one never calls cudaMalloc, cudaFree or any allocating
+ * routine.  Its scratch (the inverted diagonal blocks and the block flags) is
+ * one fixed 1 MiB + 256 B array in the library's device image, held by every
+ * GPU that loads the library until the process exits.  The first call on a
+ * device looks up that array's device address (cudaGetSymbolAddress) and
+ * should therefore come before any stream capture.  All calls share the one
+ * array: calls whose work overlaps on the GPU (different streams, threads)
+ * race and must be serialized by the caller.  Synchronous: returns after the
+ * solve with 0, a negative argument position, DDLA_ERR_TIMEOUT or
+ * DDLA_ERR_CUDA. */
+#define DDLA_NOALLOC_MAX_N 2048
+#define DDLA_NOALLOC_MAX_RHS 16
+int ddla_dev_dtrsv_noalloc(void *stream, int32_t uplo, int32_t trans, int32_t diag, int64_t n, int64_t nrhs,
+                           const double *a, int64_t rsa, int64_t csa, double *x, int64_t ldx);
+
 /* ------------------------------------------------ batched small factorizations */
 
 /* Plan for `count` square row-major matrices of uneven size (1 <= n[i] <= 1024,
