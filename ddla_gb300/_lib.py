@@ -20,7 +20,7 @@ LOWER, UPPER, DENSE = 0xC0, 0x60, 0xE0
 NONUNIT, UNIT = 0x000, 0x100
 LEFT, RIGHT = 0, 1
 
-PREC_FP64, PREC_FP32, PREC_TF32X3, PREC_BF16X3 = 0, 1, 2, 3
+PREC_FP64, PREC_FP32, PREC_TF32X3, PREC_BF16X3, PREC_OZAKI = 0, 1, 2, 3, 4
 
 ERR_CUDA, ERR_NOMEM, ERR_TIMEOUT, ERR_NOT_CONVERGED, ERR_UNSUPPORTED, ERR_NO_DEVICE = (
     -1001, -1002, -1003, -1004, -1005, -1006)
@@ -97,6 +97,8 @@ _SIGS = {
                                    C.POINTER(Opts), C.POINTER(SolveReport)]),
     "ddla_dev_dgemm": (C.c_int, [_h, _i32, _i32, _i64, _i64, _i64, _d, _pd, _i64, _i64, _pd, _i64, _i64, _d, _pd,
                                  _i64, _i64]),
+    "ddla_dev_dgemm_ex": (C.c_int, [_h, _i32, _i32, _i32, _i64, _i64, _i64, _d, _pd, _i64, _i64, _pd, _i64, _i64,
+                                    _d, _pd, _i64, _i64]),
     "ddla_dev_dgemmt": (C.c_int, [_h, _i32, _i32, _i32, _i64, _i64, _d, _pd, _i64, _i64, _pd, _i64, _i64, _d, _pd,
                                   _i64, _i64]),
     "ddla_dev_dtrsm": (C.c_int, [_h, _i32, _i32, _i32, _i32, _i64, _i64, _d, _pd, _i64, _i64, _pd, _i64, _i64]),

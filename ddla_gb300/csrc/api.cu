@@ -227,16 +227,23 @@ static int stage_out(ddla_handle h, const Staged &s, double *hp, i64 rows, i64 c
     return 0;
 }
 
+static int fprec(const ddla_opts *o) {
+    return (o && o->precision == DDLA_PREC_OZAKI) ? DDLA_PREC_OZAKI : DDLA_PREC_FP64;
+}
+
 static View<const double> cv(const View<double> &v) { return View<const double>{v.p, v.rows, v.cols, v.rs, v.cs}; }
 
 template <typename T>
 int gemm_any(ddla_handle h, int prec, i64 m, i64 n, i64 k, T alpha, View<const T> A, View<const T> B, T beta,
              View<T> C, int uplo);
 
+int gemm_ozaki(ddla_handle h, i64 m, i64 n, i64 k, double alpha, View<const double> A, View<const double> B,
+               double beta, View<double> C, int uplo = DDLA_DENSE);
+
 template <>
 int gemm_any<double>(ddla_handle h, int prec, i64 m, i64 n, i64 k, double alpha, View<const double> A,
                      View<const double> B, double beta, View<double> C, int uplo) {
-    (void)prec;
+    if (prec == DDLA_PREC_OZAKI) return gemm_ozaki(h, m, n, k, alpha, A, B, beta, C, uplo);
     return gemm_f64(h->stream, m, n, k, alpha, A, B, beta, C, uplo);
 }
 
@@ -318,6 +325,26 @@ int ddla_dev_dgemm(ddla_handle h, int32_t ta, int32_t tb, ddla_dim_t m, ddla_dim
     if (is_trans(ta)) A = A.t();
     if (is_trans(tb)) B = B.t();
     return gemm_f64(h->stream, m, n, k, alpha, A, B, beta, View<double>{c, m, n, rsc, csc});
+}
+
+int ddla_dev_dgemm_ex(ddla_handle h, int32_t precision, int32_t ta, int32_t tb, ddla_dim_t m, ddla_dim_t n,
+                      ddla_dim_t k, double alpha, const double *a, ddla_inc_t rsa, ddla_inc_t csa, const double *b,
+                      ddla_inc_t rsb, ddla_inc_t csb, double beta, double *c, ddla_inc_t rsc, ddla_inc_t csc) {
+    CHECK_ARG(h != nullptr, 1);
+    CHECK_ARG(precision == DDLA_PREC_FP64 || precision == DDLA_PREC_OZAKI, 2);
+    CHECK_ARG(valid_trans(ta), 3);
+    CHECK_ARG(valid_trans(tb), 4);
+    CHECK_ARG(m >= 0, 5);
+    CHECK_ARG(n >= 0, 6);
+    CHECK_ARG(k >= 0, 7);
+    if (m == 0 || n == 0) return 0;
+    View<const double> A{a, is_trans(ta) ? k : m, is_trans(ta) ? m : k, rsa, csa};
+    View<const double> B{b, is_trans(tb) ? n : k, is_trans(tb) ? k : n, rsb, csb};
+    if (is_trans(ta)) A = A.t();
+    if (is_trans(tb)) B = B.t();
+    View<double> C{c, m, n, rsc, csc};
+    if (precision == DDLA_PREC_OZAKI) return gemm_ozaki(h, m, n, k, alpha, A, B, beta, C);
+    return gemm_f64(h->stream, m, n, k, alpha, A, B, beta, C);
 }
 
 int ddla_dev_dgemmt(ddla_handle h, int32_t uplo, int32_t ta, int32_t tb, ddla_dim_t m, ddla_dim_t k, double alpha,
@@ -449,7 +476,7 @@ int ddla_dev_dgetrf(ddla_handle h, ddla_dim_t n, double *a, ddla_inc_t rsa, ddla
     CHECK_ARG(piv != nullptr || n == 0, 6);
     if (n == 0) return 0;
     DDLA_TRY(reset_info(h));
-    DDLA_TRY(getrf<double>(h, n, View<double>{a, n, n, rsa, csa}, piv, DDLA_PREC_FP64, opts ? opts->nb : 0));
+    DDLA_TRY(getrf<double>(h, n, View<double>{a, n, n, rsa, csa}, piv, fprec(opts), opts ? opts->nb : 0));
     int info;
     DDLA_TRY(read_info(h, &info));
     return info;
@@ -470,7 +497,7 @@ int ddla_dev_dpotrf(ddla_handle h, int32_t uplo, ddla_dim_t n, double *a, ddla_i
     CHECK_ARG(n >= 0, 3);
     if (n == 0) return 0;
     DDLA_TRY(reset_info(h));
-    DDLA_TRY(potrf<double>(h, uplo, n, View<double>{a, n, n, rsa, csa}, DDLA_PREC_FP64, opts ? opts->nb : 0));
+    DDLA_TRY(potrf<double>(h, uplo, n, View<double>{a, n, n, rsa, csa}, fprec(opts), opts ? opts->nb : 0));
     int info;
     DDLA_TRY(read_info(h, &info));
     return info;
@@ -489,7 +516,7 @@ int ddla_dev_dldlt(ddla_handle h, int32_t uplo, ddla_dim_t n, double *a, ddla_in
     CHECK_ARG(n >= 0, 3);
     if (n == 0) return 0;
     DDLA_TRY(reset_info(h));
-    DDLA_TRY(ldlt<double>(h, uplo, n, View<double>{a, n, n, rsa, csa}, DDLA_PREC_FP64, opts ? opts->nb : 0));
+    DDLA_TRY(ldlt<double>(h, uplo, n, View<double>{a, n, n, rsa, csa}, fprec(opts), opts ? opts->nb : 0));
     int info;
     DDLA_TRY(read_info(h, &info));
     return info;
@@ -518,7 +545,7 @@ int ddla_dgetrf(ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t csa, int32_t
     int32_t *dp;
     DDLA_TRY(workspace(h, WS_X, sizeof(int32_t) * (size_t)n, (void **)&dp));
     DDLA_TRY(reset_info(h));
-    DDLA_TRY(getrf<double>(h, n, sa.view, dp, DDLA_PREC_FP64, opts ? opts->nb : 0));
+    DDLA_TRY(getrf<double>(h, n, sa.view, dp, fprec(opts), opts ? opts->nb : 0));
     int info;
     DDLA_TRY(read_info(h, &info));
     DDLA_CUDA(cudaMemcpyAsync(piv, dp, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost, h->stream));
@@ -550,7 +577,7 @@ int ddla_dgetrf_nopiv(ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t csa, c
     Staged sa;
     DDLA_TRY(stage_in(h, WS_A, a, n, n, rsa, csa, true, &sa));
     DDLA_TRY(reset_info(h));
-    DDLA_TRY(getrf_nopiv<double>(h, n, sa.view, DDLA_PREC_FP64, opts ? opts->nb : 0));
+    DDLA_TRY(getrf_nopiv<double>(h, n, sa.view, fprec(opts), opts ? opts->nb : 0));
     int info;
     DDLA_TRY(read_info(h, &info));
     DDLA_TRY(stage_out(h, sa, a, n, n, rsa, csa));
@@ -578,7 +605,7 @@ int ddla_dpotrf(int32_t uplo, ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_
     Staged sa;
     DDLA_TRY(stage_in(h, WS_A, a, n, n, rsa, csa, true, &sa));
     DDLA_TRY(reset_info(h));
-    DDLA_TRY(potrf<double>(h, uplo, n, sa.view, DDLA_PREC_FP64, opts ? opts->nb : 0));
+    DDLA_TRY(potrf<double>(h, uplo, n, sa.view, fprec(opts), opts ? opts->nb : 0));
     int info;
     DDLA_TRY(read_info(h, &info));
     DDLA_TRY(stage_out(h, sa, a, n, n, rsa, csa, uplo));
@@ -607,7 +634,7 @@ int ddla_dldlt(int32_t uplo, ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t
     Staged sa;
     DDLA_TRY(stage_in(h, WS_A, a, n, n, rsa, csa, true, &sa));
     DDLA_TRY(reset_info(h));
-    DDLA_TRY(ldlt<double>(h, uplo, n, sa.view, DDLA_PREC_FP64, opts ? opts->nb : 0));
+    DDLA_TRY(ldlt<double>(h, uplo, n, sa.view, fprec(opts), opts ? opts->nb : 0));
     int info;
     DDLA_TRY(read_info(h, &info));
     DDLA_TRY(stage_out(h, sa, a, n, n, rsa, csa, uplo));

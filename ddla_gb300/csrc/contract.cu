@@ -29,7 +29,7 @@ namespace ddla {
 int gemm_f64_offsets(cudaStream_t s, i64 m, i64 n, i64 k, double alpha, View<const double> A,
                      View<const double> B, double beta, View<double> C, i64 batch, const i64 *d_offsets);
 int gemm_ozaki(ddla_handle h, i64 m, i64 n, i64 k, double alpha, View<const double> A, View<const double> B,
-               double beta, View<double> C, int slices);
+               double beta, View<double> C, int uplo = DDLA_DENSE);
 
 namespace {
 
@@ -267,7 +267,7 @@ int contract_exec(ddla_handle h, const ddla_contract_desc *d, double alpha, cons
                 for (i64 p = 0; p < npar; p++) {
                     View<const double> Ap{Av.p + poa[p], M, K, Av.rs, Av.cs}, Bp{Bv.p + pob[p], K, N, Bv.rs, Bv.cs};
                     View<double> Cp{Cv.p + poc[p], M, N, Cv.rs, Cv.cs};
-                    DDLA_TRY(gemm_ozaki(h, M, N, K, alpha, Ap, Bp, 1.0, Cp, prec));
+                    DDLA_TRY(gemm_ozaki(h, M, N, K, alpha, Ap, Bp, 1.0, Cp));
                 }
             }
         }
@@ -301,7 +301,7 @@ int contract_exec(ddla_handle h, const ddla_contract_desc *d, double alpha, cons
             View<const double> Av{dA, M, K, K, 1}, Bv{dB, K, N, N, 1};
             View<double> Cv{dC, M, N, N, 1};
             if (prec == DDLA_PREC_FP64) DDLA_TRY(gemm_f64(s, M, N, K, alpha, Av, Bv, 0.0, Cv));
-            else DDLA_TRY(gemm_ozaki(h, M, N, K, alpha, Av, Bv, 0.0, Cv, prec));
+            else DDLA_TRY(gemm_ozaki(h, M, N, K, alpha, Av, Bv, 0.0, Cv));
             k_scatter_add<<<grid_of(M * N), 256, 0, s>>>(dC, drC, dcC, M, N, c + soc[q] + poc[p]);
             DDLA_LAUNCHED();
         }
@@ -331,6 +331,7 @@ int ddla_dev_contract(ddla_handle h, const ddla_contract_desc *d, double alpha, 
                       double *c, int32_t precision) {
     if (!h) return -1;
     if (!d) return -2;
+    if (precision != DDLA_PREC_FP64 && precision != DDLA_PREC_OZAKI) return -7;
     return contract_exec(h, d, alpha, a, b, c, precision);
 }
 
@@ -340,6 +341,7 @@ int ddla_contract(const ddla_contract_desc *d, double alpha, const double *a, in
     if (na < 0) return -4;
     if (nb < 0) return -6;
     if (nc < 0) return -8;
+    if (precision != DDLA_PREC_FP64 && precision != DDLA_PREC_OZAKI) return -9;
     ddla_handle h;
     DDLA_TRY(default_handle(&h));
     cudaStream_t s = h->stream;

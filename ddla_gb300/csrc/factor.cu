@@ -153,7 +153,8 @@ int grid_for(i64 tot) { return (int)((tot + 255) / 256 < 8192 ? ((tot + 255) / 2
 
 template <typename T>
 int prec_of(int prec) {
-    return sizeof(T) == 8 ? DDLA_PREC_FP64 : (prec == DDLA_PREC_FP64 ? DDLA_PREC_FP32 : prec);
+    if (sizeof(T) == 8) return prec == DDLA_PREC_OZAKI ? DDLA_PREC_OZAKI : DDLA_PREC_FP64;
+    return prec == DDLA_PREC_FP64 || prec == DDLA_PREC_OZAKI ? DDLA_PREC_FP32 : prec;
 }
 
 int pick_nb(int nb, int dflt) { return nb > 0 ? (nb > DIAG_MAX ? DIAG_MAX : nb) : dflt; }

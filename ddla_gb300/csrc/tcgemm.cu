@@ -14,6 +14,8 @@
 //
 // gemm_ozaki: FP64 GEMM with FP64-level accuracy from BF16 slice products on
 // the same kind of kernel (see the comment at its definition).
+#include <cuda_bf16.h>
+
 #include <cstdint>
 
 #include "common.cuh"
@@ -295,11 +297,343 @@ int gemm_tc(ddla_handle h, int prec, i64 m, i64 n, i64 k, float alpha, View<cons
     return 0;
 }
 
+// ------------------------------------------------------------------ Ozaki split FP64 GEMM
+//
+// C = alpha*A*B + beta*C with FP64-level accuracy from BF16 tensor-core
+// products (Ozaki scheme, error-free splitting):
+//   * row i of A is scaled by sigma_i = 2^e_i (the smallest power of two above
+//     max_k |a_ik|) and cut into OZ_S slices of OZ_BETA bits, taken from the
+//     integer mantissa: a_ik = sigma_i sum_t q_t 2^(-beta (t+1)), 0 <= |q_t| <=
+//     2^beta - 1, all slices carrying the sign of a_ik; the remainder below
+//     2^(-beta OZ_S) sigma_i is dropped.  Columns of B likewise (tau_j).
+//   * slices are stored pre-scaled, A_t = q_t 2^(-beta t), which is exact in
+//     BF16 (8-bit integers times a power of two);
+//   * A*B = 2^(-2 beta) diag(sigma) [sum_{t+u < OZ_S} A_t B_u] diag(tau).
+//     Products of one level t+u = l are multiples of 2^(-beta l) below
+//     2^(2 beta - beta l), so a level accumulates EXACTLY in FP32 (TMEM) while
+//     its partial sum stays below 2^24 ulps: the levels l < OZ_EXACT each get
+//     their own accumulator, flushed into FP64 registers after at most
+//     oz_period(l) of K; the small levels l >= OZ_EXACT share one rounded FP32
+//     accumulator (their rounding is below 2^-(beta OZ_EXACT + 24) of the
+//     result scale).
+// The error is bounded by a small multiple of 2^-53 K sigma_i tau_j, i.e.
+// relative to max_k |a_ik| max_k |b_kj|.  Non-finite inputs make the affected
+// rows / columns of C non-finite.
+//
+// Operand slices are packed by the split kernels directly in the shared-memory
+// tile layout ([slice][row tile][K chunk][core matrices]) so that staging a
+// K chunk is a contiguous copy.
+namespace {
+
+constexpr int OZ_S = 8, OZ_BETA = 7;
+constexpr int OZ_EXACT = 5;               // levels with their own exact accumulator
+constexpr int OZ_NACC = OZ_EXACT + 1;     // + one shared accumulator for the small levels
+constexpr int OZ_TN = 32;                 // tile columns
+constexpr int OZ_KC = 64;                 // K staged per chunk (bf16)
+constexpr int OZ_SBO = (OZ_KC / 8) * 128; // bf16 core-matrix layout: 8 elements per 16-byte chunk
+constexpr int OZ_A_TILE = TM * OZ_KC * 2, OZ_B_TILE = OZ_TN * OZ_KC * 2;
+constexpr size_t OZ_SMEM = (size_t)OZ_S * (OZ_A_TILE + OZ_B_TILE);
+constexpr int OZ_TMEM_COLS = 256;         // OZ_NACC x 32 columns, rounded up to a power of two
+static_assert(OZ_NACC * OZ_TN <= OZ_TMEM_COLS, "TMEM columns");
+static_assert((size_t)TM * (OZ_TN + 1) * 8 <= OZ_SMEM, "epilogue staging");
+
+// Flush period of accumulator a in K chunks: level l sums (l+1) slice pairs of
+// products below (2^beta - 1)^2 ulps, exact while (l+1) * period * 127^2 < 2^24.
+__host__ __device__ constexpr int oz_period(int a) {
+    return a == 0 ? 16 : a == 1 ? 8 : a == 2 ? 4 : a == 3 ? 4 : a == 4 ? 2 : 16;
+}
+static_assert(1 * 16 * OZ_KC * 127 * 127 < (1 << 24) && 2 * 8 * OZ_KC * 127 * 127 < (1 << 24) &&
+                  3 * 4 * OZ_KC * 127 * 127 < (1 << 24) && 4 * 4 * OZ_KC * 127 * 127 < (1 << 24) &&
+                  5 * 2 * OZ_KC * 127 * 127 < (1 << 24),
+              "exact accumulation periods");
+
+__device__ __forceinline__ int oz_off(int r, int k) {   // byte offset of bf16 element (r, k) in a tile
+    return (r >> 3) * OZ_SBO + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2;
+}
+
+__device__ __forceinline__ uint64_t oz_desc(unsigned addr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((addr & 0x3ffff) >> 4);
+    d |= (uint64_t)(128 >> 4) << 16;
+    d |= (uint64_t)(OZ_SBO >> 4) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+
+// D f32, A and B bf16 (format 1), K-major, N = OZ_TN, M = TM
+__host__ __device__ constexpr uint32_t oz_idesc() {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(OZ_TN >> 3) << 17) | ((uint32_t)(TM >> 4) << 24);
+}
+
+// Splits the rows of a strided FP64 matrix X (rows x cols) into OZ_S packed
+// BF16 slices.  One block per padded row (row tiles of `tr` rows); the scale
+// 2^e of each row goes to scale[r] (non-finite rows store their max, which
+// makes the row of the result non-finite).
+__global__ void k_oz_split(const double *X, i64 rs, i64 cs, i64 rows, i64 cols, int tr, i64 row_tiles,
+                           i64 kchunks, __nv_bfloat16 *pack, double *scale) {
+    const i64 r = blockIdx.x;
+    __shared__ unsigned long long red[32];
+    const bool live = r < rows;
+    // row max of |x| on the integer pipe: for non-negative doubles the bit
+    // pattern orders like the value (NaN above +inf)
+    unsigned long long mx = 0;
+    if (live)
+        for (i64 c = threadIdx.x; c < cols; c += blockDim.x)
+            mx = max(mx, (unsigned long long)__double_as_longlong(X[r * rs + c * cs]) & 0x7fffffffffffffffULL);
+    for (int off = 16; off > 0; off >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        unsigned long long v = threadIdx.x < blockDim.x / 32 ? red[threadIdx.x] : 0ULL;
+        for (int off = 16; off > 0; off >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, off));
+        if (threadIdx.x == 0) red[0] = v;
+    }
+    __syncthreads();
+    mx = red[0];
+    const int bexp = (int)(mx >> 52);   // biased exponent of the row max
+    int e = 0;                          // row scale 2^e > max |x|
+    bool finite = bexp < 2047;
+    if (mx != 0 && finite) {
+        if (bexp == 0) {                // subnormal max: 2^e above its leading bit
+            e = -1074 + (64 - __clzll(mx));
+        } else {
+            e = bexp - 1022;
+        }
+    }
+    if (threadIdx.x == 0) scale[r] = finite ? ldexp(1.0, e) : __longlong_as_double((long long)mx);
+    const i64 rt = r / tr, rr = r % tr;
+    for (i64 c8 = threadIdx.x; c8 < kchunks * (OZ_KC / 8); c8 += blockDim.x) {
+        unsigned q[OZ_S][4];
+#pragma unroll
+        for (int t = 0; t < OZ_S; t++) q[t][0] = q[t][1] = q[t][2] = q[t][3] = 0;
+#pragma unroll
+        for (int x = 0; x < 8; x++) {
+            const i64 c = 8 * c8 + x;
+            long long bits = 0;
+            if (live && finite && c < cols) bits = __double_as_longlong(X[r * rs + c * cs]);
+            const unsigned long long ab = (unsigned long long)bits & 0x7fffffffffffffffULL;
+            const int ex = (int)(ab >> 52);
+            const unsigned long long man = (ab & ((1ULL << 52) - 1)) | (ex ? (1ULL << 52) : 0ULL);
+            // |x| / 2^e as a fixed-point fraction with beta*S bits (truncated)
+            const int sh = (ex ? ex - 1075 : -1074) - e + OZ_BETA * OZ_S;
+            unsigned long long F = 0;
+            if (sh >= 0) F = man << sh;   // sh <= 3 since |x| < 2^e
+            else if (sh > -64) F = man >> (-sh);
+            const unsigned sgn = bits < 0 ? 0x8000u : 0u;
+#pragma unroll
+            for (int t = 0; t < OZ_S; t++) {
+                const unsigned qt = (unsigned)(F >> (OZ_BETA * (OZ_S - 1 - t))) & ((1u << OZ_BETA) - 1);
+                // bf16 of qt * 2^(-beta t): exact (qt < 2^8), built from the float
+                const float f = __int_as_float(__float_as_int((float)qt) - ((OZ_BETA * t) << 23) * (qt != 0));
+                const unsigned hb = (__float_as_uint(f) >> 16) | (qt ? sgn : 0u);
+                q[t][x >> 1] |= hb << (16 * (x & 1));
+            }
+        }
+        const i64 kc = c8 / (OZ_KC / 8), kq = 8 * (c8 % (OZ_KC / 8));
+#pragma unroll
+        for (int t = 0; t < OZ_S; t++) {
+            const i64 tile = ((t * row_tiles + rt) * kchunks + kc);
+            unsigned char *dst = reinterpret_cast<unsigned char *>(pack) + tile * (i64)tr * OZ_KC * 2 +
+                                 oz_off((int)rr, (int)kq);
+            *reinterpret_cast<uint4 *>(dst) = make_uint4(q[t][0], q[t][1], q[t][2], q[t][3]);
+        }
+    }
+}
+
+struct OzArgs {
+    int64_t m, n, kchunks, mtiles, ntiles;
+    const __nv_bfloat16 *Ap, *Bp;   // packed slices
+    const double *sa, *sb;          // row / column scales
+    double alpha, beta;
+    double *C;
+    int64_t rsc, csc;
+    int uplo;   // DDLA_DENSE, or the triangle of C that is written (GEMMT)
+    int *err;
+};
+
+__global__ void __launch_bounds__(TC_THREADS, 1) k_oz_gemm(OzArgs g) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned char *At = smem, *Bt = smem + (size_t)OZ_S * OZ_A_TILE;
+    __shared__ __align__(8) unsigned long long mbar;
+    __shared__ unsigned tmem_slot;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int64_t mt = blockIdx.y, nt = blockIdx.x;
+    const int64_t m0 = mt * TM, n0 = nt * OZ_TN;
+    if (g.uplo == DDLA_LOWER && n0 > m0 + TM - 1) return;
+    if (g.uplo == DDLA_UPPER && m0 > n0 + OZ_TN - 1) return;
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(&tmem_slot)),
+                     "r"(OZ_TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&mbar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const unsigned tmem = tmem_slot;
+    const uint32_t id = oz_idesc();
+    unsigned phase = 0;
+    bool failed = false;
+    // FP64 accumulation: warp w reads TMEM lanes 32*(w%4).. of the accumulators
+    // in its group's mask (flush work balanced between the two halves)
+    const int q = warp & 3;
+    const unsigned mymask = (warp < 4) ? 0x13u : 0x2cu;   // {0,1,4} / {2,3,5}
+    double acc[OZ_TN];
+#pragma unroll
+    for (int j = 0; j < OZ_TN; j++) acc[j] = 0.0;
+    const size_t a_stride = (size_t)g.mtiles * g.kchunks * (TM * OZ_KC);     // elements between slices
+    const size_t b_stride = (size_t)g.ntiles * g.kchunks * (OZ_TN * OZ_KC);
+    for (int64_t c = 0; c < g.kchunks; c++) {
+        {   // stage every slice of this chunk: contiguous 16-byte copies
+            const uint4 *srcA = reinterpret_cast<const uint4 *>(g.Ap + ((size_t)mt * g.kchunks + c) * (TM * OZ_KC));
+            const uint4 *srcB =
+                reinterpret_cast<const uint4 *>(g.Bp + ((size_t)nt * g.kchunks + c) * (OZ_TN * OZ_KC));
+            constexpr int AV = OZ_A_TILE / 16, BV = OZ_B_TILE / 16;
+            for (int e = tid; e < OZ_S * AV; e += TC_THREADS) {
+                const int t = e / AV, o = e % AV;
+                reinterpret_cast<uint4 *>(At)[e] = srcA[(size_t)t * (a_stride / 8) + o];
+            }
+            for (int e = tid; e < OZ_S * BV; e += TC_THREADS) {
+                const int u = e / BV, o = e % BV;
+                reinterpret_cast<uint4 *>(Bt)[e] = srcB[(size_t)u * (b_stride / 8) + o];
+            }
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            unsigned started = 0;
+            for (int t = 0; t < OZ_S; t++)
+                for (int u = 0; t + u < OZ_S; u++) {
+                    const int a = (t + u < OZ_EXACT) ? t + u : OZ_EXACT;
+                    const bool fresh = (c % oz_period(a)) == 0 && !((started >> a) & 1u);
+                    started |= 1u << a;
+                    const unsigned dcol = tmem + (unsigned)(a * OZ_TN);
+                    for (int ks = 0; ks < OZ_KC / 16; ks++) {
+                        const uint64_t ad = oz_desc(su32(At + (size_t)t * OZ_A_TILE) + ks * 256);
+                        const uint64_t bd = oz_desc(su32(Bt + (size_t)u * OZ_B_TILE) + ks * 256);
+                        const int accum = (fresh && ks == 0) ? 0 : 1;
+                        asm volatile(
+                            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dcol),
+                            "l"(ad), "l"(bd), "r"(id), "r"(accum)
+                            : "memory");
+                    }
+                }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             su32(&mbar))
+                         : "memory");
+        }
+        bool ok = false;
+        for (long long it = 0; it < TC_SPIN; it++)
+            if (mbar_try(su32(&mbar), phase)) { ok = true; break; }
+        phase ^= 1u;
+        if (__syncthreads_or(!ok)) {
+            failed = true;
+            if (tid == 0) atomicExch(g.err, 1);
+            break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const bool last = c + 1 == g.kchunks;
+        for (int a = 0; a < OZ_NACC; a++) {
+            if (!((mymask >> a) & 1u)) continue;
+            if (!last && ((c + 1) % oz_period(a)) != 0) continue;
+            uint32_t d[32];
+            const unsigned taddr = tmem + ((unsigned)(32 * q) << 16) + (unsigned)(a * OZ_TN);
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                : "=r"(d[0]), "=r"(d[1]), "=r"(d[2]), "=r"(d[3]), "=r"(d[4]), "=r"(d[5]), "=r"(d[6]), "=r"(d[7]),
+                  "=r"(d[8]), "=r"(d[9]), "=r"(d[10]), "=r"(d[11]), "=r"(d[12]), "=r"(d[13]), "=r"(d[14]),
+                  "=r"(d[15]), "=r"(d[16]), "=r"(d[17]), "=r"(d[18]), "=r"(d[19]), "=r"(d[20]), "=r"(d[21]),
+                  "=r"(d[22]), "=r"(d[23]), "=r"(d[24]), "=r"(d[25]), "=r"(d[26]), "=r"(d[27]), "=r"(d[28]),
+                  "=r"(d[29]), "=r"(d[30]), "=r"(d[31])
+                : "r"(taddr)
+                : "memory");
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+            for (int j = 0; j < OZ_TN; j++) acc[j] += (double)__uint_as_float(d[j]);
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    }
+    // combine the two halves of each row through shared memory, then apply the
+    // scales 2^(-2 beta) sigma_i tau_j and the alpha / beta epilogue
+    __syncthreads();
+    double *stage = reinterpret_cast<double *>(smem);   // [TM][OZ_TN + 1]
+    if (!failed) {
+        if (warp >= 4) {
+            double *row = stage + (32 * q + lane) * (OZ_TN + 1);
+#pragma unroll
+            for (int j = 0; j < OZ_TN; j++) row[j] = acc[j];
+        }
+        __syncthreads();
+        if (warp < 4) {
+            const int64_t gr = m0 + 32 * q + lane;
+            const double *row = stage + (32 * q + lane) * (OZ_TN + 1);
+            if (gr < g.m) {
+                const double sr = g.sa[gr] * g.alpha * 0x1p-14;
+#pragma unroll
+                for (int j = 0; j < OZ_TN; j++) {
+                    const int64_t gc = n0 + j;
+                    if (gc >= g.n) continue;
+                    if (g.uplo == DDLA_LOWER && gc > gr) continue;
+                    if (g.uplo == DDLA_UPPER && gc < gr) continue;
+                    const double v = ((acc[j] + row[j]) * sr) * g.sb[gc];
+                    double *cp = g.C + gr * g.rsc + gc * g.csc;
+                    *cp = (g.beta == 0.0) ? v : fma(g.beta, *cp, v);
+                }
+            }
+        }
+    } else {
+        for (long long it = 0; it < TC_SPIN; it++)
+            if (mbar_try(su32(&mbar), phase ^ 1u)) break;
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(OZ_TMEM_COLS)
+                     : "memory");
+    }
+}
+
+}  // namespace
+
 int gemm_ozaki(ddla_handle h, i64 m, i64 n, i64 k, double alpha, View<const double> A, View<const double> B,
-               double beta, View<double> C, int prec) {
-    (void)h; (void)m; (void)n; (void)k; (void)alpha; (void)A; (void)B; (void)beta; (void)C; (void)prec;
-    set_error("split-precision FP64 GEMM not available in this build");
-    return DDLA_ERR_UNSUPPORTED;
+               double beta, View<double> C, int uplo) {
+    if (m <= 0 || n <= 0) return 0;
+    cudaStream_t s = h->stream;
+    if (k <= 0 || alpha == 0.0) return gemm_f64(s, m, n, 0, 0.0, A, B, beta, C, uplo);
+    static size_t avail = 0;
+    if (!avail) DDLA_TRY(max_dyn_smem((const void *)k_oz_gemm, h->smem_optin, &avail));
+    if (OZ_SMEM > avail) {
+        set_error("gemm_ozaki: not enough shared memory");
+        return DDLA_ERR_UNSUPPORTED;
+    }
+    const i64 mtiles = (m + TM - 1) / TM, ntiles = (n + OZ_TN - 1) / OZ_TN, kchunks = (k + OZ_KC - 1) / OZ_KC;
+    if (mtiles > 65535) { set_error("gemm_ozaki: m too large"); return DDLA_ERR_UNSUPPORTED; }
+    const size_t abytes = (size_t)OZ_S * mtiles * TM * kchunks * OZ_KC * 2;
+    const size_t bbytes = (size_t)OZ_S * ntiles * OZ_TN * kchunks * OZ_KC * 2;
+    void *wa, *wb;
+    DDLA_TRY(workspace(h, WS_TC, abytes + sizeof(double) * mtiles * TM, &wa));
+    DDLA_TRY(workspace(h, WS_TC2, bbytes + sizeof(double) * ntiles * OZ_TN, &wb));
+    __nv_bfloat16 *ap = (__nv_bfloat16 *)wa, *bp = (__nv_bfloat16 *)wb;
+    double *sa = (double *)((char *)wa + abytes), *sb = (double *)((char *)wb + bbytes);
+    k_oz_split<<<(unsigned)(mtiles * TM), 256, 0, s>>>(A.p, A.rs, A.cs, m, k, TM, mtiles, kchunks, ap, sa);
+    DDLA_LAUNCHED();
+    View<const double> Bt = B.t();   // columns of B as rows
+    k_oz_split<<<(unsigned)(ntiles * OZ_TN), 256, 0, s>>>(Bt.p, Bt.rs, Bt.cs, n, k, OZ_TN, ntiles, kchunks, bp,
+                                                           sb);
+    DDLA_LAUNCHED();
+    OzArgs a{m, n, kchunks, mtiles, ntiles, ap, bp, sa, sb, alpha, beta, C.p, C.rs, C.cs, uplo,
+              h->d_info + INFO_TIMEOUT};
+    k_oz_gemm<<<dim3((unsigned)ntiles, (unsigned)mtiles), TC_THREADS, OZ_SMEM, s>>>(a);
+    DDLA_LAUNCHED();
+    return 0;
 }
 
 }  // namespace ddla

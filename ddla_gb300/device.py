@@ -33,11 +33,17 @@ class Handle:
     def sync(self):
         check(lib().ddla_handle_sync(self.h), "handle_sync")
 
-    def gemm(self, alpha, A, B, beta, Cm, ta=0, tb=0):
+    def gemm(self, alpha, A, B, beta, Cm, ta=0, tb=0, precision=None):
+        """C = alpha op(A) op(B) + beta C; precision PREC_OZAKI selects the
+        split BF16 tensor-core GEMM (FP64-level accuracy)."""
         m, n = Cm.shape
         k = A.shape[0] if ta else A.shape[1]
-        check(lib().ddla_dev_dgemm(self.h, ta, tb, m, n, k, alpha, _p(A), *_st(A), _p(B), *_st(B), beta, _p(Cm),
-                                   *_st(Cm)), "dev_dgemm")
+        if precision is None:
+            check(lib().ddla_dev_dgemm(self.h, ta, tb, m, n, k, alpha, _p(A), *_st(A), _p(B), *_st(B), beta,
+                                       _p(Cm), *_st(Cm)), "dev_dgemm")
+        else:
+            check(lib().ddla_dev_dgemm_ex(self.h, precision, ta, tb, m, n, k, alpha, _p(A), *_st(A), _p(B),
+                                          *_st(B), beta, _p(Cm), *_st(Cm)), "dev_dgemm_ex")
 
     def gemmt(self, uplo, alpha, A, B, beta, Cm, ta=0, tb=0):
         m = Cm.shape[0]
@@ -50,18 +56,18 @@ class Handle:
         check(lib().ddla_dev_dtrsm(self.h, side, uplo, ta, diag, m, n, alpha, _p(A), *_st(A), _p(B), *_st(B)),
               "dev_dtrsm")
 
-    def getrf(self, A, piv, nb=0):
+    def getrf(self, A, piv, nb=0, precision=0):
         o = Opts()
-        o.nb = nb
+        o.nb, o.precision = nb, precision
         return lib().ddla_dev_dgetrf(self.h, A.shape[0], _p(A), *_st(A), _p(piv), C.byref(o))
 
     def getrs(self, LU, piv, B, trans=0):
         check(lib().ddla_dev_dgetrs(self.h, trans, LU.shape[0], B.shape[1], _p(LU), *_st(LU), _p(piv), _p(B),
                                     *_st(B)), "dev_dgetrs")
 
-    def potrf(self, uplo, A, nb=0):
+    def potrf(self, uplo, A, nb=0, precision=0):
         o = Opts()
-        o.nb = nb
+        o.nb, o.precision = nb, precision
         return lib().ddla_dev_dpotrf(self.h, uplo, A.shape[0], _p(A), *_st(A), C.byref(o))
 
     def potrs(self, uplo, A, B):

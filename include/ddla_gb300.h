@@ -206,6 +206,15 @@ int ddla_dev_dgemm(ddla_handle h, int32_t transa, int32_t transb, ddla_dim_t m, 
                    double alpha, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
                    const double *b, ddla_inc_t rsb, ddla_inc_t csb,
                    double beta, double *c, ddla_inc_t rsc, ddla_inc_t csc);
+/* FP64 GEMM with a selectable arithmetic: DDLA_PREC_FP64 (DMMA, same as
+ * ddla_dev_dgemm) or DDLA_PREC_OZAKI (error-free BF16 slices on the tensor
+ * cores, FP64-level accuracy: |error| <= a small multiple of 2^-53 k
+ * max_l|a_il| max_l|b_lj|).  The reference GEMM (DDLA/BLAS/Native/3m.cs:12-24)
+ * has a single FP64 arithmetic; the precision argument has no counterpart there. */
+int ddla_dev_dgemm_ex(ddla_handle h, int32_t precision, int32_t transa, int32_t transb, ddla_dim_t m, ddla_dim_t n,
+                      ddla_dim_t k, double alpha, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
+                      const double *b, ddla_inc_t rsb, ddla_inc_t csb,
+                      double beta, double *c, ddla_inc_t rsc, ddla_inc_t csc);
 int ddla_dev_dgemmt(ddla_handle h, int32_t uploc, int32_t transa, int32_t transb, ddla_dim_t m, ddla_dim_t k,
                     double alpha, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
                     const double *b, ddla_inc_t rsb, ddla_inc_t csb,
