@@ -21,6 +21,15 @@ are not credited).  A step only counts if it reaches the tolerance.
 --impl reference times that CPU restatement as the reference arm.
 --gpus N (torchrun, one rank per GPU) runs N independent replicas: the solve
 does not shard across devices.
+
+--workload selects one of the other configurations instead (device-resident
+timing lines used for the per-kernel measurements and profiles; the default
+is the headline LU solve):
+  gemm      C = A B + 0.5 C, 1024^3, U[-1,1]      (--precision fp64 | ozaki)
+  chol      SPD G G^T/n + I, n = 16384, 16 RHS    (--precision fp32 | fp64 | ...)
+  batched   20,000 LU / Cholesky solves, n ~ U{8..256}  (--precision fp32 | fp64)
+  einsum-a  'bik,bkj->bij', b = 512, 256^3, U[-1,1]  (--precision fp64 | ozaki)
+  einsum-b  'abcd,cdef->abef', all lengths 64        (--precision fp64 | ozaki)
 """
 import argparse
 import ctypes as C
@@ -51,6 +60,21 @@ def dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return rank, world, local
+
+
+def max_over_ranks(ms, world, device="cuda"):
+    """Step time of the job: the slowest rank's (all ranks get it)."""
+    if world <= 1:
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(flops_per_rank, world, ms):
+    """Whole-job GFLOP/s of `world` independent replicas (weak scaling)."""
+    return flops_per_rank * world / (ms * 1e-3) / 1e9
 
 
 class ClockSampler:
@@ -149,13 +173,221 @@ def reference_arm(args):
     print(json.dumps(out))
 
 
+class L2Flush:
+    """Writes a buffer larger than L2 (129 MB) between timed steps of
+    workloads whose inputs fit in L2."""
+
+    def __init__(self, torch, stream):
+        self.buf = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")   # 256 MB
+        self.stream = stream
+
+    def __call__(self):
+        self.buf.fill_(1.0)
+
+
+def secondary(args):
+    """Device-resident lines for the other configurations (same JSON keys)."""
+    import numpy as np
+    import torch
+    import ddla_gb300 as D
+    from ddla_gb300 import batched as bt
+    from ddla_gb300 import build as bld
+    from ddla_gb300 import device as dv
+    from ddla_gb300 import einsum as es
+    bld.build()
+    L = D.lib()
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    h = dv.Handle(stream)
+    g = torch.Generator(device="cuda").manual_seed(SEED + 10)
+    wl = args.workload
+    pname = args.precision if args.precision != "auto" else ("fp32" if wl in ("chol", "batched") else "fp64")
+    prec = {"fp32": D.PREC_FP32, "tf32x3": D.PREC_TF32X3, "bf16x3": D.PREC_BF16X3, "fp64": D.PREC_FP64,
+            "ozaki": D.PREC_OZAKI}[pname]
+    flush = None
+    check_err = None
+    bytes_alg = 0.0
+
+    def U(*shape):
+        return torch.rand(*shape, dtype=torch.float64, device="cuda", generator=g) * 2 - 1
+
+    if wl == "gemm":
+        n = 1024
+        A, B, C0 = U(n, n), U(n, n), U(n, n)
+        Cm = C0.clone()
+        flops = 2.0 * n ** 3
+        bytes_alg = 8.0 * 4 * n * n
+        flush = L2Flush(torch, stream)
+        desc = f"GEMM C = A B + 0.5 C, {n}^3 FP64 row-major U[-1,1], {pname}"
+
+        def step():
+            h.gemm(1.0, A, B, 0.5, Cm, precision=prec)
+
+        def check_err():
+            ref = A @ B + 0.5 * C0            # accuracy check only, outside the timed region
+            Cm.copy_(C0)
+            step()
+            return float(((Cm - ref).abs() / (A.abs() @ B.abs() + 0.5 * C0.abs())).max())
+    elif wl in ("einsum-a", "einsum-b"):
+        if wl == "einsum-a":
+            expr, sa, sb, sc = "bik,bkj->bij", (512, 256, 256), (512, 256, 256), (512, 256, 256)
+            flops = 2.0 * 512 * 256 ** 3
+        else:
+            expr, sa, sb, sc = "abcd,cdef->abef", (64,) * 4, (64,) * 4, (64,) * 4
+            flops = 2.0 * 64 ** 6
+        A, B = U(*sa), U(*sb)
+        Cm = torch.zeros(*sc, dtype=torch.float64, device="cuda")
+        bytes_alg = 8.0 * (A.numel() + B.numel() + 2 * Cm.numel())
+        d = es.plan(expr, np.empty(sa), np.empty(sb), np.empty(sc))
+        Le = es._declare()
+        flush = L2Flush(torch, stream)
+        desc = f"einsum '{expr}' {sa} x {sb}, FP64 U[-1,1], {pname}"
+
+        def step():
+            D._lib.check(Le.ddla_dev_contract(h.h, C.byref(d), 1.0, C.c_void_p(A.data_ptr()),
+                                              C.c_void_p(B.data_ptr()), C.c_void_p(Cm.data_ptr()), prec), "contract")
+
+        def check_err():
+            Cm.zero_()
+            step()
+            h.sync()
+            ref = torch.einsum(expr, A, B)
+            sc_ = torch.einsum(expr, A.abs(), B.abs())
+            return float(((Cm - ref).abs() / sc_).max())
+    elif wl == "chol":
+        n, nrhs = args.n if args.n != N_DEFAULT else 16384, 16
+        G = torch.randn(n, n, dtype=torch.float64, device="cuda", generator=g)
+        A = torch.eye(n, dtype=torch.float64, device="cuda")
+        h.gemm(1.0 / n, G, G, 1.0, A, tb=D.TRANSPOSE, precision=D.PREC_OZAKI)   # A = G G^T / n + I
+        h.sync()
+        del G
+        A = 0.5 * (A + A.T)   # exactly symmetric
+        b = torch.randn(n, nrhs, dtype=torch.float64, device="cuda", generator=g)
+        X = torch.zeros(n, nrhs, dtype=torch.float64, device="cuda")
+        flops = n ** 3 / 3.0 + 2.0 * n * n * nrhs
+        desc = f"Cholesky + solve, SPD G G^T/n + I, n={n}, {nrhs} RHS, {pname}"
+        if prec == D.PREC_FP64:
+            F = torch.empty_like(A)
+
+            def step():
+                F.copy_(A)
+                rc = h.potrf(D.LOWER, F)
+                if rc != 0:
+                    raise RuntimeError(f"potrf failed {rc}")
+                X.copy_(b)
+                h.potrs(D.LOWER, F, X)
+        else:
+            def step():
+                rc, rep = h.gesv_mixed(A, b, X, precision=prec, tol=TOL, spd=True)
+                if rc != 0 or not rep["converged"]:
+                    raise RuntimeError(f"posv_mixed failed rc={rc} rep={rep}")
+
+        def check_err():
+            step()
+            h.sync()
+            R = b - A @ X
+            an = A.abs().sum(1).max()
+            return float((R.abs().amax(0) / (an * X.abs().amax(0) + b.abs().amax(0))).max())
+    elif wl == "batched":
+        r = np.random.default_rng(SEED + 4)
+        count = 20000
+        sizes = r.integers(8, 257, count)
+        kinds = np.where(np.arange(count) % 2 == 0, 0, 2)
+        mats, rhs = [], []
+        for nn, k in zip(sizes, kinds):
+            if k == 2:
+                Gs = r.standard_normal((nn, nn))
+                mats.append(Gs @ Gs.T / nn + np.eye(nn))
+            else:
+                mats.append(r.standard_normal((nn, nn)) + nn * np.eye(nn))
+            rhs.append(r.standard_normal(nn))
+        mixed = prec != D.PREC_FP64
+        bs = bt.BatchedSolver(h, sizes, kinds, mixed=mixed, tol=TOL if mixed else 0.0)
+        bs.load(mats, rhs)
+        s3 = sizes.astype(np.float64)
+        flops = float(np.sum(np.where(kinds == 0, 2.0 / 3.0, 1.0 / 3.0) * s3 ** 3 + 2.0 * s3 ** 2))
+        bytes_alg = float(2 * 8 * np.sum(s3 ** 2))
+        desc = f"batched {count} solves (half PLU of N(0,1)+nI, half Cholesky of G G^T/n+I), n ~ U{{8..256}}, " + \
+            ("mixed fp32 + FP64 refinement" if mixed else "fp64")
+
+        def step():
+            bs.reset()
+            bs.run()
+
+        def check_err():
+            step()
+            res, info, iters = bs.results()
+            worst = 0.0
+            for i in range(0, count, 97):
+                x = res[i][1]
+                A0 = mats[i]
+                rr = rhs[i] - A0 @ x
+                worst = max(worst, np.abs(rr).max() / (np.abs(A0).sum(1).max() * np.abs(x).max() +
+                                                       np.abs(rhs[i]).max()))
+            return worst
+    else:
+        raise SystemExit(f"unknown workload {wl}")
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(0)
+    launches0 = D.kernel_launches()
+    clocks.start()
+    times = []
+    for _ in range(args.steps):
+        if flush is not None:
+            flush()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    clk = clocks.stop()
+    launches = D.kernel_launches() - launches0
+    ms = statistics.median(times)
+    value = flops / (ms * 1e-3) / 1e9
+    err = check_err() if check_err else None
+    f64_peak, f32_peak = dv.measure_peaks()
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    if prec == D.PREC_FP64:
+        roof = {"bound": "tensor", "achieved": value / 1e3, "peak": f64_peak, "unit": "TFLOP/s",
+                "frac": value / 1e3 / f64_peak, "peak_source": "live DMMA probe (ddla_measure_peaks)"}
+    elif prec == D.PREC_OZAKI:
+        roof = {"bound": "tensor", "achieved": value / 1e3, "peak": peaks.get("bf16_tflops", 1900.0) / 36.0,
+                "unit": "TFLOP/s (FP64-equivalent)", "peak_source": "MEASURED_PEAKS.json bf16_tflops / 36 slice "
+                "products (8 slices, levels 0..7)"}
+        roof["frac"] = roof["achieved"] / roof["peak"]
+    else:
+        roof = {"bound": "fp32-cuda-core", "achieved": value / 1e3, "peak": f32_peak, "unit": "TFLOP/s",
+                "frac": value / 1e3 / f32_peak, "peak_source": "live FFMA probe (ddla_measure_peaks)"}
+    roof["traffic"] = None
+    roof["note"] = "whole-step algorithmic flops / median CUDA-event step time"
+    if bytes_alg:
+        roof["hbm_gbs"] = bytes_alg / (ms * 1e-3) / 1e9
+    out = {"metric": f"{wl} GFLOP/s", "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": pname, "data": "synthetic, seeded",
+           "config": {"workload": desc, "precision": pname,
+                      "l2": "L2 flushed between steps" if flush else "inputs larger than L2"},
+           "error": err, "roofline": roof, "gpu_launches": launches, "clocks": clk,
+           "peaks_live": {"fp64_tflops": f64_peak, "fp32_tflops": f32_peak}}
+    print(json.dumps(out))
+    h.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--n", type=int, default=N_DEFAULT)
-    ap.add_argument("--precision", default="auto", choices=["auto", "fp32", "tf32x3", "bf16x3", "fp64"])
+    ap.add_argument("--precision", default="auto", choices=["auto", "fp32", "tf32x3", "bf16x3", "fp64", "ozaki"])
+    ap.add_argument("--workload", default="lu", choices=["lu", "gemm", "chol", "batched", "einsum-a", "einsum-b"])
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-n", type=int, default=4096)
     ap.add_argument("--no-cpu", action="store_true")
@@ -164,6 +396,8 @@ def main():
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return reference_arm(args)
+    if args.workload != "lu":
+        return secondary(args)
 
     import numpy as np
     import torch
@@ -219,12 +453,8 @@ def main():
     barrier()
     clk = clocks.stop()
     launches = D.kernel_launches() - launches0
-    ms = e0.elapsed_time(e1) / args.steps
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = lu_flops(n) * world / (ms * 1e-3) / 1e9
+    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, world)
+    value = replica_value(lu_flops(n), world, ms)
 
     # dominant kernel class from the per-launch CUDA-event records of the timed region
     classes = {0: "trailing_update_gemm", 1: "lu_panel", 2: "trsm", 3: "laswp", 4: "refinement"}
