@@ -22,9 +22,12 @@ import statistics
 
 from ._lib import check, lib
 
-SOLVE_GRID = {"lu.nb": [16, 32, 64], "panel.cluster": [4, 8, 16], "lu.lookahead": [0, 1]}
-BATCHED_GRID = {"batched.nb.32": [4, 8, 16, 32], "batched.nb.64": [8, 16, 32], "batched.nb.128": [16, 32],
-                "batched.nb.big": [16, 32], "batched.ctas_per_sm": [1, 2, 3, 4]}
+# The first candidate of every key is the library's automatic choice (0, or 1
+# for lu.lookahead, which is on unless set to 0): the search starts from the
+# defaults and only moves when a candidate is faster.
+SOLVE_GRID = {"lu.nb": [0, 32, 16], "panel.cluster": [0, 8], "lu.lookahead": [1, 0]}
+BATCHED_GRID = {"batched.nb.32": [0, 4, 16, 32], "batched.nb.64": [0, 8, 32], "batched.nb.128": [0, 16],
+                "batched.nb.big": [0, 16], "batched.ctas_per_sm": [0, 1, 2]}
 
 
 def tune_set(key, value):

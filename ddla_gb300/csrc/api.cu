@@ -238,7 +238,8 @@ int gemm_any(ddla_handle h, int prec, i64 m, i64 n, i64 k, T alpha, View<const T
              View<T> C, int uplo);
 
 int gemm_ozaki(ddla_handle h, i64 m, i64 n, i64 k, double alpha, View<const double> A, View<const double> B,
-               double beta, View<double> C, int uplo = DDLA_DENSE);
+               double beta, View<double> C, int uplo = DDLA_DENSE, i64 batch = 1,
+               const i64 *d_offsets = nullptr);
 
 template <>
 int gemm_any<double>(ddla_handle h, int prec, i64 m, i64 n, i64 k, double alpha, View<const double> A,

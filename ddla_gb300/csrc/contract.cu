@@ -29,7 +29,8 @@ namespace ddla {
 int gemm_f64_offsets(cudaStream_t s, i64 m, i64 n, i64 k, double alpha, View<const double> A,
                      View<const double> B, double beta, View<double> C, i64 batch, const i64 *d_offsets);
 int gemm_ozaki(ddla_handle h, i64 m, i64 n, i64 k, double alpha, View<const double> A, View<const double> B,
-               double beta, View<double> C, int uplo = DDLA_DENSE);
+               double beta, View<double> C, int uplo = DDLA_DENSE, i64 batch = 1,
+               const i64 *d_offsets = nullptr);
 
 namespace {
 
@@ -264,11 +265,7 @@ int contract_exec(ddla_handle h, const ddla_contract_desc *d, double alpha, cons
             if (prec == DDLA_PREC_FP64) {
                 DDLA_TRY(gemm_f64_offsets(s, M, N, K, alpha, Av, Bv, 1.0, Cv, npar, dtab));
             } else {
-                for (i64 p = 0; p < npar; p++) {
-                    View<const double> Ap{Av.p + poa[p], M, K, Av.rs, Av.cs}, Bp{Bv.p + pob[p], K, N, Bv.rs, Bv.cs};
-                    View<double> Cp{Cv.p + poc[p], M, N, Cv.rs, Cv.cs};
-                    DDLA_TRY(gemm_ozaki(h, M, N, K, alpha, Ap, Bp, 1.0, Cp));
-                }
+                DDLA_TRY(gemm_ozaki(h, M, N, K, alpha, Av, Bv, 1.0, Cv, DDLA_DENSE, npar, dtab));
             }
         }
         DDLA_CUDA(cudaStreamSynchronize(s));   // the host offset vectors go out of scope

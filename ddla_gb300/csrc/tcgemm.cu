@@ -369,9 +369,15 @@ __host__ __device__ constexpr uint32_t oz_idesc() {
 // BF16 slices.  One block per padded row (row tiles of `tr` rows); the scale
 // 2^e of each row goes to scale[r] (non-finite rows store their max, which
 // makes the row of the result non-finite).
+// Batched: blockIdx.y selects the product; X is offset by offs[3 y + which]
+// (when offs is given) and pack / scale by whole items.
 __global__ void k_oz_split(const double *X, i64 rs, i64 cs, i64 rows, i64 cols, int tr, i64 row_tiles,
-                           i64 kchunks, __nv_bfloat16 *pack, double *scale) {
+                           i64 kchunks, __nv_bfloat16 *pack, double *scale, const i64 *offs, int which,
+                           i64 pack_item, i64 scale_item) {
     const i64 r = blockIdx.x;
+    if (offs) X += offs[3 * (i64)blockIdx.y + which];
+    pack += (i64)blockIdx.y * pack_item;
+    scale += (i64)blockIdx.y * scale_item;
     __shared__ unsigned long long red[32];
     const bool live = r < rows;
     // row max of |x| on the integer pipe: for non-negative doubles the bit
@@ -447,6 +453,8 @@ struct OzArgs {
     double alpha, beta;
     double *C;
     int64_t rsc, csc;
+    const int64_t *offs;            // batched: C offset of product z at offs[3 z + 2]
+    int64_t a_item, b_item, s_item_a, s_item_b;   // element strides between products
     int uplo;   // DDLA_DENSE, or the triangle of C that is written (GEMMT)
     int *err;
 };
@@ -457,7 +465,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_oz_gemm(OzArgs g) {
     __shared__ __align__(8) unsigned long long mbar;
     __shared__ unsigned tmem_slot;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int64_t mt = blockIdx.y, nt = blockIdx.x;
+    const int64_t mt = blockIdx.y, nt = blockIdx.x, bz = blockIdx.z;
+    const __nv_bfloat16 *Ap = g.Ap + bz * g.a_item, *Bp = g.Bp + bz * g.b_item;
+    const double *sa = g.sa + bz * g.s_item_a, *sb = g.sb + bz * g.s_item_b;
+    double *Cz = g.C + (g.offs ? g.offs[3 * bz + 2] : 0);
     const int64_t m0 = mt * TM, n0 = nt * OZ_TN;
     if (g.uplo == DDLA_LOWER && n0 > m0 + TM - 1) return;
     if (g.uplo == DDLA_UPPER && m0 > n0 + OZ_TN - 1) return;
@@ -489,9 +500,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_oz_gemm(OzArgs g) {
     const size_t b_stride = (size_t)g.ntiles * g.kchunks * (OZ_TN * OZ_KC);
     for (int64_t c = 0; c < g.kchunks; c++) {
         {   // stage every slice of this chunk: contiguous 16-byte copies
-            const uint4 *srcA = reinterpret_cast<const uint4 *>(g.Ap + ((size_t)mt * g.kchunks + c) * (TM * OZ_KC));
+            const uint4 *srcA = reinterpret_cast<const uint4 *>(Ap + ((size_t)mt * g.kchunks + c) * (TM * OZ_KC));
             const uint4 *srcB =
-                reinterpret_cast<const uint4 *>(g.Bp + ((size_t)nt * g.kchunks + c) * (OZ_TN * OZ_KC));
+                reinterpret_cast<const uint4 *>(Bp + ((size_t)nt * g.kchunks + c) * (OZ_TN * OZ_KC));
             constexpr int AV = OZ_A_TILE / 16, BV = OZ_B_TILE / 16;
             for (int e = tid; e < OZ_S * AV; e += TC_THREADS) {
                 const int t = e / AV, o = e % AV;
@@ -575,15 +586,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_oz_gemm(OzArgs g) {
             const int64_t gr = m0 + 32 * q + lane;
             const double *row = stage + (32 * q + lane) * (OZ_TN + 1);
             if (gr < g.m) {
-                const double sr = g.sa[gr] * g.alpha * 0x1p-14;
+                const double sr = sa[gr] * g.alpha * 0x1p-14;
 #pragma unroll
                 for (int j = 0; j < OZ_TN; j++) {
                     const int64_t gc = n0 + j;
                     if (gc >= g.n) continue;
                     if (g.uplo == DDLA_LOWER && gc > gr) continue;
                     if (g.uplo == DDLA_UPPER && gc < gr) continue;
-                    const double v = ((acc[j] + row[j]) * sr) * g.sb[gc];
-                    double *cp = g.C + gr * g.rsc + gc * g.csc;
+                    const double v = ((acc[j] + row[j]) * sr) * sb[gc];
+                    double *cp = Cz + gr * g.rsc + gc * g.csc;
                     *cp = (g.beta == 0.0) ? v : fma(g.beta, *cp, v);
                 }
             }
@@ -604,10 +615,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_oz_gemm(OzArgs g) {
 }  // namespace
 
 int gemm_ozaki(ddla_handle h, i64 m, i64 n, i64 k, double alpha, View<const double> A, View<const double> B,
-               double beta, View<double> C, int uplo) {
-    if (m <= 0 || n <= 0) return 0;
+               double beta, View<double> C, int uplo, i64 batch, const i64 *d_offsets) {
+    if (m <= 0 || n <= 0 || batch <= 0) return 0;
     cudaStream_t s = h->stream;
-    if (k <= 0 || alpha == 0.0) return gemm_f64(s, m, n, 0, 0.0, A, B, beta, C, uplo);
+    if (k <= 0 || alpha == 0.0) {
+        if (batch == 1 && !d_offsets) return gemm_f64(s, m, n, 0, 0.0, A, B, beta, C, uplo);
+        if (beta == 1.0) return 0;
+        set_error("gemm_ozaki: batched beta scaling with k = 0 is not supported");
+        return DDLA_ERR_UNSUPPORTED;
+    }
     static size_t avail = 0;
     if (!avail) DDLA_TRY(max_dyn_smem((const void *)k_oz_gemm, h->smem_optin, &avail));
     if (OZ_SMEM > avail) {
@@ -616,23 +632,32 @@ int gemm_ozaki(ddla_handle h, i64 m, i64 n, i64 k, double alpha, View<const doub
     }
     const i64 mtiles = (m + TM - 1) / TM, ntiles = (n + OZ_TN - 1) / OZ_TN, kchunks = (k + OZ_KC - 1) / OZ_KC;
     if (mtiles > 65535) { set_error("gemm_ozaki: m too large"); return DDLA_ERR_UNSUPPORTED; }
-    const size_t abytes = (size_t)OZ_S * mtiles * TM * kchunks * OZ_KC * 2;
-    const size_t bbytes = (size_t)OZ_S * ntiles * OZ_TN * kchunks * OZ_KC * 2;
+    const i64 a_item = (i64)OZ_S * mtiles * TM * kchunks * OZ_KC, b_item = (i64)OZ_S * ntiles * OZ_TN * kchunks * OZ_KC;
+    const i64 sa_item = mtiles * TM, sb_item = ntiles * OZ_TN;
+    // products in groups of at most 65535 (grid y / z limit), packed slices of one group at a time
+    const i64 group = batch < 65535 ? batch : 65535;
     void *wa, *wb;
-    DDLA_TRY(workspace(h, WS_TC, abytes + sizeof(double) * mtiles * TM, &wa));
-    DDLA_TRY(workspace(h, WS_TC2, bbytes + sizeof(double) * ntiles * OZ_TN, &wb));
+    DDLA_TRY(workspace(h, WS_TC, (size_t)group * (a_item * 2 + sa_item * 8), &wa));
+    DDLA_TRY(workspace(h, WS_TC2, (size_t)group * (b_item * 2 + sb_item * 8), &wb));
     __nv_bfloat16 *ap = (__nv_bfloat16 *)wa, *bp = (__nv_bfloat16 *)wb;
-    double *sa = (double *)((char *)wa + abytes), *sb = (double *)((char *)wb + bbytes);
-    k_oz_split<<<(unsigned)(mtiles * TM), 256, 0, s>>>(A.p, A.rs, A.cs, m, k, TM, mtiles, kchunks, ap, sa);
-    DDLA_LAUNCHED();
+    double *sa = (double *)((char *)wa + (size_t)group * a_item * 2);
+    double *sb = (double *)((char *)wb + (size_t)group * b_item * 2);
     View<const double> Bt = B.t();   // columns of B as rows
-    k_oz_split<<<(unsigned)(ntiles * OZ_TN), 256, 0, s>>>(Bt.p, Bt.rs, Bt.cs, n, k, OZ_TN, ntiles, kchunks, bp,
-                                                           sb);
-    DDLA_LAUNCHED();
-    OzArgs a{m, n, kchunks, mtiles, ntiles, ap, bp, sa, sb, alpha, beta, C.p, C.rs, C.cs, uplo,
-              h->d_info + INFO_TIMEOUT};
-    k_oz_gemm<<<dim3((unsigned)ntiles, (unsigned)mtiles), TC_THREADS, OZ_SMEM, s>>>(a);
-    DDLA_LAUNCHED();
+    for (i64 z0 = 0; z0 < batch; z0 += group) {
+        const i64 nz = batch - z0 < group ? batch - z0 : group;
+        const i64 *offs = d_offsets ? d_offsets + 3 * z0 : nullptr;
+        k_oz_split<<<dim3((unsigned)(mtiles * TM), (unsigned)nz), 256, 0, s>>>(A.p, A.rs, A.cs, m, k, TM, mtiles,
+                                                                              kchunks, ap, sa, offs, 0, a_item,
+                                                                              sa_item);
+        DDLA_LAUNCHED();
+        k_oz_split<<<dim3((unsigned)(ntiles * OZ_TN), (unsigned)nz), 256, 0, s>>>(
+            Bt.p, Bt.rs, Bt.cs, n, k, OZ_TN, ntiles, kchunks, bp, sb, offs, 1, b_item, sb_item);
+        DDLA_LAUNCHED();
+        OzArgs a{m, n, kchunks, mtiles, ntiles, ap, bp, sa, sb, alpha, beta, C.p, C.rs, C.cs, offs,
+                 a_item, b_item, sa_item, sb_item, uplo, h->d_info + INFO_TIMEOUT};
+        k_oz_gemm<<<dim3((unsigned)ntiles, (unsigned)mtiles, (unsigned)nz), TC_THREADS, OZ_SMEM, s>>>(a);
+        DDLA_LAUNCHED();
+    }
     return 0;
 }
 
