@@ -104,10 +104,16 @@ namespace ddla {
 //   WS_X       device pivots                   WS_MISC TRSV flags, permutations
 //   WS_TRI     inverted diagonal blocks        WS_Y    LDL^T Y block
 //   WS_PERM    row permutation kept by getrf   WS_TC   tensor-core split operands
+//   WS_INV     inverted diagonal blocks of a factorization, kept for all of
+//              its refinement solves
+//   WS_PINV    inverses of the LU panels' L11 blocks (two, by panel parity)
 enum WsSlot {
     WS_A = 0, WS_B = 1, WS_C = 2, WS_TMP = 3, WS_PIV = 4, WS_F32 = 5, WS_X = 6, WS_MISC = 7,
-    WS_TRI = 8, WS_Y = 9, WS_PERM = 10, WS_TC = 11, WS_TC2 = 12
+    WS_TRI = 8, WS_Y = 9, WS_PERM = 10, WS_TC = 11, WS_TC2 = 12, WS_INV = 13, WS_PINV = 14
 };
+
+// Order of the diagonal blocks that the triangular solves invert.
+constexpr int TRI_TB = 64;
 
 // Raises the kernel's dynamic shared-memory limit to everything the device
 // allows beside its static shared memory; returns that limit in *avail.

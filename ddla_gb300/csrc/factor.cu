@@ -20,7 +20,10 @@ namespace ddla {
 template <typename T>
 int panel_width_for(ddla_handle h, i64 m);
 template <typename T>
-int panel_factor(ddla_handle h, cudaStream_t s, View<T> X, i64 pc, int w, int32_t *d_piv, i64 row_base, int *d_info);
+int panel_factor(ddla_handle h, cudaStream_t s, View<T> X, i64 pc, int w, int32_t *d_piv, i64 row_base, int *d_info,
+                 T *inv);
+template <typename T>
+int copy2d_on(cudaStream_t s, View<const T> X, View<T> Y);
 template <typename T>
 int panel_swap_rest(ddla_handle h, View<T> X, i64 pc, int w, int *perm);
 template <typename T>
@@ -194,9 +197,29 @@ int getrf(ddla_handle h, i64 n, View<T> A, int32_t *d_piv, int prec, int nb, int
         DDLA_CUDA(cudaEventCreateWithFlags(&h->ev_ready, cudaEventDisableTiming));
         DDLA_CUDA(cudaEventCreateWithFlags(&h->ev_panel, cudaEventDisableTiming));
     }
+    // the panel kernel also forms inv(L11) (double-buffered by panel parity:
+    // panel k+1 writes its inverse while the main stream still uses panel k's)
+    T *pinv;
+    DDLA_TRY(workspace(h, WS_PINV, sizeof(T) * 2 * TRI_TB * TRI_TB, (void **)&pinv));
+    auto inv_of = [&](i64 j0) { return pinv + ((j0 / w) & 1) * TRI_TB * TRI_TB; };
     auto panel = [&](cudaStream_t st, i64 j0, int b) -> int {
         Timed t(st, TC_PANEL, 2.0 * b * b * ((n - j0) - b / 3.0), 2.0 * sizeof(T) * (n - j0) * (double)b);
-        return panel_factor<T>(h, st, A.sub(j0, n - j0, 0, n), j0, b, d_piv + j0, j0, h->d_info + INFO_PIVOT);
+        return panel_factor<T>(h, st, A.sub(j0, n - j0, 0, n), j0, b, d_piv + j0, j0, h->d_info + INFO_PIVOT,
+                               inv_of(j0));
+    };
+    // U12 columns [c, c + nc) of the row block of panel j0: inv(L11) times a
+    // copy of them (the same blocked inverse the general TRSM applies)
+    const int tprec = sizeof(T) == 8 ? DDLA_PREC_FP64 : DDLA_PREC_FP32;
+    T *tmp;
+    DDLA_TRY(workspace(h, WS_TMP, sizeof(T) * (size_t)w * n, (void **)&tmp));
+    auto u12 = [&](i64 j0, int b, i64 c, i64 nc) -> int {
+        if (nc <= 0) return 0;
+        Timed t(s, TC_TRSM, (double)b * b * nc, sizeof(T) * (2.0 * b * nc + b * b));
+        View<T> blk = A.sub(j0, b, c, nc);
+        View<T> Tm{tmp + c, b, nc, n, 1};
+        DDLA_TRY(copy2d_on<T>(s, View<const T>{blk.p, b, nc, blk.rs, blk.cs}, Tm));
+        return gemm_any<T>(h, tprec, b, nc, b, T(1), View<const T>{inv_of(j0), b, b, TRI_TB, 1},
+                           View<const T>{Tm.p, b, nc, n, 1}, T(0), blk, DDLA_DENSE);
     };
     DDLA_TRY(panel(s, 0, (int)(n < w ? n : w)));
     for (i64 j0 = 0; j0 < n; j0 += w) {
@@ -204,17 +227,13 @@ int getrf(ddla_handle h, i64 n, View<T> A, int32_t *d_piv, int prec, int nb, int
         DDLA_TRY(panel_swap_rest<T>(h, A.sub(j0, n - j0, 0, n), j0, b, d_perm ? d_perm + j0 : nullptr));
         const i64 r = n - j0 - b;
         if (r <= 0) break;
-        View<const T> A11{A.p + j0 * A.rs + j0 * A.cs, b, b, A.rs, A.cs};
         View<T> A12 = A.sub(j0, b, j0 + b, r);
-        {
-            Timed t(s, TC_TRSM, (double)b * b * r, sizeof(T) * (2.0 * b * r + b * b));
-            DDLA_TRY(trsm<T>(h, DDLA_LEFT, DDLA_LOWER, DDLA_NO_TRANSPOSE, DDLA_UNIT_DIAG, b, r, T(1), A11, A12));
-        }
         View<const T> A21{A.p + (j0 + b) * A.rs + j0 * A.cs, r, b, A.rs, A.cs};
         const i64 j1 = j0 + b;
         const int b1 = (int)(r < w ? r : w);
         if (ahead) {
-            // next panel's columns first
+            // next panel's columns first: their U12 part, then their update
+            DDLA_TRY(u12(j0, b, j1, b1));
             {
                 Timed t(s, TC_UPDATE, 2.0 * r * b1 * b, sizeof(T) * (2.0 * r * b1 + r * b + b * b1));
                 DDLA_TRY(gemm_any<T>(h, prec, r, b1, b, T(-1), A21, View<const T>{A12.p, b, b1, A12.rs, A12.cs}, T(1),
@@ -226,6 +245,7 @@ int getrf(ddla_handle h, i64 n, View<T> A, int32_t *d_piv, int prec, int nb, int
             DDLA_CUDA(cudaEventRecord(h->ev_panel, h->side));
             const i64 rest = r - b1;
             if (rest > 0) {
+                DDLA_TRY(u12(j0, b, j1 + b1, rest));
                 Timed t(s, TC_UPDATE, 2.0 * r * rest * b, sizeof(T) * (2.0 * r * rest + r * b + b * rest));
                 DDLA_TRY(gemm_any<T>(h, prec, r, rest, b, T(-1), A21,
                                      View<const T>{A12.p + b1 * A12.cs, b, rest, A12.rs, A12.cs}, T(1),
@@ -233,6 +253,7 @@ int getrf(ddla_handle h, i64 n, View<T> A, int32_t *d_piv, int prec, int nb, int
             }
             DDLA_CUDA(cudaStreamWaitEvent(s, h->ev_panel, 0));
         } else {
+            DDLA_TRY(u12(j0, b, j1, r));
             {
                 View<const T> cA12{A12.p, b, r, A12.rs, A12.cs};
                 Timed t(s, TC_UPDATE, 2.0 * r * r * b, sizeof(T) * (2.0 * r * r + 2.0 * r * b));

@@ -48,6 +48,7 @@ struct PanelArgs {
     int *info;
     i64 row_base;
     int *touch_count, *touch_rows, *touch_src;
+    T *inv;   // optional: inverse of the unit-lower w x w block L11 (row-major, ld TRI_TB)
 };
 
 // Pivot search keys: |x| as an unsigned integer bit pattern plus one, NaN as
@@ -292,6 +293,27 @@ __global__ void __launch_bounds__(PANEL_THREADS) k_panel_lu(PanelArgs<T> a) {
     }
     // All DSMEM traffic must finish before any CTA of the cluster exits.
     cluster.sync();
+    if (a.inv && rank == 0) {
+        // inverse of the unit-lower L11 (rows 0..kmax-1 are this CTA's first
+        // rows): warp v forms columns v, v+16, .. by forward substitution, the
+        // lanes owning rows lane and lane+32; the column's solved entry y_k is
+        // broadcast with a shuffle
+        const int lane = tid & 31, wv = tid >> 5;
+        for (int c0 = wv; c0 < TRI_TB; c0 += PANEL_THREADS / 32) {
+            T y0 = (lane == c0) ? T(1) : T(0), y1 = (lane + 32 == c0) ? T(1) : T(0);
+            if (c0 < kmax) {
+                for (int k = c0; k < kmax - 1; k++) {
+                    const T yk = __shfl_sync(0xffffffffu, k < 32 ? y0 : y1, k & 31);
+                    if (lane > k && lane < kmax) y0 = fma(-rows[lane * WP + k], yk, y0);
+                    if (lane + 32 > k && lane + 32 < kmax) y1 = fma(-rows[(lane + 32) * WP + k], yk, y1);
+                }
+            } else {
+                y0 = y1 = T(0);
+            }
+            a.inv[lane * TRI_TB + c0] = lane < kmax ? y0 : T(0);
+            a.inv[(lane + 32) * TRI_TB + c0] = lane + 32 < kmax ? y1 : T(0);
+        }
+    }
     for (int e = tid; e < nloc * w; e += PANEL_THREADS) {
         int l = e / w, c = e % w;
         a.P[(i64)(base + l) * a.rs + (i64)c * a.cs] = rows[l * WP + c];
@@ -371,12 +393,22 @@ __global__ void __launch_bounds__(1024) k_panel_lu_global(PanelArgs<T> a, int *o
 // Gather-then-scatter of the touched rows for the columns outside the panel:
 // columns c' in [0, ncols) map to c' (c' < skip0) or c' + skipw.
 constexpr int LASWP_MAXT = 2 * PANEL_WMAX;
+// With perm given, the last block applies the same interchanges to the
+// permutation vector.
 template <typename T>
 __global__ void __launch_bounds__(256)
     k_laswp_list(T *X, i64 rs, i64 cs, i64 ncols, i64 skip0, i64 skipw, const int *count, const int *rows,
-                 const int *src) {
+                 const int *src, int *perm) {
     __shared__ T tmp[LASWP_MAXT][32];
     const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    if (perm && blockIdx.x == gridDim.x - 1) {
+        __shared__ int tp[LASWP_MAXT];
+        const int cnt = *count;
+        for (int t = threadIdx.x; t < cnt; t += 256) tp[t] = perm[src[t]];
+        __syncthreads();
+        for (int t = threadIdx.x; t < cnt; t += 256) perm[rows[t]] = tp[t];
+        return;
+    }
     i64 cc = (i64)blockIdx.x * 32 + lane;
     const int cnt = *count;
     const bool ok = cc < ncols;
@@ -485,8 +517,13 @@ int panel_width_for(ddla_handle h, i64 m) {
 // stream s: relative pivots into d_piv[0..w) and the touched-row list into
 // the WS_PIV scratch, which panel_swap_rest consumes.
 template <typename T>
+int tri_inverse_on(cudaStream_t s, bool lower, bool unit, View<const T> A, i64 n, T *inv);
+
+// inv (optional, TRI_TB x TRI_TB): receives the inverse of the panel's
+// unit-lower diagonal block L11 (zeros outside it), for the row-block solve.
+template <typename T>
 int panel_factor(ddla_handle h, cudaStream_t s, View<T> X, i64 pc, int w, int32_t *d_piv, i64 row_base,
-                 int *d_info) {
+                 int *d_info, T *inv) {
     const i64 m = X.rows;
     int *tbuf;
     DDLA_TRY(workspace(h, WS_PIV, sizeof(int) * (size_t)(1 + 2 * LASWP_MAXT + m), (void **)&tbuf));
@@ -503,6 +540,7 @@ int panel_factor(ddla_handle h, cudaStream_t s, View<T> X, i64 pc, int w, int32_
     a.touch_count = tcount;
     a.touch_rows = trows;
     a.touch_src = tsrc;
+    a.inv = inv;
     int cs = max_cluster<T>(h);
     if (cs <= 0) return cs < 0 ? cs : DDLA_ERR_UNSUPPORTED;
     const int64_t want = tune_get("panel.cluster", 0);
@@ -536,6 +574,10 @@ int panel_factor(ddla_handle h, cudaStream_t s, View<T> X, i64 pc, int w, int32_
         a.rows_per = (int)m;
         k_panel_lu_global<T><<<1, 1024, 0, s>>>(a, origin);
         DDLA_LAUNCHED();
+        if (inv) {
+            const i64 k = m < w ? m : w;
+            DDLA_TRY(tri_inverse_on<T>(s, true, true, View<const T>{X.p + pc * X.cs, k, k, X.rs, X.cs}, k, inv));
+        }
     }
     return 0;
 }
@@ -549,14 +591,11 @@ int panel_swap_rest(ddla_handle h, View<T> X, i64 pc, int w, int *perm) {
     DDLA_TRY(workspace(h, WS_PIV, sizeof(int) * (size_t)(1 + 2 * LASWP_MAXT + X.rows), (void **)&tbuf));
     int *tcount = tbuf, *trows = tbuf + 1, *tsrc = tbuf + 1 + LASWP_MAXT;
     i64 other = X.cols - w;
-    if (other > 0) {
-        unsigned grid = (unsigned)((other + 31) / 32);
-        k_laswp_list<T><<<grid, 256, 0, s>>>(X.p, X.rs, X.cs, other, pc, w, tcount, trows, tsrc);
-        DDLA_LAUNCHED();
-    }
-    if (perm) {
-        // the permutation vector rides along as one more column
-        k_laswp_list<int><<<1, 256, 0, s>>>(perm, 1, 0, 1, 1, 0, tcount, trows, tsrc);
+    unsigned grid = (unsigned)((other > 0 ? other + 31 : 0) / 32) + (perm ? 1u : 0u);
+    if (grid > 0) {
+        // the permutation vector, when given, rides along in one more block
+        k_laswp_list<T><<<grid, 256, 0, s>>>(X.p, X.rs, X.cs, other > 0 ? other : 0, pc, w, tcount, trows, tsrc,
+                                             perm);
         DDLA_LAUNCHED();
     }
     return 0;
@@ -607,8 +646,9 @@ int apply_perm(ddla_handle h, View<T> B, const int32_t *d_piv, i64 n, bool forwa
 
 template int panel_width_for<double>(ddla_handle, i64);
 template int panel_width_for<float>(ddla_handle, i64);
-template int panel_factor<double>(ddla_handle, cudaStream_t, View<double>, i64, int, int32_t *, i64, int *);
-template int panel_factor<float>(ddla_handle, cudaStream_t, View<float>, i64, int, int32_t *, i64, int *);
+template int panel_factor<double>(ddla_handle, cudaStream_t, View<double>, i64, int, int32_t *, i64, int *,
+                                  double *);
+template int panel_factor<float>(ddla_handle, cudaStream_t, View<float>, i64, int, int32_t *, i64, int *, float *);
 template int panel_swap_rest<double>(ddla_handle, View<double>, i64, int, int *);
 template int panel_swap_rest<float>(ddla_handle, View<float>, i64, int, int *);
 template int permute_rows<double>(ddla_handle, View<double>, const int *, i64, bool);

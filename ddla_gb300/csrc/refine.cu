@@ -230,8 +230,19 @@ int mixed_lu(ddla_handle h, i64 n, i64 nrhs, const double *A, const double *B, d
     rep->factor_ms = ms;
     rep->info = info;
     if (info) return info;
+    // the inverted diagonal blocks of L and U are formed once and serve every
+    // correction solve: d <- U^-1 L^-1 P d
+    const View<const float> F{A32, n, n, n, 1};
+    const i64 nblk = (n + TRI_TB - 1) / TRI_TB;
+    float *invL, *invU;
+    DDLA_TRY(workspace(h, WS_INV, sizeof(float) * 2 * (size_t)nblk * TRI_TB * TRI_TB, (void **)&invL));
+    invU = invL + (size_t)nblk * TRI_TB * TRI_TB;
+    DDLA_TRY(tri_inverse<float>(h, true, true, F, n, invL));
+    DDLA_TRY(tri_inverse<float>(h, false, false, F, n, invU));
     auto solve32 = [&](float *d) {
-        return getrs_perm<float>(h, n, nr, View<const float>{A32, n, n, n, 1}, perm, View<float>{d, n, nr, nr, 1});
+        DDLA_TRY(permute_rows<float>(h, View<float>{d, n, nr, nr, 1}, perm, n, true));
+        DDLA_TRY(trsv_apply<float>(h, true, F, n, invL, d, nr, nr));
+        return trsv_apply<float>(h, false, F, n, invU, d, nr, nr);
     };
     DDLA_CUDA(cudaEventRecord(h->ev0, s));
     int rc = refine(h, n, nr, A, B, X, x_ref, opts, rep, solve32, d32, R, norms);
@@ -275,8 +286,21 @@ int mixed_chol(ddla_handle h, int uplo, i64 n, i64 nrhs, const double *A, const 
     rep->factor_ms = ms;
     rep->info = info;
     if (info) return info;
+    // A = L L^T (lower) or U^T U (upper): the first solve is with the lower
+    // triangle of F (lower) or of F^T (upper), the second with its transpose;
+    // both diagonal-block inverses are formed once for all correction solves
+    const View<const float> F{A32, n, n, n, 1};
+    const View<const float> Lv = (uplo == DDLA_LOWER) ? F : F.t();
+    const View<const float> Uv = Lv.t();
+    const i64 nblk = (n + TRI_TB - 1) / TRI_TB;
+    float *invL, *invU;
+    DDLA_TRY(workspace(h, WS_INV, sizeof(float) * 2 * (size_t)nblk * TRI_TB * TRI_TB, (void **)&invL));
+    invU = invL + (size_t)nblk * TRI_TB * TRI_TB;
+    DDLA_TRY(tri_inverse<float>(h, true, false, Lv, n, invL));
+    DDLA_TRY(tri_inverse<float>(h, false, false, Uv, n, invU));
     auto solve32 = [&](float *d) {
-        return potrs<float>(h, uplo, n, nr, View<const float>{A32, n, n, n, 1}, View<float>{d, n, nr, nr, 1});
+        DDLA_TRY(trsv_apply<float>(h, true, Lv, n, invL, d, nr, nr));
+        return trsv_apply<float>(h, false, Uv, n, invU, d, nr, nr);
     };
     DDLA_CUDA(cudaEventRecord(h->ev0, s));
     int rc = refine(h, n, nr, A, B, X, x_ref, opts, rep, solve32, d32, R, norms);

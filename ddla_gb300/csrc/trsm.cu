@@ -14,6 +14,8 @@
 //   * many right-hand sides: per diagonal block X1 = inv(A11) B1 and the GEMM
 //     update B2 -= A21 X1 (DDLA's managed TrSM has the same block structure
 //     with a TRSV per column, DDLA/BLAS/Managed/3m/TrSM.cs:62-122).
+#include <cooperative_groups.h>
+
 #include <mutex>
 #include <string>
 
@@ -23,7 +25,7 @@
 namespace ddla {
 namespace {
 
-constexpr int TB = 64;
+constexpr int TB = TRI_TB;
 constexpr int CHAIN_THREADS = 256;
 constexpr long long SPIN_LIMIT = 1LL << 24;
 
@@ -200,12 +202,323 @@ int scale(cudaStream_t s, T alpha, View<T> B) {
 }
 
 template <typename T>
+int copy2d(cudaStream_t s, View<const T> X, View<T> Y);
+
+}  // namespace
+
+template <typename T>
+int copy2d_on(cudaStream_t s, View<const T> X, View<T> Y) {
+    return copy2d<T>(s, X, Y);
+}
+template int copy2d_on<double>(cudaStream_t, View<const double>, View<double>);
+template int copy2d_on<float>(cudaStream_t, View<const float>, View<float>);
+
+namespace {
+
+template <typename T>
 int copy2d(cudaStream_t s, View<const T> X, View<T> Y) {
     i64 tot = X.rows * X.cols;
     if (tot == 0) return 0;
     int blocks = (int)((tot + 255) / 256 < 8192 ? (tot + 255) / 256 : 8192);
     k_copy2d<T><<<blocks, 256, 0, s>>>(X.p, X.rs, X.cs, X.rows, X.cols, Y.p, Y.rs, Y.cs);
     DDLA_LAUNCHED();
+    return 0;
+}
+
+// ------------------------------------------------------------------ cluster solve
+//
+// Whole-system solve with <= NR right-hand sides on ONE thread-block cluster
+// (up to 16 CTAs).  Logical block l (block row l of a lower triangle, block
+// row nblk-1-l of an upper one) belongs to CTA l % CS.  Every CTA keeps a copy
+// of the whole solution x (n x NR) and one flag per block in its shared
+// memory.  A CTA solves its blocks in increasing l, left-looking:
+//   acc = b_l;  for j < l: wait for flag j (local shared memory, bounded),
+//   acc -= A_lj x_j;  x_l = inv(A_ll) acc
+// and then pushes x_l into every CTA's copy over DSMEM and raises flag l in
+// every CTA (release at cluster scope).
+// Each warp owns 8 rows of the block: it streams its own rows of the tiles
+// A_lj and of the inverted diagonal block through its own ring of
+// shared-memory stages (cp.async, STAGES-1 items ahead, in consumption
+// order) and updates its own rows of acc, so the tile loop needs no CTA-wide
+// barrier; the CTA synchronises only around the inverse, once per block.
+constexpr int CL_THREADS = 256;
+constexpr int CL_WARPS = CL_THREADS / 32;
+constexpr int CL_WROWS = TB / CL_WARPS;   // rows of a tile per warp
+constexpr int CL_MAXCS = 16;
+constexpr int CL_TLD = TB + 4;           // padded tile row (16-byte multiple for float and double)
+constexpr long long CL_SPIN = 1LL << 22;
+
+template <typename T> struct ClStages { static constexpr int value = sizeof(T) == 4 ? 8 : 4; };
+
+struct ClLayout {
+    size_t ring, xall, acc, flags, total;
+};
+
+template <typename T, int NR>
+__host__ __device__ inline ClLayout cl_layout(int nblk) {
+    ClLayout L;
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+        size_t at = o;
+        o = (o + bytes + 127) & ~(size_t)127;
+        return at;
+    };
+    L.ring = take(sizeof(T) * (size_t)ClStages<T>::value * TB * CL_TLD);
+    L.xall = take(sizeof(T) * (size_t)nblk * TB * NR);
+    L.acc = take(sizeof(T) * TB * NR);
+    L.flags = take(sizeof(int) * (size_t)nblk);
+    L.total = o;
+    return L;
+}
+
+__device__ __forceinline__ int ld_acquire_cluster(const int *p) {
+    int v;
+    asm volatile("ld.acquire.cluster.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void cp_async16(void *dst, const void *src, int src_bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
+                 "l"(src), "r"(src_bytes)
+                 : "memory");
+}
+template <int BYTES>
+__device__ __forceinline__ void cp_async_small(void *dst, const void *src, int src_bytes) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
+                 "l"(src), "n"(BYTES), "r"(src_bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+template <typename T, int NR>
+__global__ void __launch_bounds__(CL_THREADS)
+    k_trsv_cluster(i64 n, int nblk, const T *__restrict__ A, i64 rs, i64 cs, int lower, int vec,
+                   const T *__restrict__ inv, T *X, i64 ldx, int nr, int *err) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    constexpr int S = ClStages<T>::value;
+    const int CS = (int)cluster.num_blocks(), rank = (int)cluster.block_rank();
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5, r = t >> 2, q = t & 3;
+    extern __shared__ __align__(128) unsigned char smem[];
+    const ClLayout Ly = cl_layout<T, NR>(nblk);
+    T *ring = (T *)(smem + Ly.ring);
+    T *xall = (T *)(smem + Ly.xall);
+    T *acc = (T *)(smem + Ly.acc);
+    int *flags = (int *)(smem + Ly.flags);
+    __shared__ int s_abort;
+    auto phys = [&](int l) { return lower ? l : nblk - 1 - l; };
+    // ring item (l, j): this warp's rows of tile A_lj (j < l) or of the
+    // inverted diagonal block (j == l)
+    auto issue = [&](int l, int j, int stage) {
+        T *dst = ring + (size_t)stage * TB * CL_TLD;
+        const int row0 = warp * CL_WROWS;
+        constexpr int CPR = TB * (int)sizeof(T) / 16, EPC = 16 / (int)sizeof(T);
+        if (j == l) {   // inverse block: contiguous TB x TB, 16-byte aligned
+            const T *src = inv + (i64)phys(l) * TB * TB;
+            for (int e = lane; e < CL_WROWS * CPR; e += 32) {
+                const int row = row0 + e / CPR, ch = e % CPR;
+                cp_async16(dst + row * CL_TLD + ch * EPC, src + row * TB + ch * EPC, 16);
+            }
+            return;
+        }
+        const i64 r0 = (i64)phys(l) * TB, c0 = (i64)phys(j) * TB;
+        if (vec) {
+            for (int e = lane; e < CL_WROWS * CPR; e += 32) {
+                const int row = row0 + e / CPR, ch = e % CPR;
+                const i64 gr = r0 + row, gc = c0 + (i64)ch * EPC;
+                int bytes = 0;
+                const T *src = A;
+                if (gr < n && gc < n) {
+                    const i64 left = n - gc;
+                    bytes = (int)(left >= EPC ? 16 : left * (i64)sizeof(T));
+                    src = A + gr * rs + gc;
+                }
+                cp_async16(dst + row * CL_TLD + ch * EPC, src, bytes);
+            }
+        } else {
+            for (int e = lane; e < CL_WROWS * TB; e += 32) {
+                const int row = row0 + e / TB, col = e % TB;
+                const i64 gr = r0 + row, gc = c0 + col;
+                const bool in = gr < n && gc < n;
+                cp_async_small<sizeof(T)>(dst + row * CL_TLD + col, in ? A + gr * rs + gc * cs : A,
+                                          in ? (int)sizeof(T) : 0);
+            }
+        }
+    };
+    // producer state: item (pl, pj) in consumption order
+    int pl = rank, pj = 0;
+    auto advance = [&]() {
+        if (++pj > pl) {
+            pl += CS;
+            pj = 0;
+        }
+    };
+    for (int e = t; e < nblk; e += CL_THREADS) flags[e] = 0;
+    for (int e = t; e < nblk * TB * NR; e += CL_THREADS) xall[e] = T(0);
+    if (t == 0) s_abort = 0;
+    int produced = 0, consumed = 0;
+    for (int i = 0; i < S - 1; i++) {
+        if (pl < nblk) {
+            issue(pl, pj, produced % S);
+            advance();
+        }
+        produced++;
+        cp_async_commit();
+    }
+    cluster.sync();   // every CTA's flags are down before anyone raises one
+    // this warp's row r of a tile times x (sum over the 4 lanes of the row)
+    auto rowdot = [&](const T *tile, const T *xv, T *p) {
+#pragma unroll
+        for (int c = 0; c < NR; c++) p[c] = T(0);
+#pragma unroll
+        for (int i = 0; i < TB / 4; i++) {
+            const int k = q + 4 * i;
+            const T v = tile[r * CL_TLD + k];
+#pragma unroll
+            for (int c = 0; c < NR; c++) p[c] += v * xv[k * NR + c];
+        }
+#pragma unroll
+        for (int c = 0; c < NR; c++) {
+            p[c] += __shfl_xor_sync(0xffffffffu, p[c], 1);
+            p[c] += __shfl_xor_sync(0xffffffffu, p[c], 2);
+        }
+    };
+    auto next_item = [&]() {
+        consumed++;
+        if (pl < nblk) {
+            issue(pl, pj, produced % S);
+            advance();
+        }
+        produced++;
+        cp_async_commit();
+    };
+    for (int l = rank; l < nblk; l += CS) {
+        const i64 r0 = (i64)phys(l) * TB;
+        if (q == 0)
+#pragma unroll
+            for (int c = 0; c < NR; c++) acc[r * NR + c] = (r0 + r < n && c < nr) ? X[(r0 + r) * ldx + c] : T(0);
+        T p[NR];
+        bool bad = false;
+        for (int j = 0; j < l; j++) {
+            cp_async_wait<S - 2>();
+            long long it = 0;
+            while (ld_acquire_cluster(flags + j) == 0) {
+                if (++it > CL_SPIN || *(volatile int *)&s_abort) { bad = true; break; }
+                if (it > 64) __nanosleep(20);
+            }
+            if (__any_sync(0xffffffffu, bad)) { bad = true; break; }
+            __syncwarp();
+            rowdot(ring + (size_t)(consumed % S) * TB * CL_TLD, xall + (size_t)phys(j) * TB * NR, p);
+            next_item();
+            if (q == 0)
+#pragma unroll
+                for (int c = 0; c < NR; c++) acc[r * NR + c] -= p[c];
+        }
+        if (bad && lane == 0) {
+            atomicExch(err, 1);
+            s_abort = 1;
+        }
+        __syncthreads();   // every row of acc is final (or some warp gave up)
+        if (s_abort) break;
+        cp_async_wait<S - 2>();
+        __syncwarp();
+        rowdot(ring + (size_t)(consumed % S) * TB * CL_TLD, acc, p);   // x_l = inv(A_ll) acc
+        next_item();
+        const int pb = phys(l);
+        __syncthreads();   // everyone is done reading acc
+        if (q == 0) {
+#pragma unroll
+            for (int c = 0; c < NR; c++) acc[r * NR + c] = p[c];
+            if (r0 + r < n)
+                for (int c = 0; c < nr; c++) X[(r0 + r) * ldx + c] = p[c];
+        }
+        __syncthreads();
+        for (int e = t; e < CS * TB * NR; e += CL_THREADS) {
+            const int dst = e / (TB * NR), k = e % (TB * NR);
+            cluster.map_shared_rank(xall, dst)[(size_t)pb * TB * NR + k] = acc[k];
+        }
+        asm volatile("fence.acq_rel.cluster;" ::: "memory");
+        __syncthreads();
+        if (t < CS) {
+            int *f = cluster.map_shared_rank(flags, t) + l;   // flags are indexed by logical block
+            asm volatile("st.relaxed.cluster.b32 [%0], %1;" ::"l"(f), "r"(1) : "memory");
+        }
+    }
+    cp_async_wait<0>();
+    __syncthreads();
+    cluster.sync();   // no CTA leaves while another may still write or read its shared memory
+}
+
+template <typename T, int NR>
+struct ClusterCfg {
+    static int cs;       // cluster size chosen (0 = not probed, -1 = unusable)
+    static size_t avail;
+};
+template <typename T, int NR> int ClusterCfg<T, NR>::cs = 0;
+template <typename T, int NR> size_t ClusterCfg<T, NR>::avail = 0;
+
+// Cluster size for the cluster solve of nblk blocks (0 when it cannot run).
+template <typename T, int NR>
+int cluster_size(ddla_handle h, int nblk) {
+    if (tune_get("trsv.cluster", 1) == 0) return 0;
+    if (ClusterCfg<T, NR>::cs == 0) {
+        ClusterCfg<T, NR>::cs = -1;
+        if (cudaFuncSetAttribute(k_trsv_cluster<T, NR>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+                cudaSuccess ||
+            max_dyn_smem((const void *)k_trsv_cluster<T, NR>, h->smem_optin, &ClusterCfg<T, NR>::avail) != 0) {
+            cudaGetLastError();
+            return 0;
+        }
+        for (int c = CL_MAXCS; c >= 2; c /= 2) {
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(c);
+            cfg.blockDim = dim3(CL_THREADS);
+            cfg.dynamicSmemBytes = cl_layout<T, NR>(1).total;
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeClusterDimension;
+            attr[0].val.clusterDim.x = c;
+            attr[0].val.clusterDim.y = 1;
+            attr[0].val.clusterDim.z = 1;
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+            int nc = 0;
+            if (cudaOccupancyMaxActiveClusters(&nc, (const void *)k_trsv_cluster<T, NR>, &cfg) == cudaSuccess &&
+                nc > 0) {
+                ClusterCfg<T, NR>::cs = c;
+                break;
+            }
+            cudaGetLastError();
+        }
+    }
+    int c = ClusterCfg<T, NR>::cs;
+    if (c <= 0) return 0;
+    const int want = (int)tune_get("trsv.cluster.size", 0);
+    if (want >= 2 && want < c) c = want;
+    if (cl_layout<T, NR>(nblk).total > ClusterCfg<T, NR>::avail) c = 0;
+    return c;
+}
+
+template <typename T, int NR>
+int cluster_solve(ddla_handle h, int cs, i64 n, int nblk, View<const T> A, bool lower, const T *inv, T *X, i64 ldx,
+                  int nr) {
+    const bool vec = A.cs == 1 && (A.rs * (i64)sizeof(T)) % 16 == 0 && (((uintptr_t)A.p) & 15) == 0;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(cs);
+    cfg.blockDim = dim3(CL_THREADS);
+    cfg.dynamicSmemBytes = cl_layout<T, NR>(nblk).total;
+    cfg.stream = h->stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = cs;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    DDLA_CUDA(cudaLaunchKernelEx(&cfg, k_trsv_cluster<T, NR>, n, nblk, A.p, A.rs, A.cs, lower ? 1 : 0, vec ? 1 : 0,
+                                 inv, X, ldx, nr, h->d_info + INFO_TIMEOUT));
+    count_launch();
     return 0;
 }
 
@@ -227,11 +540,18 @@ int gemm_any(ddla_handle h, int prec, i64 m, i64 n, i64 k, T alpha, View<const T
 // Inverses of the diagonal blocks of tri(A) (n x n) into inv (ceil(n/TB) *
 // TB * TB elements).
 template <typename T>
-int tri_inverse(ddla_handle h, bool lower, bool unit, View<const T> A, i64 n, T *inv) {
+int tri_inverse_on(cudaStream_t s, bool lower, bool unit, View<const T> A, i64 n, T *inv) {
     int nblk = (int)((n + TB - 1) / TB);
-    k_tri_inv<T><<<nblk, TB, 0, h->stream>>>(A.p, A.rs, A.cs, n, lower ? 1 : 0, unit ? 1 : 0, inv);
+    k_tri_inv<T><<<nblk, TB, 0, s>>>(A.p, A.rs, A.cs, n, lower ? 1 : 0, unit ? 1 : 0, inv);
     DDLA_LAUNCHED();
     return 0;
+}
+template int tri_inverse_on<double>(cudaStream_t, bool, bool, View<const double>, i64, double *);
+template int tri_inverse_on<float>(cudaStream_t, bool, bool, View<const float>, i64, float *);
+
+template <typename T>
+int tri_inverse(ddla_handle h, bool lower, bool unit, View<const T> A, i64 n, T *inv) {
+    return tri_inverse_on<T>(h->stream, lower, unit, A, n, inv);
 }
 
 // Solve tri(A) X = X in place for X row-major (n x nr, leading dim ldx),
@@ -242,7 +562,11 @@ int trsv_apply(ddla_handle h, bool lower, View<const T> A, i64 n, const T *inv, 
     int *flags;
     DDLA_TRY(workspace(h, WS_MISC, sizeof(int) * (size_t)(nblk + 1), (void **)&flags));
     DDLA_CUDA(cudaMemsetAsync(flags, 0, sizeof(int) * (size_t)(nblk + 1), h->stream));
-    if (nr <= 1) return chain<T, 1>(h, n, nblk, A, lower, inv, X, ldx, nr, flags);
+    if (nr <= 1) {
+        const int cs = cluster_size<T, 1>(h, nblk);
+        if (cs > 1 && nblk > 1) return cluster_solve<T, 1>(h, cs, n, nblk, A, lower, inv, X, ldx, nr);
+        return chain<T, 1>(h, n, nblk, A, lower, inv, X, ldx, nr, flags);
+    }
     if (nr <= 2) return chain<T, 2>(h, n, nblk, A, lower, inv, X, ldx, nr, flags);
     if (nr <= 4) return chain<T, 4>(h, n, nblk, A, lower, inv, X, ldx, nr, flags);
     if (nr <= 8) return chain<T, 8>(h, n, nblk, A, lower, inv, X, ldx, nr, flags);
