@@ -68,8 +68,10 @@ __device__ __forceinline__ unsigned long long amax_key(double v) {
     return u > 0x7ff0000000000000ull ? 0ull : u + 1ull;
 }
 
+constexpr int PANEL_SUB = 8;   // sub-panel width (deferred updates)
+
 struct PanelSmem {
-    size_t rows, origin, ucur, cand_val, cand_idx, cand_org, cand_rows, jrow, jorg, red, total;
+    size_t rows, origin, ucur, u8, pub, cand_val, cand_idx, cand_org, jorg, red, total;
 };
 
 template <typename T>
@@ -84,20 +86,22 @@ __host__ __device__ inline PanelSmem panel_smem_layout(int rows_per, int w) {
     L.rows = take(sizeof(T) * (size_t)rows_per * (w + 1));
     L.origin = take(sizeof(int) * (size_t)rows_per);
     L.ucur = take(sizeof(T) * w);
+    L.u8 = take(sizeof(T) * (size_t)w * PANEL_SUB);
+    L.pub = take(sizeof(T) * 4 * w);   // [parity][candidate | row j+1][w]
     L.cand_val = take(sizeof(typename KeyT<T>::type) * 2 * PANEL_MAXCS);
     L.cand_idx = take(sizeof(int) * 2 * PANEL_MAXCS);
     L.cand_org = take(sizeof(int) * 2 * PANEL_MAXCS);
-    L.cand_rows = take(sizeof(T) * 2 * PANEL_MAXCS * w);
-    L.jrow = take(sizeof(T) * 2 * w);
     L.jorg = take(sizeof(int) * 2);
     L.red = take((sizeof(typename KeyT<T>::type) + sizeof(int)) * (PANEL_THREADS / 32) + 16);
     L.total = o;
     return L;
 }
 
-// Block-wide first-max reduction of (key, row) pairs; result in s_val/s_idx.
+// Block-wide first-max reduction of (key, row) pairs.  Every warp reduces
+// the per-warp results itself, so all threads return the block's winner after
+// a single barrier.
 template <typename K>
-__device__ __forceinline__ void block_argmax(K bv, int bi, K *red_v, int *red_i, K *s_val, int *s_idx) {
+__device__ __forceinline__ void block_argmax(K &bv, int &bi, K *red_v, int *red_i) {
     constexpr int NW = PANEL_THREADS / 32;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
@@ -108,27 +112,43 @@ __device__ __forceinline__ void block_argmax(K bv, int bi, K *red_v, int *red_i,
     }
     if (lane == 0) { red_v[warp] = bv; red_i[warp] = bi; }
     __syncthreads();
-    if (warp == 0) {
-        bv = lane < NW ? red_v[lane] : K(0);
-        bi = lane < NW ? red_i[lane] : INT_MAX;
+    bv = lane < NW ? red_v[lane] : K(0);
+    bi = lane < NW ? red_i[lane] : INT_MAX;
 #pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            K ov = __shfl_down_sync(0xffffffffu, bv, off);
-            int oi = __shfl_down_sync(0xffffffffu, bi, off);
-            if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
-        }
-        if (lane == 0) { *s_val = bv; *s_idx = bi; }
+    for (int off = 16; off > 0; off >>= 1) {
+        K ov = __shfl_xor_sync(0xffffffffu, bv, off);
+        int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+        if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
     }
-    __syncthreads();
 }
 
-// Panel factorization, one cluster (see the file comment).  Per column the
+// 8 consecutive U8 entries (one column of the sub-panel's pivot rows);
+// 16-byte aligned
+__device__ __forceinline__ void ld8(const float *p, float *v) {
+    const float4 a = *reinterpret_cast<const float4 *>(p), b = *reinterpret_cast<const float4 *>(p + 4);
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+}
+__device__ __forceinline__ void ld8(const double *p, double *v) {
+#pragma unroll
+    for (int i = 0; i < 8; i += 2) {
+        const double2 a = *reinterpret_cast<const double2 *>(p + i);
+        v[i] = a.x; v[i + 1] = a.y;
+    }
+}
+
+// Panel factorization, one cluster (see the file comment).  The columns are
+// processed in sub-panels of PANEL_SUB: within a sub-panel the rank-1 updates
+// touch only the sub-panel's columns; the columns to its right receive the
+// sub-panel's pivot rows (kept in U8) as one rank-PANEL_SUB update after its
+// last column, which divides the shared-memory traffic of the updates by
+// about PANEL_SUB.  Rows that leave their CTA (pivot candidates, row j+1) are
+// published with every pending update applied to the copy.  Per column the
 // critical path is: winner -> swap -> scale + update of the next column and
-// its local argmax -> finish the two rows that will be published -> push
-// candidates to every CTA (DSMEM stores) -> barrier arrive.  The rank-1 update
-// of the remaining columns runs between the barrier's arrive and wait.
+// its local argmax -> finished copies of the rows to publish -> push to every
+// CTA (DSMEM stores) -> barrier arrive; the remaining updates run between the
+// barrier's arrive and wait.
 template <typename T>
-__global__ void __launch_bounds__(PANEL_THREADS) k_panel_lu(PanelArgs<T> a) {
+__global__ void __launch_bounds__(PANEL_THREADS, 1) k_panel_lu(PanelArgs<T> a) {
     cg::cluster_group cluster = cg::this_cluster();
     const int CS = (int)cluster.num_blocks();
     const int rank = (int)cluster.block_rank();
@@ -140,16 +160,14 @@ __global__ void __launch_bounds__(PANEL_THREADS) k_panel_lu(PanelArgs<T> a) {
     int *origin = (int *)(smem + L.origin);
     typedef typename KeyT<T>::type K;
     T *ucur = (T *)(smem + L.ucur);
+    T *U8 = (T *)(smem + L.u8);   // [c][k]: pivot rows of the current sub-panel, column-major by k
+    T *pub = (T *)(smem + L.pub); // [parity][0: candidate, 1: row j+1][w], read by the other CTAs
     K *cand_val = (K *)(smem + L.cand_val);
     int *cand_idx = (int *)(smem + L.cand_idx);
     int *cand_org = (int *)(smem + L.cand_org);
-    T *cand_rows = (T *)(smem + L.cand_rows);
-    T *jrow = (T *)(smem + L.jrow);
     int *jorg = (int *)(smem + L.jorg);
     K *red_v = (K *)(smem + L.red);
     int *red_i = (int *)(red_v + PANEL_THREADS / 32);
-    __shared__ K s_bval;
-    __shared__ int s_best;
 
     const int base = rank * rp;
     int nloc = a.m - base;
@@ -164,32 +182,19 @@ __global__ void __launch_bounds__(PANEL_THREADS) k_panel_lu(PanelArgs<T> a) {
     for (int l = tid; l < nloc; l += PANEL_THREADS) origin[l] = base + l;
     __syncthreads();
 
-    // Publish (value, row index, row, origin) of my candidate for column jn,
-    // and row jn itself if I own it, into buffer jn&1 of every CTA.
-    auto push = [&](int jn) {
+    // Publish (value, row index, origin) of my candidate cb for column jn in
+    // buffer jn&1 of every CTA; the rows themselves (finished copies in my
+    // pub[jn&1]) are read by the other CTAs after the barrier.
+    auto push = [&](int jn, K cv, int cb) {
         const int nbf = jn & 1;
-        const int cb = s_best;
         if (tid < CS) {
-            cluster.map_shared_rank(cand_val, tid)[nbf * PANEL_MAXCS + rank] = s_bval;
+            cluster.map_shared_rank(cand_val, tid)[nbf * PANEL_MAXCS + rank] = cv;
             cluster.map_shared_rank(cand_idx, tid)[nbf * PANEL_MAXCS + rank] = cb;
             cluster.map_shared_rank(cand_org, tid)[nbf * PANEL_MAXCS + rank] = cb != INT_MAX ? origin[cb - base] : 0;
             if (owns(jn)) cluster.map_shared_rank(jorg, tid)[nbf] = origin[jn - base];
         }
-        if (cb != INT_MAX) {
-            const T *src = rows + (cb - base) * WP;
-            for (int e = tid; e < CS * w; e += PANEL_THREADS) {
-                int r2 = e / w, c = e % w;
-                cluster.map_shared_rank(cand_rows, r2)[(nbf * PANEL_MAXCS + rank) * w + c] = src[c];
-            }
-        }
-        if (owns(jn)) {
-            const T *src = rows + (jn - base) * WP;
-            for (int e = tid; e < CS * w; e += PANEL_THREADS) {
-                int r2 = e / w, c = e % w;
-                cluster.map_shared_rank(jrow, r2)[nbf * w + c] = src[c];
-            }
-        }
     };
+    auto owner = [&](int g) { return g / rp; };
 
     const int kmax = a.m < w ? a.m : w;
     {
@@ -199,13 +204,19 @@ __global__ void __launch_bounds__(PANEL_THREADS) k_panel_lu(PanelArgs<T> a) {
             K v = amax_key(rows[l * WP]);
             if (v > bv || bi == INT_MAX) { bv = v; bi = base + l; }
         }
-        block_argmax<K>(bv, bi, red_v, red_i, &s_bval, &s_best);
-        push(0);
+        block_argmax<K>(bv, bi, red_v, red_i);
+        // nothing is pending before column 0: the published rows are the rows
+        if (bi != INT_MAX)
+            for (int c = tid; c < w; c += PANEL_THREADS) pub[c] = rows[(bi - base) * WP + c];
+        if (owns(0))
+            for (int c = tid; c < w; c += PANEL_THREADS) pub[w + c] = rows[(0 - base) * WP + c];
+        push(0, bv, bi);
         cluster.sync();
     }
 
     for (int j = 0; j < kmax; j++) {
         const int buf = j & 1;
+        const int s0 = j - j % PANEL_SUB, s1 = s0 + PANEL_SUB < w ? s0 + PANEL_SUB : w;
         // winner (identical in every CTA, from local copies): lanes 0..CS-1
         // each read one candidate, then a butterfly over the warp
         const int lane = tid & 31;
@@ -221,20 +232,29 @@ __global__ void __launch_bounds__(PANEL_THREADS) k_panel_lu(PanelArgs<T> a) {
         }
         const bool none = (wi == INT_MAX);
         const int p = none ? j : wi;
-        const T *usrc = none ? jrow + buf * w : cand_rows + (buf * PANEL_MAXCS + wr) * w;
         const int uorg = none ? jorg[buf] : cand_org[buf * PANEL_MAXCS + wr];
-        for (int c = tid; c < w; c += PANEL_THREADS) ucur[c] = usrc[c];
+        // pivot row from the winner's published copy (DSMEM load); the owner
+        // of row p also fetches the old row j from its owner
+        {
+            const T *src = none ? cluster.map_shared_rank(pub, owner(j)) + (buf * 2 + 1) * w
+                                : cluster.map_shared_rank(pub, wr) + (buf * 2) * w;
+            if (tid < w) {
+                const T u = src[tid];
+                ucur[tid] = u;
+                U8[tid * PANEL_SUB + (j - s0)] = u;
+            } else if (p != j && owns(p) && tid >= 64 && tid < 64 + w) {
+                const int c = tid - 64;
+                rows[(p - base) * WP + c] = cluster.map_shared_rank(pub, owner(j))[(buf * 2 + 1) * w + c];
+                if (c == 0) origin[p - base] = jorg[buf];
+            }
+        }
         if (rank == 0 && tid == 0) a.piv[j] = p - j;
         __syncthreads();
-        if (p != j) {
-            if (owns(j)) {
-                for (int c = tid; c < w; c += PANEL_THREADS) rows[(j - base) * WP + c] = ucur[c];
-                if (tid == 0) origin[j - base] = uorg;
-            }
-            if (owns(p)) {
-                for (int c = tid; c < w; c += PANEL_THREADS) rows[(p - base) * WP + c] = jrow[buf * w + c];
-                if (tid == 0) origin[p - base] = jorg[buf];
-            }
+        // row j becomes the finished pivot row (row p, if another, already
+        // holds the old row j in its pending-update state)
+        if (owns(j)) {
+            for (int c = tid; c < w; c += PANEL_THREADS) rows[(j - base) * WP + c] = ucur[c];
+            if (tid == 0) origin[j - base] = uorg;
         }
         __syncthreads();
         const T ujj = ucur[j];
@@ -244,49 +264,87 @@ __global__ void __launch_bounds__(PANEL_THREADS) k_panel_lu(PanelArgs<T> a) {
         }
         const T rinv = T(1) / ujj;
         const bool more = j + 1 < kmax;
+        const bool edge = (j + 1 == s1);   // j is the last column of its sub-panel
         int ls = j + 1 - base;
         if (ls < 0) ls = 0;
-        // scale column j, update column j+1 and find its local first max
+        // scale column j; bring column j+1 up to date (rank-1 inside the
+        // sub-panel, the whole sub-panel at its edge) and find its local max
         K bv = 0;
         int bi = INT_MAX;
-        const T u1 = (j + 1 < w) ? ucur[j + 1] : T(0);
         for (int l = ls + tid; l < nloc; l += PANEL_THREADS) {
             T *row = rows + l * WP;
             T lv = row[j] * rinv;
             row[j] = lv;
             if (j + 1 < w) {
-                T v = fma(lv, -u1, row[j + 1]);
+                T v = row[j + 1];
+                if (!edge) {
+                    v = fma(lv, -ucur[j + 1], v);
+                } else {
+                    for (int k = s0; k <= j; k++) v = fma(row[k], -U8[(j + 1) * PANEL_SUB + (k - s0)], v);
+                }
                 row[j + 1] = v;
                 K av = amax_key(v);
                 if (av > bv || bi == INT_MAX) { bv = av; bi = base + l; }
             }
         }
-        int cb = INT_MAX;
+        // pending update of row values for columns c >= j+2 after column j:
+        // inside the sub-panel the rank-1 from column j; at or beyond its edge
+        // the sub-panel's rank-(j-s0+1) product (applied to the stored rows
+        // only at the edge)
+        auto pend = [&](const T *row, int c) -> T {
+            if (c < s1) return fma(row[j], -U8[c * PANEL_SUB + (j - s0)], row[c]);
+            T v = row[c];
+            for (int k = s0; k <= j; k++) v = fma(row[k], -U8[c * PANEL_SUB + (k - s0)], v);
+            return v;
+        };
         if (more) {
-            block_argmax<K>(bv, bi, red_v, red_i, &s_bval, &s_best);
-            cb = s_best;
-            // finish the rows that get published: the candidate and row j+1
-            for (int c = j + 2 + tid; c < w; c += PANEL_THREADS) {
+            block_argmax<K>(bv, bi, red_v, red_i);
+            const int cb = bi;
+            // finished copies, published in pub[(j+1)&1]: candidate (every
+            // pending update), row j+1 (the updates every stored row receives
+            // below)
+            T *pb = pub + ((j + 1) & 1) * 2 * w;
+            if (tid < w) {
+                const int c = tid;
                 if (cb != INT_MAX) {
-                    T *row = rows + (cb - base) * WP;
-                    row[c] = fma(row[j], -ucur[c], row[c]);
+                    const T *row = rows + (cb - base) * WP;
+                    pb[c] = c <= j + 1 ? row[c] : pend(row, c);
                 }
-                if (owns(j + 1) && j + 1 != cb) {
-                    T *row = rows + (j + 1 - base) * WP;
-                    row[c] = fma(row[j], -ucur[c], row[c]);
-                }
+            } else if (tid >= 64 && tid < 64 + w && owns(j + 1)) {
+                const int c = tid - 64;
+                const T *row = rows + (j + 1 - base) * WP;
+                pb[w + c] = (c <= j + 1 || (!edge && c >= s1)) ? row[c] : pend(row, c);
             }
-            __syncthreads();
-            push(j + 1);
+            push(j + 1, bv, cb);
+            __syncthreads();   // the finished copies are read before the rows change below
             cluster.barrier_arrive();
         }
-        // rank-1 update of the remaining columns (overlaps the barrier)
-        for (int l = ls + tid; l < nloc; l += PANEL_THREADS) {
-            const int g = base + l;
-            if (more && (g == cb || g == j + 1)) continue;
-            T *row = rows + l * WP;
-            const T lv = row[j];
-            for (int c = j + 2; c < w; c++) row[c] = fma(lv, -ucur[c], row[c]);
+        // updates of the stored rows (overlap the barrier): rank-1 on the
+        // sub-panel's remaining columns, or at the edge the whole sub-panel on
+        // every column to its right
+        const int c_lo = j + 2, c_hi = edge ? w : s1;
+        if (c_lo < c_hi) {
+            for (int l = ls + tid; l < nloc; l += PANEL_THREADS) {
+                const int g = base + l;
+                if (g == j + 1) continue;   // replaced by the next pivot row or the old row j+1
+                T *row = rows + l * WP;
+                if (!edge) {
+                    const T lv = row[j];
+                    for (int c = c_lo; c < c_hi; c++) row[c] = fma(lv, -U8[c * PANEL_SUB + (j - s0)], row[c]);
+                } else {
+                    T lk[PANEL_SUB];
+#pragma unroll
+                    for (int k = 0; k < PANEL_SUB; k++) lk[k] = (s0 + k <= j) ? row[s0 + k] : T(0);
+                    for (int c = c_lo; c < c_hi; c++) {
+                        T u[PANEL_SUB];
+                        ld8(U8 + c * PANEL_SUB, u);
+                        T v = row[c];
+#pragma unroll
+                        for (int k = 0; k < PANEL_SUB; k++) v = fma(lk[k], -u[k], v);
+                        row[c] = v;
+                    }
+                }
+            }
         }
         __syncthreads();
         if (more) cluster.barrier_wait();
