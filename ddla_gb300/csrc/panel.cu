@@ -100,26 +100,38 @@ __host__ __device__ inline PanelSmem panel_smem_layout(int rows_per, int w) {
 // Block-wide first-max reduction of (key, row) pairs.  Every warp reduces
 // the per-warp results itself, so all threads return the block's winner after
 // a single barrier.
+// Warp-wide first max of (key, row): the largest key, the lowest row among
+// equal keys (rows INT_MAX stand for "no candidate").  32-bit keys use the
+// warp reduction instructions.
+template <typename K>
+__device__ __forceinline__ void warp_argmax(K &bv, int &bi) {
+    if constexpr (sizeof(K) == 4) {
+        const unsigned m = __reduce_max_sync(0xffffffffu, (unsigned)bv);
+        bi = __reduce_min_sync(0xffffffffu, (unsigned)bv == m ? bi : INT_MAX);
+        bv = (K)m;
+    } else {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            K ov = __shfl_xor_sync(0xffffffffu, bv, off);
+            int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+            if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
+        }
+    }
+}
+
+// Block-wide first-max reduction of (key, row) pairs.  Every warp reduces
+// the per-warp results itself, so all threads return the block's winner after
+// a single barrier.
 template <typename K>
 __device__ __forceinline__ void block_argmax(K &bv, int &bi, K *red_v, int *red_i) {
     constexpr int NW = PANEL_THREADS / 32;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        K ov = __shfl_down_sync(0xffffffffu, bv, off);
-        int oi = __shfl_down_sync(0xffffffffu, bi, off);
-        if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
-    }
+    warp_argmax<K>(bv, bi);
     if (lane == 0) { red_v[warp] = bv; red_i[warp] = bi; }
     __syncthreads();
     bv = lane < NW ? red_v[lane] : K(0);
     bi = lane < NW ? red_i[lane] : INT_MAX;
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        K ov = __shfl_xor_sync(0xffffffffu, bv, off);
-        int oi = __shfl_xor_sync(0xffffffffu, bi, off);
-        if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
-    }
+    warp_argmax<K>(bv, bi);
 }
 
 // 8 consecutive U8 entries (one column of the sub-panel's pivot rows);
@@ -169,6 +181,8 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_panel_lu(PanelArgs<T> a) {
     K *red_v = (K *)(smem + L.red);
     int *red_i = (int *)(red_v + PANEL_THREADS / 32);
 
+    __shared__ int spiv[PANEL_WMAX];   // relative pivots, stored to global memory at the end
+    for (int c = tid; c < PANEL_WMAX; c += PANEL_THREADS) spiv[c] = 0;
     const int base = rank * rp;
     int nloc = a.m - base;
     nloc = nloc < 0 ? 0 : (nloc > rp ? rp : nloc);
@@ -222,14 +236,11 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_panel_lu(PanelArgs<T> a) {
         const int lane = tid & 31;
         K wv = lane < CS ? cand_val[buf * PANEL_MAXCS + lane] : K(0);
         int wi = lane < CS ? cand_idx[buf * PANEL_MAXCS + lane] : INT_MAX;
-        int wr = lane;
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            K ov = __shfl_xor_sync(0xffffffffu, wv, off);
-            int oi = __shfl_xor_sync(0xffffffffu, wi, off);
-            int orr = __shfl_xor_sync(0xffffffffu, wr, off);
-            if (oi != INT_MAX && (wi == INT_MAX || ov > wv || (ov == wv && oi < wi))) { wv = ov; wi = oi; wr = orr; }
-        }
+        const int myi = wi;
+        warp_argmax<K>(wv, wi);
+        // the winning row is unique: its CTA is the lane that proposed it
+        const unsigned hit = __ballot_sync(0xffffffffu, myi == wi && wi != INT_MAX);
+        const int wr = hit ? __ffs(hit) - 1 : 0;
         const bool none = (wi == INT_MAX);
         const int p = none ? j : wi;
         const int uorg = none ? jorg[buf] : cand_org[buf * PANEL_MAXCS + wr];
@@ -248,8 +259,8 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_panel_lu(PanelArgs<T> a) {
                 if (c == 0) origin[p - base] = jorg[buf];
             }
         }
-        if (rank == 0 && tid == 0) a.piv[j] = p - j;
-        __syncthreads();
+        if (tid == 0) spiv[j] = p - j;   // global store at the end: a store here would
+        __syncthreads();                 // delay this thread's cluster release
         // row j becomes the finished pivot row (row p, if another, already
         // holds the old row j in its pending-update state)
         if (owns(j)) {
@@ -317,7 +328,9 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_panel_lu(PanelArgs<T> a) {
             }
             push(j + 1, bv, cb);
             __syncthreads();   // the finished copies are read before the rows change below
-            cluster.barrier_arrive();
+            // warp 0 made the remote stores: its arrive (a release) waits for
+            // them, so it arrives after its share of the updates below
+            if (tid >= 32) cluster.barrier_arrive();
         }
         // updates of the stored rows (overlap the barrier): rank-1 on the
         // sub-panel's remaining columns, or at the edge the whole sub-panel on
@@ -346,11 +359,14 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_panel_lu(PanelArgs<T> a) {
                 }
             }
         }
+        if (more && tid < 32) cluster.barrier_arrive();
         __syncthreads();
         if (more) cluster.barrier_wait();
     }
     // All DSMEM traffic must finish before any CTA of the cluster exits.
     cluster.sync();
+    if (rank == 0)
+        for (int c = tid; c < kmax; c += PANEL_THREADS) a.piv[c] = spiv[c];
     if (a.inv && rank == 0) {
         // inverse of the unit-lower L11 (rows 0..kmax-1 are this CTA's first
         // rows): warp v forms columns v, v+16, .. by forward substitution, the
