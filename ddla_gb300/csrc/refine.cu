@@ -5,6 +5,7 @@
 // backward-error test
 //     max_j ||b_j - A x_j||_inf / (||A||_inf ||x_j||_inf + ||b_j||_inf) <= tol.
 // Only the correction solve (A d = r with the FP32 factors) runs in FP32.
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -88,6 +89,69 @@ __global__ void k_fwd_err(const double *X, const double *XR, i64 n, int nr, unsi
     }
 }
 
+// ---- GMRES building blocks (FP64, one right-hand side)
+// y = A x, row-major A (n x n), one warp per row
+__global__ void __launch_bounds__(256) k_matvec(i64 n, const double *__restrict__ A, const double *__restrict__ x,
+                                               double *y) {
+    const int lane = threadIdx.x & 31;
+    const i64 row = (blockIdx.x * (i64)blockDim.x + threadIdx.x) >> 5;
+    if (row >= n) return;
+    const double *ar = A + row * n;
+    double acc = 0.0;
+    for (i64 j = lane; j < n; j += 32) acc = fma(ar[j], x[j], acc);
+    for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+    if (lane == 0) y[row] = acc;
+}
+__device__ __forceinline__ double block_sum(double v, double *red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x == 0)
+        for (int i = 0; i < (int)(blockDim.x >> 5); i++) t += red[i];
+    return t;
+}
+// h[i] = V_i . w for the first kk columns of V (ld n), one block per column
+__global__ void __launch_bounds__(512) k_dots(const double *V, const double *w, i64 n, double *h) {
+    __shared__ double red[16];
+    const double *v = V + (i64)blockIdx.x * n;
+    double s = 0.0;
+    for (i64 e = threadIdx.x; e < n; e += blockDim.x) s = fma(v[e], w[e], s);
+    s = block_sum(s, red);
+    if (threadIdx.x == 0) h[blockIdx.x] = s;
+}
+// w -= V h (kk columns)
+__global__ void k_sub_vh(double *w, const double *V, const double *h, int kk, i64 n) {
+    for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < n; e += (i64)gridDim.x * blockDim.x) {
+        double v = w[e];
+        for (int i = 0; i < kk; i++) v = fma(-h[i], V[(i64)i * n + e], v);
+        w[e] = v;
+    }
+}
+// out = ||w||_2 (one block)
+__global__ void __launch_bounds__(1024) k_nrm2(const double *w, i64 n, double *out) {
+    __shared__ double red[32];
+    double s = 0.0;
+    for (i64 e = threadIdx.x; e < n; e += blockDim.x) s = fma(w[e], w[e], s);
+    s = block_sum(s, red);
+    if (threadIdx.x == 0) *out = sqrt(s);
+}
+// v = w / *nrm
+__global__ void k_scale_by(const double *w, const double *nrm, i64 n, double *v) {
+    const double inv = 1.0 / *nrm;
+    for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < n; e += (i64)gridDim.x * blockDim.x)
+        v[e] = w[e] * inv;
+}
+// x += V y (kk columns)
+__global__ void k_add_vy(double *x, const double *V, const double *y, int kk, i64 n) {
+    for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < n; e += (i64)gridDim.x * blockDim.x) {
+        double v = x[e];
+        for (int i = 0; i < kk; i++) v = fma(y[i], V[(i64)i * n + e], v);
+        x[e] = v;
+    }
+}
+
 int grid1(i64 tot) {
     i64 g = (tot + 255) / 256;
     return (int)(g < 1 ? 1 : (g > 16384 ? 16384 : g));
@@ -120,6 +184,89 @@ double u64d(unsigned long long v) { return __builtin_bit_cast(double, v); }
 
 }  // namespace
 
+constexpr int GM_MAX = 30;
+
+// One cycle of flexible GMRES(m) on A x = b, right-preconditioned by the
+// FP32 factors (z = M^-1 v = solve32(FP32(v))): starting from r = b - A x (in
+// R), it builds V (orthonormal, FP64, classical Gram-Schmidt applied twice)
+// and Z = M^-1 V, minimises ||b - A (x + Z y)||_2 with Givens rotations on the
+// host and adds Z y to x.  A z is formed in FP64, so the FP32 preconditioner
+// limits only the speed, not the attainable accuracy.  Stops when the
+// residual estimate is below `target` (2-norm, which bounds the inf-norm) or
+// after m steps.  *used = preconditioner applications made.
+template <typename F>
+int gmres_cycle(ddla_handle h, i64 n, const double *A, const double *R, double *X, F &solve32, float *d32,
+                double *V, double *Z, double *W, double *hd, int m, double target, int *used) {
+    cudaStream_t s = h->stream;
+    const unsigned gv = (unsigned)((n * 32 + 255) / 256);
+    *used = 0;
+    k_nrm2<<<1, 1024, 0, s>>>(R, n, hd);
+    DDLA_LAUNCHED();
+    double beta = 0.0;
+    DDLA_CUDA(cudaMemcpyAsync(&beta, hd, sizeof(double), cudaMemcpyDeviceToHost, s));
+    DDLA_CUDA(cudaStreamSynchronize(s));
+    if (!(beta > 0.0) || !std::isfinite(beta)) return 0;
+    k_scale_by<<<grid1(n), 256, 0, s>>>(R, hd, n, V);
+    DDLA_LAUNCHED();
+    std::vector<double> H((size_t)(m + 1) * m, 0.0), g(m + 1, 0.0), cs(m, 0.0), sn(m, 0.0), col(2 * (m + 1) + 2);
+    g[0] = beta;
+    int kk = 0;
+    for (int k = 0; k < m; k++) {
+        double *vk = V + (size_t)k * n, *vn = V + (size_t)(k + 1) * n, *zk = Z + (size_t)k * n;
+        // z_k = M^-1 v_k, w = A z_k
+        k_d2s<<<grid1(n), 256, 0, s>>>(vk, n, d32);
+        DDLA_LAUNCHED();
+        DDLA_TRY(solve32(d32));
+        k_s2d<<<grid1(n), 256, 0, s>>>(d32, n, zk);
+        DDLA_LAUNCHED();
+        (*used)++;
+        k_matvec<<<gv, 256, 0, s>>>(n, A, zk, W);
+        DDLA_LAUNCHED();
+        for (int pass = 0; pass < 2; pass++) {
+            k_dots<<<k + 1, 512, 0, s>>>(V, W, n, hd + pass * (m + 1));
+            DDLA_LAUNCHED();
+            k_sub_vh<<<grid1(n), 256, 0, s>>>(W, V, hd + pass * (m + 1), k + 1, n);
+            DDLA_LAUNCHED();
+        }
+        k_nrm2<<<1, 1024, 0, s>>>(W, n, hd + 2 * (m + 1));
+        DDLA_LAUNCHED();
+        DDLA_CUDA(cudaMemcpyAsync(col.data(), hd, sizeof(double) * (2 * (m + 1) + 1), cudaMemcpyDeviceToHost, s));
+        DDLA_CUDA(cudaStreamSynchronize(s));
+        double *hc = &H[(size_t)k * (m + 1)];   // column k of H, m+1 entries
+        for (int i = 0; i <= k; i++) hc[i] = col[i] + col[(m + 1) + i];
+        const double hn = col[2 * (m + 1)];
+        hc[k + 1] = hn;
+        kk = k + 1;
+        for (int i = 0; i < k; i++) {
+            const double t = cs[i] * hc[i] + sn[i] * hc[i + 1];
+            hc[i + 1] = -sn[i] * hc[i] + cs[i] * hc[i + 1];
+            hc[i] = t;
+        }
+        const double rr = std::hypot(hc[k], hc[k + 1]);
+        cs[k] = rr > 0 ? hc[k] / rr : 1.0;
+        sn[k] = rr > 0 ? hc[k + 1] / rr : 0.0;
+        hc[k] = rr;
+        hc[k + 1] = 0.0;
+        g[k + 1] = -sn[k] * g[k];
+        g[k] = cs[k] * g[k];
+        if (!(hn > 0.0) || !std::isfinite(hn) || std::fabs(g[k + 1]) <= target) break;
+        k_scale_by<<<grid1(n), 256, 0, s>>>(W, hd + 2 * (m + 1), n, vn);
+        DDLA_LAUNCHED();
+    }
+    std::vector<double> y(kk, 0.0);
+    for (int i = kk - 1; i >= 0; i--) {
+        double t = g[i];
+        for (int j = i + 1; j < kk; j++) t -= H[(size_t)j * (m + 1) + i] * y[j];
+        const double d = H[(size_t)i * (m + 1) + i];
+        y[i] = d != 0.0 ? t / d : 0.0;
+    }
+    DDLA_CUDA(cudaMemcpyAsync(hd, y.data(), sizeof(double) * kk, cudaMemcpyHostToDevice, s));
+    k_add_vy<<<grid1(n), 256, 0, s>>>(X, Z, hd, kk, n);
+    DDLA_LAUNCHED();
+    DDLA_CUDA(cudaStreamSynchronize(s));   // y lives on this stack frame
+    return 0;
+}
+
 // Shared refinement loop.  `solve32(d)` overwrites the FP32 right-hand side d
 // (n x nr) with the correction.
 template <typename F>
@@ -145,6 +292,17 @@ int refine(ddla_handle h, i64 n, int nr, const double *A, const double *B, doubl
     int it = 0;
     double berr = INFINITY;
     const int iters = max_iter < 0 ? 0 : max_iter;
+    // flexible GMRES for one right-hand side (tuning key refine.gmres, on by
+    // default); classical refinement otherwise
+    const bool gm = nr == 1 && tune_get("refine.gmres", 1) != 0;
+    const int gm_m = (int)std::max<int64_t>(2, std::min<int64_t>(GM_MAX, tune_get("refine.gmres.m", 10)));
+    double *gV = nullptr, *gZ = nullptr, *gW = nullptr, *gh = nullptr;
+    if (gm) {
+        DDLA_TRY(workspace(h, WS_Y, sizeof(double) * ((size_t)(2 * GM_MAX + 2) * n + 4 * GM_MAX + 8), (void **)&gV));
+        gZ = gV + (size_t)(GM_MAX + 1) * n;
+        gW = gZ + (size_t)GM_MAX * n;
+        gh = gW + n;
+    }
     std::vector<unsigned long long> hn(1 + 3 * MAX_RHS);
     for (;;) {
         DDLA_TRY(residual(s, n, nr, A, X, B, R));
@@ -165,12 +323,22 @@ int refine(ddla_handle h, i64 n, int nr, const double *A, const double *B, doubl
             if (!(e <= berr)) berr = e;  // NaN propagates
         }
         if (berr <= tol || it >= iters) break;
-        k_d2s<<<grid1(tot), 256, 0, s>>>(R, tot, d32);
-        DDLA_LAUNCHED();
-        DDLA_TRY(solve32(d32));
-        k_s2d_add<<<grid1(tot), 256, 0, s>>>(d32, tot, X);
-        DDLA_LAUNCHED();
-        it++;
+        if (gm) {
+            // one restart cycle of flexible GMRES from the current x, aiming
+            // straight at the backward-error target
+            int used = 0;
+            double an = u64d(hn[0]), xn = u64d(hn[1 + nr]), bn = u64d(hn[1]);
+            const double target = 0.5 * tol * (an * xn + bn);
+            DDLA_TRY(gmres_cycle(h, n, A, R, X, solve32, d32, gV, gZ, gW, gh, gm_m, target, &used));
+            it += used;
+        } else {
+            k_d2s<<<grid1(tot), 256, 0, s>>>(R, tot, d32);
+            DDLA_LAUNCHED();
+            DDLA_TRY(solve32(d32));
+            k_s2d_add<<<grid1(tot), 256, 0, s>>>(d32, tot, X);
+            DDLA_LAUNCHED();
+            it++;
+        }
     }
     rep->iterations = it;
     rep->backward_error = berr;

@@ -76,7 +76,8 @@ enum {
  * Cholesky.BlockSize, LDLT.BlockSize = 128, DDLA/Factorizations/LU.cs:131,235,
  * Cholesky.cs:125, LDLT.cs:139.) */
 typedef struct ddla_opts {
-    int32_t precision;     /* DDLA_PREC_*, default TF32X3 for the mixed solvers */
+    int32_t precision;     /* DDLA_PREC_*; 0 = FP32 for the mixed solvers, FP64 for the plain
+                              factorizations (which also accept DDLA_PREC_OZAKI updates) */
     int32_t nb;            /* outer block size; 0 = automatic */
     int32_t max_iter;      /* refinement iterations; 0 = default 30; <0 = none */
     int32_t reserved;
@@ -85,7 +86,8 @@ typedef struct ddla_opts {
 
 /* Result record of a mixed-precision solve. */
 typedef struct ddla_solve_report {
-    int32_t iterations;        /* refinement steps taken */
+    int32_t iterations;        /* correction solves with the low-precision factors (classical steps, or
+                                  GMRES preconditioner applications for one right-hand side) */
     int32_t converged;         /* 1 when backward_error <= tol */
     int32_t precision;         /* precision actually used for the factorization */
     int32_t info;              /* factorization status (0 or failing pivot) */
@@ -127,8 +129,13 @@ int ddla_timing_read(int cls, double *total_ms, int64_t *launches, double *flops
 
 /* Tuning parameters (no DDLA counterpart; DDLA hard-codes its blocking in
  * GEMMKernel, DDLA/Einsum/GEMMKernel.cs:11-21, and LU/Cholesky/LDLT.BlockSize).
- * Keys: "lu.nb" (LU panel width), "panel.cluster" (CTAs per panel cluster),
- * "chol.nb", "ldlt.nb", "batched.*".  value == INT64_MIN removes a key. */
+ * Keys: "lu.nb" (LU panel width cap), "lu.lookahead" (0 turns the look-ahead
+ * panel off), "panel.cluster" (CTAs per panel cluster), "trsv.cluster" (0 uses
+ * the chained per-block triangular solve instead of the cluster solve),
+ * "trsv.cluster.size", "refine.gmres" (0 = classical refinement for one
+ * right-hand side), "refine.gmres.m" (GMRES restart length),
+ * "batched.nb.{32,64,128,big}", "batched.ctas_per_sm".  value == INT64_MIN
+ * removes a key. */
 int ddla_tune_set(const char *key, int64_t value);
 int64_t ddla_tune_get(const char *key, int64_t dflt);
 

@@ -43,3 +43,28 @@ def test_mixed_no_refinement_reports_not_converged(ddla):
     with pytest.raises(ddla.DDLAError) as e:
         ddla.solve_mixed(A, B, precision=ddla.PREC_FP32, max_iter=-1)
     assert e.value.code == -1004
+
+
+def test_gmres_refinement_on_ill_conditioned(ddla):
+    # kappa ~ 1e7 or more: classical refinement contracts slowly or not at
+    # all, GMRES-IR (the default for one right-hand side) reaches the FP64
+    # backward-error target
+    from ddla_gb300 import autotune
+    from helpers import berr, rng
+    r = rng(321)
+    n = 1024
+    A = r.standard_normal((n, n))
+    U, sv, Vt = np.linalg.svd(A)
+    A = A - (sv[-1] - sv[-1] / 3e3) * np.outer(U[:, -1], Vt[-1])
+    b = r.standard_normal((n, 1))
+    x, rep = ddla.solve_mixed(A, b)
+    assert rep["converged"] and berr(A, x, b) <= 1e-14
+    # classical refinement: slower, or no convergence at all at this kappa
+    try:
+        autotune.tune_set("refine.gmres", 0)
+        x2, rep2 = ddla.solve_mixed(A, b, max_iter=80)
+        assert rep["iterations"] <= rep2["iterations"]
+    except ddla.DDLAError as e:
+        assert e.code == ddla._lib.ERR_NOT_CONVERGED
+    finally:
+        autotune.tune_set("refine.gmres", 1)
