@@ -283,6 +283,127 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// Rank-k update C += alpha * A * B for k <= 64 (the trailing updates of the
+// FP32 factorizations): the 128 x 128 tile of C is loaded straight into the
+// accumulators at the start (16 float4 loads per thread, in flight together
+// with the A and B tiles), the whole K range of A and B is staged once, and
+// the tile goes back with float4 stores.  Needs row-major C, A and B with
+// 16-byte aligned rows.
+constexpr int UK = 64;
+__global__ void __launch_bounds__(256, 2)
+    k_supdate(i64 m, i64 n, int k, float alpha, const float *__restrict__ A, i64 rsa, const float *__restrict__ B,
+              i64 rsb, float *C, i64 rsc, int uplo) {
+    extern __shared__ __align__(16) float upd_smem[];
+    float (*As)[SBM] = reinterpret_cast<float (*)[SBM]>(upd_smem);
+    float (*Bs)[SBN] = reinterpret_cast<float (*)[SBN]>(upd_smem + UK * SBM);
+    const i64 m0 = (i64)blockIdx.y * SBM, n0 = (i64)blockIdx.x * SBN;
+    if (uplo == DDLA_LOWER && n0 > m0 + SBM - 1) return;
+    if (uplo == DDLA_UPPER && m0 > n0 + SBN - 1) return;
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    float acc[8][8];
+    // C tile into the accumulators: rows ty*4+i (+64), columns tx*4 (+64)
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        const i64 gr = m0 + (i < 4 ? ty * 4 + i : 64 + ty * 4 + i - 4);
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const i64 gc = n0 + h * 64 + tx * 4;
+            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (gr < m) {
+                const float *cp = C + gr * rsc + gc;
+                if (gc + 3 < n) {
+                    v = *reinterpret_cast<const float4 *>(cp);
+                } else {
+                    float t[4] = {0.f, 0.f, 0.f, 0.f};
+                    for (int e = 0; e < 4; e++)
+                        if (gc + e < n) t[e] = cp[e];
+                    v = make_float4(t[0], t[1], t[2], t[3]);
+                }
+            }
+            acc[i][h * 4 + 0] = v.x;
+            acc[i][h * 4 + 1] = v.y;
+            acc[i][h * 4 + 2] = v.z;
+            acc[i][h * 4 + 3] = v.w;
+        }
+    }
+    // A tile (128 x k, K-contiguous rows) transposed into As[k][row], scaled
+    // by alpha; B tile (k x 128) into Bs[k][col]
+    // consecutive threads take consecutive rows, so the transposed stores
+    // As[k][r] hit 32 different banks
+    for (int e = tid; e < SBM * (UK / 4); e += 256) {
+        const int r = e % SBM, kq = (e / SBM) * 4;
+        const i64 gr = m0 + r;
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (gr < m && kq < k) {
+            const float *ap = A + gr * rsa + kq;
+            if (kq + 3 < k) {
+                v = *reinterpret_cast<const float4 *>(ap);
+            } else {
+                float t[4] = {0.f, 0.f, 0.f, 0.f};
+                for (int x = 0; x < 4; x++)
+                    if (kq + x < k) t[x] = ap[x];
+                v = make_float4(t[0], t[1], t[2], t[3]);
+            }
+        }
+        As[kq + 0][r] = alpha * v.x;
+        As[kq + 1][r] = alpha * v.y;
+        As[kq + 2][r] = alpha * v.z;
+        As[kq + 3][r] = alpha * v.w;
+    }
+    for (int e = tid; e < UK * (SBN / 4); e += 256) {
+        const int kk = e / (SBN / 4), c = (e % (SBN / 4)) * 4;
+        const i64 gc = n0 + c;
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (kk < k && gc < n) {
+            const float *bp = B + (i64)kk * rsb + gc;
+            if (gc + 3 < n) {
+                v = *reinterpret_cast<const float4 *>(bp);
+            } else {
+                float t[4] = {0.f, 0.f, 0.f, 0.f};
+                for (int x = 0; x < 4; x++)
+                    if (gc + x < n) t[x] = bp[x];
+                v = make_float4(t[0], t[1], t[2], t[3]);
+            }
+        }
+        *reinterpret_cast<float4 *>(&Bs[kk][c]) = v;
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int kk = 0; kk < UK; kk++) {
+        const float4 a0 = *reinterpret_cast<const float4 *>(&As[kk][ty * 4]);
+        const float4 a1 = *reinterpret_cast<const float4 *>(&As[kk][64 + ty * 4]);
+        const float4 b0 = *reinterpret_cast<const float4 *>(&Bs[kk][tx * 4]);
+        const float4 b1 = *reinterpret_cast<const float4 *>(&Bs[kk][64 + tx * 4]);
+        const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+        const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+        for (int i = 0; i < 8; i++)
+#pragma unroll
+            for (int j = 0; j < 8; j++) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
+    }
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        const i64 gr = m0 + (i < 4 ? ty * 4 + i : 64 + ty * 4 + i - 4);
+        if (gr >= m) continue;
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const i64 gc = n0 + h * 64 + tx * 4;
+            float *cp = C + gr * rsc + gc;
+            if (uplo == DDLA_DENSE && gc + 3 < n) {
+                *reinterpret_cast<float4 *>(cp) =
+                    make_float4(acc[i][h * 4], acc[i][h * 4 + 1], acc[i][h * 4 + 2], acc[i][h * 4 + 3]);
+            } else {
+                for (int e = 0; e < 4; e++) {
+                    if (gc + e >= n) break;
+                    if (uplo == DDLA_LOWER && gc + e > gr) continue;
+                    if (uplo == DDLA_UPPER && gc + e < gr) continue;
+                    cp[e] = acc[i][h * 4 + e];
+                }
+            }
+        }
+    }
+}
+
 }  // namespace
 
 int gemm_f32(cudaStream_t s, i64 m, i64 n, i64 k, float alpha, View<const float> A, View<const float> B,
@@ -291,6 +412,20 @@ int gemm_f32(cudaStream_t s, i64 m, i64 n, i64 k, float alpha, View<const float>
     if (k < 0 || alpha == 0.f) k = 0;
     i64 gx = (n + SBN - 1) / SBN, gy = (m + SBM - 1) / SBM;
     if (gy > 65535) { set_error("gemm_f32: m too large"); return DDLA_ERR_UNSUPPORTED; }
+    auto al16 = [](const void *p, i64 rs) { return ((((uintptr_t)p) & 15) == 0) && (rs & 3) == 0; };
+    if (beta == 1.f && k > 0 && k <= UK && C.cs == 1 && A.cs == 1 && B.cs == 1 && al16(C.p, C.rs) &&
+        al16(A.p, A.rs) && al16(B.p, B.rs)) {
+        constexpr size_t sm = sizeof(float) * UK * (SBM + SBN);
+        static bool attr = false;
+        if (!attr) {
+            DDLA_CUDA(cudaFuncSetAttribute(k_supdate, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+            attr = true;
+        }
+        k_supdate<<<dim3((unsigned)gx, (unsigned)gy), 256, sm, s>>>(m, n, (int)k, alpha, A.p, A.rs, B.p, B.rs, C.p,
+                                                                   C.rs, uplo);
+        DDLA_LAUNCHED();
+        return 0;
+    }
     k_sgemm<<<dim3((unsigned)gx, (unsigned)gy), 256, 0, s>>>(m, n, k, alpha, A.p, A.rs, A.cs, B.p, B.rs, B.cs,
                                                             beta, C.p, C.rs, C.cs, uplo);
     DDLA_LAUNCHED();
