@@ -62,6 +62,14 @@ def dist_env():
     return rank, world, local
 
 
+def apply_tune(args):
+    """--tune KEY=VALUE options -> the library's tuning table."""
+    from ddla_gb300 import autotune
+    for kv in args.tune:
+        k, v = kv.split("=", 1)
+        autotune.tune_set(k, int(v))
+
+
 def max_over_ranks(ms, world, device="cuda"):
     """Step time of the job: the slowest rank's (all ranks get it)."""
     if world <= 1:
@@ -196,6 +204,7 @@ def secondary(args):
     from ddla_gb300 import einsum as es
     bld.build()
     L = D.lib()
+    apply_tune(args)
     torch.cuda.set_device(0)
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
@@ -387,6 +396,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--precision", default="auto", choices=["auto", "fp32", "tf32x3", "bf16x3", "fp64", "ozaki"])
+    ap.add_argument("--tune", action="append", default=[], metavar="KEY=VALUE",
+                    help="library tuning key (ddla_tune_set) applied before the run; repeatable")
     ap.add_argument("--workload", default="lu", choices=["lu", "gemm", "chol", "batched", "einsum-a", "einsum-b"])
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-n", type=int, default=4096)
@@ -413,6 +424,7 @@ def main():
     from ddla_gb300 import build as bld
     bld.build()
     L = D.lib()
+    apply_tune(args)
 
     prec_map = {"fp32": D.PREC_FP32, "tf32x3": D.PREC_TF32X3, "bf16x3": D.PREC_BF16X3, "fp64": D.PREC_FP64}
     prec_name = args.precision if args.precision != "auto" else os.environ.get("DDLA_BENCH_PREC", "fp32")

@@ -290,24 +290,29 @@ __global__ void __launch_bounds__(256)
 // the tile goes back with float4 stores.  Needs row-major C, A and B with
 // 16-byte aligned rows.
 constexpr int UK = 64;
-__global__ void __launch_bounds__(256, 2)
+// TN = 128 (256 threads) or 64 (128 threads, four CTAs per SM): the thread's
+// 8 x 8 block is rows ty*4..+3 and 64+ty*4..+3, columns tx*4..+3 and
+// TN/2+tx*4..+3
+template <int TN>
+__global__ void __launch_bounds__(TN * 2, TN == 128 ? 2 : 4)
     k_supdate(i64 m, i64 n, int k, float alpha, const float *__restrict__ A, i64 rsa, const float *__restrict__ B,
               i64 rsb, float *C, i64 rsc, int uplo) {
+    constexpr int NT = TN * 2, TXN = TN / 8, HN = TN / 2;
     extern __shared__ __align__(16) float upd_smem[];
     float (*As)[SBM] = reinterpret_cast<float (*)[SBM]>(upd_smem);
-    float (*Bs)[SBN] = reinterpret_cast<float (*)[SBN]>(upd_smem + UK * SBM);
-    const i64 m0 = (i64)blockIdx.y * SBM, n0 = (i64)blockIdx.x * SBN;
+    float (*Bs)[TN] = reinterpret_cast<float (*)[TN]>(upd_smem + UK * SBM);
+    const i64 m0 = (i64)blockIdx.y * SBM, n0 = (i64)blockIdx.x * TN;
     if (uplo == DDLA_LOWER && n0 > m0 + SBM - 1) return;
-    if (uplo == DDLA_UPPER && m0 > n0 + SBN - 1) return;
-    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    if (uplo == DDLA_UPPER && m0 > n0 + TN - 1) return;
+    const int tid = threadIdx.x, tx = tid % TXN, ty = tid / TXN;
     float acc[8][8];
-    // C tile into the accumulators: rows ty*4+i (+64), columns tx*4 (+64)
+    // C tile into the accumulators
 #pragma unroll
     for (int i = 0; i < 8; i++) {
         const i64 gr = m0 + (i < 4 ? ty * 4 + i : 64 + ty * 4 + i - 4);
 #pragma unroll
         for (int h = 0; h < 2; h++) {
-            const i64 gc = n0 + h * 64 + tx * 4;
+            const i64 gc = n0 + h * HN + tx * 4;
             float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
             if (gr < m) {
                 const float *cp = C + gr * rsc + gc;
@@ -327,10 +332,9 @@ __global__ void __launch_bounds__(256, 2)
         }
     }
     // A tile (128 x k, K-contiguous rows) transposed into As[k][row], scaled
-    // by alpha; B tile (k x 128) into Bs[k][col]
-    // consecutive threads take consecutive rows, so the transposed stores
-    // As[k][r] hit 32 different banks
-    for (int e = tid; e < SBM * (UK / 4); e += 256) {
+    // by alpha; consecutive threads take consecutive rows, so the transposed
+    // stores hit different banks.  B tile (k x TN) into Bs[k][col].
+    for (int e = tid; e < SBM * (UK / 4); e += NT) {
         const int r = e % SBM, kq = (e / SBM) * 4;
         const i64 gr = m0 + r;
         float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -350,8 +354,8 @@ __global__ void __launch_bounds__(256, 2)
         As[kq + 2][r] = alpha * v.z;
         As[kq + 3][r] = alpha * v.w;
     }
-    for (int e = tid; e < UK * (SBN / 4); e += 256) {
-        const int kk = e / (SBN / 4), c = (e % (SBN / 4)) * 4;
+    for (int e = tid; e < UK * (TN / 4); e += NT) {
+        const int kk = e / (TN / 4), c = (e % (TN / 4)) * 4;
         const i64 gc = n0 + c;
         float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
         if (kk < k && gc < n) {
@@ -373,7 +377,7 @@ __global__ void __launch_bounds__(256, 2)
         const float4 a0 = *reinterpret_cast<const float4 *>(&As[kk][ty * 4]);
         const float4 a1 = *reinterpret_cast<const float4 *>(&As[kk][64 + ty * 4]);
         const float4 b0 = *reinterpret_cast<const float4 *>(&Bs[kk][tx * 4]);
-        const float4 b1 = *reinterpret_cast<const float4 *>(&Bs[kk][64 + tx * 4]);
+        const float4 b1 = *reinterpret_cast<const float4 *>(&Bs[kk][HN + tx * 4]);
         const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
         const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
 #pragma unroll
@@ -387,7 +391,7 @@ __global__ void __launch_bounds__(256, 2)
         if (gr >= m) continue;
 #pragma unroll
         for (int h = 0; h < 2; h++) {
-            const i64 gc = n0 + h * 64 + tx * 4;
+            const i64 gc = n0 + h * HN + tx * 4;
             float *cp = C + gr * rsc + gc;
             if (uplo == DDLA_DENSE && gc + 3 < n) {
                 *reinterpret_cast<float4 *>(cp) =
@@ -404,6 +408,22 @@ __global__ void __launch_bounds__(256, 2)
     }
 }
 
+template <int TN>
+int launch_supdate(cudaStream_t s, i64 m, i64 n, int k, float alpha, View<const float> A, View<const float> B,
+                   View<float> C, int uplo) {
+    constexpr size_t sm = sizeof(float) * UK * (SBM + TN);
+    static bool attr = false;
+    if (!attr) {
+        DDLA_CUDA(cudaFuncSetAttribute(k_supdate<TN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        attr = true;
+    }
+    const i64 gx = (n + TN - 1) / TN, gy = (m + SBM - 1) / SBM;
+    k_supdate<TN><<<dim3((unsigned)gx, (unsigned)gy), TN * 2, sm, s>>>(m, n, k, alpha, A.p, A.rs, B.p, B.rs, C.p,
+                                                                      C.rs, uplo);
+    DDLA_LAUNCHED();
+    return 0;
+}
+
 }  // namespace
 
 int gemm_f32(cudaStream_t s, i64 m, i64 n, i64 k, float alpha, View<const float> A, View<const float> B,
@@ -415,15 +435,8 @@ int gemm_f32(cudaStream_t s, i64 m, i64 n, i64 k, float alpha, View<const float>
     auto al16 = [](const void *p, i64 rs) { return ((((uintptr_t)p) & 15) == 0) && (rs & 3) == 0; };
     if (beta == 1.f && k > 0 && k <= UK && C.cs == 1 && A.cs == 1 && B.cs == 1 && al16(C.p, C.rs) &&
         al16(A.p, A.rs) && al16(B.p, B.rs)) {
-        constexpr size_t sm = sizeof(float) * UK * (SBM + SBN);
-        static bool attr = false;
-        if (!attr) {
-            DDLA_CUDA(cudaFuncSetAttribute(k_supdate, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-            attr = true;
-        }
-        k_supdate<<<dim3((unsigned)gx, (unsigned)gy), 256, sm, s>>>(m, n, (int)k, alpha, A.p, A.rs, B.p, B.rs, C.p,
-                                                                   C.rs, uplo);
-        DDLA_LAUNCHED();
+        if (tune_get("update.tn", 128) == 64) return launch_supdate<64>(s, m, n, (int)k, alpha, A, B, C, uplo);
+        return launch_supdate<128>(s, m, n, (int)k, alpha, A, B, C, uplo);
         return 0;
     }
     k_sgemm<<<dim3((unsigned)gx, (unsigned)gy), 256, 0, s>>>(m, n, k, alpha, A.p, A.rs, A.cs, B.p, B.rs, B.cs,

@@ -230,12 +230,13 @@ int copy2d(cudaStream_t s, View<const T> X, View<T> Y) {
 // Whole-system solve with <= NR right-hand sides on ONE thread-block cluster
 // (up to 16 CTAs).  Logical block l (block row l of a lower triangle, block
 // row nblk-1-l of an upper one) belongs to CTA l % CS.  Every CTA keeps a copy
-// of the whole solution x (n x NR) and one flag per block in its shared
-// memory.  A CTA solves its blocks in increasing l, left-looking:
-//   acc = b_l;  for j < l: wait for flag j (local shared memory, bounded),
-//   acc -= A_lj x_j;  x_l = inv(A_ll) acc
-// and then pushes x_l into every CTA's copy over DSMEM and raises flag l in
-// every CTA (release at cluster scope).
+// of the whole solution x (n x NR) in its shared memory, filled with a marker
+// value that no arithmetic produces.  A CTA solves its blocks in increasing l,
+// left-looking:
+//   acc = b_l;  for j < l: acc -= A_lj x_j  (waiting, bounded, until this
+//   lane's entries of x_j no longer hold the marker);  x_l = inv(A_ll) acc
+// and then stores x_l into every CTA's copy over DSMEM: the values mark
+// themselves, so the chain needs no flags and no fences.
 // Each warp owns 8 rows of the block: it streams its own rows of the tiles
 // A_lj and of the inverted diagonal block through its own ring of
 // shared-memory stages (cp.async, STAGES-1 items ahead, in consumption
@@ -251,7 +252,7 @@ constexpr long long CL_SPIN = 1LL << 22;
 template <typename T> struct ClStages { static constexpr int value = sizeof(T) == 4 ? 8 : 4; };
 
 struct ClLayout {
-    size_t ring, xall, acc, flags, total;
+    size_t ring, xall, acc, total;
 };
 
 template <typename T, int NR>
@@ -266,16 +267,24 @@ __host__ __device__ inline ClLayout cl_layout(int nblk) {
     L.ring = take(sizeof(T) * (size_t)ClStages<T>::value * TB * CL_TLD);
     L.xall = take(sizeof(T) * (size_t)nblk * TB * NR);
     L.acc = take(sizeof(T) * TB * NR);
-    L.flags = take(sizeof(int) * (size_t)nblk);
     L.total = o;
     return L;
 }
 
-__device__ __forceinline__ int ld_acquire_cluster(const int *p) {
-    int v;
-    asm volatile("ld.acquire.cluster.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
+// "Not yet written" marker of the x copies: a signaling-NaN bit pattern, which
+// no arithmetic result can have (results that are NaN are quiet NaNs), so each
+// value announces its own arrival and needs no flag or fence.
+__device__ __forceinline__ bool cl_pending(float v) { return __float_as_uint(v) == 0x7FBADBADu; }
+__device__ __forceinline__ bool cl_pending(double v) {
+    return (unsigned long long)__double_as_longlong(v) == 0x7FF4DEADBEEFBADDull;
 }
+template <typename T> __device__ __forceinline__ T cl_marker();
+template <> __device__ __forceinline__ float cl_marker<float>() { return __uint_as_float(0x7FBADBADu); }
+template <> __device__ __forceinline__ double cl_marker<double>() {
+    return __longlong_as_double((long long)0x7FF4DEADBEEFBADDull);
+}
+__device__ __forceinline__ float ld_volatile(const float *p) { return *(const volatile float *)p; }
+__device__ __forceinline__ double ld_volatile(const double *p) { return *(const volatile double *)p; }
 
 __device__ __forceinline__ void cp_async16(void *dst, const void *src, int src_bytes) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
@@ -306,28 +315,41 @@ __global__ void __launch_bounds__(CL_THREADS)
     T *ring = (T *)(smem + Ly.ring);
     T *xall = (T *)(smem + Ly.xall);
     T *acc = (T *)(smem + Ly.acc);
-    int *flags = (int *)(smem + Ly.flags);
     __shared__ int s_abort;
     auto phys = [&](int l) { return lower ? l : nblk - 1 - l; };
     // ring item (l, j): this warp's rows of tile A_lj (j < l) or of the
-    // inverted diagonal block (j == l)
+    // inverted diagonal block (j == l).  Each lane copies the same chunks
+    // (row, 16-byte column chunk) of every item: their offsets are formed once.
+    constexpr int CPR = TB * (int)sizeof(T) / 16, EPC = 16 / (int)sizeof(T);
+    constexpr int CPL = CL_WROWS * CPR / 32;   // chunks per lane
+    const int row0 = warp * CL_WROWS;
+    int c_row[CPL], c_col[CPL];
+    i64 c_goff[CPL];
+#pragma unroll
+    for (int i = 0; i < CPL; i++) {
+        const int e = lane + 32 * i;
+        c_row[i] = row0 + e / CPR;
+        c_col[i] = (e % CPR) * EPC;
+        c_goff[i] = (i64)c_row[i] * rs + c_col[i];
+    }
     auto issue = [&](int l, int j, int stage) {
         T *dst = ring + (size_t)stage * TB * CL_TLD;
-        const int row0 = warp * CL_WROWS;
-        constexpr int CPR = TB * (int)sizeof(T) / 16, EPC = 16 / (int)sizeof(T);
         if (j == l) {   // inverse block: contiguous TB x TB, 16-byte aligned
             const T *src = inv + (i64)phys(l) * TB * TB;
-            for (int e = lane; e < CL_WROWS * CPR; e += 32) {
-                const int row = row0 + e / CPR, ch = e % CPR;
-                cp_async16(dst + row * CL_TLD + ch * EPC, src + row * TB + ch * EPC, 16);
-            }
+#pragma unroll
+            for (int i = 0; i < CPL; i++)
+                cp_async16(dst + c_row[i] * CL_TLD + c_col[i], src + c_row[i] * TB + c_col[i], 16);
             return;
         }
         const i64 r0 = (i64)phys(l) * TB, c0 = (i64)phys(j) * TB;
-        if (vec) {
-            for (int e = lane; e < CL_WROWS * CPR; e += 32) {
-                const int row = row0 + e / CPR, ch = e % CPR;
-                const i64 gr = r0 + row, gc = c0 + (i64)ch * EPC;
+        if (vec && r0 + TB <= n && c0 + TB <= n) {   // full tile
+            const T *base = A + r0 * rs + c0;
+#pragma unroll
+            for (int i = 0; i < CPL; i++) cp_async16(dst + c_row[i] * CL_TLD + c_col[i], base + c_goff[i], 16);
+        } else if (vec) {
+#pragma unroll
+            for (int i = 0; i < CPL; i++) {
+                const i64 gr = r0 + c_row[i], gc = c0 + c_col[i];
                 int bytes = 0;
                 const T *src = A;
                 if (gr < n && gc < n) {
@@ -335,7 +357,7 @@ __global__ void __launch_bounds__(CL_THREADS)
                     bytes = (int)(left >= EPC ? 16 : left * (i64)sizeof(T));
                     src = A + gr * rs + gc;
                 }
-                cp_async16(dst + row * CL_TLD + ch * EPC, src, bytes);
+                cp_async16(dst + c_row[i] * CL_TLD + c_col[i], src, bytes);
             }
         } else {
             for (int e = lane; e < CL_WROWS * TB; e += 32) {
@@ -355,8 +377,7 @@ __global__ void __launch_bounds__(CL_THREADS)
             pj = 0;
         }
     };
-    for (int e = t; e < nblk; e += CL_THREADS) flags[e] = 0;
-    for (int e = t; e < nblk * TB * NR; e += CL_THREADS) xall[e] = T(0);
+    for (int e = t; e < nblk * TB * NR; e += CL_THREADS) xall[e] = cl_marker<T>();
     if (t == 0) s_abort = 0;
     int produced = 0, consumed = 0;
     for (int i = 0; i < S - 1; i++) {
@@ -367,7 +388,7 @@ __global__ void __launch_bounds__(CL_THREADS)
         produced++;
         cp_async_commit();
     }
-    cluster.sync();   // every CTA's flags are down before anyone raises one
+    cluster.sync();   // every CTA's copy holds markers before anyone writes x into it
     // this warp's row r of a tile times x (sum over the 4 lanes of the row)
     auto rowdot = [&](const T *tile, const T *xv, T *p) {
 #pragma unroll
@@ -403,14 +424,40 @@ __global__ void __launch_bounds__(CL_THREADS)
         bool bad = false;
         for (int j = 0; j < l; j++) {
             cp_async_wait<S - 2>();
+            // this lane's entries of x_j (rows k = q + 4i): wait until none is
+            // the marker any more (bounded)
+            const T *xj = xall + (size_t)phys(j) * TB * NR;
+            T xv[TB / 4][NR];
             long long it = 0;
-            while (ld_acquire_cluster(flags + j) == 0) {
+            for (;;) {
+                bool pend = false;
+#pragma unroll
+                for (int i = 0; i < TB / 4; i++)
+#pragma unroll
+                    for (int c = 0; c < NR; c++) {
+                        xv[i][c] = ld_volatile(xj + (q + 4 * i) * NR + c);
+                        pend |= cl_pending(xv[i][c]);
+                    }
+                if (!__any_sync(0xffffffffu, pend)) break;
                 if (++it > CL_SPIN || *(volatile int *)&s_abort) { bad = true; break; }
                 if (it > 64) __nanosleep(20);
             }
             if (__any_sync(0xffffffffu, bad)) { bad = true; break; }
             __syncwarp();
-            rowdot(ring + (size_t)(consumed % S) * TB * CL_TLD, xall + (size_t)phys(j) * TB * NR, p);
+            const T *tile = ring + (size_t)(consumed % S) * TB * CL_TLD;
+#pragma unroll
+            for (int c = 0; c < NR; c++) p[c] = T(0);
+#pragma unroll
+            for (int i = 0; i < TB / 4; i++) {
+                const T v = tile[r * CL_TLD + q + 4 * i];
+#pragma unroll
+                for (int c = 0; c < NR; c++) p[c] += v * xv[i][c];
+            }
+#pragma unroll
+            for (int c = 0; c < NR; c++) {
+                p[c] += __shfl_xor_sync(0xffffffffu, p[c], 1);
+                p[c] += __shfl_xor_sync(0xffffffffu, p[c], 2);
+            }
             next_item();
             if (q == 0)
 #pragma unroll
@@ -426,25 +473,17 @@ __global__ void __launch_bounds__(CL_THREADS)
         __syncwarp();
         rowdot(ring + (size_t)(consumed % S) * TB * CL_TLD, acc, p);   // x_l = inv(A_ll) acc
         next_item();
+        // publish x_l: the 4 lanes of row r each store it into a quarter of
+        // the CTAs' copies (plain DSMEM stores; the values mark themselves)
         const int pb = phys(l);
-        __syncthreads();   // everyone is done reading acc
-        if (q == 0) {
+        for (int dst = q; dst < CS; dst += 4) {
+            T *xd = cluster.map_shared_rank(xall, dst) + (size_t)pb * TB * NR + r * NR;
 #pragma unroll
-            for (int c = 0; c < NR; c++) acc[r * NR + c] = p[c];
-            if (r0 + r < n)
-                for (int c = 0; c < nr; c++) X[(r0 + r) * ldx + c] = p[c];
+            for (int c = 0; c < NR; c++) xd[c] = p[c];
         }
-        __syncthreads();
-        for (int e = t; e < CS * TB * NR; e += CL_THREADS) {
-            const int dst = e / (TB * NR), k = e % (TB * NR);
-            cluster.map_shared_rank(xall, dst)[(size_t)pb * TB * NR + k] = acc[k];
-        }
-        asm volatile("fence.acq_rel.cluster;" ::: "memory");
-        __syncthreads();
-        if (t < CS) {
-            int *f = cluster.map_shared_rank(flags, t) + l;   // flags are indexed by logical block
-            asm volatile("st.relaxed.cluster.b32 [%0], %1;" ::"l"(f), "r"(1) : "memory");
-        }
+        if (q == 0 && r0 + r < n)
+            for (int c = 0; c < nr; c++) X[(r0 + r) * ldx + c] = p[c];
+        __syncthreads();   // acc is read above before the next block overwrites it
     }
     cp_async_wait<0>();
     __syncthreads();
@@ -563,7 +602,9 @@ int trsv_apply(ddla_handle h, bool lower, View<const T> A, i64 n, const T *inv, 
     DDLA_TRY(workspace(h, WS_MISC, sizeof(int) * (size_t)(nblk + 1), (void **)&flags));
     DDLA_CUDA(cudaMemsetAsync(flags, 0, sizeof(int) * (size_t)(nblk + 1), h->stream));
     if (nr <= 1) {
-        const int cs = cluster_size<T, 1>(h, nblk);
+        // FP64 on 16 SMs is bounded by their FP64 units: past ~96 blocks the
+        // chained solve over one CTA per block is faster
+        const int cs = (sizeof(T) == 8 && nblk > 96) ? 0 : cluster_size<T, 1>(h, nblk);
         if (cs > 1 && nblk > 1) return cluster_solve<T, 1>(h, cs, n, nblk, A, lower, inv, X, ldx, nr);
         return chain<T, 1>(h, n, nblk, A, lower, inv, X, ldx, nr, flags);
     }
