@@ -273,6 +273,234 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_tf32x3(TcArgs g) {
 
 constexpr size_t TC_SMEM = 2 * A_BYTES + 2 * B_BYTES;
 
+// ------------------------------------------------------------------ rank-64 update, 3xTF32
+//
+// C += alpha * A * B for K <= 64 (the trailing updates of the FP32
+// factorizations) on the tensor cores.  A (m x K) and B (K x n) are split once
+// into TF32 hi / lo parts packed per 128-row (128-column) tile in the
+// core-matrix layout the MMA reads (k_tc_pack).  A persistent kernel walks
+// the 128 x 128 tiles of C with every data movement asynchronous:
+//   * the four 32 KB operand tiles arrive by bulk copy on one mbarrier, and
+//     the next tile's copies start as soon as the current MMAs are done;
+//   * the C tile is loaded with coalesced float4 loads (a warp per 512-byte
+//     row) before the MMAs are issued and parked in a shared staging tile S
+//     while they run;
+//   * one thread issues 8 k-steps x 3 MMAs (hi*hi + hi*lo + lo*hi) into a
+//     128-column TMEM accumulator;
+//   * each thread adds alpha * (its TMEM row) into S, and S goes back to C
+//     with coalesced float4 stores.
+// Every mbarrier wait is bounded as in k_tc_tf32x3.  Needs n, the row stride
+// of C and the C pointer 16-byte aligned (checked by the host).
+constexpr int UT = 128;                       // tile rows = tile columns
+constexpr int UT_PART = UT * TK;              // floats of one packed operand part
+constexpr int UT_SLD = UT + 4;                // staging tile row (floats)
+constexpr size_t UT_OPS = 4 * (size_t)UT_PART * 4;
+constexpr size_t UT_SMEM = UT_OPS + (size_t)UT * UT_SLD * 4;
+
+__host__ __device__ constexpr uint32_t idesc_tf32_128() {
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(UT >> 3) << 17) | ((uint32_t)(UT >> 4) << 24);
+}
+
+// rows r of X (rows x kdim, strides rs / cs) -> packed [tile][hi | lo][UT x TK]
+// (element (r, k) at cm_off); rows beyond `rows` and k beyond kdim are zero
+__global__ void k_tc_pack(const float *X, i64 rs, i64 cs, i64 rows, int kdim, float *out, i64 tiles) {
+    const i64 tot = tiles * UT * (TK / 4);
+    for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < tot; e += (i64)gridDim.x * blockDim.x) {
+        const i64 tile = e / (UT * (TK / 4));
+        const int rem = (int)(e % (UT * (TK / 4))), r = rem / (TK / 4), k4 = (rem % (TK / 4)) * 4;
+        const i64 gr = tile * UT + r;
+        float hi[4], lo[4];
+#pragma unroll
+        for (int x = 0; x < 4; x++) {
+            const float v = (gr < rows && k4 + x < kdim) ? X[gr * rs + (i64)(k4 + x) * cs] : 0.f;
+            hi[x] = tf32_round(v);
+            lo[x] = tf32_round(v - hi[x]);
+        }
+        float *base = out + tile * 2 * UT_PART;
+        const int off = cm_off(r, k4) / 4;
+        *reinterpret_cast<float4 *>(base + off) = make_float4(hi[0], hi[1], hi[2], hi[3]);
+        *reinterpret_cast<float4 *>(base + UT_PART + off) = make_float4(lo[0], lo[1], lo[2], lo[3]);
+    }
+}
+
+struct TuArgs {
+    int64_t m, n;
+    int ntm, ntn;
+    const float *Ap, *Bp;   // packed operands
+    float alpha;
+    float *C;
+    int64_t rsc;
+    int *err;
+};
+
+__device__ __forceinline__ void bulk_g2s(unsigned dst, const void *src, unsigned bytes, unsigned mbar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(mbar)
+                 : "memory");
+}
+
+__global__ void __launch_bounds__(TC_THREADS, 1) k_tc_update(TuArgs g) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned char *Ahi = smem, *Alo = smem + UT_PART * 4, *Bhi = smem + 2 * UT_PART * 4, *Blo = smem + 3 * UT_PART * 4;
+    float *S = reinterpret_cast<float *>(smem + UT_OPS);
+    __shared__ __align__(8) unsigned long long mb_ld, mb_mma;
+    __shared__ unsigned tmem_slot;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int total = g.ntm * g.ntn;
+    if ((int)blockIdx.x >= total) return;
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(&tmem_slot)),
+                     "r"(UT)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&mb_ld)) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&mb_mma)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const unsigned tmem = tmem_slot;
+    constexpr uint32_t id = idesc_tf32_128();
+    auto issue_ops = [&](int t) {   // thread 0: the four operand tiles of tile t
+        const int mt = t / g.ntn, nt = t % g.ntn;
+        const float *a = g.Ap + (size_t)mt * 2 * UT_PART, *b = g.Bp + (size_t)nt * 2 * UT_PART;
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(&mb_ld)),
+                     "r"((unsigned)UT_OPS)
+                     : "memory");
+        bulk_g2s(su32(Ahi), a, UT_PART * 4, su32(&mb_ld));
+        bulk_g2s(su32(Alo), a + UT_PART, UT_PART * 4, su32(&mb_ld));
+        bulk_g2s(su32(Bhi), b, UT_PART * 4, su32(&mb_ld));
+        bulk_g2s(su32(Blo), b + UT_PART, UT_PART * 4, su32(&mb_ld));
+    };
+    // rows and bytes per row of tile t
+    auto tile_rows = [&](int t, int *rows, unsigned *bytes) {
+        const int mt = t / g.ntn, nt = t % g.ntn;
+        const int64_t r_left = g.m - (int64_t)mt * UT, c_left = g.n - (int64_t)nt * UT;
+        *rows = (int)(r_left < UT ? r_left : UT);
+        *bytes = (unsigned)((c_left < UT ? c_left : UT) * 4);
+    };
+    auto wait_mb = [&](unsigned long long *mb, unsigned ph) -> bool {
+        for (long long it = 0; it < TC_SPIN; it++)
+            if (mbar_try(su32(mb), ph)) return true;
+        return false;
+    };
+    unsigned ph_ld = 0, ph_mma = 0;
+    bool failed = false, ops_out = false, mma_out = false;
+    if (tid == 0) issue_ops(blockIdx.x);
+    ops_out = true;
+    const int q = warp & 3, h = warp >> 2;   // TMEM lanes 32q.., columns 64h..
+    // coalesced view of a tile: item e = tid + 256 i is row e / 32, columns
+    // 4 (e % 32) .. +3 (a warp covers one 512-byte row).  The C tile of the
+    // next tile is loaded into registers while the current one finishes.
+    float4 creg[16];
+    auto load_c = [&](int t) {
+        int rows;
+        unsigned bytes;
+        tile_rows(t, &rows, &bytes);
+        const int cols = (int)(bytes / 4);
+        const float *ct = g.C + (int64_t)(t / g.ntn) * UT * g.rsc + (int64_t)(t % g.ntn) * UT;
+#pragma unroll
+        for (int i = 0; i < 16; i++) {
+            const int e = tid + 256 * i, r = e >> 5, c4 = (e & 31) * 4;
+            creg[i] = (r < rows && c4 < cols) ? *reinterpret_cast<const float4 *>(ct + (int64_t)r * g.rsc + c4)
+                                              : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+    };
+    load_c(blockIdx.x);
+    for (int t = blockIdx.x; t < total; t += gridDim.x) {
+        int rows;
+        unsigned bytes;
+        tile_rows(t, &rows, &bytes);
+        const int cols = (int)(bytes / 4);
+        const int mt = t / g.ntn, nt = t % g.ntn;
+        float *ctile = g.C + (int64_t)mt * UT * g.rsc + (int64_t)nt * UT;
+        const bool more = t + (int)gridDim.x < total;
+        if (__syncthreads_or(!wait_mb(&mb_ld, ph_ld))) { failed = true; break; }
+        ph_ld ^= 1u;
+        ops_out = false;
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            for (int s = 0; s < TK / 8; s++) {
+                const unsigned off = s * 2 * LBO;
+                const uint64_t ah = sdesc(su32(Ahi) + off), al = sdesc(su32(Alo) + off);
+                const uint64_t bh = sdesc(su32(Bhi) + off), bl = sdesc(su32(Blo) + off);
+                mma_tf32(tmem, ah, bh, id, s == 0 ? 0 : 1);
+                mma_tf32(tmem, ah, bl, id, 1);
+                mma_tf32(tmem, al, bh, id, 1);
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             su32(&mb_mma))
+                         : "memory");
+        }
+        mma_out = true;
+        // C into the staging tile while the MMAs run, then the next tile's C
+#pragma unroll
+        for (int i = 0; i < 16; i++) {
+            const int e = tid + 256 * i, r = e >> 5, c4 = (e & 31) * 4;
+            *reinterpret_cast<float4 *>(S + r * UT_SLD + c4) = creg[i];
+        }
+        if (more) load_c(t + gridDim.x);
+        if (__syncthreads_or(!wait_mb(&mb_mma, ph_mma))) { failed = true; break; }
+        ph_mma ^= 1u;
+        mma_out = false;
+        if (more && tid == 0) issue_ops(t + gridDim.x);   // operands are free
+        ops_out = more;
+        // S[row][64h + j] += alpha * acc(row, 64h + j), row = 32q + lane
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        float *srow = S + (32 * q + lane) * UT_SLD + 64 * h;
+#pragma unroll
+        for (int half = 0; half < 2; half++) {
+            uint32_t d[32];
+            const unsigned taddr = tmem + ((unsigned)(32 * q) << 16) + (unsigned)(64 * h + 32 * half);
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                : "=r"(d[0]), "=r"(d[1]), "=r"(d[2]), "=r"(d[3]), "=r"(d[4]), "=r"(d[5]), "=r"(d[6]), "=r"(d[7]),
+                  "=r"(d[8]), "=r"(d[9]), "=r"(d[10]), "=r"(d[11]), "=r"(d[12]), "=r"(d[13]), "=r"(d[14]),
+                  "=r"(d[15]), "=r"(d[16]), "=r"(d[17]), "=r"(d[18]), "=r"(d[19]), "=r"(d[20]), "=r"(d[21]),
+                  "=r"(d[22]), "=r"(d[23]), "=r"(d[24]), "=r"(d[25]), "=r"(d[26]), "=r"(d[27]), "=r"(d[28]),
+                  "=r"(d[29]), "=r"(d[30]), "=r"(d[31])
+                : "r"(taddr)
+                : "memory");
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+            for (int j = 0; j < 32; j += 4) {
+                float4 v = *reinterpret_cast<float4 *>(srow + 32 * half + j);
+                v.x = fmaf(g.alpha, __uint_as_float(d[j]), v.x);
+                v.y = fmaf(g.alpha, __uint_as_float(d[j + 1]), v.y);
+                v.z = fmaf(g.alpha, __uint_as_float(d[j + 2]), v.z);
+                v.w = fmaf(g.alpha, __uint_as_float(d[j + 3]), v.w);
+                *reinterpret_cast<float4 *>(srow + 32 * half + j) = v;
+            }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();   // S complete; TMEM read out before the next tile's MMAs
+#pragma unroll
+        for (int i = 0; i < 16; i++) {
+            const int e = tid + 256 * i, r = e >> 5, c4 = (e & 31) * 4;
+            if (r < rows && c4 < cols)
+                *reinterpret_cast<float4 *>(ctile + (int64_t)r * g.rsc + c4) =
+                    *reinterpret_cast<const float4 *>(S + r * UT_SLD + c4);
+        }
+        __syncthreads();   // S is read out before the next tile refills it
+    }
+    if (failed) {
+        if (tid == 0) atomicExch(g.err, 1);
+        // our copies / MMAs may still be in flight: wait (bounded) before leaving
+        if (ops_out) wait_mb(&mb_ld, ph_ld);
+        if (mma_out) wait_mb(&mb_mma, ph_mma);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(UT) : "memory");
+    }
+}
+
 }  // namespace
 
 int gemm_tc(ddla_handle h, int prec, i64 m, i64 n, i64 k, float alpha, View<const float> A, View<const float> B,
@@ -281,6 +509,30 @@ int gemm_tc(ddla_handle h, int prec, i64 m, i64 n, i64 k, float alpha, View<cons
     if (prec != DDLA_PREC_TF32X3) {
         set_error("gemm_tc: only the 3xTF32 split is implemented");
         return DDLA_ERR_UNSUPPORTED;
+    }
+    if (beta == 1.f && k > 0 && k <= TK && uplo == DDLA_DENSE && C.cs == 1 && (n & 3) == 0 && (C.rs & 3) == 0 &&
+        (((uintptr_t)C.p) & 15) == 0 && tune_get("update.tc", 1) != 0) {
+        // rank-<=64 update: packed operands + persistent tensor-core kernel
+        static size_t uavail = 0;
+        if (!uavail) DDLA_TRY(max_dyn_smem((const void *)k_tc_update, h->smem_optin, &uavail));
+        if (UT_SMEM <= uavail) {
+            const i64 ntm = (m + UT - 1) / UT, ntn = (n + UT - 1) / UT;
+            float *pa, *pb;
+            DDLA_TRY(workspace(h, WS_TC, sizeof(float) * 2 * (size_t)UT_PART * (ntm + ntn), (void **)&pa));
+            pb = pa + 2 * (size_t)UT_PART * ntm;
+            auto grid_of = [](i64 tot) { return (unsigned)((tot + 255) / 256 < 4096 ? (tot + 255) / 256 : 4096); };
+            k_tc_pack<<<grid_of(ntm * UT * (TK / 4)), 256, 0, h->stream>>>(A.p, A.rs, A.cs, m, (int)k, pa, ntm);
+            DDLA_LAUNCHED();
+            View<const float> Bt = B.t();   // n x k: columns of B as rows
+            k_tc_pack<<<grid_of(ntn * UT * (TK / 4)), 256, 0, h->stream>>>(Bt.p, Bt.rs, Bt.cs, n, (int)k, pb, ntn);
+            DDLA_LAUNCHED();
+            const i64 tiles = ntm * ntn;
+            const int grid = (int)(tiles < h->sm_count ? tiles : h->sm_count);
+            TuArgs a{m, n, (int)ntm, (int)ntn, pa, pb, alpha, C.p, C.rs, h->d_info + INFO_TIMEOUT};
+            k_tc_update<<<grid, TC_THREADS, UT_SMEM, h->stream>>>(a);
+            DDLA_LAUNCHED();
+            return 0;
+        }
     }
     static size_t avail = 0;
     if (!avail) DDLA_TRY(max_dyn_smem((const void *)k_tc_tf32x3, h->smem_optin, &avail));

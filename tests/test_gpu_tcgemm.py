@@ -46,3 +46,11 @@ def test_tf32x3_alpha_beta(ddla):
 
 def test_fp32_reference_path(ddla):
     assert _run(ddla, ddla.PREC_FP32, 300, 200, 64, -1.0, 1.0, 5) <= 2e-6
+
+
+@pytest.mark.parametrize("m,n,k", [(128, 128, 64), (300, 200, 64), (129, 257, 17), (1000, 900, 64), (64, 1, 64),
+                                   (2000, 4100, 64), (1, 300, 8)])
+def test_tf32x3_rank_update_path(ddla, m, n, k):
+    # beta = 1 and k <= 64: the packed-operand persistent update kernel
+    err = _run(ddla, ddla.PREC_TF32X3, m, n, k, -1.0, 1.0, m + 3 * n + k)
+    assert err <= 2e-5, err
