@@ -7,7 +7,10 @@ precision, then FP64 refinement on the GPU until the relative backward error
 max ||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf) <= 1e-14.
 
 A step = one complete solve (FP64 -> FP32 conversion, factorization, initial
-solve, refinement loop) from the FP64 A and b resident in HBM.  The credited
+solve, refinement loop) from the FP64 A and b resident in HBM.  The default
+precision is FP32 storage with 3xTF32 tensor-core trailing updates; the
+refinement for one right-hand side is flexible GMRES in FP64 preconditioned
+by the FP32 factors.  The credited
 work is the algorithmic LU+solve count 2/3 n^3 + 2 n^2 flops (refinement flops
 are not credited).  A step only counts if it reaches the tolerance.
 
@@ -427,7 +430,7 @@ def main():
     apply_tune(args)
 
     prec_map = {"fp32": D.PREC_FP32, "tf32x3": D.PREC_TF32X3, "bf16x3": D.PREC_BF16X3, "fp64": D.PREC_FP64}
-    prec_name = args.precision if args.precision != "auto" else os.environ.get("DDLA_BENCH_PREC", "fp32")
+    prec_name = args.precision if args.precision != "auto" else os.environ.get("DDLA_BENCH_PREC", "tf32x3")
     prec = prec_map[prec_name]
     n = args.n
     stream = torch.cuda.Stream()
@@ -478,24 +481,38 @@ def main():
                              "bytes": by.value}
     L.ddla_timing_enable(0)
     f64_peak, f32_peak = dv.measure_peaks()
-    upd = per["trailing_update_gemm"]
     dom = max(per, key=lambda k: per[k]["ms_per_step"])
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
-    if prec in (D.PREC_TF32X3, D.PREC_BF16X3):
-        bound, peak, peak_src = "tensor", peaks.get("bf16_tflops", 1900.0), "MEASURED_PEAKS.json bf16_tflops (burst)"
-    elif prec == D.PREC_FP64:
-        bound, peak, peak_src = "tensor", f64_peak, "live DMMA probe (ddla_measure_peaks)"
-    else:
-        bound, peak, peak_src = "fp32-cuda-core", f32_peak, "live FFMA probe (ddla_measure_peaks)"
-    upd_ms_launch = upd["ms_per_step"] * args.steps / max(upd["launches"], 1)
-    upd_flops_launch = upd["flops"] / max(upd["launches"], 1)
-    achieved = upd_flops_launch / (upd_ms_launch * 1e-3) / 1e12 if upd["launches"] else 0.0
-    roofline = {"bound": bound, "kernel": "trailing_update_gemm", "achieved": achieved, "peak": peak,
-                "unit": "TFLOP/s", "frac": achieved / peak if peak else None, "traffic": None,
-                "peak_source": peak_src, "dominant_class": dom,
-                "classes_ms_per_step": {k: round(v["ms_per_step"], 4) for k, v in per.items()},
-                "note": "achieved = algorithmic 2*m*n*k per trailing-update launch / its CUDA-event duration"}
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    hbm_src = "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6.8 TB/s"
+
+    def hbm_entry(cls, kernel, traffic, note):
+        v = per[cls]
+        nl = max(v["launches"], 1)
+        ms_launch = v["ms_per_step"] * args.steps / nl
+        gbs = (v["bytes"] / nl) / (ms_launch * 1e-3) / 1e9 if v["launches"] else 0.0
+        tfs = (v["flops"] / nl) / (ms_launch * 1e-3) / 1e12 if v["launches"] else 0.0
+        return {"bound": "hbm", "kernel": kernel, "achieved": gbs, "peak": hbm, "unit": "GB/s",
+                "frac": gbs / hbm if hbm else None, "traffic": traffic, "peak_source": hbm_src,
+                "launches_per_step": v["launches"] / args.steps, "us_per_launch": ms_launch * 1e3,
+                "algorithmic_bytes_per_launch": v["bytes"] / nl, "tflops": tfs, "note": note}
+
+    upd_kernel = {D.PREC_TF32X3: "k_tc_update (tcgen05 3xTF32, persistent)", D.PREC_FP64: "k_gemm_f64 (DMMA)"}.get(
+        prec, "k_supdate (FP32 CUDA cores)")
+    # DRAM bytes of one launch from the ncu captures summarised in profiles/
+    # (k_panel_lu: panel of 6912 x 64 FP32, the 21st launch of the solve)
+    roof_panel = hbm_entry("lu_panel", "k_panel_lu (LU panel, 16-CTA cluster)",
+                           1.81e6 if prec != D.PREC_FP64 else None,
+                           "latency-bound: one cluster barrier and two DSMEM round trips per column; algorithmic "
+                           "bytes = the panel read and written once (2 m w 4 B)")
+    roof_update = hbm_entry("trailing_update_gemm", upd_kernel, None,
+                            "rank-64 update C -= L21 U12: algorithmic bytes = C read + written + the two panels; "
+                            "tflops = 2 m n k per launch over its duration")
+    roofline = dict(roof_panel if dom == "lu_panel" else roof_update)
+    roofline["dominant_class"] = dom
+    roofline["classes_ms_per_step"] = {k: round(v["ms_per_step"], 4) for k, v in per.items()}
+    roofline["other"] = roof_update if dom == "lu_panel" else roof_panel
 
     # end-to-end through the host C ABI with pinned host buffers
     e2e = None
@@ -535,10 +552,12 @@ def main():
         last = reps[-1]
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-               "vs_baseline": None, "dtype": "f32-factor+f64-refine" if prec != D.PREC_FP64 else "f64",
+               "vs_baseline": None, "dtype": {D.PREC_TF32X3: "f32 factor with 3xTF32 tensor-core updates + f64 refinement",
+                         D.PREC_FP64: "f64"}.get(prec, "f32 factor + f64 refinement"),
                "data": "synthetic N(0,1), seeded, inputs 512 MB > L2 (no flush needed)",
                "config": {"workload": f"LU (partial pivoting) + solve, n={n}, 1 RHS, mixed {prec_name} factor + "
-                                      f"FP64 iterative refinement to backward error <= {TOL:g}",
+                                      f"FP64 refinement (flexible GMRES preconditioned by the factors) to "
+                                      f"backward error <= {TOL:g}",
                           "n": n, "nrhs": 1, "precision": prec_name, "tol": TOL, "parallelism": f"replicas{world}",
                           "l2": "inputs larger than L2"},
                "backward_error": last["backward_error"], "refine_iterations": last["iterations"],
