@@ -165,6 +165,32 @@ int pick_nb(int nb, int dflt) { return nb > 0 ? (nb > DIAG_MAX ? DIAG_MAX : nb) 
 }  // namespace
 
 // ------------------------------------------------------------------ LU (pivoted)
+// U12 columns in place: X[0:b, c] <- inv(L11)[0:b, 0:b] X[0:b, c] for the
+// U12CW columns of this CTA (inv row-major, ld TRI_TB).  The CTA reads its
+// columns whole into shared memory first, so the product can overwrite them;
+// thread t forms column t % U12CW, rows t / U12CW + 8 i.
+constexpr int U12CW = 32;
+template <typename T>
+__global__ void __launch_bounds__(256) k_u12_inplace(T *X, i64 rs, i64 cs, int b, i64 ncol, const T *inv) {
+    __shared__ T si[TRI_TB][TRI_TB + 1];
+    __shared__ T sx[TRI_TB][U12CW + 1];
+    const i64 c0 = (i64)blockIdx.x * U12CW;
+    const int tid = threadIdx.x;
+    for (int e = tid; e < b * b; e += 256) si[e / b][e % b] = inv[(e / b) * TRI_TB + (e % b)];
+    for (int e = tid; e < b * U12CW; e += 256) {
+        const int r = e / U12CW, c = e % U12CW;
+        sx[r][c] = (c0 + c < ncol) ? X[r * rs + (c0 + c) * cs] : T(0);
+    }
+    __syncthreads();
+    const int c = tid % U12CW, r0 = tid / U12CW;   // 8 row groups
+    if (c0 + c >= ncol) return;
+    for (int r = r0; r < b; r += 256 / U12CW) {
+        T acc = T(0);
+        for (int k = 0; k < b; k++) acc = fma(si[r][k], sx[k][c], acc);
+        X[r * rs + (c0 + c) * cs] = acc;
+    }
+}
+
 __global__ void k_iota(int *p, i64 n) {
     for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < n; e += (i64)gridDim.x * blockDim.x) p[e] = (int)e;
 }
@@ -216,6 +242,13 @@ int getrf(ddla_handle h, i64 n, View<T> A, int32_t *d_piv, int prec, int nb, int
         if (nc <= 0) return 0;
         Timed t(s, TC_TRSM, (double)b * b * nc, sizeof(T) * (2.0 * b * nc + b * b));
         View<T> blk = A.sub(j0, b, c, nc);
+        if (nc <= 4 * U12CW * 152 || tune_get("u12.gemm", 0) == 0) {
+            // one kernel, in place: each CTA owns 32 whole columns
+            k_u12_inplace<T><<<(unsigned)((nc + U12CW - 1) / U12CW), 256, 0, s>>>(blk.p, blk.rs, blk.cs, b, nc,
+                                                                                  inv_of(j0));
+            DDLA_LAUNCHED();
+            return 0;
+        }
         View<T> Tm{tmp + c, b, nc, n, 1};
         DDLA_TRY(copy2d_on<T>(s, View<const T>{blk.p, b, nc, blk.rs, blk.cs}, Tm));
         return gemm_any<T>(h, tprec, b, nc, b, T(1), View<const T>{inv_of(j0), b, b, TRI_TB, 1},
@@ -236,8 +269,9 @@ int getrf(ddla_handle h, i64 n, View<T> A, int32_t *d_piv, int prec, int nb, int
             DDLA_TRY(u12(j0, b, j1, b1));
             {
                 Timed t(s, TC_UPDATE, 2.0 * r * b1 * b, sizeof(T) * (2.0 * r * b1 + r * b + b * b1));
-                DDLA_TRY(gemm_any<T>(h, prec, r, b1, b, T(-1), A21, View<const T>{A12.p, b, b1, A12.rs, A12.cs}, T(1),
-                                     A.sub(j1, r, j1, b1)));
+                // narrow: one launch on the CUDA cores (FP32) beats packing for the tensor cores
+                DDLA_TRY(gemm_any<T>(h, sizeof(T) == 4 ? DDLA_PREC_FP32 : prec, r, b1, b, T(-1), A21,
+                                     View<const T>{A12.p, b, b1, A12.rs, A12.cs}, T(1), A.sub(j1, r, j1, b1)));
             }
             DDLA_CUDA(cudaEventRecord(h->ev_ready, s));
             DDLA_CUDA(cudaStreamWaitEvent(h->side, h->ev_ready, 0));
