@@ -21,11 +21,13 @@ template <typename T>
 int panel_width_for(ddla_handle h, i64 m);
 template <typename T>
 int panel_factor(ddla_handle h, cudaStream_t s, View<T> X, i64 pc, int w, int32_t *d_piv, i64 row_base, int *d_info,
-                 T *inv);
+                 T *inv, int slot);
+template <typename T>
+int panel_swap_cols(ddla_handle h, View<T> X, i64 ncols, i64 skip0, i64 skipw, int *perm, int slot);
 template <typename T>
 int copy2d_on(cudaStream_t s, View<const T> X, View<T> Y);
 template <typename T>
-int panel_swap_rest(ddla_handle h, View<T> X, i64 pc, int w, int *perm);
+int panel_swap_rest(ddla_handle h, View<T> X, i64 pc, int w, int *perm, int slot);
 template <typename T>
 int apply_perm(ddla_handle h, View<T> B, const int32_t *d_piv, i64 n, bool forward);
 
@@ -231,7 +233,7 @@ int getrf(ddla_handle h, i64 n, View<T> A, int32_t *d_piv, int prec, int nb, int
     auto panel = [&](cudaStream_t st, i64 j0, int b) -> int {
         Timed t(st, TC_PANEL, 2.0 * b * b * ((n - j0) - b / 3.0), 2.0 * sizeof(T) * (n - j0) * (double)b);
         return panel_factor<T>(h, st, A.sub(j0, n - j0, 0, n), j0, b, d_piv + j0, j0, h->d_info + INFO_PIVOT,
-                               inv_of(j0));
+                               inv_of(j0), (int)((j0 / w) & 1));
     };
     // U12 columns [c, c + nc) of the row block of panel j0: inv(L11) times a
     // copy of them (the same blocked inverse the general TRSM applies)
@@ -257,8 +259,15 @@ int getrf(ddla_handle h, i64 n, View<T> A, int32_t *d_piv, int prec, int nb, int
     DDLA_TRY(panel(s, 0, (int)(n < w ? n : w)));
     for (i64 j0 = 0; j0 < n; j0 += w) {
         const int b = (int)(n - j0 < w ? n - j0 : w);
-        DDLA_TRY(panel_swap_rest<T>(h, A.sub(j0, n - j0, 0, n), j0, b, d_perm ? d_perm + j0 : nullptr));
+        const int slot = (int)((j0 / w) & 1);
         const i64 r = n - j0 - b;
+        const int b1n = (int)(r < w ? r : w);
+        if (!ahead || r <= 0) {
+            DDLA_TRY(panel_swap_rest<T>(h, A.sub(j0, n - j0, 0, n), j0, b, d_perm ? d_perm + j0 : nullptr, slot));
+        } else {
+            // the next panel's columns now; the rest after the next panel started
+            DDLA_TRY(panel_swap_cols<T>(h, A.sub(j0, n - j0, j0 + b, b1n), b1n, b1n, 0, nullptr, slot));
+        }
         if (r <= 0) break;
         View<T> A12 = A.sub(j0, b, j0 + b, r);
         View<const T> A21{A.p + (j0 + b) * A.rs + j0 * A.cs, r, b, A.rs, A.cs};
@@ -277,6 +286,11 @@ int getrf(ddla_handle h, i64 n, View<T> A, int32_t *d_piv, int prec, int nb, int
             DDLA_CUDA(cudaStreamWaitEvent(h->side, h->ev_ready, 0));
             DDLA_TRY(panel(h->side, j1, b1));
             DDLA_CUDA(cudaEventRecord(h->ev_panel, h->side));
+            // interchanges of every other column: left of the panel and right
+            // of the next panel (the touched-row list of this panel is kept in
+            // its own slot while the next panel writes the other)
+            DDLA_TRY(panel_swap_cols<T>(h, A.sub(j0, n - j0, 0, n), n - b - b1, j0, (i64)b + b1,
+                                        d_perm ? d_perm + j0 : nullptr, slot));
             const i64 rest = r - b1;
             if (rest > 0) {
                 DDLA_TRY(u12(j0, b, j1 + b1, rest));

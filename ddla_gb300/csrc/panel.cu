@@ -595,13 +595,20 @@ int tri_inverse_on(cudaStream_t s, bool lower, bool unit, View<const T> A, i64 n
 
 // inv (optional, TRI_TB x TRI_TB): receives the inverse of the panel's
 // unit-lower diagonal block L11 (zeros outside it), for the row-block solve.
+// WS_PIV layout: two touched-row lists (count, rows, sources), selected by
+// `slot`, so that the interchanges of panel k can still be applied while
+// panel k+1 is being factored; then the origin scratch of the fallback kernel.
+constexpr int TOUCH_INTS = 1 + 2 * LASWP_MAXT;
+
 template <typename T>
 int panel_factor(ddla_handle h, cudaStream_t s, View<T> X, i64 pc, int w, int32_t *d_piv, i64 row_base,
-                 int *d_info, T *inv) {
+                 int *d_info, T *inv, int slot) {
     const i64 m = X.rows;
     int *tbuf;
-    DDLA_TRY(workspace(h, WS_PIV, sizeof(int) * (size_t)(1 + 2 * LASWP_MAXT + m), (void **)&tbuf));
-    int *tcount = tbuf, *trows = tbuf + 1, *tsrc = tbuf + 1 + LASWP_MAXT, *origin = tbuf + 1 + 2 * LASWP_MAXT;
+    DDLA_TRY(workspace(h, WS_PIV, sizeof(int) * (size_t)(2 * TOUCH_INTS + m), (void **)&tbuf));
+    int *origin = tbuf + 2 * TOUCH_INTS;
+    tbuf += slot * TOUCH_INTS;
+    int *tcount = tbuf, *trows = tbuf + 1, *tsrc = tbuf + 1 + LASWP_MAXT;
     PanelArgs<T> a;
     a.P = X.p + pc * X.cs;
     a.rs = X.rs;
@@ -656,23 +663,30 @@ int panel_factor(ddla_handle h, cudaStream_t s, View<T> X, i64 pc, int w, int32_
     return 0;
 }
 
-// Apply the interchanges of the last panel_factor to the other columns of the
-// rows of X (and to the permutation vector), on the handle's stream.
+// Apply the interchanges of the panel factored with `slot` to the columns
+// c' of the rows of X, for c' in [0, ncols) mapped to c' (c' < skip0) or
+// c' + skipw, and to the permutation vector (if given), on the handle's stream.
 template <typename T>
-int panel_swap_rest(ddla_handle h, View<T> X, i64 pc, int w, int *perm) {
+int panel_swap_cols(ddla_handle h, View<T> X, i64 ncols, i64 skip0, i64 skipw, int *perm, int slot) {
     cudaStream_t s = h->stream;
     int *tbuf;
-    DDLA_TRY(workspace(h, WS_PIV, sizeof(int) * (size_t)(1 + 2 * LASWP_MAXT + X.rows), (void **)&tbuf));
+    DDLA_TRY(workspace(h, WS_PIV, sizeof(int) * (size_t)(2 * TOUCH_INTS + X.rows), (void **)&tbuf));
+    tbuf += slot * TOUCH_INTS;
     int *tcount = tbuf, *trows = tbuf + 1, *tsrc = tbuf + 1 + LASWP_MAXT;
-    i64 other = X.cols - w;
-    unsigned grid = (unsigned)((other > 0 ? other + 31 : 0) / 32) + (perm ? 1u : 0u);
+    unsigned grid = (unsigned)((ncols > 0 ? ncols + 31 : 0) / 32) + (perm ? 1u : 0u);
     if (grid > 0) {
         // the permutation vector, when given, rides along in one more block
-        k_laswp_list<T><<<grid, 256, 0, s>>>(X.p, X.rs, X.cs, other > 0 ? other : 0, pc, w, tcount, trows, tsrc,
-                                             perm);
+        k_laswp_list<T><<<grid, 256, 0, s>>>(X.p, X.rs, X.cs, ncols > 0 ? ncols : 0, skip0, skipw, tcount, trows,
+                                             tsrc, perm);
         DDLA_LAUNCHED();
     }
     return 0;
+}
+
+// All columns of X outside the panel at pc (width w).
+template <typename T>
+int panel_swap_rest(ddla_handle h, View<T> X, i64 pc, int w, int *perm, int slot) {
+    return panel_swap_cols<T>(h, X, X.cols - w, pc, w, perm, slot);
 }
 
 // Y[k] = X[perm[k]] for the rows of B (forward) using a precomputed
@@ -721,10 +735,13 @@ int apply_perm(ddla_handle h, View<T> B, const int32_t *d_piv, i64 n, bool forwa
 template int panel_width_for<double>(ddla_handle, i64);
 template int panel_width_for<float>(ddla_handle, i64);
 template int panel_factor<double>(ddla_handle, cudaStream_t, View<double>, i64, int, int32_t *, i64, int *,
-                                  double *);
-template int panel_factor<float>(ddla_handle, cudaStream_t, View<float>, i64, int, int32_t *, i64, int *, float *);
-template int panel_swap_rest<double>(ddla_handle, View<double>, i64, int, int *);
-template int panel_swap_rest<float>(ddla_handle, View<float>, i64, int, int *);
+                                  double *, int);
+template int panel_factor<float>(ddla_handle, cudaStream_t, View<float>, i64, int, int32_t *, i64, int *, float *,
+                                 int);
+template int panel_swap_rest<double>(ddla_handle, View<double>, i64, int, int *, int);
+template int panel_swap_rest<float>(ddla_handle, View<float>, i64, int, int *, int);
+template int panel_swap_cols<double>(ddla_handle, View<double>, i64, i64, i64, int *, int);
+template int panel_swap_cols<float>(ddla_handle, View<float>, i64, i64, i64, int *, int);
 template int permute_rows<double>(ddla_handle, View<double>, const int *, i64, bool);
 template int permute_rows<float>(ddla_handle, View<float>, const int *, i64, bool);
 template int apply_perm<double>(ddla_handle, View<double>, const int32_t *, i64, bool);

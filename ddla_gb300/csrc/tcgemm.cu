@@ -16,6 +16,7 @@
 // the same kind of kernel (see the comment at its definition).
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <cstdint>
 
 #include "common.cuh"
@@ -526,8 +527,14 @@ int gemm_tc(ddla_handle h, int prec, i64 m, i64 n, i64 k, float alpha, View<cons
             View<const float> Bt = B.t();   // n x k: columns of B as rows
             k_tc_pack<<<grid_of(ntn * UT * (TK / 4)), 256, 0, h->stream>>>(Bt.p, Bt.rs, Bt.cs, n, (int)k, pb, ntn);
             DDLA_LAUNCHED();
+            // a few tiles per CTA rather than one CTA per SM for the whole
+            // update: CTAs retire often, so the look-ahead panel (a 16-CTA
+            // cluster on a high-priority stream) finds free SMs while the
+            // update runs
             const i64 tiles = ntm * ntn;
-            const int grid = (int)(tiles < h->sm_count ? tiles : h->sm_count);
+            const i64 per = std::max<int64_t>(1, tune_get("update.tiles_per_cta", 4));
+            const i64 want = (tiles + per - 1) / per;
+            const int grid = (int)(want < 65535 ? want : 65535);
             TuArgs a{m, n, (int)ntm, (int)ntn, pa, pb, alpha, C.p, C.rs, h->d_info + INFO_TIMEOUT};
             k_tc_update<<<grid, TC_THREADS, UT_SMEM, h->stream>>>(a);
             DDLA_LAUNCHED();
