@@ -381,7 +381,9 @@ template <typename T>
 int potrf(ddla_handle h, int uplo, i64 n, View<T> A, int prec, int nb) {
     if (n == 0) return 0;
     prec = prec_of<T>(prec);
-    nb = pick_nb(nb, DIAG_MAX);
+    // FP32 factors of the mixed solver: 64-wide blocks, so the trailing
+    // updates are rank-64 (the tensor-core update kernel's shape)
+    nb = pick_nb(nb, sizeof(T) == 4 ? 64 : DIAG_MAX);
     // The upper factorization is the lower one of the transposed view.
     View<T> L = (uplo == DDLA_UPPER) ? A.t() : A;
     for (i64 j0 = 0; j0 < n; j0 += nb) {

@@ -331,8 +331,25 @@ struct TuArgs {
     float alpha;
     float *C;
     int64_t rsc;
+    int uplo;               // DDLA_DENSE, or the triangle of C that is updated (m == n)
     int *err;
 };
+
+// Tile t of the enumeration: row-major over all tiles (dense), or over the
+// tiles on and below (DDLA_LOWER) / on and above (DDLA_UPPER) the diagonal.
+__device__ __forceinline__ void tu_tile(const TuArgs &g, int t, int *mt, int *nt) {
+    if (g.uplo == DDLA_DENSE) {
+        *mt = t / g.ntn;
+        *nt = t % g.ntn;
+        return;
+    }
+    // triangular numbering: row i holds tiles i*(i+1)/2 .. i*(i+1)/2 + i
+    int i = (int)((sqrtf(8.f * (float)t + 1.f) - 1.f) * 0.5f);
+    while ((i + 1) * (i + 2) / 2 <= t) i++;
+    while (i * (i + 1) / 2 > t) i--;
+    const int j = t - i * (i + 1) / 2;
+    if (g.uplo == DDLA_LOWER) { *mt = i; *nt = j; } else { *mt = j; *nt = i; }
+}
 
 __device__ __forceinline__ void bulk_g2s(unsigned dst, const void *src, unsigned bytes, unsigned mbar) {
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
@@ -347,7 +364,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_update(TuArgs g) {
     __shared__ __align__(8) unsigned long long mb_ld, mb_mma;
     __shared__ unsigned tmem_slot;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int total = g.ntm * g.ntn;
+    const int total = g.uplo == DDLA_DENSE ? g.ntm * g.ntn : g.ntm * (g.ntm + 1) / 2;
     if ((int)blockIdx.x >= total) return;
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(&tmem_slot)),
@@ -366,7 +383,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_update(TuArgs g) {
     const unsigned tmem = tmem_slot;
     constexpr uint32_t id = idesc_tf32_128();
     auto issue_ops = [&](int t) {   // thread 0: the four operand tiles of tile t
-        const int mt = t / g.ntn, nt = t % g.ntn;
+        int mt, nt;
+        tu_tile(g, t, &mt, &nt);
         const float *a = g.Ap + (size_t)mt * 2 * UT_PART, *b = g.Bp + (size_t)nt * 2 * UT_PART;
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(&mb_ld)),
                      "r"((unsigned)UT_OPS)
@@ -378,7 +396,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_update(TuArgs g) {
     };
     // rows and bytes per row of tile t
     auto tile_rows = [&](int t, int *rows, unsigned *bytes) {
-        const int mt = t / g.ntn, nt = t % g.ntn;
+        int mt, nt;
+        tu_tile(g, t, &mt, &nt);
         const int64_t r_left = g.m - (int64_t)mt * UT, c_left = g.n - (int64_t)nt * UT;
         *rows = (int)(r_left < UT ? r_left : UT);
         *bytes = (unsigned)((c_left < UT ? c_left : UT) * 4);
@@ -402,7 +421,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_update(TuArgs g) {
         unsigned bytes;
         tile_rows(t, &rows, &bytes);
         const int cols = (int)(bytes / 4);
-        const float *ct = g.C + (int64_t)(t / g.ntn) * UT * g.rsc + (int64_t)(t % g.ntn) * UT;
+        int tm, tn;
+        tu_tile(g, t, &tm, &tn);
+        const float *ct = g.C + (int64_t)tm * UT * g.rsc + (int64_t)tn * UT;
 #pragma unroll
         for (int i = 0; i < 16; i++) {
             const int e = tid + 256 * i, r = e >> 5, c4 = (e & 31) * 4;
@@ -416,8 +437,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_update(TuArgs g) {
         unsigned bytes;
         tile_rows(t, &rows, &bytes);
         const int cols = (int)(bytes / 4);
-        const int mt = t / g.ntn, nt = t % g.ntn;
+        int mt, nt;
+        tu_tile(g, t, &mt, &nt);
         float *ctile = g.C + (int64_t)mt * UT * g.rsc + (int64_t)nt * UT;
+        const bool diag = g.uplo != DDLA_DENSE && mt == nt;
         const bool more = t + (int)gridDim.x < total;
         if (__syncthreads_or(!wait_mb(&mb_ld, ph_ld))) { failed = true; break; }
         ph_ld ^= 1u;
@@ -482,9 +505,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_update(TuArgs g) {
 #pragma unroll
         for (int i = 0; i < 16; i++) {
             const int e = tid + 256 * i, r = e >> 5, c4 = (e & 31) * 4;
-            if (r < rows && c4 < cols)
-                *reinterpret_cast<float4 *>(ctile + (int64_t)r * g.rsc + c4) =
-                    *reinterpret_cast<const float4 *>(S + r * UT_SLD + c4);
+            if (r < rows && c4 < cols) {
+                if (!diag) {
+                    *reinterpret_cast<float4 *>(ctile + (int64_t)r * g.rsc + c4) =
+                        *reinterpret_cast<const float4 *>(S + r * UT_SLD + c4);
+                } else {   // diagonal tile of a triangular update: its triangle only
+#pragma unroll
+                    for (int x = 0; x < 4; x++) {
+                        const int c = c4 + x;
+                        if (g.uplo == DDLA_LOWER ? c <= r : c >= r) ctile[(int64_t)r * g.rsc + c] = S[r * UT_SLD + c];
+                    }
+                }
+            }
         }
         __syncthreads();   // S is read out before the next tile refills it
     }
@@ -511,8 +543,8 @@ int gemm_tc(ddla_handle h, int prec, i64 m, i64 n, i64 k, float alpha, View<cons
         set_error("gemm_tc: only the 3xTF32 split is implemented");
         return DDLA_ERR_UNSUPPORTED;
     }
-    if (beta == 1.f && k > 0 && k <= TK && uplo == DDLA_DENSE && C.cs == 1 && (n & 3) == 0 && (C.rs & 3) == 0 &&
-        (((uintptr_t)C.p) & 15) == 0 && tune_get("update.tc", 1) != 0) {
+    if (beta == 1.f && k > 0 && k <= TK && (uplo == DDLA_DENSE || m == n) && C.cs == 1 && (n & 3) == 0 &&
+        (C.rs & 3) == 0 && (((uintptr_t)C.p) & 15) == 0 && tune_get("update.tc", 1) != 0) {
         // rank-<=64 update: packed operands + persistent tensor-core kernel
         static size_t uavail = 0;
         if (!uavail) DDLA_TRY(max_dyn_smem((const void *)k_tc_update, h->smem_optin, &uavail));
@@ -531,11 +563,11 @@ int gemm_tc(ddla_handle h, int prec, i64 m, i64 n, i64 k, float alpha, View<cons
             // update: CTAs retire often, so the look-ahead panel (a 16-CTA
             // cluster on a high-priority stream) finds free SMs while the
             // update runs
-            const i64 tiles = ntm * ntn;
+            const i64 tiles = uplo == DDLA_DENSE ? ntm * ntn : ntm * (ntm + 1) / 2;
             const i64 per = std::max<int64_t>(1, tune_get("update.tiles_per_cta", 4));
             const i64 want = (tiles + per - 1) / per;
             const int grid = (int)(want < 65535 ? want : 65535);
-            TuArgs a{m, n, (int)ntm, (int)ntn, pa, pb, alpha, C.p, C.rs, h->d_info + INFO_TIMEOUT};
+            TuArgs a{m, n, (int)ntm, (int)ntn, pa, pb, alpha, C.p, C.rs, uplo, h->d_info + INFO_TIMEOUT};
             k_tc_update<<<grid, TC_THREADS, UT_SMEM, h->stream>>>(a);
             DDLA_LAUNCHED();
             return 0;

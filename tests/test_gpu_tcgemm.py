@@ -54,3 +54,25 @@ def test_tf32x3_rank_update_path(ddla, m, n, k):
     # beta = 1 and k <= 64: the packed-operand persistent update kernel
     err = _run(ddla, ddla.PREC_TF32X3, m, n, k, -1.0, 1.0, m + 3 * n + k)
     assert err <= 2e-5, err
+
+
+@pytest.mark.parametrize("n,k", [(128, 64), (300, 64), (515, 40), (1000, 64), (257, 8)])
+def test_tf32x3_update_transposed_b(ddla, n, k):
+    # C (n x n) += -A A^T with B = A^T given as a transposed view (rs = 1,
+    # cs = k): the shape of the Cholesky trailing update
+    import torch
+    from ddla_gb300 import device
+    g = torch.Generator().manual_seed(n + k)
+    A = torch.rand(n, k, generator=g, dtype=torch.float64) * 2 - 1
+    Cm = torch.rand(n, n, generator=g, dtype=torch.float64) * 2 - 1
+    ref = Cm.numpy() - A.numpy() @ A.numpy().T
+    scale = np.abs(A.numpy()) @ np.abs(A.numpy().T) + np.abs(Cm.numpy())
+    a, c = A.float().cuda(), Cm.float().cuda()
+    h = device.Handle(torch.cuda.current_stream())
+    rc = ddla.lib().ddla_dev_sgemm_tc(h.h, ddla.PREC_TF32X3, n, n, k, -1.0, C.c_void_p(a.data_ptr()), k, 1,
+                                      C.c_void_p(a.data_ptr()), 1, k, 1.0, C.c_void_p(c.data_ptr()), n, 1)
+    ddla._lib.check(rc, "sgemm_tc")
+    h.sync()
+    out = c.double().cpu().numpy()
+    h.close()
+    assert np.max(np.abs(out - ref) / scale) <= 2e-5
