@@ -241,6 +241,49 @@ def secondary(args):
             Cm.copy_(C0)
             step()
             return float(((Cm - ref).abs() / (A.abs() @ B.abs() + 0.5 * C0.abs())).max())
+    elif wl in ("symm", "trmm", "syr2k"):
+        n = args.n if args.n != N_DEFAULT else 4096
+        A, B, C0 = U(n, n), U(n, n), U(n, n)
+        Cm = C0.clone()
+        flush = L2Flush(torch, stream)
+        if wl == "symm":
+            flops = 2.0 * n ** 3
+            desc = f"SYMM C = A_sym B + 0.5 C (left, lower), {n}^3 FP64 U[-1,1]"
+
+            def step():
+                h.symm(D.LEFT, D.LOWER, 1.0, A, B, 0.5, Cm)
+
+            def ref_fn():
+                S = torch.tril(A) + torch.tril(A, -1).T
+                return S @ B + 0.5 * C0, S.abs() @ B.abs() + 0.5 * C0.abs()
+        elif wl == "trmm":
+            flops = 1.0 * n ** 3
+            desc = f"TRMM B = U B in place (left, upper, non-unit), {n}^3 FP64 U[-1,1]"
+
+            def step():
+                h.trmm(D.LEFT, D.UPPER, 0, 0, 1.0, A, Cm)
+
+            def ref_fn():
+                Tu = torch.triu(A)
+                return Tu @ C0, Tu.abs() @ C0.abs()
+        else:
+            flops = 2.0 * n ** 3
+            desc = f"SYR2K lower(C) = A B^T + B A^T + 0.5 C, m = k = {n}, FP64 U[-1,1]"
+
+            def step():
+                h.syr2k(D.LOWER, 1.0, A, B, 0.5, Cm)
+
+            def ref_fn():
+                return (torch.tril(A @ B.T + B @ A.T + 0.5 * C0),
+                        torch.tril(A.abs() @ B.abs().T + B.abs() @ A.abs().T + 0.5 * C0.abs()) + 1e-300)
+
+        def check_err():
+            Cm.copy_(C0)
+            step()
+            h.sync()
+            ref, scale = ref_fn()
+            got = torch.tril(Cm) if wl == "syr2k" else Cm
+            return float(((got - ref).abs() / scale).max())
     elif wl in ("einsum-a", "einsum-b"):
         if wl == "einsum-a":
             expr, sa, sb, sc = "bik,bkj->bij", (512, 256, 256), (512, 256, 256), (512, 256, 256)
@@ -401,7 +444,8 @@ def main():
     ap.add_argument("--precision", default="auto", choices=["auto", "fp32", "tf32x3", "bf16x3", "fp64", "ozaki"])
     ap.add_argument("--tune", action="append", default=[], metavar="KEY=VALUE",
                     help="library tuning key (ddla_tune_set) applied before the run; repeatable")
-    ap.add_argument("--workload", default="lu", choices=["lu", "gemm", "chol", "batched", "einsum-a", "einsum-b"])
+    ap.add_argument("--workload", default="lu", choices=["lu", "gemm", "chol", "batched", "einsum-a", "einsum-b",
+                                                         "symm", "trmm", "syr2k"])
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-n", type=int, default=4096)
     ap.add_argument("--no-cpu", action="store_true")

@@ -83,6 +83,13 @@ _SIGS = {
     "ddla_dsyrk": (C.c_int, [_i32, _i32, _i64, _i64, C.POINTER(_d), _pd, _i64, _i64, C.POINTER(_d), _pd, _i64,
                              _i64]),
     "ddla_dtrsm": (C.c_int, [_i32, _i32, _i32, _i32, _i64, _i64, C.POINTER(_d), _pd, _i64, _i64, _pd, _i64, _i64]),
+    "ddla_dsymm": (C.c_int, [_i32, _i32, _i32, _i32, _i64, _i64, C.POINTER(_d), _pd, _i64, _i64, _pd, _i64, _i64,
+                             C.POINTER(_d), _pd, _i64, _i64]),
+    "ddla_dsyr2k": (C.c_int, [_i32, _i32, _i32, _i64, _i64, C.POINTER(_d), _pd, _i64, _i64, _pd, _i64, _i64,
+                              C.POINTER(_d), _pd, _i64, _i64]),
+    "ddla_dtrmm": (C.c_int, [_i32, _i32, _i32, _i32, _i64, _i64, C.POINTER(_d), _pd, _i64, _i64, _pd, _i64, _i64]),
+    "ddla_dtrmm3": (C.c_int, [_i32, _i32, _i32, _i32, _i32, _i64, _i64, C.POINTER(_d), _pd, _i64, _i64, _pd, _i64,
+                              _i64, C.POINTER(_d), _pd, _i64, _i64]),
     "ddla_dgetrf": (C.c_int, [_i64, _pd, _i64, _i64, _pi, C.POINTER(Opts)]),
     "ddla_dgetrs": (C.c_int, [_i32, _i64, _i64, _pd, _i64, _i64, _pi, _pd, _i64, _i64]),
     "ddla_dgetrf_nopiv": (C.c_int, [_i64, _pd, _i64, _i64, C.POINTER(Opts)]),
@@ -102,6 +109,13 @@ _SIGS = {
     "ddla_dev_dgemmt": (C.c_int, [_h, _i32, _i32, _i32, _i64, _i64, _d, _pd, _i64, _i64, _pd, _i64, _i64, _d, _pd,
                                   _i64, _i64]),
     "ddla_dev_dtrsm": (C.c_int, [_h, _i32, _i32, _i32, _i32, _i64, _i64, _d, _pd, _i64, _i64, _pd, _i64, _i64]),
+    "ddla_dev_dsymm": (C.c_int, [_h, _i32, _i32, _i32, _i32, _i64, _i64, _d, _pd, _i64, _i64, _pd, _i64, _i64, _d,
+                                 _pd, _i64, _i64]),
+    "ddla_dev_dsyr2k": (C.c_int, [_h, _i32, _i32, _i32, _i64, _i64, _d, _pd, _i64, _i64, _pd, _i64, _i64, _d, _pd,
+                                  _i64, _i64]),
+    "ddla_dev_dtrmm": (C.c_int, [_h, _i32, _i32, _i32, _i32, _i64, _i64, _d, _pd, _i64, _i64, _pd, _i64, _i64]),
+    "ddla_dev_dtrmm3": (C.c_int, [_h, _i32, _i32, _i32, _i32, _i32, _i64, _i64, _d, _pd, _i64, _i64, _pd, _i64,
+                                  _i64, _d, _pd, _i64, _i64]),
     "ddla_dev_dgetrf": (C.c_int, [_h, _i64, _pd, _i64, _i64, _pi, C.POINTER(Opts)]),
     "ddla_dev_dgetrs": (C.c_int, [_h, _i32, _i64, _i64, _pd, _i64, _i64, _pi, _pd, _i64, _i64]),
     "ddla_dev_dpotrf": (C.c_int, [_h, _i32, _i64, _pd, _i64, _i64, C.POINTER(Opts)]),

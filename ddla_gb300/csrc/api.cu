@@ -276,6 +276,46 @@ static bool valid_trans(int t) { return t == DDLA_NO_TRANSPOSE || t == DDLA_TRAN
 static bool is_trans(int t) { return (t & DDLA_TRANSPOSE) != 0; }
 static bool valid_tri(int u) { return u == DDLA_LOWER || u == DDLA_UPPER; }
 
+static bool valid_conj(int c) { return c == 0 || c == 0x10; }  // ConjType, DDLA/Misc/Flags/ConjType.cs
+
+// op(X) as a view of shape rows x cols, X stored with strides (rs, cs).
+static View<const double> op_view(const double *p, i64 rows, i64 cols, i64 rs, i64 cs, int trans) {
+    if (is_trans(trans)) return View<const double>{p, cols, rows, rs, cs}.t();
+    return View<const double>{p, rows, cols, rs, cs};
+}
+
+// Structured-operand mode of a triangular op(A) (transposing flips the triangle).
+static int tri_mode(int uplo, int trans, int diag) {
+    int u = is_trans(trans) ? flip_uplo(uplo) : uplo;
+    return OP_TRI | (u == DDLA_LOWER ? OP_LOWER : 0) | (diag == DDLA_UNIT_DIAG ? OP_UNIT : 0);
+}
+
+// SYMM on device views: A the symmetric na x na operand, opB m x n.
+// DDLA/BLAS/Managed/3m.cs:144-188 (the operands trade places on the right).
+static int symm_dev(ddla_handle h, int side, int uplo, i64 m, i64 n, double alpha, View<const double> A,
+                    View<const double> opB, double beta, View<double> C) {
+    int mode = OP_SYM | (uplo == DDLA_LOWER ? OP_LOWER : 0);
+    if (side == DDLA_LEFT) return gemm_f64_struct(h->stream, m, n, m, alpha, A, mode, opB, OP_DENSE, beta, C);
+    return gemm_f64_struct(h->stream, m, n, n, alpha, opB, OP_DENSE, A, mode, beta, C);
+}
+
+// TRMM3 on device views: A the stored na x na triangle, opB m x n.
+// DDLA/BLAS/Managed/3m.cs:308-356.
+static int trmm3_dev(ddla_handle h, int side, int uplo, int ta, int diag, i64 m, i64 n, double alpha,
+                     View<const double> A, View<const double> opB, double beta, View<double> C) {
+    View<const double> opA = is_trans(ta) ? A.t() : A;
+    int mode = tri_mode(uplo, ta, diag);
+    if (side == DDLA_LEFT) return gemm_f64_struct(h->stream, m, n, m, alpha, opA, mode, opB, OP_DENSE, beta, C);
+    return gemm_f64_struct(h->stream, m, n, n, alpha, opB, OP_DENSE, opA, mode, beta, C);
+}
+
+// SYR2K as two triangle-only GEMMs, DDLA/BLAS/Managed/3m.cs:227-246.
+static int syr2k_dev(ddla_handle h, int uplo, i64 m, i64 k, double alpha, View<const double> opA,
+                     View<const double> opB, double beta, View<double> C) {
+    DDLA_TRY(gemm_f64(h->stream, m, m, k, alpha, opA, opB.t(), beta, C, uplo));
+    return gemm_f64(h->stream, m, m, k, alpha, opB, opA.t(), 1.0, C, uplo);
+}
+
 #define GET_HANDLE(h)                  \
     ddla_handle h;                     \
     do {                               \
@@ -379,6 +419,73 @@ int ddla_dev_dtrsm(ddla_handle h, int32_t side, int32_t uplo, int32_t ta, int32_
                         View<double>{b, m, n, rsb, csb});
 }
 
+int ddla_dev_dsymm(ddla_handle h, int32_t side, int32_t uplo, int32_t conja, int32_t tb, ddla_dim_t m, ddla_dim_t n,
+                   double alpha, const double *a, ddla_inc_t rsa, ddla_inc_t csa, const double *b, ddla_inc_t rsb,
+                   ddla_inc_t csb, double beta, double *c, ddla_inc_t rsc, ddla_inc_t csc) {
+    CHECK_ARG(h != nullptr, 1);
+    CHECK_ARG(side == DDLA_LEFT || side == DDLA_RIGHT, 2);
+    CHECK_ARG(valid_tri(uplo), 3);
+    CHECK_ARG(valid_conj(conja), 4);
+    CHECK_ARG(valid_trans(tb), 5);
+    CHECK_ARG(m >= 0, 6);
+    CHECK_ARG(n >= 0, 7);
+    if (m == 0 || n == 0) return 0;
+    i64 na = side == DDLA_LEFT ? m : n;
+    return symm_dev(h, side, uplo, m, n, alpha, View<const double>{a, na, na, rsa, csa},
+                    op_view(b, m, n, rsb, csb, tb), beta, View<double>{c, m, n, rsc, csc});
+}
+
+int ddla_dev_dsyr2k(ddla_handle h, int32_t uplo, int32_t ta, int32_t tb, ddla_dim_t m, ddla_dim_t k, double alpha,
+                    const double *a, ddla_inc_t rsa, ddla_inc_t csa, const double *b, ddla_inc_t rsb,
+                    ddla_inc_t csb, double beta, double *c, ddla_inc_t rsc, ddla_inc_t csc) {
+    CHECK_ARG(h != nullptr, 1);
+    CHECK_ARG(valid_tri(uplo), 2);
+    CHECK_ARG(valid_trans(ta), 3);
+    CHECK_ARG(valid_trans(tb), 4);
+    CHECK_ARG(m >= 0, 5);
+    CHECK_ARG(k >= 0, 6);
+    if (m == 0) return 0;
+    return syr2k_dev(h, uplo, m, k, alpha, op_view(a, m, k, rsa, csa, ta), op_view(b, m, k, rsb, csb, tb), beta,
+                     View<double>{c, m, m, rsc, csc});
+}
+
+int ddla_dev_dtrmm(ddla_handle h, int32_t side, int32_t uplo, int32_t ta, int32_t diag, ddla_dim_t m, ddla_dim_t n,
+                   double alpha, const double *a, ddla_inc_t rsa, ddla_inc_t csa, double *b, ddla_inc_t rsb,
+                   ddla_inc_t csb) {
+    CHECK_ARG(h != nullptr, 1);
+    CHECK_ARG(side == DDLA_LEFT || side == DDLA_RIGHT, 2);
+    CHECK_ARG(valid_tri(uplo), 3);
+    CHECK_ARG(valid_trans(ta), 4);
+    CHECK_ARG(diag == DDLA_UNIT_DIAG || diag == DDLA_NONUNIT_DIAG, 5);
+    CHECK_ARG(m >= 0, 6);
+    CHECK_ARG(n >= 0, 7);
+    if (m == 0 || n == 0) return 0;
+    i64 na = side == DDLA_LEFT ? m : n;
+    void *tmp;
+    DDLA_TRY(workspace(h, WS_TMP, sizeof(double) * (size_t)(m * n), &tmp));
+    View<double> Bc{(double *)tmp, m, n, n, 1};
+    View<double> Bv{b, m, n, rsb, csb};
+    DDLA_TRY(copy2d_on<double>(h->stream, cv(Bv), Bc));
+    return trmm3_dev(h, side, uplo, ta, diag, m, n, alpha, View<const double>{a, na, na, rsa, csa}, cv(Bc), 0.0, Bv);
+}
+
+int ddla_dev_dtrmm3(ddla_handle h, int32_t side, int32_t uplo, int32_t ta, int32_t diag, int32_t tb, ddla_dim_t m,
+                    ddla_dim_t n, double alpha, const double *a, ddla_inc_t rsa, ddla_inc_t csa, const double *b,
+                    ddla_inc_t rsb, ddla_inc_t csb, double beta, double *c, ddla_inc_t rsc, ddla_inc_t csc) {
+    CHECK_ARG(h != nullptr, 1);
+    CHECK_ARG(side == DDLA_LEFT || side == DDLA_RIGHT, 2);
+    CHECK_ARG(valid_tri(uplo), 3);
+    CHECK_ARG(valid_trans(ta), 4);
+    CHECK_ARG(diag == DDLA_UNIT_DIAG || diag == DDLA_NONUNIT_DIAG, 5);
+    CHECK_ARG(valid_trans(tb), 6);
+    CHECK_ARG(m >= 0, 7);
+    CHECK_ARG(n >= 0, 8);
+    if (m == 0 || n == 0) return 0;
+    i64 na = side == DDLA_LEFT ? m : n;
+    return trmm3_dev(h, side, uplo, ta, diag, m, n, alpha, View<const double>{a, na, na, rsa, csa},
+                     op_view(b, m, n, rsb, csb, tb), beta, View<double>{c, m, n, rsc, csc});
+}
+
 // ------------------------------------------------------------------ level 3, host
 int ddla_dgemm(int32_t ta, int32_t tb, ddla_dim_t m, ddla_dim_t n, ddla_dim_t k, const double *alpha,
                const double *a, ddla_inc_t rsa, ddla_inc_t csa, const double *b, ddla_inc_t rsb, ddla_inc_t csb,
@@ -468,6 +575,100 @@ int ddla_dtrsm(int32_t side, int32_t uplo, int32_t ta, int32_t diag, ddla_dim_t 
     DDLA_TRY(stage_in(h, WS_B, b, m, n, rsb, csb, true, &sb));
     DDLA_TRY(trsm<double>(h, side, uplo, ta, diag, m, n, *alpha, cv(sa.view), sb.view));
     return stage_out(h, sb, b, m, n, rsb, csb);
+}
+
+int ddla_dsymm(int32_t side, int32_t uplo, int32_t conja, int32_t tb, ddla_dim_t m, ddla_dim_t n, const double *alpha,
+               const double *a, ddla_inc_t rsa, ddla_inc_t csa, const double *b, ddla_inc_t rsb, ddla_inc_t csb,
+               const double *beta, double *c, ddla_inc_t rsc, ddla_inc_t csc) {
+    CHECK_ARG(side == DDLA_LEFT || side == DDLA_RIGHT, 1);
+    CHECK_ARG(valid_tri(uplo), 2);
+    CHECK_ARG(valid_conj(conja), 3);
+    CHECK_ARG(valid_trans(tb), 4);
+    CHECK_ARG(m >= 0, 5);
+    CHECK_ARG(n >= 0, 6);
+    CHECK_ARG(alpha != nullptr, 7);
+    CHECK_ARG(beta != nullptr, 14);
+    if (m == 0 || n == 0) return 0;
+    GET_HANDLE(h);
+    i64 na = side == DDLA_LEFT ? m : n;
+    Staged sa, sb, sc;
+    DDLA_TRY(stage_in(h, WS_A, a, na, na, rsa, csa, true, &sa));
+    DDLA_TRY(stage_in(h, WS_B, b, is_trans(tb) ? n : m, is_trans(tb) ? m : n, rsb, csb, true, &sb));
+    DDLA_TRY(stage_in(h, WS_C, c, m, n, rsc, csc, *beta != 0.0, &sc));
+    View<const double> B = cv(sb.view);
+    if (is_trans(tb)) B = B.t();
+    DDLA_TRY(symm_dev(h, side, uplo, m, n, *alpha, cv(sa.view), B, *beta, sc.view));
+    return stage_out(h, sc, c, m, n, rsc, csc);
+}
+
+int ddla_dsyr2k(int32_t uplo, int32_t ta, int32_t tb, ddla_dim_t m, ddla_dim_t k, const double *alpha,
+                const double *a, ddla_inc_t rsa, ddla_inc_t csa, const double *b, ddla_inc_t rsb, ddla_inc_t csb,
+                const double *beta, double *c, ddla_inc_t rsc, ddla_inc_t csc) {
+    CHECK_ARG(valid_tri(uplo), 1);
+    CHECK_ARG(valid_trans(ta), 2);
+    CHECK_ARG(valid_trans(tb), 3);
+    CHECK_ARG(m >= 0, 4);
+    CHECK_ARG(k >= 0, 5);
+    CHECK_ARG(alpha != nullptr, 6);
+    CHECK_ARG(beta != nullptr, 13);
+    if (m == 0) return 0;
+    GET_HANDLE(h);
+    i64 ar = is_trans(ta) ? k : m, ac = is_trans(ta) ? m : k;
+    i64 br = is_trans(tb) ? k : m, bc = is_trans(tb) ? m : k;
+    Staged sa, sb, sc;
+    DDLA_TRY(stage_in(h, WS_A, a, ar, ac, rsa, csa, k > 0, &sa));
+    DDLA_TRY(stage_in(h, WS_B, b, br, bc, rsb, csb, k > 0, &sb));
+    DDLA_TRY(stage_in(h, WS_C, c, m, m, rsc, csc, *beta != 0.0, &sc));
+    View<const double> A = cv(sa.view), B = cv(sb.view);
+    if (is_trans(ta)) A = A.t();
+    if (is_trans(tb)) B = B.t();
+    DDLA_TRY(syr2k_dev(h, uplo, m, k, *alpha, A, B, *beta, sc.view));
+    return stage_out(h, sc, c, m, m, rsc, csc, uplo);
+}
+
+int ddla_dtrmm(int32_t side, int32_t uplo, int32_t ta, int32_t diag, ddla_dim_t m, ddla_dim_t n, const double *alpha,
+               const double *a, ddla_inc_t rsa, ddla_inc_t csa, double *b, ddla_inc_t rsb, ddla_inc_t csb) {
+    CHECK_ARG(side == DDLA_LEFT || side == DDLA_RIGHT, 1);
+    CHECK_ARG(valid_tri(uplo), 2);
+    CHECK_ARG(valid_trans(ta), 3);
+    CHECK_ARG(diag == DDLA_UNIT_DIAG || diag == DDLA_NONUNIT_DIAG, 4);
+    CHECK_ARG(m >= 0, 5);
+    CHECK_ARG(n >= 0, 6);
+    CHECK_ARG(alpha != nullptr, 7);
+    if (m == 0 || n == 0) return 0;
+    GET_HANDLE(h);
+    i64 na = side == DDLA_LEFT ? m : n;
+    Staged sa, sb, sc;
+    DDLA_TRY(stage_in(h, WS_A, a, na, na, rsa, csa, true, &sa));
+    DDLA_TRY(stage_in(h, WS_B, b, m, n, rsb, csb, true, &sb));
+    DDLA_TRY(stage_in(h, WS_C, b, m, n, rsb, csb, false, &sc));   // product lands here, then back in b
+    DDLA_TRY(trmm3_dev(h, side, uplo, ta, diag, m, n, *alpha, cv(sa.view), cv(sb.view), 0.0, sc.view));
+    return stage_out(h, sc, b, m, n, rsb, csb);
+}
+
+int ddla_dtrmm3(int32_t side, int32_t uplo, int32_t ta, int32_t diag, int32_t tb, ddla_dim_t m, ddla_dim_t n,
+                const double *alpha, const double *a, ddla_inc_t rsa, ddla_inc_t csa, const double *b, ddla_inc_t rsb,
+                ddla_inc_t csb, const double *beta, double *c, ddla_inc_t rsc, ddla_inc_t csc) {
+    CHECK_ARG(side == DDLA_LEFT || side == DDLA_RIGHT, 1);
+    CHECK_ARG(valid_tri(uplo), 2);
+    CHECK_ARG(valid_trans(ta), 3);
+    CHECK_ARG(diag == DDLA_UNIT_DIAG || diag == DDLA_NONUNIT_DIAG, 4);
+    CHECK_ARG(valid_trans(tb), 5);
+    CHECK_ARG(m >= 0, 6);
+    CHECK_ARG(n >= 0, 7);
+    CHECK_ARG(alpha != nullptr, 8);
+    CHECK_ARG(beta != nullptr, 15);
+    if (m == 0 || n == 0) return 0;
+    GET_HANDLE(h);
+    i64 na = side == DDLA_LEFT ? m : n;
+    Staged sa, sb, sc;
+    DDLA_TRY(stage_in(h, WS_A, a, na, na, rsa, csa, true, &sa));
+    DDLA_TRY(stage_in(h, WS_B, b, is_trans(tb) ? n : m, is_trans(tb) ? m : n, rsb, csb, true, &sb));
+    DDLA_TRY(stage_in(h, WS_C, c, m, n, rsc, csc, *beta != 0.0, &sc));
+    View<const double> B = cv(sb.view);
+    if (is_trans(tb)) B = B.t();
+    DDLA_TRY(trmm3_dev(h, side, uplo, ta, diag, m, n, *alpha, cv(sa.view), B, *beta, sc.view));
+    return stage_out(h, sc, c, m, n, rsc, csc);
 }
 
 // ------------------------------------------------------------------ factorizations, device

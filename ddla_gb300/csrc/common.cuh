@@ -146,6 +146,10 @@ int gemm_f64(cudaStream_t s, i64 m, i64 n, i64 k, double alpha, View<const doubl
              double beta, View<double> C, int uplo = DDLA_DENSE, i64 batch = 1, i64 sa = 0, i64 sb = 0, i64 sc = 0);
 int gemm_f32(cudaStream_t s, i64 m, i64 n, i64 k, float alpha, View<const float> A, View<const float> B,
              float beta, View<float> C, int uplo = DDLA_DENSE);
+// Structured FP64 operands of gemm_f64_struct: kind in bits 0-1, then flags.
+enum OpMode : int { OP_DENSE = 0, OP_SYM = 1, OP_TRI = 2, OP_LOWER = 4, OP_UNIT = 8 };
+int gemm_f64_struct(cudaStream_t s, i64 m, i64 n, i64 k, double alpha, View<const double> A, int amode,
+                    View<const double> B, int bmode, double beta, View<double> C, int uplo = DDLA_DENSE);
 
 // Triangular solve, B <- op(A)^-1 alpha B (left) or alpha B op(A)^-1 (right).
 template <typename T>
@@ -185,6 +189,9 @@ template <typename T>
 int tri_inverse(ddla_handle h, bool lower, bool unit, View<const T> A, i64 n, T *inv);
 template <typename T>
 int trsv_apply(ddla_handle h, bool lower, View<const T> A, i64 n, const T *inv, T *X, i64 ldx, int nr);
+// Y = X element by element (any strides; trsm.cu).
+template <typename T>
+int copy2d_on(cudaStream_t s, View<const T> X, View<T> Y);
 // Rows of B reordered by a permutation (forward: row k <- row perm[k]).
 template <typename T>
 int permute_rows(ddla_handle h, View<T> B, const int *perm, i64 n, bool forward);

@@ -15,6 +15,13 @@
 // and optionally only the lower or upper triangle of C (GEMMT / SYRK), skipping
 // tiles that do not intersect it (DDLA's GEMMTMacroKernel computes and masks
 // them, DDLA/BLAS/Managed/3m/MacroKernel.cs:158-216).
+//
+// The FP64 kernel also reads structured operands (SYMM, TRMM, TRMM3): a
+// symmetric operand stored in one triangle is mirrored on load, a triangular
+// one reads zeros outside its triangle (ones on a unit diagonal) and its CTA's
+// k loop is cut to the k range the triangle covers.  This is what DDLA's
+// structured packing does (SYPack / TRPack, DDLA/BLAS/Managed/3m/Packing.cs:
+// 105-374) before its ordinary macro kernel, without the packed copy.
 #include "common.cuh"
 
 namespace ddla {
@@ -24,11 +31,30 @@ namespace {
 
 constexpr int BK64 = 16;
 
-template <int BM, int BN, int WM, int WN>
+// Element (i, j) of a structured operand (mode: OP_* bits, see gemm_f64_struct).
+template <bool STRUCT>
+__device__ __forceinline__ double ld_op(const double *__restrict__ P, i64 rs, i64 cs, i64 i, i64 j, int mode) {
+    if (STRUCT) {
+        const bool outside = (mode & OP_LOWER) ? (j > i) : (j < i);
+        if ((mode & 3) == OP_SYM) {
+            if (outside) {
+                i64 t = i;
+                i = j;
+                j = t;
+            }
+        } else if ((mode & 3) == OP_TRI) {
+            if (outside) return 0.0;
+            if (i == j && (mode & OP_UNIT)) return 1.0;
+        }
+    }
+    return P[i * rs + j * cs];
+}
+
+template <int BM, int BN, int WM, int WN, bool STRUCT>
 __global__ void __launch_bounds__(WM *WN * 32)
     k_gemm_f64(i64 m, i64 n, i64 k, double alpha, const double *__restrict__ A, i64 rsa, i64 csa,
                const double *__restrict__ B, i64 rsb, i64 csb, double beta, double *C, i64 rsc, i64 csc,
-               int uplo, i64 sa, i64 sb, i64 sc, const i64 *__restrict__ boff) {
+               int uplo, i64 sa, i64 sb, i64 sc, const i64 *__restrict__ boff, int amode, int bmode) {
     constexpr int NT = WM * WN * 32;
     constexpr int TWM = BM / WM, TWN = BN / WN;  // warp tile
     constexpr int FM = TWM / 8, FN = TWN / 8;   // 8x8 fragments per warp
@@ -60,20 +86,34 @@ __global__ void __launch_bounds__(WM *WN * 32)
 
     const bool a_kfast = (csa == 1);  // K contiguous in A
     const bool b_nfast = (csb == 1);  // N contiguous in B
-    for (i64 k0 = 0; k0 < k; k0 += BK64) {
+    // k range of this tile: a triangular A (k == m) is zero right of its
+    // diagonal when lower (left of it when upper); a triangular B (k == n) is
+    // zero above its diagonal when lower (below it when upper).
+    i64 kb = 0, ke = k;
+    if (STRUCT) {
+        if ((amode & 3) == OP_TRI) {
+            if (amode & OP_LOWER) ke = min(ke, m0 + BM);
+            else kb = m0;
+        }
+        if ((bmode & 3) == OP_TRI) {
+            if (bmode & OP_LOWER) kb = max(kb, n0);
+            else ke = min(ke, n0 + BN);
+        }
+    }
+    for (i64 k0 = kb; k0 < ke; k0 += BK64) {
         // A tile BM x BK
         for (int e = tid; e < BM * BK64; e += NT) {
             int r, kk;
             if (a_kfast) { kk = e % BK64; r = e / BK64; } else { r = e % BM; kk = e / BM; }
             i64 gr = m0 + r, gk = k0 + kk;
-            As[kk][r] = (gr < m && gk < k) ? A[gr * rsa + gk * csa] : 0.0;
+            As[kk][r] = (gr < m && gk < k) ? ld_op<STRUCT>(A, rsa, csa, gr, gk, amode) : 0.0;
         }
         // B tile BK x BN
         for (int e = tid; e < BN * BK64; e += NT) {
             int c, kk;
             if (b_nfast) { c = e % BN; kk = e / BN; } else { kk = e % BK64; c = e / BK64; }
             i64 gc = n0 + c, gk = k0 + kk;
-            Bs[kk][c] = (gc < n && gk < k) ? B[gk * rsb + gc * csb] : 0.0;
+            Bs[kk][c] = (gc < n && gk < k) ? ld_op<STRUCT>(B, rsb, csb, gk, gc, bmode) : 0.0;
         }
         __syncthreads();
 #pragma unroll
@@ -114,15 +154,22 @@ __global__ void __launch_bounds__(WM *WN * 32)
 
 template <int BM, int BN, int WM, int WN>
 int launch_f64(cudaStream_t s, i64 m, i64 n, i64 k, double alpha, View<const double> A, View<const double> B,
-               double beta, View<double> C, int uplo, i64 batch, i64 sa, i64 sb, i64 sc, const i64 *boff) {
+               double beta, View<double> C, int uplo, i64 batch, i64 sa, i64 sb, i64 sc, const i64 *boff,
+               int amode, int bmode) {
     i64 gx = (n + BN - 1) / BN, gy = (m + BM - 1) / BM;
     if (gy > 65535) { set_error("gemm_f64: m too large for one launch"); return DDLA_ERR_UNSUPPORTED; }
     for (i64 b0 = 0; b0 < batch; b0 += 65535) {
         i64 nb = batch - b0 < 65535 ? batch - b0 : 65535;
         dim3 grid((unsigned)gx, (unsigned)gy, (unsigned)nb);
-        k_gemm_f64<BM, BN, WM, WN><<<grid, WM * WN * 32, 0, s>>>(
-            m, n, k, alpha, A.p + (boff ? 0 : b0 * sa), A.rs, A.cs, B.p + (boff ? 0 : b0 * sb), B.rs, B.cs, beta,
-            C.p + (boff ? 0 : b0 * sc), C.rs, C.cs, uplo, sa, sb, sc, boff ? boff + 3 * b0 : nullptr);
+        if (amode | bmode)
+            k_gemm_f64<BM, BN, WM, WN, true><<<grid, WM * WN * 32, 0, s>>>(
+                m, n, k, alpha, A.p + (boff ? 0 : b0 * sa), A.rs, A.cs, B.p + (boff ? 0 : b0 * sb), B.rs, B.cs,
+                beta, C.p + (boff ? 0 : b0 * sc), C.rs, C.cs, uplo, sa, sb, sc, boff ? boff + 3 * b0 : nullptr,
+                amode, bmode);
+        else
+            k_gemm_f64<BM, BN, WM, WN, false><<<grid, WM * WN * 32, 0, s>>>(
+                m, n, k, alpha, A.p + (boff ? 0 : b0 * sa), A.rs, A.cs, B.p + (boff ? 0 : b0 * sb), B.rs, B.cs,
+                beta, C.p + (boff ? 0 : b0 * sc), C.rs, C.cs, uplo, sa, sb, sc, boff ? boff + 3 * b0 : nullptr, 0, 0);
         DDLA_LAUNCHED();
     }
     return 0;
@@ -150,29 +197,42 @@ double balance(i64 tiles, int sms) {
 
 static int gemm_f64_any(cudaStream_t s, i64 m, i64 n, i64 k, double alpha, View<const double> A,
                         View<const double> B, double beta, View<double> C, int uplo, i64 batch, i64 sa, i64 sb, i64 sc,
-                        const i64 *boff) {
+                        const i64 *boff, int amode = 0, int bmode = 0) {
     if (m <= 0 || n <= 0 || batch <= 0) return 0;
     if (k <= 0 || alpha == 0.0) {
         // C = beta*C on the requested part: reuse the kernel with k = 0.
         k = 0;
     }
     if (n <= 16)
-        return launch_f64<128, 16, 4, 1>(s, m, n, k, alpha, A, B, beta, C, uplo, batch, sa, sb, sc, boff);
+        return launch_f64<128, 16, 4, 1>(s, m, n, k, alpha, A, B, beta, C, uplo, batch, sa, sb, sc, boff, amode, bmode);
     int sms = sm_count();
     i64 t64 = ((m + 63) / 64) * ((n + 63) / 64) * batch;
     i64 t32 = ((m + 31) / 32) * ((n + 63) / 64) * batch;
     i64 t3232 = ((m + 31) / 32) * ((n + 31) / 32) * batch;
     double b64 = balance(t64, sms), b32 = balance(t32, sms), b3232 = balance(t3232, sms);
     if (t64 >= 8 * sms || (b64 >= 0.9 && b64 >= b32 - 0.02))
-        return launch_f64<64, 64, 2, 2>(s, m, n, k, alpha, A, B, beta, C, uplo, batch, sa, sb, sc, boff);
+        return launch_f64<64, 64, 2, 2>(s, m, n, k, alpha, A, B, beta, C, uplo, batch, sa, sb, sc, boff, amode, bmode);
     if (b32 >= 0.9 || b32 >= b3232 - 0.02)
-        return launch_f64<32, 64, 2, 2>(s, m, n, k, alpha, A, B, beta, C, uplo, batch, sa, sb, sc, boff);
-    return launch_f64<32, 32, 2, 2>(s, m, n, k, alpha, A, B, beta, C, uplo, batch, sa, sb, sc, boff);
+        return launch_f64<32, 64, 2, 2>(s, m, n, k, alpha, A, B, beta, C, uplo, batch, sa, sb, sc, boff, amode, bmode);
+    return launch_f64<32, 32, 2, 2>(s, m, n, k, alpha, A, B, beta, C, uplo, batch, sa, sb, sc, boff, amode, bmode);
 }
 
 int gemm_f64(cudaStream_t s, i64 m, i64 n, i64 k, double alpha, View<const double> A, View<const double> B,
              double beta, View<double> C, int uplo, i64 batch, i64 sa, i64 sb, i64 sc) {
     return gemm_f64_any(s, m, n, k, alpha, A, B, beta, C, uplo, batch, sa, sb, sc, nullptr);
+}
+
+// C = alpha*A*B + beta*C where A and / or B is structured (amode / bmode: OP_SYM
+// or OP_TRI, plus OP_LOWER for the stored / nonzero triangle and OP_UNIT for an
+// implicit unit diagonal that is never read).  A triangular A needs k == m, a
+// triangular B needs k == n.
+int gemm_f64_struct(cudaStream_t s, i64 m, i64 n, i64 k, double alpha, View<const double> A, int amode,
+                    View<const double> B, int bmode, double beta, View<double> C, int uplo) {
+    if (((amode & 3) == OP_TRI && k != m) || ((bmode & 3) == OP_TRI && k != n)) {
+        set_error("gemm_f64_struct: triangular operand must be square");
+        return DDLA_ERR_UNSUPPORTED;
+    }
+    return gemm_f64_any(s, m, n, k, alpha, A, B, beta, C, uplo, 1, 0, 0, 0, nullptr, amode, bmode);
 }
 
 // Batched GEMM whose problem z starts at element offsets d_offsets[3z..3z+2]

@@ -56,6 +56,27 @@ class Handle:
         check(lib().ddla_dev_dtrsm(self.h, side, uplo, ta, diag, m, n, alpha, _p(A), *_st(A), _p(B), *_st(B)),
               "dev_dtrsm")
 
+    def symm(self, side, uplo, alpha, A, B, beta, Cm, tb=0):
+        m, n = Cm.shape
+        check(lib().ddla_dev_dsymm(self.h, side, uplo, 0, tb, m, n, alpha, _p(A), *_st(A), _p(B), *_st(B), beta,
+                                   _p(Cm), *_st(Cm)), "dev_dsymm")
+
+    def syr2k(self, uplo, alpha, A, B, beta, Cm, ta=0, tb=0):
+        m = Cm.shape[0]
+        k = A.shape[0] if ta else A.shape[1]
+        check(lib().ddla_dev_dsyr2k(self.h, uplo, ta, tb, m, k, alpha, _p(A), *_st(A), _p(B), *_st(B), beta,
+                                    _p(Cm), *_st(Cm)), "dev_dsyr2k")
+
+    def trmm(self, side, uplo, ta, diag, alpha, A, B):
+        m, n = B.shape
+        check(lib().ddla_dev_dtrmm(self.h, side, uplo, ta, diag, m, n, alpha, _p(A), *_st(A), _p(B), *_st(B)),
+              "dev_dtrmm")
+
+    def trmm3(self, side, uplo, ta, diag, alpha, A, B, beta, Cm, tb=0):
+        m, n = Cm.shape
+        check(lib().ddla_dev_dtrmm3(self.h, side, uplo, ta, diag, tb, m, n, alpha, _p(A), *_st(A), _p(B), *_st(B),
+                                    beta, _p(Cm), *_st(Cm)), "dev_dtrmm3")
+
     def getrf(self, A, piv, nb=0, precision=0):
         o = Opts()
         o.nb, o.precision = nb, precision

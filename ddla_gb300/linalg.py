@@ -111,6 +111,88 @@ class BlasProvider:
                                C.byref(C.c_double(beta)), _p(Cm), *_st(Cm)), "SyRk")
 
     @staticmethod
+    def SyMM(*args):
+        """SyMM(aSide, aUplo, bTrans, alpha, A, B, beta, C) or
+        SyMM(aSide, aUplo, alpha, A, B, beta, C): C = beta C + alpha A op(B)
+        (Left) or alpha op(B) A (Right), A symmetric in aUplo (DDLA/BLAS/3m.cs:83-116)."""
+        if len(args) == 7:
+            args = (args[0], args[1], NO_TRANSPOSE) + tuple(args[2:])
+        side, uplo, tb, alpha, A, B, beta, Cm = args
+        A, B, Cm = _view(A, "A"), _view(B, "B"), _view(Cm, "C")
+        m, n = Cm.shape
+        if m == 0 or n == 0:
+            return
+        if _dims_after(B, tb) != (m, n):
+            raise ValueError("Dimensions of matrix B must be match!")
+        if A.shape[0] != A.shape[1] or A.shape[0] != (m if side == LEFT else n):
+            raise ValueError("Dimensions of matrixs must be match!")
+        check(lib().ddla_dsymm(side, uplo, 0, tb, m, n, C.byref(C.c_double(alpha)), _p(A), *_st(A), _p(B),
+                               *_st(B), C.byref(C.c_double(beta)), _p(Cm), *_st(Cm)), "SyMM")
+
+    @staticmethod
+    def SyR2k(*args):
+        """SyR2k(cUplo, aTrans, bTrans, alpha, A, B, beta, C) or
+        SyR2k(cUplo, alpha, A, B, beta, C): triangle of C = beta C +
+        alpha (op(A) op(B)^T + op(B) op(A)^T) (DDLA/BLAS/3m.cs:149-183)."""
+        if len(args) == 6:
+            args = (args[0], NO_TRANSPOSE, NO_TRANSPOSE) + tuple(args[1:])
+        uplo, ta, tb, alpha, A, B, beta, Cm = args
+        A, B, Cm = _view(A, "A"), _view(B, "B"), _view(Cm, "C")
+        m = Cm.shape[0]
+        if Cm.shape[1] != m:
+            raise ValueError("C must be square")
+        if m == 0:
+            return
+        ma, k = _dims_after(A, ta)
+        if k == 0:
+            return
+        if _dims_after(B, tb) != (m, k) or ma != m:
+            raise ValueError("Dimensions of matrixs A and B must be match!")
+        check(lib().ddla_dsyr2k(uplo, ta, tb, m, k, C.byref(C.c_double(alpha)), _p(A), *_st(A), _p(B), *_st(B),
+                                C.byref(C.c_double(beta)), _p(Cm), *_st(Cm)), "SyR2k")
+
+    @staticmethod
+    def TrMM(*args):
+        """TrMM(aSide, aUplo, aTrans, aDiag, alpha, A, B), TrMM(aSide, aUplo, aDiag,
+        alpha, A, B) or TrMM(aSide, aUplo, alpha, A, B): B <- alpha op(A) B (Left)
+        or alpha B op(A) (Right), A triangular (DDLA/BLAS/3m.cs:185-223)."""
+        if len(args) == 5:
+            args = (args[0], args[1], NO_TRANSPOSE, NONUNIT) + tuple(args[2:])
+        elif len(args) == 6:
+            args = (args[0], args[1], NO_TRANSPOSE) + tuple(args[2:])
+        side, uplo, ta, diag, alpha, A, B = args
+        A, B = _view(A, "A"), _view(B, "B")
+        m, n = B.shape
+        if m == 0 or n == 0:
+            return
+        if A.shape[0] != A.shape[1] or A.shape[0] != (m if side == LEFT else n):
+            raise ValueError("Dimensions of matrixs A must be match!")
+        check(lib().ddla_dtrmm(side, uplo, ta, diag, m, n, C.byref(C.c_double(alpha)), _p(A), *_st(A), _p(B),
+                               *_st(B)), "TrMM")
+
+    @staticmethod
+    def TrMM3(*args):
+        """TrMM3(aSide, aUplo, aTrans, aDiag, bTrans, alpha, A, B, beta, C),
+        TrMM3(aSide, aUplo, aDiag, alpha, A, B, beta, C) or
+        TrMM3(aSide, aUplo, alpha, A, B, beta, C): C = beta C + alpha op(A) op(B)
+        (Left) or alpha op(B) op(A) (Right) (DDLA/BLAS/3m.cs:225-274)."""
+        if len(args) == 7:
+            args = (args[0], args[1], NO_TRANSPOSE, NONUNIT, NO_TRANSPOSE) + tuple(args[2:])
+        elif len(args) == 8:
+            args = (args[0], args[1], NO_TRANSPOSE, args[2], NO_TRANSPOSE) + tuple(args[3:])
+        side, uplo, ta, diag, tb, alpha, A, B, beta, Cm = args
+        A, B, Cm = _view(A, "A"), _view(B, "B"), _view(Cm, "C")
+        m, n = Cm.shape
+        if m == 0 or n == 0:
+            return
+        if _dims_after(B, tb) != (m, n):
+            raise ValueError("Dimensions of matrix B must be match!")
+        if A.shape[0] != A.shape[1] or A.shape[0] != (m if side == LEFT else n):
+            raise ValueError("Dimensions of matrixs A must be match!")
+        check(lib().ddla_dtrmm3(side, uplo, ta, diag, tb, m, n, C.byref(C.c_double(alpha)), _p(A), *_st(A), _p(B),
+                                *_st(B), C.byref(C.c_double(beta)), _p(Cm), *_st(Cm)), "TrMM3")
+
+    @staticmethod
     def TrSM(*args):
         """TrSM(aSide, aUplo, aTrans, aDiag, alpha, A, B) or TrSM(aSide, aUplo, alpha, A, B):
         B <- op(A)^-1 alpha B (Left) or alpha B op(A)^-1 (Right) (DDLA/BLAS/3m.cs:276-314)."""

@@ -161,6 +161,39 @@ int ddla_dsyrk(int32_t uploc, int32_t transa, ddla_dim_t m, ddla_dim_t k,
                const double *alpha, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
                const double *beta, double *c, ddla_inc_t rsc, ddla_inc_t csc);
 
+/* C = beta*C + alpha*A*op(B) (left) or beta*C + alpha*op(B)*A (right), A
+ * symmetric (m x m left, n x n right) and read only in its uploa triangle;
+ * conja is accepted and ignored (real data).  Replaces bli_dsymm,
+ * DDLA/BLAS/Native/3m.cs:81-94 (wrapper DDLA/BLAS/3m.cs:83-106). */
+int ddla_dsymm(int32_t sidea, int32_t uploa, int32_t conja, int32_t transb, ddla_dim_t m, ddla_dim_t n,
+               const double *alpha, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
+               const double *b, ddla_inc_t rsb, ddla_inc_t csb,
+               const double *beta, double *c, ddla_inc_t rsc, ddla_inc_t csc);
+
+/* Triangle of C (uploc, m x m) = beta*C + alpha*op(A)*op(B)^T +
+ * alpha*op(B)*op(A)^T, op(A) and op(B) m x k.  Replaces bli_dsyr2k,
+ * DDLA/BLAS/Native/3m.cs:108-120 (wrapper DDLA/BLAS/3m.cs:149-172). */
+int ddla_dsyr2k(int32_t uploc, int32_t transa, int32_t transb, ddla_dim_t m, ddla_dim_t k,
+                const double *alpha, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
+                const double *b, ddla_inc_t rsb, ddla_inc_t csb,
+                const double *beta, double *c, ddla_inc_t rsc, ddla_inc_t csc);
+
+/* B = alpha*op(A)*B (left) or alpha*B*op(A) (right) in place, A triangular
+ * (uploa, diaga; the other triangle and a unit diagonal are never read).
+ * Replaces bli_dtrmm, DDLA/BLAS/Native/3m.cs:122-133 (wrapper
+ * DDLA/BLAS/3m.cs:185-204). */
+int ddla_dtrmm(int32_t sidea, int32_t uploa, int32_t transa, int32_t diaga, ddla_dim_t m, ddla_dim_t n,
+               const double *alpha, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
+               double *b, ddla_inc_t rsb, ddla_inc_t csb);
+
+/* C = beta*C + alpha*op(A)*op(B) (left) or beta*C + alpha*op(B)*op(A)
+ * (right), A triangular, C m x n.  Replaces bli_dtrmm3,
+ * DDLA/BLAS/Native/3m.cs:135-149 (wrapper DDLA/BLAS/3m.cs:225-250). */
+int ddla_dtrmm3(int32_t sidea, int32_t uploa, int32_t transa, int32_t diaga, int32_t transb, ddla_dim_t m,
+                ddla_dim_t n, const double *alpha, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
+                const double *b, ddla_inc_t rsb, ddla_inc_t csb,
+                const double *beta, double *c, ddla_inc_t rsc, ddla_inc_t csc);
+
 /* Left: solve op(A) X = alpha B; Right: X op(A) = alpha B; B <- X.  Replaces
  * bli_dtrsm, DDLA/BLAS/Native/3m.cs:151-162 (wrapper DDLA/BLAS/3m.cs:287-305). */
 int ddla_dtrsm(int32_t side, int32_t uploa, int32_t transa, int32_t diaga, ddla_dim_t m, ddla_dim_t n,
@@ -229,6 +262,23 @@ int ddla_dev_dgemmt(ddla_handle h, int32_t uploc, int32_t transa, int32_t transb
 int ddla_dev_dtrsm(ddla_handle h, int32_t side, int32_t uploa, int32_t transa, int32_t diaga, ddla_dim_t m,
                    ddla_dim_t n, double alpha, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
                    double *b, ddla_inc_t rsb, ddla_inc_t csb);
+int ddla_dev_dsymm(ddla_handle h, int32_t sidea, int32_t uploa, int32_t conja, int32_t transb, ddla_dim_t m,
+                   ddla_dim_t n, double alpha, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
+                   const double *b, ddla_inc_t rsb, ddla_inc_t csb,
+                   double beta, double *c, ddla_inc_t rsc, ddla_inc_t csc);
+int ddla_dev_dsyr2k(ddla_handle h, int32_t uploc, int32_t transa, int32_t transb, ddla_dim_t m, ddla_dim_t k,
+                    double alpha, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
+                    const double *b, ddla_inc_t rsb, ddla_inc_t csb,
+                    double beta, double *c, ddla_inc_t rsc, ddla_inc_t csc);
+/* In place: the product is formed from a copy of B kept in the handle's
+ * scratch (m*n doubles). */
+int ddla_dev_dtrmm(ddla_handle h, int32_t sidea, int32_t uploa, int32_t transa, int32_t diaga, ddla_dim_t m,
+                   ddla_dim_t n, double alpha, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
+                   double *b, ddla_inc_t rsb, ddla_inc_t csb);
+int ddla_dev_dtrmm3(ddla_handle h, int32_t sidea, int32_t uploa, int32_t transa, int32_t diaga, int32_t transb,
+                    ddla_dim_t m, ddla_dim_t n, double alpha, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
+                    const double *b, ddla_inc_t rsb, ddla_inc_t csb,
+                    double beta, double *c, ddla_inc_t rsc, ddla_inc_t csc);
 int ddla_dev_dgetrf(ddla_handle h, ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t csa, int32_t *piv,
                     const ddla_opts *opts);
 int ddla_dev_dgetrs(ddla_handle h, int32_t trans, ddla_dim_t n, ddla_dim_t nrhs, const double *lu, ddla_inc_t rsa,

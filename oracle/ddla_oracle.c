@@ -280,6 +280,140 @@ void orc_dsyrk(int uplo, int ta, i64 m, i64 k, double alpha, const double *a, i6
 }
 
 /* ------------------------------------------------------------------------ */
+/* SYMM / SYR2K / TRMM / TRMM3                                               */
+/* ------------------------------------------------------------------------ */
+
+/* A structured operand as DDLA's packing sees it: kind 0 dense, 1 symmetric
+ * (stored in `uplo`), 2 triangular (`uplo` nonzero triangle, `unit` implicit
+ * unit diagonal). */
+enum { SK_DENSE = 0, SK_SYM = 1, SK_TRI = 2 };
+typedef struct { mat M; int kind, uplo, unit; } smat;
+
+static smat sm(mat M, int kind, int uplo, int unit) { smat S = {M, kind, uplo, unit}; return S; }
+static smat str_s(smat S) { S.M = tr(S.M); S.uplo = flip_uplo(S.uplo); return S; }
+
+/* Element (i, j): SYPack mirrors the unstored triangle, TRPack reads zeros
+ * outside the triangle and 1 on a unit diagonal
+ * (DDLA/BLAS/Managed/3m/Packing.cs:172-197 and 282-340). */
+static double sget(smat S, i64 i, i64 j) {
+    int outside = S.uplo == UL_LOWER ? (j > i) : (j < i);
+    if (S.kind == SK_SYM && outside) return *AT(S.M, j, i);
+    if (S.kind == SK_TRI) {
+        if (outside) return 0.0;
+        if (i == j && S.unit) return 1.0;
+    }
+    return *AT(S.M, i, j);
+}
+
+/* pack(sub(S, i0, ni, j0, nj), buf, blk) for a structured operand. */
+static void spack(smat S, i64 i0, i64 ni, i64 j0, i64 nj, double *buf, int blk) {
+    i64 np = align_up(ni, blk) / blk;
+    for (i64 pi = 0; pi < np; pi++) {
+        double *dst = buf + pi * nj * blk;
+        i64 r0 = pi * blk, ar = ni - r0 < blk ? ni - r0 : blk;
+        for (i64 col = 0; col < nj; col++)
+            for (int r = 0; r < blk; r++) *dst++ = r < ar ? sget(S, i0 + r0 + r, j0 + col) : 0.0;
+    }
+}
+
+/* SyMMInner / TrMM3Inner, DDLA/BLAS/Managed/3m/SyMM.cs:13-71 and
+ * TrMM3.cs:13-76: the GeMM loops with structured packing.  C is already
+ * beta-scaled. */
+static void gemm_core_s(double alpha, smat A, smat B, mat C) {
+    i64 m = C.r, n = C.c, k = A.M.c;
+    if (C.cs < C.rs) {
+        smat T = A; A = str_s(B); B = str_s(T); C = tr(C);
+        m = C.r; n = C.c;
+    }
+    if (m == 0 || n == 0 || k == 0) return;
+    i64 mce = MC < align_up(m, MR) ? MC : align_up(m, MR);
+    i64 nce = NC < align_up(n, NR) ? NC : align_up(n, NR);
+    double *bufA = (double *)malloc(sizeof(double) * mce * KC);
+    double *bufB = (double *)malloc(sizeof(double) * KC * nce);
+    smat Bt = str_s(B);
+    for (i64 ic = 0; ic < m; ic += MC) {
+        i64 mc = m - ic < MC ? m - ic : MC;
+        for (i64 pc = 0; pc < k; pc += KC) {
+            i64 kc = k - pc < KC ? k - pc : KC;
+            spack(A, ic, mc, pc, kc, bufA, MR);
+            for (i64 jc = 0; jc < n; jc += NC) {
+                i64 nc = n - jc < NC ? n - jc : NC;
+                spack(Bt, jc, nc, pc, kc, bufB, NR);
+                macro(mc, nc, kc, alpha, bufA, bufB, sub(C, ic, mc, jc, nc), 0, 0);
+            }
+        }
+    }
+    free(bufA); free(bufB);
+}
+
+static mat opm(const double *p, i64 r, i64 c, i64 rs, i64 cs, int t) {
+    return t == TR_T ? tr(mk((double *)p, c, r, rs, cs)) : mk((double *)p, r, c, rs, cs);
+}
+
+/* bli_dsymm semantics (DDLA/BLAS/3m.cs:83-106; managed DDLA/BLAS/Managed/3m.cs:
+ * 144-188): C = beta*C + alpha*A*op(B) (left) / alpha*op(B)*A (right), A
+ * symmetric in its `uplo` triangle. */
+void orc_dsymm(int side, int uplo, int conja, int tb, i64 m, i64 n, double alpha,
+               const double *a, i64 rsa, i64 csa, const double *b, i64 rsb, i64 csb,
+               double beta, double *c, i64 rsc, i64 csc) {
+    (void)conja;
+    i64 na = side == SD_LEFT ? m : n;
+    smat A = sm(mk((double *)a, na, na, rsa, csa), SK_SYM, uplo, 0);
+    smat B = sm(opm(b, m, n, rsb, csb, tb), SK_DENSE, UL_DENSE, 0);
+    mat C = mk(c, m, n, rsc, csc);
+    if (m == 0 || n == 0) return;
+    scal_m(UL_DENSE, beta, C);
+    if (side == SD_LEFT) gemm_core_s(alpha, A, B, C);
+    else gemm_core_s(alpha, B, A, C);
+}
+
+/* bli_dsyr2k semantics (DDLA/BLAS/3m.cs:149-172): two triangle-only GEMMs as
+ * DDLA/BLAS/Managed/3m.cs:227-246 does. */
+void orc_dsyr2k(int uplo, int ta, int tb, i64 m, i64 k, double alpha,
+                const double *a, i64 rsa, i64 csa, const double *b, i64 rsb, i64 csb,
+                double beta, double *c, i64 rsc, i64 csc) {
+    mat A = opm(a, m, k, rsa, csa, ta), B = opm(b, m, k, rsb, csb, tb);
+    mat C = mk(c, m, m, rsc, csc);
+    if (m == 0) return;
+    scal_m(uplo, beta, C);
+    if (k == 0) return;
+    gemm_core(alpha, A, tr(B), C, uplo);
+    gemm_core(alpha, B, tr(A), C, uplo);
+}
+
+/* bli_dtrmm3 semantics (DDLA/BLAS/3m.cs:225-250; managed
+ * DDLA/BLAS/Managed/3m.cs:308-356): C = beta*C + alpha*op(A)*op(B) (left) or
+ * alpha*op(B)*op(A) (right), A triangular. */
+void orc_dtrmm3(int side, int uplo, int ta, int diag, int tb, i64 m, i64 n, double alpha,
+                const double *a, i64 rsa, i64 csa, const double *b, i64 rsb, i64 csb,
+                double beta, double *c, i64 rsc, i64 csc) {
+    i64 na = side == SD_LEFT ? m : n;
+    smat A = sm(mk((double *)a, na, na, rsa, csa), SK_TRI, uplo, diag == DG_UNIT);
+    if (ta == TR_T) A = str_s(A);
+    smat B = sm(opm(b, m, n, rsb, csb, tb), SK_DENSE, UL_DENSE, 0);
+    mat C = mk(c, m, n, rsc, csc);
+    if (m == 0 || n == 0) return;
+    scal_m(UL_DENSE, beta, C);
+    if (side == SD_LEFT) gemm_core_s(alpha, A, B, C);
+    else gemm_core_s(alpha, B, A, C);
+}
+
+/* bli_dtrmm semantics (DDLA/BLAS/3m.cs:185-204): B = alpha*op(A)*B (left) or
+ * alpha*B*op(A) (right) in place.  DDLA's managed TrMM
+ * (DDLA/BLAS/Managed/3m/TrMM.cs:14-207) walks KC blocks with a TrMV per
+ * column of the diagonal block; this restatement forms the same product with
+ * the structured GEMM of TRMM3 from a copy of B, so the two agree to rounding. */
+void orc_dtrmm(int side, int uplo, int ta, int diag, i64 m, i64 n, double alpha,
+               const double *a, i64 rsa, i64 csa, double *b, i64 rsb, i64 csb) {
+    if (m == 0 || n == 0) return;
+    double *t = (double *)malloc(sizeof(double) * m * n);
+    for (i64 i = 0; i < m; i++)
+        for (i64 j = 0; j < n; j++) t[i * n + j] = b[i * rsb + j * csb];
+    orc_dtrmm3(side, uplo, ta, diag, TR_NO, m, n, alpha, a, rsa, csa, t, n, 1, 0.0, b, rsb, csb);
+    free(t);
+}
+
+/* ------------------------------------------------------------------------ */
 /* TRSM / TRSV                                                              */
 /* ------------------------------------------------------------------------ */
 

@@ -66,6 +66,14 @@ def lib():
         L.orc_dtrsm.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, _i64, _i64, C.c_double,
                                 _dp, _i64, _i64, _dp, _i64, _i64]
         L.orc_dtrsm.restype = None
+        L.orc_dsymm.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, _i64, _i64, C.c_double, _dp, _i64, _i64,
+                                _dp, _i64, _i64, C.c_double, _dp, _i64, _i64]
+        L.orc_dsyr2k.argtypes = [C.c_int, C.c_int, C.c_int, _i64, _i64, C.c_double, _dp, _i64, _i64,
+                                 _dp, _i64, _i64, C.c_double, _dp, _i64, _i64]
+        L.orc_dtrmm3.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _i64, _i64, C.c_double,
+                                 _dp, _i64, _i64, _dp, _i64, _i64, C.c_double, _dp, _i64, _i64]
+        L.orc_dtrmm.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, _i64, _i64, C.c_double,
+                                _dp, _i64, _i64, _dp, _i64, _i64]
         L.orc_set_threads.argtypes = [C.c_int]
         L.orc_contract_plan.argtypes = [C.c_char_p, C.c_int, C.POINTER(_i64), C.POINTER(_i64),
                                         C.c_int, C.POINTER(_i64), C.POINTER(_i64),
@@ -115,6 +123,28 @@ def dsyrk(uplo, alpha, A, beta, Cm, ta=TRANS_NO):
     m = Cm.shape[0]
     k = A.shape[0] if ta == TRANS_T else A.shape[1]
     lib().orc_dsyrk(uplo, ta, m, k, alpha, _ptr(A), *_st(A), beta, _ptr(Cm), *_st(Cm))
+
+
+def dsymm(side, uplo, alpha, A, B, beta, Cm, tb=TRANS_NO):
+    m, n = Cm.shape
+    lib().orc_dsymm(side, uplo, 0, tb, m, n, alpha, _ptr(A), *_st(A), _ptr(B), *_st(B), beta, _ptr(Cm), *_st(Cm))
+
+
+def dsyr2k(uplo, alpha, A, B, beta, Cm, ta=TRANS_NO, tb=TRANS_NO):
+    m = Cm.shape[0]
+    k = A.shape[0] if ta == TRANS_T else A.shape[1]
+    lib().orc_dsyr2k(uplo, ta, tb, m, k, alpha, _ptr(A), *_st(A), _ptr(B), *_st(B), beta, _ptr(Cm), *_st(Cm))
+
+
+def dtrmm3(side, uplo, ta, diag, alpha, A, B, beta, Cm, tb=TRANS_NO):
+    m, n = Cm.shape
+    lib().orc_dtrmm3(side, uplo, ta, diag, tb, m, n, alpha, _ptr(A), *_st(A), _ptr(B), *_st(B), beta,
+                     _ptr(Cm), *_st(Cm))
+
+
+def dtrmm(side, uplo, ta, diag, alpha, A, B):
+    m, n = B.shape
+    lib().orc_dtrmm(side, uplo, ta, diag, m, n, alpha, _ptr(A), *_st(A), _ptr(B), *_st(B))
 
 
 def dtrsm(side, uplo, ta, diag, alpha, A, B):

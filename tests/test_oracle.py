@@ -69,6 +69,83 @@ def test_gemmt_syrk(orc, uplo):
     assert np.max(np.abs(tri(Cm) - tri(C0 - A @ A.T))) < 1e-10
 
 
+def _tri(X, uplo, diag):
+    T = np.tril(X) if uplo == 0xC0 else np.triu(X)
+    if diag:
+        np.fill_diagonal(T, 1.0)
+    return T
+
+
+def _sym(X, uplo):
+    L = np.tril(X) if uplo == 0xC0 else np.triu(X)
+    return L + L.T - np.diag(np.diag(X))
+
+
+@pytest.mark.parametrize("side", [0, 1])
+@pytest.mark.parametrize("uplo", [0xC0, 0x60])
+@pytest.mark.parametrize("m,n", [(64, 64), (300, 64), (64, 300), (150, 151)])
+def test_symm(orc, side, uplo, m, n):
+    # TestSyMM.cs:40-69: alpha 1/pi, beta e, sizes small/large in both roles;
+    # DDLA's bound is Nrm1(diff) <= 2e-5, this one is elementwise 1e-12.
+    r = rng(20 + m + n)
+    na = m if side == 0 else n
+    A = uniform(r, (na, na))
+    # the unreferenced triangle is garbage: it must never be read
+    junk = np.triu(np.full((na, na), np.nan), 1) if uplo == 0xC0 else np.tril(np.full((na, na), np.nan), -1)
+    As = np.where(np.isnan(junk), np.nan, A)
+    B, C0 = uniform(r, (m, n)), uniform(r, (m, n))
+    S = _sym(A, uplo)
+    ref = np.e * C0 + (1 / np.pi) * (S @ B if side == 0 else B @ S)
+    Cm = C0.copy()
+    orc.dsymm(side, uplo, 1 / np.pi, As, B, np.e, Cm)
+    assert np.max(np.abs(Cm - ref)) < 1e-12
+
+
+@pytest.mark.parametrize("uplo", [0xC0, 0x60])
+@pytest.mark.parametrize("ta,tb", [(0, 0), (8, 8), (0, 8)])
+def test_syr2k(orc, uplo, ta, tb):
+    # TestSyR2k.cs:24-40: m 512, k 260, alpha 1/pi, beta e
+    r = rng(21)
+    m, k = 512, 260
+    A = uniform(r, (k, m) if ta else (m, k))
+    B = uniform(r, (k, m) if tb else (m, k))
+    opA, opB = (A.T if ta else A), (B.T if tb else B)
+    C0 = uniform(r, (m, m))
+    tri = np.tril if uplo == 0xC0 else np.triu
+    anti = (lambda x: np.triu(x, 1)) if uplo == 0xC0 else (lambda x: np.tril(x, -1))
+    Cm = C0.copy()
+    orc.dsyr2k(uplo, 1 / np.pi, A, B, np.e, Cm, ta=ta, tb=tb)
+    ref = np.e * C0 + (1 / np.pi) * (opA @ opB.T + opB @ opA.T)
+    assert np.max(np.abs(tri(Cm) - tri(ref))) < 1e-11
+    assert np.array_equal(anti(Cm), anti(C0))
+
+
+@pytest.mark.parametrize("side", [0, 1])
+@pytest.mark.parametrize("uplo", [0xC0, 0x60])
+@pytest.mark.parametrize("trans", [0, 8])
+@pytest.mark.parametrize("diag", [0, 0x100])
+def test_trmm_trmm3(orc, side, uplo, trans, diag):
+    # TestTrMM.cs:195-207 (alpha 1.2, tol 1e-10) and TestTrMM3.cs:195-213
+    # (alpha = beta = 1, tol 1e-10); square, rectangular here.
+    r = rng(22)
+    m, n = 200, 150
+    na = m if side == 0 else n
+    A = uniform(r, (na, na))
+    opT = _tri(A, uplo, diag)
+    opT = opT.T if trans else opT
+    B = uniform(r, (m, n))
+    X = B.copy()
+    orc.dtrmm(side, uplo, trans, diag, 1.2, A, X)
+    ref = 1.2 * (opT @ B if side == 0 else B @ opT)
+    assert np.max(np.abs(X - ref)) < 1e-10
+    C0 = uniform(r, (m, n))
+    Cm = C0.copy()
+    Bt = np.ascontiguousarray(B.T)
+    orc.dtrmm3(side, uplo, trans, diag, 1.0, A, Bt, 1.0, Cm, tb=8)
+    ref = C0 + (opT @ B if side == 0 else B @ opT)
+    assert np.max(np.abs(Cm - ref)) < 1e-10
+
+
 @pytest.mark.parametrize("side", [0, 1])
 @pytest.mark.parametrize("uplo", [0xC0, 0x60])
 @pytest.mark.parametrize("trans", [0, 8])
