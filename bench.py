@@ -284,6 +284,27 @@ def secondary(args):
             ref, scale = ref_fn()
             got = torch.tril(Cm) if wl == "syr2k" else Cm
             return float(((got - ref).abs() / scale).max())
+    elif wl == "qr":
+        n = args.n if args.n != N_DEFAULT else 8192
+        A0 = U(n, n)
+        Aw = torch.empty_like(A0)
+        Tw = torch.zeros(min(256, n), n, dtype=torch.float64, device="cuda")
+        flops = 4.0 * n ** 3 / 3.0
+        qprec = D.PREC_OZAKI if prec == D.PREC_OZAKI else 0
+        desc = f"Householder QR (UT-transform T blocks of 256), {n}x{n} FP64 U[-1,1], {pname} block reflectors"
+
+        def step():
+            Aw.copy_(A0)
+            h.geqrf(Aw, Tw, precision=qprec)
+
+        def check_err():
+            step()
+            b = U(n, 1)
+            x = torch.zeros(n, 1, dtype=torch.float64, device="cuda")
+            h.geqrs(Aw, Tw, b, x)
+            h.sync()
+            R = b - A0 @ x
+            return float(R.abs().max() / (A0.abs().sum(1).max() * x.abs().max() + b.abs().max()))
     elif wl in ("einsum-a", "einsum-b"):
         if wl == "einsum-a":
             expr, sa, sb, sc = "bik,bkj->bij", (512, 256, 256), (512, 256, 256), (512, 256, 256)
@@ -405,6 +426,19 @@ def secondary(args):
     launches = D.kernel_launches() - launches0
     ms = statistics.median(times)
     value = flops / (ms * 1e-3) / 1e9
+    classes = None
+    if wl == "qr":
+        # one more step with per-class CUDA-event brackets (outside the timed steps)
+        L.ddla_timing_enable(1)
+        step()
+        torch.cuda.synchronize()
+        classes = {}
+        for cls, name in {1: "qr_panel", 7: "qr_t_factor", 0: "block_reflector_gemm", 2: "trsm"}.items():
+            t_ms, cnt, fl, by = C.c_double(), C.c_int64(), C.c_double(), C.c_double()
+            L.ddla_timing_read(cls, C.byref(t_ms), C.byref(cnt), C.byref(fl), C.byref(by))
+            classes[name] = {"ms": t_ms.value, "launches": cnt.value,
+                             "gflops": fl.value / (t_ms.value * 1e-3) / 1e9 if t_ms.value else 0.0}
+        L.ddla_timing_enable(0)
     err = check_err() if check_err else None
     f64_peak, f32_peak = dv.measure_peaks()
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
@@ -429,7 +463,7 @@ def secondary(args):
            "vs_baseline": None, "dtype": pname, "data": "synthetic, seeded",
            "config": {"workload": desc, "precision": pname,
                       "l2": "L2 flushed between steps" if flush else "inputs larger than L2"},
-           "error": err, "roofline": roof, "gpu_launches": launches, "clocks": clk,
+           "error": err, "roofline": roof, "gpu_launches": launches, "clocks": clk, "classes": classes,
            "peaks_live": {"fp64_tflops": f64_peak, "fp32_tflops": f32_peak}}
     print(json.dumps(out))
     h.close()
@@ -445,7 +479,7 @@ def main():
     ap.add_argument("--tune", action="append", default=[], metavar="KEY=VALUE",
                     help="library tuning key (ddla_tune_set) applied before the run; repeatable")
     ap.add_argument("--workload", default="lu", choices=["lu", "gemm", "chol", "batched", "einsum-a", "einsum-b",
-                                                         "symm", "trmm", "syr2k"])
+                                                         "symm", "trmm", "syr2k", "qr"])
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-n", type=int, default=4096)
     ap.add_argument("--no-cpu", action="store_true")

@@ -90,6 +90,17 @@ _SIGS = {
     "ddla_dtrmm": (C.c_int, [_i32, _i32, _i32, _i32, _i64, _i64, C.POINTER(_d), _pd, _i64, _i64, _pd, _i64, _i64]),
     "ddla_dtrmm3": (C.c_int, [_i32, _i32, _i32, _i32, _i32, _i64, _i64, C.POINTER(_d), _pd, _i64, _i64, _pd, _i64,
                               _i64, C.POINTER(_d), _pd, _i64, _i64]),
+    "ddla_dgeqrf": (C.c_int, [_i64, _i64, _pd, _i64, _i64, _pd, _i64, _i64, _i64, C.POINTER(Opts)]),
+    "ddla_dormqr": (C.c_int, [_i32, _i64, _i64, _i64, _pd, _i64, _i64, _pd, _i64, _i64, _i64, _pd, _i64, _i64]),
+    "ddla_dgeqrs": (C.c_int, [_i64, _i64, _i64, _pd, _i64, _i64, _pd, _i64, _i64, _i64, _pd, _i64, _i64, _pd, _i64,
+                              _i64]),
+    "ddla_dorgqr": (C.c_int, [_i64, _i64, _pd, _i64, _i64, _pd, _i64, _i64, _i64, _pd, _i64, _i64]),
+    "ddla_dev_dgeqrf": (C.c_int, [_h, _i64, _i64, _pd, _i64, _i64, _pd, _i64, _i64, _i64, C.POINTER(Opts)]),
+    "ddla_dev_dormqr": (C.c_int, [_h, _i32, _i64, _i64, _i64, _pd, _i64, _i64, _pd, _i64, _i64, _i64, _pd, _i64,
+                                  _i64]),
+    "ddla_dev_dgeqrs": (C.c_int, [_h, _i64, _i64, _i64, _pd, _i64, _i64, _pd, _i64, _i64, _i64, _pd, _i64, _i64,
+                                  _pd, _i64, _i64]),
+    "ddla_dev_dorgqr": (C.c_int, [_h, _i64, _i64, _pd, _i64, _i64, _pd, _i64, _i64, _i64, _pd, _i64, _i64]),
     "ddla_dgetrf": (C.c_int, [_i64, _pd, _i64, _i64, _pi, C.POINTER(Opts)]),
     "ddla_dgetrs": (C.c_int, [_i32, _i64, _i64, _pd, _i64, _i64, _pi, _pd, _i64, _i64]),
     "ddla_dgetrf_nopiv": (C.c_int, [_i64, _pd, _i64, _i64, C.POINTER(Opts)]),

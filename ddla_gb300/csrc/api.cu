@@ -671,6 +671,131 @@ int ddla_dtrmm3(int32_t side, int32_t uplo, int32_t ta, int32_t diag, int32_t tb
     return stage_out(h, sc, c, m, n, rsc, csc);
 }
 
+// ------------------------------------------------------------------ QR
+int ddla_dev_dgeqrf(ddla_handle h, ddla_dim_t m, ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t csa, double *t,
+                    ddla_dim_t t_rows, ddla_inc_t rst, ddla_inc_t cst, const ddla_opts *opts) {
+    CHECK_ARG(h != nullptr, 1);
+    CHECK_ARG(m >= 0, 2);
+    CHECK_ARG(n >= 0, 3);
+    CHECK_ARG(t_rows >= 1, 8);
+    CHECK_ARG(!opts || opts->precision == 0 || opts->precision == DDLA_PREC_FP64 ||
+                  opts->precision == DDLA_PREC_OZAKI, 11);
+    if (m == 0 || n == 0) return 0;
+    return geqrf(h, m, n, View<double>{a, m, n, rsa, csa}, View<double>{t, t_rows, n, rst, cst}, t_rows, fprec(opts),
+                 opts ? opts->nb : 0);
+}
+
+int ddla_dev_dormqr(ddla_handle h, int32_t trans, ddla_dim_t m, ddla_dim_t n, ddla_dim_t nrhs, const double *a,
+                    ddla_inc_t rsa, ddla_inc_t csa, const double *t, ddla_dim_t t_rows, ddla_inc_t rst,
+                    ddla_inc_t cst, double *b, ddla_inc_t rsb, ddla_inc_t csb) {
+    CHECK_ARG(h != nullptr, 1);
+    CHECK_ARG(m >= 0, 3);
+    CHECK_ARG(n >= 0, 4);
+    CHECK_ARG(nrhs >= 0, 5);
+    CHECK_ARG(t_rows >= 1, 10);
+    if (m == 0 || n == 0 || nrhs == 0) return 0;
+    return ormqr(h, trans != 0, m, n, View<const double>{a, m, n, rsa, csa},
+                 View<const double>{t, t_rows, n, rst, cst}, t_rows, View<double>{b, m, nrhs, rsb, csb});
+}
+
+int ddla_dev_dgeqrs(ddla_handle h, ddla_dim_t m, ddla_dim_t n, ddla_dim_t nrhs, const double *a, ddla_inc_t rsa,
+                    ddla_inc_t csa, const double *t, ddla_dim_t t_rows, ddla_inc_t rst, ddla_inc_t cst,
+                    const double *b, ddla_inc_t rsb, ddla_inc_t csb, double *x, ddla_inc_t rsx, ddla_inc_t csx) {
+    CHECK_ARG(h != nullptr, 1);
+    CHECK_ARG(m >= 0, 2);
+    CHECK_ARG(n >= 0 && n <= m, 3);
+    CHECK_ARG(nrhs >= 0, 4);
+    CHECK_ARG(t_rows >= 1, 9);
+    if (n == 0 || nrhs == 0) return 0;
+    void *y;
+    DDLA_TRY(workspace(h, WS_Y, sizeof(double) * (size_t)(m * nrhs), &y));
+    return geqrs(h, m, n, View<const double>{a, m, n, rsa, csa}, View<const double>{t, t_rows, n, rst, cst}, t_rows,
+                 View<const double>{b, m, nrhs, rsb, csb}, View<double>{(double *)y, m, nrhs, nrhs, 1},
+                 View<double>{x, n, nrhs, rsx, csx});
+}
+
+int ddla_dev_dorgqr(ddla_handle h, ddla_dim_t m, ddla_dim_t n, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
+                    const double *t, ddla_dim_t t_rows, ddla_inc_t rst, ddla_inc_t cst, double *q, ddla_inc_t rsq,
+                    ddla_inc_t csq) {
+    CHECK_ARG(h != nullptr, 1);
+    CHECK_ARG(m >= 0, 2);
+    CHECK_ARG(n >= 0, 3);
+    CHECK_ARG(t_rows >= 1, 8);
+    if (m == 0) return 0;
+    return orgqr(h, m, n, View<const double>{a, m, n, rsa, csa}, View<const double>{t, t_rows, n, rst, cst}, t_rows,
+                 View<double>{q, m, m, rsq, csq});
+}
+
+int ddla_dgeqrf(ddla_dim_t m, ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t csa, double *t, ddla_dim_t t_rows,
+                ddla_inc_t rst, ddla_inc_t cst, const ddla_opts *opts) {
+    CHECK_ARG(m >= 0, 1);
+    CHECK_ARG(n >= 0, 2);
+    CHECK_ARG(t_rows >= 1, 7);
+    CHECK_ARG(!opts || opts->precision == 0 || opts->precision == DDLA_PREC_FP64 ||
+                  opts->precision == DDLA_PREC_OZAKI, 10);
+    if (m == 0 || n == 0) return 0;
+    GET_HANDLE(h);
+    Staged sa, st;
+    DDLA_TRY(stage_in(h, WS_A, a, m, n, rsa, csa, true, &sa));
+    DDLA_TRY(stage_in(h, WS_C, t, t_rows, n, rst, cst, true, &st));
+    DDLA_TRY(geqrf(h, m, n, sa.view, st.view, t_rows, fprec(opts), opts ? opts->nb : 0));
+    DDLA_TRY(stage_out(h, sa, a, m, n, rsa, csa));
+    return stage_out(h, st, t, t_rows, n, rst, cst);
+}
+
+int ddla_dormqr(int32_t trans, ddla_dim_t m, ddla_dim_t n, ddla_dim_t nrhs, const double *a, ddla_inc_t rsa,
+                ddla_inc_t csa, const double *t, ddla_dim_t t_rows, ddla_inc_t rst, ddla_inc_t cst, double *b,
+                ddla_inc_t rsb, ddla_inc_t csb) {
+    CHECK_ARG(m >= 0, 2);
+    CHECK_ARG(n >= 0, 3);
+    CHECK_ARG(nrhs >= 0, 4);
+    CHECK_ARG(t_rows >= 1, 9);
+    if (m == 0 || n == 0 || nrhs == 0) return 0;
+    GET_HANDLE(h);
+    Staged sa, st, sb;
+    DDLA_TRY(stage_in(h, WS_A, a, m, n, rsa, csa, true, &sa));
+    DDLA_TRY(stage_in(h, WS_C, t, t_rows, n, rst, cst, true, &st));
+    DDLA_TRY(stage_in(h, WS_B, b, m, nrhs, rsb, csb, true, &sb));
+    DDLA_TRY(ormqr(h, trans != 0, m, n, cv(sa.view), cv(st.view), t_rows, sb.view));
+    return stage_out(h, sb, b, m, nrhs, rsb, csb);
+}
+
+int ddla_dgeqrs(ddla_dim_t m, ddla_dim_t n, ddla_dim_t nrhs, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
+                const double *t, ddla_dim_t t_rows, ddla_inc_t rst, ddla_inc_t cst, const double *b, ddla_inc_t rsb,
+                ddla_inc_t csb, double *x, ddla_inc_t rsx, ddla_inc_t csx) {
+    CHECK_ARG(m >= 0, 1);
+    CHECK_ARG(n >= 0 && n <= m, 2);
+    CHECK_ARG(nrhs >= 0, 3);
+    CHECK_ARG(t_rows >= 1, 8);
+    if (n == 0 || nrhs == 0) return 0;
+    GET_HANDLE(h);
+    Staged sa, st, sb, sx;
+    DDLA_TRY(stage_in(h, WS_A, a, m, n, rsa, csa, true, &sa));
+    DDLA_TRY(stage_in(h, WS_C, t, t_rows, n, rst, cst, true, &st));
+    DDLA_TRY(stage_in(h, WS_B, b, m, nrhs, rsb, csb, true, &sb));
+    DDLA_TRY(stage_in(h, WS_F32, x, n, nrhs, rsx, csx, false, &sx));
+    void *y;
+    DDLA_TRY(workspace(h, WS_Y, sizeof(double) * (size_t)(m * nrhs), &y));
+    DDLA_TRY(geqrs(h, m, n, cv(sa.view), cv(st.view), t_rows, cv(sb.view),
+                   View<double>{(double *)y, m, nrhs, nrhs, 1}, sx.view));
+    return stage_out(h, sx, x, n, nrhs, rsx, csx);
+}
+
+int ddla_dorgqr(ddla_dim_t m, ddla_dim_t n, const double *a, ddla_inc_t rsa, ddla_inc_t csa, const double *t,
+                ddla_dim_t t_rows, ddla_inc_t rst, ddla_inc_t cst, double *q, ddla_inc_t rsq, ddla_inc_t csq) {
+    CHECK_ARG(m >= 0, 1);
+    CHECK_ARG(n >= 0, 2);
+    CHECK_ARG(t_rows >= 1, 7);
+    if (m == 0) return 0;
+    GET_HANDLE(h);
+    Staged sa, st, sq;
+    DDLA_TRY(stage_in(h, WS_A, a, m, n, rsa, csa, true, &sa));
+    DDLA_TRY(stage_in(h, WS_C, t, t_rows, n, rst, cst, true, &st));
+    DDLA_TRY(stage_in(h, WS_B, q, m, m, rsq, csq, false, &sq));
+    DDLA_TRY(orgqr(h, m, n, cv(sa.view), cv(st.view), t_rows, sq.view));
+    return stage_out(h, sq, q, m, m, rsq, csq);
+}
+
 // ------------------------------------------------------------------ factorizations, device
 int ddla_dev_dgetrf(ddla_handle h, ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t csa, int32_t *piv,
                     const ddla_opts *opts) {

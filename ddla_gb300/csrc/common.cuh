@@ -82,7 +82,7 @@ struct ddla_handle_s {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     // Growable device scratch areas (indexed by purpose).
-    ddla::Workspace ws[16];
+    ddla::Workspace ws[20];
     // Pinned host staging for host-pointer calls.
     void *pinned = nullptr;
     size_t pinned_bytes = 0;
@@ -107,9 +107,13 @@ namespace ddla {
 //   WS_INV     inverted diagonal blocks of a factorization, kept for all of
 //              its refinement solves
 //   WS_PINV    inverses of the LU panels' L11 blocks (two, by panel parity)
+//   WS_QR      QR: tau, a panel's block factor, the block-reflector scratch
+//   WS_SPLIT   partial products of split-k FP64 GEMMs
+//   WS_QRU     QR: explicit copy of a block's Householder vectors
 enum WsSlot {
     WS_A = 0, WS_B = 1, WS_C = 2, WS_TMP = 3, WS_PIV = 4, WS_F32 = 5, WS_X = 6, WS_MISC = 7,
-    WS_TRI = 8, WS_Y = 9, WS_PERM = 10, WS_TC = 11, WS_TC2 = 12, WS_INV = 13, WS_PINV = 14
+    WS_TRI = 8, WS_Y = 9, WS_PERM = 10, WS_TC = 11, WS_TC2 = 12, WS_INV = 13, WS_PINV = 14, WS_QR = 15,
+    WS_SPLIT = 16, WS_QRU = 17
 };
 
 // Order of the diagonal blocks that the triangular solves invert.
@@ -147,9 +151,16 @@ int gemm_f64(cudaStream_t s, i64 m, i64 n, i64 k, double alpha, View<const doubl
 int gemm_f32(cudaStream_t s, i64 m, i64 n, i64 k, float alpha, View<const float> A, View<const float> B,
              float beta, View<float> C, int uplo = DDLA_DENSE);
 // Structured FP64 operands of gemm_f64_struct: kind in bits 0-1, then flags.
+// OP_TRI operands may be trapezoidal (element (i, j) is zero for j > i when
+// OP_LOWER, for j < i otherwise).
 enum OpMode : int { OP_DENSE = 0, OP_SYM = 1, OP_TRI = 2, OP_LOWER = 4, OP_UNIT = 8 };
 int gemm_f64_struct(cudaStream_t s, i64 m, i64 n, i64 k, double alpha, View<const double> A, int amode,
                     View<const double> B, int bmode, double beta, View<double> C, int uplo = DDLA_DENSE);
+// The same with the k range split over extra CTAs when C has too few tiles to
+// fill the GPU (partial products in the handle's WS_SPLIT scratch, summed in a
+// fixed order, so results do not depend on scheduling).
+int gemm_f64_struct_h(ddla_handle h, i64 m, i64 n, i64 k, double alpha, View<const double> A, int amode,
+                      View<const double> B, int bmode, double beta, View<double> C, int uplo = DDLA_DENSE);
 
 // Triangular solve, B <- op(A)^-1 alpha B (left) or alpha B op(A)^-1 (right).
 template <typename T>
@@ -182,6 +193,18 @@ template <typename T>
 int ldlt(ddla_handle h, int uplo, i64 n, View<T> A, int prec, int nb);
 template <typename T>
 int ldlts(ddla_handle h, int uplo, i64 n, i64 nrhs, View<const T> A, View<T> B);
+
+// Householder QR in DDLA's UT-transform storage (qr.cu); T has tb rows and
+// holds the factor of every block of tb columns.
+// prec DDLA_PREC_OZAKI runs the block reflectors' large products through the
+// split-precision tensor-core GEMM; wcap caps the panel width (0 = automatic).
+int geqrf(ddla_handle h, i64 m, i64 n, View<double> A, View<double> T, i64 tb, int prec = DDLA_PREC_FP64,
+          int wcap = 0);
+int ormqr(ddla_handle h, bool trans, i64 m, i64 n, View<const double> A, View<const double> T, i64 tb,
+          View<double> B, int prec = DDLA_PREC_FP64);
+int geqrs(ddla_handle h, i64 m, i64 n, View<const double> A, View<const double> T, i64 tb, View<const double> B,
+          View<double> Y, View<double> X);
+int orgqr(ddla_handle h, i64 m, i64 n, View<const double> A, View<const double> T, i64 tb, View<double> Q);
 
 // Triangular-solve building blocks (trsm.cu): inverses of the 64 x 64
 // diagonal blocks, and the chained whole-system solve for <= 16 columns.

@@ -54,7 +54,7 @@ template <int BM, int BN, int WM, int WN, bool STRUCT>
 __global__ void __launch_bounds__(WM *WN * 32)
     k_gemm_f64(i64 m, i64 n, i64 k, double alpha, const double *__restrict__ A, i64 rsa, i64 csa,
                const double *__restrict__ B, i64 rsb, i64 csb, double beta, double *C, i64 rsc, i64 csc,
-               int uplo, i64 sa, i64 sb, i64 sc, const i64 *__restrict__ boff, int amode, int bmode) {
+               int uplo, i64 sa, i64 sb, i64 sc, const i64 *__restrict__ boff, int amode, int bmode, i64 kslice) {
     constexpr int NT = WM * WN * 32;
     constexpr int TWM = BM / WM, TWN = BN / WN;  // warp tile
     constexpr int FM = TWM / 8, FN = TWN / 8;   // 8x8 fragments per warp
@@ -86,14 +86,18 @@ __global__ void __launch_bounds__(WM *WN * 32)
 
     const bool a_kfast = (csa == 1);  // K contiguous in A
     const bool b_nfast = (csb == 1);  // N contiguous in B
-    // k range of this tile: a triangular A (k == m) is zero right of its
-    // diagonal when lower (left of it when upper); a triangular B (k == n) is
-    // zero above its diagonal when lower (below it when upper).
+    // k range of this tile: a triangular A is zero right of its diagonal when
+    // lower (left of it when upper); a triangular B is zero above its diagonal
+    // when lower (below it when upper).
     i64 kb = 0, ke = k;
+    if (kslice > 0) {   // split k: problem z sums k in [z*kslice, (z+1)*kslice)
+        kb = bz * kslice;
+        ke = min(k, kb + kslice);
+    }
     if (STRUCT) {
         if ((amode & 3) == OP_TRI) {
             if (amode & OP_LOWER) ke = min(ke, m0 + BM);
-            else kb = m0;
+            else kb = max(kb, m0);
         }
         if ((bmode & 3) == OP_TRI) {
             if (bmode & OP_LOWER) kb = max(kb, n0);
@@ -106,14 +110,14 @@ __global__ void __launch_bounds__(WM *WN * 32)
             int r, kk;
             if (a_kfast) { kk = e % BK64; r = e / BK64; } else { r = e % BM; kk = e / BM; }
             i64 gr = m0 + r, gk = k0 + kk;
-            As[kk][r] = (gr < m && gk < k) ? ld_op<STRUCT>(A, rsa, csa, gr, gk, amode) : 0.0;
+            As[kk][r] = (gr < m && gk < ke) ? ld_op<STRUCT>(A, rsa, csa, gr, gk, amode) : 0.0;
         }
         // B tile BK x BN
         for (int e = tid; e < BN * BK64; e += NT) {
             int c, kk;
             if (b_nfast) { c = e % BN; kk = e / BN; } else { kk = e % BK64; c = e / BK64; }
             i64 gc = n0 + c, gk = k0 + kk;
-            Bs[kk][c] = (gc < n && gk < k) ? ld_op<STRUCT>(B, rsb, csb, gk, gc, bmode) : 0.0;
+            Bs[kk][c] = (gc < n && gk < ke) ? ld_op<STRUCT>(B, rsb, csb, gk, gc, bmode) : 0.0;
         }
         __syncthreads();
 #pragma unroll
@@ -155,7 +159,7 @@ __global__ void __launch_bounds__(WM *WN * 32)
 template <int BM, int BN, int WM, int WN>
 int launch_f64(cudaStream_t s, i64 m, i64 n, i64 k, double alpha, View<const double> A, View<const double> B,
                double beta, View<double> C, int uplo, i64 batch, i64 sa, i64 sb, i64 sc, const i64 *boff,
-               int amode, int bmode) {
+               int amode, int bmode, i64 kslice = 0) {
     i64 gx = (n + BN - 1) / BN, gy = (m + BM - 1) / BM;
     if (gy > 65535) { set_error("gemm_f64: m too large for one launch"); return DDLA_ERR_UNSUPPORTED; }
     for (i64 b0 = 0; b0 < batch; b0 += 65535) {
@@ -165,11 +169,12 @@ int launch_f64(cudaStream_t s, i64 m, i64 n, i64 k, double alpha, View<const dou
             k_gemm_f64<BM, BN, WM, WN, true><<<grid, WM * WN * 32, 0, s>>>(
                 m, n, k, alpha, A.p + (boff ? 0 : b0 * sa), A.rs, A.cs, B.p + (boff ? 0 : b0 * sb), B.rs, B.cs,
                 beta, C.p + (boff ? 0 : b0 * sc), C.rs, C.cs, uplo, sa, sb, sc, boff ? boff + 3 * b0 : nullptr,
-                amode, bmode);
+                amode, bmode, kslice);
         else
             k_gemm_f64<BM, BN, WM, WN, false><<<grid, WM * WN * 32, 0, s>>>(
                 m, n, k, alpha, A.p + (boff ? 0 : b0 * sa), A.rs, A.cs, B.p + (boff ? 0 : b0 * sb), B.rs, B.cs,
-                beta, C.p + (boff ? 0 : b0 * sc), C.rs, C.cs, uplo, sa, sb, sc, boff ? boff + 3 * b0 : nullptr, 0, 0);
+                beta, C.p + (boff ? 0 : b0 * sc), C.rs, C.cs, uplo, sa, sb, sc, boff ? boff + 3 * b0 : nullptr, 0, 0,
+                kslice);
         DDLA_LAUNCHED();
     }
     return 0;
@@ -197,24 +202,24 @@ double balance(i64 tiles, int sms) {
 
 static int gemm_f64_any(cudaStream_t s, i64 m, i64 n, i64 k, double alpha, View<const double> A,
                         View<const double> B, double beta, View<double> C, int uplo, i64 batch, i64 sa, i64 sb, i64 sc,
-                        const i64 *boff, int amode = 0, int bmode = 0) {
+                        const i64 *boff, int amode = 0, int bmode = 0, i64 kslice = 0) {
     if (m <= 0 || n <= 0 || batch <= 0) return 0;
     if (k <= 0 || alpha == 0.0) {
         // C = beta*C on the requested part: reuse the kernel with k = 0.
         k = 0;
     }
     if (n <= 16)
-        return launch_f64<128, 16, 4, 1>(s, m, n, k, alpha, A, B, beta, C, uplo, batch, sa, sb, sc, boff, amode, bmode);
+        return launch_f64<128, 16, 4, 1>(s, m, n, k, alpha, A, B, beta, C, uplo, batch, sa, sb, sc, boff, amode, bmode, kslice);
     int sms = sm_count();
     i64 t64 = ((m + 63) / 64) * ((n + 63) / 64) * batch;
     i64 t32 = ((m + 31) / 32) * ((n + 63) / 64) * batch;
     i64 t3232 = ((m + 31) / 32) * ((n + 31) / 32) * batch;
     double b64 = balance(t64, sms), b32 = balance(t32, sms), b3232 = balance(t3232, sms);
     if (t64 >= 8 * sms || (b64 >= 0.9 && b64 >= b32 - 0.02))
-        return launch_f64<64, 64, 2, 2>(s, m, n, k, alpha, A, B, beta, C, uplo, batch, sa, sb, sc, boff, amode, bmode);
+        return launch_f64<64, 64, 2, 2>(s, m, n, k, alpha, A, B, beta, C, uplo, batch, sa, sb, sc, boff, amode, bmode, kslice);
     if (b32 >= 0.9 || b32 >= b3232 - 0.02)
-        return launch_f64<32, 64, 2, 2>(s, m, n, k, alpha, A, B, beta, C, uplo, batch, sa, sb, sc, boff, amode, bmode);
-    return launch_f64<32, 32, 2, 2>(s, m, n, k, alpha, A, B, beta, C, uplo, batch, sa, sb, sc, boff, amode, bmode);
+        return launch_f64<32, 64, 2, 2>(s, m, n, k, alpha, A, B, beta, C, uplo, batch, sa, sb, sc, boff, amode, bmode, kslice);
+    return launch_f64<32, 32, 2, 2>(s, m, n, k, alpha, A, B, beta, C, uplo, batch, sa, sb, sc, boff, amode, bmode, kslice);
 }
 
 int gemm_f64(cudaStream_t s, i64 m, i64 n, i64 k, double alpha, View<const double> A, View<const double> B,
@@ -224,15 +229,72 @@ int gemm_f64(cudaStream_t s, i64 m, i64 n, i64 k, double alpha, View<const doubl
 
 // C = alpha*A*B + beta*C where A and / or B is structured (amode / bmode: OP_SYM
 // or OP_TRI, plus OP_LOWER for the stored / nonzero triangle and OP_UNIT for an
-// implicit unit diagonal that is never read).  A triangular A needs k == m, a
-// triangular B needs k == n.
+// implicit unit diagonal that is never read).  A symmetric operand is square; a
+// triangular one may be trapezoidal (the block of Householder vectors of a QR
+// panel is unit-lower trapezoidal), the triangle being the one of element
+// (i, j) with j <= i (lower) or j >= i (upper).
 int gemm_f64_struct(cudaStream_t s, i64 m, i64 n, i64 k, double alpha, View<const double> A, int amode,
                     View<const double> B, int bmode, double beta, View<double> C, int uplo) {
-    if (((amode & 3) == OP_TRI && k != m) || ((bmode & 3) == OP_TRI && k != n)) {
-        set_error("gemm_f64_struct: triangular operand must be square");
+    if (((amode & 3) == OP_SYM && k != m) || ((bmode & 3) == OP_SYM && k != n)) {
+        set_error("gemm_f64_struct: symmetric operand must be square");
         return DDLA_ERR_UNSUPPORTED;
     }
     return gemm_f64_any(s, m, n, k, alpha, A, B, beta, C, uplo, 1, 0, 0, 0, nullptr, amode, bmode);
+}
+
+namespace {
+// C = alpha * sum_z P_z + beta * C on C's triangle (the partials P_z are m x n
+// row-major, z ascending).
+__global__ void k_splitk_reduce(i64 m, i64 n, int parts, const double *__restrict__ P, double alpha, double beta,
+                                double *C, i64 rsc, i64 csc, int uplo) {
+    const i64 tot = m * n;
+    for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < tot; e += (i64)gridDim.x * blockDim.x) {
+        const i64 i = e / n, j = e % n;
+        if (uplo == DDLA_LOWER && j > i) continue;
+        if (uplo == DDLA_UPPER && j < i) continue;
+        double acc = 0.0;
+        for (int z = 0; z < parts; z++) acc += P[z * tot + e];
+        double *cp = C + i * rsc + j * csc;
+        const double v = alpha * acc;
+        *cp = (beta == 0.0) ? v : fma(beta, *cp, v);
+    }
+}
+}  // namespace
+
+int gemm_f64_struct_h(ddla_handle h, i64 m, i64 n, i64 k, double alpha, View<const double> A, int amode,
+                      View<const double> B, int bmode, double beta, View<double> C, int uplo) {
+    if (m <= 0 || n <= 0) return 0;
+    const int sms = sm_count();
+    // tiles of the configuration gemm_f64_any picks for this shape (an upper
+    // bound for a triangular C)
+    const i64 tiles = n <= 16 ? (m + 127) / 128 : ((m + 31) / 32) * ((n + 63) / 64);
+    i64 parts = 1;
+    if (alpha != 0.0 && k >= 1024 && tiles < sms) {
+        parts = (2 * sms + tiles - 1) / tiles;
+        if (parts > k / 256) parts = k / 256;
+        if (parts > 64) parts = 64;
+    }
+    if (parts < 2) return gemm_f64_struct(h->stream, m, n, k, alpha, A, amode, B, bmode, beta, C, uplo);
+    if ((amode & 3) == OP_SYM || (bmode & 3) == OP_SYM) {
+        if (k != ((amode & 3) == OP_SYM ? m : n)) {
+            set_error("gemm_f64_struct: symmetric operand must be square");
+            return DDLA_ERR_UNSUPPORTED;
+        }
+    }
+    i64 kslice = (k + parts - 1) / parts;
+    kslice = (kslice + 15) / 16 * 16;
+    parts = (k + kslice - 1) / kslice;
+    void *ws;
+    DDLA_TRY(workspace(h, WS_SPLIT, sizeof(double) * (size_t)(parts * m * n), &ws));
+    double *P = (double *)ws;
+    DDLA_TRY(gemm_f64_any(h->stream, m, n, k, 1.0, A, B, 0.0, View<double>{P, m, n, n, 1}, uplo, parts, 0, 0, m * n,
+                          nullptr, amode, bmode, kslice));
+    const i64 tot = m * n;
+    const i64 blocks = (tot + 255) / 256 < 2048 ? (tot + 255) / 256 : 2048;
+    k_splitk_reduce<<<(unsigned)blocks, 256, 0, h->stream>>>(m, n, (int)parts, P, alpha, beta, C.p, C.rs, C.cs,
+                                                               uplo);
+    DDLA_LAUNCHED();
+    return 0;
 }
 
 // Batched GEMM whose problem z starts at element offsets d_offsets[3z..3z+2]

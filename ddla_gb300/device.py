@@ -22,7 +22,9 @@ class Handle:
 
     def __init__(self, stream=None):
         self.h = C.c_void_p()
-        s = None if stream is None else C.c_void_p(stream.cuda_stream)
+        # torch reports the legacy default stream as 0, which the library reads
+        # as "make a stream of your own": pass cudaStreamLegacy (1) instead
+        s = None if stream is None else C.c_void_p(stream.cuda_stream or 1)
         check(lib().ddla_handle_create(C.byref(self.h), s), "handle_create")
 
     def close(self):
@@ -76,6 +78,28 @@ class Handle:
         m, n = Cm.shape
         check(lib().ddla_dev_dtrmm3(self.h, side, uplo, ta, diag, tb, m, n, alpha, _p(A), *_st(A), _p(B), *_st(B),
                                     beta, _p(Cm), *_st(Cm)), "dev_dtrmm3")
+
+    def geqrf(self, A, T, precision=0, nb=0):
+        m, n = A.shape
+        o = Opts()
+        o.precision, o.nb = precision, nb
+        check(lib().ddla_dev_dgeqrf(self.h, m, n, _p(A), *_st(A), _p(T), T.shape[0], *_st(T), C.byref(o)),
+              "dev_dgeqrf")
+
+    def ormqr(self, trans, A, T, B):
+        m, n = A.shape
+        check(lib().ddla_dev_dormqr(self.h, 1 if trans else 0, m, n, B.shape[1], _p(A), *_st(A), _p(T), T.shape[0],
+                                    *_st(T), _p(B), *_st(B)), "dev_dormqr")
+
+    def geqrs(self, A, T, B, X):
+        m, n = A.shape
+        check(lib().ddla_dev_dgeqrs(self.h, m, n, B.shape[1], _p(A), *_st(A), _p(T), T.shape[0], *_st(T), _p(B),
+                                    *_st(B), _p(X), *_st(X)), "dev_dgeqrs")
+
+    def orgqr(self, A, T, Q):
+        m, n = A.shape
+        check(lib().ddla_dev_dorgqr(self.h, m, n, _p(A), *_st(A), _p(T), T.shape[0], *_st(T), _p(Q), *_st(Q)),
+              "dev_dorgqr")
 
     def getrf(self, A, piv, nb=0, precision=0):
         o = Opts()

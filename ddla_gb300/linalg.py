@@ -8,6 +8,7 @@ tests read like DDLA's own tests:
   LU                                        DDLA/Factorizations/LU.cs:13-128
   Cholesky                                  DDLA/Factorizations/Cholesky.cs:10-88
   LDLT                                      DDLA/Factorizations/LDLT.cs:9-137
+  QR                                        DDLA/Factorizations/QR.cs:14-534
 
 Matrices are float64 numpy arrays; any 2-D view works (its element strides
 are DDLA's RowStride / ColStride), and in-place operations write through the
@@ -21,7 +22,7 @@ from . import _lib
 from ._lib import (LEFT, LOWER, NO_TRANSPOSE, NONUNIT, RIGHT, TRANSPOSE, UNIT, UPPER, LinalgError, Opts,
                    SolveReport, check, lib)
 
-__all__ = ["BlasProvider", "LU", "Cholesky", "LDLT", "solve_mixed", "LinalgError"]
+__all__ = ["BlasProvider", "LU", "Cholesky", "LDLT", "QR", "solve_mixed", "LinalgError"]
 
 
 def _view(x, name):
@@ -402,6 +403,130 @@ class LDLT:
         if B.shape[0] != A.shape[0]:
             raise ValueError("Matrix dimensions do not match for Cholesky solve.")
         check(lib().ddla_dldlts(uplo, A.shape[0], B.shape[1], _p(A), *_st(A), _p(B), *_st(B)), "LDLTSolve")
+
+
+class _InstanceOrStatic:
+    """A name that is an instance method on instances and a static method on
+    the class, like C#'s overloads QR.Solve(B) / QR.Solve(A, T, B, X)."""
+
+    def __init__(self, inst, static):
+        self.inst, self.static = inst, static
+
+    def __get__(self, obj, objtype=None):
+        if obj is None:
+            return self.static
+        return lambda *a, **k: self.inst(obj, *a, **k)
+
+
+class QR:
+    """QR(A, inplace=False) -- DDLA/Factorizations/QR.cs:14-122.  A is m x n
+    (any m, n); Solve needs m >= n and returns the least-squares solution."""
+    BlockSize = 256   # QR.cs:16
+
+    def __init__(self, A, inplace=False):
+        A = _view(A, "A")
+        self.matrix = A if inplace else A.copy()
+        self.aux = QR.CreateT(self.matrix)
+        self.computed = False
+        self.deconstructed = False
+
+    def ComputeOnce(self):
+        if self.deconstructed:
+            raise RuntimeError("Matrix has been deconstructed, cannot compute again.")
+        if self.computed:
+            return
+        self.computed = True
+        QR.QRDecompose(self.matrix, self.aux)
+
+    def _solve_inst(self, b, output=None):
+        """QR.cs:45-77: the least-squares solution of A X = b."""
+        self.ComputeOnce()
+        vec = b.ndim == 1
+        B = _view(b, "b")
+        X = np.zeros((self.matrix.shape[1], B.shape[1])) if output is None else _view(output, "output")
+        if X.shape != (self.matrix.shape[1], B.shape[1]):
+            raise ValueError("Output matrix has incorrect dimensions.")
+        QR._solve_static(self.matrix, self.aux, B, X)
+        return X[:, 0] if vec else X
+
+    def ApplyQ(self, b):
+        """b <- Q b in place (QR.cs:79-93)."""
+        B = _view(b, "b")
+        QR.ApplyQlnfc(self.matrix, self.aux, B)
+        return b
+
+    def ApplyQT(self, b):
+        """b <- Q^T b in place (QR.cs:95-109)."""
+        B = _view(b, "b")
+        QR.ApplyQlhfc(self.matrix, self.aux, B)
+        return b
+
+    def Deconstruct(self):
+        """(Q m x m, R) as QR.cs:111-122."""
+        self.ComputeOnce()
+        m = self.matrix.shape[0]
+        Q = np.zeros((m, m))
+        QR.FormQ(self.matrix, self.aux, Q)
+        R = np.triu(self.matrix)
+        self.deconstructed = True
+        return Q, R
+
+    @staticmethod
+    def CreateT(A):
+        m, n = A.shape
+        return np.zeros((min(QR.BlockSize, max(m, n)), n))
+
+    @staticmethod
+    def QRDecompose(A, T=None, precision=0, nb=0):
+        A = _view(A, "A")
+        if T is None:
+            T = QR.CreateT(A)
+        T = _view(T, "T")
+        if T.shape[1] != A.shape[1]:
+            raise ValueError("Matrix T and A must have the same number of columns.")
+        check(lib().ddla_dgeqrf(A.shape[0], A.shape[1], _p(A), *_st(A), _p(T), T.shape[0], *_st(T),
+                                C.byref(_opts(nb, precision))), "QRDecompose")
+        return T
+
+    @staticmethod
+    def _solve_static(A, T, B, X):
+        """QR.cs:151-168: X = argmin |A X - B| with the factors (A, T)."""
+        A, T, B, X = _view(A, "A"), _view(T, "T"), _view(B, "B"), _view(X, "X")
+        if A.shape[1] != T.shape[1]:
+            raise ValueError("Matrix T and A must have the same number of columns.")
+        if A.shape[0] != B.shape[0]:
+            raise ValueError("Matrix A and B must have the same number of rows.")
+        if A.shape[1] != X.shape[0]:
+            raise ValueError("The number of columns in A must match the number of rows in X.")
+        if X.shape[1] != B.shape[1]:
+            raise ValueError("Matrix X and B must have the same number of columns.")
+        m, n = A.shape
+        check(lib().ddla_dgeqrs(m, n, B.shape[1], _p(A), *_st(A), _p(T), T.shape[0], *_st(T), _p(B), *_st(B),
+                                _p(X), *_st(X)), "QR.Solve")
+
+    Solve = _InstanceOrStatic(_solve_inst, _solve_static.__func__)
+
+    @staticmethod
+    def ApplyQlhfc(A, T, B):
+        A, T, B = _view(A, "A"), _view(T, "T"), _view(B, "B")
+        check(lib().ddla_dormqr(1, A.shape[0], A.shape[1], B.shape[1], _p(A), *_st(A), _p(T), T.shape[0], *_st(T),
+                                _p(B), *_st(B)), "ApplyQlhfc")
+
+    @staticmethod
+    def ApplyQlnfc(A, T, B):
+        A, T, B = _view(A, "A"), _view(T, "T"), _view(B, "B")
+        check(lib().ddla_dormqr(0, A.shape[0], A.shape[1], B.shape[1], _p(A), *_st(A), _p(T), T.shape[0], *_st(T),
+                                _p(B), *_st(B)), "ApplyQlnfc")
+
+    @staticmethod
+    def FormQ(A, T, Q):
+        A, T, Q = _view(A, "A"), _view(T, "T"), _view(Q, "Q")
+        if A.shape[1] != T.shape[1]:
+            raise ValueError("Matrix T and A must have the same number of columns.")
+        if Q.shape != (A.shape[0], A.shape[0]):
+            raise ValueError("The dimension of Q must be equal to the number of rows in A.")
+        check(lib().ddla_dorgqr(A.shape[0], A.shape[1], _p(A), *_st(A), _p(T), T.shape[0], *_st(T), _p(Q), *_st(Q)),
+              "FormQ")
 
 
 def solve_mixed(A, B, spd=False, uplo=LOWER, precision=_lib.PREC_FP32, x_ref=None, tol=0.0, max_iter=0, nb=0):

@@ -110,7 +110,8 @@ int64_t ddla_kernel_launches(void);
 
 typedef struct ddla_handle_s *ddla_handle;
 /* Create a handle bound to the current device and a stream (cudaStream_t cast
- * to void*; NULL = a new non-blocking stream owned by the handle). */
+ * to void*; NULL = a new non-blocking stream owned by the handle; the legacy
+ * default stream is cudaStreamLegacy, (void *)1). */
 int ddla_handle_create(ddla_handle *h, void *stream);
 int ddla_handle_destroy(ddla_handle h);
 int ddla_handle_sync(ddla_handle h);
@@ -134,7 +135,10 @@ int ddla_timing_read(int cls, double *total_ms, int64_t *launches, double *flops
  * the chained per-block triangular solve instead of the cluster solve),
  * "trsv.cluster.size", "refine.gmres" (0 = classical refinement for one
  * right-hand side), "refine.gmres.m" (GMRES restart length),
- * "batched.nb.{32,64,128,big}", "batched.ctas_per_sm".  value == INT64_MIN
+ * "batched.nb.{32,64,128,big}", "batched.ctas_per_sm", "update.tc",
+ * "update.tn", "update.tiles_per_cta", "u12.gemm", "qr.nb" (QR panel width
+ * cap), "qr.cluster" (CTAs per QR panel cluster), "qr.resident" (0 factors QR
+ * panels in place through L2 instead of in shared memory).  value == INT64_MIN
  * removes a key. */
 int ddla_tune_set(const char *key, int64_t value);
 int64_t ddla_tune_get(const char *key, int64_t dflt);
@@ -199,6 +203,35 @@ int ddla_dtrmm3(int32_t sidea, int32_t uploa, int32_t transa, int32_t diaga, int
 int ddla_dtrsm(int32_t side, int32_t uploa, int32_t transa, int32_t diaga, ddla_dim_t m, ddla_dim_t n,
                const double *alpha, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
                double *b, ddla_inc_t rsb, ddla_inc_t csb);
+
+/* ------------------------------------------------ QR (host) */
+
+/* Householder QR in place: R on and above the diagonal, the Householder
+ * vectors u_j (u_j(j) = 1 implicit) below it.  T (t_rows x n, element strides
+ * rst / cst) receives, for every block of t_rows columns starting at j0, the
+ * upper triangular UT factor S of that block in T[0:b, j0:j0+b]
+ * (S(j,j) = tau_j, S(i,j) = u_i^T u_j); the rest of T is not written.
+ * QR.QRDecompose(A, T), DDLA/Factorizations/QR.cs:130-149, 314-389; DDLA
+ * sizes T with QR.CreateT (QR.cs:124-128): t_rows = min(256, max(m, n)).
+ * opts (may be NULL): precision DDLA_PREC_OZAKI runs the large block-reflector
+ * products through the split-precision tensor-core GEMM (FP64-level accuracy),
+ * nb caps the panel width. */
+int ddla_dgeqrf(ddla_dim_t m, ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t csa,
+                double *t, ddla_dim_t t_rows, ddla_inc_t rst, ddla_inc_t cst, const ddla_opts *opts);
+/* B (m x nrhs) = Q^T B (trans != 0) or Q B with the factors of ddla_dgeqrf.
+ * QR.ApplyQT / ApplyQ, QR.cs:79-109 (ApplyQlhfc / ApplyQlnfc, QR.cs:417-534). */
+int ddla_dormqr(int32_t trans, ddla_dim_t m, ddla_dim_t n, ddla_dim_t nrhs, const double *a, ddla_inc_t rsa,
+                ddla_inc_t csa, const double *t, ddla_dim_t t_rows, ddla_inc_t rst, ddla_inc_t cst,
+                double *b, ddla_inc_t rsb, ddla_inc_t csb);
+/* X (n x nrhs) = least-squares solution of A X = B (m >= n): Q^T B, then R.
+ * QR.Solve, QR.cs:151-168, 391-415. */
+int ddla_dgeqrs(ddla_dim_t m, ddla_dim_t n, ddla_dim_t nrhs, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
+                const double *t, ddla_dim_t t_rows, ddla_inc_t rst, ddla_inc_t cst,
+                const double *b, ddla_inc_t rsb, ddla_inc_t csb, double *x, ddla_inc_t rsx, ddla_inc_t csx);
+/* Q (m x m) = H_0 H_1 ... H_{k-1}.  QR.FormQ(A, T, Q), QR.cs:179-201. */
+int ddla_dorgqr(ddla_dim_t m, ddla_dim_t n, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
+                const double *t, ddla_dim_t t_rows, ddla_inc_t rst, ddla_inc_t cst,
+                double *q, ddla_inc_t rsq, ddla_inc_t csq);
 
 /* ------------------------------------------------ factorizations (host) */
 
@@ -279,6 +312,17 @@ int ddla_dev_dtrmm3(ddla_handle h, int32_t sidea, int32_t uploa, int32_t transa,
                     ddla_dim_t m, ddla_dim_t n, double alpha, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
                     const double *b, ddla_inc_t rsb, ddla_inc_t csb,
                     double beta, double *c, ddla_inc_t rsc, ddla_inc_t csc);
+int ddla_dev_dgeqrf(ddla_handle h, ddla_dim_t m, ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t csa,
+                    double *t, ddla_dim_t t_rows, ddla_inc_t rst, ddla_inc_t cst, const ddla_opts *opts);
+int ddla_dev_dormqr(ddla_handle h, int32_t trans, ddla_dim_t m, ddla_dim_t n, ddla_dim_t nrhs, const double *a,
+                    ddla_inc_t rsa, ddla_inc_t csa, const double *t, ddla_dim_t t_rows, ddla_inc_t rst,
+                    ddla_inc_t cst, double *b, ddla_inc_t rsb, ddla_inc_t csb);
+int ddla_dev_dgeqrs(ddla_handle h, ddla_dim_t m, ddla_dim_t n, ddla_dim_t nrhs, const double *a, ddla_inc_t rsa,
+                    ddla_inc_t csa, const double *t, ddla_dim_t t_rows, ddla_inc_t rst, ddla_inc_t cst,
+                    const double *b, ddla_inc_t rsb, ddla_inc_t csb, double *x, ddla_inc_t rsx, ddla_inc_t csx);
+int ddla_dev_dorgqr(ddla_handle h, ddla_dim_t m, ddla_dim_t n, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
+                    const double *t, ddla_dim_t t_rows, ddla_inc_t rst, ddla_inc_t cst,
+                    double *q, ddla_inc_t rsq, ddla_inc_t csq);
 int ddla_dev_dgetrf(ddla_handle h, ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t csa, int32_t *piv,
                     const ddla_opts *opts);
 int ddla_dev_dgetrs(ddla_handle h, int32_t trans, ddla_dim_t n, ddla_dim_t nrhs, const double *lu, ddla_inc_t rsa,

@@ -473,6 +473,154 @@ void orc_dtrsm(int side, int uplo, int ta, int diag, i64 m, i64 n, double alpha,
 }
 
 /* ------------------------------------------------------------------------ */
+/* Householder QR, DDLA/Factorizations/QR.cs (UT transform, as libflame)     */
+/* ------------------------------------------------------------------------ */
+
+#define QR_BLOCKED_ABOVE 256   /* QR.BlockSize, QR.cs:16; blocked iff n > 256 (QR.cs:139-149) */
+
+/* Vector 2-norm (NrmF of a vector, bli_dnormfv): plain sum of squares. */
+static double nrm2(const double *x, i64 n, i64 inc) {
+    double s = 0.0;
+    for (i64 i = 0; i < n; i++) s = fma(x[i * inc], x[i * inc], s);
+    return sqrt(s);
+}
+
+/* BuildHouseHolder, DDLA/Transformations/HouseHolder.cs:34-58: chi <- rho,
+ * x <- u2 = x / (chi - rho), tau = (1 + |u2|^2) / 2; an all-zero x gives the
+ * reflection chi <- -chi with tau = 1/2. */
+static void house_build(double *chi, double *x, i64 n, i64 inc, double *tau) {
+    double len = nrm2(x, n, inc);
+    if (len == 0.0) { *chi = -*chi; *tau = 0.5; return; }
+    double alpha = hypot(*chi, len);
+    double rho = -copysign(alpha, *chi);
+    double miu = *chi - rho;
+    *chi = rho;
+    double s = 1.0 / miu;                   /* InvScal = scal by 1/alpha, BLAS/1v.cs:97-103 */
+    for (i64 i = 0; i < n; i++) x[i * inc] *= s;
+    double sc = len / fabs(miu);
+    *tau = (1.0 + sc * sc) / 2.0;
+}
+
+/* ApplyHouseHolder(Left), HouseHolder.cs:95-115: w = a1 + A2^T u2, w /= tau,
+ * a1 -= w, A2 -= u2 w^T.  a1 is a 1 x c row, A2 n x c, u2 n long. */
+static void house_apply_left(double tau, const double *u2, i64 incu, mat a1, mat A2) {
+    i64 c = a1.c;
+    if (c == 0 || tau == 0.0) return;
+    double *w = (double *)malloc(sizeof(double) * c);
+    for (i64 j = 0; j < c; j++) w[j] = *AT(a1, 0, j);
+    for (i64 j = 0; j < c; j++)
+        for (i64 i = 0; i < A2.r; i++) w[j] = fma(*AT(A2, i, j), u2[i * incu], w[j]);
+    double s = 1.0 / tau;
+    for (i64 j = 0; j < c; j++) { w[j] *= s; *AT(a1, 0, j) -= w[j]; }
+    for (i64 i = 0; i < A2.r; i++) {
+        double ui = -u2[i * incu];
+        for (i64 j = 0; j < c; j++) *AT(A2, i, j) = fma(ui, w[j], *AT(A2, i, j));
+    }
+    free(w);
+}
+
+/* QRDecUnblock, QR.cs:314-350: one reflector per column; T(i, i) = tau_i and
+ * T(0:i, i) = A(i, 0:i)^T + A(i+1:, 0:i)^T A(i+1:, i) = u_j^T u_i. */
+static void qr_unblock(mat A, mat T) {
+    i64 m = A.r, n = A.c, k = m < n ? m : n;
+    for (i64 i = 0; i < k; i++) {
+        double *tau = AT(T, i, i);
+        house_build(AT(A, i, i), AT(A, i + 1 < m ? i + 1 : i, i), m - i - 1, A.rs, tau);
+        house_apply_left(*tau, AT(A, i + 1 < m ? i + 1 : i, i), A.rs, sub(A, i, 1, i + 1, n - i - 1),
+                         sub(A, i + 1, m - i - 1, i + 1, n - i - 1));
+        for (i64 j = 0; j < i; j++) {
+            double t = *AT(A, i, j);
+            for (i64 r = i + 1; r < m; r++) t = fma(*AT(A, r, j), *AT(A, r, i), t);
+            *AT(T, j, i) = t;
+        }
+    }
+}
+
+/* One block of ApplyQlhfc (QR.cs:417-467, trans) or ApplyQlnfc (QR.cs:469-533):
+ * W = B1 (copy); W = A11^T W; W += A21^T B2; W = S^-T W (trans) or S^-1 W;
+ * B2 -= A21 W; W = -A11 W; B1 += W.  A11 unit lower (b x b), A21 below it. */
+static void qr_apply_one(int trans, mat A11, mat A21, mat S, mat B1, mat B2) {
+    i64 b = A11.r, c = B1.c;
+    if (c == 0) return;
+    double *w = (double *)malloc(sizeof(double) * b * c);
+    mat W = mk(w, b, c, c, 1);
+    for (i64 i = 0; i < b; i++) for (i64 j = 0; j < c; j++) *AT(W, i, j) = *AT(B1, i, j);
+    orc_dtrmm(SD_LEFT, UL_LOWER, TR_T, DG_UNIT, b, c, 1.0, A11.p, A11.rs, A11.cs, w, c, 1);
+    if (A21.r > 0) gemm_core(1.0, tr(A21), B2, W, 0);
+    orc_dtrsm(SD_LEFT, UL_UPPER, trans ? TR_T : TR_NO, DG_NONUNIT, b, c, 1.0, S.p, S.rs, S.cs, w, c, 1);
+    if (A21.r > 0) gemm_core(-1.0, A21, W, B2, 0);
+    orc_dtrmm(SD_LEFT, UL_LOWER, TR_NO, DG_UNIT, b, c, -1.0, A11.p, A11.rs, A11.cs, w, c, 1);
+    for (i64 i = 0; i < b; i++) for (i64 j = 0; j < c; j++) *AT(B1, i, j) += *AT(W, i, j);
+    free(w);
+}
+
+/* Q^T B (trans, blocks first to last) or Q B (last to first); blocks of T.r
+ * columns over the k = min(m, n) reflectors.  ApplyQlnfc (QR.cs:479-503) sizes
+ * its first (= last) block by T.Cols % block, which is the same partition when
+ * m >= n; this follows the forward partition in both directions. */
+static void qr_apply(int trans, mat A, mat T, mat B) {
+    i64 m = A.r, k = A.r < A.c ? A.r : A.c, tb = T.r;
+    i64 nblk = (k + tb - 1) / tb;
+    for (i64 bi = 0; bi < nblk; bi++) {
+        i64 blk = trans ? bi : nblk - 1 - bi;
+        i64 j0 = blk * tb, b = k - j0 < tb ? k - j0 : tb;
+        qr_apply_one(trans, sub(A, j0, b, j0, b), sub(A, j0 + b, m - j0 - b, j0, b), sub(T, 0, b, j0, b),
+                     sub(B, j0, b, 0, B.c), sub(B, j0 + b, m - j0 - b, 0, B.c));
+    }
+}
+
+/* QR.QRDecompose(A, T) (QR.cs:139-149): unblocked (QR.cs:314-350) when
+ * n <= 256, else QRDecBlock (QR.cs:352-389) in blocks of T.Rows columns, each
+ * factored unblocked and applied to the columns on its right with
+ * ApplyQlhfc.  Returns -7 if T is too short for the unblocked form. */
+int orc_dgeqrf(i64 m, i64 n, double *a, i64 rsa, i64 csa, double *t, i64 t_rows, i64 rst, i64 cst) {
+    mat A = mk(a, m, n, rsa, csa), T = mk(t, t_rows, n, rst, cst);
+    i64 k = m < n ? m : n;
+    if (k == 0) return 0;
+    if (n <= QR_BLOCKED_ABOVE) {
+        if (t_rows < k) return -7;
+        qr_unblock(A, T);
+        return 0;
+    }
+    for (i64 j0 = 0; j0 < k; j0 += t_rows) {
+        i64 b = k - j0 < t_rows ? k - j0 : t_rows;
+        mat Ab1 = sub(A, j0, m - j0, j0, b), S = sub(T, 0, b, j0, b);
+        qr_unblock(Ab1, S);
+        if (j0 + b < n)
+            qr_apply_one(1, sub(A, j0, b, j0, b), sub(A, j0 + b, m - j0 - b, j0, b), S,
+                         sub(A, j0, b, j0 + b, n - j0 - b), sub(A, j0 + b, m - j0 - b, j0 + b, n - j0 - b));
+    }
+    return 0;
+}
+
+/* ApplyQT / ApplyQ (QR.cs:79-109): B (m x nrhs) = Q^T B or Q B. */
+void orc_dormqr(int trans, i64 m, i64 n, i64 nrhs, const double *a, i64 rsa, i64 csa, const double *t, i64 t_rows,
+                i64 rst, i64 cst, double *b, i64 rsb, i64 csb) {
+    if (m == 0 || n == 0 || nrhs == 0) return;
+    qr_apply(trans != 0, mk((double *)a, m, n, rsa, csa), mk((double *)t, t_rows, n, rst, cst),
+             mk(b, m, nrhs, rsb, csb));
+}
+
+/* QR.Solve (QR.cs:391-415): Y = Q^T B, then R X = Y(0:n). */
+void orc_dgeqrs(i64 m, i64 n, i64 nrhs, const double *a, i64 rsa, i64 csa, const double *t, i64 t_rows, i64 rst,
+                i64 cst, const double *b, i64 rsb, i64 csb, double *x, i64 rsx, i64 csx) {
+    if (n == 0 || nrhs == 0) return;
+    double *y = (double *)malloc(sizeof(double) * m * nrhs);
+    for (i64 i = 0; i < m; i++) for (i64 j = 0; j < nrhs; j++) y[i * nrhs + j] = b[i * rsb + j * csb];
+    qr_apply(1, mk((double *)a, m, n, rsa, csa), mk((double *)t, t_rows, n, rst, cst), mk(y, m, nrhs, nrhs, 1));
+    orc_dtrsm(SD_LEFT, UL_UPPER, TR_NO, DG_NONUNIT, n, nrhs, 1.0, a, rsa, csa, y, nrhs, 1);
+    for (i64 i = 0; i < n; i++) for (i64 j = 0; j < nrhs; j++) x[i * rsx + j * csx] = y[i * nrhs + j];
+    free(y);
+}
+
+/* QR.FormQ(A, T, Q) (QR.cs:192-201): Q = I, then Q = H_0 ... H_{k-1} Q. */
+void orc_dorgqr(i64 m, i64 n, const double *a, i64 rsa, i64 csa, const double *t, i64 t_rows, i64 rst, i64 cst,
+                double *q, i64 rsq, i64 csq) {
+    for (i64 i = 0; i < m; i++) for (i64 j = 0; j < m; j++) q[i * rsq + j * csq] = i == j ? 1.0 : 0.0;
+    orc_dormqr(0, m, n, m, a, rsa, csa, t, t_rows, rst, cst, q, rsq, csq);
+}
+
+/* ------------------------------------------------------------------------ */
 /* LU with partial pivoting, DDLA/Factorizations/LU.cs                      */
 /* ------------------------------------------------------------------------ */
 

@@ -74,6 +74,11 @@ def lib():
                                  _dp, _i64, _i64, _dp, _i64, _i64, C.c_double, _dp, _i64, _i64]
         L.orc_dtrmm.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, _i64, _i64, C.c_double,
                                 _dp, _i64, _i64, _dp, _i64, _i64]
+        L.orc_dgeqrf.argtypes = [_i64, _i64, _dp, _i64, _i64, _dp, _i64, _i64, _i64]
+        L.orc_dormqr.argtypes = [C.c_int, _i64, _i64, _i64, _dp, _i64, _i64, _dp, _i64, _i64, _i64, _dp, _i64, _i64]
+        L.orc_dgeqrs.argtypes = [_i64, _i64, _i64, _dp, _i64, _i64, _dp, _i64, _i64, _i64, _dp, _i64, _i64,
+                                 _dp, _i64, _i64]
+        L.orc_dorgqr.argtypes = [_i64, _i64, _dp, _i64, _i64, _dp, _i64, _i64, _i64, _dp, _i64, _i64]
         L.orc_set_threads.argtypes = [C.c_int]
         L.orc_contract_plan.argtypes = [C.c_char_p, C.c_int, C.POINTER(_i64), C.POINTER(_i64),
                                         C.c_int, C.POINTER(_i64), C.POINTER(_i64),
@@ -145,6 +150,39 @@ def dtrmm3(side, uplo, ta, diag, alpha, A, B, beta, Cm, tb=TRANS_NO):
 def dtrmm(side, uplo, ta, diag, alpha, A, B):
     m, n = B.shape
     lib().orc_dtrmm(side, uplo, ta, diag, m, n, alpha, _ptr(A), *_st(A), _ptr(B), *_st(B))
+
+
+def qr_t_rows(m, n):
+    """Rows of DDLA's T for an m x n QR (QR.CreateT, DDLA/Factorizations/QR.cs:124-128)."""
+    return min(256, max(m, n))
+
+
+def dgeqrf(A, T):
+    """In-place QR of A; T (t_rows x n) receives the block factors."""
+    m, n = A.shape
+    rc = lib().orc_dgeqrf(m, n, _ptr(A), *_st(A), _ptr(T), T.shape[0], *_st(T))
+    if rc:
+        raise ValueError(f"orc_dgeqrf: argument {-rc}")
+
+
+def dormqr(trans, A, T, B):
+    m, n = A.shape
+    lib().orc_dormqr(trans, m, n, B.shape[1], _ptr(A), *_st(A), _ptr(T), T.shape[0], *_st(T), _ptr(B), *_st(B))
+
+
+def dgeqrs(A, T, B):
+    m, n = A.shape
+    X = np.zeros((n, B.shape[1]))
+    lib().orc_dgeqrs(m, n, B.shape[1], _ptr(A), *_st(A), _ptr(T), T.shape[0], *_st(T), _ptr(B), *_st(B),
+                     _ptr(X), *_st(X))
+    return X
+
+
+def dorgqr(A, T):
+    m, n = A.shape
+    Q = np.zeros((m, m))
+    lib().orc_dorgqr(m, n, _ptr(A), *_st(A), _ptr(T), T.shape[0], *_st(T), _ptr(Q), *_st(Q))
+    return Q
 
 
 def dtrsm(side, uplo, ta, diag, alpha, A, B):

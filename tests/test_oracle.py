@@ -331,3 +331,71 @@ def test_contract_plan_folds_to_single_gemm(orc):
     d = orc.plan_dict(orc.contract_plan("abcd,cdef->abef", A, B, Cm))
     assert len(d["m"]) == 1 and len(d["n"]) == 1 and len(d["k"]) == 1 and d["batch"] == []
     assert d["m"][0][0] == 64 and d["n"][0][0] == 64 and d["k"][0][0] == 64
+
+
+@pytest.mark.parametrize("m,n", [(TINY, TINY), (SMALL * 3 + 1, SMALL), (MEDIUM, MEDIUM), (MEDIUM * 3 + 1, MEDIUM),
+                                 (600, 300), (200, 300)])
+def test_qr_property_and_lapack(orc, m, n):
+    # TestQR.cs:58-79: Q R = A with 1e-10 in the 1-, Frobenius and inf-norms
+    r = rng(40 + m + n)
+    A0 = uniform(r, (m, n))
+    A = A0.copy()
+    T = np.zeros((orc.qr_t_rows(m, n), n))
+    orc.dgeqrf(A, T)
+    Q = orc.dorgqr(A, T)
+    R = np.triu(A)
+    for nv in norms(Q @ R - A0):
+        assert nv < 1e-10
+    assert np.max(np.abs(Q.T @ Q - np.eye(m))) < 1e-13
+    # LAPACK (scipy) uses the same sign rule (beta = -sign(alpha) |x|) and the
+    # same vectors; it leaves a column with nothing below the diagonal alone
+    # where DDLA reflects it (rho = -chi), so its last row of a square R differs
+    # in sign.
+    (raw, tau), _ = sl.qr(A0, mode="raw")
+    k = min(m, n)
+    kk = k - 1 if m <= n else k
+    assert np.max(np.abs(np.triu(A)[:kk] - np.triu(raw)[:kk])) < 1e-12 * max(1.0, np.abs(raw).max())
+    assert np.max(np.abs(np.tril(A, -1)[:, :kk] - np.tril(raw, -1)[:, :kk])) < 1e-11
+    # T's diagonal blocks: tau_ddla = 1 / tau_lapack, S(i, j) = u_i^T u_j
+    tb = T.shape[0]
+    U = np.tril(A, -1)[:, :k] + np.eye(m, k)
+    for j0 in range(0, k, tb):
+        b = min(tb, k - j0)
+        Ub = U[:, j0:j0 + b]
+        S = Ub.T @ Ub
+        np.fill_diagonal(S, np.diag(S) / 2)
+        assert np.max(np.abs(np.triu(T[:b, j0:j0 + b]) - np.triu(S))) < 1e-12 * max(1.0, np.abs(S).max())
+
+
+def test_qr_apply_and_solve(orc):
+    # TestQR.cs:30-56: solve at 1e-6 (here 1024 x 1024 with 64 right-hand sides)
+    r = rng(41)
+    m, n, nrhs = 1024, 1024, 64
+    A0 = uniform(r, (m, n))
+    X0 = uniform(r, (n, nrhs))
+    B = A0 @ X0
+    A = A0.copy()
+    T = np.zeros((orc.qr_t_rows(m, n), n))
+    orc.dgeqrf(A, T)
+    X = orc.dgeqrs(A, T, B)
+    for nv in norms(X - X0):
+        assert nv < 1e-6
+    Y = B.copy()
+    orc.dormqr(8, A, T, Y)                       # Q^T B
+    Z = Y.copy()
+    orc.dormqr(0, A, T, Z)                       # Q Q^T B = B
+    assert np.max(np.abs(Z - B)) < 1e-10 * np.abs(B).max()
+    assert np.max(np.abs(np.tril(Y[:n], -1) * 0 + Y[:n] - np.triu(A)[:n] @ X0)) < 1e-9 * np.abs(B).max()
+
+
+def test_qr_least_squares_tall(orc):
+    r = rng(42)
+    m, n = 700, 300
+    A0 = uniform(r, (m, n))
+    B = uniform(r, (m, 3))
+    A = A0.copy()
+    T = np.zeros((orc.qr_t_rows(m, n), n))
+    orc.dgeqrf(A, T)
+    X = orc.dgeqrs(A, T, B)
+    Xl = np.linalg.lstsq(A0, B, rcond=None)[0]
+    assert np.max(np.abs(X - Xl)) < 1e-10
