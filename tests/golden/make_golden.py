@@ -115,6 +115,44 @@ def main():
     out.update(ein3_l=L, ein3_r=R, ein3_c=Cm)
     np.savez_compressed(os.path.join(HERE, "ddla_golden.npz"), **out)
     print("wrote", os.path.join(HERE, "ddla_golden.npz"), len(out), "arrays")
+    next_rows()
+
+
+def next_rows():
+    """ddla_golden_next.npz: SYMM, TRMM, TRMM3, SYR2K and Householder QR
+    (unblocked n <= 256 and blocked n > 256, DDLA/Factorizations/QR.cs:139-149)."""
+    r = np.random.default_rng(SEED + 1)
+    out = {}
+    A, B, C0 = r.uniform(-1, 1, (70, 70)), r.uniform(-1, 1, (70, 50)), r.uniform(-1, 1, (70, 50))
+    Cm = C0.copy()
+    orc.dsymm(orc.LEFT, orc.LOWER, 1 / np.pi, A, B, np.e, Cm)
+    out.update(symm_a=np.tril(A), symm_b=B, symm_c0=C0, symm_c=Cm)
+    A, B = r.uniform(-1, 1, (45, 45)), r.uniform(-1, 1, (60, 45))
+    X = B.copy()
+    orc.dtrmm(orc.RIGHT, orc.UPPER, orc.TRANS_T, orc.UNIT, 1.2, A, X)
+    out.update(trmm_a=np.triu(A, 1), trmm_b=B, trmm_x=X)
+    A, Bt, C0 = r.uniform(-1, 1, (50, 50)), r.uniform(-1, 1, (40, 50)), r.uniform(-1, 1, (50, 40))
+    Cm = C0.copy()
+    orc.dtrmm3(orc.LEFT, orc.LOWER, orc.TRANS_NO, orc.NONUNIT, 1.0, A, Bt, 1.0, Cm, tb=orc.TRANS_T)
+    out.update(trmm3_a=np.tril(A), trmm3_bt=Bt, trmm3_c0=C0, trmm3_c=Cm)
+    A, B, C0 = r.uniform(-1, 1, (60, 30)), r.uniform(-1, 1, (60, 30)), r.uniform(-1, 1, (60, 60))
+    Cm = C0.copy()
+    orc.dsyr2k(orc.UPPER, 1 / np.pi, A, B, np.e, Cm)
+    out.update(syr2k_a=A, syr2k_b=B, syr2k_c0=C0, syr2k_c=np.triu(Cm))
+    for name, (m, n) in (("qr1", (130, 70)), ("qr2", (300, 280))):
+        A = r.uniform(-1, 1, (m, n))
+        F, T = A.copy(), np.zeros((orc.qr_t_rows(m, n), n))
+        orc.dgeqrf(F, T)
+        b = r.uniform(-1, 1, (m, 2))
+        x = orc.dgeqrs(F, T, b)
+        k = min(m, n)
+        Tu = np.zeros_like(T)
+        for j0 in range(0, k, T.shape[0]):
+            bb = min(T.shape[0], k - j0)
+            Tu[:bb, j0:j0 + bb] = np.triu(T[:bb, j0:j0 + bb])
+        out.update({f"{name}_a": A, f"{name}_f": F, f"{name}_t": Tu, f"{name}_b": b, f"{name}_x": x})
+    np.savez_compressed(os.path.join(HERE, "ddla_golden_next.npz"), **out)
+    print("wrote", os.path.join(HERE, "ddla_golden_next.npz"), len(out), "arrays")
 
 
 if __name__ == "__main__":

@@ -88,3 +88,42 @@ def test_einsum_golden(orc, g, i, expr):
     orc.contract(expr, 1.0, g[f"ein{i}_l"], g[f"ein{i}_r"], Cm)
     assert np.array_equal(Cm, g[f"ein{i}_c"])
     assert np.allclose(Cm, np.einsum(expr, g[f"ein{i}_l"], g[f"ein{i}_r"]), rtol=0, atol=1e-12)
+
+
+@pytest.fixture(scope="module")
+def gn():
+    return np.load(os.path.join(HERE, "golden", "ddla_golden_next.npz"))
+
+
+def test_level3_next_golden(orc, gn):
+    """SYMM / TRMM / TRMM3 / SYR2K: the stored triangles only (the other
+    triangle is NaN here, and must not be read)."""
+    nan_up = lambda x: x + np.triu(np.full(x.shape, np.nan), 1)      # noqa: E731
+    Cm = gn["symm_c0"].copy()
+    orc.dsymm(orc.LEFT, orc.LOWER, 1 / np.pi, nan_up(gn["symm_a"]), gn["symm_b"], np.e, Cm)
+    assert np.array_equal(Cm, gn["symm_c"])
+    A = gn["trmm_a"] + np.tril(np.full((45, 45), np.nan))              # strict upper stored, unit diagonal
+    X = gn["trmm_b"].copy()
+    orc.dtrmm(orc.RIGHT, orc.UPPER, orc.TRANS_T, orc.UNIT, 1.2, A, X)
+    assert np.array_equal(X, gn["trmm_x"])
+    Cm = gn["trmm3_c0"].copy()
+    orc.dtrmm3(orc.LEFT, orc.LOWER, orc.TRANS_NO, orc.NONUNIT, 1.0, nan_up(gn["trmm3_a"]), gn["trmm3_bt"], 1.0, Cm,
+               tb=orc.TRANS_T)
+    assert np.array_equal(Cm, gn["trmm3_c"])
+    Cm = gn["syr2k_c0"].copy()
+    orc.dsyr2k(orc.UPPER, 1 / np.pi, gn["syr2k_a"], gn["syr2k_b"], np.e, Cm)
+    assert np.array_equal(np.triu(Cm), gn["syr2k_c"])
+
+
+@pytest.mark.parametrize("name", ["qr1", "qr2"])
+def test_qr_golden(orc, gn, name):
+    A = gn[f"{name}_a"]
+    m, n = A.shape
+    F, T = A.copy(), np.zeros((orc.qr_t_rows(m, n), n))
+    orc.dgeqrf(F, T)
+    assert np.array_equal(F, gn[f"{name}_f"])
+    k = min(m, n)
+    for j0 in range(0, k, T.shape[0]):
+        b = min(T.shape[0], k - j0)
+        assert np.array_equal(np.triu(T[:b, j0:j0 + b]), gn[f"{name}_t"][:b, j0:j0 + b])
+    assert np.array_equal(orc.dgeqrs(F, T, gn[f"{name}_b"]), gn[f"{name}_x"])

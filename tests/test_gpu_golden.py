@@ -94,3 +94,43 @@ def test_einsum_golden(ddla, g, i, expr):
     Cm = np.zeros_like(g[f"ein{i}_c"])
     einsum.Contract(Cm, expr, 1.0, g[f"ein{i}_l"], g[f"ein{i}_r"])
     assert rel_max(Cm, g[f"ein{i}_c"]) <= 1e-13
+
+
+@pytest.fixture(scope="module")
+def gn():
+    return np.load(os.path.join(HERE, "golden", "ddla_golden_next.npz"))
+
+
+def test_level3_next_golden(ddla, gn):
+    nan_up = lambda x: x + np.triu(np.full(x.shape, np.nan), 1)      # noqa: E731
+    Cm = gn["symm_c0"].copy()
+    ddla.BlasProvider.SyMM(ddla.LEFT, ddla.LOWER, 1 / np.pi, nan_up(gn["symm_a"]), gn["symm_b"], np.e, Cm)
+    assert rel_max(Cm, gn["symm_c"]) <= 1e-13
+    A = gn["trmm_a"] + np.tril(np.full((45, 45), np.nan))
+    X = gn["trmm_b"].copy()
+    ddla.BlasProvider.TrMM(ddla.RIGHT, ddla.UPPER, ddla.TRANSPOSE, ddla.UNIT, 1.2, A, X)
+    assert rel_max(X, gn["trmm_x"]) <= 1e-13
+    Cm = gn["trmm3_c0"].copy()
+    ddla.BlasProvider.TrMM3(ddla.LEFT, ddla.LOWER, ddla.NO_TRANSPOSE, ddla.NONUNIT, ddla.TRANSPOSE, 1.0,
+                            nan_up(gn["trmm3_a"]), gn["trmm3_bt"], 1.0, Cm)
+    assert rel_max(Cm, gn["trmm3_c"]) <= 1e-13
+    Cm = gn["syr2k_c0"].copy()
+    ddla.BlasProvider.SyR2k(ddla.UPPER, 1 / np.pi, gn["syr2k_a"], gn["syr2k_b"], np.e, Cm)
+    assert rel_max(np.triu(Cm), gn["syr2k_c"]) <= 1e-13
+
+
+@pytest.mark.parametrize("name", ["qr1", "qr2"])
+def test_qr_golden(ddla, gn, name):
+    A = gn[f"{name}_a"]
+    m, n = A.shape
+    F = A.copy()
+    T = ddla.QR.QRDecompose(F)
+    assert rel_max(np.triu(F), np.triu(gn[f"{name}_f"])) <= 1e-12
+    assert rel_max(np.tril(F, -1), np.tril(gn[f"{name}_f"], -1)) <= 1e-11
+    k = min(m, n)
+    for j0 in range(0, k, T.shape[0]):
+        b = min(T.shape[0], k - j0)
+        assert rel_max(np.triu(T[:b, j0:j0 + b]), gn[f"{name}_t"][:b, j0:j0 + b]) <= 1e-11
+    X = np.zeros((n, 2))
+    ddla.QR.Solve(F, T, gn[f"{name}_b"], X)
+    assert rel_max(X, gn[f"{name}_x"]) <= 1e-10
