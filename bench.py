@@ -284,6 +284,25 @@ def secondary(args):
             ref, scale = ref_fn()
             got = torch.tril(Cm) if wl == "syr2k" else Cm
             return float(((got - ref).abs() / scale).max())
+    elif wl == "einsum-chain":
+        n = args.n if args.n != N_DEFAULT else 4096
+        expr = "ab,bc,cd,de->ae"
+        ops = [U(n, n) for _ in range(4)]
+        Cm = torch.zeros(n, n, dtype=torch.float64, device="cuda")
+        flops = 3 * 2.0 * n ** 3
+        bytes_alg = 8.0 * 5 * n * n
+        flush = L2Flush(torch, stream)
+        desc = f"einsum '{expr}' (DDLA's pairwise path, intermediates on the device), all modes {n}, {pname}"
+
+        def step():
+            es.dev_einsum(h, expr, ops, Cm, precision=prec)
+
+        def check_err():
+            step()
+            h.sync()
+            ref = ops[0] @ ops[1] @ ops[2] @ ops[3]
+            sc_ = ops[0].abs() @ ops[1].abs() @ ops[2].abs() @ ops[3].abs()
+            return float(((Cm - ref).abs() / sc_).max())
     elif wl == "qr":
         n = args.n if args.n != N_DEFAULT else 8192
         A0 = U(n, n)
@@ -479,7 +498,7 @@ def main():
     ap.add_argument("--tune", action="append", default=[], metavar="KEY=VALUE",
                     help="library tuning key (ddla_tune_set) applied before the run; repeatable")
     ap.add_argument("--workload", default="lu", choices=["lu", "gemm", "chol", "batched", "einsum-a", "einsum-b",
-                                                         "symm", "trmm", "syr2k", "qr"])
+                                                         "symm", "trmm", "syr2k", "qr", "einsum-chain"])
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-n", type=int, default=4096)
     ap.add_argument("--no-cpu", action="store_true")

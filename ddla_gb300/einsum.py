@@ -115,3 +115,89 @@ def Contract(*args, precision=0):
                                    C.c_void_p(right.ctypes.data), _span(right), C.c_void_p(result.ctypes.data),
                                    _span(result), precision), "Contract")
     return result
+
+
+def _declare_multi():
+    L = _declare()
+    if not getattr(L, "_einsum_declared", False):
+        PP = C.POINTER(C.POINTER(_i64))
+        L.ddla_einsum_path.argtypes = [C.c_char_p, C.c_int32, C.POINTER(C.c_int32), PP, C.c_char_p, C.c_int32]
+        L.ddla_einsum_path.restype = C.c_int
+        L.ddla_einsum.argtypes = [C.c_char_p, C.c_int32, C.POINTER(C.c_int32), PP, PP, C.POINTER(C.c_void_p),
+                                  C.POINTER(_i64), C.c_double, C.c_double, C.c_int32, C.POINTER(_i64),
+                                  C.POINTER(_i64), C.c_void_p, _i64, C.c_int32]
+        L.ddla_einsum.restype = C.c_int
+        L.ddla_dev_einsum.argtypes = [C.c_void_p, C.c_char_p, C.c_int32, C.POINTER(C.c_int32), PP, PP,
+                                      C.POINTER(C.c_void_p), C.c_double, C.c_double, C.c_int32, C.POINTER(_i64),
+                                      C.POINTER(_i64), C.c_void_p, C.c_int32]
+        L.ddla_dev_einsum.restype = C.c_int
+        L._einsum_declared = True
+    return L
+
+
+def _tables(shapes, strides=None):
+    n = len(shapes)
+    ranks = (C.c_int32 * n)(*[len(s) for s in shapes])
+    keep = [_arr(list(s)) for s in shapes]
+    lens = (C.POINTER(_i64) * n)(*[C.cast(k, C.POINTER(_i64)) for k in keep])
+    sk, st = None, None
+    if strides is not None:
+        sk = [_arr(list(s)) for s in strides]
+        st = (C.POINTER(_i64) * n)(*[C.cast(k, C.POINTER(_i64)) for k in sk])
+    return ranks, lens, st, (keep, sk)
+
+
+def _target_shape(expr, shapes):
+    lhs, tgt = expr.replace(" ", "").split("->")
+    dims = {}
+    for name, shp in zip(lhs.split(","), shapes):
+        for s, t in zip(name, shp):
+            dims[s] = t
+    return [dims[s] for s in tgt]
+
+
+def einsum_path(expr, *operands):
+    """DDLA's pairwise contraction order for `expr` (EinsumTree/EinsumState.cs:
+    45-419) as a list of "ab,bc->ac" steps; operands are arrays or shapes."""
+    shapes = [tuple(o.shape) if hasattr(o, "shape") else tuple(o) for o in operands]
+    ranks, lens, _, keep = _tables(shapes)
+    buf = C.create_string_buffer(4096)
+    check(_declare_multi().ddla_einsum_path(expr.encode(), len(shapes), ranks, lens, buf, 4096), "einsum_path")
+    s = buf.value.decode()
+    return s.split(";") if s else []
+
+
+def Einsum(expr, *operands, alpha=1.0, out=None, beta=0.0, precision=0):
+    """MArray.Einsum (DDLA/Einsum/MArray.Contract.cs:409-427) on host arrays:
+    out = beta*out + alpha*einsum(expr, operands).  Without `out` a new
+    C-contiguous result is returned (DDLA's Einsum(expr, alpha, inputs));
+    beta = 1 with `out` is DDLA's Einsum(result, expr, alpha, inputs)."""
+    for i, x in enumerate(operands):
+        _check_base(x, f"operand {i}")
+    shapes = [x.shape for x in operands]
+    if out is None:
+        out = np.zeros(_target_shape(expr, shapes))
+        beta = 0.0
+    _check_base(out, "out")
+    ranks, lens, strides, keep = _tables(shapes, [[s // 8 for s in x.strides] for x in operands])
+    n = len(operands)
+    ptrs = (C.c_void_p * n)(*[x.ctypes.data for x in operands])
+    counts = (_i64 * n)(*[_span(x) for x in operands])
+    lo, so = _arr(list(out.shape)), _arr([s // 8 for s in out.strides])
+    check(_declare_multi().ddla_einsum(expr.encode(), n, ranks, lens, strides, ptrs, counts, float(alpha),
+                                       float(beta), out.ndim, lo, so, C.c_void_p(out.ctypes.data), _span(out),
+                                       precision), "Einsum")
+    return out
+
+
+def dev_einsum(handle, expr, operands, out, alpha=1.0, beta=0.0, precision=0):
+    """The same on torch CUDA tensors (intermediates stay on the device)."""
+    shapes = [tuple(x.shape) for x in operands]
+    ranks, lens, strides, keep = _tables(shapes, [list(x.stride()) for x in operands])
+    n = len(operands)
+    ptrs = (C.c_void_p * n)(*[x.data_ptr() for x in operands])
+    lo, so = _arr(list(out.shape)), _arr(list(out.stride()))
+    check(_declare_multi().ddla_dev_einsum(handle.h, expr.encode(), n, ranks, lens, strides, ptrs, float(alpha),
+                                           float(beta), out.dim(), lo, so, C.c_void_p(out.data_ptr()), precision),
+          "dev_einsum")
+    return out

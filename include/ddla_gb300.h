@@ -432,6 +432,31 @@ int ddla_dev_contract(ddla_handle h, const ddla_contract_desc *d, double alpha, 
 int ddla_contract(const ddla_contract_desc *d, double alpha, const double *a, int64_t na, const double *b,
                   int64_t nb, double *c, int64_t nc, int32_t precision);
 
+/* ------------------------------------------------ multi-operand einsum */
+
+/* out = beta*out + alpha*einsum(expr, inputs) for any number of inputs
+ * ("ab,bc,cd->ad").  MArray.Einsum (DDLA/Einsum/MArray.Contract.cs:409-427):
+ * beta = 1 is Einsum(result, expr, alpha, inputs), beta = 0 the returning
+ * form.  The pairwise order is DDLA's greedy path
+ * (DDLA/Einsum/EinsumTree/EinsumState.cs:45-419); intermediates stay on the
+ * device.  One input is contracted with the scalar 1 (transpose, diagonal,
+ * sums), where DDLA returns the input unchanged (EinsumNodes.cs:97-100).
+ * Tensor i has ranks[i] modes with lengths lens[i][.] and element strides
+ * strides[i][.]; precision DDLA_PREC_FP64 or DDLA_PREC_OZAKI. */
+int ddla_dev_einsum(ddla_handle h, const char *expr, int32_t n_inputs, const int32_t *ranks,
+                    const int64_t *const *lens, const int64_t *const *strides, const double *const *inputs,
+                    double alpha, double beta, int32_t rank_out, const int64_t *len_out, const int64_t *str_out,
+                    double *out, int32_t precision);
+/* Host arrays: counts[i] / out_count are the element spans from index 0. */
+int ddla_einsum(const char *expr, int32_t n_inputs, const int32_t *ranks, const int64_t *const *lens,
+                const int64_t *const *strides, const double *const *inputs, const int64_t *counts, double alpha,
+                double beta, int32_t rank_out, const int64_t *len_out, const int64_t *str_out, double *out,
+                int64_t out_count, int32_t precision);
+/* The pairwise path, "ab,bc->ac;ac,cd->ad" (NUL-terminated, at most buflen
+ * bytes). */
+int ddla_einsum_path(const char *expr, int32_t n_inputs, const int32_t *ranks, const int64_t *const *lens, char *buf,
+                     int32_t buflen);
+
 #ifdef __cplusplus
 }
 #endif

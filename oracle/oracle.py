@@ -255,3 +255,72 @@ def plan_dict(d):
         return [(arr[i].len, arr[i].sa, arr[i].sb, arr[i].sc) for i in range(cnt)]
     return {"batch": modes(d.batch, d.nbatch), "m": modes(d.m, d.nm), "n": modes(d.n, d.nn),
             "k": modes(d.k, d.nk), "swapped": d.swapped}
+
+
+def einsum_path(expr, shapes):
+    """DDLA's greedy pairwise order for a multi-operand einsum, restated from
+    EinsumState (DDLA/Einsum/EinsumTree/EinsumState.cs:45-419): over all pairs
+    (l < r) the smallest cost |result| - (|l| + |r|) wins, ties to the smaller
+    l then r (OrderBy(Cost).ThenBy(Left + const), :362-368, stable); inputs
+    count with size 0 (their size product starts at 0, :122-131); the result
+    keeps the symbols of l and r that another tensor or the target uses, in
+    first-appearance order, replaces l, and r is dropped (:162-260).  The last
+    step writes the target (EinsumNodes.cs:82-93)."""
+    lhs, target = expr.replace(" ", "").split("->")
+    names = lhs.split(",")
+    order, dims = [], {}
+    for nm, shp in zip(names, shapes):
+        for s, t in zip(nm, shp):
+            if s not in dims:
+                order.append(s)
+                dims[s] = t
+    sizes = [0.0] * len(names)
+    steps = []
+    while len(names) > 1:
+        best = None
+        for l in range(len(names) - 1):
+            for r in range(l + 1, len(names)):
+                others = set(target)
+                for j, nm in enumerate(names):
+                    if j not in (l, r):
+                        others |= set(nm)
+                out = "".join(s for s in order if (s in names[l] or s in names[r]) and s in others)
+                rs = 1.0
+                for s in out:
+                    rs *= dims[s]
+                cost = rs - (sizes[l] + sizes[r])
+                if best is None or cost < best[0]:
+                    best = (cost, l, r, out, rs)
+        _, l, r, out, rs = best
+        steps.append((names[l], names[r], out))
+        names[l], sizes[l] = out, rs
+        del names[r], sizes[r]
+    if steps:
+        steps[-1] = (steps[-1][0], steps[-1][1], target)
+    return [f"{a},{b}->{c}" for a, b, c in steps]
+
+
+def einsum(expr, operands):
+    """Einsum with DDLA's path, every pairwise step through the oracle's
+    MArray.Contract restatement (intermediates row-major over their symbols)."""
+    lhs, target = expr.replace(" ", "").split("->")
+    names = lhs.split(",")
+    dims = {}
+    for nm, x in zip(names, operands):
+        for s, t in zip(nm, x.shape):
+            dims[s] = t
+    tensors = dict()
+    cur = list(zip(names, operands))
+    for step in einsum_path(expr, [x.shape for x in operands]):
+        a, rest = step.split(",")
+        b, out = rest.split("->")
+        ia = next(i for i, (nm, _) in enumerate(cur) if nm == a)
+        ib = next(i for i, (nm, _) in enumerate(cur) if nm == b and i != ia)
+        A, B = cur[ia][1], cur[ib][1]
+        R = np.zeros([dims[s] for s in out])
+        contract(step, 1.0, np.ascontiguousarray(A), np.ascontiguousarray(B), R)
+        cur[ia] = (out, R)
+        del cur[ib]
+    if len(operands) == 1:
+        raise ValueError("oracle einsum: one operand (DDLA returns it unchanged)")
+    return cur[0][1]
