@@ -284,6 +284,28 @@ def secondary(args):
             ref, scale = ref_fn()
             got = torch.tril(Cm) if wl == "syr2k" else Cm
             return float(((got - ref).abs() / scale).max())
+    elif wl == "tridiag":
+        n = args.n if args.n != N_DEFAULT else 4096
+        G = U(n, n)
+        S = G + G.T
+        del G
+        Aw = torch.empty_like(S)
+        Tw = torch.zeros(64, n, dtype=torch.float64, device="cuda")
+        dw = torch.zeros(n, dtype=torch.float64, device="cuda")
+        ew = torch.zeros(n - 1, dtype=torch.float64, device="cuda")
+        tprec = D.PREC_OZAKI if prec == D.PREC_OZAKI else 0
+        flops = 8.0 * n ** 3 / 3.0   # reduction 4/3 n^3 + forming Q 4/3 n^3
+        desc = f"symmetric tridiagonal reduction + Q (T blocks of 64), {n}x{n} FP64 U[-1,1], {pname} Q formation"
+
+        def step():
+            Aw.copy_(S)
+            h.sytrd(Aw, Tw, dw, ew, precision=tprec)
+
+        def check_err():
+            step()
+            h.sync()
+            Tr = torch.diag(dw) + torch.diag(ew, -1) + torch.diag(ew, 1)
+            return float((Aw.T @ S @ Aw - Tr).abs().max() / S.abs().max())
     elif wl == "einsum-chain":
         n = args.n if args.n != N_DEFAULT else 4096
         expr = "ab,bc,cd,de->ae"
@@ -446,13 +468,15 @@ def secondary(args):
     ms = statistics.median(times)
     value = flops / (ms * 1e-3) / 1e9
     classes = None
-    if wl == "qr":
+    if wl in ("qr", "tridiag"):
         # one more step with per-class CUDA-event brackets (outside the timed steps)
         L.ddla_timing_enable(1)
         step()
         torch.cuda.synchronize()
         classes = {}
-        for cls, name in {1: "qr_panel", 7: "qr_t_factor", 0: "block_reflector_gemm", 2: "trsm"}.items():
+        names = {1: "qr_panel", 7: "qr_t_factor", 0: "block_reflector_gemm", 2: "trsm"} if wl == "qr" else \
+            {1: "reduction", 0: "form_q"}
+        for cls, name in names.items():
             t_ms, cnt, fl, by = C.c_double(), C.c_int64(), C.c_double(), C.c_double()
             L.ddla_timing_read(cls, C.byref(t_ms), C.byref(cnt), C.byref(fl), C.byref(by))
             classes[name] = {"ms": t_ms.value, "launches": cnt.value,
@@ -498,7 +522,8 @@ def main():
     ap.add_argument("--tune", action="append", default=[], metavar="KEY=VALUE",
                     help="library tuning key (ddla_tune_set) applied before the run; repeatable")
     ap.add_argument("--workload", default="lu", choices=["lu", "gemm", "chol", "batched", "einsum-a", "einsum-b",
-                                                         "symm", "trmm", "syr2k", "qr", "einsum-chain"])
+                                                         "symm", "trmm", "syr2k", "qr", "einsum-chain",
+                                                         "tridiag"])
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-n", type=int, default=4096)
     ap.add_argument("--no-cpu", action="store_true")

@@ -796,6 +796,46 @@ int ddla_dorgqr(ddla_dim_t m, ddla_dim_t n, const double *a, ddla_inc_t rsa, ddl
     return stage_out(h, sq, q, m, m, rsq, csq);
 }
 
+// ------------------------------------------------------------------ tridiagonal reduction
+int ddla_dev_dsytrd(ddla_handle h, ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t csa, double *t,
+                    ddla_dim_t t_rows, ddla_inc_t rst, ddla_inc_t cst, double *d, double *e, const ddla_opts *opts) {
+    CHECK_ARG(h != nullptr, 1);
+    CHECK_ARG(n >= 0, 2);
+    CHECK_ARG(t_rows >= 1, 7);
+    CHECK_ARG(d != nullptr || n == 0, 10);
+    CHECK_ARG(e != nullptr || n <= 1, 11);
+    CHECK_ARG(!opts || opts->precision == 0 || opts->precision == DDLA_PREC_FP64 ||
+                  opts->precision == DDLA_PREC_OZAKI, 12);
+    if (n == 0) return 0;
+    return sytrd(h, n, View<double>{a, n, n, rsa, csa}, View<double>{t, t_rows, n, rst, cst}, t_rows, d, e,
+                 fprec(opts));
+}
+
+int ddla_dsytrd(ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t csa, double *t, ddla_dim_t t_rows, ddla_inc_t rst,
+                ddla_inc_t cst, double *d, double *e, const ddla_opts *opts) {
+    CHECK_ARG(n >= 0, 1);
+    CHECK_ARG(t_rows >= 1, 6);
+    CHECK_ARG(d != nullptr || n == 0, 9);
+    CHECK_ARG(e != nullptr || n <= 1, 10);
+    CHECK_ARG(!opts || opts->precision == 0 || opts->precision == DDLA_PREC_FP64 ||
+                  opts->precision == DDLA_PREC_OZAKI, 11);
+    if (n == 0) return 0;
+    GET_HANDLE(h);
+    Staged sa, st;
+    DDLA_TRY(stage_in(h, WS_A, a, n, n, rsa, csa, true, &sa));
+    DDLA_TRY(stage_in(h, WS_C, t, t_rows, n, rst, cst, true, &st));
+    void *de;
+    DDLA_TRY(workspace(h, WS_PIV, sizeof(double) * (size_t)(2 * n), &de));
+    double *dd = (double *)de, *ed = dd + n;
+    DDLA_TRY(sytrd(h, n, sa.view, st.view, t_rows, dd, ed, fprec(opts)));
+    DDLA_TRY(stage_out(h, sa, a, n, n, rsa, csa));
+    DDLA_TRY(stage_out(h, st, t, t_rows, n, rst, cst));
+    DDLA_CUDA(cudaMemcpyAsync(d, dd, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, h->stream));
+    if (n > 1) DDLA_CUDA(cudaMemcpyAsync(e, ed, sizeof(double) * (size_t)(n - 1), cudaMemcpyDeviceToHost, h->stream));
+    DDLA_CUDA(cudaStreamSynchronize(h->stream));
+    return 0;
+}
+
 // ------------------------------------------------------------------ factorizations, device
 int ddla_dev_dgetrf(ddla_handle h, ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t csa, int32_t *piv,
                     const ddla_opts *opts) {

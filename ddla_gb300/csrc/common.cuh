@@ -110,10 +110,12 @@ namespace ddla {
 //   WS_QR      QR: tau, a panel's block factor, the block-reflector scratch
 //   WS_SPLIT   partial products of split-k FP64 GEMMs
 //   WS_QRU     QR: explicit copy of a block's Householder vectors
+//   WS_TRD     tridiagonal reduction: vectors and partial sums
+//   WS_TRDQ    tridiagonal reduction: Q of the trailing block before its copy
 enum WsSlot {
     WS_A = 0, WS_B = 1, WS_C = 2, WS_TMP = 3, WS_PIV = 4, WS_F32 = 5, WS_X = 6, WS_MISC = 7,
     WS_TRI = 8, WS_Y = 9, WS_PERM = 10, WS_TC = 11, WS_TC2 = 12, WS_INV = 13, WS_PINV = 14, WS_QR = 15,
-    WS_SPLIT = 16, WS_QRU = 17
+    WS_SPLIT = 16, WS_QRU = 17, WS_TRD = 18, WS_TRDQ = 19
 };
 
 // Order of the diagonal blocks that the triangular solves invert.
@@ -204,7 +206,12 @@ int ormqr(ddla_handle h, bool trans, i64 m, i64 n, View<const double> A, View<co
           View<double> B, int prec = DDLA_PREC_FP64);
 int geqrs(ddla_handle h, i64 m, i64 n, View<const double> A, View<const double> T, i64 tb, View<const double> B,
           View<double> Y, View<double> X);
-int orgqr(ddla_handle h, i64 m, i64 n, View<const double> A, View<const double> T, i64 tb, View<double> Q);
+int orgqr(ddla_handle h, i64 m, i64 n, View<const double> A, View<const double> T, i64 tb, View<double> Q,
+          int prec = DDLA_PREC_FP64);
+// Tridiagonaling.Tridiag on device data (tridiag.cu): A (lower triangle read)
+// becomes Q, d (n) and e (n - 1) the tridiagonal, T (tb rows) the factors.
+int sytrd(ddla_handle h, i64 n, View<double> A, View<double> T, i64 tb, double *d, double *e,
+          int prec = DDLA_PREC_FP64);
 
 // Triangular-solve building blocks (trsm.cu): inverses of the 64 x 64
 // diagonal blocks, and the chained whole-system solve for <= 16 columns.

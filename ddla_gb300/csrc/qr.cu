@@ -437,12 +437,12 @@ int ormqr(ddla_handle h, bool trans, i64 m, i64 n, View<const double> A, View<co
 }
 
 // Q (m x m) = H_0 ... H_{k-1}: Q = I, then Q = Q I.
-int orgqr(ddla_handle h, i64 m, i64 n, View<const double> A, View<const double> T, i64 tb, View<double> Q) {
+int orgqr(ddla_handle h, i64 m, i64 n, View<const double> A, View<const double> T, i64 tb, View<double> Q, int prec) {
     if (m == 0) return 0;
     i64 blocks = (m * m + 255) / 256;
     k_eye<<<(unsigned)(blocks < 4096 ? blocks : 4096), 256, 0, h->stream>>>(Q.p, m, Q.rs, Q.cs);
     DDLA_LAUNCHED();
-    return ormqr(h, false, m, n, A, T, tb, Q, DDLA_PREC_FP64);
+    return ormqr(h, false, m, n, A, T, tb, Q, prec);
 }
 
 // Least squares X (n x nrhs) = argmin |A X - B| for m >= n; Y (m x nrhs)

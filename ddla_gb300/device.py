@@ -101,6 +101,13 @@ class Handle:
         check(lib().ddla_dev_dorgqr(self.h, m, n, _p(A), *_st(A), _p(T), T.shape[0], *_st(T), _p(Q), *_st(Q)),
               "dev_dorgqr")
 
+    def sytrd(self, A, T, d, e, precision=0):
+        n = A.shape[0]
+        o = Opts()
+        o.precision = precision
+        check(lib().ddla_dev_dsytrd(self.h, n, _p(A), *_st(A), _p(T), T.shape[0], *_st(T), _p(d),
+                                    _p(e) if n > 1 else None, C.byref(o)), "dev_dsytrd")
+
     def getrf(self, A, piv, nb=0, precision=0):
         o = Opts()
         o.nb, o.precision = nb, precision

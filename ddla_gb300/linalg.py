@@ -9,6 +9,7 @@ tests read like DDLA's own tests:
   Cholesky                                  DDLA/Factorizations/Cholesky.cs:10-88
   LDLT                                      DDLA/Factorizations/LDLT.cs:9-137
   QR                                        DDLA/Factorizations/QR.cs:14-534
+  Tridiagonaling                            DDLA/Transformations/Tridiagonaling.cs:10-232
 
 Matrices are float64 numpy arrays; any 2-D view works (its element strides
 are DDLA's RowStride / ColStride), and in-place operations write through the
@@ -22,7 +23,7 @@ from . import _lib
 from ._lib import (LEFT, LOWER, NO_TRANSPOSE, NONUNIT, RIGHT, TRANSPOSE, UNIT, UPPER, LinalgError, Opts,
                    SolveReport, check, lib)
 
-__all__ = ["BlasProvider", "LU", "Cholesky", "LDLT", "QR", "solve_mixed", "LinalgError"]
+__all__ = ["BlasProvider", "LU", "Cholesky", "LDLT", "QR", "Tridiagonaling", "solve_mixed", "LinalgError"]
 
 
 def _view(x, name):
@@ -527,6 +528,33 @@ class QR:
             raise ValueError("The dimension of Q must be equal to the number of rows in A.")
         check(lib().ddla_dorgqr(A.shape[0], A.shape[1], _p(A), *_st(A), _p(T), T.shape[0], *_st(T), _p(Q), *_st(Q)),
               "FormQ")
+
+
+class Tridiagonaling:
+    """Tridiagonaling.Tridiag -- DDLA/Transformations/Tridiagonaling.cs:10-232."""
+    BlockSize = 64   # Tridiagonaling.cs:12
+
+    @staticmethod
+    def CreateT(A):
+        n = A.shape[0]
+        return np.zeros((min(Tridiagonaling.BlockSize, n), n))
+
+    @staticmethod
+    def Tridiag(A, T=None, d=None, e=None, precision=0):
+        """Reduces the symmetric A (lower triangle read) in place: A <- Q with
+        Q^T A Q = tridiag(d, e).  Returns (T, d, e)."""
+        A = _view(A, "A")
+        n = A.shape[0]
+        if A.shape[1] != n:
+            raise ValueError("A must be square")
+        T = Tridiagonaling.CreateT(A) if T is None else _view(T, "T")
+        d = np.zeros(n) if d is None else d
+        e = np.zeros(max(n - 1, 0)) if e is None else e
+        if T.shape[1] != n or d.shape != (n,) or e.shape != (max(n - 1, 0),):
+            raise ValueError("T, d or e has the wrong shape")
+        check(lib().ddla_dsytrd(n, _p(A), *_st(A), _p(T), T.shape[0], *_st(T), _p(d), _p(e) if n > 1 else None,
+                                C.byref(_opts(0, precision))), "Tridiag")
+        return T, d, e
 
 
 def solve_mixed(A, B, spd=False, uplo=LOWER, precision=_lib.PREC_FP32, x_ref=None, tol=0.0, max_iter=0, nb=0):

@@ -233,6 +233,19 @@ int ddla_dorgqr(ddla_dim_t m, ddla_dim_t n, const double *a, ddla_inc_t rsa, ddl
                 const double *t, ddla_dim_t t_rows, ddla_inc_t rst, ddla_inc_t cst,
                 double *q, ddla_inc_t rsq, ddla_inc_t csq);
 
+/* ------------------------------------------------ tridiagonal reduction (host) */
+
+/* Householder reduction of the symmetric n x n A (its lower triangle is read)
+ * to tridiagonal form: on return A holds Q with Q^T A Q = tridiag(d, e),
+ * d (n) the diagonal, e (n - 1) the subdiagonal, T (t_rows x n) the block
+ * factors of the reflectors.  Tridiagonaling.Tridiag(A, T, d, e),
+ * DDLA/Transformations/Tridiagonaling.cs:33-56 (Step :72-112, FormQ
+ * :122-203); DDLA sizes T with CreateT (:15-19): t_rows = min(64, n).
+ * opts (may be NULL): precision DDLA_PREC_OZAKI forms Q with split-precision
+ * block-reflector products. */
+int ddla_dsytrd(ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t csa, double *t, ddla_dim_t t_rows,
+                ddla_inc_t rst, ddla_inc_t cst, double *d, double *e, const ddla_opts *opts);
+
 /* ------------------------------------------------ factorizations (host) */
 
 /* In-place LU with partial pivoting; piv[i] is RELATIVE (row i swapped with
@@ -312,6 +325,8 @@ int ddla_dev_dtrmm3(ddla_handle h, int32_t sidea, int32_t uploa, int32_t transa,
                     ddla_dim_t m, ddla_dim_t n, double alpha, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
                     const double *b, ddla_inc_t rsb, ddla_inc_t csb,
                     double beta, double *c, ddla_inc_t rsc, ddla_inc_t csc);
+int ddla_dev_dsytrd(ddla_handle h, ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t csa, double *t,
+                    ddla_dim_t t_rows, ddla_inc_t rst, ddla_inc_t cst, double *d, double *e, const ddla_opts *opts);
 int ddla_dev_dgeqrf(ddla_handle h, ddla_dim_t m, ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t csa,
                     double *t, ddla_dim_t t_rows, ddla_inc_t rst, ddla_inc_t cst, const ddla_opts *opts);
 int ddla_dev_dormqr(ddla_handle h, int32_t trans, ddla_dim_t m, ddla_dim_t n, ddla_dim_t nrhs, const double *a,

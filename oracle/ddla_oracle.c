@@ -621,6 +621,95 @@ void orc_dorgqr(i64 m, i64 n, const double *a, i64 rsa, i64 csa, const double *t
 }
 
 /* ------------------------------------------------------------------------ */
+/* Tridiagonal reduction, DDLA/Transformations/Tridiagonaling.cs             */
+/* ------------------------------------------------------------------------ */
+
+/* BuildHH, Tridiagonaling.cs:205-230: x(0) <- 1, x(1:) <- x(1:)/(chi - sigma)
+ * with sigma = sign(chi) |x|, tau = (1 + |u(1:)|^2) / 2; a zero tail gives
+ * sigma = -chi, tau = 1/2. */
+static void trd_build(double *x, i64 n, i64 inc, double *sigma, double *tau) {
+    double chi = x[0];
+    double len = nrm2(x + inc, n - 1, inc);
+    if (len == 0.0) { *sigma = -chi; x[0] = 1.0; *tau = 0.5; return; }
+    double lenx = hypot(chi, len);
+    *sigma = copysign(lenx, chi);
+    double inv = 1.0 / (chi - *sigma);
+    x[0] = 1.0;
+    for (i64 i = 1; i < n; i++) x[i * inc] *= inv;
+    len *= inv;
+    *tau = (1.0 + len * len) / 2.0;
+}
+
+/* Tridiag(A, T, d, e), Tridiagonaling.cs:33-56 with Step (:72-112) and FormQ
+ * (:122-203): one Householder reflector per column from the lower triangle
+ * (SyMV, then the symmetric rank-2 update of the trailing matrix), T holding
+ * the block factors per block of t_rows columns; A is then overwritten by Q
+ * (Q^T A Q = tridiag(d, e)).  FormQ shifts the vectors one column right and
+ * accumulates Q' = H_0 ... H_{n-2} on the trailing (n-1) x (n-1) identity;
+ * here that product is formed with the blocked ApplyQlnfc of the QR. */
+int orc_dsytrd(i64 n, double *a, i64 rsa, i64 csa, double *t, i64 t_rows, i64 rst, i64 cst, double *d, double *e) {
+    mat A = mk(a, n, n, rsa, csa), T = mk(t, t_rows, n, rst, cst);
+    if (n == 0) return 0;
+    double *p = (double *)malloc(sizeof(double) * (size_t)n);
+    for (i64 index = 0; index < n; index += t_rows) {
+        i64 block = n - index < t_rows ? n - index : t_rows;
+        for (i64 il = 0; il < block; il++) {
+            i64 i = index + il;
+            d[i] = *AT(A, i, i);
+            if (i >= n - 1) continue;
+            i64 m = n - i - 1;
+            double *x = AT(A, i + 1, i);
+            double sigma, tau;
+            trd_build(x, m, A.rs, &sigma, &tau);
+            *AT(T, il, i) = tau;
+            /* p = A22 x (lower storage), Managed SyMV */
+            for (i64 r = 0; r < m; r++) p[r] = 0.0;
+            for (i64 r = 0; r < m; r++) {
+                for (i64 c = 0; c <= r; c++) {
+                    double v = *AT(A, i + 1 + r, i + 1 + c);
+                    p[r] = fma(v, x[c * A.rs], p[r]);
+                    if (c != r) p[c] = fma(v, x[r * A.rs], p[c]);
+                }
+            }
+            double dot = 0.0;
+            for (i64 r = 0; r < m; r++) dot = fma(x[r * A.rs], p[r], dot);
+            double beta = dot / (2.0 * tau);
+            double s = 1.0 / tau;
+            for (i64 r = 0; r < m; r++) p[r] = (p[r] - beta * x[r * A.rs]) * s;
+            /* A22 -= x p^T + p x^T on the lower triangle (Rank2, alpha = -1) */
+            for (i64 r = 0; r < m; r++)
+                for (i64 c = 0; c <= r; c++) {
+                    double *v = AT(A, i + 1 + r, i + 1 + c);
+                    *v = *v - (x[r * A.rs] * p[c] + p[r] * x[c * A.rs]);
+                }
+            /* t01 = A20^T x over this block's earlier columns */
+            for (i64 j = 0; j < il; j++) {
+                double acc = 0.0;
+                for (i64 r = 0; r < m; r++) acc = fma(*AT(A, i + 1 + r, index + j), x[r * A.rs], acc);
+                *AT(T, j, i) = acc;
+            }
+            x[0] = sigma;
+            e[i] = sigma;
+        }
+    }
+    free(p);
+    /* FormQ */
+    for (i64 j = n - 2; j > 0; j--)
+        for (i64 r = j + 1; r < n; r++) *AT(A, r, j) = *AT(A, r, j - 1);
+    if (n > 1) {
+        i64 m = n - 1;
+        double *q = (double *)malloc(sizeof(double) * (size_t)(m * m));
+        mat Ap = sub(A, 1, m, 1, m), Tp = sub(T, 0, t_rows, 0, m);
+        for (i64 r = 0; r < m; r++) for (i64 c = 0; c < m; c++) q[r * m + c] = r == c ? 1.0 : 0.0;
+        qr_apply(0, Ap, Tp, mk(q, m, m, m, 1));
+        for (i64 r = 0; r < m; r++) for (i64 c = 0; c < m; c++) *AT(Ap, r, c) = q[r * m + c];
+        free(q);
+    }
+    for (i64 k = 0; k < n; k++) { *AT(A, 0, k) = k == 0 ? 1.0 : 0.0; *AT(A, k, 0) = k == 0 ? 1.0 : 0.0; }
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
 /* LU with partial pivoting, DDLA/Factorizations/LU.cs                      */
 /* ------------------------------------------------------------------------ */
 

@@ -79,6 +79,7 @@ def lib():
         L.orc_dgeqrs.argtypes = [_i64, _i64, _i64, _dp, _i64, _i64, _dp, _i64, _i64, _i64, _dp, _i64, _i64,
                                  _dp, _i64, _i64]
         L.orc_dorgqr.argtypes = [_i64, _i64, _dp, _i64, _i64, _dp, _i64, _i64, _i64, _dp, _i64, _i64]
+        L.orc_dsytrd.argtypes = [_i64, _dp, _i64, _i64, _dp, _i64, _i64, _i64, _dp, _dp]
         L.orc_set_threads.argtypes = [C.c_int]
         L.orc_contract_plan.argtypes = [C.c_char_p, C.c_int, C.POINTER(_i64), C.POINTER(_i64),
                                         C.c_int, C.POINTER(_i64), C.POINTER(_i64),
@@ -183,6 +184,19 @@ def dorgqr(A, T):
     Q = np.zeros((m, m))
     lib().orc_dorgqr(m, n, _ptr(A), *_st(A), _ptr(T), T.shape[0], *_st(T), _ptr(Q), *_st(Q))
     return Q
+
+
+def trd_t_rows(n):
+    """Rows of DDLA's T for a tridiagonal reduction (Tridiagonaling.CreateT, :15-19)."""
+    return min(64, n)
+
+
+def dsytrd(A, T):
+    """Tridiag(A, T, d, e): A (lower triangle read) is overwritten by Q; returns (d, e)."""
+    n = A.shape[0]
+    d, e = np.zeros(n), np.zeros(max(n - 1, 1))
+    lib().orc_dsytrd(n, _ptr(A), *_st(A), _ptr(T), T.shape[0], *_st(T), _ptr(d), _ptr(e))
+    return d, e[:max(n - 1, 0)]
 
 
 def dtrsm(side, uplo, ta, diag, alpha, A, B):

@@ -399,3 +399,27 @@ def test_qr_least_squares_tall(orc):
     X = orc.dgeqrs(A, T, B)
     Xl = np.linalg.lstsq(A0, B, rcond=None)[0]
     assert np.max(np.abs(X - Xl)) < 1e-10
+
+
+@pytest.mark.parametrize("n", [1, 2, 5, 64, 65, 150])
+def test_tridiag_property_and_lapack(orc, n):
+    # Tridiagonaling.Tridiag: Q^T A Q = tridiag(d, e) from the lower triangle;
+    # the upper triangle is never read (NaN here).  LAPACK's dsytrd (uplo L)
+    # makes the same reduction with reflectors of the opposite sign, so d
+    # agrees and e agrees in magnitude.
+    from scipy.linalg import lapack
+    r = rng(80 + n)
+    G = uniform(r, (n, n))
+    S = G + G.T
+    A = np.tril(S) + np.triu(np.full((n, n), np.nan), 1)
+    T = np.zeros((orc.trd_t_rows(n), n))
+    d, e = orc.dsytrd(A, T)
+    Q = A
+    Tr = np.diag(d) + np.diag(e, -1) + np.diag(e, 1)
+    assert np.max(np.abs(Q.T @ S @ Q - Tr)) < 1e-12 * max(1.0, np.abs(S).max()) * max(n, 1) ** 0.5
+    assert np.max(np.abs(Q.T @ Q - np.eye(n))) < 1e-13
+    if n > 1:
+        _, dl, el, _, info = lapack.dsytrd(S, lower=1)
+        assert info == 0
+        assert np.max(np.abs(d - dl)) < 1e-12 * max(1.0, np.abs(S).max()) * n ** 0.5
+        assert np.max(np.abs(np.abs(e) - np.abs(el))) < 1e-12 * max(1.0, np.abs(S).max()) * n ** 0.5
