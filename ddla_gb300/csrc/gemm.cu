@@ -271,7 +271,7 @@ int gemm_f64_struct_h(ddla_handle h, i64 m, i64 n, i64 k, double alpha, View<con
     i64 parts = 1;
     if (alpha != 0.0 && k >= 1024 && tiles < sms) {
         parts = (2 * sms + tiles - 1) / tiles;
-        if (parts > k / 256) parts = k / 256;
+        if (parts > k / 128) parts = k / 128;
         if (parts > 64) parts = 64;
     }
     if (parts < 2) return gemm_f64_struct(h->stream, m, n, k, alpha, A, amode, B, bmode, beta, C, uplo);

@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(QR_THREADS, 1) k_qr_panel(QrPanelArgs a) {
     double *wred = cl_dot + QR_MAXCS * QR_WMAX;                     // [QR_WARPS][QR_WMAX]
     double *csum = wred + QR_WARPS * QR_WMAX;                       // [QR_WMAX]
     double *nred = csum + QR_WMAX;                                  // [QR_WARPS]
-    double *tau_s = nred + QR_WARPS;                                // current tau
+    double *tau_s = nred + QR_WARPS;                                // tau, 1/tau, 1/(chi-rho), rho, |x(i+1:)|
 
     auto at = [&](int lr, int c) -> double & {
         if (RES) return X[lr * WP + c];
@@ -117,31 +117,43 @@ __global__ void __launch_bounds__(QR_THREADS, 1) k_qr_panel(QrPanelArgs a) {
         }
         cluster.sync();
 
-        // 2. the reflector (every thread computes the same values)
-        double ss = 0.0, chi = 0.0;
-        for (int q = 0; q < CS; q++) {
-            ss += cl_norm[2 * q];
-            chi += cl_norm[2 * q + 1];
+        // 2. the reflector, formed once per CTA (FP64 division, square root
+        // and hypot are long instruction sequences on this GPU's FP64 pipe)
+        if (tid == 0) {
+            double ss = 0.0, chi = 0.0;
+            for (int q = 0; q < CS; q++) {
+                ss += cl_norm[2 * q];
+                chi += cl_norm[2 * q + 1];
+            }
+            const double len = sqrt(ss);
+            double rho, tau, inv = 1.0;
+            if (len == 0.0) {
+                rho = -chi;
+                tau = 0.5;
+            } else {
+                const double alpha = hypot(chi, len);
+                rho = -copysign(alpha, chi);
+                const double miu = chi - rho;
+                inv = 1.0 / miu;
+                const double sc = len / fabs(miu);
+                tau = (1.0 + sc * sc) / 2.0;
+            }
+            tau_s[0] = tau;
+            tau_s[1] = 1.0 / tau;
+            tau_s[2] = inv;
+            tau_s[3] = rho;
+            tau_s[4] = len;
         }
-        const double len = sqrt(ss);
-        double rho, tau, inv = 1.0;
-        if (len == 0.0) {
-            rho = -chi;
-            tau = 0.5;
-        } else {
-            const double alpha = hypot(chi, len);
-            rho = -copysign(alpha, chi);
-            const double miu = chi - rho;
-            inv = 1.0 / miu;
-            const double sc = len / fabs(miu);
-            tau = (1.0 + sc * sc) / 2.0;
+        __syncthreads();
+        {
+            const double inv = tau_s[2], rho = tau_s[3];
+            const bool scale = tau_s[4] != 0.0;
+            for (int lr = tid; lr < nr; lr += QR_THREADS) {
+                const int r = r0 + lr;
+                if (r > i && scale) at(lr, i) *= inv;
+                else if (r == i) at(lr, i) = rho;
+            }
         }
-        for (int lr = tid; lr < nr; lr += QR_THREADS) {
-            const int r = r0 + lr;
-            if (r > i && len != 0.0) at(lr, i) *= inv;
-            else if (r == i) at(lr, i) = rho;
-        }
-        if (tid == 0) tau_s[0] = tau;
         __syncthreads();
 
         // 3. this CTA's share of x(i, c) + u2^T x(i+1:, c) for every column
@@ -175,11 +187,17 @@ __global__ void __launch_bounds__(QR_THREADS, 1) k_qr_panel(QrPanelArgs a) {
 
         // 4. rank-1 update of the later columns: a1 -= w, A2 -= u2 w^T with
         // w = (sum of shares) / tau; the factor column S(0:i, i) and S(i, i) = tau
-        if (nc > 0 && c < w) {
+        if (warp == 0) {
             double t = 0.0;
-            for (int q = 0; q < CS; q++) t += cl_dot[q * QR_WMAX + lane];
+            if (lane < nc)
+                for (int q = 0; q < CS; q++) t += cl_dot[q * QR_WMAX + lane];
+            csum[lane] = (c > i) ? t * tau_s[1] : t;
+        }
+        __syncthreads();
+        if (nc > 0 && c < w) {
+            const double t = csum[lane];
             if (c > i) {
-                const double wv = t * (1.0 / tau_s[0]);
+                const double wv = t;
                 for (int lr = warp; lr < nr; lr += QR_WARPS) {
                     const int r = r0 + lr;
                     if (r > i) at(lr, c) = fma(-at(lr, i), wv, at(lr, c));
@@ -190,8 +208,8 @@ __global__ void __launch_bounds__(QR_THREADS, 1) k_qr_panel(QrPanelArgs a) {
             }
         }
         if (rank == 0 && tid == 0) {
-            a.tau[i] = tau;
-            a.S[(i64)i * a.lds + i] = tau;
+            a.tau[i] = tau_s[0];
+            a.S[(i64)i * a.lds + i] = tau_s[0];
         }
         __syncthreads();
     }
@@ -289,9 +307,10 @@ int qr_panel(ddla_handle h, View<double> P, int w, double *tau, double *S, i64 l
     const int64_t want = tune_get("qr.cluster", 0);
     if (want > 0 && want < cs) cs = (int)want;
     const i64 m = P.rows;
-    // smallest cluster with at most 512 rows per CTA whose rows fit on chip
+    // the panel is bound by the FP64 pipes of its CTAs: as many CTAs as keep
+    // at least 64 rows each (and fit the rows on chip)
     int use = 1;
-    while (use < cs && ((m + use - 1) / use > 512 || qr_panel_smem(true, (int)((m + use - 1) / use), w) > g_qr_smem))
+    while (use < cs && ((m + use - 1) / use > 64 || qr_panel_smem(true, (int)((m + use - 1) / use), w) > g_qr_smem))
         use *= 2;
     const i64 rp = (m + use - 1) / use;
     const bool res = qr_panel_smem(true, (int)rp, w) <= g_qr_smem && tune_get("qr.resident", 1) != 0;

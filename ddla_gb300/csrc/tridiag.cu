@@ -38,6 +38,7 @@ struct TrdWs {
     double *u[2];   // reflector vectors by column parity (full length n)
     double *p;      // unscaled p = A22 u of the last column (full length n)
     double *tau;    // tau per column
+    double *tinv;   // 1 / tau per column (one FP64 division per column, not per thread)
     double *dotp;   // per 64-row block share of u^T p
     double *prow;   // [tile][64] row partial sums
     double *pcol;   // [tile][64] column partial sums
@@ -74,7 +75,7 @@ __global__ void __launch_bounds__(1024) k_trd_column(TrdArgs a) {
     // 1. the pending rank-2 update of column i (from column i - 1)
     if (i > 0) {
         const double *uo = a.w.u[(i - 1) & 1];
-        const double tau = a.w.tau[i - 1], inv = 1.0 / tau;
+        const double inv = a.w.tinv[i - 1];
         const double beta = a.w.beta[i - 1];
         const double ui = uo[i], pi = p_fin(a.w, uo, beta, inv, i);
         for (int r = i + tid; r < n; r += blockDim.x) {
@@ -132,6 +133,7 @@ __global__ void __launch_bounds__(1024) k_trd_column(TrdArgs a) {
     }
     if (tid == 0) {
         a.w.tau[i] = tau;
+        a.w.tinv[i] = 1.0 / tau;
         a.e[i] = sigma;
         a.T[(i64)a.il * a.rst + (i64)i * a.cst] = tau;
     }
@@ -175,7 +177,7 @@ __global__ void __launch_bounds__(SW_THREADS) k_trd_sweep(TrdArgs a) {
     const double *uo = i > 0 ? a.w.u[(i - 1) & 1] : nullptr;
     double beta = 0.0, inv = 0.0;
     if (pend) {
-        inv = 1.0 / a.w.tau[i - 1];
+        inv = a.w.tinv[i - 1];
         beta = a.w.beta[i - 1];
     }
     if (tid < TT) {
@@ -317,7 +319,7 @@ int sytrd(ddla_handle h, i64 n, View<double> A, View<double> T, i64 tb, double *
     }
     cudaStream_t s = h->stream;
     const i64 ntm = (n + TT - 1) / TT;
-    const size_t nd = (size_t)(3 * n + n + ntm + 2 * ntm * (ntm + 1) / 2 * TT + ntm * TT + n + 16);
+    const size_t nd = (size_t)(3 * n + n + ntm + 2 * ntm * (ntm + 1) / 2 * TT + ntm * TT + 2 * n + 16);
     void *ws;
     DDLA_TRY(workspace(h, WS_TRD, sizeof(double) * nd, &ws));
     TrdWs w;
@@ -331,7 +333,8 @@ int sytrd(ddla_handle h, i64 n, View<double> A, View<double> T, i64 tb, double *
     w.pcol = w.prow + ntm * (ntm + 1) / 2 * TT;
     w.pt = w.pcol + ntm * (ntm + 1) / 2 * TT;
     w.beta = w.pt + ntm * TT;
-    w.ticket = (unsigned *)(w.beta + n);
+    w.tinv = w.beta + n;
+    w.ticket = (unsigned *)(w.tinv + n);
     DDLA_CUDA(cudaMemsetAsync(w.ticket, 0, sizeof(unsigned), s));
     TrdArgs a;
     a.A = A.p;
