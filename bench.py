@@ -306,6 +306,27 @@ def secondary(args):
             h.sync()
             Tr = torch.diag(dw) + torch.diag(ew, -1) + torch.diag(ew, 1)
             return float((Aw.T @ S @ Aw - Tr).abs().max() / S.abs().max())
+    elif wl == "bidiag":
+        n = args.n if args.n != N_DEFAULT else 4096
+        A0 = U(n, n)
+        Aw = torch.empty_like(A0)
+        Uw = torch.empty_like(A0)
+        Vw = torch.empty_like(A0)
+        dw = torch.zeros(n, dtype=torch.float64, device="cuda")
+        ew = torch.zeros(n - 1, dtype=torch.float64, device="cuda")
+        bprec = D.PREC_OZAKI if prec == D.PREC_OZAKI else 0
+        flops = 8.0 * n ** 3 / 3.0 + 4.0 * n ** 3 / 3.0 * 2   # reduction 8/3 n^3 + U and V 4/3 n^3 each
+        desc = f"one-stage bidiagonal reduction + U, V, {n}x{n} FP64 U[-1,1], {pname} U/V formation"
+
+        def step():
+            Aw.copy_(A0)
+            h.bidiag(Aw, dw, ew, Uw, Vw, precision=bprec)
+
+        def check_err():
+            step()
+            h.sync()
+            B = torch.diag(dw) + torch.diag(ew, 1)
+            return float((Uw.T @ A0 @ Vw - B).abs().max() / A0.abs().max())
     elif wl == "einsum-chain":
         n = args.n if args.n != N_DEFAULT else 4096
         expr = "ab,bc,cd,de->ae"
@@ -468,7 +489,7 @@ def secondary(args):
     ms = statistics.median(times)
     value = flops / (ms * 1e-3) / 1e9
     classes = None
-    if wl in ("qr", "tridiag"):
+    if wl in ("qr", "tridiag", "bidiag"):
         # one more step with per-class CUDA-event brackets (outside the timed steps)
         L.ddla_timing_enable(1)
         step()
@@ -523,7 +544,7 @@ def main():
                     help="library tuning key (ddla_tune_set) applied before the run; repeatable")
     ap.add_argument("--workload", default="lu", choices=["lu", "gemm", "chol", "batched", "einsum-a", "einsum-b",
                                                          "symm", "trmm", "syr2k", "qr", "einsum-chain",
-                                                         "tridiag"])
+                                                         "tridiag", "bidiag"])
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-n", type=int, default=4096)
     ap.add_argument("--no-cpu", action="store_true")

@@ -6,8 +6,8 @@ BlasProvider / LU / Cholesky / LDLT / QR / MArray.Contract interface.
 """
 from ._lib import (DENSE, LEFT, LOWER, NO_TRANSPOSE, NONUNIT, PREC_BF16X3, PREC_FP32, PREC_FP64, PREC_OZAKI,
                    PREC_TF32X3, RIGHT, TRANSPOSE, UNIT, UPPER, DDLAError, LinalgError, kernel_launches, lib)
-from .linalg import LDLT, LU, QR, BlasProvider, Cholesky, Tridiagonaling, solve_mixed
+from .linalg import LDLT, LU, QR, BlasProvider, Bidiagonaling, Cholesky, Tridiagonaling, solve_mixed
 
-__all__ = ["lib", "BlasProvider", "LU", "Cholesky", "LDLT", "QR", "Tridiagonaling", "solve_mixed", "LinalgError", "DDLAError",
+__all__ = ["lib", "BlasProvider", "LU", "Cholesky", "LDLT", "QR", "Tridiagonaling", "Bidiagonaling", "solve_mixed", "LinalgError", "DDLAError",
            "kernel_launches", "NO_TRANSPOSE", "TRANSPOSE", "LOWER", "UPPER", "DENSE", "UNIT", "NONUNIT", "LEFT",
            "RIGHT", "PREC_FP64", "PREC_FP32", "PREC_TF32X3", "PREC_BF16X3", "PREC_OZAKI"]

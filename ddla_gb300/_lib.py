@@ -103,6 +103,10 @@ _SIGS = {
     "ddla_dev_dorgqr": (C.c_int, [_h, _i64, _i64, _pd, _i64, _i64, _pd, _i64, _i64, _i64, _pd, _i64, _i64]),
     "ddla_dsytrd": (C.c_int, [_i64, _pd, _i64, _i64, _pd, _i64, _i64, _i64, _pd, _pd, C.POINTER(Opts)]),
     "ddla_dev_dsytrd": (C.c_int, [_h, _i64, _pd, _i64, _i64, _pd, _i64, _i64, _i64, _pd, _pd, C.POINTER(Opts)]),
+    "ddla_dbidiag": (C.c_int, [_i64, _i64, _pd, _i64, _i64, _pd, _pd, _pd, _i64, _i64, _pd, _i64, _i64,
+                               C.POINTER(Opts)]),
+    "ddla_dev_dbidiag": (C.c_int, [_h, _i64, _i64, _pd, _i64, _i64, _pd, _pd, _pd, _i64, _i64, _pd, _i64, _i64,
+                                   C.POINTER(Opts)]),
     "ddla_dgetrf": (C.c_int, [_i64, _pd, _i64, _i64, _pi, C.POINTER(Opts)]),
     "ddla_dgetrs": (C.c_int, [_i32, _i64, _i64, _pd, _i64, _i64, _pi, _pd, _i64, _i64]),
     "ddla_dgetrf_nopiv": (C.c_int, [_i64, _pd, _i64, _i64, C.POINTER(Opts)]),

@@ -212,6 +212,11 @@ int orgqr(ddla_handle h, i64 m, i64 n, View<const double> A, View<const double> 
 // becomes Q, d (n) and e (n - 1) the tridiagonal, T (tb rows) the factors.
 int sytrd(ddla_handle h, i64 n, View<double> A, View<double> T, i64 tb, double *d, double *e,
           int prec = DDLA_PREC_FP64);
+// Bidiagonaling.Bidiag2 on device data (bidiag.cu), m >= n: A becomes the
+// reflectors, d (n) / e (n - 1) the upper bidiagonal, U (m x m) and V (n x n)
+// the orthogonal factors with U^T A V = bidiag(d, e).
+int bidiag(ddla_handle h, i64 m, i64 n, View<double> A, double *d, double *e, View<double> U, View<double> V,
+           int prec = DDLA_PREC_FP64);
 
 // Triangular-solve building blocks (trsm.cu): inverses of the 64 x 64
 // diagonal blocks, and the chained whole-system solve for <= 16 columns.

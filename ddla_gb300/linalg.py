@@ -10,6 +10,7 @@ tests read like DDLA's own tests:
   LDLT                                      DDLA/Factorizations/LDLT.cs:9-137
   QR                                        DDLA/Factorizations/QR.cs:14-534
   Tridiagonaling                            DDLA/Transformations/Tridiagonaling.cs:10-232
+  Bidiagonaling.Bidiag2                     DDLA/Transformations/Bidiagonaling.cs:35-143
 
 Matrices are float64 numpy arrays; any 2-D view works (its element strides
 are DDLA's RowStride / ColStride), and in-place operations write through the
@@ -23,7 +24,8 @@ from . import _lib
 from ._lib import (LEFT, LOWER, NO_TRANSPOSE, NONUNIT, RIGHT, TRANSPOSE, UNIT, UPPER, LinalgError, Opts,
                    SolveReport, check, lib)
 
-__all__ = ["BlasProvider", "LU", "Cholesky", "LDLT", "QR", "Tridiagonaling", "solve_mixed", "LinalgError"]
+__all__ = ["BlasProvider", "LU", "Cholesky", "LDLT", "QR", "Tridiagonaling", "Bidiagonaling", "solve_mixed",
+           "LinalgError"]
 
 
 def _view(x, name):
@@ -555,6 +557,25 @@ class Tridiagonaling:
         check(lib().ddla_dsytrd(n, _p(A), *_st(A), _p(T), T.shape[0], *_st(T), _p(d), _p(e) if n > 1 else None,
                                 C.byref(_opts(0, precision))), "Tridiag")
         return T, d, e
+
+
+class Bidiagonaling:
+    """Bidiagonaling.Bidiag2 -- DDLA/Transformations/Bidiagonaling.cs:35-143
+    (the one-stage Householder reduction, m >= n)."""
+
+    @staticmethod
+    def Bidiag2(A, precision=0):
+        """Returns (U, V, d, e) with U^T A V = bidiag(d, e); A (m x n, m >= n)
+        is overwritten by the reflectors, as in DDLA."""
+        A = _view(A, "A")
+        m, n = A.shape
+        if m < n:
+            raise ValueError("Only support m >= n")
+        U, V = np.zeros((m, m)), np.zeros((n, n))
+        d, e = np.zeros(n), np.zeros(max(n - 1, 0))
+        check(lib().ddla_dbidiag(m, n, _p(A), *_st(A), _p(d), _p(e) if n > 1 else None, _p(U), *_st(U), _p(V),
+                                 *_st(V), C.byref(_opts(0, precision))), "Bidiag2")
+        return U, V, d, e
 
 
 def solve_mixed(A, B, spd=False, uplo=LOWER, precision=_lib.PREC_FP32, x_ref=None, tol=0.0, max_iter=0, nb=0):

@@ -246,6 +246,17 @@ int ddla_dorgqr(ddla_dim_t m, ddla_dim_t n, const double *a, ddla_inc_t rsa, ddl
 int ddla_dsytrd(ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t csa, double *t, ddla_dim_t t_rows,
                 ddla_inc_t rst, ddla_inc_t cst, double *d, double *e, const ddla_opts *opts);
 
+/* ------------------------------------------------ bidiagonal reduction (host) */
+
+/* One-stage Householder reduction of A (m x n, m >= n) to upper bidiagonal
+ * form: U^T A V = bidiag(d, e) with U (m x m) and V (n x n) orthogonal; A is
+ * overwritten by the reflectors.  Bidiagonaling.Bidiag2 (HHStepBlock and
+ * BuildUV), DDLA/Transformations/Bidiagonaling.cs:48-143.  opts (may be NULL):
+ * precision DDLA_PREC_OZAKI forms U and V with split-precision products. */
+int ddla_dbidiag(ddla_dim_t m, ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t csa, double *d, double *e,
+                 double *u, ddla_inc_t rsu, ddla_inc_t csu, double *v, ddla_inc_t rsv, ddla_inc_t csv,
+                 const ddla_opts *opts);
+
 /* ------------------------------------------------ factorizations (host) */
 
 /* In-place LU with partial pivoting; piv[i] is RELATIVE (row i swapped with
@@ -325,6 +336,9 @@ int ddla_dev_dtrmm3(ddla_handle h, int32_t sidea, int32_t uploa, int32_t transa,
                     ddla_dim_t m, ddla_dim_t n, double alpha, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
                     const double *b, ddla_inc_t rsb, ddla_inc_t csb,
                     double beta, double *c, ddla_inc_t rsc, ddla_inc_t csc);
+int ddla_dev_dbidiag(ddla_handle h, ddla_dim_t m, ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t csa, double *d,
+                     double *e, double *u, ddla_inc_t rsu, ddla_inc_t csu, double *v, ddla_inc_t rsv, ddla_inc_t csv,
+                     const ddla_opts *opts);
 int ddla_dev_dsytrd(ddla_handle h, ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t csa, double *t,
                     ddla_dim_t t_rows, ddla_inc_t rst, ddla_inc_t cst, double *d, double *e, const ddla_opts *opts);
 int ddla_dev_dgeqrf(ddla_handle h, ddla_dim_t m, ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t csa,

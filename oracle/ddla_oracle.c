@@ -710,6 +710,88 @@ int orc_dsytrd(i64 n, double *a, i64 rsa, i64 csa, double *t, i64 t_rows, i64 rs
 }
 
 /* ------------------------------------------------------------------------ */
+/* One-stage bidiagonal reduction, DDLA/Transformations/Bidiagonaling.cs     */
+/* ------------------------------------------------------------------------ */
+
+#define BD_BLOCK 128   /* Bidiagonaling.BlockSize, :62 */
+
+/* Bidiag2(A, U, V, d, e), Bidiagonaling.cs:48-60: HHStepBlock (:64-123) and
+ * BuildUV (:125-143) for m >= n.  Per column g: the column reflector (BuildHH
+ * of Tridiagonaling, u(g) = 1 kept in A), d(g) = sigma, A(g:, g+1:) -= u
+ * (u^T A(g:, g+1:)) / tau, TU(0:j, g) = A(g, j) + A(g+1:, j)^T u(g+1:) over the
+ * block's earlier columns; then (except for the last column) the row
+ * reflector of A(g, g+1:), e(g) = sigma, A(g+1:, g+1:) -= (A v) v^T / tau and
+ * TV(0:j, g) likewise from the rows above.  U (m x m) and V (n x n) start as
+ * the identity and receive the block reflectors (ApplyQ, :159-182: backward
+ * blocks, the first one T.Cols % block wide, which the QR's partition matches
+ * when it divides evenly and is otherwise the same product). */
+int orc_dbidiag(i64 m, i64 n, double *a, i64 rsa, i64 csa, double *tu, i64 tu_rows, double *tv, i64 tv_rows,
+                double *d, double *e, double *u, i64 rsu, i64 csu, double *v, i64 rsv, i64 csv) {
+    if (m < n) return -1;
+    mat A = mk(a, m, n, rsa, csa);
+    mat TU = mk(tu, tu_rows, n, n, 1), TV = mk(tv, tv_rows, n, n, 1);
+    if (n == 0) return 0;
+    double *buf = (double *)malloc(sizeof(double) * (size_t)(m > n ? m : n));
+    for (i64 bs = 0; bs < n; bs += BD_BLOCK) {
+        i64 block = n - bs < BD_BLOCK ? n - bs : BD_BLOCK;
+        i64 be = bs + block;
+        for (i64 il = 0; il < block; il++) {
+            i64 g = bs + il;
+            double tau, sig;
+            /* column reflector */
+            trd_build(AT(A, g, g), m - g, A.rs, &sig, &tau);
+            d[g] = sig;
+            *AT(TU, il, g) = tau;
+            i64 nr = n - g - 1;
+            for (i64 c = 0; c < nr; c++) {
+                double acc = 0.0;
+                for (i64 r = g; r < m; r++) acc = fma(*AT(A, r, g), *AT(A, r, g + 1 + c), acc);
+                buf[c] = acc * (1.0 / tau);
+            }
+            for (i64 r = g; r < m; r++) {
+                double ur = -*AT(A, r, g);
+                for (i64 c = 0; c < nr; c++) *AT(A, r, g + 1 + c) = fma(ur, buf[c], *AT(A, r, g + 1 + c));
+            }
+            for (i64 j = 0; j < il; j++) {
+                double acc = *AT(A, g, bs + j);
+                for (i64 r = g + 1; r < m; r++) acc = fma(*AT(A, r, bs + j), *AT(A, r, g), acc);
+                *AT(TU, j, g) = acc;
+            }
+            /* row reflector (Bidiagonaling.cs:92-119) */
+            if ((g < n - 1 && il < block - 1) || be < n) {
+                trd_build(AT(A, g, g + 1), nr, A.cs, &sig, &tau);
+                e[g] = sig;
+                *AT(TV, il, g) = tau;
+                i64 mr = m - g - 1;
+                for (i64 r = 0; r < mr; r++) {
+                    double acc = 0.0;
+                    for (i64 c = 0; c < nr; c++) acc = fma(*AT(A, g + 1 + r, g + 1 + c), *AT(A, g, g + 1 + c), acc);
+                    buf[r] = acc * (1.0 / tau);
+                }
+                for (i64 r = 0; r < mr; r++) {
+                    double br = -buf[r];
+                    for (i64 c = 0; c < nr; c++)
+                        *AT(A, g + 1 + r, g + 1 + c) = fma(br, *AT(A, g, g + 1 + c), *AT(A, g + 1 + r, g + 1 + c));
+                }
+                for (i64 j = 0; j < il; j++) {
+                    double acc = *AT(A, bs + j, g + 1);
+                    for (i64 c = g + 2; c < n; c++) acc = fma(*AT(A, bs + j, c), *AT(A, g, c), acc);
+                    *AT(TV, j, g) = acc;
+                }
+            }
+        }
+    }
+    free(buf);
+    /* BuildUV: U = H_0 ... H_{n-1} I, V = [1, 0; 0, G_0 ... G_{n-2} I] */
+    mat U = mk(u, m, m, rsu, csu), V = mk(v, n, n, rsv, csv);
+    for (i64 r = 0; r < m; r++) for (i64 c = 0; c < m; c++) *AT(U, r, c) = r == c ? 1.0 : 0.0;
+    for (i64 r = 0; r < n; r++) for (i64 c = 0; c < n; c++) *AT(V, r, c) = r == c ? 1.0 : 0.0;
+    qr_apply(0, A, TU, U);
+    if (n > 1) qr_apply(0, tr(sub(A, 0, n - 1, 1, n - 1)), sub(TV, 0, tv_rows, 0, n - 1), sub(V, 1, n - 1, 0, n));
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
 /* LU with partial pivoting, DDLA/Factorizations/LU.cs                      */
 /* ------------------------------------------------------------------------ */
 

@@ -80,6 +80,8 @@ def lib():
                                  _dp, _i64, _i64]
         L.orc_dorgqr.argtypes = [_i64, _i64, _dp, _i64, _i64, _dp, _i64, _i64, _i64, _dp, _i64, _i64]
         L.orc_dsytrd.argtypes = [_i64, _dp, _i64, _i64, _dp, _i64, _i64, _i64, _dp, _dp]
+        L.orc_dbidiag.argtypes = [_i64, _i64, _dp, _i64, _i64, _dp, _i64, _dp, _i64, _dp, _dp, _dp, _i64, _i64,
+                                  _dp, _i64, _i64]
         L.orc_set_threads.argtypes = [C.c_int]
         L.orc_contract_plan.argtypes = [C.c_char_p, C.c_int, C.POINTER(_i64), C.POINTER(_i64),
                                         C.c_int, C.POINTER(_i64), C.POINTER(_i64),
@@ -197,6 +199,21 @@ def dsytrd(A, T):
     d, e = np.zeros(n), np.zeros(max(n - 1, 1))
     lib().orc_dsytrd(n, _ptr(A), *_st(A), _ptr(T), T.shape[0], *_st(T), _ptr(d), _ptr(e))
     return d, e[:max(n - 1, 0)]
+
+
+def bidiag(A):
+    """Bidiagonaling.Bidiag2 (one stage, m >= n): returns (U, V, d, e, TU, TV)
+    with U^T A V = bidiag(d, e); A is overwritten by the reflectors."""
+    m, n = A.shape
+    tur, tvr = min(128, n), max(min(128, n - 1), 1)
+    TU, TV = np.zeros((tur, n)), np.zeros((tvr, n))
+    d, e = np.zeros(n), np.zeros(max(n - 1, 1))
+    U, V = np.zeros((m, m)), np.zeros((n, n))
+    rc = lib().orc_dbidiag(m, n, _ptr(A), *_st(A), _ptr(TU), tur, _ptr(TV), tvr, _ptr(d), _ptr(e), _ptr(U), *_st(U),
+                           _ptr(V), *_st(V))
+    if rc:
+        raise ValueError("orc_dbidiag: m < n")
+    return U, V, d, e[:max(n - 1, 0)], TU, TV
 
 
 def dtrsm(side, uplo, ta, diag, alpha, A, B):

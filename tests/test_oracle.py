@@ -423,3 +423,22 @@ def test_tridiag_property_and_lapack(orc, n):
         assert info == 0
         assert np.max(np.abs(d - dl)) < 1e-12 * max(1.0, np.abs(S).max()) * n ** 0.5
         assert np.max(np.abs(np.abs(e) - np.abs(el))) < 1e-12 * max(1.0, np.abs(S).max()) * n ** 0.5
+
+
+@pytest.mark.parametrize("m,n", [(1, 1), (5, 5), (9, 4), (200, 130), (300, 300), (301, 260)])
+def test_bidiag_property(orc, m, n):
+    # Bidiagonaling.Bidiag2 (one stage): U^T A V = bidiag(d, e), U and V
+    # orthogonal, singular values of the bidiagonal equal numpy's of A.
+    # (scipy has no dgebrd, so this oracle is pinned by these properties.)
+    r = rng(100 + m + n)
+    A0 = uniform(r, (m, n))
+    U, V, d, e, TU, TV = orc.bidiag(A0.copy())
+    B = np.zeros((m, n))
+    B[np.arange(n), np.arange(n)] = d
+    if n > 1:
+        B[np.arange(n - 1), np.arange(1, n)] = e
+    assert np.max(np.abs(U.T @ A0 @ V - B)) < 1e-13 * max(m, 1)
+    assert np.max(np.abs(U.T @ U - np.eye(m))) < 1e-13
+    assert np.max(np.abs(V.T @ V - np.eye(n))) < 1e-13
+    sv = np.sort(np.abs(np.linalg.svd(B, compute_uv=False)))
+    assert np.max(np.abs(sv - np.sort(np.linalg.svd(A0, compute_uv=False)))) < 1e-12 * max(m, 1)
