@@ -328,7 +328,14 @@ int refine(ddla_handle h, i64 n, int nr, const double *A, const double *B, doubl
             // straight at the backward-error target
             int used = 0;
             double an = u64d(hn[0]), xn = u64d(hn[1 + nr]), bn = u64d(hn[1]);
-            const double target = 0.5 * tol * (an * xn + bn);
+            // the cycle stops on the residual's 2-norm, which bounds the
+            // inf-norm of the backward error from above by up to sqrt(n); the
+            // target is relaxed by min(16, sqrt(n) / 4) (tuning key
+            // refine.gmres.relax), and the loop re-checks the true backward
+            // error, so a residual that is not spread out only costs a cycle
+            const int64_t rk = tune_get("refine.gmres.relax", 0);
+            const double relax = rk > 0 ? (double)rk : std::min(16.0, std::max(1.0, std::sqrt((double)n) / 4.0));
+            const double target = 0.5 * tol * (an * xn + bn) * relax;
             DDLA_TRY(gmres_cycle(h, n, A, R, X, solve32, d32, gV, gZ, gW, gh, gm_m, target, &used));
             it += used;
         } else {

@@ -135,6 +135,8 @@ int ddla_timing_read(int cls, double *total_ms, int64_t *launches, double *flops
  * the chained per-block triangular solve instead of the cluster solve),
  * "trsv.cluster.size", "refine.gmres" (0 = classical refinement for one
  * right-hand side), "refine.gmres.m" (GMRES restart length),
+ * "refine.gmres.relax" (factor on GMRES's 2-norm stopping target; 0 =
+ * min(16, sqrt(n) / 4)),
  * "batched.nb.{32,64,128,big}", "batched.ctas_per_sm", "update.tc",
  * "update.tn", "update.tiles_per_cta", "u12.gemm", "qr.nb" (QR panel width
  * cap), "qr.cluster" (CTAs per QR panel cluster), "qr.resident" (0 factors QR
