@@ -49,6 +49,7 @@ struct PanelArgs {
     i64 row_base;
     int *touch_count, *touch_rows, *touch_src;
     T *inv;   // optional: inverse of the unit-lower w x w block L11 (row-major, ld TRI_TB)
+    int *calu;   // tournament-pivoting scratch (k_panel_calu)
 };
 
 // Pivot search keys: |x| as an unsigned integer bit pattern plus one, NaN as
@@ -401,6 +402,294 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_panel_lu(PanelArgs<T> a) {
     }
 }
 
+// ------------------------------------------------------------------ tournament pivoting
+//
+// k_panel_calu: the same panel with communication-avoiding pivoting (CALU,
+// tournament pivoting), for the FP32 factorizations of the mixed-precision
+// solvers, whose pivots only have to be good, not DDLA's (FP64 refinement
+// makes the solution FP64-accurate; the solve report gives the agreement with
+// partial pivoting).  Each CTA selects w candidate rows by partial pivoting on
+// its own rows, with no cluster traffic per column; groups of 4 CTAs then
+// merge their candidates (partial pivoting on the candidates' original rows)
+// until one set of w winners remains, in pivot order, with the LU of their
+// block.  The panel is then the no-pivot LU of the permuted rows: every other
+// row becomes a row of L21 = A21 U11^-1.  A cluster barrier separates the
+// levels, so a panel costs a few barriers instead of one per column.
+
+constexpr int CALU_LEVELS = 3;   // local, groups of 4, groups of 16 (16 CTAs at most)
+constexpr int CALU_INTS = CALU_LEVELS * PANEL_MAXCS * PANEL_WMAX + CALU_LEVELS * PANEL_MAXCS + 64;
+
+struct CaluSmem {
+    size_t rows, org, merge, morg, ut, dinv, red, win, dtop, isw, total;
+};
+
+__host__ __device__ inline CaluSmem calu_smem_layout(int rp, int w) {
+    CaluSmem L;
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+        size_t at = o;
+        o = (o + bytes + 15) & ~(size_t)15;
+        return at;
+    };
+    L.rows = take(sizeof(float) * (size_t)rp * (w + 1));
+    L.org = take(sizeof(int) * (size_t)rp);
+    L.merge = take(sizeof(float) * (size_t)4 * w * (w + 1));
+    L.morg = take(sizeof(int) * (size_t)4 * w);
+    L.ut = take(sizeof(float) * (size_t)w * (w + 1));
+    L.dinv = take(sizeof(float) * (size_t)w);
+    L.red = take((sizeof(unsigned) + sizeof(int)) * (PANEL_THREADS / 32) + 16);
+    L.win = take(sizeof(int) * (size_t)w);
+    L.dtop = take(sizeof(int) * (size_t)w);
+    L.isw = take((size_t)rp);
+    L.total = o;
+    return L;
+}
+
+// Partial-pivoting LU of the nr x w matrix M (row stride WP) in place; the
+// rows carry their origins in org.  Pivot: the largest |x| (amax_key: NaN
+// lowest), the lower row on ties.  A zero column keeps its first row as the
+// pivot and is not scaled.
+__device__ void calu_lu(float *M, int *org, int nr, int w, int WP, unsigned *red_v, int *red_i) {
+    const int tid = threadIdx.x;
+    const int kk = nr < w ? nr : w;
+    for (int j = 0; j < kk; j++) {
+        unsigned bv = 0;
+        int bi = INT_MAX;
+        for (int r = j + tid; r < nr; r += PANEL_THREADS) {
+            const unsigned v = amax_key(M[r * WP + j]);
+            if (v > bv || bi == INT_MAX) {
+                bv = v;
+                bi = r;
+            }
+        }
+        block_argmax<unsigned>(bv, bi, red_v, red_i);
+        const int p = bi == INT_MAX ? j : bi;
+        if (p != j) {
+            for (int c = tid; c < w; c += PANEL_THREADS) {
+                const float t = M[j * WP + c];
+                M[j * WP + c] = M[p * WP + c];
+                M[p * WP + c] = t;
+            }
+            if (tid == 0) {
+                const int t = org[j];
+                org[j] = org[p];
+                org[p] = t;
+            }
+        }
+        __syncthreads();
+        const float pv = M[j * WP + j];
+        if (pv != 0.0f) {
+            const float rinv = 1.0f / pv;
+            for (int r = j + 1 + tid; r < nr; r += PANEL_THREADS) {
+                float *row = M + r * WP;
+                const float l = row[j] * rinv;
+                row[j] = l;
+                for (int c = j + 1; c < w; c++) row[c] = fmaf(-l, M[j * WP + c], row[c]);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(PANEL_THREADS, 1) k_panel_calu(PanelArgs<float> a) {
+    cg::cluster_group cluster = cg::this_cluster();
+    const int CS = (int)cluster.num_blocks();
+    const int rank = (int)cluster.block_rank();
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int w = a.w, WP = w + 1, rp = a.rows_per;
+    const CaluSmem L = calu_smem_layout(rp, w);
+    float *rows = (float *)(smem + L.rows), *merge = (float *)(smem + L.merge), *ut = (float *)(smem + L.ut);
+    float *dinv = (float *)(smem + L.dinv);
+    int *org = (int *)(smem + L.org), *morg = (int *)(smem + L.morg);
+    int *win = (int *)(smem + L.win), *dtop = (int *)(smem + L.dtop);
+    unsigned char *isw = smem + L.isw;
+    unsigned *red_v = (unsigned *)(smem + L.red);
+    int *red_i = (int *)(red_v + PANEL_THREADS / 32);
+    int *cand = a.calu;                                            // [level][rank][64]
+    int *ccnt = cand + CALU_LEVELS * PANEL_MAXCS * PANEL_WMAX;     // [level][rank]
+    const int base = rank * rp;
+    int nloc = a.m - base;
+    nloc = nloc < 0 ? 0 : (nloc > rp ? rp : nloc);
+    const int kmax = a.m < w ? a.m : w;
+    auto ld = [&](int r, int c) { return a.P[(i64)r * a.rs + (i64)c * a.cs]; };
+
+    // 1. local candidates
+    for (int e = tid; e < nloc * w; e += PANEL_THREADS) rows[(e / w) * WP + e % w] = ld(base + e / w, e % w);
+    for (int l = tid; l < nloc; l += PANEL_THREADS) org[l] = base + l;
+    __syncthreads();
+    calu_lu(rows, org, nloc, w, WP, red_v, red_i);
+    {
+        const int k0 = nloc < w ? nloc : w;
+        for (int i = tid; i < k0; i += PANEL_THREADS) cand[rank * PANEL_WMAX + i] = org[i];
+        if (tid == 0) ccnt[rank] = k0;
+    }
+    // 2. merges in groups of 4 until one CTA holds the winners
+    const float *fin = rows;
+    const int *finorg = org;
+    int level = 0;
+    for (int span = 1; span < CS; span *= 4, level++) {
+        __threadfence();
+        cluster.sync();
+        if (rank % (4 * span) == 0) {
+            int nr = 0;
+            for (int q = 0; q < 4; q++) {
+                const int src = rank + q * span;
+                if (src >= CS) break;
+                const int cnt = ((volatile int *)ccnt)[level * PANEL_MAXCS + src];
+                const int *cl = cand + (level * PANEL_MAXCS + src) * PANEL_WMAX;
+                for (int e = tid; e < cnt * w; e += PANEL_THREADS) {
+                    const int r = e / w, c = e % w;
+                    merge[(nr + r) * WP + c] = ld(((volatile int *)cl)[r], c);
+                }
+                for (int i = tid; i < cnt; i += PANEL_THREADS) morg[nr + i] = ((volatile int *)cl)[i];
+                nr += cnt;
+            }
+            __syncthreads();
+            calu_lu(merge, morg, nr, w, WP, red_v, red_i);
+            const int kk = nr < w ? nr : w;
+            for (int i = tid; i < kk; i += PANEL_THREADS)
+                cand[((level + 1) * PANEL_MAXCS + rank) * PANEL_WMAX + i] = morg[i];
+            if (tid == 0) ccnt[(level + 1) * PANEL_MAXCS + rank] = kk;
+        }
+        fin = merge;
+        finorg = morg;
+    }
+    // 3. CTA 0: the winners' block, the interchanges as LAPACK-style swaps
+    if (rank == 0) {
+        for (int e = tid; e < kmax * w; e += PANEL_THREADS) ut[(e / w) * WP + e % w] = fin[(e / w) * WP + e % w];
+        for (int j = tid; j < kmax; j += PANEL_THREADS) {
+            win[j] = finorg[j];
+            dtop[j] = -1;
+        }
+        __syncthreads();
+        if (tid < kmax) {
+            const float d = ut[tid * WP + tid];
+            if (d == 0.0f) atomicMin(a.info, (int)(a.row_base + tid + 1));
+            dinv[tid] = 1.0f / d;
+        }
+        if (warp == 0) {
+            // slots 0..kmax-1 hold origins cur[]; rows moved below hold
+            // (dorg, dpos); lane l owns slots / entries l and l + 32
+            int cur0 = lane, cur1 = lane + 32;
+            int dorg0 = -1, dorg1 = -1, dpos0 = 0, dpos1 = 0;
+            int nd = 0;
+            for (int j = 0; j < kmax; j++) {
+                const int o = win[j];
+                const unsigned hc0 = __ballot_sync(0xffffffffu, lane >= j && lane < kmax && cur0 == o);
+                const unsigned hc1 = __ballot_sync(0xffffffffu, lane + 32 >= j && lane + 32 < kmax && cur1 == o);
+                const unsigned hd0 = __ballot_sync(0xffffffffu, lane < nd && dorg0 == o);
+                const unsigned hd1 = __ballot_sync(0xffffffffu, lane + 32 < nd && dorg1 == o);
+                const int cj = __shfl_sync(0xffffffffu, j < 32 ? cur0 : cur1, j & 31);   // origin now in slot j
+                int p;
+                if (hc0) p = __ffs(hc0) - 1;
+                else if (hc1) p = __ffs(hc1) - 1 + 32;
+                else if (hd0) p = __shfl_sync(0xffffffffu, dpos0, __ffs(hd0) - 1);
+                else if (hd1) p = __shfl_sync(0xffffffffu, dpos1, __ffs(hd1) - 1);
+                else p = o;
+                if (lane == 0) a.piv[j] = p - j;
+                if (p != j) {
+                    if (p < kmax) {
+                        if (p < 32) { if (lane == p) cur0 = cj; }
+                        else { if (lane == p - 32) cur1 = cj; }
+                    } else if (hd0 | hd1) {
+                        const int di = hd0 ? __ffs(hd0) - 1 : __ffs(hd1) - 1 + 32;
+                        if (di < 32) { if (lane == di) dorg0 = cj; }
+                        else { if (lane == di - 32) dorg1 = cj; }
+                    } else {
+                        if (nd < 32) { if (lane == nd) { dorg0 = cj; dpos0 = p; } }
+                        else { if (lane == nd - 32) { dorg1 = cj; dpos1 = p; } }
+                        nd++;
+                    }
+                    if (j < 32) { if (lane == j) cur0 = o; }
+                    else { if (lane == j - 32) cur1 = o; }
+                }
+            }
+            // displaced top rows: final positions; the touched-row list
+            if (lane < nd) dtop[dorg0] = dpos0;
+            if (lane + 32 < nd) dtop[dorg1] = dpos1;
+            int tc = 0;
+            for (int j = 0; j < kmax; j++)
+                if (win[j] != j) {
+                    if (lane == 0) {
+                        a.touch_rows[tc] = j;
+                        a.touch_src[tc] = win[j];
+                    }
+                    tc++;
+                }
+            for (int i = 0; i < nd; i++) {
+                const int dor = __shfl_sync(0xffffffffu, i < 32 ? dorg0 : dorg1, i & 31);
+                const int dps = __shfl_sync(0xffffffffu, i < 32 ? dpos0 : dpos1, i & 31);
+                if (lane == 0) {
+                    a.touch_rows[tc] = dps;
+                    a.touch_src[tc] = dor;
+                }
+                tc++;
+            }
+            if (lane == 0) *a.touch_count = tc;
+        }
+        __syncthreads();
+        if (a.inv) {
+            // inverse of the unit-lower L11 (forward substitution per column)
+            for (int c0 = warp; c0 < TRI_TB; c0 += PANEL_THREADS / 32) {
+                float y0 = (lane == c0) ? 1.0f : 0.0f, y1 = (lane + 32 == c0) ? 1.0f : 0.0f;
+                if (c0 < kmax) {
+                    for (int k = c0; k < kmax - 1; k++) {
+                        const float yk = __shfl_sync(0xffffffffu, k < 32 ? y0 : y1, k & 31);
+                        if (lane > k && lane < kmax) y0 = fmaf(-ut[lane * WP + k], yk, y0);
+                        if (lane + 32 > k && lane + 32 < kmax) y1 = fmaf(-ut[(lane + 32) * WP + k], yk, y1);
+                    }
+                } else {
+                    y0 = y1 = 0.0f;
+                }
+                a.inv[lane * TRI_TB + c0] = lane < kmax ? y0 : 0.0f;
+                a.inv[(lane + 32) * TRI_TB + c0] = lane + 32 < kmax ? y1 : 0.0f;
+            }
+        }
+    }
+    cluster.sync();
+    // 4. every CTA: the winners, the displaced rows' positions and U11 from
+    // CTA 0; the original rows again (nothing of the panel is written before
+    // the barrier below)
+    if (rank != 0) {
+        const float *ut0 = cluster.map_shared_rank(ut, 0);
+        for (int e = tid; e < kmax * w; e += PANEL_THREADS) ut[(e / w) * WP + e % w] = ut0[(e / w) * WP + e % w];
+        for (int j = tid; j < kmax; j += PANEL_THREADS) {
+            win[j] = cluster.map_shared_rank(win, 0)[j];
+            dtop[j] = cluster.map_shared_rank(dtop, 0)[j];
+            dinv[j] = cluster.map_shared_rank(dinv, 0)[j];
+        }
+    }
+    for (int e = tid; e < nloc * w; e += PANEL_THREADS) rows[(e / w) * WP + e % w] = ld(base + e / w, e % w);
+    for (int l = tid; l < nloc; l += PANEL_THREADS) isw[l] = 0;
+    __syncthreads();
+    for (int j = tid; j < kmax; j += PANEL_THREADS) {
+        const int o = win[j];
+        if (o >= base && o < base + nloc) isw[o - base] = 1;
+    }
+    cluster.sync();
+    // 5. L21 = A21 U11^-1 for the other rows, written to their final rows;
+    // CTA 0 writes the winners' block
+    for (int l = tid; l < nloc; l += PANEL_THREADS) {
+        if (isw[l]) continue;
+        const int o = base + l;
+        const int dest = o < kmax ? dtop[o] : o;
+        if (dest < kmax || dest >= a.m) continue;   // cannot happen: every displaced top row has a place
+        float *x = rows + l * WP;
+        for (int j = 0; j < kmax; j++) {
+            const float lj = x[j] * dinv[j];
+            x[j] = lj;
+            for (int c = j + 1; c < w; c++) x[c] = fmaf(-lj, ut[j * WP + c], x[c]);
+        }
+        for (int c = 0; c < w; c++) a.P[(i64)dest * a.rs + (i64)c * a.cs] = x[c];
+    }
+    if (rank == 0)
+        for (int e = tid; e < kmax * w; e += PANEL_THREADS)
+            a.P[(i64)(e / w) * a.rs + (i64)(e % w) * a.cs] = ut[(e / w) * WP + e % w];
+    // all DSMEM reads done before any CTA exits
+    cluster.sync();
+}
+
 // Fallback for panels that do not fit in one cluster's shared memory: one CTA
 // factors the panel in global memory (same arithmetic, same pivot rule).
 template <typename T>
@@ -605,8 +894,9 @@ int panel_factor(ddla_handle h, cudaStream_t s, View<T> X, i64 pc, int w, int32_
                  int *d_info, T *inv, int slot) {
     const i64 m = X.rows;
     int *tbuf;
-    DDLA_TRY(workspace(h, WS_PIV, sizeof(int) * (size_t)(2 * TOUCH_INTS + m), (void **)&tbuf));
+    DDLA_TRY(workspace(h, WS_PIV, sizeof(int) * (size_t)(2 * TOUCH_INTS + m + CALU_INTS), (void **)&tbuf));
     int *origin = tbuf + 2 * TOUCH_INTS;
+    int *calu = origin + m;
     tbuf += slot * TOUCH_INTS;
     int *tcount = tbuf, *trows = tbuf + 1, *tsrc = tbuf + 1 + LASWP_MAXT;
     PanelArgs<T> a;
@@ -622,11 +912,46 @@ int panel_factor(ddla_handle h, cudaStream_t s, View<T> X, i64 pc, int w, int32_
     a.touch_rows = trows;
     a.touch_src = tsrc;
     a.inv = inv;
+    a.calu = calu;
     int cs = max_cluster<T>(h);
     if (cs <= 0) return cs < 0 ? cs : DDLA_ERR_UNSUPPORTED;
     const int64_t want = tune_get("panel.cluster", 0);
     if (want > 0 && want < cs) cs = (int)want;
     const size_t avail = panel_smem_avail<T>();
+    if constexpr (sizeof(T) == 4) {
+        // tournament pivoting for the FP32 factorizations (tuning key panel.calu)
+        if (tune_get("panel.calu", 0) != 0 && w <= PANEL_WMAX) {
+            int use = 1;
+            while (use < cs && ((m + use - 1) / use > 512 || calu_smem_layout((int)((m + use - 1) / use), w).total > avail))
+                use *= 2;
+            const i64 rp = (m + use - 1) / use;
+            const size_t smem = calu_smem_layout((int)rp, w).total;
+            if (smem <= avail) {
+                static bool attr = false;
+                if (!attr) {
+                    DDLA_CUDA(cudaFuncSetAttribute(k_panel_calu, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+                    DDLA_CUDA(cudaFuncSetAttribute(k_panel_calu, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)avail));
+                    attr = true;
+                }
+                a.rows_per = (int)rp;
+                cudaLaunchConfig_t cfg = {};
+                cfg.gridDim = dim3(use);
+                cfg.blockDim = dim3(PANEL_THREADS);
+                cfg.dynamicSmemBytes = smem;
+                cfg.stream = s;
+                cudaLaunchAttribute attr1[1];
+                attr1[0].id = cudaLaunchAttributeClusterDimension;
+                attr1[0].val.clusterDim.x = use;
+                attr1[0].val.clusterDim.y = 1;
+                attr1[0].val.clusterDim.z = 1;
+                cfg.attrs = attr1;
+                cfg.numAttrs = 1;
+                DDLA_CUDA(cudaLaunchKernelEx(&cfg, k_panel_calu, a));
+                DDLA_LAUNCHED();
+                return 0;
+            }
+        }
+    }
     // smallest cluster that holds the rows with at most 512 rows per CTA
     int use = 1;
     while (use < cs && ((m + use - 1) / use > 512 ||
