@@ -139,8 +139,123 @@ __global__ void k_copy(const T *X, i64 rs, i64 cs, i64 m, i64 n, T *Y, i64 ld) {
     }
 }
 
+// The same factorizations with the block in registers: 1024 threads in a
+// 32 x 32 grid, thread (tr, tc) owning the R x R elements (tr R + u, tc R + v)
+// (R = 2 for bs <= 64, 4 for bs <= 128).  Per column: the owner of the
+// diagonal forms the pivot, the owners of the column (and, without pivoting,
+// of the row) publish the scaled column / the pivot row in shared memory,
+// every thread updates its elements -- two barriers per column and no index
+// arithmetic per element.  The arithmetic per element is k_diag's, operation
+// for operation, so the results are the same bits.
+template <typename T, int R>
+__global__ void __launch_bounds__(DIAG_THREADS)
+    k_diag_reg(T *A, i64 rs, i64 cs, int bs, int kind, int *info, i64 row_base) {
+    __shared__ T lcol[32 * R], urow[32 * R];
+    __shared__ T s_piv;
+    __shared__ int s_fail;
+    const int tid = threadIdx.x, tr = tid >> 5, tc = tid & 31;
+    T a[R][R];
+#pragma unroll
+    for (int u = 0; u < R; u++)
+#pragma unroll
+        for (int v = 0; v < R; v++) {
+            const int r = tr * R + u, c = tc * R + v;
+            a[u][v] = (r < bs && c < bs) ? A[r * rs + c * cs] : T(0);
+        }
+    const int last = (kind == DK_CHOL) ? bs : bs - 1;
+    for (int i = 0; i < last; i++) {
+        const int oi = i / R, li = i - oi * R;
+        if (tr == oi && tc == oi) {
+            T piv = T(0);
+#pragma unroll
+            for (int u = 0; u < R; u++)
+                if (u == li) piv = a[u][u];
+            bool fail = false;
+            if (kind == DK_CHOL) {
+                if (isfinite(piv) && piv <= T(0)) fail = true;
+                else {
+                    piv = sqrt(piv);
+                    if (!isfinite(piv) || piv == T(0)) fail = true;
+                }
+#pragma unroll
+                for (int u = 0; u < R; u++)
+                    if (u == li && !fail) a[u][u] = piv;
+            } else {
+                if (piv == T(0) || (kind == DK_LDLT && !isfinite(piv))) fail = true;
+            }
+            s_piv = piv;
+            s_fail = fail ? 1 : 0;
+        }
+        __syncthreads();
+        if (s_fail) {
+            if (tid == 0) atomicMin(info, (int)(row_base + i + 1));
+            break;
+        }
+        const T piv = s_piv, rinv = T(1) / piv;
+        if (tc == oi) {
+#pragma unroll
+            for (int u = 0; u < R; u++) {
+                const int r = tr * R + u;
+#pragma unroll
+                for (int v = 0; v < R; v++)
+                    if (v == li && r > i && r < bs) {
+                        const T l = a[u][v] * rinv;
+                        a[u][v] = l;
+                        lcol[r] = l;
+                    }
+            }
+        }
+        if (kind == DK_LU_NOPIV && tr == oi) {
+#pragma unroll
+            for (int u = 0; u < R; u++)
+                if (u == li)
+#pragma unroll
+                    for (int v = 0; v < R; v++) {
+                        const int c = tc * R + v;
+                        if (c > i && c < bs) urow[c] = a[u][v];
+                    }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int u = 0; u < R; u++) {
+            const int r = tr * R + u;
+            if (r <= i || r >= bs) continue;
+            const T lr = lcol[r];
+            const T sc = (kind == DK_CHOL) ? -lr : -piv * lr;
+#pragma unroll
+            for (int v = 0; v < R; v++) {
+                const int c = tc * R + v;
+                if (c <= i || c >= bs) continue;
+                if (kind == DK_LU_NOPIV) a[u][v] = fma(lr, -urow[c], a[u][v]);
+                else if (c <= r) a[u][v] = fma(lcol[c], sc, a[u][v]);
+            }
+        }
+    }
+#pragma unroll
+    for (int u = 0; u < R; u++)
+#pragma unroll
+        for (int v = 0; v < R; v++) {
+            const int r = tr * R + u, c = tc * R + v;
+            if (r >= bs || c >= bs) continue;
+            if (kind != DK_LU_NOPIV && c > r) continue;   // only the factored triangle
+            A[r * rs + c * cs] = a[u][v];
+        }
+}
+
 template <typename T>
 int diag_kernel(ddla_handle h, View<T> A11, int bs, int kind, i64 row_base) {
+    if (bs <= 64) {
+        k_diag_reg<T, 2><<<1, DIAG_THREADS, 0, h->stream>>>(A11.p, A11.rs, A11.cs, bs, kind, h->d_info + INFO_PIVOT,
+                                                           row_base);
+        DDLA_LAUNCHED();
+        return 0;
+    }
+    if (sizeof(T) == 4 && bs <= 128) {   // (4 x 4 doubles per thread would spill)
+        k_diag_reg<T, 4><<<1, DIAG_THREADS, 0, h->stream>>>(A11.p, A11.rs, A11.cs, bs, kind, h->d_info + INFO_PIVOT,
+                                                           row_base);
+        DDLA_LAUNCHED();
+        return 0;
+    }
     size_t smem = sizeof(T) * (size_t)bs * (bs + 1);
     static size_t avail[2] = {0, 0};
     if (!avail[sizeof(T) == 8]) DDLA_TRY(max_dyn_smem((const void *)k_diag<T>, h->smem_optin, &avail[sizeof(T) == 8]));

@@ -51,36 +51,53 @@ __global__ void k_copy2d(const T *X, i64 rs, i64 cs, i64 m, i64 n, T *Y, i64 yrs
 // Inverse of each TB x TB diagonal block of tri(A) (lower/upper, unit or not),
 // stored row-major per block, zero outside the triangle.  One thread per
 // column of the identity; forward (lower) or backward (upper) substitution.
+// Column c of the inverse by column-oriented substitution: one warp per
+// column, lanes own rows lane and lane + 32; the finished entry y_k is
+// broadcast with a shuffle and the lanes below (above, for upper) subtract
+// its column of L.  16 warps, so the 64 columns take 4 passes.
+constexpr int TI_THREADS = 512;
+
 template <typename T>
-__global__ void __launch_bounds__(TB) k_tri_inv(const T *A, i64 rs, i64 cs, i64 n, int lower, int unit, T *inv) {
+__global__ void __launch_bounds__(TI_THREADS) k_tri_inv(const T *A, i64 rs, i64 cs, i64 n, int lower, int unit, T *inv) {
     __shared__ T L[TB][TB + 1];
-    __shared__ T Y[TB][TB + 1];
-    const int b = blockIdx.x, c = threadIdx.x;
+    __shared__ T dinv[TB];
+    const int b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const i64 r0 = (i64)b * TB;
     const int bs = (int)(n - r0 < TB ? n - r0 : TB);
-    for (int i = 0; i < TB; i++) {
+    for (int e = tid; e < TB * TB; e += TI_THREADS) {
+        const int i = e / TB, c = e % TB;
         L[i][c] = (i < bs && c < bs) ? A[(r0 + i) * rs + (r0 + c) * cs] : T(0);
-        Y[i][c] = T(0);
     }
     __syncthreads();
-    if (c < bs) {
-        if (lower) {
-            for (int r = c; r < bs; r++) {
-                T s = (r == c) ? T(1) : T(0);
-                for (int k = c; k < r; k++) s -= L[r][k] * Y[k][c];
-                Y[r][c] = unit ? s : s / L[r][r];
-            }
-        } else {
-            for (int r = c; r >= 0; r--) {
-                T s = (r == c) ? T(1) : T(0);
-                for (int k = r + 1; k <= c; k++) s -= L[r][k] * Y[k][c];
-                Y[r][c] = unit ? s : s / L[r][r];
-            }
-        }
-    }
+    if (tid < TB) dinv[tid] = (tid < bs && !unit) ? T(1) / L[tid][tid] : T(1);
     __syncthreads();
     T *out = inv + (i64)b * TB * TB;
-    for (int i = 0; i < TB; i++) out[i * TB + c] = Y[i][c];
+    for (int c = warp; c < TB; c += TI_THREADS / 32) {
+        T y0 = (lane == c) ? T(1) : T(0), y1 = (lane + 32 == c) ? T(1) : T(0);
+        if (c < bs) {
+            if (lower) {
+                for (int k = c; k < bs; k++) {
+                    const T yk = __shfl_sync(0xffffffffu, k < 32 ? y0 : y1, k & 31) * dinv[k];
+                    if (lane == k) y0 = yk;
+                    if (lane + 32 == k) y1 = yk;
+                    if (lane > k && lane < bs) y0 -= L[lane][k] * yk;
+                    if (lane + 32 > k && lane + 32 < bs) y1 -= L[lane + 32][k] * yk;
+                }
+            } else {
+                for (int k = c; k >= 0; k--) {
+                    const T yk = __shfl_sync(0xffffffffu, k < 32 ? y0 : y1, k & 31) * dinv[k];
+                    if (lane == k) y0 = yk;
+                    if (lane + 32 == k) y1 = yk;
+                    if (lane < k) y0 -= L[lane][k] * yk;
+                    if (lane + 32 < k) y1 -= L[lane + 32][k] * yk;
+                }
+            }
+        } else {
+            y0 = y1 = T(0);
+        }
+        out[lane * TB + c] = lane < bs ? y0 : T(0);
+        out[(lane + 32) * TB + c] = lane + 32 < bs ? y1 : T(0);
+    }
 }
 
 __device__ __forceinline__ int ld_acquire(const int *p) {
@@ -581,7 +598,7 @@ int gemm_any(ddla_handle h, int prec, i64 m, i64 n, i64 k, T alpha, View<const T
 template <typename T>
 int tri_inverse_on(cudaStream_t s, bool lower, bool unit, View<const T> A, i64 n, T *inv) {
     int nblk = (int)((n + TB - 1) / TB);
-    k_tri_inv<T><<<nblk, TB, 0, s>>>(A.p, A.rs, A.cs, n, lower ? 1 : 0, unit ? 1 : 0, inv);
+    k_tri_inv<T><<<nblk, TI_THREADS, 0, s>>>(A.p, A.rs, A.cs, n, lower ? 1 : 0, unit ? 1 : 0, inv);
     DDLA_LAUNCHED();
     return 0;
 }
@@ -755,7 +772,7 @@ extern "C" int ddla_dev_dtrsv_noalloc(void *stream, int32_t uplo, int32_t trans,
         A = A.t();
         lower = !lower;
     }
-    k_tri_inv<double><<<nblk, TB, 0, s>>>(A.p, A.rs, A.cs, n, lower ? 1 : 0, diag == DDLA_UNIT_DIAG ? 1 : 0, inv);
+    k_tri_inv<double><<<nblk, TI_THREADS, 0, s>>>(A.p, A.rs, A.cs, n, lower ? 1 : 0, diag == DDLA_UNIT_DIAG ? 1 : 0, inv);
     DDLA_LAUNCHED();
     const int nr = (int)nrhs;
 #define NOALLOC_CHAIN(NRV)                                                                                      \
