@@ -220,6 +220,7 @@ def secondary(args):
     flush = None
     check_err = None
     bytes_alg = 0.0
+    last_rep = {}
 
     def U(*shape):
         return torch.rand(*shape, dtype=torch.float64, device="cuda", generator=g) * 2 - 1
@@ -420,6 +421,7 @@ def secondary(args):
                 rc, rep = h.gesv_mixed(A, b, X, precision=prec, tol=TOL, spd=True)
                 if rc != 0 or not rep["converged"]:
                     raise RuntimeError(f"posv_mixed failed rc={rc} rep={rep}")
+                last_rep.update(rep)
 
         def check_err():
             step()
@@ -528,6 +530,7 @@ def secondary(args):
            "config": {"workload": desc, "precision": pname,
                       "l2": "L2 flushed between steps" if flush else "inputs larger than L2"},
            "error": err, "roofline": roof, "gpu_launches": launches, "clocks": clk, "classes": classes,
+           "solve_report": {k: last_rep[k] for k in ("iterations", "factor_ms", "refine_ms") if k in last_rep} or None,
            "peaks_live": {"fp64_tflops": f64_peak, "fp32_tflops": f32_peak}}
     print(json.dumps(out))
     h.close()

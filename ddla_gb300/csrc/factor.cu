@@ -139,21 +139,20 @@ __global__ void k_copy(const T *X, i64 rs, i64 cs, i64 m, i64 n, T *Y, i64 ld) {
     }
 }
 
-// The same factorizations with the block in registers: 1024 threads in a
-// 32 x 32 grid, thread (tr, tc) owning the R x R elements (tr R + u, tc R + v)
-// (R = 2 for bs <= 64, 4 for bs <= 128).  Per column: the owner of the
+// The same factorizations with the block in registers: G x G threads,
+// thread (tr, tc) owning the R x R elements (tr R + u, tc R + v).  Per column: the owner of the
 // diagonal forms the pivot, the owners of the column (and, without pivoting,
 // of the row) publish the scaled column / the pivot row in shared memory,
 // every thread updates its elements -- two barriers per column and no index
 // arithmetic per element.  The arithmetic per element is k_diag's, operation
 // for operation, so the results are the same bits.
-template <typename T, int R>
-__global__ void __launch_bounds__(DIAG_THREADS)
+template <typename T, int R, int G>
+__global__ void __launch_bounds__(G *G)
     k_diag_reg(T *A, i64 rs, i64 cs, int bs, int kind, int *info, i64 row_base) {
-    __shared__ T lcol[32 * R], urow[32 * R];
+    __shared__ T lcol[G * R], urow[G * R];
     __shared__ T s_piv;
     __shared__ int s_fail;
-    const int tid = threadIdx.x, tr = tid >> 5, tc = tid & 31;
+    const int tid = threadIdx.x, tr = tid / G, tc = tid % G;
     T a[R][R];
 #pragma unroll
     for (int u = 0; u < R; u++)
@@ -244,17 +243,21 @@ __global__ void __launch_bounds__(DIAG_THREADS)
 
 template <typename T>
 int diag_kernel(ddla_handle h, View<T> A11, int bs, int kind, i64 row_base) {
+    // 16 x 16 threads (8 warps: cheap barriers) with 4 x 4 elements each for
+    // bs <= 64; 32 x 32 threads with 4 x 4 FP32 elements for bs <= 128
     if (bs <= 64) {
-        k_diag_reg<T, 2><<<1, DIAG_THREADS, 0, h->stream>>>(A11.p, A11.rs, A11.cs, bs, kind, h->d_info + INFO_PIVOT,
-                                                           row_base);
+        k_diag_reg<T, 4, 16><<<1, 256, 0, h->stream>>>(A11.p, A11.rs, A11.cs, bs, kind, h->d_info + INFO_PIVOT,
+                                                       row_base);
         DDLA_LAUNCHED();
         return 0;
     }
-    if (sizeof(T) == 4 && bs <= 128) {   // (4 x 4 doubles per thread would spill)
-        k_diag_reg<T, 4><<<1, DIAG_THREADS, 0, h->stream>>>(A11.p, A11.rs, A11.cs, bs, kind, h->d_info + INFO_PIVOT,
-                                                           row_base);
-        DDLA_LAUNCHED();
-        return 0;
+    if constexpr (sizeof(T) == 4) {   // (4 x 4 doubles per thread would spill at 1024 threads)
+        if (bs <= 128) {
+            k_diag_reg<T, 4, 32><<<1, DIAG_THREADS, 0, h->stream>>>(A11.p, A11.rs, A11.cs, bs, kind,
+                                                                   h->d_info + INFO_PIVOT, row_base);
+            DDLA_LAUNCHED();
+            return 0;
+        }
     }
     size_t smem = sizeof(T) * (size_t)bs * (bs + 1);
     static size_t avail[2] = {0, 0};
