@@ -165,19 +165,19 @@ int residual_nr(cudaStream_t s, i64 n, const double *A, const double *X, const d
     return 0;
 }
 
-int residual(cudaStream_t s, i64 n, int nr, const double *A, const double *X, const double *B, double *R) {
+int residual(ddla_handle h, i64 n, int nr, const double *A, const double *X, const double *B, double *R) {
+    cudaStream_t s = h->stream;
     switch (nr) {
         case 1: return residual_nr<1>(s, n, A, X, B, R);
         case 2: return residual_nr<2>(s, n, A, X, B, R);
-        case 4: return residual_nr<4>(s, n, A, X, B, R);
-        case 8: return residual_nr<8>(s, n, A, X, B, R);
-        case 16: return residual_nr<16>(s, n, A, X, B, R);
         default: break;
     }
-    // generic width: FP64 GEMM on the DMMA path (R = B - A X)
+    // 3 or more right-hand sides: FP64 GEMM on the DMMA path (R = B - A X),
+    // k split over extra CTAs when the n x nr result has few tiles (the
+    // row-sum kernel above reaches ~0.55 of the FP64 peak at 16 columns)
     DDLA_CUDA(cudaMemcpyAsync(R, B, sizeof(double) * n * nr, cudaMemcpyDeviceToDevice, s));
-    return gemm_f64(s, n, nr, n, -1.0, View<const double>{A, n, n, n, 1}, View<const double>{X, n, nr, nr, 1}, 1.0,
-                    View<double>{R, n, nr, nr, 1});
+    return gemm_f64_struct_h(h, n, nr, n, -1.0, View<const double>{A, n, n, n, 1}, OP_DENSE,
+                             View<const double>{X, n, nr, nr, 1}, OP_DENSE, 1.0, View<double>{R, n, nr, nr, 1});
 }
 
 double u64d(unsigned long long v) { return __builtin_bit_cast(double, v); }
@@ -305,7 +305,7 @@ int refine(ddla_handle h, i64 n, int nr, const double *A, const double *B, doubl
     }
     std::vector<unsigned long long> hn(1 + 3 * MAX_RHS);
     for (;;) {
-        DDLA_TRY(residual(s, n, nr, A, X, B, R));
+        DDLA_TRY(residual(h, n, nr, A, X, B, R));
         DDLA_CUDA(cudaMemsetAsync(norms + 1 + nr, 0, sizeof(unsigned long long) * 2 * nr, s));
         k_colmax_abs<<<grid1(tot), 256, 0, s>>>(X, n, nr, norms + 1 + nr);
         DDLA_LAUNCHED();

@@ -112,14 +112,19 @@ __device__ __forceinline__ void st_release(int *p, int v) {
 // Whole-system solve with <= NR right-hand sides, X row-major n x ldx.
 // Thread t works on block row r = t/4, k-quarter q = t%4 (16 columns of the
 // tile), reduces its partial dot products over the 4 threads of the row.
-template <typename T, int NR>
-__global__ void __launch_bounds__(CHAIN_THREADS)
+// G groups of 256 threads split the right-hand sides (NR / G each), so the
+// tile products on the chain's critical path are shorter for 16 of them.
+template <typename T, int NR, int G>
+__global__ void __launch_bounds__(CHAIN_THREADS *G)
     k_trsv_chain(i64 n, int nblk, const T *__restrict__ A, i64 rs, i64 cs, int lower, const T *__restrict__ inv,
                  T *X, i64 ldx, int nr, int *flags, int *ticket, int *err) {
+    constexpr int NC = NR / G;
+    constexpr int NT = CHAIN_THREADS * G;
     __shared__ T s_acc[TB][NR];
     __shared__ T s_x[TB][NR];
     __shared__ int s_blk, s_abort;
-    const int t = threadIdx.x, r = t >> 2, q = t & 3;
+    const int t = threadIdx.x, g = t / CHAIN_THREADS, tt = t % CHAIN_THREADS, r = tt >> 2, q = tt & 3;
+    const int cb = g * NC;
     if (t == 0) {
         s_blk = atomicAdd(ticket, 1);
         s_abort = 0;
@@ -129,7 +134,7 @@ __global__ void __launch_bounds__(CHAIN_THREADS)
     const int blk = lower ? logical : nblk - 1 - logical;
     const i64 r0 = (i64)blk * TB;
     const int rows = (int)(n - r0 < TB ? n - r0 : TB);
-    for (int e = t; e < TB * NR; e += CHAIN_THREADS) {
+    for (int e = t; e < TB * NR; e += NT) {
         int i = e / NR, c = e % NR;
         s_acc[i][c] = (i < rows && c < nr) ? X[(r0 + i) * ldx + c] : T(0);
     }
@@ -158,26 +163,26 @@ __global__ void __launch_bounds__(CHAIN_THREADS)
         }
         __syncthreads();
         if (s_abort) return;
-        for (int e = t; e < TB * NR; e += CHAIN_THREADS) {
+        for (int e = t; e < TB * NR; e += NT) {
             int i = e / NR, c = e % NR;
             s_x[i][c] = (i < cols && c < nr) ? __ldcg(&X[(c0 + i) * ldx + c]) : T(0);
         }
         __syncthreads();
-        T p[NR];
+        T p[NC];
 #pragma unroll
-        for (int c = 0; c < NR; c++) p[c] = T(0);
+        for (int c = 0; c < NC; c++) p[c] = T(0);
 #pragma unroll
         for (int k = 0; k < 16; k++)
 #pragma unroll
-            for (int c = 0; c < NR; c++) p[c] += a[k] * s_x[q * 16 + k][c];
+            for (int c = 0; c < NC; c++) p[c] += a[k] * s_x[q * 16 + k][cb + c];
 #pragma unroll
-        for (int c = 0; c < NR; c++) {
+        for (int c = 0; c < NC; c++) {
             p[c] += __shfl_xor_sync(0xffffffffu, p[c], 1);
             p[c] += __shfl_xor_sync(0xffffffffu, p[c], 2);
         }
         if (q == 0)
 #pragma unroll
-            for (int c = 0; c < NR; c++) s_acc[r][c] -= p[c];
+            for (int c = 0; c < NC; c++) s_acc[r][cb + c] -= p[c];
         __syncthreads();
     }
     // x_blk = inv(A_blk,blk) * acc
@@ -186,20 +191,21 @@ __global__ void __launch_bounds__(CHAIN_THREADS)
         T a[16];
 #pragma unroll
         for (int k = 0; k < 16; k++) a[k] = iv[r * TB + q * 16 + k];
-        T p[NR];
+        T p[NC];
 #pragma unroll
-        for (int c = 0; c < NR; c++) p[c] = T(0);
+        for (int c = 0; c < NC; c++) p[c] = T(0);
 #pragma unroll
         for (int k = 0; k < 16; k++)
 #pragma unroll
-            for (int c = 0; c < NR; c++) p[c] += a[k] * s_acc[q * 16 + k][c];
+            for (int c = 0; c < NC; c++) p[c] += a[k] * s_acc[q * 16 + k][cb + c];
 #pragma unroll
-        for (int c = 0; c < NR; c++) {
+        for (int c = 0; c < NC; c++) {
             p[c] += __shfl_xor_sync(0xffffffffu, p[c], 1);
             p[c] += __shfl_xor_sync(0xffffffffu, p[c], 2);
         }
         if (q == 0 && r < rows)
-            for (int c = 0; c < nr; c++) X[(r0 + r) * ldx + c] = p[c];
+            for (int c = 0; c < NC; c++)
+                if (cb + c < nr) X[(r0 + r) * ldx + cb + c] = p[c];
     }
     __syncthreads();
     if (t == 0) {
@@ -581,8 +587,10 @@ int cluster_solve(ddla_handle h, int cs, i64 n, int nblk, View<const T> A, bool 
 template <typename T, int NR>
 int chain(ddla_handle h, i64 n, int nblk, View<const T> A, bool lower, const T *inv, T *X, i64 ldx, int nr,
           int *flags) {
-    k_trsv_chain<T, NR><<<nblk, CHAIN_THREADS, 0, h->stream>>>(n, nblk, A.p, A.rs, A.cs, lower ? 1 : 0, inv, X, ldx,
-                                                              nr, flags, flags + nblk, h->d_info + INFO_TIMEOUT);
+    constexpr int G = NR >= 16 ? 4 : 1;
+    k_trsv_chain<T, NR, G><<<nblk, CHAIN_THREADS * G, 0, h->stream>>>(n, nblk, A.p, A.rs, A.cs, lower ? 1 : 0, inv, X,
+                                                                      ldx, nr, flags, flags + nblk,
+                                                                      h->d_info + INFO_TIMEOUT);
     DDLA_LAUNCHED();
     return 0;
 }
@@ -775,9 +783,9 @@ extern "C" int ddla_dev_dtrsv_noalloc(void *stream, int32_t uplo, int32_t trans,
     k_tri_inv<double><<<nblk, TI_THREADS, 0, s>>>(A.p, A.rs, A.cs, n, lower ? 1 : 0, diag == DDLA_UNIT_DIAG ? 1 : 0, inv);
     DDLA_LAUNCHED();
     const int nr = (int)nrhs;
-#define NOALLOC_CHAIN(NRV)                                                                                      \
-    k_trsv_chain<double, NRV><<<nblk, CHAIN_THREADS, 0, s>>>(n, nblk, A.p, A.rs, A.cs, lower ? 1 : 0, inv, x, ldx, \
-                                                             nr, flags, ticket, err)
+#define NOALLOC_CHAIN(NRV)                                                                                  \
+    k_trsv_chain<double, NRV, 1><<<nblk, CHAIN_THREADS, 0, s>>>(n, nblk, A.p, A.rs, A.cs, lower ? 1 : 0, inv, x, \
+                                                                ldx, nr, flags, ticket, err)
     if (nr <= 1) NOALLOC_CHAIN(1);
     else if (nr <= 2) NOALLOC_CHAIN(2);
     else if (nr <= 4) NOALLOC_CHAIN(4);
