@@ -620,23 +620,47 @@ constexpr int OZ_S = 8, OZ_BETA = 7;
 constexpr int OZ_EXACT = 5;               // levels with their own exact accumulator
 constexpr int OZ_NACC = OZ_EXACT + 1;     // + one shared accumulator for the small levels
 constexpr int OZ_TN = 32;                 // tile columns
-constexpr int OZ_KC = 64;                 // K staged per chunk (bf16)
+constexpr int OZ_KC = 32;                 // K staged per chunk (bf16)
+constexpr int OZ_NS = 2;                  // shared-memory stages (chunks in flight)
 constexpr int OZ_SBO = (OZ_KC / 8) * 128; // bf16 core-matrix layout: 8 elements per 16-byte chunk
 constexpr int OZ_A_TILE = TM * OZ_KC * 2, OZ_B_TILE = OZ_TN * OZ_KC * 2;
-constexpr size_t OZ_SMEM = (size_t)OZ_S * (OZ_A_TILE + OZ_B_TILE);
-constexpr int OZ_TMEM_COLS = 256;         // OZ_NACC x 32 columns, rounded up to a power of two
-static_assert(OZ_NACC * OZ_TN <= OZ_TMEM_COLS, "TMEM columns");
-static_assert((size_t)TM * (OZ_TN + 1) * 8 <= OZ_SMEM, "epilogue staging");
+constexpr int OZ_STAGE = OZ_S * (OZ_A_TILE + OZ_B_TILE);   // every slice of one K chunk
+constexpr size_t OZ_SMEM = (size_t)OZ_NS * OZ_STAGE;
+// two buffers of OZ_NACC accumulators (OZ_TN columns each): the MMAs of a new
+// flush period write one while the previous period's sums are read from the other
+constexpr int OZ_TMEM_COLS = 512;
+static_assert(2 * OZ_NACC * OZ_TN <= OZ_TMEM_COLS, "TMEM columns");
 
 // Flush period of accumulator a in K chunks: level l sums (l+1) slice pairs of
-// products below (2^beta - 1)^2 ulps, exact while (l+1) * period * 127^2 < 2^24.
+// products below (2^beta - 1)^2 ulps, exact while (l+1) * period * OZ_KC *
+// 127^2 < 2^24.  The shared small-level accumulator (a = OZ_EXACT) rounds
+// anyway; its period bounds that rounding.
 __host__ __device__ constexpr int oz_period(int a) {
-    return a == 0 ? 16 : a == 1 ? 8 : a == 2 ? 4 : a == 3 ? 4 : a == 4 ? 2 : 16;
+    return a == 0 ? 32 : a == 1 ? 16 : a == 2 ? 8 : a == 3 ? 8 : a == 4 ? 4 : 32;
 }
-static_assert(1 * 16 * OZ_KC * 127 * 127 < (1 << 24) && 2 * 8 * OZ_KC * 127 * 127 < (1 << 24) &&
-                  3 * 4 * OZ_KC * 127 * 127 < (1 << 24) && 4 * 4 * OZ_KC * 127 * 127 < (1 << 24) &&
-                  5 * 2 * OZ_KC * 127 * 127 < (1 << 24),
+// Phase of each accumulator's flush periods: a period of accumulator a ends
+// before chunk c when (c + oz_phase(a)) % oz_period(a) == 0.  The phases put
+// at most one flush on any chunk (a = 4 on c = 0 mod 4, a = 3 / 2 on c = 2 / 6
+// mod 8, a = 1 on c = 1 mod 16, a = 0 / 5 on c = 3 / 19 mod 32), so the FP64
+// flush work spreads evenly under the MMAs.  The first period of an
+// accumulator is shorter than oz_period, never longer.
+__host__ __device__ constexpr int oz_phase(int a) {
+    return a == 0 ? 29 : a == 1 ? 15 : a == 2 ? 2 : a == 3 ? 6 : a == 4 ? 0 : 13;
+}
+static_assert(1 * 32 * OZ_KC * 127 * 127 < (1 << 24) && 2 * 16 * OZ_KC * 127 * 127 < (1 << 24) &&
+                  3 * 8 * OZ_KC * 127 * 127 < (1 << 24) && 4 * 8 * OZ_KC * 127 * 127 < (1 << 24) &&
+                  5 * 4 * OZ_KC * 127 * 127 < (1 << 24),
               "exact accumulation periods");
+
+// FP32 -> FP64 by the IEEE field layout (exponent rebias 1023 - 127 = 896,
+// mantissa shifted by 52 - 23 = 29) on the integer pipe.  Only for zeros and
+// normal values, which is all the level sums hold: they are multiples of
+// 2^-(beta (OZ_S - 1)) far above the FP32 subnormal range, and finite.
+__device__ __forceinline__ double oz_f2d(uint32_t u) {
+    const uint32_t mag = u & 0x7fffffffu;
+    const uint32_t hi = (u & 0x80000000u) | (mag ? (mag >> 3) + (896u << 20) : 0u);
+    return __hiloint2double((int)hi, (int)(u << 29));
+}
 
 __device__ __forceinline__ int oz_off(int r, int k) {   // byte offset of bf16 element (r, k) in a tile
     return (r >> 3) * OZ_SBO + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2;
@@ -750,11 +774,32 @@ struct OzArgs {
     int *err;
 };
 
-__global__ void __launch_bounds__(TC_THREADS, 1) k_oz_gemm(OzArgs g) {
+// One CTA per 128 x OZ_TN tile of C, OZ_THREADS threads.  Warp 8 (lane 0) is
+// the issuer: it moves each K chunk's slices (OZ_S A tiles + OZ_S B tiles,
+// contiguous in the packed layout) with bulk asynchronous copies into one of
+// OZ_NS shared-memory stages and issues the chunk's slice-pair MMAs into the
+// accumulators of the running flush periods.  Warps 0-7 are the flushers: for
+// every chunk f they wait for its MMAs and add the accumulator whose period
+// ended with f into FP64 registers, while the issuer runs ahead on the other
+// TMEM buffer.  Warp w < 8 reads TMEM lanes 32 (w % 4).. and columns
+// 16 (w / 4).. of each accumulator, so it owns 16 columns of one row of C.
+// Barriers (all waits bounded):
+//   full[st]   copies of a stage landed        (issuer waits)
+//   mdone[st]  MMAs that read a stage retired  (issuer waits, then reloads it)
+//   mready[f % 4]  MMAs of chunk f retired      (flushers wait)
+//   fdone[f % 4]   flush of chunk f done, one arrival per flusher warp
+//                                              (issuer waits)
+// The issuer starts chunk c only after flush c - 3, so
+//   each ring slot completes again only after its previous phase was awaited;
+//   a buffer refilled at chunk c was flushed at f = c - oz_period - 1 <= c - 5.
+constexpr int OZ_THREADS = 288;
+constexpr int OZ_RING = 4;
+
+__global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_gemm(OzArgs g) {
     extern __shared__ __align__(1024) unsigned char smem[];
-    unsigned char *At = smem, *Bt = smem + (size_t)OZ_S * OZ_A_TILE;
-    __shared__ __align__(8) unsigned long long mbar;
+    __shared__ __align__(8) unsigned long long full[OZ_NS], mdone[OZ_NS], mready[OZ_RING], fdone[OZ_RING];
     __shared__ unsigned tmem_slot;
+    __shared__ volatile int abort_flag;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int64_t mt = blockIdx.y, nt = blockIdx.x, bz = blockIdx.z;
     const __nv_bfloat16 *Ap = g.Ap + bz * g.a_item, *Bp = g.Bp + bz * g.b_item;
@@ -770,129 +815,183 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_oz_gemm(OzArgs g) {
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&mbar)) : "memory");
+        for (int st = 0; st < OZ_NS; st++) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&full[st])) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&mdone[st])) : "memory");
+        }
+        for (int r = 0; r < OZ_RING; r++) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&mready[r])) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 8;" ::"r"(su32(&fdone[r])) : "memory");
+        }
+        abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const unsigned tmem = tmem_slot;
-    const uint32_t id = oz_idesc();
-    unsigned phase = 0;
-    bool failed = false;
-    // FP64 accumulation: warp w reads TMEM lanes 32*(w%4).. of the accumulators
-    // in its group's mask (flush work balanced between the two halves)
-    const int q = warp & 3;
-    const unsigned mymask = (warp < 4) ? 0x13u : 0x2cu;   // {0,1,4} / {2,3,5}
-    double acc[OZ_TN];
-#pragma unroll
-    for (int j = 0; j < OZ_TN; j++) acc[j] = 0.0;
-    const size_t a_stride = (size_t)g.mtiles * g.kchunks * (TM * OZ_KC);     // elements between slices
-    const size_t b_stride = (size_t)g.ntiles * g.kchunks * (OZ_TN * OZ_KC);
-    for (int64_t c = 0; c < g.kchunks; c++) {
-        {   // stage every slice of this chunk: contiguous 16-byte copies
-            const uint4 *srcA = reinterpret_cast<const uint4 *>(Ap + ((size_t)mt * g.kchunks + c) * (TM * OZ_KC));
-            const uint4 *srcB =
-                reinterpret_cast<const uint4 *>(Bp + ((size_t)nt * g.kchunks + c) * (OZ_TN * OZ_KC));
-            constexpr int AV = OZ_A_TILE / 16, BV = OZ_B_TILE / 16;
-            for (int e = tid; e < OZ_S * AV; e += TC_THREADS) {
-                const int t = e / AV, o = e % AV;
-                reinterpret_cast<uint4 *>(At)[e] = srcA[(size_t)t * (a_stride / 8) + o];
-            }
-            for (int e = tid; e < OZ_S * BV; e += TC_THREADS) {
-                const int u = e / BV, o = e % BV;
-                reinterpret_cast<uint4 *>(Bt)[e] = srcB[(size_t)u * (b_stride / 8) + o];
-            }
+    const int K = (int)g.kchunks;
+    // bounded wait; flushers also give up once the issuer has aborted
+    auto wait_mb = [&](unsigned long long *mb, unsigned ph, bool watch) -> bool {
+        for (long long it = 0; it < TC_SPIN; it++) {
+            if (mbar_try(su32(mb), ph)) return true;
+            if (watch && abort_flag) return false;
         }
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
-        if (tid == 0) {
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            unsigned started = 0;
-            for (int t = 0; t < OZ_S; t++)
-                for (int u = 0; t + u < OZ_S; u++) {
-                    const int a = (t + u < OZ_EXACT) ? t + u : OZ_EXACT;
-                    const bool fresh = (c % oz_period(a)) == 0 && !((started >> a) & 1u);
-                    started |= 1u << a;
-                    const unsigned dcol = tmem + (unsigned)(a * OZ_TN);
-                    for (int ks = 0; ks < OZ_KC / 16; ks++) {
-                        const uint64_t ad = oz_desc(su32(At + (size_t)t * OZ_A_TILE) + ks * 256);
-                        const uint64_t bd = oz_desc(su32(Bt + (size_t)u * OZ_B_TILE) + ks * 256);
-                        const int accum = (fresh && ks == 0) ? 0 : 1;
-                        asm volatile(
-                            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-                            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dcol),
-                            "l"(ad), "l"(bd), "r"(id), "r"(accum)
-                            : "memory");
+        return false;
+    };
+    // buffer of accumulator a while chunk c is accumulated
+    auto buf = [](int a, int c) -> unsigned { return (unsigned)(((c + oz_phase(a)) / oz_period(a)) & 1); };
+    bool failed = false;
+    if (warp == 8) {
+        if (lane == 0) {
+            const uint32_t id = oz_idesc();
+            const size_t a_stride = (size_t)g.mtiles * K * (TM * OZ_KC);     // elements between slices
+            const size_t b_stride = (size_t)g.ntiles * K * (OZ_TN * OZ_KC);
+            auto load = [&](int c, int st) {   // every slice of chunk c into stage st
+                unsigned char *base = smem + (size_t)st * OZ_STAGE;
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(&full[st])),
+                             "r"((unsigned)OZ_STAGE)
+                             : "memory");
+                const __nv_bfloat16 *a = Ap + ((size_t)mt * K + c) * (TM * OZ_KC);
+                const __nv_bfloat16 *b = Bp + ((size_t)nt * K + c) * (OZ_TN * OZ_KC);
+                for (int t = 0; t < OZ_S; t++)
+                    bulk_g2s(su32(base + (size_t)t * OZ_A_TILE), a + t * a_stride, OZ_A_TILE, su32(&full[st]));
+                for (int u = 0; u < OZ_S; u++)
+                    bulk_g2s(su32(base + (size_t)OZ_S * OZ_A_TILE + (size_t)u * OZ_B_TILE), b + u * b_stride,
+                             OZ_B_TILE, su32(&full[st]));
+            };
+            // chunk of the copy / MMA batch in flight per stage (-1: none), for the drain
+            int ld_c[OZ_NS], mm_last = -1;
+            for (int st = 0; st < OZ_NS; st++) ld_c[st] = -1;
+            for (int st = 0; st < OZ_NS && st < K; st++) {
+                load(st, st);
+                ld_c[st] = st;
+            }
+            for (int c = 0; c < K; c++) {
+                const int s = c % OZ_NS;
+                if (!wait_mb(&full[s], (unsigned)(c / OZ_NS) & 1u, false)) { failed = true; break; }
+                ld_c[s] = -1;
+                if (c >= 3 && !wait_mb(&fdone[(c - 3) % OZ_RING], (unsigned)((c - 3) / OZ_RING) & 1u, false)) {
+                    failed = true;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                // per accumulator: its TMEM buffer and whether this chunk starts a period
+                unsigned dcol[OZ_NACC], fresh = 0;
+#pragma unroll
+                for (int a = 0; a < OZ_NACC; a++) {
+                    dcol[a] = tmem + (buf(a, c) * OZ_NACC + (unsigned)a) * OZ_TN;
+                    if (c == 0 || (c + oz_phase(a)) % oz_period(a) == 0) fresh |= 1u << a;
+                }
+                const unsigned char *At = smem + (size_t)s * OZ_STAGE;
+                const uint64_t ad0 = oz_desc(su32(At)), bd0 = oz_desc(su32(At + (size_t)OZ_S * OZ_A_TILE));
+                // slice pairs (t, u), t + u < OZ_S; the first pair of level a is (0, a)
+#pragma unroll
+                for (int t = 0; t < OZ_S; t++)
+#pragma unroll
+                    for (int u = 0; u < OZ_S - t; u++) {
+                        const int a = (t + u < OZ_EXACT) ? t + u : OZ_EXACT;
+                        const bool first = t == 0 && u == a;
+#pragma unroll
+                        for (int ks = 0; ks < OZ_KC / 16; ks++) {
+                            // descriptor start addresses are in 16-byte units
+                            const uint64_t ad = ad0 + (uint64_t)((t * OZ_A_TILE + ks * 256) >> 4);
+                            const uint64_t bd = bd0 + (uint64_t)((u * OZ_B_TILE + ks * 256) >> 4);
+                            const int accum = (first && ks == 0 && ((fresh >> a) & 1u)) ? 0 : 1;
+                            asm volatile(
+                                "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                                " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dcol[a]),
+                                "l"(ad), "l"(bd), "r"(id), "r"(accum)
+                                : "memory");
+                        }
+                    }
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 su32(&mdone[s]))
+                             : "memory");
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 su32(&mready[c % OZ_RING]))
+                             : "memory");
+                mm_last = c;
+                // chunk c - 1's stage is free once its MMAs retired: refill it
+                if (c >= 1) {
+                    const int sp = (c - 1) % OZ_NS;
+                    if (!wait_mb(&mdone[sp], (unsigned)((c - 1) / OZ_NS) & 1u, false)) { failed = true; break; }
+                    if (c - 1 + OZ_NS < K) {
+                        load(c - 1 + OZ_NS, sp);
+                        ld_c[sp] = c - 1 + OZ_NS;
                     }
                 }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                             su32(&mbar))
-                         : "memory");
+            }
+            if (failed) {
+                atomicExch(g.err, 1);
+                abort_flag = 1;
+                // copies and MMAs of this CTA still in flight (bounded waits)
+                for (int st = 0; st < OZ_NS; st++)
+                    if (ld_c[st] >= 0) wait_mb(&full[st], (unsigned)(ld_c[st] / OZ_NS) & 1u, false);
+                if (mm_last >= 0) wait_mb(&mdone[mm_last % OZ_NS], (unsigned)(mm_last / OZ_NS) & 1u, false);
+            }
         }
-        bool ok = false;
-        for (long long it = 0; it < TC_SPIN; it++)
-            if (mbar_try(su32(&mbar), phase)) { ok = true; break; }
-        phase ^= 1u;
-        if (__syncthreads_or(!ok)) {
-            failed = true;
-            if (tid == 0) atomicExch(g.err, 1);
-            break;
-        }
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const bool last = c + 1 == g.kchunks;
-        for (int a = 0; a < OZ_NACC; a++) {
-            if (!((mymask >> a) & 1u)) continue;
-            if (!last && ((c + 1) % oz_period(a)) != 0) continue;
-            uint32_t d[32];
-            const unsigned taddr = tmem + ((unsigned)(32 * q) << 16) + (unsigned)(a * OZ_TN);
+    } else {
+        const int q = warp & 3, hcol = 16 * (warp >> 2);
+        double acc[16];
+#pragma unroll
+        for (int j = 0; j < 16; j++) acc[j] = 0.0;
+        auto flush = [&](int a, unsigned b) {   // add this warp's 32 x 16 block of accumulator a, buffer b
+            uint32_t d[16];
+            const unsigned taddr =
+                tmem + ((unsigned)(32 * q) << 16) + (unsigned)((b * OZ_NACC + a) * OZ_TN + hcol);
             asm volatile(
-                "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-                "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                "[%16];"
                 : "=r"(d[0]), "=r"(d[1]), "=r"(d[2]), "=r"(d[3]), "=r"(d[4]), "=r"(d[5]), "=r"(d[6]), "=r"(d[7]),
                   "=r"(d[8]), "=r"(d[9]), "=r"(d[10]), "=r"(d[11]), "=r"(d[12]), "=r"(d[13]), "=r"(d[14]),
-                  "=r"(d[15]), "=r"(d[16]), "=r"(d[17]), "=r"(d[18]), "=r"(d[19]), "=r"(d[20]), "=r"(d[21]),
-                  "=r"(d[22]), "=r"(d[23]), "=r"(d[24]), "=r"(d[25]), "=r"(d[26]), "=r"(d[27]), "=r"(d[28]),
-                  "=r"(d[29]), "=r"(d[30]), "=r"(d[31])
+                  "=r"(d[15])
                 : "r"(taddr)
                 : "memory");
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-            for (int j = 0; j < OZ_TN; j++) acc[j] += (double)__uint_as_float(d[j]);
-        }
-        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    }
-    // combine the two halves of each row through shared memory, then apply the
-    // scales 2^(-2 beta) sigma_i tau_j and the alpha / beta epilogue
-    __syncthreads();
-    double *stage = reinterpret_cast<double *>(smem);   // [TM][OZ_TN + 1]
-    if (!failed) {
-        if (warp >= 4) {
-            double *row = stage + (32 * q + lane) * (OZ_TN + 1);
+            for (int j = 0; j < 16; j++) acc[j] += oz_f2d(d[j]);
+        };
+        for (int f = 0; f < K; f++) {
+            const bool ok = wait_mb(&mready[f % OZ_RING], (unsigned)(f / OZ_RING) & 1u, true);
+            if (!__all_sync(0xffffffffu, ok)) {
+                failed = true;
+                if (lane == 0) atomicExch(g.err, 1);
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            if (f + 1 < K) {
+                // accumulators whose period ends with chunk f
 #pragma unroll
-            for (int j = 0; j < OZ_TN; j++) row[j] = acc[j];
+                for (int a = 0; a < OZ_NACC; a++)
+                    if ((f + 1 + oz_phase(a)) % oz_period(a) == 0) flush(a, buf(a, f));
+                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                __syncwarp();
+                if (lane == 0)
+                    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(&fdone[f % OZ_RING]))
+                                 : "memory");
+            } else {
+#pragma unroll
+                for (int a = 0; a < OZ_NACC; a++) flush(a, buf(a, f));
+            }
         }
-        __syncthreads();
-        if (warp < 4) {
+        if (!failed) {
+            // scales 2^(-2 beta) sigma_i tau_j and the alpha / beta epilogue
             const int64_t gr = m0 + 32 * q + lane;
-            const double *row = stage + (32 * q + lane) * (OZ_TN + 1);
             if (gr < g.m) {
                 const double sr = sa[gr] * g.alpha * 0x1p-14;
 #pragma unroll
-                for (int j = 0; j < OZ_TN; j++) {
-                    const int64_t gc = n0 + j;
+                for (int j = 0; j < 16; j++) {
+                    const int64_t gc = n0 + hcol + j;
                     if (gc >= g.n) continue;
                     if (g.uplo == DDLA_LOWER && gc > gr) continue;
                     if (g.uplo == DDLA_UPPER && gc < gr) continue;
-                    const double v = ((acc[j] + row[j]) * sr) * sb[gc];
+                    const double v = (acc[j] * sr) * sb[gc];
                     double *cp = Cz + gr * g.rsc + gc * g.csc;
                     *cp = (g.beta == 0.0) ? v : fma(g.beta, *cp, v);
                 }
             }
         }
-    } else {
-        for (long long it = 0; it < TC_SPIN; it++)
-            if (mbar_try(su32(&mbar), phase ^ 1u)) break;
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -923,6 +1022,7 @@ int gemm_ozaki(ddla_handle h, i64 m, i64 n, i64 k, double alpha, View<const doub
     }
     const i64 mtiles = (m + TM - 1) / TM, ntiles = (n + OZ_TN - 1) / OZ_TN, kchunks = (k + OZ_KC - 1) / OZ_KC;
     if (mtiles > 65535) { set_error("gemm_ozaki: m too large"); return DDLA_ERR_UNSUPPORTED; }
+    if (kchunks > (i64)INT32_MAX) { set_error("gemm_ozaki: k too large"); return DDLA_ERR_UNSUPPORTED; }
     const i64 a_item = (i64)OZ_S * mtiles * TM * kchunks * OZ_KC, b_item = (i64)OZ_S * ntiles * OZ_TN * kchunks * OZ_KC;
     const i64 sa_item = mtiles * TM, sb_item = ntiles * OZ_TN;
     // products in groups of at most 65535 (grid y / z limit), packed slices of one group at a time
@@ -946,7 +1046,7 @@ int gemm_ozaki(ddla_handle h, i64 m, i64 n, i64 k, double alpha, View<const doub
         DDLA_LAUNCHED();
         OzArgs a{m, n, kchunks, mtiles, ntiles, ap, bp, sa, sb, alpha, beta, C.p, C.rs, C.cs, offs,
                  a_item, b_item, sa_item, sb_item, uplo, h->d_info + INFO_TIMEOUT};
-        k_oz_gemm<<<dim3((unsigned)ntiles, (unsigned)mtiles, (unsigned)nz), TC_THREADS, OZ_SMEM, s>>>(a);
+        k_oz_gemm<<<dim3((unsigned)ntiles, (unsigned)mtiles, (unsigned)nz), OZ_THREADS, OZ_SMEM, s>>>(a);
         DDLA_LAUNCHED();
     }
     return 0;
