@@ -619,17 +619,18 @@ namespace {
 constexpr int OZ_S = 8, OZ_BETA = 7;
 constexpr int OZ_EXACT = 5;               // levels with their own exact accumulator
 constexpr int OZ_NACC = OZ_EXACT + 1;     // + one shared accumulator for the small levels
-constexpr int OZ_TN = 32;                 // tile columns
+constexpr int OZ_TN = 64;                 // tile columns
 constexpr int OZ_KC = 32;                 // K staged per chunk (bf16)
 constexpr int OZ_NS = 2;                  // shared-memory stages (chunks in flight)
 constexpr int OZ_SBO = (OZ_KC / 8) * 128; // bf16 core-matrix layout: 8 elements per 16-byte chunk
 constexpr int OZ_A_TILE = TM * OZ_KC * 2, OZ_B_TILE = OZ_TN * OZ_KC * 2;
 constexpr int OZ_STAGE = OZ_S * (OZ_A_TILE + OZ_B_TILE);   // every slice of one K chunk
 constexpr size_t OZ_SMEM = (size_t)OZ_NS * OZ_STAGE;
-// two buffers of OZ_NACC accumulators (OZ_TN columns each): the MMAs of a new
-// flush period write one while the previous period's sums are read from the other
+// OZ_NACC live accumulators plus two spare slots of OZ_TN columns: a period
+// that ends hands its slot to the flush and continues in the oldest spare
+constexpr int OZ_SLOTS = OZ_NACC + 2;
 constexpr int OZ_TMEM_COLS = 512;
-static_assert(2 * OZ_NACC * OZ_TN <= OZ_TMEM_COLS, "TMEM columns");
+static_assert(OZ_SLOTS * OZ_TN <= OZ_TMEM_COLS, "TMEM columns");
 
 // Flush period of accumulator a in K chunks: level l sums (l+1) slice pairs of
 // products below (2^beta - 1)^2 ulps, exact while (l+1) * period * OZ_KC *
@@ -780,20 +781,44 @@ struct OzArgs {
 // OZ_NS shared-memory stages and issues the chunk's slice-pair MMAs into the
 // accumulators of the running flush periods.  Warps 0-7 are the flushers: for
 // every chunk f they wait for its MMAs and add the accumulator whose period
-// ended with f into FP64 registers, while the issuer runs ahead on the other
-// TMEM buffer.  Warp w < 8 reads TMEM lanes 32 (w % 4).. and columns
-// 16 (w / 4).. of each accumulator, so it owns 16 columns of one row of C.
+// ended with f into FP64 registers, while the issuer runs ahead.  TMEM holds
+// OZ_SLOTS slots: when a period of accumulator a ends, a continues in the
+// oldest spare slot and its old slot, once flushed, becomes the newest spare
+// (OzSlots; issuer and flushers replay the same sequence).  With at most one
+// period end per chunk, a spare taken at chunk c was released at a chunk
+// <= c - 2 and flushed by flush c - 3.  Warp w < 8 reads TMEM lanes
+// 32 (w % 4).. and columns 32 (w / 4).. of each slot, so it owns 32 columns of
+// one row of C.
 // Barriers (all waits bounded):
 //   full[st]   copies of a stage landed        (issuer waits)
 //   mdone[st]  MMAs that read a stage retired  (issuer waits, then reloads it)
 //   mready[f % 4]  MMAs of chunk f retired      (flushers wait)
 //   fdone[f % 4]   flush of chunk f done, one arrival per flusher warp
 //                                              (issuer waits)
-// The issuer starts chunk c only after flush c - 3, so
-//   each ring slot completes again only after its previous phase was awaited;
-//   a buffer refilled at chunk c was flushed at f = c - oz_period - 1 <= c - 5.
+// The issuer starts chunk c only after flush c - 3, so each ring slot
+// completes again only after its previous phase was awaited.
 constexpr int OZ_THREADS = 288;
 constexpr int OZ_RING = 4;
+
+// TMEM slot of each accumulator: OZ_NACC live slots and a FIFO of two spares.
+struct OzSlots {
+    int slot[OZ_NACC], spare0, spare1;
+    __device__ __forceinline__ void init() {
+#pragma unroll
+        for (int a = 0; a < OZ_NACC; a++) slot[a] = a;
+        spare0 = OZ_NACC;
+        spare1 = OZ_NACC + 1;
+    }
+    // a period of accumulator a ends before chunk c: a moves to the oldest
+    // spare, its old slot (to be flushed) becomes the newest; returns the old slot
+    __device__ __forceinline__ int turn(int a) {
+        const int old = slot[a];
+        slot[a] = spare0;
+        spare0 = spare1;
+        spare1 = old;
+        return old;
+    }
+};
 
 __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_gemm(OzArgs g) {
     extern __shared__ __align__(1024) unsigned char smem[];
@@ -839,8 +864,6 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_gemm(OzArgs g) {
         }
         return false;
     };
-    // buffer of accumulator a while chunk c is accumulated
-    auto buf = [](int a, int c) -> unsigned { return (unsigned)(((c + oz_phase(a)) / oz_period(a)) & 1); };
     bool failed = false;
     if (warp == 8) {
         if (lane == 0) {
@@ -860,6 +883,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_gemm(OzArgs g) {
                     bulk_g2s(su32(base + (size_t)OZ_S * OZ_A_TILE + (size_t)u * OZ_B_TILE), b + u * b_stride,
                              OZ_B_TILE, su32(&full[st]));
             };
+            OzSlots slots;
+            slots.init();
             // chunk of the copy / MMA batch in flight per stage (-1: none), for the drain
             int ld_c[OZ_NS], mm_last = -1;
             for (int st = 0; st < OZ_NS; st++) ld_c[st] = -1;
@@ -876,12 +901,15 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_gemm(OzArgs g) {
                     break;
                 }
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                // per accumulator: its TMEM buffer and whether this chunk starts a period
-                unsigned dcol[OZ_NACC], fresh = 0;
+                // per accumulator: its TMEM slot and whether this chunk starts a period
+                unsigned dcol[OZ_NACC], fresh = c == 0 ? (1u << OZ_NACC) - 1u : 0u;
 #pragma unroll
                 for (int a = 0; a < OZ_NACC; a++) {
-                    dcol[a] = tmem + (buf(a, c) * OZ_NACC + (unsigned)a) * OZ_TN;
-                    if (c == 0 || (c + oz_phase(a)) % oz_period(a) == 0) fresh |= 1u << a;
+                    if (c > 0 && (c + oz_phase(a)) % oz_period(a) == 0) {
+                        slots.turn(a);
+                        fresh |= 1u << a;
+                    }
+                    dcol[a] = tmem + (unsigned)(slots.slot[a] * OZ_TN);
                 }
                 const unsigned char *At = smem + (size_t)s * OZ_STAGE;
                 const uint64_t ad0 = oz_desc(su32(At)), bd0 = oz_desc(su32(At + (size_t)OZ_S * OZ_A_TILE));
@@ -932,25 +960,28 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_gemm(OzArgs g) {
             }
         }
     } else {
-        const int q = warp & 3, hcol = 16 * (warp >> 2);
-        double acc[16];
+        const int q = warp & 3, hcol = 32 * (warp >> 2);
+        double acc[32];
 #pragma unroll
-        for (int j = 0; j < 16; j++) acc[j] = 0.0;
-        auto flush = [&](int a, unsigned b) {   // add this warp's 32 x 16 block of accumulator a, buffer b
-            uint32_t d[16];
-            const unsigned taddr =
-                tmem + ((unsigned)(32 * q) << 16) + (unsigned)((b * OZ_NACC + a) * OZ_TN + hcol);
+        for (int j = 0; j < 32; j++) acc[j] = 0.0;
+        OzSlots slots;
+        slots.init();
+        auto flush = [&](int sl) {   // add this warp's 32 x 32 block of TMEM slot sl
+            uint32_t d[32];
+            const unsigned taddr = tmem + ((unsigned)(32 * q) << 16) + (unsigned)(sl * OZ_TN + hcol);
             asm volatile(
-                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
-                "[%16];"
+                "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
                 : "=r"(d[0]), "=r"(d[1]), "=r"(d[2]), "=r"(d[3]), "=r"(d[4]), "=r"(d[5]), "=r"(d[6]), "=r"(d[7]),
                   "=r"(d[8]), "=r"(d[9]), "=r"(d[10]), "=r"(d[11]), "=r"(d[12]), "=r"(d[13]), "=r"(d[14]),
-                  "=r"(d[15])
+                  "=r"(d[15]), "=r"(d[16]), "=r"(d[17]), "=r"(d[18]), "=r"(d[19]), "=r"(d[20]), "=r"(d[21]),
+                  "=r"(d[22]), "=r"(d[23]), "=r"(d[24]), "=r"(d[25]), "=r"(d[26]), "=r"(d[27]), "=r"(d[28]),
+                  "=r"(d[29]), "=r"(d[30]), "=r"(d[31])
                 : "r"(taddr)
                 : "memory");
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-            for (int j = 0; j < 16; j++) acc[j] += oz_f2d(d[j]);
+            for (int j = 0; j < 32; j++) acc[j] += oz_f2d(d[j]);
         };
         for (int f = 0; f < K; f++) {
             const bool ok = wait_mb(&mready[f % OZ_RING], (unsigned)(f / OZ_RING) & 1u, true);
@@ -961,10 +992,11 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_gemm(OzArgs g) {
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             if (f + 1 < K) {
-                // accumulators whose period ends with chunk f
+                // the accumulator whose period ends with chunk f (the issuer
+                // turns the same slot before chunk f + 1)
 #pragma unroll
                 for (int a = 0; a < OZ_NACC; a++)
-                    if ((f + 1 + oz_phase(a)) % oz_period(a) == 0) flush(a, buf(a, f));
+                    if ((f + 1 + oz_phase(a)) % oz_period(a) == 0) flush(slots.turn(a));
                 asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
                 __syncwarp();
                 if (lane == 0)
@@ -972,7 +1004,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_gemm(OzArgs g) {
                                  : "memory");
             } else {
 #pragma unroll
-                for (int a = 0; a < OZ_NACC; a++) flush(a, buf(a, f));
+                for (int a = 0; a < OZ_NACC; a++) flush(slots.slot[a]);
             }
         }
         if (!failed) {
@@ -981,7 +1013,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_gemm(OzArgs g) {
             if (gr < g.m) {
                 const double sr = sa[gr] * g.alpha * 0x1p-14;
 #pragma unroll
-                for (int j = 0; j < 16; j++) {
+                for (int j = 0; j < 32; j++) {
                     const int64_t gc = n0 + hcol + j;
                     if (gc >= g.n) continue;
                     if (g.uplo == DDLA_LOWER && gc > gr) continue;
