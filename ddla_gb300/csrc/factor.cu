@@ -315,6 +315,18 @@ __global__ void k_iota(int *p, i64 n) {
     for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < n; e += (i64)gridDim.x * blockDim.x) p[e] = (int)e;
 }
 
+// The handle's high-priority side stream and its two events, created on first
+// use by the look-ahead factorizations.
+static int ensure_side(ddla_handle h) {
+    if (h->side) return 0;
+    int lo = 0, hi = 0;
+    DDLA_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    DDLA_CUDA(cudaStreamCreateWithPriority(&h->side, cudaStreamNonBlocking, hi));
+    DDLA_CUDA(cudaEventCreateWithFlags(&h->ev_ready, cudaEventDisableTiming));
+    DDLA_CUDA(cudaEventCreateWithFlags(&h->ev_panel, cudaEventDisableTiming));
+    return 0;
+}
+
 template <typename T>
 int getrf(ddla_handle h, i64 n, View<T> A, int32_t *d_piv, int prec, int nb, int *d_perm) {
     if (n == 0) return 0;
@@ -336,13 +348,7 @@ int getrf(ddla_handle h, i64 n, View<T> A, int32_t *d_piv, int prec, int nb, int
     // the big update (panel_swap_rest), so the two streams never overlap in
     // memory.
     const bool ahead = tune_get("lu.lookahead", 1) != 0 && n > 2 * (i64)w;
-    if (ahead && !h->side) {
-        int lo = 0, hi = 0;
-        DDLA_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
-        DDLA_CUDA(cudaStreamCreateWithPriority(&h->side, cudaStreamNonBlocking, hi));
-        DDLA_CUDA(cudaEventCreateWithFlags(&h->ev_ready, cudaEventDisableTiming));
-        DDLA_CUDA(cudaEventCreateWithFlags(&h->ev_panel, cudaEventDisableTiming));
-    }
+    if (ahead) DDLA_TRY(ensure_side(h));
     // the panel kernel also forms inv(L11) (double-buffered by panel parity:
     // panel k+1 writes its inverse while the main stream still uses panel k's)
     T *pinv;
@@ -504,20 +510,71 @@ int potrf(ddla_handle h, int uplo, i64 n, View<T> A, int prec, int nb) {
     nb = pick_nb(nb, sizeof(T) == 4 ? 64 : DIAG_MAX);
     // The upper factorization is the lower one of the transposed view.
     View<T> L = (uplo == DDLA_UPPER) ? A.t() : A;
-    for (i64 j0 = 0; j0 < n; j0 += nb) {
-        int b = (int)(n - j0 < nb ? n - j0 : nb);
-        i64 r = n - j0 - b;
+    // block column j0 (width b): L11 = chol(A11), L21 = A21 L11^-T, on the
+    // handle's current stream
+    auto column = [&](i64 j0, int b) -> int {
+        const i64 r = n - j0 - b;
         View<T> L11 = L.sub(j0, b, j0, b);
         DDLA_TRY(diag_kernel<T>(h, L11, b, DK_CHOL, j0));
         if (r > 0) {
             View<const T> cL11{L11.p, b, b, L11.rs, L11.cs};
-            View<T> L21 = L.sub(j0 + b, r, j0, b);
-            DDLA_TRY(trsm<T>(h, DDLA_RIGHT, DDLA_LOWER, DDLA_TRANSPOSE, DDLA_NONUNIT_DIAG, r, b, T(1), cL11, L21));
-            View<const T> cL21{L21.p, r, b, L21.rs, L21.cs};
-            Timed t(h->stream, TC_UPDATE, 1.0 * r * (r + 1) * b, sizeof(T) * (1.0 * r * (r + 1) + r * b));
-            DDLA_TRY(gemm_any<T>(h, prec, r, r, b, T(-1), cL21, cL21.t(), T(1), L.sub(j0 + b, r, j0 + b, r),
-                                 DDLA_LOWER));
+            DDLA_TRY(trsm<T>(h, DDLA_RIGHT, DDLA_LOWER, DDLA_TRANSPOSE, DDLA_NONUNIT_DIAG, r, b, T(1), cL11,
+                             L.sub(j0 + b, r, j0, b)));
         }
+        return 0;
+    };
+    // Look-ahead of depth one (as in getrf): after block column k, the columns
+    // of block k+1 are updated first, and block column k+1 is factored on the
+    // high-priority side stream while the main stream updates the rest of the
+    // trailing matrix.  The side stream touches only the columns of block k+1;
+    // its diagonal kernel and triangular solve use the WS_TRI / WS_TMP
+    // workspaces, the updates on the main stream none of them (WS_TMP is
+    // largest for block 0, which the main stream solves, so it never grows
+    // while the side stream holds it).
+    const bool ahead = tune_get("chol.lookahead", 1) != 0 && n > 2 * (i64)nb;
+    if (ahead) DDLA_TRY(ensure_side(h));
+    cudaStream_t s = h->stream;
+    if (ahead) DDLA_TRY(column(0, (int)nb));
+    for (i64 j0 = 0; j0 < n; j0 += nb) {
+        int b = (int)(n - j0 < nb ? n - j0 : nb);
+        i64 r = n - j0 - b;
+        if (!ahead) DDLA_TRY(column(j0, b));
+        if (r <= 0) break;
+        View<const T> cL21{L.p + (j0 + b) * L.rs + j0 * L.cs, r, b, L.rs, L.cs};
+        const i64 j1 = j0 + b;
+        if (!ahead) {
+            Timed t(s, TC_UPDATE, 1.0 * r * (r + 1) * b, sizeof(T) * (1.0 * r * (r + 1) + r * b));
+            DDLA_TRY(gemm_any<T>(h, prec, r, r, b, T(-1), cL21, cL21.t(), T(1), L.sub(j1, r, j1, r), DDLA_LOWER));
+            continue;
+        }
+        const int b1 = (int)(r < nb ? r : nb);
+        const i64 rest = r - b1;
+        {   // block k+1's columns: its diagonal block (lower triangle) and the rows below it;
+            // narrow, so FP32 on the CUDA cores for the FP32 factors
+            Timed t(s, TC_UPDATE, 1.0 * b1 * (b1 + 1) * b + 2.0 * rest * b1 * b,
+                    sizeof(T) * (2.0 * r * b1 + r * b));
+            const int np = sizeof(T) == 4 ? DDLA_PREC_FP32 : prec;
+            View<const T> top{cL21.p, b1, b, cL21.rs, cL21.cs};
+            DDLA_TRY(gemm_any<T>(h, np, b1, b1, b, T(-1), top, top.t(), T(1), L.sub(j1, b1, j1, b1), DDLA_LOWER));
+            if (rest > 0)
+                DDLA_TRY(gemm_any<T>(h, np, rest, b1, b, T(-1),
+                                     View<const T>{cL21.p + b1 * cL21.rs, rest, b, cL21.rs, cL21.cs}, top.t(), T(1),
+                                     L.sub(j1 + b1, rest, j1, b1), DDLA_DENSE));
+        }
+        DDLA_CUDA(cudaEventRecord(h->ev_ready, s));
+        DDLA_CUDA(cudaStreamWaitEvent(h->side, h->ev_ready, 0));
+        h->stream = h->side;
+        const int rc = column(j1, b1);
+        h->stream = s;
+        DDLA_TRY(rc);
+        DDLA_CUDA(cudaEventRecord(h->ev_panel, h->side));
+        if (rest > 0) {
+            View<const T> low{cL21.p + b1 * cL21.rs, rest, b, cL21.rs, cL21.cs};
+            Timed t(s, TC_UPDATE, 1.0 * rest * (rest + 1) * b, sizeof(T) * (1.0 * rest * (rest + 1) + rest * b));
+            DDLA_TRY(gemm_any<T>(h, prec, rest, rest, b, T(-1), low, low.t(), T(1),
+                                 L.sub(j1 + b1, rest, j1 + b1, rest), DDLA_LOWER));
+        }
+        DDLA_CUDA(cudaStreamWaitEvent(s, h->ev_panel, 0));
     }
     return 0;
 }
