@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "timing.cuh"
 
 namespace ddla {
 
@@ -305,7 +306,10 @@ int refine(ddla_handle h, i64 n, int nr, const double *A, const double *B, doubl
     }
     std::vector<unsigned long long> hn(1 + 3 * MAX_RHS);
     for (;;) {
-        DDLA_TRY(residual(h, n, nr, A, X, B, R));
+        {
+            Timed t(s, TC_REFINE, 2.0 * n * n * nr, 8.0 * n * n);
+            DDLA_TRY(residual(h, n, nr, A, X, B, R));
+        }
         DDLA_CUDA(cudaMemsetAsync(norms + 1 + nr, 0, sizeof(unsigned long long) * 2 * nr, s));
         k_colmax_abs<<<grid1(tot), 256, 0, s>>>(X, n, nr, norms + 1 + nr);
         DDLA_LAUNCHED();
@@ -415,6 +419,7 @@ int mixed_lu(ddla_handle h, i64 n, i64 nrhs, const double *A, const double *B, d
     DDLA_TRY(tri_inverse<float>(h, true, true, F, n, invL));
     DDLA_TRY(tri_inverse<float>(h, false, false, F, n, invU));
     auto solve32 = [&](float *d) {
+        Timed t(s, TC_SOLVE, 2.0 * n * n * nr, 4.0 * n * n);
         DDLA_TRY(permute_rows<float>(h, View<float>{d, n, nr, nr, 1}, perm, n, true));
         DDLA_TRY(trsv_apply<float>(h, true, F, n, invL, d, nr, nr));
         return trsv_apply<float>(h, false, F, n, invU, d, nr, nr);
@@ -474,6 +479,7 @@ int mixed_chol(ddla_handle h, int uplo, i64 n, i64 nrhs, const double *A, const 
     DDLA_TRY(tri_inverse<float>(h, true, false, Lv, n, invL));
     DDLA_TRY(tri_inverse<float>(h, false, false, Uv, n, invU));
     auto solve32 = [&](float *d) {
+        Timed t(s, TC_SOLVE, 2.0 * n * n * nr, 4.0 * n * n);
         DDLA_TRY(trsv_apply<float>(h, true, Lv, n, invL, d, nr, nr));
         return trsv_apply<float>(h, false, Uv, n, invU, d, nr, nr);
     };

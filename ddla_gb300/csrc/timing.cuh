@@ -5,7 +5,7 @@
 namespace ddla {
 
 enum TimingClass { TC_UPDATE = 0, TC_PANEL = 1, TC_TRSM = 2, TC_LASWP = 3, TC_REFINE = 4, TC_BATCHED = 5,
-                   TC_CONTRACT = 6, TC_QR_T = 7, TC_COUNT = 8 };
+                   TC_CONTRACT = 6, TC_QR_T = 7, TC_SOLVE = 8, TC_COUNT = 9 };
 
 bool timing_on();
 

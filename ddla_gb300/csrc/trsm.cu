@@ -324,6 +324,120 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
+// Whole-system solve with 9-16 right-hand sides (the mixed Cholesky's
+// correction solves).  Same chain as k_trsv_chain (ticket order, one CTA per
+// block row, a flag per published block), but thread t owns row t / 16 and
+// right-hand side t % 16 of its block, so a tile product needs no reduction.
+// The off-diagonal tiles do not depend on the chain: they stream through
+// CH16_STAGES shared-memory stages (cp.async) ahead of the flag waits, and the
+// block's inverse is prefetched with them.  x_j is read once per tile into one
+// of two buffers, so a tile costs two barriers.  Needs 16-byte rows (cs == 1)
+// or columns (rs == 1) and n a multiple of the 16-byte vector.
+constexpr int CH16_STAGES = 3;
+constexpr int CH16_THREADS = TB * 16;
+template <typename T>
+constexpr size_t ch16_smem() {
+    return sizeof(T) * ((size_t)(CH16_STAGES + 1) * TB * TB + 3 * TB * 16);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(CH16_THREADS)
+    k_trsv_chain16(i64 n, int nblk, const T *__restrict__ A, i64 rs, i64 cs, int lower, int trans,
+                   const T *__restrict__ inv, T *X, i64 ldx, int nr, int *flags, int *ticket, int *err) {
+    extern __shared__ __align__(16) unsigned char ch_smem[];
+    T *sA = reinterpret_cast<T *>(ch_smem);            // [CH16_STAGES][TB * TB]
+    T *sInv = sA + (size_t)CH16_STAGES * TB * TB;       // [TB][TB]
+    T *sx = sInv + TB * TB;                             // [2][TB][16]
+    T *sacc = sx + 2 * TB * 16;                         // [TB][16]
+    __shared__ int s_blk, s_abort;
+    const int t = threadIdx.x, r = t >> 4, c = t & 15;
+    if (t == 0) {
+        s_blk = atomicAdd(ticket, 1);
+        s_abort = 0;
+    }
+    __syncthreads();
+    const int logical = s_blk;
+    const int blk = lower ? logical : nblk - 1 - logical;
+    const i64 r0 = (i64)blk * TB;
+    const int rows = (int)(n - r0 < TB ? n - r0 : TB);
+    constexpr int VEC = 16 / (int)sizeof(T);   // elements per 16-byte copy
+    constexpr int NV = TB * TB / VEC;          // copies per tile
+    // tile d (the d-th block before the diagonal in solve order) into stage
+    // st: stored [i][k] (trans = 0, rows contiguous) or [k][i] (trans = 1)
+    auto issue = [&](int d, int st) {
+        const int j = lower ? d : nblk - 1 - d;
+        const i64 c0 = (i64)j * TB;
+        T *dst = sA + (size_t)st * TB * TB;
+        for (int v = t; v < NV; v += CH16_THREADS) {
+            const int a = v / (TB / VEC), b = (v % (TB / VEC)) * VEC;
+            const i64 gi = trans ? r0 + b : r0 + a, gk = trans ? c0 + a : c0 + b;
+            const bool in = gi < n && gk < n;
+            cp_async16(dst + a * TB + b, in ? A + gi * rs + gk * cs : A, in ? 16 : 0);
+        }
+    };
+    {
+        const T *iv = inv + (i64)blk * TB * TB;
+        for (int v = t; v < NV; v += CH16_THREADS) cp_async16(sInv + v * VEC, iv + v * VEC, 16);
+    }
+    cp_async_commit();
+    for (int p = 0; p < CH16_STAGES - 1; p++) {
+        if (p < logical) issue(p, p);
+        cp_async_commit();
+    }
+    T acc = (r < rows && c < nr) ? X[(r0 + r) * ldx + c] : T(0);
+    for (int d = 0; d < logical; d++) {
+        const int j = lower ? d : nblk - 1 - d;
+        const i64 c0 = (i64)j * TB;
+        const int cols = (int)(n - c0 < TB ? n - c0 : TB);
+        if (t == 0) {
+            long long it = 0;
+            while (ld_acquire(flags + j) == 0) {
+                if (++it > SPIN_LIMIT) {
+                    atomicExch(err, 1);
+                    s_abort = 1;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        // groups so far: inverse, tiles 0 .. d + CH16_STAGES - 2; tile d is
+        // complete when at most CH16_STAGES - 2 groups are pending
+        cp_async_wait<CH16_STAGES - 2>();
+        __syncthreads();
+        if (s_abort) break;
+        // every thread is past tile d - 1: its stage takes tile d + CH16_STAGES - 1
+        if (d + CH16_STAGES - 1 < logical) issue(d + CH16_STAGES - 1, (d + CH16_STAGES - 1) % CH16_STAGES);
+        cp_async_commit();
+        T *xb = sx + (d & 1) * TB * 16;
+        xb[r * 16 + c] = (r < cols && c < nr) ? __ldcg(&X[(c0 + r) * ldx + c]) : T(0);
+        __syncthreads();
+        const T *tile = sA + (size_t)(d % CH16_STAGES) * TB * TB;
+        if (!trans) {
+            const T *arow = tile + r * TB;
+#pragma unroll 16
+            for (int k = 0; k < TB; k++) acc -= arow[k] * xb[k * 16 + c];
+        } else {
+#pragma unroll 16
+            for (int k = 0; k < TB; k++) acc -= tile[k * TB + r] * xb[k * 16 + c];
+        }
+    }
+    cp_async_wait<0>();
+    if (s_abort) return;
+    // x_blk = inv(A_blk,blk) * acc
+    sacc[r * 16 + c] = acc;
+    __syncthreads();
+    T v = T(0);
+    const T *irow = sInv + r * TB;
+#pragma unroll 16
+    for (int k = 0; k < TB; k++) v += irow[k] * sacc[k * 16 + c];
+    if (r < rows && c < nr) X[(r0 + r) * ldx + c] = v;
+    __syncthreads();
+    if (t == 0) {
+        __threadfence();
+        st_release(flags + blk, 1);
+    }
+}
+
 template <typename T, int NR>
 __global__ void __launch_bounds__(CL_THREADS)
     k_trsv_cluster(i64 n, int nblk, const T *__restrict__ A, i64 rs, i64 cs, int lower, int vec,
@@ -584,6 +698,33 @@ int cluster_solve(ddla_handle h, int cs, i64 n, int nblk, View<const T> A, bool 
     return 0;
 }
 
+// The 16-wide chain applies when the tiles can move as 16-byte copies.
+template <typename T>
+bool chain16_fits(i64 n, View<const T> A, const T *inv) {
+    constexpr i64 VEC = 16 / (i64)sizeof(T);
+    const bool aligned = (((uintptr_t)A.p) & 15) == 0 && (((uintptr_t)inv) & 15) == 0 && n % VEC == 0;
+    const bool rows = A.cs == 1 && (A.rs * (i64)sizeof(T)) % 16 == 0;
+    const bool cols = A.rs == 1 && (A.cs * (i64)sizeof(T)) % 16 == 0;
+    return aligned && (rows || cols) && tune_get("trsv.chain16", 1) != 0;
+}
+
+template <typename T>
+int chain16(ddla_handle h, i64 n, int nblk, View<const T> A, bool lower, const T *inv, T *X, i64 ldx, int nr,
+            int *flags) {
+    static bool attr = false;
+    if (!attr) {
+        DDLA_CUDA(cudaFuncSetAttribute(k_trsv_chain16<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)ch16_smem<T>()));
+        attr = true;
+    }
+    const int trans = A.cs == 1 ? 0 : 1;
+    k_trsv_chain16<T><<<nblk, CH16_THREADS, ch16_smem<T>(), h->stream>>>(
+        n, nblk, A.p, A.rs, A.cs, lower ? 1 : 0, trans, inv, X, ldx, nr, flags, flags + nblk,
+        h->d_info + INFO_TIMEOUT);
+    DDLA_LAUNCHED();
+    return 0;
+}
+
 template <typename T, int NR>
 int chain(ddla_handle h, i64 n, int nblk, View<const T> A, bool lower, const T *inv, T *X, i64 ldx, int nr,
           int *flags) {
@@ -636,7 +777,10 @@ int trsv_apply(ddla_handle h, bool lower, View<const T> A, i64 n, const T *inv, 
     if (nr <= 2) return chain<T, 2>(h, n, nblk, A, lower, inv, X, ldx, nr, flags);
     if (nr <= 4) return chain<T, 4>(h, n, nblk, A, lower, inv, X, ldx, nr, flags);
     if (nr <= 8) return chain<T, 8>(h, n, nblk, A, lower, inv, X, ldx, nr, flags);
-    if (nr <= 16) return chain<T, 16>(h, n, nblk, A, lower, inv, X, ldx, nr, flags);
+    if (nr <= 16) {
+        if (chain16_fits<T>(n, A, inv)) return chain16<T>(h, n, nblk, A, lower, inv, X, ldx, nr, flags);
+        return chain<T, 16>(h, n, nblk, A, lower, inv, X, ldx, nr, flags);
+    }
     set_error("trsv_apply: more than 16 right-hand sides");
     return DDLA_ERR_UNSUPPORTED;
 }
