@@ -132,8 +132,11 @@ int ddla_timing_read(int cls, double *total_ms, int64_t *launches, double *flops
 /* Tuning parameters (no DDLA counterpart; DDLA hard-codes its blocking in
  * GEMMKernel, DDLA/Einsum/GEMMKernel.cs:11-21, and LU/Cholesky/LDLT.BlockSize).
  * Keys: "lu.nb" (LU panel width cap), "lu.lookahead" (0 turns the look-ahead
- * panel off), "panel.cluster" (CTAs per panel cluster), "trsv.cluster" (0 uses
+ * panel off), "chol.lookahead" (0 turns the Cholesky look-ahead off),
+ * "panel.cluster" (CTAs per panel cluster), "panel.calu" (1 = tournament-
+ * pivoting FP32 panels), "trsv.cluster" (0 uses
  * the chained per-block triangular solve instead of the cluster solve),
+ * "trsv.chain16" (0 keeps the 4-group chained solve for 9-16 right-hand sides),
  * "trsv.cluster.size", "refine.gmres" (0 = classical refinement for one
  * right-hand side), "refine.gmres.m" (GMRES restart length),
  * "refine.gmres.relax" (factor on GMRES's 2-norm stopping target; 0 =
