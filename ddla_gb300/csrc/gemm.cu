@@ -268,11 +268,25 @@ int gemm_f64_struct_h(ddla_handle h, i64 m, i64 n, i64 k, double alpha, View<con
     // tiles of the configuration gemm_f64_any picks for this shape (an upper
     // bound for a triangular C)
     const i64 tiles = n <= 16 ? (m + 127) / 128 : ((m + 31) / 32) * ((n + 63) / 64);
+    // k-slices: at least ~2 CTAs per SM, at most ~6 (every configuration keeps
+    // 7 or more resident, so all slices run in one wave); among those, the
+    // count whose CTAs spread most evenly over the SMs (tiles * parts close to
+    // a multiple of the SM count), the smallest on ties
     i64 parts = 1;
     if (alpha != 0.0 && k >= 1024 && tiles < sms) {
-        parts = (2 * sms + tiles - 1) / tiles;
-        if (parts > k / 128) parts = k / 128;
-        if (parts > 64) parts = 64;
+        i64 lo = (2 * sms + tiles - 1) / tiles, hi = (6 * sms) / tiles;
+        const i64 cap = k / 128 < 64 ? k / 128 : 64;
+        if (hi > cap) hi = cap;
+        if (lo > hi) lo = hi;
+        double best = -1.0;
+        for (i64 p = lo; p <= hi; p++) {
+            const i64 ctas = tiles * p, per = (ctas + sms - 1) / sms;
+            const double balance = (double)ctas / (double)(per * sms);
+            if (balance > best + 1e-9) {
+                best = balance;
+                parts = p;
+            }
+        }
     }
     if (parts < 2) return gemm_f64_struct(h->stream, m, n, k, alpha, A, amode, B, bmode, beta, C, uplo);
     if ((amode & 3) == OP_SYM || (bmode & 3) == OP_SYM) {
