@@ -52,3 +52,33 @@ def test_cluster_solve_in_mixed_refinement(ddla):
         b = r.standard_normal((n, 1))
         x, rep = ddla.solve_mixed(A, b)
         assert rep["converged"] and berr(A, x, b) <= 1e-14
+
+
+@pytest.mark.parametrize("n", [64, 200, 1000, 2051])
+@pytest.mark.parametrize("nrhs", [9, 13, 16])
+def test_chain16_vs_chain_vs_oracle(ddla, orc, n, nrhs):
+    # 9-16 right-hand sides: the 16-wide chained solve (one thread per row and
+    # right-hand side, tiles by 16-byte copies; n = 2051 has unaligned rows and
+    # keeps the 4-group chain) against the 4-group chain and the oracle, both
+    # triangles, both transposes (the transposed views stream column tiles)
+    from ddla_gb300 import autotune
+    r = rng(n * 5 + nrhs)
+    for lower in (True, False):
+        for trans in (ddla.NO_TRANSPOSE, ddla.TRANSPOSE):
+            for unit in (False, True):
+                A = _tri(r, n, lower, unit)
+                B = r.standard_normal((n, nrhs))
+                u = ddla.LOWER if lower else ddla.UPPER
+                d = ddla.UNIT if unit else ddla.NONUNIT
+                xo = B.copy()
+                orc.dtrsm(orc.LEFT, u, trans, d, 1.0, A, xo)
+                x16 = B.copy()
+                ddla.BlasProvider.TrSM(ddla.LEFT, u, trans, d, 1.0, A, x16)
+                try:
+                    autotune.tune_set("trsv.chain16", 0)
+                    x4 = B.copy()
+                    ddla.BlasProvider.TrSM(ddla.LEFT, u, trans, d, 1.0, A, x4)
+                finally:
+                    autotune.tune_set("trsv.chain16", 1)
+                assert rel_max(x16, xo) <= 1e-12
+                assert rel_max(x4, xo) <= 1e-12
