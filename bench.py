@@ -50,6 +50,9 @@ sys.path.insert(0, ROOT)
 N_DEFAULT = 8192
 SEED = 0xDD1A0002
 TOL = 1e-14
+# DRAM bytes (read + write) of one k_panel_lu launch from the ncu capture in
+# profiles/k_panel_lu_fp32_n8192.md (panel of 6912 x 64 FP32)
+PANEL_TRAFFIC = 1.81e6
 METRIC = "Solve GFLOP/s at FP64-level residual: mixed+refined vs plain FP64, 1 GB300"
 UNIT = "GFLOP/s"
 
@@ -139,47 +142,69 @@ class ClockSampler:
                 "reasons": sorted(reasons)}
 
 
-def cpu_sample(n, threads, reps=1):
-    """Oracle LU + solve (DDLA's managed algorithm restated in C) on n x n."""
+def headline_inputs(n, seed):
+    """A (n x n) and b (n x 1), i.i.d. N(0,1) from a seeded host generator, so
+    that the GPU arm, the oracle checks and the reference arm all solve the
+    same system."""
     import numpy as np
-    from oracle import oracle
-    oracle.set_threads(threads)
-    r = np.random.default_rng(SEED)
+    r = np.random.default_rng(seed)
     A = r.standard_normal((n, n))
     b = r.standard_normal((n, 1))
-    best = None
-    for _ in range(reps):
-        F = A.copy()
-        x = b.copy()
-        t = time.perf_counter()
-        info, piv = oracle.dgetrf(F)
-        oracle.dgetrs(F, piv, x)
-        dt = time.perf_counter() - t
-        assert info == 0
-        best = dt if best is None else min(best, dt)
-    return lu_flops(n) / best / 1e9, best
+    return A, b
+
+
+def headline_config(n, world):
+    """The workload both arms report (the problem, not the method)."""
+    return {"workload": f"LU (partial pivoting) + solve, n={n}, 1 RHS, A and b i.i.d. N(0,1) from a fixed seed, "
+                        f"to relative backward error <= {TOL:g}",
+            "n": n, "nrhs": 1, "tol": TOL, "parallelism": f"replicas{world}", "l2": "inputs larger than L2"}
+
+
+def oracle_solve(A, b, threads):
+    """Oracle LU + solve (DDLA's managed algorithm restated in C): factors,
+    relative pivots, x and the wall time."""
+    from oracle import oracle
+    oracle.set_threads(threads)
+    F = A.copy()
+    x = b.copy()
+    t = time.perf_counter()
+    info, piv = oracle.dgetrf(F)
+    oracle.dgetrs(F, piv, x)
+    dt = time.perf_counter() - t
+    if info != 0:
+        raise RuntimeError(f"oracle dgetrf failed at pivot {info}")
+    return F, piv, x, dt
 
 
 def reference_arm(args):
+    """The reference's CPU path on this machine's host cores: DDLA's managed LU +
+    solve (the oracle's C restatement), all host threads, on the headline
+    workload itself (same n, same seeded A and b)."""
     rank, world, _ = dist_env()
     if world > 1 and rank != 0:
         return
     cores = os.cpu_count() or 1
-    n = args.cpu_n
-    vals = []
+    n = args.n
+    A, b = headline_inputs(n, SEED)
+    times = []
     for i in range(args.warmup + args.steps):
-        v, dt = cpu_sample(n, cores)
-        if i >= args.warmup:
-            vals.append(v)
-    value = statistics.median(vals)
+        if i < args.warmup:
+            # warm-up: a small solve brings up the thread pool and the pages of
+            # the library; the full-size solves are all timed
+            oracle_solve(A[:512, :512].copy(), b[:512].copy(), cores)
+            continue
+        _, _, _, dt = oracle_solve(A, b, cores)
+        times.append(dt)
+    ms = statistics.median(times) * 1e3
+    value = lu_flops(n) / (ms * 1e-3) / 1e9
     out = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
-           "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f64", "data": "synthetic N(0,1), seeded",
-           "config": {"workload": f"LU (partial pivoting) + solve, n={n} sample of n={args.n}, 1 RHS, FP64, CPU",
-                      "n": n},
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic N(0,1), seeded",
+           "config": headline_config(n, 1),
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                            "sample": f"oracle dgetrf+dgetrs (C restatement of DDLA managed LU) n={n}, "
-                                      f"{cores} OpenMP threads, one solve per step"},
+                            "sample": f"oracle dgetrf+dgetrs (C restatement of DDLA's managed blocked LU, nb = 128) "
+                                      f"on the full n={n} system, {cores} OpenMP threads, one solve per timed step "
+                                      f"(median of {args.steps}); warm-up steps are n=512 solves"},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
 
@@ -536,6 +561,74 @@ def secondary(args):
     h.close()
 
 
+def timed_steps(step, steps, warmup, stream, torch):
+    """Run `warmup` untimed steps, then time `steps` with CUDA events on the
+    solve stream (device synchronised on both sides); ms per step."""
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def gpu_berr(A, X, b):
+    """max ||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf), FP64 on the
+    device (torch), outside every timed region."""
+    R = b - A @ X
+    return float((R.abs().amax() / (A.abs().sum(1).amax() * X.abs().amax() + b.abs().amax())).item())
+
+
+def rel_inf(x, ref):
+    return float(((x - ref).abs().max() / ref.abs().max()).item())
+
+
+def lu_pair(h, D, torch, A, b, prec, steps, warmup, stream, piv_out=None):
+    """The mixed solve and the plain FP64 LU + solve on the same A and b.
+    Returns (mixed ms, plain ms, dict of accuracy figures)."""
+    n = A.shape[0]
+    X = torch.zeros(n, 1, dtype=torch.float64, device="cuda")
+    X64 = torch.zeros_like(X)
+    F = torch.empty_like(A)
+    piv64 = torch.zeros(n, dtype=torch.int32, device="cuda")
+
+    def plain():
+        F.copy_(A)
+        rc = h.getrf(F, piv64)
+        if rc != 0:
+            raise RuntimeError(f"getrf failed rc={rc} err={D._lib.last_error()}")
+        X64.copy_(b)
+        h.getrs(F, piv64, X64)
+
+    reps = []
+
+    def mixed():
+        rc, rep = h.gesv_mixed(A, b, X, precision=prec, tol=TOL)
+        if rc != 0 or not rep["converged"]:
+            raise RuntimeError(f"solve failed rc={rc} rep={rep} err={D._lib.last_error()}")
+        reps.append(rep)
+
+    ms_plain = timed_steps(plain, steps[1], warmup[1], stream, torch)
+    ms_mixed = timed_steps(mixed, steps[0], warmup[0], stream, torch)
+    # one more mixed solve, untimed, that also compares its pivots with the
+    # FP64 ones and its solution with the FP64 solution
+    pv = piv_out if piv_out is not None else torch.zeros(n, dtype=torch.int32, device="cuda")
+    rc, rep = h.gesv_mixed(A, b, X, x_ref=X64, precision=prec, tol=TOL, piv_ref=piv64, piv_out=pv)
+    if rc != 0:
+        raise RuntimeError(f"solve failed rc={rc}")
+    acc = {"mixed_backward_error": gpu_berr(A, X, b), "plain_backward_error": gpu_berr(A, X64, b),
+           "mixed_vs_plain_forward_error": rep["forward_error"],
+           "pivots_agree": rep["pivots_agree"], "pivots_first_diff": rep["pivots_first_diff"],
+           "refine_iterations": reps[-1]["iterations"], "factor_ms": reps[-1]["factor_ms"],
+           "refine_ms": reps[-1]["refine_ms"], "library_backward_error": reps[-1]["backward_error"]}
+    return ms_mixed, ms_plain, acc, X, X64, piv64
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -549,9 +642,9 @@ def main():
                                                          "symm", "trmm", "syr2k", "qr", "einsum-chain",
                                                          "tridiag", "bidiag"])
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-n", type=int, default=4096)
-    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the oracle (CPU baseline and its checks)")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-big", action="store_true", help="skip the n = 16384 sub-record")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -575,39 +668,24 @@ def main():
     L = D.lib()
     apply_tune(args)
 
-    prec_map = {"fp32": D.PREC_FP32, "tf32x3": D.PREC_TF32X3, "bf16x3": D.PREC_BF16X3, "fp64": D.PREC_FP64}
-    prec_name = args.precision if args.precision != "auto" else os.environ.get("DDLA_BENCH_PREC", "tf32x3")
+    prec_map = {"fp32": D.PREC_FP32, "tf32x3": D.PREC_TF32X3, "bf16x3": D.PREC_BF16X3}
+    prec_name = args.precision if args.precision not in ("auto", "fp64", "ozaki") else "tf32x3"
     prec = prec_map[prec_name]
     n = args.n
     stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     h = dv.Handle(stream)
-    g = torch.Generator(device="cuda").manual_seed(SEED + rank)
-    A = torch.randn(n, n, dtype=torch.float64, device="cuda", generator=g)
-    b = torch.randn(n, 1, dtype=torch.float64, device="cuda", generator=g)
+    Ah, bh = headline_inputs(n, SEED + rank)
+    A = torch.from_numpy(Ah).cuda()
+    b = torch.from_numpy(bh).cuda()
     X = torch.zeros(n, 1, dtype=torch.float64, device="cuda")
     torch.cuda.synchronize()
 
-    if prec == D.PREC_FP64:
-        # the plain FP64 path: DMMA-based LU with partial pivoting (the panel
-        # and pivots of DDLA's algorithm) and the FP64 triangular solves, on a
-        # fresh copy of A each step
-        F = torch.empty_like(A)
-        piv = torch.zeros(n, dtype=torch.int32, device="cuda")
-
-        def step():
-            F.copy_(A)
-            rc = h.getrf(F, piv)
-            if rc != 0:
-                raise RuntimeError(f"getrf failed rc={rc} err={D._lib.last_error()}")
-            X.copy_(b)
-            h.getrs(F, piv, X)
-            return None
-    else:
-        def step():
-            rc, rep = h.gesv_mixed(A, b, X, precision=prec, tol=TOL)
-            if rc != 0 or not rep["converged"]:
-                raise RuntimeError(f"solve failed rc={rc} rep={rep} err={D._lib.last_error()}")
-            return rep
+    def step():
+        rc, rep = h.gesv_mixed(A, b, X, precision=prec, tol=TOL)
+        if rc != 0 or not rep["converged"]:
+            raise RuntimeError(f"solve failed rc={rc} rep={rep} err={D._lib.last_error()}")
+        return rep
 
     for _ in range(args.warmup):
         step()
@@ -634,7 +712,8 @@ def main():
     value = replica_value(lu_flops(n), world, ms)
 
     # dominant kernel class from the per-launch CUDA-event records of the timed region
-    classes = {0: "trailing_update_gemm", 1: "lu_panel", 2: "trsm", 3: "laswp", 4: "refinement"}
+    classes = {0: "trailing_update_gemm", 1: "lu_panel", 2: "trsm", 3: "laswp", 4: "refinement_residual",
+               8: "refinement_solves"}
     per = {}
     for cls in classes:
         t_ms, cnt, fl, by = C.c_double(), C.c_int64(), C.c_double(), C.c_double()
@@ -643,11 +722,11 @@ def main():
                              "bytes": by.value}
     L.ddla_timing_enable(0)
     f64_peak, f32_peak = dv.measure_peaks()
-    dom = max(per, key=lambda k: per[k]["ms_per_step"])
+    dom = max(("trailing_update_gemm", "lu_panel"), key=lambda k: per[k]["ms_per_step"])
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
     hbm = peaks.get("hbm_gbs", 6800.0)
-    hbm_src = "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6.8 TB/s"
+    hbm_src = "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks else "fallback 6.8 TB/s (of fallback)"
 
     def hbm_entry(cls, kernel, traffic, note):
         v = per[cls]
@@ -660,14 +739,12 @@ def main():
                 "launches_per_step": v["launches"] / args.steps, "us_per_launch": ms_launch * 1e3,
                 "algorithmic_bytes_per_launch": v["bytes"] / nl, "tflops": tfs, "note": note}
 
-    upd_kernel = {D.PREC_TF32X3: "k_tc_update (tcgen05 3xTF32, persistent)", D.PREC_FP64: "k_gemm_f64 (DMMA)"}.get(
-        prec, "k_supdate (FP32 CUDA cores)")
+    upd_kernel = {D.PREC_TF32X3: "k_tc_update (tcgen05 3xTF32, persistent)",
+                  D.PREC_BF16X3: "k_tc_update (tcgen05 3xBF16, persistent)"}.get(prec, "k_supdate (FP32 CUDA cores)")
     # DRAM bytes of one launch from the ncu captures summarised in profiles/
-    # (k_panel_lu: panel of 6912 x 64 FP32, the 21st launch of the solve)
-    roof_panel = hbm_entry("lu_panel", "k_panel_lu (LU panel, 16-CTA cluster)",
-                           1.81e6 if prec != D.PREC_FP64 else None,
-                           "latency-bound: one cluster barrier and two DSMEM round trips per column; algorithmic "
-                           "bytes = the panel read and written once (2 m w 4 B)")
+    roof_panel = hbm_entry("lu_panel", "k_panel_lu (LU panel, 16-CTA cluster)", PANEL_TRAFFIC,
+                           "latency-bound: one candidate exchange per column; algorithmic bytes = the panel read "
+                           "and written once (2 m w 4 B)")
     roof_update = hbm_entry("trailing_update_gemm", upd_kernel, None,
                             "rank-64 update C -= L21 U12: algorithmic bytes = C read + written + the two panels; "
                             "tflops = 2 m n k per launch over its duration")
@@ -678,20 +755,20 @@ def main():
 
     # end-to-end through the host C ABI with pinned host buffers
     e2e = None
-    if not args.no_e2e and rank == 0 and prec != D.PREC_FP64:
-        Ah = A.cpu().pin_memory()
-        bh = b.cpu().pin_memory()
+    if not args.no_e2e and rank == 0:
+        Ahp = torch.from_numpy(Ah).pin_memory()
+        bhp = torch.from_numpy(bh).pin_memory()
         xh = torch.zeros(n, 1, dtype=torch.float64).pin_memory()
         opts = D._lib.Opts()
         opts.precision, opts.tol = prec, TOL
         rep = D._lib.SolveReport()
 
         def e2e_step():
-            rc = L.ddla_dgesv_mixed(n, 1, C.c_void_p(Ah.data_ptr()), n, 1, C.c_void_p(bh.data_ptr()), 1, 1,
+            rc = L.ddla_dgesv_mixed(n, 1, C.c_void_p(Ahp.data_ptr()), n, 1, C.c_void_p(bhp.data_ptr()), 1, 1,
                                     C.c_void_p(xh.data_ptr()), 1, 1, None, C.byref(opts), C.byref(rep))
             if rc != 0:
                 raise RuntimeError(f"e2e solve failed {rc}: {D._lib.last_error()}")
-        for _ in range(2):
+        for _ in range(3):
             e2e_step()
         k2 = max(3, min(args.steps, 5))
         t = time.perf_counter()
@@ -700,34 +777,77 @@ def main():
         dt = (time.perf_counter() - t) / k2
         e2e = {"value": lu_flops(n) / dt / 1e9, "unit": UNIT, "ms_per_step": dt * 1e3,
                "h2d_bytes_per_step": n * n * 8 + n * 8, "d2h_bytes_per_step": n * 8,
-               "api": "ddla_dgesv_mixed (host pointers)"}
+               "api": "ddla_dgesv_mixed (host pointers, synchronous)"}
 
+    # the plain FP64 GPU path on the same A and b (the metric's comparison),
+    # and the accuracy figures of both
+    ms_m2, ms_plain, acc, Xm, X64, piv64 = lu_pair(h, D, torch, A, b, prec, (3, 3), (3, 3), stream)
+    plain = {"ms_per_step": ms_plain, "value": lu_flops(n) / (ms_plain * 1e-3) / 1e9, "unit": UNIT,
+             "backward_error": acc["plain_backward_error"],
+             "path": "ddla_dev_dgetrf + ddla_dev_dgetrs: FP64 LU with partial pivoting (DMMA trailing updates, "
+                     "cluster panels) and FP64 triangular solves, on a fresh copy of A each step",
+             "steps": 3, "warmup": 3}
+
+    # CPU baseline on the same system (rank 0, one GPU): the oracle, which also
+    # checks the pivots of the FP64 GPU path and gives an independent FP64
+    # solution for the forward errors
     cpu = None
+    oracle_check = None
     if not args.no_cpu and rank == 0 and world == 1:
         threads = max(1, (os.cpu_count() or 2) // 2)
-        v, dt = cpu_sample(args.cpu_n, threads)
-        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"oracle dgetrf+dgetrs (C restatement of DDLA managed LU) n={args.cpu_n}, one solve, "
-                         f"{dt:.2f} s, ProcessorCount/2 threads like ParallelHelperEX"}
+        Fo, po, xo, dt = oracle_solve(Ah, bh, threads)
+        cpu = {"value": lu_flops(n) / dt / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"oracle dgetrf+dgetrs (C restatement of DDLA's managed LU) on the same n={n} system, one "
+                         f"solve, {dt:.2f} s, ProcessorCount/2 threads like ParallelHelperEX"}
+        xo_t = torch.from_numpy(xo).cuda()
+        p64 = piv64.cpu().numpy()
+        diff = np.nonzero(p64 != po)[0]
+        oracle_check = {"plain_pivots_identical": bool(diff.size == 0),
+                        "plain_pivots_first_diff": int(diff[0]) if diff.size else -1,
+                        "mixed_pivots_agree_with_oracle": None,
+                        "plain_forward_error_vs_oracle": rel_inf(X64, xo_t),
+                        "mixed_forward_error_vs_oracle": rel_inf(Xm, xo_t),
+                        "oracle_backward_error": float(np.max(np.abs(bh - Ah @ xo)) /
+                                                       (np.abs(Ah).sum(1).max() * np.abs(xo).max() +
+                                                        np.abs(bh).max()))}
+        po_d = torch.from_numpy(po.astype(np.int32)).cuda()
+        rc, rep = h.gesv_mixed(A, b, X, x_ref=xo_t, precision=prec, tol=TOL, piv_ref=po_d)
+        oracle_check["mixed_pivots_agree_with_oracle"] = rep["pivots_agree"]
+        oracle_check["mixed_pivots_first_diff_vs_oracle"] = rep["pivots_first_diff"]
+
+    # the spec size: n = 16384, mixed and plain FP64 (a few steps each)
+    big = None
+    if not args.no_big and rank == 0:
+        del Xm, X64
+        nb_ = 16384
+        g = torch.Generator(device="cuda").manual_seed(SEED + 16384)
+        Ab = torch.randn(nb_, nb_, dtype=torch.float64, device="cuda", generator=g)
+        bb = torch.randn(nb_, 1, dtype=torch.float64, device="cuda", generator=g)
+        msb, msb_plain, accb, _, _, _ = lu_pair(h, D, torch, Ab, bb, prec, (5, 2), (3, 1), stream)
+        big = {"n": nb_, "data": "A, b i.i.d. N(0,1) (seeded device generator)",
+               "mixed": {"ms_per_step": msb, "value": lu_flops(nb_) / (msb * 1e-3) / 1e9, "steps": 5, "warmup": 3},
+               "plain_fp64": {"ms_per_step": msb_plain, "value": lu_flops(nb_) / (msb_plain * 1e-3) / 1e9,
+                              "steps": 2, "warmup": 1},
+               "vs_plain_fp64": msb_plain / msb, **accb}
+        del Ab, bb
+        torch.cuda.empty_cache()
 
     if rank == 0:
         last = reps[-1]
-        if last is None:   # plain FP64: backward error of the last solve, outside the timed region
-            R = b - A @ X
-            berr = float((R.abs().amax() / (A.abs().sum(1).amax() * X.abs().amax() + b.abs().amax())).item())
-            last = {"backward_error": berr, "iterations": 0, "factor_ms": None, "refine_ms": None}
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-               "vs_baseline": None, "dtype": {D.PREC_TF32X3: "f32 factor with 3xTF32 tensor-core updates + f64 refinement",
-                         D.PREC_FP64: "f64"}.get(prec, "f32 factor + f64 refinement"),
-               "data": "synthetic N(0,1), seeded, inputs 512 MB > L2 (no flush needed)",
-               "config": {"workload": f"LU (partial pivoting) + solve, n={n}, 1 RHS, mixed {prec_name} factor + "
-                                      f"FP64 refinement (flexible GMRES preconditioned by the factors) to "
-                                      f"backward error <= {TOL:g}",
-                          "n": n, "nrhs": 1, "precision": prec_name, "tol": TOL, "parallelism": f"replicas{world}",
-                          "l2": "inputs larger than L2"},
+               "vs_baseline": None,
+               "dtype": {D.PREC_TF32X3: "f32 factor with 3xTF32 tensor-core updates + f64 refinement",
+                         D.PREC_BF16X3: "f32 factor with 3xBF16 tensor-core updates + f64 refinement"}.get(
+                             prec, "f32 factor + f64 refinement"),
+               "data": "synthetic N(0,1), seeded host generator, inputs 512 MB > L2 (no flush needed)",
+               "config": headline_config(n, world),
+               "method": f"mixed {prec_name} factor + FP64 refinement (flexible GMRES preconditioned by the "
+                         f"factors)",
+               "plain_fp64": plain, "vs_plain_fp64": ms_plain / ms,
                "backward_error": last["backward_error"], "refine_iterations": last["iterations"],
-               "factor_ms": last["factor_ms"], "refine_ms": last["refine_ms"],
+               "factor_ms": last["factor_ms"], "refine_ms": last["refine_ms"], "accuracy": acc,
+               "oracle_check": oracle_check, "n16384": big,
                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
                "clocks": clk, "peaks_live": {"fp64_tflops": f64_peak, "fp32_tflops": f32_peak}}
         print(json.dumps(out))

@@ -50,10 +50,10 @@ class SolveReport(C.Structure):
     _fields_ = [("iterations", C.c_int32), ("converged", C.c_int32), ("precision", C.c_int32),
                 ("info", C.c_int32), ("backward_error", C.c_double), ("forward_error", C.c_double),
                 ("factor_ms", C.c_double), ("refine_ms", C.c_double), ("pivots_agree", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("pivots_first_diff", C.c_int32)]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 _i32, _i64, _d = C.c_int32, C.c_int64, C.c_double
@@ -143,6 +143,8 @@ _SIGS = {
                                        C.POINTER(SolveReport)]),
     "ddla_dev_dposv_mixed": (C.c_int, [_h, _i32, _i64, _i64, _pd, _pd, _pd, _pd, C.POINTER(Opts),
                                        C.POINTER(SolveReport)]),
+    "ddla_dev_dgesv_mixed_piv": (C.c_int, [_h, _i64, _i64, _pd, _pd, _pd, _pd, _pi, _pi, C.POINTER(Opts),
+                                           C.POINTER(SolveReport)]),
 }
 
 

@@ -6,6 +6,7 @@
 //     max_j ||b_j - A x_j||_inf / (||A||_inf ||x_j||_inf + ||b_j||_inf) <= tol.
 // Only the correction solve (A d = r with the FP32 factors) runs in FP32.
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <vector>
 
@@ -79,6 +80,16 @@ __global__ void k_norm_inf(i64 n, const double *A, i64 lda, unsigned long long *
     for (i64 j = lane; j < n; j += 32) s += fabs(A[row * lda + j]);
     for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
     if (lane == 0) atomicMax(out, (unsigned long long)__double_as_longlong(s));
+}
+
+// Pivot agreement of the mixed LU with a reference pivot vector (both in
+// DDLA's relative convention, LU.cs:367-374): out[0] counts the equal
+// entries, out[1] is the first index where they differ (INT_MAX if none).
+__global__ void k_piv_cmp(const int32_t *piv, const int32_t *ref, i64 n, int *out) {
+    for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
+        if (piv[i] == ref[i]) atomicAdd(&out[0], 1);
+        else atomicMin(&out[1], (int)i);
+    }
 }
 
 // Max |x - xr| and |xr| per column.
@@ -373,13 +384,15 @@ int refine(ddla_handle h, i64 n, int nr, const double *A, const double *B, doubl
 }
 
 int mixed_lu(ddla_handle h, i64 n, i64 nrhs, const double *A, const double *B, double *X, const double *x_ref,
-             const ddla_opts *opts, ddla_solve_report *rep) {
+             const ddla_opts *opts, ddla_solve_report *rep, const int32_t *piv_ref = nullptr,
+             int32_t *piv_out = nullptr) {
     cudaStream_t s = h->stream;
     const int prec = (opts && opts->precision) ? opts->precision : DDLA_PREC_FP32;
     const int nb = opts ? opts->nb : 0;
     *rep = ddla_solve_report{};
     rep->precision = prec;
     rep->pivots_agree = -1;
+    rep->pivots_first_diff = -1;
     if (nrhs > MAX_RHS) {
         set_error("mixed solve: at most 16 right-hand sides per call");
         return DDLA_ERR_UNSUPPORTED;
@@ -395,7 +408,7 @@ int mixed_lu(ddla_handle h, i64 n, i64 nrhs, const double *A, const double *B, d
     DDLA_TRY(workspace(h, WS_B, sizeof(float) * (size_t)n * nr + 256, (void **)&d32));
     DDLA_TRY(workspace(h, WS_C, sizeof(double) * (size_t)n * nr, (void **)&R));
     DDLA_TRY(workspace(h, WS_X, sizeof(int32_t) * (size_t)n, (void **)&piv));
-    DDLA_TRY(workspace(h, WS_A, sizeof(unsigned long long) * (2 + 3 * MAX_RHS + 2), (void **)&norms));
+    DDLA_TRY(workspace(h, WS_A, sizeof(unsigned long long) * (2 + 3 * MAX_RHS + 3), (void **)&norms));
     DDLA_TRY(reset_info(h));
     DDLA_CUDA(cudaEventRecord(h->ev0, s));
     k_d2s<<<grid1(n * n), 256, 0, s>>>(A, n * n, A32);
@@ -408,6 +421,20 @@ int mixed_lu(ddla_handle h, i64 n, i64 nrhs, const double *A, const double *B, d
     cudaEventElapsedTime(&ms, h->ev0, h->ev1);
     rep->factor_ms = ms;
     rep->info = info;
+    if (piv_out) DDLA_CUDA(cudaMemcpyAsync(piv_out, piv, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, s));
+    if (piv_ref) {
+        // how far the FP32 factor followed the FP64 pivot sequence
+        int *cmp = (int *)(norms + 3 + 3 * MAX_RHS);   // after the forward-error pair
+        const int init[2] = {0, INT_MAX};
+        DDLA_CUDA(cudaMemcpyAsync(cmp, init, sizeof(init), cudaMemcpyHostToDevice, s));
+        k_piv_cmp<<<grid1(n), 256, 0, s>>>(piv, piv_ref, n, cmp);
+        DDLA_LAUNCHED();
+        int got[2];
+        DDLA_CUDA(cudaMemcpyAsync(got, cmp, sizeof(got), cudaMemcpyDeviceToHost, s));
+        DDLA_CUDA(cudaStreamSynchronize(s));
+        rep->pivots_agree = got[0];
+        rep->pivots_first_diff = got[1] == INT_MAX ? -1 : got[1];
+    }
     if (info) return info;
     // the inverted diagonal blocks of L and U are formed once and serve every
     // correction solve: d <- U^-1 L^-1 P d
@@ -441,6 +468,7 @@ int mixed_chol(ddla_handle h, int uplo, i64 n, i64 nrhs, const double *A, const 
     *rep = ddla_solve_report{};
     rep->precision = prec;
     rep->pivots_agree = -1;
+    rep->pivots_first_diff = -1;
     if (nrhs > MAX_RHS) {
         set_error("mixed solve: at most 16 right-hand sides per call");
         return DDLA_ERR_UNSUPPORTED;
@@ -505,6 +533,16 @@ int ddla_dev_dgesv_mixed(ddla_handle h, ddla_dim_t n, ddla_dim_t nrhs, const dou
     if (!report) return -9;
     if (n == 0 || nrhs == 0) { *report = ddla_solve_report{}; return 0; }
     return mixed_lu(h, n, nrhs, a, b, x, x_ref, opts, report);
+}
+
+int ddla_dev_dgesv_mixed_piv(ddla_handle h, ddla_dim_t n, ddla_dim_t nrhs, const double *a, const double *b,
+                             double *x, const double *x_ref, const int32_t *piv_ref, int32_t *piv_out,
+                             const ddla_opts *opts, ddla_solve_report *report) {
+    if (n < 0) return -2;
+    if (nrhs < 0) return -3;
+    if (!report) return -11;
+    if (n == 0 || nrhs == 0) { *report = ddla_solve_report{}; return 0; }
+    return mixed_lu(h, n, nrhs, a, b, x, x_ref, opts, report, piv_ref, piv_out);
 }
 
 int ddla_dev_dposv_mixed(ddla_handle h, int32_t uplo, ddla_dim_t n, ddla_dim_t nrhs, const double *a,

@@ -274,63 +274,119 @@ __global__ void __launch_bounds__(TC_THREADS) k_tc_tf32x3(TcArgs g) {
 
 constexpr size_t TC_SMEM = 2 * A_BYTES + 2 * B_BYTES;
 
-// ------------------------------------------------------------------ rank-64 update, 3xTF32
+// ------------------------------------------------------------------ rank-64 update, split products
 //
 // C += alpha * A * B for K <= 64 (the trailing updates of the FP32
-// factorizations) on the tensor cores.  A (m x K) and B (K x n) are split once
-// into TF32 hi / lo parts packed per 128-row (128-column) tile in the
-// core-matrix layout the MMA reads (k_tc_pack).  A persistent kernel walks
-// the 128 x 128 tiles of C with every data movement asynchronous:
-//   * the four 32 KB operand tiles arrive by bulk copy on one mbarrier, and
-//     the next tile's copies start as soon as the current MMAs are done;
+// factorizations) on the tensor cores, with FP32 operands split once into two
+// parts x = hi + lo packed per 128-row (128-column) tile in the core-matrix
+// layout the MMA reads (k_tc_pack):
+//   3xTF32  hi = tf32(x), lo = tf32(x - hi); 8 k-steps of kind::tf32 (K = 8)
+//   3xBF16  hi = bf16(x), lo = bf16(x - hi); 4 k-steps of kind::f16 (K = 16)
+// and A*B ~ hi*hi + hi*lo + lo*hi accumulated in FP32 in TMEM.  Both splits
+// move 32 bytes of K per k-step, so the shared-memory descriptors differ only
+// in the distance between 8-row core-matrix groups (TK * element size * 8).
+// A persistent kernel walks the 128 x 128 tiles of C with every data movement
+// asynchronous:
+//   * the four operand tiles arrive by bulk copy on one mbarrier, and the next
+//     tile's copies start as soon as the current MMAs are done;
 //   * the C tile is loaded with coalesced float4 loads (a warp per 512-byte
 //     row) before the MMAs are issued and parked in a shared staging tile S
 //     while they run;
-//   * one thread issues 8 k-steps x 3 MMAs (hi*hi + hi*lo + lo*hi) into a
-//     128-column TMEM accumulator;
+//   * one thread issues the k-steps x 3 MMAs into a 128-column TMEM
+//     accumulator;
 //   * each thread adds alpha * (its TMEM row) into S, and S goes back to C
 //     with coalesced float4 stores.
-// Every mbarrier wait is bounded as in k_tc_tf32x3.  Needs n, the row stride
-// of C and the C pointer 16-byte aligned (checked by the host).
+// C views that are not 16-byte aligned (or have a column stride) take scalar
+// loads and stores.  Every mbarrier wait is bounded as in k_tc_tf32x3.
 constexpr int UT = 128;                       // tile rows = tile columns
-constexpr int UT_PART = UT * TK;              // floats of one packed operand part
 constexpr int UT_SLD = UT + 4;                // staging tile row (floats)
-constexpr size_t UT_OPS = 4 * (size_t)UT_PART * 4;
-constexpr size_t UT_SMEM = UT_OPS + (size_t)UT * UT_SLD * 4;
 
-__host__ __device__ constexpr uint32_t idesc_tf32_128() {
-    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(UT >> 3) << 17) | ((uint32_t)(UT >> 4) << 24);
+template <bool BF> struct UtSplit {
+    static constexpr int ESZ = BF ? 2 : 4;                       // bytes per packed element
+    static constexpr int PART = UT * TK * ESZ;                   // bytes of one packed operand part
+    static constexpr int SBO = (TK / (16 / ESZ)) * 128;          // next 8-row core-matrix group
+    static constexpr int KSTEPS = TK * ESZ / 32;                 // MMAs of 32 bytes of K each
+    static constexpr size_t OPS = 4 * (size_t)PART;
+    static constexpr size_t SMEM = OPS + (size_t)UT * UT_SLD * 4;
+    // D f32, A / B tf32 (2) or bf16 (1), both K-major, N = M = 128
+    static constexpr uint32_t IDESC =
+        (1u << 4) | ((BF ? 1u : 2u) << 7) | ((BF ? 1u : 2u) << 10) | ((uint32_t)(UT >> 3) << 17) |
+        ((uint32_t)(UT >> 4) << 24);
+};
+
+__device__ __forceinline__ uint64_t sdesc_sbo(unsigned addr, int sbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((addr & 0x3ffff) >> 4);
+    d |= (uint64_t)(LBO >> 4) << 16;
+    d |= (uint64_t)(sbo >> 4) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+
+template <bool BF>
+__device__ __forceinline__ void mma_split(unsigned tmem, uint64_t a, uint64_t b, uint32_t id, int acc) {
+    if constexpr (BF) {
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+            "l"(a), "l"(b), "r"(id), "r"(acc)
+            : "memory");
+    } else {
+        mma_tf32(tmem, a, b, id, acc);
+    }
 }
 
 // rows r of X (rows x kdim, strides rs / cs) -> packed [tile][hi | lo][UT x TK]
-// (element (r, k) at cm_off); rows beyond `rows` and k beyond kdim are zero
-__global__ void k_tc_pack(const float *X, i64 rs, i64 cs, i64 rows, int kdim, float *out, i64 tiles) {
-    const i64 tot = tiles * UT * (TK / 4);
+// in the core-matrix layout (16-byte rows of 4 tf32 or 8 bf16 values); rows
+// beyond `rows` and k beyond kdim are zero
+template <bool BF>
+__global__ void k_tc_pack(const float *X, i64 rs, i64 cs, i64 rows, int kdim, unsigned char *out, i64 tiles) {
+    typedef UtSplit<BF> S;
+    constexpr int PER = 16 / S::ESZ;   // elements per 16-byte core-matrix row
+    const i64 tot = tiles * UT * (TK / PER);
     for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < tot; e += (i64)gridDim.x * blockDim.x) {
-        const i64 tile = e / (UT * (TK / 4));
-        const int rem = (int)(e % (UT * (TK / 4))), r = rem / (TK / 4), k4 = (rem % (TK / 4)) * 4;
+        const i64 tile = e / (UT * (TK / PER));
+        const int rem = (int)(e % (UT * (TK / PER))), r = rem / (TK / PER), k0 = (rem % (TK / PER)) * PER;
         const i64 gr = tile * UT + r;
-        float hi[4], lo[4];
+        unsigned char *base = out + tile * 2 * S::PART;
+        const int off = (r >> 3) * S::SBO + (k0 / PER) * LBO + (r & 7) * 16;
+        if constexpr (BF) {
+            unsigned short hi[8], lo[8];
 #pragma unroll
-        for (int x = 0; x < 4; x++) {
-            const float v = (gr < rows && k4 + x < kdim) ? X[gr * rs + (i64)(k4 + x) * cs] : 0.f;
-            hi[x] = tf32_round(v);
-            lo[x] = tf32_round(v - hi[x]);
+            for (int x = 0; x < 8; x++) {
+                const float v = (gr < rows && k0 + x < kdim) ? X[gr * rs + (i64)(k0 + x) * cs] : 0.f;
+                const __nv_bfloat16 h = __float2bfloat16_rn(v);
+                hi[x] = __bfloat16_as_ushort(h);
+                lo[x] = __bfloat16_as_ushort(__float2bfloat16_rn(v - __bfloat162float(h)));
+            }
+            uint4 qh, ql;
+            qh.x = hi[0] | ((unsigned)hi[1] << 16); qh.y = hi[2] | ((unsigned)hi[3] << 16);
+            qh.z = hi[4] | ((unsigned)hi[5] << 16); qh.w = hi[6] | ((unsigned)hi[7] << 16);
+            ql.x = lo[0] | ((unsigned)lo[1] << 16); ql.y = lo[2] | ((unsigned)lo[3] << 16);
+            ql.z = lo[4] | ((unsigned)lo[5] << 16); ql.w = lo[6] | ((unsigned)lo[7] << 16);
+            *reinterpret_cast<uint4 *>(base + off) = qh;
+            *reinterpret_cast<uint4 *>(base + S::PART + off) = ql;
+        } else {
+            float hi[4], lo[4];
+#pragma unroll
+            for (int x = 0; x < 4; x++) {
+                const float v = (gr < rows && k0 + x < kdim) ? X[gr * rs + (i64)(k0 + x) * cs] : 0.f;
+                hi[x] = tf32_round(v);
+                lo[x] = tf32_round(v - hi[x]);
+            }
+            *reinterpret_cast<float4 *>(base + off) = make_float4(hi[0], hi[1], hi[2], hi[3]);
+            *reinterpret_cast<float4 *>(base + S::PART + off) = make_float4(lo[0], lo[1], lo[2], lo[3]);
         }
-        float *base = out + tile * 2 * UT_PART;
-        const int off = cm_off(r, k4) / 4;
-        *reinterpret_cast<float4 *>(base + off) = make_float4(hi[0], hi[1], hi[2], hi[3]);
-        *reinterpret_cast<float4 *>(base + UT_PART + off) = make_float4(lo[0], lo[1], lo[2], lo[3]);
     }
 }
 
 struct TuArgs {
     int64_t m, n;
     int ntm, ntn;
-    const float *Ap, *Bp;   // packed operands
+    const unsigned char *Ap, *Bp;   // packed operands
     float alpha;
     float *C;
-    int64_t rsc;
+    int64_t rsc, csc;
     int uplo;               // DDLA_DENSE, or the triangle of C that is updated (m == n)
     int *err;
 };
@@ -357,10 +413,12 @@ __device__ __forceinline__ void bulk_g2s(unsigned dst, const void *src, unsigned
                  : "memory");
 }
 
+template <bool BF, bool VEC>
 __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_update(TuArgs g) {
+    typedef UtSplit<BF> SP;
     extern __shared__ __align__(1024) unsigned char smem[];
-    unsigned char *Ahi = smem, *Alo = smem + UT_PART * 4, *Bhi = smem + 2 * UT_PART * 4, *Blo = smem + 3 * UT_PART * 4;
-    float *S = reinterpret_cast<float *>(smem + UT_OPS);
+    unsigned char *Ahi = smem, *Alo = smem + SP::PART, *Bhi = smem + 2 * SP::PART, *Blo = smem + 3 * SP::PART;
+    float *S = reinterpret_cast<float *>(smem + SP::OPS);
     __shared__ __align__(8) unsigned long long mb_ld, mb_mma;
     __shared__ unsigned tmem_slot;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -381,26 +439,26 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_update(TuArgs g) {
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const unsigned tmem = tmem_slot;
-    constexpr uint32_t id = idesc_tf32_128();
+    constexpr uint32_t id = SP::IDESC;
     auto issue_ops = [&](int t) {   // thread 0: the four operand tiles of tile t
         int mt, nt;
         tu_tile(g, t, &mt, &nt);
-        const float *a = g.Ap + (size_t)mt * 2 * UT_PART, *b = g.Bp + (size_t)nt * 2 * UT_PART;
+        const unsigned char *a = g.Ap + (size_t)mt * 2 * SP::PART, *b = g.Bp + (size_t)nt * 2 * SP::PART;
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(&mb_ld)),
-                     "r"((unsigned)UT_OPS)
+                     "r"((unsigned)SP::OPS)
                      : "memory");
-        bulk_g2s(su32(Ahi), a, UT_PART * 4, su32(&mb_ld));
-        bulk_g2s(su32(Alo), a + UT_PART, UT_PART * 4, su32(&mb_ld));
-        bulk_g2s(su32(Bhi), b, UT_PART * 4, su32(&mb_ld));
-        bulk_g2s(su32(Blo), b + UT_PART, UT_PART * 4, su32(&mb_ld));
+        bulk_g2s(su32(Ahi), a, SP::PART, su32(&mb_ld));
+        bulk_g2s(su32(Alo), a + SP::PART, SP::PART, su32(&mb_ld));
+        bulk_g2s(su32(Bhi), b, SP::PART, su32(&mb_ld));
+        bulk_g2s(su32(Blo), b + SP::PART, SP::PART, su32(&mb_ld));
     };
-    // rows and bytes per row of tile t
-    auto tile_rows = [&](int t, int *rows, unsigned *bytes) {
+    // rows and columns of tile t
+    auto tile_rc = [&](int t, int *rows, int *cols) {
         int mt, nt;
         tu_tile(g, t, &mt, &nt);
         const int64_t r_left = g.m - (int64_t)mt * UT, c_left = g.n - (int64_t)nt * UT;
         *rows = (int)(r_left < UT ? r_left : UT);
-        *bytes = (unsigned)((c_left < UT ? c_left : UT) * 4);
+        *cols = (int)(c_left < UT ? c_left : UT);
     };
     auto wait_mb = [&](unsigned long long *mb, unsigned ph) -> bool {
         for (long long it = 0; it < TC_SPIN; it++)
@@ -417,29 +475,33 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_update(TuArgs g) {
     // next tile is loaded into registers while the current one finishes.
     float4 creg[16];
     auto load_c = [&](int t) {
-        int rows;
-        unsigned bytes;
-        tile_rows(t, &rows, &bytes);
-        const int cols = (int)(bytes / 4);
+        int rows, cols;
+        tile_rc(t, &rows, &cols);
         int tm, tn;
         tu_tile(g, t, &tm, &tn);
-        const float *ct = g.C + (int64_t)tm * UT * g.rsc + (int64_t)tn * UT;
+        const float *ct = g.C + (int64_t)tm * UT * g.rsc + (int64_t)tn * UT * g.csc;
 #pragma unroll
         for (int i = 0; i < 16; i++) {
             const int e = tid + 256 * i, r = e >> 5, c4 = (e & 31) * 4;
-            creg[i] = (r < rows && c4 < cols) ? *reinterpret_cast<const float4 *>(ct + (int64_t)r * g.rsc + c4)
-                                              : make_float4(0.f, 0.f, 0.f, 0.f);
+            if constexpr (VEC) {
+                creg[i] = (r < rows && c4 < cols) ? *reinterpret_cast<const float4 *>(ct + (int64_t)r * g.rsc + c4)
+                                                  : make_float4(0.f, 0.f, 0.f, 0.f);
+            } else {
+                float v[4];
+#pragma unroll
+                for (int x = 0; x < 4; x++)
+                    v[x] = (r < rows && c4 + x < cols) ? ct[(int64_t)r * g.rsc + (int64_t)(c4 + x) * g.csc] : 0.f;
+                creg[i] = make_float4(v[0], v[1], v[2], v[3]);
+            }
         }
     };
     load_c(blockIdx.x);
     for (int t = blockIdx.x; t < total; t += gridDim.x) {
-        int rows;
-        unsigned bytes;
-        tile_rows(t, &rows, &bytes);
-        const int cols = (int)(bytes / 4);
+        int rows, cols;
+        tile_rc(t, &rows, &cols);
         int mt, nt;
         tu_tile(g, t, &mt, &nt);
-        float *ctile = g.C + (int64_t)mt * UT * g.rsc + (int64_t)nt * UT;
+        float *ctile = g.C + (int64_t)mt * UT * g.rsc + (int64_t)nt * UT * g.csc;
         const bool diag = g.uplo != DDLA_DENSE && mt == nt;
         const bool more = t + (int)gridDim.x < total;
         if (__syncthreads_or(!wait_mb(&mb_ld, ph_ld))) { failed = true; break; }
@@ -447,13 +509,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_update(TuArgs g) {
         ops_out = false;
         if (tid == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            for (int s = 0; s < TK / 8; s++) {
+            for (int s = 0; s < SP::KSTEPS; s++) {
                 const unsigned off = s * 2 * LBO;
-                const uint64_t ah = sdesc(su32(Ahi) + off), al = sdesc(su32(Alo) + off);
-                const uint64_t bh = sdesc(su32(Bhi) + off), bl = sdesc(su32(Blo) + off);
-                mma_tf32(tmem, ah, bh, id, s == 0 ? 0 : 1);
-                mma_tf32(tmem, ah, bl, id, 1);
-                mma_tf32(tmem, al, bh, id, 1);
+                const uint64_t ah = sdesc_sbo(su32(Ahi) + off, SP::SBO), al = sdesc_sbo(su32(Alo) + off, SP::SBO);
+                const uint64_t bh = sdesc_sbo(su32(Bhi) + off, SP::SBO), bl = sdesc_sbo(su32(Blo) + off, SP::SBO);
+                mma_split<BF>(tmem, ah, bh, id, s == 0 ? 0 : 1);
+                mma_split<BF>(tmem, ah, bl, id, 1);
+                mma_split<BF>(tmem, al, bh, id, 1);
             }
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                              su32(&mb_mma))
@@ -506,14 +568,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_update(TuArgs g) {
         for (int i = 0; i < 16; i++) {
             const int e = tid + 256 * i, r = e >> 5, c4 = (e & 31) * 4;
             if (r < rows && c4 < cols) {
-                if (!diag) {
+                if (VEC && !diag) {
                     *reinterpret_cast<float4 *>(ctile + (int64_t)r * g.rsc + c4) =
                         *reinterpret_cast<const float4 *>(S + r * UT_SLD + c4);
-                } else {   // diagonal tile of a triangular update: its triangle only
+                } else {   // scalar: unaligned C, or the diagonal tile of a triangular update
 #pragma unroll
                     for (int x = 0; x < 4; x++) {
                         const int c = c4 + x;
-                        if (g.uplo == DDLA_LOWER ? c <= r : c >= r) ctile[(int64_t)r * g.rsc + c] = S[r * UT_SLD + c];
+                        if (c >= cols) break;
+                        if (diag && !(g.uplo == DDLA_LOWER ? c <= r : c >= r)) continue;
+                        ctile[(int64_t)r * g.rsc + (int64_t)c * g.csc] = S[r * UT_SLD + c];
                     }
                 }
             }
@@ -534,44 +598,72 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_update(TuArgs g) {
     }
 }
 
+template <bool BF>
+int tc_update(ddla_handle h, i64 m, i64 n, i64 k, float alpha, View<const float> A, View<const float> B,
+              View<float> C, int uplo) {
+    typedef UtSplit<BF> SP;
+    static size_t uavail = 0;
+    if (!uavail) {
+        DDLA_TRY(max_dyn_smem((const void *)k_tc_update<BF, true>, h->smem_optin, &uavail));
+        size_t u2 = 0;
+        DDLA_TRY(max_dyn_smem((const void *)k_tc_update<BF, false>, h->smem_optin, &u2));
+        uavail = std::min(uavail, u2);
+    }
+    if (SP::SMEM > uavail) {
+        set_error("gemm_tc: not enough shared memory for the rank-64 update");
+        return DDLA_ERR_UNSUPPORTED;
+    }
+    const i64 ntm = (m + UT - 1) / UT, ntn = (n + UT - 1) / UT;
+    unsigned char *pa, *pb;
+    DDLA_TRY(workspace(h, WS_TC, 2 * (size_t)SP::PART * (ntm + ntn), (void **)&pa));
+    pb = pa + 2 * (size_t)SP::PART * ntm;
+    constexpr int PER = 16 / SP::ESZ;
+    auto grid_of = [](i64 tot) { return (unsigned)((tot + 255) / 256 < 4096 ? (tot + 255) / 256 : 4096); };
+    k_tc_pack<BF><<<grid_of(ntm * UT * (TK / PER)), 256, 0, h->stream>>>(A.p, A.rs, A.cs, m, (int)k, pa, ntm);
+    DDLA_LAUNCHED();
+    View<const float> Bt = B.t();   // n x k: columns of B as rows
+    k_tc_pack<BF><<<grid_of(ntn * UT * (TK / PER)), 256, 0, h->stream>>>(Bt.p, Bt.rs, Bt.cs, n, (int)k, pb, ntn);
+    DDLA_LAUNCHED();
+    // a few tiles per CTA rather than one CTA per SM for the whole update:
+    // CTAs retire often, so the look-ahead panel (a 16-CTA cluster on a
+    // high-priority stream) finds free SMs while the update runs
+    const i64 tiles = uplo == DDLA_DENSE ? ntm * ntn : ntm * (ntm + 1) / 2;
+    const i64 per = std::max<int64_t>(1, tune_get("update.tiles_per_cta", 4));
+    const i64 want = (tiles + per - 1) / per;
+    const int grid = (int)(want < 65535 ? want : 65535);
+    // float4 accesses to C when its rows are 16-byte aligned with a unit column stride
+    const bool vec = C.cs == 1 && (C.rs & 3) == 0 && (((uintptr_t)C.p) & 15) == 0 && (n & 3) == 0;
+    TuArgs a{m, n, (int)ntm, (int)ntn, pa, pb, alpha, C.p, C.rs, C.cs, uplo, h->d_info + INFO_TIMEOUT};
+    if (vec) k_tc_update<BF, true><<<grid, TC_THREADS, SP::SMEM, h->stream>>>(a);
+    else k_tc_update<BF, false><<<grid, TC_THREADS, SP::SMEM, h->stream>>>(a);
+    DDLA_LAUNCHED();
+    return 0;
+}
+
 }  // namespace
 
 int gemm_tc(ddla_handle h, int prec, i64 m, i64 n, i64 k, float alpha, View<const float> A, View<const float> B,
             float beta, View<float> C, int uplo) {
     if (m <= 0 || n <= 0) return 0;
+    const bool update = beta == 1.f && k > 0 && k <= TK && (uplo == DDLA_DENSE || m == n) &&
+                        tune_get("update.tc", 1) != 0;
+    if (prec == DDLA_PREC_BF16X3) {
+        // 3xBF16 runs only as the rank-<=64 update (the trailing updates of the
+        // FP32 factorizations)
+        if (!update) {
+            set_error("gemm_tc: 3xBF16 products cover the rank-64 update C += alpha A B (beta = 1, k <= 64) only");
+            return DDLA_ERR_UNSUPPORTED;
+        }
+        return tc_update<true>(h, m, n, k, alpha, A, B, C, uplo);
+    }
     if (prec != DDLA_PREC_TF32X3) {
-        set_error("gemm_tc: only the 3xTF32 split is implemented");
+        set_error("gemm_tc: precision must be DDLA_PREC_TF32X3 or DDLA_PREC_BF16X3");
         return DDLA_ERR_UNSUPPORTED;
     }
-    if (beta == 1.f && k > 0 && k <= TK && (uplo == DDLA_DENSE || m == n) && C.cs == 1 && (n & 3) == 0 &&
-        (C.rs & 3) == 0 && (((uintptr_t)C.p) & 15) == 0 && tune_get("update.tc", 1) != 0) {
+    if (update && C.cs == 1 && (n & 3) == 0 && (C.rs & 3) == 0 && (((uintptr_t)C.p) & 15) == 0) {
         // rank-<=64 update: packed operands + persistent tensor-core kernel
-        static size_t uavail = 0;
-        if (!uavail) DDLA_TRY(max_dyn_smem((const void *)k_tc_update, h->smem_optin, &uavail));
-        if (UT_SMEM <= uavail) {
-            const i64 ntm = (m + UT - 1) / UT, ntn = (n + UT - 1) / UT;
-            float *pa, *pb;
-            DDLA_TRY(workspace(h, WS_TC, sizeof(float) * 2 * (size_t)UT_PART * (ntm + ntn), (void **)&pa));
-            pb = pa + 2 * (size_t)UT_PART * ntm;
-            auto grid_of = [](i64 tot) { return (unsigned)((tot + 255) / 256 < 4096 ? (tot + 255) / 256 : 4096); };
-            k_tc_pack<<<grid_of(ntm * UT * (TK / 4)), 256, 0, h->stream>>>(A.p, A.rs, A.cs, m, (int)k, pa, ntm);
-            DDLA_LAUNCHED();
-            View<const float> Bt = B.t();   // n x k: columns of B as rows
-            k_tc_pack<<<grid_of(ntn * UT * (TK / 4)), 256, 0, h->stream>>>(Bt.p, Bt.rs, Bt.cs, n, (int)k, pb, ntn);
-            DDLA_LAUNCHED();
-            // a few tiles per CTA rather than one CTA per SM for the whole
-            // update: CTAs retire often, so the look-ahead panel (a 16-CTA
-            // cluster on a high-priority stream) finds free SMs while the
-            // update runs
-            const i64 tiles = uplo == DDLA_DENSE ? ntm * ntn : ntm * (ntm + 1) / 2;
-            const i64 per = std::max<int64_t>(1, tune_get("update.tiles_per_cta", 4));
-            const i64 want = (tiles + per - 1) / per;
-            const int grid = (int)(want < 65535 ? want : 65535);
-            TuArgs a{m, n, (int)ntm, (int)ntn, pa, pb, alpha, C.p, C.rs, uplo, h->d_info + INFO_TIMEOUT};
-            k_tc_update<<<grid, TC_THREADS, UT_SMEM, h->stream>>>(a);
-            DDLA_LAUNCHED();
-            return 0;
-        }
+        const int rc = tc_update<false>(h, m, n, k, alpha, A, B, C, uplo);
+        if (rc != DDLA_ERR_UNSUPPORTED) return rc;
     }
     static size_t avail = 0;
     if (!avail) DDLA_TRY(max_dyn_smem((const void *)k_tc_tf32x3, h->smem_optin, &avail));

@@ -134,7 +134,10 @@ class Handle:
               "dev_dpotrs")
 
     def gesv_mixed(self, A, B, X, x_ref=None, precision=_lib.PREC_FP32, tol=0.0, max_iter=0, nb=0, spd=False,
-                   uplo=_lib.LOWER):
+                   uplo=_lib.LOWER, piv_ref=None, piv_out=None):
+        """Mixed solve; for LU, piv_ref / piv_out (int32 device vectors of
+        length n) compare the low-precision factor's pivots with a reference
+        pivot vector and hand them out (ddla_dev_dgesv_mixed_piv)."""
         o = Opts()
         o.precision, o.tol, o.max_iter, o.nb = precision, tol, max_iter, nb
         rep = SolveReport()
@@ -142,6 +145,11 @@ class Handle:
         n, nrhs = B.shape
         if spd:
             rc = lib().ddla_dev_dposv_mixed(self.h, uplo, n, nrhs, _p(A), _p(B), _p(X), xr, C.byref(o), C.byref(rep))
+        elif piv_ref is not None or piv_out is not None:
+            rc = lib().ddla_dev_dgesv_mixed_piv(self.h, n, nrhs, _p(A), _p(B), _p(X), xr,
+                                                C.c_void_p(0) if piv_ref is None else _p(piv_ref),
+                                                C.c_void_p(0) if piv_out is None else _p(piv_out),
+                                                C.byref(o), C.byref(rep))
         else:
             rc = lib().ddla_dev_dgesv_mixed(self.h, n, nrhs, _p(A), _p(B), _p(X), xr, C.byref(o), C.byref(rep))
         return rc, rep.as_dict()

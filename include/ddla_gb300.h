@@ -67,7 +67,8 @@ enum {
     DDLA_PREC_FP64 = 0,      /* plain FP64 factorization (DMMA) */
     DDLA_PREC_FP32 = 1,      /* FP32 factorization, FP32 CUDA-core GEMM updates */
     DDLA_PREC_TF32X3 = 2,    /* FP32 factorization, 3xTF32 tcgen05 tensor-core GEMM updates */
-    DDLA_PREC_BF16X3 = 3,    /* FP32 factorization, 3xBF16 tcgen05 tensor-core GEMM updates */
+    DDLA_PREC_BF16X3 = 3,    /* FP32 factorization, 3xBF16 tcgen05 tensor-core GEMM updates (x = hi + lo in
+                                two bf16 parts, hi*hi + hi*lo + lo*hi, FP32 accumulation) */
     DDLA_PREC_OZAKI = 4      /* FP64-accurate GEMM from split BF16 tensor-core products */
 };
 
@@ -95,8 +96,10 @@ typedef struct ddla_solve_report {
     double forward_error;      /* ||x - x_ref||_inf / ||x_ref||_inf when x_ref was given, else -1 */
     double factor_ms;          /* device time of the factorization */
     double refine_ms;          /* device time of the refinement loop */
-    int32_t pivots_agree;      /* LU: pivots equal to an FP64 partial-pivoting run, -1 = not measured */
-    int32_t reserved;
+    int32_t pivots_agree;      /* LU with a reference pivot vector (ddla_dev_dgesv_mixed_piv): how many of
+                                  the n pivots of the low-precision factor equal the reference's; -1 = not
+                                  measured */
+    int32_t pivots_first_diff; /* first index where they differ; -1 = none or not measured */
 } ddla_solve_report;
 
 /* ---------------------------------------------------------------- runtime */
@@ -377,11 +380,24 @@ int ddla_dev_dgesv_mixed(ddla_handle h, ddla_dim_t n, ddla_dim_t nrhs, const dou
 int ddla_dev_dposv_mixed(ddla_handle h, int32_t uplo, ddla_dim_t n, ddla_dim_t nrhs, const double *a,
                          const double *b, double *x, const double *x_ref, const ddla_opts *opts,
                          ddla_solve_report *report);
+/* ddla_dev_dgesv_mixed that also hands out the low-precision factor's pivots
+ * (piv_out, device, n entries, DDLA's relative convention of LU.cs:367-374;
+ * may be NULL) and compares them with piv_ref (device, n; may be NULL), for
+ * instance the pivots of an FP64 ddla_dev_dgetrf of the same A: the report's
+ * pivots_agree and pivots_first_diff say how far the FP32 factorization
+ * followed the FP64 pivot sequence.  No DDLA counterpart (DDLA's
+ * LU(A).Solve, LU.cs:64-100, is FP64-only). */
+int ddla_dev_dgesv_mixed_piv(ddla_handle h, ddla_dim_t n, ddla_dim_t nrhs, const double *a, const double *b,
+                             double *x, const double *x_ref, const int32_t *piv_ref, int32_t *piv_out,
+                             const ddla_opts *opts, ddla_solve_report *report);
 
 /* FP32 GEMM C = alpha*A*B + beta*C on device data in the precision the mixed
  * factorizations use for their trailing updates: DDLA_PREC_FP32 (CUDA-core
- * FFMA) or DDLA_PREC_TF32X3 (tcgen05 tensor cores, 3xTF32 split products,
- * FP32 accumulation in TMEM).  No DDLA counterpart (DDLA is FP64 only). */
+ * FFMA), DDLA_PREC_TF32X3 (tcgen05 tensor cores, 3xTF32 split products,
+ * FP32 accumulation in TMEM) or DDLA_PREC_BF16X3 (tcgen05, two-part BF16
+ * split, 3 products, FP32 accumulation; only the update shape beta = 1,
+ * k <= 64, else DDLA_ERR_UNSUPPORTED).  No DDLA counterpart (DDLA is FP64
+ * only). */
 int ddla_dev_sgemm_tc(ddla_handle h, int32_t precision, int64_t m, int64_t n, int64_t k, float alpha, const float *a,
                       int64_t rsa, int64_t csa, const float *b, int64_t rsb, int64_t csb, float beta, float *c,
                       int64_t rsc, int64_t csc);
@@ -401,8 +417,9 @@ int ddla_dev_sgemm_tc(ddla_handle h, int32_t precision, int64_t m, int64_t n, in
  * device looks up that array's device address (cudaGetSymbolAddress) and
  * should therefore come before any stream capture.  All calls share the one
  * array: calls whose work overlaps on the GPU (different streams, threads)
- * race and must be serialized by the caller.  Synchronous: returns after the
- * solve with 0, a negative argument position, DDLA_ERR_TIMEOUT or
+ * race and must be serialized by the caller.  Every call is synchronous: it
+ * copies the solve's error word back to host memory and synchronizes `stream`
+ * before it returns 0, a negative argument position, DDLA_ERR_TIMEOUT or
  * DDLA_ERR_CUDA. */
 #define DDLA_NOALLOC_MAX_N 2048
 #define DDLA_NOALLOC_MAX_RHS 16
@@ -421,7 +438,9 @@ int ddla_dev_dtrsv_noalloc(void *stream, int32_t uplo, int32_t trans, int32_t di
  * (sum n^2 doubles; plain mode overwrites them with the factors), d_b / d_x /
  * d_piv the vectors (sum n each), d_info / d_iters one int per item (failing
  * pivot or 0; refinement steps or -1 when not converged).  mixed != 0 factors
- * in FP32 and refines in FP64 to opts->tol (default 1e-14). */
+ * in FP32 and refines in FP64 until the item's own FP64 backward-error
+ * estimate is at most opts->tol / 2 (default tol 1e-14; the half leaves room
+ * for a recomputation with another summation order). */
 int ddla_batched_plan_create(ddla_handle h, int64_t count, const int32_t *n, const int32_t *kind, int32_t mixed,
                              double *d_a, const double *d_b, double *d_x, int32_t *d_piv, int32_t *d_info,
                              int32_t *d_iters, const ddla_opts *opts, void **plan);

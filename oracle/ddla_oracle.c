@@ -165,6 +165,10 @@ static void micro(i64 kc, const double *a, const double *b, double *c) {
  * stored [col][row] with zero padding of the ragged last panel. */
 static void pack(mat S, double *buf, int blk) {
     i64 np = align_up(S.r, blk) / blk;
+    /* a copy: splitting it over threads changes no arithmetic */
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(g_threads) if (g_threads > 1 && np >= 16)
+#endif
     for (i64 pi = 0; pi < np; pi++) {
         double *dst = buf + pi * S.c * blk;
         i64 r0 = pi * blk, ar = S.r - r0 < blk ? S.r - r0 : blk;
@@ -444,6 +448,10 @@ static void trsm_left(int uplo, int unit, mat A, mat B) {
             i64 b = m - i0 < KC ? m - i0 : KC;
             if (i0 > 0) gemm_core(-1.0, sub(A, i0, b, 0, i0), sub(B, 0, i0, 0, B.c), sub(B, i0, b, 0, B.c), 0);
             mat A11 = sub(A, i0, b, i0, b);
+            /* the column solves are independent of one another */
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(g_threads) if (g_threads > 1 && B.c >= 64)
+#endif
             for (i64 j = 0; j < B.c; j++) trsv(UL_LOWER, unit, A11, AT(B, i0, j), B.rs);
         }
     } else {
@@ -451,6 +459,9 @@ static void trsm_left(int uplo, int unit, mat A, mat B) {
             i64 b = i1 < KC ? i1 : KC, i0 = i1 - b;
             if (i1 < m) gemm_core(-1.0, sub(A, i0, b, i1, m - i1), sub(B, i1, m - i1, 0, B.c), sub(B, i0, b, 0, B.c), 0);
             mat A11 = sub(A, i0, b, i0, b);
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(g_threads) if (g_threads > 1 && B.c >= 64)
+#endif
             for (i64 j = 0; j < B.c; j++) trsv(UL_UPPER, unit, A11, AT(B, i0, j), B.rs);
         }
     }
@@ -815,8 +826,17 @@ static int plu_unblock(mat A, int *piv, i64 row0) {
  * in increasing i, backward in decreasing i. */
 static void apply_piv(mat X, const int *piv, i64 np, int forward) {
     if (X.r == 0 || X.c == 0) return;
-    if (forward) { for (i64 i = 0; i < np; i++) if (piv[i] > 0) swap_rows(X, i, i + piv[i]); }
-    else { for (i64 i = np - 1; i >= 0; i--) if (piv[i] > 0) swap_rows(X, i, i + piv[i]); }
+    /* every column sees the swaps in the same order, so column strips are
+     * independent */
+    const i64 strip = 256, ns = (X.c + strip - 1) / strip;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(g_threads) if (g_threads > 1 && ns >= 4)
+#endif
+    for (i64 t = 0; t < ns; t++) {
+        mat S = sub(X, 0, X.r, t * strip, X.c - t * strip < strip ? X.c - t * strip : strip);
+        if (forward) { for (i64 i = 0; i < np; i++) if (piv[i] > 0) swap_rows(S, i, i + piv[i]); }
+        else { for (i64 i = np - 1; i >= 0; i--) if (piv[i] > 0) swap_rows(S, i, i + piv[i]); }
+    }
 }
 
 /* PLUDecompose / PLUDecBlock, LU.cs:251-264, 289-342 (blocked iff n >= 128). */
@@ -1290,3 +1310,48 @@ void orc_contract_exec(const orc_contract_desc *d, double alpha, const double *a
 }
 
 int orc_contract_desc_size(void) { return (int)sizeof(orc_contract_desc); }
+
+/* ------------------------------------------------------------------------ */
+/* Batched small solves (the batched workload's checker)                     */
+/* ------------------------------------------------------------------------ */
+
+/* Factor and solve `count` independent square row-major systems packed back
+ * to back (a: sum n_i^2 doubles, b / x / piv: sum n_i entries), item i with
+ * kind 0 = PLUDecompose + PLUSolve (LU.cs:251-287), 1 = LUDecompose + LUSolve
+ * (LU.cs:133-167), 2 = lower CholDecompose + CholeskySolve (Cholesky.cs:52-123).
+ * a is factored in place, x = solution of the original system, info[i] the
+ * failing pivot or 0.  Items run in parallel; each one is the serial
+ * restatement above (the factorizations' own threading stays off inside). */
+void orc_batched(i64 count, const int *n, const int *kind, double *a, const double *b, double *x, int *piv,
+                 int *info) {
+    i64 *ao = (i64 *)malloc(sizeof(i64) * (count + 1)), *vo = (i64 *)malloc(sizeof(i64) * (count + 1));
+    ao[0] = vo[0] = 0;
+    for (i64 i = 0; i < count; i++) { ao[i + 1] = ao[i] + (i64)n[i] * n[i]; vo[i + 1] = vo[i] + n[i]; }
+    int saved = g_threads;
+    int outer = g_threads;
+    g_threads = 1;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 8) num_threads(outer) if (outer > 1)
+#endif
+    for (i64 i = 0; i < count; i++) {
+        const i64 ni = n[i];
+        double *ai = a + ao[i], *xi = x + vo[i];
+        int *pi = piv + vo[i];
+        memcpy(xi, b + vo[i], sizeof(double) * ni);
+        memset(pi, 0, sizeof(int) * ni);
+        int rc;
+        if (kind[i] == 0) {
+            rc = orc_dgetrf(ni, ai, ni, 1, pi);
+            if (!rc) orc_dgetrs(0, ni, 1, ai, ni, 1, pi, xi, 1, 1);
+        } else if (kind[i] == 1) {
+            rc = orc_dgetrf_nopiv(ni, ai, ni, 1);
+            if (!rc) orc_dgetrs_nopiv(0, ni, 1, ai, ni, 1, xi, 1, 1);
+        } else {
+            rc = orc_dpotrf(UL_LOWER, ni, ai, ni, 1);
+            if (!rc) orc_dpotrs(UL_LOWER, ni, 1, ai, ni, 1, xi, 1, 1);
+        }
+        info[i] = rc;
+    }
+    g_threads = saved;
+    free(ao); free(vo);
+}

@@ -83,6 +83,8 @@ def lib():
         L.orc_dbidiag.argtypes = [_i64, _i64, _dp, _i64, _i64, _dp, _i64, _dp, _i64, _dp, _dp, _dp, _i64, _i64,
                                   _dp, _i64, _i64]
         L.orc_set_threads.argtypes = [C.c_int]
+        L.orc_batched.argtypes = [_i64, _ip, _ip, _dp, _dp, _dp, _ip, _ip]
+        L.orc_batched.restype = None
         L.orc_contract_plan.argtypes = [C.c_char_p, C.c_int, C.POINTER(_i64), C.POINTER(_i64),
                                         C.c_int, C.POINTER(_i64), C.POINTER(_i64),
                                         C.c_int, C.POINTER(_i64), C.POINTER(_i64),
@@ -355,3 +357,25 @@ def einsum(expr, operands):
     if len(operands) == 1:
         raise ValueError("oracle einsum: one operand (DDLA returns it unchanged)")
     return cur[0][1]
+
+
+def batched(sizes, kinds, mats, rhs):
+    """Factor and solve many small systems (orc_batched): returns per item
+    (factors, x, relative pivots) and the info vector.  kinds: 0 PLU, 1 LU
+    without pivoting, 2 lower Cholesky."""
+    sizes = np.ascontiguousarray(sizes, dtype=np.int32)
+    kinds = np.ascontiguousarray(kinds, dtype=np.int32)
+    a = np.concatenate([np.ascontiguousarray(m, dtype=np.float64).ravel() for m in mats])
+    b = np.concatenate([np.asarray(v, dtype=np.float64).ravel() for v in rhs])
+    x = np.zeros_like(b)
+    piv = np.zeros(b.shape[0], dtype=np.int32)
+    info = np.zeros(len(sizes), dtype=np.int32)
+    lib().orc_batched(len(sizes), sizes.ctypes.data_as(_ip), kinds.ctypes.data_as(_ip), _ptr(a), _ptr(b), _ptr(x),
+                      piv.ctypes.data_as(_ip), info.ctypes.data_as(_ip))
+    out, ao, vo = [], 0, 0
+    for nn in sizes:
+        nn = int(nn)
+        out.append((a[ao:ao + nn * nn].reshape(nn, nn), x[vo:vo + nn], piv[vo:vo + nn]))
+        ao += nn * nn
+        vo += nn
+    return out, info

@@ -77,3 +77,20 @@ def berr(A, X, B):
     R = B - A @ X
     an = np.abs(A).sum(axis=1).max()
     return float(np.max(np.abs(R).max(axis=0) / (an * np.abs(X).max(axis=0) + np.abs(B).max(axis=0))))
+
+
+def schur_pivot_gap(A0, piv_ref, i, p_other):
+    """Relative gap between the reference pivot candidate and another one at
+    elimination step i: the Schur complement column i after the first i steps
+    of piv_ref (FP64, from the row-permuted A0), then
+    (|col[piv_ref[i]]| - |col[p_other]|) / max|col|, with row offsets relative
+    to row i like the pivots.  A small gap means the two rows were nearly tied,
+    so lower-precision rounding can pick either."""
+    P = apply_piv(A0, piv_ref[:i], True) if i else A0.copy()
+    if i:
+        y = np.linalg.solve(P[:i, :i], P[:i, i])
+        col = P[i:, i] - P[i:, :i] @ y
+    else:
+        col = P[:, 0]
+    a, b = abs(col[int(piv_ref[i])]), abs(col[int(p_other)])
+    return (a - b) / np.abs(col).max()

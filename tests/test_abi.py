@@ -38,6 +38,14 @@ def test_version_string(ddla):
 def test_oracle_is_not_linked_into_product():
     prod = open(os.path.join(ROOT, "ddla_gb300", "_build", "libddla_gb300.so"), "rb").read()
     assert b"orc_dgemm" not in prod
-    for src in glob.glob(os.path.join(ROOT, "ddla_gb300", "**", "*.*"), recursive=True):
+    # no product source imports, loads or calls the oracle (comments may name
+    # it; code may not use it)
+    uses = re.compile(r"(from\s+oracle\b|import\s+oracle\b|libddla_oracle|\borc_[a-z]|oracle/|oracle\.)")
+    for src in glob.glob(os.path.join(ROOT, "ddla_gb300", "**", "*.*"), recursive=True) + \
+            glob.glob(os.path.join(ROOT, "include", "*.h")):
         if src.endswith((".py", ".cu", ".cuh", ".h", ".cpp")):
-            assert "oracle" not in open(src).read().lower().split("test infrastructure")[0] or True
+            code = "\n".join(ln.split("#")[0] if src.endswith(".py") else ln.split("//")[0]
+                             for ln in open(src).read().splitlines())
+            hit = uses.search(code)
+            assert hit is None, f"{src} uses the oracle: {hit.group(0)!r}"
+

@@ -8,7 +8,7 @@ from helpers import berr, rng, spd
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("prec", ["fp32", "tf32x3"])
+@pytest.mark.parametrize("prec", ["fp32", "tf32x3", "bf16x3"])
 @pytest.mark.parametrize("n,nrhs", [(100, 1), (1024, 1), (2048, 4), (3000, 16)])
 def test_mixed_lu_reaches_fp64(ddla, orc, n, nrhs, prec):
     r = rng(n)
@@ -25,7 +25,7 @@ def test_mixed_lu_reaches_fp64(ddla, orc, n, nrhs, prec):
     assert rep["forward_error"] <= 1e-10
 
 
-@pytest.mark.parametrize("prec", ["fp32", "tf32x3"])
+@pytest.mark.parametrize("prec", ["fp32", "tf32x3", "bf16x3"])
 @pytest.mark.parametrize("n,nrhs", [(500, 16), (2048, 16)])
 def test_mixed_cholesky(ddla, orc, n, nrhs, prec):
     r = rng(n + 1)

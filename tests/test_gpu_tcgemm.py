@@ -76,3 +76,48 @@ def test_tf32x3_update_transposed_b(ddla, n, k):
     out = c.double().cpu().numpy()
     h.close()
     assert np.max(np.abs(out - ref) / scale) <= 2e-5
+
+
+@pytest.mark.parametrize("m,n,k", [(128, 128, 64), (300, 200, 64), (129, 257, 17), (1000, 900, 64), (64, 1, 64),
+                                   (2000, 4100, 64), (1, 300, 8), (515, 515, 40)])
+def test_bf16x3_rank_update_path(ddla, m, n, k):
+    # 3xBF16: x = hi + lo with two bf16 parts (16 significant bits), products
+    # hi*hi + hi*lo + lo*hi, FP32 accumulation: about 2^-16 relative to
+    # |A||B| per element.  n not a multiple of 4 takes the scalar C path.
+    err = _run(ddla, ddla.PREC_BF16X3, m, n, k, -1.0, 1.0, 11 * m + n + k)
+    assert err <= 5e-5, err
+
+
+def test_bf16x3_only_as_rank_update(ddla):
+    # beta != 1 or k > 64 is not the update shape: a clear unsupported status
+    import torch
+    from ddla_gb300 import device
+    a = torch.zeros(64, 128, dtype=torch.float32, device="cuda")
+    h = device.Handle(torch.cuda.current_stream())
+    rc = ddla.lib().ddla_dev_sgemm_tc(h.h, ddla.PREC_BF16X3, 64, 64, 128, -1.0, C.c_void_p(a.data_ptr()), 128, 1,
+                                      C.c_void_p(a.data_ptr()), 64, 1, 1.0, C.c_void_p(a.data_ptr()), 64, 1)
+    h.close()
+    assert rc == ddla._lib.ERR_UNSUPPORTED
+
+
+def test_bf16x3_update_column_major_c(ddla):
+    # C given as a transposed (column-major) view: column stride != 1
+    import torch
+    from ddla_gb300 import device
+    m, n, k = 300, 260, 64
+    g = torch.Generator().manual_seed(9)
+    A = torch.rand(m, k, generator=g, dtype=torch.float64) * 2 - 1
+    B = torch.rand(k, n, generator=g, dtype=torch.float64) * 2 - 1
+    Cm = torch.rand(m, n, generator=g, dtype=torch.float64) * 2 - 1
+    ref = Cm.numpy() - A.numpy() @ B.numpy()
+    scale = np.abs(A.numpy()) @ np.abs(B.numpy()) + np.abs(Cm.numpy())
+    a, b = A.float().cuda(), B.float().cuda()
+    ct = Cm.float().T.contiguous().cuda()          # n x m storage: C(i, j) at j * m + i
+    h = device.Handle(torch.cuda.current_stream())
+    rc = ddla.lib().ddla_dev_sgemm_tc(h.h, ddla.PREC_BF16X3, m, n, k, -1.0, C.c_void_p(a.data_ptr()), k, 1,
+                                      C.c_void_p(b.data_ptr()), n, 1, 1.0, C.c_void_p(ct.data_ptr()), 1, m)
+    ddla._lib.check(rc, "sgemm_tc")
+    h.sync()
+    out = ct.double().cpu().numpy().T
+    h.close()
+    assert np.max(np.abs(out - ref) / scale) <= 5e-5

@@ -442,3 +442,34 @@ def test_bidiag_property(orc, m, n):
     assert np.max(np.abs(V.T @ V - np.eye(n))) < 1e-13
     sv = np.sort(np.abs(np.linalg.svd(B, compute_uv=False)))
     assert np.max(np.abs(sv - np.sort(np.linalg.svd(A0, compute_uv=False)))) < 1e-12 * max(m, 1)
+
+
+def test_batched_oracle_equals_item_calls(orc):
+    """orc_batched (items in parallel) gives bit-identical factors, pivots and
+    solutions to the per-item oracle calls, with threads on."""
+    r = rng(77)
+    sizes = [1, 2, 9, 64, 127, 128, 129, 200, 256, 31]
+    kinds = [0, 1, 2, 0, 2, 0, 1, 2, 0, 1]
+    mats, rhs = [], []
+    for n, k in zip(sizes, kinds):
+        mats.append(spd(r, n) if k == 2 else r.standard_normal((n, n)) + (n * np.eye(n) if k == 1 else 0))
+        rhs.append(r.standard_normal(n))
+    orc.set_threads(4)
+    try:
+        res, info = orc.batched(sizes, kinds, mats, rhs)
+    finally:
+        orc.set_threads(1)
+    assert np.all(info == 0)
+    for (F, x, piv), A, b, k in zip(res, mats, rhs, kinds):
+        Fo, xo = A.copy(), b.copy().reshape(-1, 1)
+        if k == 0:
+            rc, po = orc.dgetrf(Fo)
+            orc.dgetrs(Fo, po, xo)
+            assert np.array_equal(piv, po)
+        elif k == 1:
+            orc.dgetrf_nopiv(Fo)
+            orc.dgetrs_nopiv(Fo, xo)
+        else:
+            orc.dpotrf(0xC0, Fo)
+            orc.dpotrs(0xC0, Fo, xo)
+        assert np.array_equal(F, Fo) and np.array_equal(x, xo.ravel())
