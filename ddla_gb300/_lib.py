@@ -50,7 +50,7 @@ class SolveReport(C.Structure):
     _fields_ = [("iterations", C.c_int32), ("converged", C.c_int32), ("precision", C.c_int32),
                 ("info", C.c_int32), ("backward_error", C.c_double), ("forward_error", C.c_double),
                 ("factor_ms", C.c_double), ("refine_ms", C.c_double), ("pivots_agree", C.c_int32),
-                ("pivots_first_diff", C.c_int32)]
+                ("pivots_first_diff", C.c_int32), ("growth", C.c_double), ("diag_ratio", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -145,6 +145,10 @@ _SIGS = {
                                        C.POINTER(SolveReport)]),
     "ddla_dev_dgesv_mixed_piv": (C.c_int, [_h, _i64, _i64, _pd, _pd, _pd, _pd, _pi, _pi, C.POINTER(Opts),
                                            C.POINTER(SolveReport)]),
+    "ddla_dev_dsysv_mixed": (C.c_int, [_h, _i32, _i64, _i64, _pd, _pd, _pd, _pd, C.POINTER(Opts),
+                                       C.POINTER(SolveReport)]),
+    "ddla_dsysv_mixed": (C.c_int, [_i32, _i64, _i64, _pd, _i64, _i64, _pd, _i64, _i64, _pd, _i64, _i64, _pd,
+                                   C.POINTER(Opts), C.POINTER(SolveReport)]),
 }
 
 

@@ -7,20 +7,21 @@
 //   1. each CTA finds the first largest |a(r,j)| among its rows r >= j
 //      (NaN compares smaller than everything, like bli_damaxv as DDLA
 //      documents it, DDLA/BLAS/1v.cs:29-42);
-//   2. it stores (value, row) into every CTA's candidate table (DSMEM) and a
-//      copy of its candidate row, plus row j if it owns it, in local
-//      double-buffered slots;
-//   3. one cluster barrier;
-//   4. every CTA picks the same winner (largest value, lowest row on ties),
-//      reads the pivot row from the winner's shared memory, and the owners of
-//      rows j and p swap them (whole panel rows, LU.cs:367-374);
-//   5. rows below j are scaled by 1/pivot (InvScal, a zero pivot stops the
+//   2. it pushes a package -- (value, row, origin) and a finished copy of the
+//      candidate row -- into an inbox slot of every CTA of the cluster with
+//      st.async stores that complete on the receiver's mbarrier; the owner of
+//      row j pushes row j as well;
+//   3. every CTA waits on its own mbarrier until all packages of column j have
+//      landed (no cluster barrier, no remote loads), picks the same winner
+//      (largest value, lowest row on ties) from its local inbox, and the owners
+//      of rows j and p swap them (whole panel rows, LU.cs:367-374);
+//   4. rows below j are scaled by 1/pivot (InvScal, a zero pivot stops the
 //      factorization and reports it, DDLA/BLAS/1v.cs:97-103) and rank-1
 //      updated (GeR(-1), LU.cs:357-360).
-// The published slots are double-buffered on the column parity, so one
-// cluster barrier per column orders all cross-CTA traffic: a slot written in
-// column j+2 was last read in column j, before its reader reached the barrier
-// of column j+1.
+// The inboxes are double-buffered on the column parity.  A CTA pushes the
+// packages of column j+1 only after it has read its inbox of column j, and no
+// CTA can send packages of column j+2 before it received those of column j+1
+// from every CTA, so a slot is never overwritten while it is being read.
 //
 // Every row carries its origin (row index at panel start), so the interchange
 // of the rest of the matrix is a gather of the touched rows (at most 2w),
@@ -50,6 +51,7 @@ struct PanelArgs {
     int *touch_count, *touch_rows, *touch_src;
     T *inv;   // optional: inverse of the unit-lower w x w block L11 (row-major, ld TRI_TB)
     int *calu;   // tournament-pivoting scratch (k_panel_calu)
+    int *err;    // set to 1 when a bounded wait of the cluster panel gives up
 };
 
 // Pivot search keys: |x| as an unsigned integer bit pattern plus one, NaN as
@@ -71,8 +73,14 @@ __device__ __forceinline__ unsigned long long amax_key(double v) {
 
 constexpr int PANEL_SUB = 8;   // sub-panel width (deferred updates)
 
+// A package: 16-byte header (key at byte 0, row at 8, origin at 12), then
+// the row's w values; slots are sized for PANEL_WMAX values.
+constexpr int PKG_HDR = 16;
+template <typename T> constexpr int pkg_stride() { return PKG_HDR + PANEL_WMAX * (int)sizeof(T); }
+constexpr long long PANEL_SPIN = 1LL << 22;   // bounded waits (try_wait rounds)
+
 struct PanelSmem {
-    size_t rows, origin, ucur, u8, pub, cand_val, cand_idx, cand_org, jorg, red, total;
+    size_t rows, origin, u8, inbox, outbox, red, total;
 };
 
 template <typename T>
@@ -86,13 +94,9 @@ __host__ __device__ inline PanelSmem panel_smem_layout(int rows_per, int w) {
     };
     L.rows = take(sizeof(T) * (size_t)rows_per * (w + 1));
     L.origin = take(sizeof(int) * (size_t)rows_per);
-    L.ucur = take(sizeof(T) * w);
     L.u8 = take(sizeof(T) * (size_t)w * PANEL_SUB);
-    L.pub = take(sizeof(T) * 4 * w);   // [parity][candidate | row j+1][w]
-    L.cand_val = take(sizeof(typename KeyT<T>::type) * 2 * PANEL_MAXCS);
-    L.cand_idx = take(sizeof(int) * 2 * PANEL_MAXCS);
-    L.cand_org = take(sizeof(int) * 2 * PANEL_MAXCS);
-    L.jorg = take(sizeof(int) * 2);
+    L.inbox = take((size_t)2 * (PANEL_MAXCS + 1) * pkg_stride<T>());   // [parity][sender | row j][package]
+    L.outbox = take((size_t)2 * pkg_stride<T>());                        // [candidate | row j+1]
     L.red = take((sizeof(typename KeyT<T>::type) + sizeof(int)) * (PANEL_THREADS / 32) + 16);
     L.total = o;
     return L;
@@ -149,45 +153,80 @@ __device__ __forceinline__ void ld8(const double *p, double *v) {
     }
 }
 
+__device__ __forceinline__ unsigned su32p(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+// Shared-memory address of the same variable in CTA `rank` of the cluster.
+__device__ __forceinline__ unsigned cluster_addr(const void *p, int rank) {
+    unsigned out;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(out) : "r"((unsigned)__cvta_generic_to_shared(p)),
+                 "r"(rank));
+    return out;
+}
+// 16 bytes into another CTA's shared memory; the store completes 16 bytes of
+// the transaction count of that CTA's mbarrier
+__device__ __forceinline__ void st_async16(unsigned addr, uint4 v, unsigned mbar) {
+    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.b32 [%0], {%1, %2, %3, %4}, [%5];" ::"r"(
+                     addr),
+                 "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w), "r"(mbar)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_cluster(unsigned mbar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(mbar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ void mbar_expect(unsigned mbar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
+}
+
 // Panel factorization, one cluster (see the file comment).  The columns are
 // processed in sub-panels of PANEL_SUB: within a sub-panel the rank-1 updates
 // touch only the sub-panel's columns; the columns to its right receive the
 // sub-panel's pivot rows (kept in U8) as one rank-PANEL_SUB update after its
 // last column, which divides the shared-memory traffic of the updates by
 // about PANEL_SUB.  Rows that leave their CTA (pivot candidates, row j+1) are
-// published with every pending update applied to the copy.  Per column the
-// critical path is: winner -> swap -> scale + update of the next column and
-// its local argmax -> finished copies of the rows to publish -> push to every
-// CTA (DSMEM stores) -> barrier arrive; the remaining updates run between the
-// barrier's arrive and wait.
+// packaged with every pending update applied to the copy.  Per column the
+// critical path is: wait for the packages -> winner -> swap -> scale + update
+// of the next column and its local argmax -> packages of the next column ->
+// push to every CTA; the remaining updates run while the other CTAs' packages
+// are in flight.  Every wait is bounded: on timeout the CTA records the error
+// in a.err, stops factoring and meets the others at the final cluster barrier
+// (they time out the same way, waiting for its packages).
 template <typename T>
 __global__ void __launch_bounds__(PANEL_THREADS, 1) k_panel_lu(PanelArgs<T> a) {
     cg::cluster_group cluster = cg::this_cluster();
     const int CS = (int)cluster.num_blocks();
     const int rank = (int)cluster.block_rank();
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     extern __shared__ __align__(16) unsigned char smem[];
     const int w = a.w, WP = w + 1, rp = a.rows_per;
     const PanelSmem L = panel_smem_layout<T>(rp, w);
     T *rows = (T *)(smem + L.rows);
     int *origin = (int *)(smem + L.origin);
     typedef typename KeyT<T>::type K;
-    T *ucur = (T *)(smem + L.ucur);
     T *U8 = (T *)(smem + L.u8);   // [c][k]: pivot rows of the current sub-panel, column-major by k
-    T *pub = (T *)(smem + L.pub); // [parity][0: candidate, 1: row j+1][w], read by the other CTAs
-    K *cand_val = (K *)(smem + L.cand_val);
-    int *cand_idx = (int *)(smem + L.cand_idx);
-    int *cand_org = (int *)(smem + L.cand_org);
-    int *jorg = (int *)(smem + L.jorg);
+    unsigned char *inbox = smem + L.inbox;
+    unsigned char *outbox = smem + L.outbox;
     K *red_v = (K *)(smem + L.red);
     int *red_i = (int *)(red_v + PANEL_THREADS / 32);
+    constexpr int STRIDE = pkg_stride<T>();
+    // bytes pushed per package (header + w values, whole 16-byte chunks)
+    const int PKG = PKG_HDR + (((int)sizeof(T) * w + 15) & ~15);
+    auto slot = [&](int parity, int src) { return inbox + (parity * (PANEL_MAXCS + 1) + src) * STRIDE; };
 
     __shared__ int spiv[PANEL_WMAX];   // relative pivots, stored to global memory at the end
+    __shared__ __align__(8) unsigned long long full[2];   // inbox mbarriers, by column parity
     for (int c = tid; c < PANEL_WMAX; c += PANEL_THREADS) spiv[c] = 0;
     const int base = rank * rp;
     int nloc = a.m - base;
     nloc = nloc < 0 ? 0 : (nloc > rp ? rp : nloc);
     auto owns = [&](int g) { return g >= base && g < base + nloc; };
+    const int kmax = a.m < w ? a.m : w;
+    const unsigned col_bytes = (unsigned)((CS + 1) * PKG);   // every CTA's candidate + row j
 
     if (rank == 0 && tid == 0) *a.touch_count = 0;
     for (int e = tid; e < nloc * w; e += PANEL_THREADS) {
@@ -195,24 +234,55 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_panel_lu(PanelArgs<T> a) {
         rows[l * WP + c] = a.P[(i64)(base + l) * a.rs + (i64)c * a.cs];
     }
     for (int l = tid; l < nloc; l += PANEL_THREADS) origin[l] = base + l;
-    __syncthreads();
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32p(&full[0])) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32p(&full[1])) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        if (kmax > 0) mbar_expect(su32p(&full[0]), col_bytes);
+        if (kmax > 1) mbar_expect(su32p(&full[1]), col_bytes);
+    }
+    // every CTA's mbarriers are armed before anyone pushes
+    cluster.sync();
 
-    // Publish (value, row index, origin) of my candidate cb for column jn in
-    // buffer jn&1 of every CTA; the rows themselves (finished copies in my
-    // pub[jn&1]) are read by the other CTAs after the barrier.
-    auto push = [&](int jn, K cv, int cb) {
-        const int nbf = jn & 1;
-        if (tid < CS) {
-            cluster.map_shared_rank(cand_val, tid)[nbf * PANEL_MAXCS + rank] = cv;
-            cluster.map_shared_rank(cand_idx, tid)[nbf * PANEL_MAXCS + rank] = cb;
-            cluster.map_shared_rank(cand_org, tid)[nbf * PANEL_MAXCS + rank] = cb != INT_MAX ? origin[cb - base] : 0;
-            if (owns(jn)) cluster.map_shared_rank(jorg, tid)[nbf] = origin[jn - base];
+    // Stage the packages of column c in the outbox (candidate cb with key cv;
+    // row c if this CTA owns it; `val(row, col)` gives a row's finished
+    // value) and push them: warp d sends to CTA d, the candidate into slot
+    // `rank`, row c into slot PANEL_MAXCS.
+    auto stage_push = [&](int c, K cv, int cb, auto val) {
+        const bool with_row = owns(c);
+        unsigned char *ob_c = outbox, *ob_r = outbox + STRIDE;
+        if (tid < w) {
+            if (cb != INT_MAX) ((T *)(ob_c + PKG_HDR))[tid] = val(rows + (cb - base) * WP, tid, false);
+        } else if (tid >= 64 && tid < 64 + w && with_row) {
+            ((T *)(ob_r + PKG_HDR))[tid - 64] = val(rows + (c - base) * WP, tid - 64, true);
+        }
+        if (tid == PANEL_THREADS - 1) {
+            *(K *)ob_c = cv;
+            *(int *)(ob_c + 8) = cb;
+            *(int *)(ob_c + 12) = cb != INT_MAX ? origin[cb - base] : 0;
+        } else if (tid == PANEL_THREADS - 2 && with_row) {
+            *(K *)ob_r = K(0);
+            *(int *)(ob_r + 8) = c;
+            *(int *)(ob_r + 12) = origin[c - base];
+        }
+        __syncthreads();
+        if (warp < CS) {
+            const int par = c & 1;
+            const unsigned mb = cluster_addr(&full[par], warp);
+            const unsigned dc = cluster_addr(slot(par, rank), warp);
+            const int chunks = PKG / 16;
+            for (int q = lane; q < chunks; q += 32)
+                st_async16(dc + 16 * q, *reinterpret_cast<const uint4 *>(ob_c + 16 * q), mb);
+            if (with_row) {
+                const unsigned dr = cluster_addr(slot(par, PANEL_MAXCS), warp);
+                for (int q = lane; q < chunks; q += 32)
+                    st_async16(dr + 16 * q, *reinterpret_cast<const uint4 *>(ob_r + 16 * q), mb);
+            }
         }
     };
-    auto owner = [&](int g) { return g / rp; };
 
-    const int kmax = a.m < w ? a.m : w;
-    {
+    bool failed = false;
+    if (kmax > 0) {
         K bv = 0;
         int bi = INT_MAX;
         for (int l = tid; l < nloc; l += PANEL_THREADS) {
@@ -220,23 +290,25 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_panel_lu(PanelArgs<T> a) {
             if (v > bv || bi == INT_MAX) { bv = v; bi = base + l; }
         }
         block_argmax<K>(bv, bi, red_v, red_i);
-        // nothing is pending before column 0: the published rows are the rows
-        if (bi != INT_MAX)
-            for (int c = tid; c < w; c += PANEL_THREADS) pub[c] = rows[(bi - base) * WP + c];
-        if (owns(0))
-            for (int c = tid; c < w; c += PANEL_THREADS) pub[w + c] = rows[(0 - base) * WP + c];
-        push(0, bv, bi);
-        cluster.sync();
+        // nothing is pending before column 0: the packages are the rows
+        stage_push(0, bv, bi, [&](const T *row, int c, bool) { return row[c]; });
     }
 
     for (int j = 0; j < kmax; j++) {
         const int buf = j & 1;
         const int s0 = j - j % PANEL_SUB, s1 = s0 + PANEL_SUB < w ? s0 + PANEL_SUB : w;
-        // winner (identical in every CTA, from local copies): lanes 0..CS-1
-        // each read one candidate, then a butterfly over the warp
-        const int lane = tid & 31;
-        K wv = lane < CS ? cand_val[buf * PANEL_MAXCS + lane] : K(0);
-        int wi = lane < CS ? cand_idx[buf * PANEL_MAXCS + lane] : INT_MAX;
+        bool ok = false;
+        {
+            const unsigned mb = su32p(&full[buf]), par = (unsigned)((j >> 1) & 1);
+            for (long long it = 0; it < PANEL_SPIN && !ok; it++) ok = mbar_try_cluster(mb, par);
+        }
+        // (also orders the previous column's row updates before the swap below)
+        if (__syncthreads_or(!ok)) { failed = true; break; }
+        if (tid == 0 && j + 2 < kmax) mbar_expect(su32p(&full[buf]), col_bytes);   // re-arm for column j+2
+        // winner (identical in every CTA, from the local inbox): lanes
+        // 0..CS-1 each read one candidate, then a butterfly over the warp
+        K wv = lane < CS ? *(const K *)slot(buf, lane) : K(0);
+        int wi = lane < CS ? *(const int *)(slot(buf, lane) + 8) : INT_MAX;
         const int myi = wi;
         warp_argmax<K>(wv, wi);
         // the winning row is unique: its CTA is the lane that proposed it
@@ -244,32 +316,23 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_panel_lu(PanelArgs<T> a) {
         const int wr = hit ? __ffs(hit) - 1 : 0;
         const bool none = (wi == INT_MAX);
         const int p = none ? j : wi;
-        const int uorg = none ? jorg[buf] : cand_org[buf * PANEL_MAXCS + wr];
-        // pivot row from the winner's published copy (DSMEM load); the owner
-        // of row p also fetches the old row j from its owner
-        {
-            const T *src = none ? cluster.map_shared_rank(pub, owner(j)) + (buf * 2 + 1) * w
-                                : cluster.map_shared_rank(pub, wr) + (buf * 2) * w;
-            if (tid < w) {
-                const T u = src[tid];
-                ucur[tid] = u;
-                U8[tid * PANEL_SUB + (j - s0)] = u;
-            } else if (p != j && owns(p) && tid >= 64 && tid < 64 + w) {
-                const int c = tid - 64;
-                rows[(p - base) * WP + c] = cluster.map_shared_rank(pub, owner(j))[(buf * 2 + 1) * w + c];
-                if (c == 0) origin[p - base] = jorg[buf];
-            }
+        const unsigned char *upkg = slot(buf, none ? PANEL_MAXCS : wr), *rpkg = slot(buf, PANEL_MAXCS);
+        const T *U = (const T *)(upkg + PKG_HDR);   // the finished pivot row (valid until column j+2)
+        if (tid < w) {
+            const T u = U[tid];
+            U8[tid * PANEL_SUB + (j - s0)] = u;
+            if (owns(j)) rows[(j - base) * WP + tid] = u;   // row j becomes the pivot row
+        } else if (p != j && owns(p) && tid >= 64 && tid < 64 + w) {
+            // row p receives the old row j, in the same pending-update state as the stored rows
+            rows[(p - base) * WP + (tid - 64)] = ((const T *)(rpkg + PKG_HDR))[tid - 64];
         }
-        if (tid == 0) spiv[j] = p - j;   // global store at the end: a store here would
-        __syncthreads();                 // delay this thread's cluster release
-        // row j becomes the finished pivot row (row p, if another, already
-        // holds the old row j in its pending-update state)
-        if (owns(j)) {
-            for (int c = tid; c < w; c += PANEL_THREADS) rows[(j - base) * WP + c] = ucur[c];
-            if (tid == 0) origin[j - base] = uorg;
+        if (tid == PANEL_THREADS - 1) {
+            spiv[j] = p - j;
+            if (owns(j)) origin[j - base] = *(const int *)(upkg + 12);
+            if (p != j && owns(p)) origin[p - base] = *(const int *)(rpkg + 12);
         }
         __syncthreads();
-        const T ujj = ucur[j];
+        const T ujj = U[j];
         if (ujj == T(0)) {
             if (rank == 0 && tid == 0) atomicMin(a.info, (int)(a.row_base + j + 1));
             break;
@@ -283,6 +346,7 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_panel_lu(PanelArgs<T> a) {
         // sub-panel, the whole sub-panel at its edge) and find its local max
         K bv = 0;
         int bi = INT_MAX;
+        const T uj1 = j + 1 < w ? U[j + 1] : T(0);
         for (int l = ls + tid; l < nloc; l += PANEL_THREADS) {
             T *row = rows + l * WP;
             T lv = row[j] * rinv;
@@ -290,7 +354,7 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_panel_lu(PanelArgs<T> a) {
             if (j + 1 < w) {
                 T v = row[j + 1];
                 if (!edge) {
-                    v = fma(lv, -ucur[j + 1], v);
+                    v = fma(lv, -uj1, v);
                 } else {
                     for (int k = s0; k <= j; k++) v = fma(row[k], -U8[(j + 1) * PANEL_SUB + (k - s0)], v);
                 }
@@ -311,31 +375,17 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_panel_lu(PanelArgs<T> a) {
         };
         if (more) {
             block_argmax<K>(bv, bi, red_v, red_i);
-            const int cb = bi;
-            // finished copies, published in pub[(j+1)&1]: candidate (every
-            // pending update), row j+1 (the updates every stored row receives
-            // below)
-            T *pb = pub + ((j + 1) & 1) * 2 * w;
-            if (tid < w) {
-                const int c = tid;
-                if (cb != INT_MAX) {
-                    const T *row = rows + (cb - base) * WP;
-                    pb[c] = c <= j + 1 ? row[c] : pend(row, c);
-                }
-            } else if (tid >= 64 && tid < 64 + w && owns(j + 1)) {
-                const int c = tid - 64;
-                const T *row = rows + (j + 1 - base) * WP;
-                pb[w + c] = (c <= j + 1 || (!edge && c >= s1)) ? row[c] : pend(row, c);
-            }
-            push(j + 1, bv, cb);
-            __syncthreads();   // the finished copies are read before the rows change below
-            // warp 0 made the remote stores: its arrive (a release) waits for
-            // them, so it arrives after its share of the updates below
-            if (tid >= 32) cluster.barrier_arrive();
+            // packages of column j+1: the candidate with every pending update;
+            // row j+1 with the updates every stored row receives below
+            stage_push(j + 1, bv, bi, [&](const T *row, int c, bool is_row) -> T {
+                if (c <= j + 1) return row[c];
+                if (is_row && !edge && c >= s1) return row[c];
+                return pend(row, c);
+            });
         }
-        // updates of the stored rows (overlap the barrier): rank-1 on the
-        // sub-panel's remaining columns, or at the edge the whole sub-panel on
-        // every column to its right
+        // updates of the stored rows (overlap the other CTAs' pushes): rank-1
+        // on the sub-panel's remaining columns, or at the edge the whole
+        // sub-panel on every column to its right
         const int c_lo = j + 2, c_hi = edge ? w : s1;
         if (c_lo < c_hi) {
             for (int l = ls + tid; l < nloc; l += PANEL_THREADS) {
@@ -360,11 +410,10 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_panel_lu(PanelArgs<T> a) {
                 }
             }
         }
-        if (more && tid < 32) cluster.barrier_arrive();
-        __syncthreads();
-        if (more) cluster.barrier_wait();
     }
-    // All DSMEM traffic must finish before any CTA of the cluster exits.
+    if (failed && tid == 0) atomicExch(a.err, 1);
+    // every package sent to this CTA has landed (it waited for all of them),
+    // and no CTA leaves before all have
     cluster.sync();
     if (rank == 0)
         for (int c = tid; c < kmax; c += PANEL_THREADS) a.piv[c] = spiv[c];
@@ -373,7 +422,7 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_panel_lu(PanelArgs<T> a) {
         // rows): warp v forms columns v, v+16, .. by forward substitution, the
         // lanes owning rows lane and lane+32; the column's solved entry y_k is
         // broadcast with a shuffle
-        const int lane = tid & 31, wv = tid >> 5;
+        const int wv = tid >> 5;
         for (int c0 = wv; c0 < TRI_TB; c0 += PANEL_THREADS / 32) {
             T y0 = (lane == c0) ? T(1) : T(0), y1 = (lane + 32 == c0) ? T(1) : T(0);
             if (c0 < kmax) {
@@ -913,6 +962,7 @@ int panel_factor(ddla_handle h, cudaStream_t s, View<T> X, i64 pc, int w, int32_
     a.touch_src = tsrc;
     a.inv = inv;
     a.calu = calu;
+    a.err = h->d_info + INFO_TIMEOUT;
     int cs = max_cluster<T>(h);
     if (cs <= 0) return cs < 0 ? cs : DDLA_ERR_UNSUPPORTED;
     const int64_t want = tune_get("panel.cluster", 0);

@@ -383,9 +383,71 @@ int refine(ddla_handle h, i64 n, int nr, const double *A, const double *B, doubl
     return 0;
 }
 
-int mixed_lu(ddla_handle h, i64 n, i64 nrhs, const double *A, const double *B, double *X, const double *x_ref,
-             const ddla_opts *opts, ddla_solve_report *rep, const int32_t *piv_ref = nullptr,
-             int32_t *piv_out = nullptr) {
+// ---- growth monitor: FP64 figures of the low-precision factors
+//
+// kind 0 (LU, U on and above the diagonal): row value max_j>=i |u_ij|,
+// diagonal |u_ii|; kind 1 (Cholesky, L): sum_k<=i l_ik^2 (= a_ii for an exact
+// factor), diagonal l_ii^2; kind 2 (LDL^T, unit L and D on the diagonal):
+// sum_k<i l_ik^2 |d_k| + |d_i|, diagonal |d_i|.  For Cholesky and LDL^T the
+// row value bounds the entries of |L||D||L^T|, which bounds the backward error
+// of the factorization (so a value far above max|a_ij| signals instability).
+// out[0] max row value, out[1] max diagonal, out[2] min diagonal (bit patterns
+// of non-negative doubles, which order like the values).  One warp per row.
+__global__ void k_growth(const float *F, i64 rs, i64 cs, i64 n, int kind, unsigned long long *out) {
+    const int lane = threadIdx.x & 31;
+    const i64 i = (blockIdx.x * (i64)blockDim.x + threadIdx.x) >> 5;
+    if (i >= n) return;
+    double v = 0.0;
+    if (kind == 0) {
+        for (i64 j = i + lane; j < n; j += 32) v = fmax(v, fabs((double)F[i * rs + j * cs]));
+        for (int off = 16; off > 0; off >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, off));
+    } else {
+        const i64 kend = kind == 1 ? i + 1 : i;
+        for (i64 k = lane; k < kend; k += 32) {
+            const double l = (double)F[i * rs + k * cs];
+            v = fma(l, kind == 1 ? l : l * fabs((double)F[k * rs + k * cs]), v);
+        }
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+        if (kind == 2) v += fabs((double)F[i * rs + i * cs]);
+    }
+    if (lane == 0) {
+        double d = fabs((double)F[i * rs + i * cs]);
+        if (kind == 1) d *= d;
+        if (v == v) atomicMax(&out[0], (unsigned long long)__double_as_longlong(v));
+        if (d == d) {
+            atomicMax(&out[1], (unsigned long long)__double_as_longlong(d));
+            atomicMin(&out[2], (unsigned long long)__double_as_longlong(d));
+        }
+    }
+}
+// max |a_ij| of the FP64 matrix
+__global__ void k_absmax(const double *A, i64 tot, unsigned long long *out) {
+    double v = 0.0;
+    for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < tot; e += (i64)gridDim.x * blockDim.x)
+        v = fmax(v, fabs(A[e]));
+    for (int off = 16; off > 0; off >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, off));
+    if ((threadIdx.x & 31) == 0 && v == v) atomicMax(out, (unsigned long long)__double_as_longlong(v));
+}
+// D z = y for the LDL^T correction solve: row i of Y (n x nr) divided by d_i
+__global__ void k_rows_by_diag(float *Y, i64 n, int nr, const float *F, i64 dstride) {
+    for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < n * nr; e += (i64)gridDim.x * blockDim.x)
+        Y[e] /= F[(e / nr) * dstride];
+}
+// columns c0 .. c0+nr of X (n x ld) <-> a dense n x nr block
+__global__ void k_cols_copy(const double *S, i64 lds, double *D, i64 ldd, i64 n, int nr) {
+    for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < n * nr; e += (i64)gridDim.x * blockDim.x)
+        D[(e / nr) * ldd + e % nr] = S[(e / nr) * lds + e % nr];
+}
+
+enum MixedKind { MIX_LU = 0, MIX_CHOL = 1, MIX_LDLT = 2 };
+
+// Mixed-precision solve of A X = B: factor a FP32 copy of A (LU with partial
+// pivoting, Cholesky or unpivoted LDL^T, trailing updates in opts->precision),
+// measure the factor's growth in FP64, then refine every block of up to
+// MAX_RHS right-hand sides in FP64 (refine above) with the same factors.
+int mixed_solve(ddla_handle h, int kind, int uplo, i64 n, i64 nrhs, const double *A, const double *B, double *X,
+                const double *x_ref, const ddla_opts *opts, ddla_solve_report *rep, const int32_t *piv_ref = nullptr,
+                int32_t *piv_out = nullptr) {
     cudaStream_t s = h->stream;
     const int prec = (opts && opts->precision) ? opts->precision : DDLA_PREC_FP32;
     const int nb = opts ? opts->nb : 0;
@@ -393,27 +455,32 @@ int mixed_lu(ddla_handle h, i64 n, i64 nrhs, const double *A, const double *B, d
     rep->precision = prec;
     rep->pivots_agree = -1;
     rep->pivots_first_diff = -1;
-    if (nrhs > MAX_RHS) {
-        set_error("mixed solve: at most 16 right-hand sides per call");
-        return DDLA_ERR_UNSUPPORTED;
-    }
-    const int nr = (int)nrhs;
+    const int nr0 = (int)std::min<i64>(nrhs, MAX_RHS);
     float *A32, *d32;
     double *R;
-    int32_t *piv;
-    int *perm;
+    int32_t *piv = nullptr;
+    int *perm = nullptr;
     unsigned long long *norms;
-    DDLA_TRY(workspace(h, WS_PERM, sizeof(int) * (size_t)n, (void **)&perm));
+    if (kind == MIX_LU) {
+        DDLA_TRY(workspace(h, WS_PERM, sizeof(int) * (size_t)n, (void **)&perm));
+        DDLA_TRY(workspace(h, WS_X, sizeof(int32_t) * (size_t)n, (void **)&piv));
+    }
     DDLA_TRY(workspace(h, WS_F32, sizeof(float) * (size_t)n * n, (void **)&A32));
-    DDLA_TRY(workspace(h, WS_B, sizeof(float) * (size_t)n * nr + 256, (void **)&d32));
-    DDLA_TRY(workspace(h, WS_C, sizeof(double) * (size_t)n * nr, (void **)&R));
-    DDLA_TRY(workspace(h, WS_X, sizeof(int32_t) * (size_t)n, (void **)&piv));
-    DDLA_TRY(workspace(h, WS_A, sizeof(unsigned long long) * (2 + 3 * MAX_RHS + 3), (void **)&norms));
+    DDLA_TRY(workspace(h, WS_B, sizeof(float) * (size_t)n * nr0 + 256, (void **)&d32));
+    DDLA_TRY(workspace(h, WS_C, sizeof(double) * (size_t)n * nr0, (void **)&R));
+    // norms: [0] ||A||, [1 .. 3 MAX_RHS] column norms, then the forward-error
+    // pair, the pivot comparison and the four growth figures
+    constexpr int NORMS = 1 + 3 * MAX_RHS + 2 + 1 + 4;
+    DDLA_TRY(workspace(h, WS_A, sizeof(unsigned long long) * NORMS, (void **)&norms));
     DDLA_TRY(reset_info(h));
     DDLA_CUDA(cudaEventRecord(h->ev0, s));
     k_d2s<<<grid1(n * n), 256, 0, s>>>(A, n * n, A32);
     DDLA_LAUNCHED();
-    DDLA_TRY(getrf<float>(h, n, View<float>{A32, n, n, n, 1}, piv, prec, nb, perm));
+    const View<float> F{A32, n, n, n, 1};
+    if (kind == MIX_LU) DDLA_TRY(getrf<float>(h, n, F, piv, prec, nb, perm));
+    // FP32 blocks of 64, so the trailing updates are rank-64 (the tensor-core update's shape)
+    else if (kind == MIX_CHOL) DDLA_TRY(potrf<float>(h, uplo, n, F, prec, nb));
+    else DDLA_TRY(ldlt<float>(h, uplo, n, F, prec, nb > 0 ? nb : 64));
     DDLA_CUDA(cudaEventRecord(h->ev1, s));
     int info;
     DDLA_TRY(read_info(h, &info));
@@ -421,38 +488,106 @@ int mixed_lu(ddla_handle h, i64 n, i64 nrhs, const double *A, const double *B, d
     cudaEventElapsedTime(&ms, h->ev0, h->ev1);
     rep->factor_ms = ms;
     rep->info = info;
-    if (piv_out) DDLA_CUDA(cudaMemcpyAsync(piv_out, piv, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, s));
-    if (piv_ref) {
-        // how far the FP32 factor followed the FP64 pivot sequence
-        int *cmp = (int *)(norms + 3 + 3 * MAX_RHS);   // after the forward-error pair
-        const int init[2] = {0, INT_MAX};
-        DDLA_CUDA(cudaMemcpyAsync(cmp, init, sizeof(init), cudaMemcpyHostToDevice, s));
-        k_piv_cmp<<<grid1(n), 256, 0, s>>>(piv, piv_ref, n, cmp);
-        DDLA_LAUNCHED();
-        int got[2];
-        DDLA_CUDA(cudaMemcpyAsync(got, cmp, sizeof(got), cudaMemcpyDeviceToHost, s));
+    if (piv_out && piv) DDLA_CUDA(cudaMemcpyAsync(piv_out, piv, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, s));
+    unsigned long long *grow = norms + 1 + 3 * MAX_RHS + 2 + 1;
+    {
+        // pivot agreement (LU) and growth, one read-back
+        if (piv_ref && piv) {
+            int *cmp = (int *)(norms + 1 + 3 * MAX_RHS + 2);
+            const int init[2] = {0, INT_MAX};
+            DDLA_CUDA(cudaMemcpyAsync(cmp, init, sizeof(init), cudaMemcpyHostToDevice, s));
+            k_piv_cmp<<<grid1(n), 256, 0, s>>>(piv, piv_ref, n, cmp);
+            DDLA_LAUNCHED();
+        }
+        const unsigned long long ginit[4] = {0ull, 0ull, 0x7ff0000000000000ull, 0ull};
+        DDLA_CUDA(cudaMemcpyAsync(grow, ginit, sizeof(ginit), cudaMemcpyHostToDevice, s));
+        if (!info) {
+            // the factor as the lower triangle L (Cholesky / LDL^T upper: the transpose)
+            const View<const float> Fg = (kind != MIX_LU && uplo == DDLA_UPPER) ? View<const float>{A32, n, n, 1, n}
+                                                                                 : View<const float>{A32, n, n, n, 1};
+            k_growth<<<(unsigned)((n * 32 + 255) / 256), 256, 0, s>>>(Fg.p, Fg.rs, Fg.cs, n, kind, grow);
+            DDLA_LAUNCHED();
+            k_absmax<<<grid1(n * n), 256, 0, s>>>(A, n * n, grow + 3);
+            DDLA_LAUNCHED();
+        }
+        unsigned long long got[5];
+        DDLA_CUDA(cudaMemcpyAsync(got, norms + 1 + 3 * MAX_RHS + 2, sizeof(got), cudaMemcpyDeviceToHost, s));
         DDLA_CUDA(cudaStreamSynchronize(s));
-        rep->pivots_agree = got[0];
-        rep->pivots_first_diff = got[1] == INT_MAX ? -1 : got[1];
+        if (piv_ref && piv) {
+            const int *cmp = (const int *)&got[0];
+            rep->pivots_agree = cmp[0];
+            rep->pivots_first_diff = cmp[1] == INT_MAX ? -1 : cmp[1];
+        }
+        if (!info) {
+            const double gmax = u64d(got[1]), dmax = u64d(got[2]), dmin = u64d(got[3]), amax = u64d(got[4]);
+            rep->growth = amax > 0 ? gmax / amax : gmax;
+            rep->diag_ratio = dmin > 0 ? dmax / dmin : INFINITY;
+        }
     }
     if (info) return info;
-    // the inverted diagonal blocks of L and U are formed once and serve every
-    // correction solve: d <- U^-1 L^-1 P d
-    const View<const float> F{A32, n, n, n, 1};
+    // the inverted 64 x 64 diagonal blocks of the two triangular factors are
+    // formed once and serve every correction solve
+    const View<const float> Fc{A32, n, n, n, 1};
+    const View<const float> Lv = (kind == MIX_LU || uplo == DDLA_LOWER) ? Fc : Fc.t();
+    const View<const float> Uv = kind == MIX_LU ? Fc : Lv.t();
+    const bool unit_l = kind != MIX_CHOL, unit_u = kind == MIX_LDLT;
     const i64 nblk = (n + TRI_TB - 1) / TRI_TB;
     float *invL, *invU;
     DDLA_TRY(workspace(h, WS_INV, sizeof(float) * 2 * (size_t)nblk * TRI_TB * TRI_TB, (void **)&invL));
     invU = invL + (size_t)nblk * TRI_TB * TRI_TB;
-    DDLA_TRY(tri_inverse<float>(h, true, true, F, n, invL));
-    DDLA_TRY(tri_inverse<float>(h, false, false, F, n, invU));
-    auto solve32 = [&](float *d) {
+    DDLA_TRY(tri_inverse<float>(h, true, unit_l, Lv, n, invL));
+    DDLA_TRY(tri_inverse<float>(h, false, unit_u, Uv, n, invU));
+    int nr = nr0;
+    // d <- U^-1 (D^-1) L^-1 (P) d with the FP32 factors, nr columns
+    auto solve32 = [&](float *d) -> int {
         Timed t(s, TC_SOLVE, 2.0 * n * n * nr, 4.0 * n * n);
-        DDLA_TRY(permute_rows<float>(h, View<float>{d, n, nr, nr, 1}, perm, n, true));
-        DDLA_TRY(trsv_apply<float>(h, true, F, n, invL, d, nr, nr));
-        return trsv_apply<float>(h, false, F, n, invU, d, nr, nr);
+        if (kind == MIX_LU) DDLA_TRY(permute_rows<float>(h, View<float>{d, n, nr, nr, 1}, perm, n, true));
+        DDLA_TRY(trsv_apply<float>(h, true, Lv, n, invL, d, nr, nr));
+        if (kind == MIX_LDLT) {
+            k_rows_by_diag<<<grid1(n * nr), 256, 0, s>>>(d, n, nr, A32, n + 1);
+            DDLA_LAUNCHED();
+        }
+        return trsv_apply<float>(h, false, Uv, n, invU, d, nr, nr);
     };
     DDLA_CUDA(cudaEventRecord(h->ev0, s));
-    int rc = refine(h, n, nr, A, B, X, x_ref, opts, rep, solve32, d32, R, norms);
+    int rc = 0;
+    if (nrhs <= MAX_RHS) {
+        rc = refine(h, n, nr, A, B, X, x_ref, opts, rep, solve32, d32, R, norms);
+    } else {
+        // blocks of MAX_RHS columns, copied into dense n x nr blocks and back
+        double *blk;
+        DDLA_TRY(workspace(h, WS_RHS, sizeof(double) * 3 * (size_t)n * MAX_RHS, (void **)&blk));
+        double *Bc = blk, *Xc = blk + (size_t)n * MAX_RHS, *XRc = Xc + (size_t)n * MAX_RHS;
+        int iters = 0;
+        double berr = 0.0, ferr = x_ref ? 0.0 : -1.0;
+        bool conv = true;
+        for (i64 c0 = 0; c0 < nrhs; c0 += MAX_RHS) {
+            nr = (int)std::min<i64>(MAX_RHS, nrhs - c0);
+            k_cols_copy<<<grid1(n * nr), 256, 0, s>>>(B + c0, nrhs, Bc, nr, n, nr);
+            DDLA_LAUNCHED();
+            if (x_ref) {
+                k_cols_copy<<<grid1(n * nr), 256, 0, s>>>(x_ref + c0, nrhs, XRc, nr, n, nr);
+                DDLA_LAUNCHED();
+            }
+            ddla_solve_report part = *rep;
+            const int prc = refine(h, n, nr, A, Bc, Xc, x_ref ? XRc : nullptr, opts, &part, solve32, d32, R, norms);
+            if (prc != 0 && prc != DDLA_ERR_NOT_CONVERGED) return prc;
+            k_cols_copy<<<grid1(n * nr), 256, 0, s>>>(Xc, nr, X + c0, nrhs, n, nr);
+            DDLA_LAUNCHED();
+            iters = std::max(iters, part.iterations);
+            if (!(part.backward_error <= berr)) berr = part.backward_error;
+            if (x_ref && !(part.forward_error <= ferr)) ferr = part.forward_error;
+            conv = conv && part.converged;
+        }
+        rep->iterations = iters;
+        rep->backward_error = berr;
+        rep->forward_error = ferr;
+        rep->converged = conv;
+        if (!conv) {
+            set_error("iterative refinement did not reach the backward-error tolerance");
+            rc = DDLA_ERR_NOT_CONVERGED;
+        }
+    }
     DDLA_CUDA(cudaEventRecord(h->ev1, s));
     DDLA_CUDA(cudaEventSynchronize(h->ev1));
     cudaEventElapsedTime(&ms, h->ev0, h->ev1);
@@ -460,64 +595,20 @@ int mixed_lu(ddla_handle h, i64 n, i64 nrhs, const double *A, const double *B, d
     return rc;
 }
 
+int mixed_lu(ddla_handle h, i64 n, i64 nrhs, const double *A, const double *B, double *X, const double *x_ref,
+             const ddla_opts *opts, ddla_solve_report *rep, const int32_t *piv_ref = nullptr,
+             int32_t *piv_out = nullptr) {
+    return mixed_solve(h, MIX_LU, 0, n, nrhs, A, B, X, x_ref, opts, rep, piv_ref, piv_out);
+}
+
 int mixed_chol(ddla_handle h, int uplo, i64 n, i64 nrhs, const double *A, const double *B, double *X,
                const double *x_ref, const ddla_opts *opts, ddla_solve_report *rep) {
-    cudaStream_t s = h->stream;
-    const int prec = (opts && opts->precision) ? opts->precision : DDLA_PREC_FP32;
-    const int nb = opts ? opts->nb : 0;
-    *rep = ddla_solve_report{};
-    rep->precision = prec;
-    rep->pivots_agree = -1;
-    rep->pivots_first_diff = -1;
-    if (nrhs > MAX_RHS) {
-        set_error("mixed solve: at most 16 right-hand sides per call");
-        return DDLA_ERR_UNSUPPORTED;
-    }
-    const int nr = (int)nrhs;
-    float *A32, *d32;
-    double *R;
-    unsigned long long *norms;
-    DDLA_TRY(workspace(h, WS_F32, sizeof(float) * (size_t)n * n, (void **)&A32));
-    DDLA_TRY(workspace(h, WS_B, sizeof(float) * (size_t)n * nr + 256, (void **)&d32));
-    DDLA_TRY(workspace(h, WS_C, sizeof(double) * (size_t)n * nr, (void **)&R));
-    DDLA_TRY(workspace(h, WS_A, sizeof(unsigned long long) * (2 + 3 * MAX_RHS + 2), (void **)&norms));
-    DDLA_TRY(reset_info(h));
-    DDLA_CUDA(cudaEventRecord(h->ev0, s));
-    k_d2s<<<grid1(n * n), 256, 0, s>>>(A, n * n, A32);
-    DDLA_LAUNCHED();
-    DDLA_TRY(potrf<float>(h, uplo, n, View<float>{A32, n, n, n, 1}, prec, nb));
-    DDLA_CUDA(cudaEventRecord(h->ev1, s));
-    int info;
-    DDLA_TRY(read_info(h, &info));
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, h->ev0, h->ev1);
-    rep->factor_ms = ms;
-    rep->info = info;
-    if (info) return info;
-    // A = L L^T (lower) or U^T U (upper): the first solve is with the lower
-    // triangle of F (lower) or of F^T (upper), the second with its transpose;
-    // both diagonal-block inverses are formed once for all correction solves
-    const View<const float> F{A32, n, n, n, 1};
-    const View<const float> Lv = (uplo == DDLA_LOWER) ? F : F.t();
-    const View<const float> Uv = Lv.t();
-    const i64 nblk = (n + TRI_TB - 1) / TRI_TB;
-    float *invL, *invU;
-    DDLA_TRY(workspace(h, WS_INV, sizeof(float) * 2 * (size_t)nblk * TRI_TB * TRI_TB, (void **)&invL));
-    invU = invL + (size_t)nblk * TRI_TB * TRI_TB;
-    DDLA_TRY(tri_inverse<float>(h, true, false, Lv, n, invL));
-    DDLA_TRY(tri_inverse<float>(h, false, false, Uv, n, invU));
-    auto solve32 = [&](float *d) {
-        Timed t(s, TC_SOLVE, 2.0 * n * n * nr, 4.0 * n * n);
-        DDLA_TRY(trsv_apply<float>(h, true, Lv, n, invL, d, nr, nr));
-        return trsv_apply<float>(h, false, Uv, n, invU, d, nr, nr);
-    };
-    DDLA_CUDA(cudaEventRecord(h->ev0, s));
-    int rc = refine(h, n, nr, A, B, X, x_ref, opts, rep, solve32, d32, R, norms);
-    DDLA_CUDA(cudaEventRecord(h->ev1, s));
-    DDLA_CUDA(cudaEventSynchronize(h->ev1));
-    cudaEventElapsedTime(&ms, h->ev0, h->ev1);
-    rep->refine_ms = ms;
-    return rc;
+    return mixed_solve(h, MIX_CHOL, uplo, n, nrhs, A, B, X, x_ref, opts, rep);
+}
+
+int mixed_ldlt(ddla_handle h, int uplo, i64 n, i64 nrhs, const double *A, const double *B, double *X,
+               const double *x_ref, const ddla_opts *opts, ddla_solve_report *rep) {
+    return mixed_solve(h, MIX_LDLT, uplo, n, nrhs, A, B, X, x_ref, opts, rep);
 }
 
 }  // namespace ddla
@@ -545,6 +636,17 @@ int ddla_dev_dgesv_mixed_piv(ddla_handle h, ddla_dim_t n, ddla_dim_t nrhs, const
     return mixed_lu(h, n, nrhs, a, b, x, x_ref, opts, report, piv_ref, piv_out);
 }
 
+int ddla_dev_dsysv_mixed(ddla_handle h, int32_t uplo, ddla_dim_t n, ddla_dim_t nrhs, const double *a,
+                         const double *b, double *x, const double *x_ref, const ddla_opts *opts,
+                         ddla_solve_report *report) {
+    if (uplo != DDLA_LOWER && uplo != DDLA_UPPER) return -2;
+    if (n < 0) return -3;
+    if (nrhs < 0) return -4;
+    if (!report) return -10;
+    if (n == 0 || nrhs == 0) { *report = ddla_solve_report{}; return 0; }
+    return mixed_ldlt(h, uplo, n, nrhs, a, b, x, x_ref, opts, report);
+}
+
 int ddla_dev_dposv_mixed(ddla_handle h, int32_t uplo, ddla_dim_t n, ddla_dim_t nrhs, const double *a,
                          const double *b, double *x, const double *x_ref, const ddla_opts *opts,
                          ddla_solve_report *report) {
@@ -558,11 +660,11 @@ int ddla_dev_dposv_mixed(ddla_handle h, int32_t uplo, ddla_dim_t n, ddla_dim_t n
 
 // Host-pointer variants: A (n x n) and B (n x nrhs) are arbitrary strided host
 // views; X receives the solution.
-static int host_mixed(bool chol, int32_t uplo, ddla_dim_t n, ddla_dim_t nrhs, const double *a, ddla_inc_t rsa,
+static int host_mixed(int kind, int32_t uplo, ddla_dim_t n, ddla_dim_t nrhs, const double *a, ddla_inc_t rsa,
                       ddla_inc_t csa, const double *b, ddla_inc_t rsb, ddla_inc_t csb, double *x, ddla_inc_t rsx,
                       ddla_inc_t csx, const double *x_ref, const ddla_opts *opts, ddla_solve_report *report) {
     if (n < 0) return -1;
-    if (nrhs < 0 || nrhs > 16) return -2;
+    if (nrhs < 0) return -2;
     if (!report) return -15;
     if (n == 0 || nrhs == 0) { *report = ddla_solve_report{}; return 0; }
     ddla_handle h;
@@ -590,8 +692,7 @@ static int host_mixed(bool chol, int32_t uplo, ddla_dim_t n, ddla_dim_t nrhs, co
     int rc = pack_in(a, n, n, rsa, csa, dA);
     if (!rc) rc = pack_in(b, n, nrhs, rsb, csb, dB);
     if (!rc && x_ref) rc = pack_in(x_ref, n, nrhs, nrhs, 1, dR);
-    if (!rc) rc = chol ? mixed_chol(h, uplo, n, nrhs, dA, dB, dX, dR, opts, report)
-                       : mixed_lu(h, n, nrhs, dA, dB, dX, dR, opts, report);
+    if (!rc) rc = mixed_solve(h, kind, uplo, n, nrhs, dA, dB, dX, dR, opts, report);
     if (rc == 0 || rc == DDLA_ERR_NOT_CONVERGED) {
         std::vector<double> tmp(nb);
         if (cudaMemcpyAsync(tmp.data(), dX, nb * 8, cudaMemcpyDeviceToHost, s) == cudaSuccess &&
@@ -611,14 +712,21 @@ static int host_mixed(bool chol, int32_t uplo, ddla_dim_t n, ddla_dim_t nrhs, co
 int ddla_dgesv_mixed(ddla_dim_t n, ddla_dim_t nrhs, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
                      const double *b, ddla_inc_t rsb, ddla_inc_t csb, double *x, ddla_inc_t rsx, ddla_inc_t csx,
                      const double *x_ref, const ddla_opts *opts, ddla_solve_report *report) {
-    return host_mixed(false, 0, n, nrhs, a, rsa, csa, b, rsb, csb, x, rsx, csx, x_ref, opts, report);
+    return host_mixed(MIX_LU, 0, n, nrhs, a, rsa, csa, b, rsb, csb, x, rsx, csx, x_ref, opts, report);
 }
 
 int ddla_dposv_mixed(int32_t uplo, ddla_dim_t n, ddla_dim_t nrhs, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
                      const double *b, ddla_inc_t rsb, ddla_inc_t csb, double *x, ddla_inc_t rsx, ddla_inc_t csx,
                      const double *x_ref, const ddla_opts *opts, ddla_solve_report *report) {
     if (uplo != DDLA_LOWER && uplo != DDLA_UPPER) return -1;
-    return host_mixed(true, uplo, n, nrhs, a, rsa, csa, b, rsb, csb, x, rsx, csx, x_ref, opts, report);
+    return host_mixed(MIX_CHOL, uplo, n, nrhs, a, rsa, csa, b, rsb, csb, x, rsx, csx, x_ref, opts, report);
+}
+
+int ddla_dsysv_mixed(int32_t uplo, ddla_dim_t n, ddla_dim_t nrhs, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
+                     const double *b, ddla_inc_t rsb, ddla_inc_t csb, double *x, ddla_inc_t rsx, ddla_inc_t csx,
+                     const double *x_ref, const ddla_opts *opts, ddla_solve_report *report) {
+    if (uplo != DDLA_LOWER && uplo != DDLA_UPPER) return -1;
+    return host_mixed(MIX_LDLT, uplo, n, nrhs, a, rsa, csa, b, rsb, csb, x, rsx, csx, x_ref, opts, report);
 }
 
 }  // extern "C"

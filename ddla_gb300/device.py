@@ -134,7 +134,7 @@ class Handle:
               "dev_dpotrs")
 
     def gesv_mixed(self, A, B, X, x_ref=None, precision=_lib.PREC_FP32, tol=0.0, max_iter=0, nb=0, spd=False,
-                   uplo=_lib.LOWER, piv_ref=None, piv_out=None):
+                   uplo=_lib.LOWER, piv_ref=None, piv_out=None, ldlt=False):
         """Mixed solve; for LU, piv_ref / piv_out (int32 device vectors of
         length n) compare the low-precision factor's pivots with a reference
         pivot vector and hand them out (ddla_dev_dgesv_mixed_piv)."""
@@ -143,7 +143,9 @@ class Handle:
         rep = SolveReport()
         xr = C.c_void_p(0) if x_ref is None else _p(x_ref)
         n, nrhs = B.shape
-        if spd:
+        if ldlt:
+            rc = lib().ddla_dev_dsysv_mixed(self.h, uplo, n, nrhs, _p(A), _p(B), _p(X), xr, C.byref(o), C.byref(rep))
+        elif spd:
             rc = lib().ddla_dev_dposv_mixed(self.h, uplo, n, nrhs, _p(A), _p(B), _p(X), xr, C.byref(o), C.byref(rep))
         elif piv_ref is not None or piv_out is not None:
             rc = lib().ddla_dev_dgesv_mixed_piv(self.h, n, nrhs, _p(A), _p(B), _p(X), xr,

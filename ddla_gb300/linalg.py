@@ -578,9 +578,12 @@ class Bidiagonaling:
         return U, V, d, e
 
 
-def solve_mixed(A, B, spd=False, uplo=LOWER, precision=_lib.PREC_FP32, x_ref=None, tol=0.0, max_iter=0, nb=0):
+def solve_mixed(A, B, spd=False, uplo=LOWER, precision=_lib.PREC_FP32, x_ref=None, tol=0.0, max_iter=0, nb=0,
+                ldlt=False):
     """Mixed-precision solve with FP64 iterative refinement (no DDLA
-    counterpart).  Returns (X, report dict).  Raises on non-convergence."""
+    counterpart): LU (default), Cholesky (spd=True) or the unpivoted LDL^T of
+    DDLA's LDLT (ldlt=True), any number of right-hand sides.  Returns
+    (X, report dict with the growth monitor).  Raises on non-convergence."""
     A, B = _view(A, "A"), _view(B, "B")
     n, nrhs = B.shape
     X = np.zeros((n, nrhs))
@@ -588,7 +591,10 @@ def solve_mixed(A, B, spd=False, uplo=LOWER, precision=_lib.PREC_FP32, x_ref=Non
     xr = None if x_ref is None else np.ascontiguousarray(_view(x_ref, "x_ref"))
     xp = C.c_void_p(0) if xr is None else _p(xr)
     o = _opts(nb, precision, max_iter, tol)
-    if spd:
+    if ldlt:
+        rc = lib().ddla_dsysv_mixed(uplo, n, nrhs, _p(A), *_st(A), _p(B), *_st(B), _p(X), *_st(X), xp, C.byref(o),
+                                    C.byref(rep))
+    elif spd:
         rc = lib().ddla_dposv_mixed(uplo, n, nrhs, _p(A), *_st(A), _p(B), *_st(B), _p(X), *_st(X), xp, C.byref(o),
                                     C.byref(rep))
     else:

@@ -100,6 +100,14 @@ typedef struct ddla_solve_report {
                                   the n pivots of the low-precision factor equal the reference's; -1 = not
                                   measured */
     int32_t pivots_first_diff; /* first index where they differ; -1 = none or not measured */
+    /* Growth monitor, computed in FP64 on the GPU from the low-precision factors (0 when the
+     * factorization failed).  growth: LU max|u_ij| / max|a_ij| (the pivot growth factor);
+     * Cholesky max_i sum_k l_ik^2 / max|a_ij|; LDL^T max_i (sum_k<i l_ik^2 |d_k| + |d_i|) /
+     * max|a_ij| -- for Cholesky and LDL^T a bound on the entries of |L||D||L^T| relative to A,
+     * which bounds the factorization's backward error.  diag_ratio: max / min over the
+     * diagonal of U (LU), of L^2 (Cholesky) or of |D| (LDL^T, its pivots d_i). */
+    double growth;
+    double diag_ratio;
 } ddla_solve_report;
 
 /* ---------------------------------------------------------------- runtime */
@@ -295,12 +303,21 @@ int ddla_dldlts(int32_t uplo, ddla_dim_t n, ddla_dim_t nrhs, const double *a, dd
 /* Mixed-precision solves: factor in opts->precision, refine in FP64 until the
  * relative backward error is <= opts->tol.  A and B are read only; X receives
  * the solution.  x_ref (may be NULL) is an oracle solution for the forward
- * error.  No reference counterpart: DDLA's LU(A).Solve / Cholesky(A).Solve
- * (LU.cs:64-100, Cholesky.cs:71-88) are FP64-only. */
+ * error.  Any number of right-hand sides: they are refined in blocks of 16
+ * with the same factors (the report gives the worst block).  No reference
+ * counterpart: DDLA's LU(A).Solve / Cholesky(A).Solve / LDLT.Solve
+ * (LU.cs:64-100, Cholesky.cs:71-88, LDLT.cs:75-100) are FP64-only.
+ * ddla_dsysv_mixed is the unpivoted LDL^T of DDLA's LDLT (LDLT.cs:56-295) in
+ * FP32 with FP64 refinement: like DDLA's it needs A's leading blocks
+ * non-singular; the report's growth and diag_ratio tell how much the
+ * unpivoted factorization amplified A. */
 int ddla_dgesv_mixed(ddla_dim_t n, ddla_dim_t nrhs, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
                      const double *b, ddla_inc_t rsb, ddla_inc_t csb, double *x, ddla_inc_t rsx, ddla_inc_t csx,
                      const double *x_ref, const ddla_opts *opts, ddla_solve_report *report);
 int ddla_dposv_mixed(int32_t uplo, ddla_dim_t n, ddla_dim_t nrhs, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
+                     const double *b, ddla_inc_t rsb, ddla_inc_t csb, double *x, ddla_inc_t rsx, ddla_inc_t csx,
+                     const double *x_ref, const ddla_opts *opts, ddla_solve_report *report);
+int ddla_dsysv_mixed(int32_t uplo, ddla_dim_t n, ddla_dim_t nrhs, const double *a, ddla_inc_t rsa, ddla_inc_t csa,
                      const double *b, ddla_inc_t rsb, ddla_inc_t csb, double *x, ddla_inc_t rsx, ddla_inc_t csx,
                      const double *x_ref, const ddla_opts *opts, ddla_solve_report *report);
 
@@ -378,6 +395,9 @@ int ddla_dev_dldlts(ddla_handle h, int32_t uplo, ddla_dim_t n, ddla_dim_t nrhs, 
 int ddla_dev_dgesv_mixed(ddla_handle h, ddla_dim_t n, ddla_dim_t nrhs, const double *a, const double *b, double *x,
                          const double *x_ref, const ddla_opts *opts, ddla_solve_report *report);
 int ddla_dev_dposv_mixed(ddla_handle h, int32_t uplo, ddla_dim_t n, ddla_dim_t nrhs, const double *a,
+                         const double *b, double *x, const double *x_ref, const ddla_opts *opts,
+                         ddla_solve_report *report);
+int ddla_dev_dsysv_mixed(ddla_handle h, int32_t uplo, ddla_dim_t n, ddla_dim_t nrhs, const double *a,
                          const double *b, double *x, const double *x_ref, const ddla_opts *opts,
                          ddla_solve_report *report);
 /* ddla_dev_dgesv_mixed that also hands out the low-precision factor's pivots

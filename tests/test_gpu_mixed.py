@@ -68,3 +68,84 @@ def test_gmres_refinement_on_ill_conditioned(ddla):
         assert e.code == ddla._lib.ERR_NOT_CONVERGED
     finally:
         autotune.tune_set("refine.gmres", 1)
+
+
+def _growth_of(kind, F, A):
+    """The report's growth figures from an FP64 factor (oracle): LU
+    max|U|/max|A| and the U diagonal ratio; Cholesky max_i sum_k l_ik^2 /
+    max|A| and the ratio of l_ii^2; LDL^T max_i (sum_k<i l_ik^2 |d_k| + |d_i|) /
+    max|A| and the ratio of |d_i|."""
+    amax = np.abs(A).max()
+    if kind == "lu":
+        U = np.triu(F)
+        d = np.abs(np.diag(F))
+        return np.abs(U).max() / amax, d.max() / d.min()
+    L = np.tril(F)
+    if kind == "chol":
+        d = np.diag(F) ** 2
+        return (L * L).sum(1).max() / amax, d.max() / d.min()
+    d = np.abs(np.diag(F))
+    Ls = np.tril(F, -1)
+    return ((Ls * Ls) @ d + d).max() / amax, d.max() / d.min()
+
+
+def _sym_indefinite(r, n):
+    # symmetric, indefinite, leading blocks far from singular: the unpivoted
+    # LDL^T of DDLA's LDLT applies
+    S = r.standard_normal((n, n))
+    S = (S + S.T) / 2
+    return S + np.diag(np.where(np.arange(n) % 3 == 0, -1.0, 1.0) * 2.0 * np.sqrt(n))
+
+
+@pytest.mark.parametrize("prec", ["fp32", "tf32x3", "bf16x3"])
+@pytest.mark.parametrize("n,nrhs,kind", [(300, 1, "spd"), (2048, 4, "spd"), (1500, 3, "indef"), (3000, 16, "indef")])
+def test_mixed_ldlt_reaches_fp64(ddla, orc, n, nrhs, kind, prec):
+    r = rng(n + nrhs)
+    A = spd(r, n) if kind == "spd" else _sym_indefinite(r, n)
+    B = r.standard_normal((n, nrhs))
+    F = A.copy()
+    assert orc.dldlt(ddla.LOWER, F) == 0
+    Xo = B.copy()
+    orc.dldlts(ddla.LOWER, F, Xo)
+    X, rep = ddla.solve_mixed(A, B, ldlt=True, precision=getattr(ddla, "PREC_" + prec.upper()), x_ref=Xo)
+    assert rep["converged"] == 1 and rep["backward_error"] <= 1e-14
+    assert berr(A, X, B) <= 1e-14
+    assert rep["forward_error"] <= 1e-10
+    g, dr = _growth_of("ldlt", F, A)
+    assert abs(rep["growth"] - g) <= 1e-3 * g
+    assert abs(rep["diag_ratio"] - dr) <= 1e-3 * dr
+
+
+@pytest.mark.parametrize("kind", ["lu", "chol"])
+def test_growth_monitor_matches_fp64_factor(ddla, orc, kind):
+    n = 1200
+    r = rng(4321)
+    A = spd(r, n) if kind == "chol" else r.standard_normal((n, n))
+    B = r.standard_normal((n, 1))
+    F = A.copy()
+    if kind == "lu":
+        info, piv = orc.dgetrf(F)
+    else:
+        info = orc.dpotrf(ddla.LOWER, F)
+    assert info == 0
+    X, rep = ddla.solve_mixed(A, B, spd=kind == "chol")
+    g, dr = _growth_of(kind, F, A)
+    # FP32 factors of the same matrix; LU may pivot differently after a near-tie
+    tol = 1e-3 if kind == "chol" else 0.25
+    assert abs(rep["growth"] - g) <= tol * g, (rep["growth"], g)
+    assert rep["diag_ratio"] >= 1.0
+
+
+@pytest.mark.parametrize("mode", ["lu", "chol", "ldlt"])
+def test_mixed_more_than_16_rhs(ddla, orc, mode):
+    # DDLA's Cholesky tests solve 256 right-hand sides
+    # (Tests/TestFlame/TestChol.cs:101-162); the mixed solvers refine them in
+    # blocks of 16 with one factorization
+    n, nrhs = 700, 41
+    r = rng(99)
+    A = spd(r, n) if mode != "lu" else r.standard_normal((n, n))
+    B = r.standard_normal((n, nrhs))
+    X, rep = ddla.solve_mixed(A, B, spd=mode == "chol", ldlt=mode == "ldlt")
+    assert rep["converged"] == 1
+    assert berr(A, X, B) <= 1e-14
+    assert np.max(np.abs(X - np.linalg.solve(A, B))) / np.abs(X).max() <= 1e-10
