@@ -47,11 +47,15 @@ __device__ __forceinline__ unsigned long long bkey(float v) {
     return u > 0x7f800000u ? 0ull : (unsigned long long)u + 1ull;
 }
 
+constexpr int BMV = 2 * NBMAX;     // rows a panel's interchanges can move
+
 struct BScratch {
     unsigned long long key[BT / 32];
     int idx[BT / 32];
-    int best;
-    int fail;
+    int fail;   // the pivot row and the row it displaces (LU), the scaled column (Cholesky)
+    int nmv;            // rows moved by the current panel's interchanges
+    int mv[BMV];        // those rows (relative to the panel's first row) ...
+    int src[BMV];       // ... and the row each receives
 };
 
 // Block-wide first-max over rows of column j of the panel.
@@ -72,16 +76,17 @@ __device__ int panel_argmax(const T *Ps, int ld, int m, int j, BScratch &S) {
     }
     if (lane == 0) { S.key[warp] = bv; S.idx[warp] = bi; }
     __syncthreads();
-    if (tid == 0) {
-        for (int q = 1; q < BT / 32; q++) {
-            unsigned long long ov = S.key[q];
-            int oi = S.idx[q];
-            if (oi != INT_MAX && (bi == INT_MAX || ov > bv || (ov == bv && oi < bi))) { bv = ov; bi = oi; }
-        }
-        S.best = bi == INT_MAX ? j : bi;
+    // every warp reduces the per-warp results itself (no second barrier)
+    bv = lane < BT / 32 ? S.key[lane] : 0ull;
+    bi = lane < BT / 32 ? S.idx[lane] : INT_MAX;
+#pragma unroll
+    for (int off = 4; off > 0; off >>= 1) {
+        unsigned long long ov = __shfl_down_sync(0xffffffffu, bv, off);
+        int oi = __shfl_down_sync(0xffffffffu, bi, off);
+        if (oi != INT_MAX && (bi == INT_MAX || ov > bv || (ov == bv && oi < bi))) { bv = ov; bi = oi; }
     }
-    __syncthreads();
-    return S.best;
+    bi = __shfl_sync(0xffffffffu, bi, 0);
+    return bi == INT_MAX ? j : bi;
 }
 
 // In-place blocked factorization of one n x n row-major matrix W (ld = n).
@@ -170,20 +175,49 @@ __device__ int factor_item(T *W, int n, int kind, int nb, int *piv, T *Ps, T *Us
         }
         __syncthreads();
         if (kind == 0) {
-            // 4. the panel's interchanges on the other columns of rows j0..n
-            for (int c = tid; c < n; c += BT) {
-                if (c >= j0 && c < j0 + jb) continue;
+            // 4. the panel's interchanges on the other columns of rows j0..n,
+            //    as one gather: the panel's permutation (thread 0 composes
+            //    its jb swaps), the rows it moves (at most 2 jb), then those
+            //    rows' elements in chunks of 32 columns, all loads before all
+            //    stores of a chunk
+            if (tid == 0) {
+                // mv[k]: a position (relative to j0) whose content changes,
+                // src[k]: the row whose original content ends there; the
+                // first jb entries are positions 0 .. jb-1
+                int cnt = 0;
+                for (int j = 0; j < jb; j++) { S.mv[j] = j; S.src[j] = j; }
                 for (int j = 0; j < jb; j++) {
-                    int p = piv[j0 + j];
-                    if (p) {
-                        T *a = &W[(i64)(j0 + j) * n + c], *b = &W[(i64)(j0 + j + p) * n + c];
-                        T t = *a;
-                        *a = *b;
-                        *b = t;
-                    }
+                    const int p = piv[j0 + j] + j;
+                    if (p == j) continue;
+                    int kp = -1;   // slot of position p
+                    if (p < jb) kp = p;
+                    else
+                        for (int k = jb; k < jb + cnt; k++)
+                            if (S.mv[k] == p) { kp = k; break; }
+                    if (kp < 0) { kp = jb + cnt++; S.mv[kp] = p; S.src[kp] = p; }
+                    const int t = S.src[j];
+                    S.src[j] = S.src[kp];
+                    S.src[kp] = t;
                 }
+                S.nmv = jb + cnt;
             }
             __syncthreads();
+            const int nmv = S.nmv;
+            for (int cb = 0; cb < n; cb += 32) {
+                T v[BMV / (BT / 32)];
+#pragma unroll
+                for (int t = 0; t < BMV / (BT / 32); t++) {
+                    const int e = tid + BT * t, ri = e >> 5, c = cb + (e & 31);
+                    if (ri < nmv && c < n && (c < j0 || c >= j0 + jb)) v[t] = W[(i64)(j0 + S.src[ri]) * n + c];
+                }
+                __syncthreads();
+#pragma unroll
+                for (int t = 0; t < BMV / (BT / 32); t++) {
+                    const int e = tid + BT * t, ri = e >> 5, c = cb + (e & 31);
+                    if (ri < nmv && c < n && (c < j0 || c >= j0 + jb)) W[(i64)(j0 + S.mv[ri]) * n + c] = v[t];
+                }
+                __syncthreads();
+            }
         }
         if (r2 == 0) break;
         // 5. U12 = L11^-1 A12 (LU) or Us = L21^T (Cholesky), into shared memory
@@ -193,18 +227,14 @@ __device__ int factor_item(T *W, int n, int kind, int nb, int *piv, T *Ps, T *Us
                 Us[i * n + c] = Ps[(jb + c) * LDP + i];
             }
         } else {
+            // one thread per column c of U12, which it builds in Us (its own
+            // column only: no barrier), forward substitution with unit L11
             for (int c = tid; c < r2; c += BT) {
-                T u[NBMAX];
-#pragma unroll
-                for (int i = 0; i < NBMAX; i++) {
-                    if (i >= jb) break;
-                    T s = W[(i64)(j0 + i) * n + j0 + jb + c];
-                    for (int k = 0; k < i; k++) s = fma(-Ps[i * LDP + k], u[k], s);
-                    u[i] = s;
-                }
                 for (int i = 0; i < jb; i++) {
-                    Us[i * n + c] = u[i];
-                    W[(i64)(j0 + i) * n + j0 + jb + c] = u[i];
+                    T s = W[(i64)(j0 + i) * n + j0 + jb + c];
+                    for (int k = 0; k < i; k++) s = fma(-Ps[i * LDP + k], Us[k * n + c], s);
+                    Us[i * n + c] = s;
+                    W[(i64)(j0 + i) * n + j0 + jb + c] = s;
                 }
             }
         }
@@ -249,7 +279,10 @@ __device__ int factor_item(T *W, int n, int kind, int nb, int *piv, T *Ps, T *Us
 
 // Triangular solve with one right-hand side x (shared memory, length n) and
 // the factor in W (row-major).  lower: L (unit if `unit`) forward; else upper
-// backward.  `trans` reads the triangle transposed (Cholesky's L^T).
+// backward.  `trans` reads the triangle transposed (Cholesky's L^T).  Blocks
+// of 32 rows: warp 0 loads its lanes' rows of the 32 x 32 diagonal block into
+// registers first (independent loads, one L2 latency), then solves the block
+// with shuffles; then every thread updates its rows outside the block.
 template <typename T, typename X>
 __device__ void trsv_item(const T *W, int n, bool lower, bool unit, bool trans, X *x) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -259,51 +292,158 @@ __device__ void trsv_item(const T *W, int n, bool lower, bool unit, bool trans, 
         const int b = lower ? bi : nblk - 1 - bi;
         const int i0 = b * 32, bs = min(32, n - i0);
         if (warp == 0) {
+            X lr[32];
+#pragma unroll
+            for (int k = 0; k < 32; k++) lr[k] = (lane < bs && k < bs) ? L(i0 + lane, i0 + k) : X(0);
             X xi = lane < bs ? x[i0 + lane] : X(0);
             if (lower) {
-                for (int k = 0; k < bs; k++) {
-                    if (lane == k && !unit) xi /= L(i0 + k, i0 + k);
-                    X xk = __shfl_sync(0xffffffffu, xi, k);
-                    if (lane > k && lane < bs) xi = fma(-L(i0 + lane, i0 + k), xk, xi);
+#pragma unroll
+                for (int k = 0; k < 32; k++) {
+                    if (k >= bs) break;
+                    if (lane == k && !unit) xi /= lr[k];
+                    const X xk = __shfl_sync(0xffffffffu, xi, k);
+                    if (lane > k && lane < bs) xi = fma(-lr[k], xk, xi);
                 }
             } else {
-                for (int k = bs - 1; k >= 0; k--) {
-                    if (lane == k && !unit) xi /= L(i0 + k, i0 + k);
-                    X xk = __shfl_sync(0xffffffffu, xi, k);
-                    if (lane < k) xi = fma(-L(i0 + lane, i0 + k), xk, xi);
+#pragma unroll
+                for (int k = 31; k >= 0; k--) {
+                    if (k >= bs) continue;
+                    if (lane == k && !unit) xi /= lr[k];
+                    const X xk = __shfl_sync(0xffffffffu, xi, k);
+                    if (lane < k) xi = fma(-lr[k], xk, xi);
                 }
             }
             if (lane < bs) x[i0 + lane] = xi;
         }
         __syncthreads();
         // rows outside the block
-        if (lower) {
-            for (int r = i0 + bs + tid; r < n; r += BT) {
-                X s = x[r];
-                for (int k = 0; k < bs; k++) s = fma(-L(r, i0 + k), x[i0 + k], s);
-                x[r] = s;
-            }
-        } else {
-            for (int r = tid; r < i0; r += BT) {
-                X s = x[r];
-                for (int k = 0; k < bs; k++) s = fma(-L(r, i0 + k), x[i0 + k], s);
-                x[r] = s;
-            }
+        const int r0 = lower ? i0 + bs : 0, r1 = lower ? n : i0;
+        for (int r = r0 + tid; r < r1; r += BT) {
+            X s = x[r];
+#pragma unroll 8
+            for (int k = 0; k < 32; k++)
+                if (k < bs) s = fma(-L(r, i0 + k), x[i0 + k], s);
+            x[r] = s;
         }
         __syncthreads();
     }
 }
 
-template <typename T, typename X>
-__device__ void solve_item(const T *W, int n, int kind, const int *piv, X *x) {
-    if (kind == 0 && threadIdx.x == 0)
-        for (int i = 0; i < n; i++)
-            if (piv[i]) {
-                X t = x[i];
-                x[i] = x[i + piv[i]];
-                x[i + piv[i]] = t;
+// The relative pivots of an LU item as one permutation: x_perm[i] =
+// x[perm[i]] applies the interchanges i <-> i + piv[i] in increasing i
+// (LU.cs:431-440) in one gather.  One thread, once per item.
+__device__ void pivots_to_perm(const int *piv, int n, int kind, int *perm) {
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < n; i++) perm[i] = i;
+        if (kind == 0)
+            for (int i = 0; i < n; i++) {
+                const int p = piv[i];
+                if (p) {
+                    const int t = perm[i];
+                    perm[i] = perm[i + p];
+                    perm[i + p] = t;
+                }
             }
+    }
     __syncthreads();
+}
+
+// Mixed mode keeps its FP32 factor only for the correction solves, so each
+// 32 x 32 diagonal block of it is replaced by its inverse once after the
+// factorization (LU: strict lower part inv(L_kk), unit; upper part with the
+// diagonal inv(U_kk); Cholesky: lower part with the diagonal inv(L_kk)).
+// Every later block solve is then a product with the inverse (a lane per
+// row, no sequential chain).  Warp w inverts the blocks w, w + 8, ..: the
+// block goes through a 32 x 33 shared tile (tiles[w]), lane c forms column c
+// of the inverse in registers (static indices).
+__device__ void invert_diag_blocks(float *W, int n, int kind, float *tiles) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float *Tl = tiles + warp * 32 * 33;
+    const int nblk = (n + 31) / 32;
+    for (int b = warp; b < nblk; b += BT / 32) {
+        const int i0 = b * 32, bs = min(32, n - i0);
+        // the block, padded with the identity
+        for (int r = 0; r < 32; r++)
+            Tl[r * 33 + lane] = (r < bs && lane < bs) ? W[(i64)(i0 + r) * n + i0 + lane] : (r == lane ? 1.f : 0.f);
+        __syncwarp();
+        const int c = lane;
+        {
+            // lower triangle: unit (LU) or with the diagonal (Cholesky)
+            float x[32];
+#pragma unroll
+            for (int i = 0; i < 32; i++) {
+                float s = (i == c) ? 1.f : 0.f;
+#pragma unroll
+                for (int k = 0; k < i; k++) s = fmaf(-Tl[i * 33 + k], x[k], s);
+                x[i] = kind == 2 ? s / Tl[i * 33 + i] : s;
+            }
+            // column c below (Cholesky: and on) the diagonal
+#pragma unroll
+            for (int r = 0; r < 32; r++)
+                if (r < bs && c < bs && (kind == 2 ? r >= c : r > c)) W[(i64)(i0 + r) * n + i0 + c] = x[r];
+        }
+        if (kind != 2) {
+            // upper triangle with the diagonal (LU's U)
+            float y[32];
+#pragma unroll
+            for (int i = 31; i >= 0; i--) {
+                float s = (i == c) ? 1.f : 0.f;
+#pragma unroll
+                for (int k = i + 1; k < 32; k++) s = fmaf(-Tl[i * 33 + k], y[k], s);
+                y[i] = s / Tl[i * 33 + i];
+            }
+#pragma unroll
+            for (int r = 0; r < 32; r++)
+                if (r < bs && c < bs && r <= c) W[(i64)(i0 + r) * n + i0 + c] = y[r];
+        }
+        __syncwarp();
+    }
+    __syncthreads();
+}
+
+// Triangular solve with the inverted diagonal blocks (invert_diag_blocks):
+// per 32-row block, warp 0 forms x_blk = inv(T_kk) x_blk (lane i: one row or,
+// transposed, one column of the inverse), then every thread updates its rows
+// outside the block with the off-diagonal part of the factor.
+__device__ void trsv_item_inv(const float *W, int n, bool lower, bool unit, bool trans, float *x) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    auto L = [&](int i, int k) -> float { return trans ? W[(i64)k * n + i] : W[(i64)i * n + k]; };
+    const int nblk = (n + 31) / 32;
+    for (int bi = 0; bi < nblk; bi++) {
+        const int b = lower ? bi : nblk - 1 - bi;
+        const int i0 = b * 32, bs = min(32, n - i0);
+        if (warp == 0) {
+            float li[32];
+#pragma unroll
+            for (int k = 0; k < 32; k++) {
+                const bool in = lane < bs && k < bs && (lower ? k <= lane : k >= lane);
+                li[k] = in ? L(i0 + lane, i0 + k) : 0.f;
+            }
+            float xv[32];
+#pragma unroll
+            for (int k = 0; k < 32; k++) xv[k] = k < bs ? x[i0 + k] : 0.f;
+            __syncwarp();
+            float y = 0.f;   // a unit diagonal is implicit: 1 in place of the stored entry
+#pragma unroll
+            for (int k = 0; k < 32; k++) y = fmaf((unit && k == lane) ? 1.f : li[k], xv[k], y);
+            if (lane < bs) x[i0 + lane] = y;
+        }
+        __syncthreads();
+        const int r0 = lower ? i0 + bs : 0, r1 = lower ? n : i0;
+        for (int r = r0 + tid; r < r1; r += BT) {
+            float s = x[r];
+#pragma unroll 8
+            for (int k = 0; k < 32; k++)
+                if (k < bs) s = fmaf(-L(r, i0 + k), x[i0 + k], s);
+            x[r] = s;
+        }
+        __syncthreads();
+    }
+}
+
+// x holds the right-hand side already permuted (pivots_to_perm)
+template <typename T, typename X>
+__device__ void solve_item(const T *W, int n, int kind, X *x) {
     if (kind == 2) {
         trsv_item<T, X>(W, n, true, false, false, x);
         trsv_item<T, X>(W, n, false, false, true, x);
@@ -340,7 +480,10 @@ struct BArgs {
     double tol;
 };
 
-__global__ void __launch_bounds__(BT) k_batched(BArgs a) {
+// MIXED: FP32 factor + FP64 refinement (two CTAs per SM); plain: FP64 (its
+// shared memory allows one CTA per SM, so it may use more registers)
+template <bool MIXED>
+__global__ void __launch_bounds__(BT, MIXED ? 2 : 1) k_batched(BArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ BScratch S;
     __shared__ int s_item;
@@ -358,16 +501,18 @@ __global__ void __launch_bounds__(BT) k_batched(BArgs a) {
         double *x = a.X + it.v;
         int *piv = a.piv + it.v;
         int rc;
-        if (!a.mixed) {
+        if constexpr (!MIXED) {
             double *Ps = (double *)smem;
             double *Us = Ps + (size_t)n * (it.nb + 1);
             double *xs = Us + (size_t)it.nb * n;
+            int *perm = (int *)(xs + n);
             rc = factor_item<double>(A, n, it.kind, it.nb, piv, Ps, Us, S);
             if (tid == 0) a.info[a.order[q]] = rc;
             if (rc == 0) {
-                for (int i = tid; i < n; i += BT) xs[i] = b[i];
+                pivots_to_perm(piv, n, it.kind, perm);
+                for (int i = tid; i < n; i += BT) xs[i] = b[perm[i]];
                 __syncthreads();
-                solve_item<double, double>(A, n, it.kind, piv, xs);
+                solve_item<double, double>(A, n, it.kind, xs);
                 for (int i = tid; i < n; i += BT) x[i] = xs[i];
             }
             if (tid == 0) a.iters[a.order[q]] = 0;
@@ -378,6 +523,7 @@ __global__ void __launch_bounds__(BT) k_batched(BArgs a) {
             float *ds = Us + (size_t)it.nb * n;
             double *xs = (double *)(((uintptr_t)(ds + n) + 15) & ~(uintptr_t)15);
             double *rs = xs + n;
+            int *perm = (int *)(rs + n);
             for (int e = tid; e < n * n; e += BT) Wf[e] = (float)A[e];
             __syncthreads();
             // ||A||_inf of the FP64 matrix and ||b||_inf, before the copy is
@@ -396,13 +542,21 @@ __global__ void __launch_bounds__(BT) k_batched(BArgs a) {
             if (tid == 0) a.info[a.order[q]] = rc;
             int iters = -1;
             if (rc == 0) {
+                invert_diag_blocks(Wf, n, it.kind, Ps);   // the panel buffer is free now
+                pivots_to_perm(piv, n, it.kind, perm);
                 for (int i = tid; i < n; i += BT) { xs[i] = 0.0; rs[i] = b[i]; }
                 __syncthreads();
                 for (int k = 0; k <= a.max_iter; k++) {
-                    // d = LU \ r in FP32, x += d in FP64
-                    for (int i = tid; i < n; i += BT) ds[i] = (float)rs[i];
+                    // d = LU \ P r in FP32, x += d in FP64
+                    for (int i = tid; i < n; i += BT) ds[i] = (float)rs[perm[i]];
                     __syncthreads();
-                    solve_item<float, float>(Wf, n, it.kind, piv, ds);
+                    if (it.kind == 2) {
+                        trsv_item_inv(Wf, n, true, false, false, ds);
+                        trsv_item_inv(Wf, n, false, false, true, ds);
+                    } else {
+                        trsv_item_inv(Wf, n, true, true, false, ds);
+                        trsv_item_inv(Wf, n, false, false, false, ds);
+                    }
                     for (int i = tid; i < n; i += BT) xs[i] += (double)ds[i];
                     __syncthreads();
                     // r = b - A x in FP64
@@ -498,8 +652,13 @@ int ddla_batched_plan_create(ddla_handle h, int64_t count, const int32_t *n, con
         vo += ni;
         P->max_n = std::max(P->max_n, ni);
         // plain: Ps, Us, x in FP64; mixed: Ps, Us, d in FP32 + x, r in FP64
+        // + the item's permutation (n ints)
         size_t sm = mixed ? sizeof(float) * ((size_t)ni * (nb + 1) + (size_t)nb * ni + ni) + 16 + sizeof(double) * 2 * ni
                           : sizeof(double) * ((size_t)ni * (nb + 1) + (size_t)nb * ni + ni);
+        sm += sizeof(int) * (size_t)ni;
+        // mixed: the panel buffer also holds one 32 x 33 tile per warp while
+        // the diagonal blocks are inverted
+        if (mixed) sm = std::max(sm, sizeof(float) * (BT / 32) * 32 * 33);
         smem = std::max(smem, sm);
         P->flops += (ki == 2 ? 1.0 / 3.0 : 2.0 / 3.0) * (double)ni * ni * ni + 2.0 * ni * ni;
         P->n_host.push_back(ni);
@@ -508,7 +667,6 @@ int ddla_batched_plan_create(ddla_handle h, int64_t count, const int32_t *n, con
     std::vector<int> order((size_t)count);
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return items[x].n > items[y].n; });
-    cudaStream_t s = h->stream;
     int rc = 0;
     auto fail = [&](int code) {
         if (P->d_items) cudaFree(P->d_items);
@@ -532,14 +690,15 @@ int ddla_batched_plan_create(ddla_handle h, int64_t count, const int32_t *n, con
         return fail(DDLA_ERR_CUDA);
     }
     size_t avail = 0;
-    rc = max_dyn_smem((const void *)k_batched, h->smem_optin, &avail);
+    const void *kfn = mixed ? (const void *)k_batched<true> : (const void *)k_batched<false>;
+    rc = max_dyn_smem(kfn, h->smem_optin, &avail);
     if (rc) return fail(rc);
     if (smem > avail) {
         set_error("batched plan: items too large for shared memory");
         return fail(DDLA_ERR_UNSUPPORTED);
     }
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batched, BT, smem) != cudaSuccess || per_sm < 1)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, BT, smem) != cudaSuccess || per_sm < 1)
         per_sm = 1;
     int64_t want = tune_get("batched.ctas_per_sm", 0);
     if (want > 0 && want < per_sm) per_sm = (int)want;
@@ -554,7 +713,8 @@ int ddla_batched_plan_create(ddla_handle h, int64_t count, const int32_t *n, con
     bool ok = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
     if (ok) {
         cudaMemsetAsync(P->d_counter, 0, sizeof(int), cap);
-        k_batched<<<P->grid, BT, smem, cap>>>(P->args);
+        if (mixed) k_batched<true><<<P->grid, BT, smem, cap>>>(P->args);
+        else k_batched<false><<<P->grid, BT, smem, cap>>>(P->args);
         count_launch();
         ok = cudaStreamEndCapture(cap, &P->graph) == cudaSuccess;
     }
@@ -565,7 +725,6 @@ int ddla_batched_plan_create(ddla_handle h, int64_t count, const int32_t *n, con
         set_error("batched plan: CUDA graph capture failed");
         return fail(DDLA_ERR_CUDA);
     }
-    (void)s;
     *plan_out = P;
     return 0;
 }
