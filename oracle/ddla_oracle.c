@@ -1355,3 +1355,169 @@ void orc_batched(i64 count, const int *n, const int *kind, double *a, const doub
     g_threads = saved;
     free(ao); free(vo);
 }
+
+/* ------------------------------------------------------------------------ */
+/* Two-stage bidiagonal reduction, DDLA/Transformations/Bidiagonaling.cs     */
+/* (Bidiag -> TwoStageBidiag, :14-33 and :334-582)                           */
+/* ------------------------------------------------------------------------ */
+
+#define BD2_BLOCK 32   /* TwoStageBidiag.MaxBlockSize, Bidiagonaling.cs:336 */
+
+/* BidHelper.BuildHH (Bidiagonaling.cs:705-718): |x| from the sum of squares,
+ * rho = -sign(a11) |x|, x2 *= 1 / (a11 - rho), tau = (1 + |x2|^2) / 2. */
+static void bd2_build_hh(double *a11, double *x, i64 n, i64 inc, double *tau) {
+    double xsq = 0.0;
+    for (i64 i = 0; i < n; i++) xsq = fma(x[i * inc], x[i * inc], xsq);
+    double alphasq = *a11 * *a11 + xsq;
+    double alpha = sqrt(alphasq);
+    double sign = *a11 > 0 ? 1.0 : (*a11 < 0 ? -1.0 : 0.0);   /* Math.Sign */
+    double rho = -sign * alpha;
+    double miu = *a11 - rho;
+    double s = 1.0 / miu;
+    for (i64 i = 0; i < n; i++) x[i * inc] *= s;
+    double t = 0.0;
+    for (i64 i = 0; i < n; i++) t = fma(x[i * inc], x[i * inc], t);
+    *tau = 1.0 + t;
+    *a11 = rho;
+    *tau /= 2.0;
+}
+
+/* BidHelper.ApplyHH (Bidiagonaling.cs:752-764), per column of A2:
+ * w = a12 + a21 . a22, w /= tau, a12 -= w, a22 -= w a21. */
+static void bd2_apply_hh(const double *a21, i64 n, i64 inc, mat A2, double tau) {
+    for (i64 c = 0; c < A2.c; c++) {
+        double dot = 0.0;
+        for (i64 i = 0; i < n; i++) dot = fma(a21[i * inc], *AT(A2, 1 + i, c), dot);
+        double w = *AT(A2, 0, c) + dot;
+        w /= tau;
+        *AT(A2, 0, c) -= w;
+        for (i64 i = 0; i < n; i++) *AT(A2, 1 + i, c) = fma(-w, a21[i * inc], *AT(A2, 1 + i, c));
+    }
+}
+
+/* BidHelper.QRUnblock (Bidiagonaling.cs:594-615): the QR of one block column
+ * with its UT factor: T(i, i) = tau_i, T(0:i, i) = A(i, 0:i)^T + A20^T a21. */
+static void bd2_qr_unblock(mat A, mat T) {
+    i64 m = A.r, n = A.c, k = m < n ? m : n;
+    for (i64 i = 0; i < k; i++) {
+        double *x = AT(A, i + 1 < m ? i + 1 : i, i);
+        bd2_build_hh(AT(A, i, i), x, m - i - 1, A.rs, AT(T, i, i));
+        bd2_apply_hh(x, m - i - 1, A.rs, sub(A, i, m - i, i + 1, n - i - 1), *AT(T, i, i));
+        for (i64 j = 0; j < i; j++) {
+            double t = *AT(A, i, j);
+            for (i64 r = i + 1; r < m; r++) t = fma(*AT(A, r, j), *AT(A, r, i), t);
+            *AT(T, j, i) = t;
+        }
+    }
+}
+
+/* Bd2Bi_StepSide (Bidiagonaling.cs:539-551): the reflector of A's first
+ * column (HouseHolder.BuildHouseHolder) applied from the left to the other
+ * columns; tau and the vector go to t, the column's tail is cleared. */
+static void bd2_step_side(mat A, double *t, i64 tinc) {
+    i64 len = A.r - 1;
+    double *chi = AT(A, 0, 0);
+    double *x = AT(A, A.r > 1 ? 1 : 0, 0);
+    house_build(chi, x, len, A.rs, &t[0]);
+    house_apply_left(t[0], x, A.rs, sub(A, 0, 1, 1, A.c - 1), sub(A, 1, len, 1, A.c - 1));
+    for (i64 i = 0; i < len; i++) { t[(1 + i) * tinc] = x[i * A.rs]; x[i * A.rs] = 0.0; }
+}
+
+/* Bd2Bi_StepCycle (Bidiagonaling.cs:489-516): chase row i's band to the
+ * superdiagonal, alternating right (transposed view) and left reflectors. */
+static void bd2_step_cycle(mat A, double *tu, double *tv, i64 tinc, i64 block) {
+    i64 is = 1, ie = is + block, ie2 = ie + block;
+    i64 rows = A.r;
+    if (rows <= ie) {
+        bd2_step_side(tr(sub(A, 0, A.r, is, A.c - is)), tv + is * tinc, tinc);
+        bd2_step_side(sub(A, is, A.r - is, is, A.c - is), tu + is * tinc, tinc);
+        return;
+    }
+    bd2_step_side(tr(sub(A, 0, ie, is, ie - is)), tv + is * tinc, tinc);
+    while (ie2 < rows) {
+        bd2_step_side(sub(A, is, ie - is, is, ie2 - is), tu + is * tinc, tinc);
+        bd2_step_side(tr(sub(A, is, ie2 - is, ie, ie2 - ie)), tv + ie * tinc, tinc);
+        is += block; ie += block; ie2 += block;
+    }
+    bd2_step_side(sub(A, is, ie - is, is, A.c - is), tu + is * tinc, tinc);
+    bd2_step_side(tr(sub(A, is, A.r - is, ie, A.c - ie)), tv + ie * tinc, tinc);
+    bd2_step_side(sub(A, ie, A.r - ie, ie, A.c - ie), tu + ie * tinc, tinc);
+}
+
+/* Bd2Bi_Back (Bidiagonaling.cs:553-558): Q <- Q H, H = I - u u^T / tau with
+ * u = (1, t[1..]) (ApplyHouseHolder on Q^T from the left). */
+static void bd2_back(const double *t, i64 tinc, i64 len, mat Q) {
+    if (len <= 0) return;
+    mat QT = tr(Q);
+    double *u2 = (double *)malloc(sizeof(double) * (len > 1 ? len - 1 : 1));
+    for (i64 i = 0; i + 1 < len; i++) u2[i] = t[(1 + i) * tinc];
+    house_apply_left(t[0], u2, 1, sub(QT, 0, 1, 0, QT.c), sub(QT, 1, len - 1, 0, QT.c));
+    free(u2);
+}
+
+/* Bidiagonaling.Bidiag(A, U, V, d, e) through TwoStageBidiag, m >= n: A is a
+ * work copy (overwritten), U m x m, V n x n, d (n), e (n - 1).  Ge2Bd
+ * (Bidiagonaling.cs:384-474): blocks of BD2_BLOCK columns, each a QR of the
+ * block column (its reflector applied to the columns right of it) and an LQ
+ * of the block row right of it (a QR of its transpose, applied to the rows
+ * below); U and V from the two sets of block reflectors (ApplyQlnfc), which
+ * leaves an upper band of width BD2_BLOCK.  Bd2Bi (:478-487): for each row a
+ * bulge-chasing cycle of small reflectors down the band, stored in TU2 / TV2,
+ * then every cycle's reflectors applied to U and V. */
+int orc_dbidiag2s(i64 m, i64 n, double *a, i64 rsa, i64 csa, double *u, i64 rsu, i64 csu, double *v, i64 rsv,
+                  i64 csv, double *d, double *e) {
+    if (m < n) return -1;
+    if (n == 0) return 0;
+    mat W = mk(a, m, n, rsa, csa), U = mk(u, m, m, rsu, csu), V = mk(v, n, n, rsv, csv);
+    const i64 bs = n < BD2_BLOCK ? n : BD2_BLOCK;          /* TUBlockSize */
+    const i64 tvc = n - bs;
+    double *tu = (double *)calloc((size_t)bs * n, sizeof(double));
+    double *tv = (double *)calloc((size_t)bs * (tvc > 0 ? tvc : 1), sizeof(double));
+    mat TU = mk(tu, bs, n, n, 1), TV = mk(tv, bs, tvc > 0 ? tvc : 1, tvc > 0 ? tvc : 1, 1);
+    for (i64 i = 0; i < m; i++) for (i64 j = 0; j < m; j++) *AT(U, i, j) = i == j;
+    for (i64 i = 0; i < n; i++) for (i64 j = 0; j < n; j++) *AT(V, i, j) = i == j;
+    /* Ge2Bd */
+    for (i64 i0 = 0; i0 < n; ) {
+        i64 b = n - i0 < BD2_BLOCK ? n - i0 : BD2_BLOCK;
+        mat AB1 = sub(W, i0, m - i0, i0, b), AB2 = sub(W, i0, m - i0, i0 + b, n - i0 - b);
+        mat TUT1 = sub(TU, 0, b, i0, b);
+        bd2_qr_unblock(AB1, TUT1);
+        qr_apply_one(1, sub(AB1, 0, b, 0, b), sub(AB1, b, m - i0 - b, 0, b), TUT1, sub(AB2, 0, b, 0, AB2.c),
+                     sub(AB2, b, m - i0 - b, 0, AB2.c));
+        i64 c22 = n - i0 - b;
+        if (c22 > 0) {
+            i64 b2 = c22 < BD2_BLOCK ? c22 : b;   /* the ragged last block row: block2 = A22.Cols */
+            mat R = tr(sub(W, i0, b2, i0 + b, c22));           /* c22 x b2 */
+            mat below = tr(sub(W, i0 + b2, m - i0 - b2, i0 + b, c22));
+            mat TVT1 = sub(TV, 0, b2, i0, b2);
+            bd2_qr_unblock(R, TVT1);
+            qr_apply_one(1, sub(R, 0, b2, 0, b2), sub(R, b2, c22 - b2, 0, b2), TVT1, sub(below, 0, b2, 0, below.c),
+                         sub(below, b2, c22 - b2, 0, below.c));
+        }
+        i0 += b;
+    }
+    qr_apply(0, W, TU, U);
+    for (i64 i = 0; i < m; i++) for (i64 j = 0; j < i && j < n; j++) *AT(W, i, j) = 0.0;
+    if (tvc > 0) {
+        mat A = tr(sub(W, 0, tvc, bs, tvc));
+        qr_apply(0, A, TV, sub(V, bs, tvc, bs, tvc));
+        for (i64 i = 0; i < tvc; i++) for (i64 j = 0; j < i; j++) *AT(A, i, j) = 0.0;
+    }
+    /* Bd2Bi */
+    double *tu2 = (double *)calloc((size_t)n * n, sizeof(double));
+    double *tv2 = (double *)calloc((size_t)n * n, sizeof(double));
+    for (i64 i = 0; i + 1 < n; i++)
+        bd2_step_cycle(sub(W, i, n - i, i, n - i), tu2 + i * n + i, tv2 + i * n + i, 1, bs);
+    for (i64 i = 0; i + 1 < n; i++) {
+        const i64 rows = n - i, maxu = (rows - 2) / bs + 1;
+        for (i64 k = 0; k < maxu; k++) {
+            i64 is = 1 + k * bs, ie = is + bs < rows ? is + bs : rows;
+            bd2_back(tv2 + i * n + i + is, 1, ie - is, sub(V, 0, n, i + is, ie - is));
+            bd2_back(tu2 + i * n + i + is, 1, ie - is, sub(U, 0, m, i + is, ie - is));
+        }
+    }
+    for (i64 i = 0; i < n; i++) d[i] = *AT(W, i, i);
+    for (i64 i = 0; i + 1 < n; i++) e[i] = *AT(W, i, i + 1);
+    free(tu); free(tv); free(tu2); free(tv2);
+    return 0;
+}

@@ -84,6 +84,7 @@ def lib():
                                   _dp, _i64, _i64]
         L.orc_set_threads.argtypes = [C.c_int]
         L.orc_batched.argtypes = [_i64, _ip, _ip, _dp, _dp, _dp, _ip, _ip]
+        L.orc_dbidiag2s.argtypes = [_i64, _i64, _dp, _i64, _i64, _dp, _i64, _i64, _dp, _i64, _i64, _dp, _dp]
         L.orc_batched.restype = None
         L.orc_contract_plan.argtypes = [C.c_char_p, C.c_int, C.POINTER(_i64), C.POINTER(_i64),
                                         C.c_int, C.POINTER(_i64), C.POINTER(_i64),
@@ -216,6 +217,18 @@ def bidiag(A):
     if rc:
         raise ValueError("orc_dbidiag: m < n")
     return U, V, d, e[:max(n - 1, 0)], TU, TV
+
+
+def bidiag2s(A):
+    """Bidiagonaling.Bidiag (two stages through TwoStageBidiag, m >= n):
+    returns (U, V, d, e) with U^T A V = bidiag(d, e); A is overwritten."""
+    m, n = A.shape
+    U, V = np.zeros((m, m)), np.zeros((n, n))
+    d, e = np.zeros(n), np.zeros(max(n - 1, 1))
+    rc = lib().orc_dbidiag2s(m, n, _ptr(A), *_st(A), _ptr(U), *_st(U), _ptr(V), *_st(V), _ptr(d), _ptr(e))
+    if rc:
+        raise ValueError("orc_dbidiag2s: m < n")
+    return U, V, d, e[:max(n - 1, 0)]
 
 
 def dtrsm(side, uplo, ta, diag, alpha, A, B):

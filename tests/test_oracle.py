@@ -473,3 +473,44 @@ def test_batched_oracle_equals_item_calls(orc):
             orc.dpotrf(0xC0, Fo)
             orc.dpotrs(0xC0, Fo, xo)
         assert np.array_equal(F, Fo) and np.array_equal(x, xo.ravel())
+
+
+@pytest.mark.parametrize("m,n", [(5, 3), (7, 7), (33, 32), (64, 64), (95, 61), (131, 131), (300, 257)])
+def test_bidiag2s_oracle_properties(orc, m, n):
+    """The oracle's two-stage bidiagonal reduction (Bidiagonaling.Bidiag through
+    TwoStageBidiag) pinned by properties, with the bars of DDLA's SVD tests
+    (Tests/TestFlame/TestSVD.cs:31-72: reconstruction norms < 1e-10,
+    orthogonality < 1e-8) and the singular values against LAPACK."""
+    r = rng(m * 1000 + n)
+    A = uniform(r, (m, n))
+    W = A.copy()
+    U, V, d, e = orc.bidiag2s(W)
+    B = np.zeros((m, n))
+    B[np.arange(n), np.arange(n)] = d
+    if n > 1:
+        B[np.arange(n - 1), np.arange(1, n)] = e
+    for v in norms(A - U @ B @ V.T):
+        assert v < 1e-10
+    assert np.linalg.norm(U @ U.T - np.eye(m)) < 1e-8
+    assert np.linalg.norm(V @ V.T - np.eye(n)) < 1e-8
+    sv = np.sort(np.linalg.svd(B, compute_uv=False))
+    ref = np.sort(np.linalg.svd(A, compute_uv=False))
+    assert np.max(np.abs(sv - ref)) <= 1e-13 * ref.max()
+
+
+def test_bidiag2s_oracle_band_after_stage_one(orc):
+    """Same singular values as the one-stage reduction (Bidiag2) of the same
+    matrix: both are orthogonal reductions of A."""
+    r = rng(4242)
+    A = uniform(r, (90, 70))
+    U1, V1, d1, e1, _, _ = orc.bidiag(A.copy())
+    U2, V2, d2, e2 = orc.bidiag2s(A.copy())
+
+    def bd(d, e):
+        B = np.diag(d)
+        if len(e):
+            B[np.arange(len(e)), np.arange(1, len(e) + 1)] = e
+        return B
+    s1 = np.sort(np.linalg.svd(bd(d1, e1), compute_uv=False))
+    s2 = np.sort(np.linalg.svd(bd(d2, e2), compute_uv=False))
+    assert np.max(np.abs(s1 - s2)) <= 1e-13 * s1.max()
