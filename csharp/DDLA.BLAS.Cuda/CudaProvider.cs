@@ -132,6 +132,22 @@ public static class CudaProvider
         return rep;
     }
 
+    // Bidiagonaling.Bidiag(A, U, V, d, e) (DDLA/Transformations/Bidiagonaling.cs:24-32): the two-stage
+    // reduction on a column-major clone of A, as TwoStageBidiag works (Bidiagonaling.cs:250-257)
+    public static void Bidiag(MatrixView A, MatrixView U, MatrixView V, VectorView d, VectorView e)
+    {
+        if (A.Rows < A.Cols) throw new ArgumentException("Only support m >= n");
+        if (A.Cols == 0) return;
+        var W = A.Clone(colMajor: true);
+        var dd = VectorView.Create(A.Cols);
+        var ee = VectorView.Create(Math.Max(A.Cols - 1, 1));
+        Source.Check(Source.Bidiag(A.Rows, A.Cols, ref W.GetHeadRef(), W.RowStride, W.ColStride, ref dd.GetHeadRef(),
+            ref ee.GetHeadRef(), ref U.GetHeadRef(), U.RowStride, U.ColStride, ref V.GetHeadRef(), V.RowStride,
+            V.ColStride, in Options), "Bidiag");
+        dd.CopyTo(d);
+        if (A.Cols > 1) ee[..(A.Cols - 1)].CopyTo(e);
+    }
+
     // BlasProvider.GeMM's checked wrapper (DDLA/BLAS/3m.cs:10-31) on the GPU
     public static void GeMM(double alpha, MatrixView A, MatrixView B, double beta, MatrixView C)
     {

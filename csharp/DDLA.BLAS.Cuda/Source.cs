@@ -180,6 +180,12 @@ public static partial class Source
     public static extern int Bidiag2(dim_t m, dim_t n, ref double a, inc_t rsa, inc_t csa, ref double d, ref double e,
         ref double u, inc_t rsu, inc_t csu, ref double v, inc_t rsv, inc_t csv, in Opts opts);
 
+    // Bidiagonaling.Bidiag(A, U, V, d, e) through TwoStageBidiag (Bidiagonaling.cs:24-32, 334-582), m >= n;
+    // a is overwritten (pass a clone: DDLA's Bidiag leaves A unchanged)
+    [DllImport(Lib, EntryPoint = "ddla_dbidiag_twostage")]
+    public static extern int Bidiag(dim_t m, dim_t n, ref double a, inc_t rsa, inc_t csa, ref double d, ref double e,
+        ref double u, inc_t rsu, inc_t csu, ref double v, inc_t rsv, inc_t csv, in Opts opts);
+
     // ------------------------------------------------------------ einsum
 
     /// <summary>ddla_contract_mode: length and element strides in A, B, C.</summary>

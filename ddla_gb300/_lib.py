@@ -107,6 +107,10 @@ _SIGS = {
                                C.POINTER(Opts)]),
     "ddla_dev_dbidiag": (C.c_int, [_h, _i64, _i64, _pd, _i64, _i64, _pd, _pd, _pd, _i64, _i64, _pd, _i64, _i64,
                                    C.POINTER(Opts)]),
+    "ddla_dbidiag_twostage": (C.c_int, [_i64, _i64, _pd, _i64, _i64, _pd, _pd, _pd, _i64, _i64, _pd, _i64, _i64,
+                                        C.POINTER(Opts)]),
+    "ddla_dev_dbidiag_twostage": (C.c_int, [_h, _i64, _i64, _pd, _i64, _i64, _pd, _pd, _pd, _i64, _i64, _pd, _i64,
+                                            _i64, C.POINTER(Opts)]),
     "ddla_dgetrf": (C.c_int, [_i64, _pd, _i64, _i64, _pi, C.POINTER(Opts)]),
     "ddla_dgetrs": (C.c_int, [_i32, _i64, _i64, _pd, _i64, _i64, _pi, _pd, _i64, _i64]),
     "ddla_dgetrf_nopiv": (C.c_int, [_i64, _pd, _i64, _i64, C.POINTER(Opts)]),

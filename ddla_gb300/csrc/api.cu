@@ -884,6 +884,53 @@ int ddla_dbidiag(ddla_dim_t m, ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc
     return 0;
 }
 
+int ddla_dev_dbidiag_twostage(ddla_handle h, ddla_dim_t m, ddla_dim_t n, double *a, ddla_inc_t rsa,
+                              ddla_inc_t csa, double *d, double *e, double *u, ddla_inc_t rsu, ddla_inc_t csu,
+                              double *v, ddla_inc_t rsv, ddla_inc_t csv, const ddla_opts *opts) {
+    CHECK_ARG(h != nullptr, 1);
+    CHECK_ARG(m >= 0, 2);
+    CHECK_ARG(n >= 0 && n <= m, 3);
+    CHECK_ARG(d != nullptr || n == 0, 7);
+    CHECK_ARG(e != nullptr || n <= 1, 8);
+    CHECK_ARG(u != nullptr || m == 0, 9);
+    CHECK_ARG(v != nullptr || n == 0, 12);
+    CHECK_ARG(!opts || opts->precision == 0 || opts->precision == DDLA_PREC_FP64 ||
+                  opts->precision == DDLA_PREC_OZAKI, 15);
+    if (n == 0) return 0;
+    return bidiag2s(h, m, n, View<double>{a, m, n, rsa, csa}, View<double>{u, m, m, rsu, csu},
+                    View<double>{v, n, n, rsv, csv}, d, e, fprec(opts));
+}
+
+int ddla_dbidiag_twostage(ddla_dim_t m, ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t csa, double *d,
+                          double *e, double *u, ddla_inc_t rsu, ddla_inc_t csu, double *v, ddla_inc_t rsv,
+                          ddla_inc_t csv, const ddla_opts *opts) {
+    CHECK_ARG(m >= 0, 1);
+    CHECK_ARG(n >= 0 && n <= m, 2);
+    CHECK_ARG(d != nullptr || n == 0, 6);
+    CHECK_ARG(e != nullptr || n <= 1, 7);
+    CHECK_ARG(u != nullptr || m == 0, 8);
+    CHECK_ARG(v != nullptr || n == 0, 11);
+    CHECK_ARG(!opts || opts->precision == 0 || opts->precision == DDLA_PREC_FP64 ||
+                  opts->precision == DDLA_PREC_OZAKI, 14);
+    if (n == 0) return 0;
+    GET_HANDLE(h);
+    Staged sa, su, sv;
+    DDLA_TRY(stage_in(h, WS_A, a, m, n, rsa, csa, true, &sa));
+    DDLA_TRY(stage_in(h, WS_B, u, m, m, rsu, csu, false, &su));
+    DDLA_TRY(stage_in(h, WS_C, v, n, n, rsv, csv, false, &sv));
+    void *de;
+    DDLA_TRY(workspace(h, WS_PIV, sizeof(double) * (size_t)(2 * n), &de));
+    double *dd = (double *)de, *ed = dd + n;
+    DDLA_TRY(bidiag2s(h, m, n, sa.view, su.view, sv.view, dd, ed, fprec(opts)));
+    DDLA_TRY(stage_out(h, sa, a, m, n, rsa, csa));
+    DDLA_TRY(stage_out(h, su, u, m, m, rsu, csu));
+    DDLA_TRY(stage_out(h, sv, v, n, n, rsv, csv));
+    DDLA_CUDA(cudaMemcpyAsync(d, dd, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, h->stream));
+    if (n > 1) DDLA_CUDA(cudaMemcpyAsync(e, ed, sizeof(double) * (size_t)(n - 1), cudaMemcpyDeviceToHost, h->stream));
+    DDLA_CUDA(cudaStreamSynchronize(h->stream));
+    return 0;
+}
+
 // ------------------------------------------------------------------ factorizations, device
 int ddla_dev_dgetrf(ddla_handle h, ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t csa, int32_t *piv,
                     const ddla_opts *opts) {

@@ -82,7 +82,7 @@ struct ddla_handle_s {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     // Growable device scratch areas (indexed by purpose).
-    ddla::Workspace ws[21];
+    ddla::Workspace ws[22];
     // Pinned host staging for host-pointer calls.
     void *pinned = nullptr;
     size_t pinned_bytes = 0;
@@ -112,10 +112,12 @@ namespace ddla {
 //   WS_QRU     QR: explicit copy of a block's Householder vectors
 //   WS_TRD     tridiagonal reduction: vectors and partial sums
 //   WS_TRDQ    tridiagonal reduction: Q of the trailing block before its copy
+//   WS_RHS     mixed solves: a block of right-hand sides
+//   WS_BD2     two-stage bidiagonal reduction: block factors, chase reflectors
 enum WsSlot {
     WS_A = 0, WS_B = 1, WS_C = 2, WS_TMP = 3, WS_PIV = 4, WS_F32 = 5, WS_X = 6, WS_MISC = 7,
     WS_TRI = 8, WS_Y = 9, WS_PERM = 10, WS_TC = 11, WS_TC2 = 12, WS_INV = 13, WS_PINV = 14, WS_QR = 15,
-    WS_SPLIT = 16, WS_QRU = 17, WS_TRD = 18, WS_TRDQ = 19, WS_RHS = 20
+    WS_SPLIT = 16, WS_QRU = 17, WS_TRD = 18, WS_TRDQ = 19, WS_RHS = 20, WS_BD2 = 21
 };
 
 // Order of the diagonal blocks that the triangular solves invert.
@@ -217,6 +219,11 @@ int sytrd(ddla_handle h, i64 n, View<double> A, View<double> T, i64 tb, double *
 // the orthogonal factors with U^T A V = bidiag(d, e).
 int bidiag(ddla_handle h, i64 m, i64 n, View<double> A, double *d, double *e, View<double> U, View<double> V,
            int prec = DDLA_PREC_FP64);
+// Bidiagonaling.Bidiag (two-stage) on device data (bidiag2s.cu), m >= n: A
+// becomes the band and zeros, U (m x m) and V (n x n) the orthogonal factors
+// with U^T A V = bidiag(d, e).
+int bidiag2s(ddla_handle h, i64 m, i64 n, View<double> A, View<double> U, View<double> V, double *d, double *e,
+             int prec = DDLA_PREC_FP64);
 
 // Triangular-solve building blocks (trsm.cu): inverses of the 64 x 64
 // diagonal blocks, and the chained whole-system solve for <= 16 columns.

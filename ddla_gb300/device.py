@@ -108,6 +108,13 @@ class Handle:
         check(lib().ddla_dev_dbidiag(self.h, m, n, _p(A), *_st(A), _p(d), _p(e) if n > 1 else None, _p(U), *_st(U),
                                      _p(V), *_st(V), C.byref(o)), "dev_dbidiag")
 
+    def bidiag_twostage(self, A, d, e, U, V, precision=0):
+        m, n = A.shape
+        o = Opts()
+        o.precision = precision
+        check(lib().ddla_dev_dbidiag_twostage(self.h, m, n, _p(A), *_st(A), _p(d), _p(e) if n > 1 else None, _p(U),
+                                              *_st(U), _p(V), *_st(V), C.byref(o)), "dev_dbidiag_twostage")
+
     def sytrd(self, A, T, d, e, precision=0):
         n = A.shape[0]
         o = Opts()

@@ -10,6 +10,7 @@ tests read like DDLA's own tests:
   LDLT                                      DDLA/Factorizations/LDLT.cs:9-137
   QR                                        DDLA/Factorizations/QR.cs:14-534
   Tridiagonaling                            DDLA/Transformations/Tridiagonaling.cs:10-232
+  Bidiagonaling.Bidiag (two-stage)          DDLA/Transformations/Bidiagonaling.cs:14-33, 334-582
   Bidiagonaling.Bidiag2                     DDLA/Transformations/Bidiagonaling.cs:35-143
 
 Matrices are float64 numpy arrays; any 2-D view works (its element strides
@@ -560,8 +561,25 @@ class Tridiagonaling:
 
 
 class Bidiagonaling:
-    """Bidiagonaling.Bidiag2 -- DDLA/Transformations/Bidiagonaling.cs:35-143
-    (the one-stage Householder reduction, m >= n)."""
+    """Bidiagonaling.Bidiag -- DDLA/Transformations/Bidiagonaling.cs:14-33
+    (the two-stage reduction DDLA's SVD uses) and Bidiag2, :35-143 (the
+    one-stage Householder reduction); both m >= n."""
+
+    @staticmethod
+    def Bidiag(A, precision=0):
+        """Returns (U, V, d, e) with U^T A V = bidiag(d, e); A (m x n, m >= n)
+        is left unchanged, as in DDLA (TwoStageBidiag works on a column-major
+        clone, Bidiagonaling.cs:250-257)."""
+        A = _view(A, "A")
+        m, n = A.shape
+        if m < n:
+            raise ValueError("Only support m >= n")
+        W = np.array(A, order="F")
+        U, V = np.zeros((m, m), order="F"), np.zeros((n, n), order="F")
+        d, e = np.zeros(n), np.zeros(max(n - 1, 0))
+        check(lib().ddla_dbidiag_twostage(m, n, _p(W), *_st(W), _p(d), _p(e) if n > 1 else None, _p(U), *_st(U),
+                                          _p(V), *_st(V), C.byref(_opts(0, precision))), "Bidiag")
+        return U, V, d, e
 
     @staticmethod
     def Bidiag2(A, precision=0):

@@ -273,6 +273,19 @@ int ddla_dsytrd(ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t csa, double 
 int ddla_dbidiag(ddla_dim_t m, ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t csa, double *d, double *e,
                  double *u, ddla_inc_t rsu, ddla_inc_t csu, double *v, ddla_inc_t rsv, ddla_inc_t csv,
                  const ddla_opts *opts);
+/* Two-stage reduction of A (m x n, m >= n) to upper bidiagonal form, the one
+ * DDLA's SVD calls: Bidiagonaling.Bidiag through TwoStageBidiag,
+ * DDLA/Transformations/Bidiagonaling.cs:14-33 and 334-582.  Stage 1 reduces
+ * A to an upper band of width 32 with blocked QR / LQ steps (Ge2Bd), stage 2
+ * chases the band to the bidiagonal with small reflectors (Bd2Bi), whose
+ * products are accumulated into U and V.  U^T A_in V = bidiag(d, e); A is
+ * overwritten (band and zeros).  opts (may be NULL): precision
+ * DDLA_PREC_OZAKI runs stage 1's block-reflector products through the
+ * split-precision tensor-core GEMM.  DDLA_ERR_TIMEOUT if a bounded wait of
+ * the band chase gave up. */
+int ddla_dbidiag_twostage(ddla_dim_t m, ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t csa, double *d,
+                          double *e, double *u, ddla_inc_t rsu, ddla_inc_t csu, double *v, ddla_inc_t rsv,
+                          ddla_inc_t csv, const ddla_opts *opts);
 
 /* ------------------------------------------------ factorizations (host) */
 
@@ -365,6 +378,9 @@ int ddla_dev_dtrmm3(ddla_handle h, int32_t sidea, int32_t uploa, int32_t transa,
 int ddla_dev_dbidiag(ddla_handle h, ddla_dim_t m, ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t csa, double *d,
                      double *e, double *u, ddla_inc_t rsu, ddla_inc_t csu, double *v, ddla_inc_t rsv, ddla_inc_t csv,
                      const ddla_opts *opts);
+int ddla_dev_dbidiag_twostage(ddla_handle h, ddla_dim_t m, ddla_dim_t n, double *a, ddla_inc_t rsa,
+                              ddla_inc_t csa, double *d, double *e, double *u, ddla_inc_t rsu, ddla_inc_t csu,
+                              double *v, ddla_inc_t rsv, ddla_inc_t csv, const ddla_opts *opts);
 int ddla_dev_dsytrd(ddla_handle h, ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t csa, double *t,
                     ddla_dim_t t_rows, ddla_inc_t rst, ddla_inc_t cst, double *d, double *e, const ddla_opts *opts);
 int ddla_dev_dgeqrf(ddla_handle h, ddla_dim_t m, ddla_dim_t n, double *a, ddla_inc_t rsa, ddla_inc_t csa,
