@@ -22,15 +22,15 @@
 // run at the same time on disjoint parts of the band (the schedule test
 // tests/test_bd_chase_schedule.py enumerates the regions and checks it).  The
 // reflectors are stored in TU2 / TV2 (row i for cycle i) and applied to U and
-// V afterwards, cycle by cycle (BackCycle, :518-537): the reflectors of one
-// cycle act on disjoint column blocks, so one launch per cycle applies them
-// all, a warp per (row, reflector).
+// V afterwards (BackCycle, :518-537), 32 cycles per launch with the rows of U
+// and V streamed through shared memory once per launch (k_bd_back).
 //
 // Every wait is bounded: on timeout the kernel sets an error word and
 // returns; the host reports DDLA_ERR_TIMEOUT.
 #include <algorithm>
 
 #include "common.cuh"
+#include "timing.cuh"
 
 namespace ddla {
 namespace {
@@ -50,6 +50,13 @@ __global__ void k_zero_lower(double *A, i64 rs, i64 cs, i64 rows, i64 cols) {
 __global__ void k_eye2(double *Q, i64 n, i64 rs, i64 cs) {
     for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < n * n; e += (i64)gridDim.x * blockDim.x)
         Q[(e / n) * rs + (e % n) * cs] = (e / n) == (e % n) ? 1.0 : 0.0;
+}
+
+// tau of reflector j from the diagonal of its block's factor: T (bs rows,
+// leading dimension ldt) holds block i0's factor at columns i0 .. i0 + bs.
+__global__ void k_taus(const double *T, i64 ldt, i64 k, int bs, double *tau) {
+    for (i64 j = blockIdx.x * (i64)blockDim.x + threadIdx.x; j < k; j += (i64)gridDim.x * blockDim.x)
+        tau[j] = T[(j % bs) * ldt + j];
 }
 
 __global__ void k_extract_bd(const double *A, i64 rs, i64 cs, i64 n, double *d, double *e) {
@@ -77,146 +84,232 @@ struct ChaseArgs {
     int *err;
 };
 
-// StepSide (Bidiagonaling.cs:539-551) on the view M = sub(W, r0, nr, c0, nc),
-// transposed when `trans`: the reflector of M's first column
-// (HouseHolder.BuildHouseHolder, HouseHolder.cs:34-58) is applied from the
-// left to M's other columns (ApplyHouseHolder, HouseHolder.cs:95-115); tau and
-// the vector go to t, the column's tail is cleared.  All threads of the CTA.
-__device__ void step_side(const ChaseArgs &a, i64 r0, i64 nr, i64 c0, i64 nc, bool trans, double *t) {
-    __shared__ double s_u[BD2_BLOCK];
-    __shared__ double s_tau;
-    const int tid = threadIdx.x, lane = tid & 31;
-    double *p = a.W + r0 * a.rs + c0 * a.cs;
-    const i64 R = trans ? nc : nr, Cc = trans ? nr : nc;
-    auto M = [&](i64 r, i64 c) -> double & { return trans ? p[c * a.rs + r * a.cs] : p[r * a.rs + c * a.cs]; };
-    const int len = (int)(R - 1);
-    if (tid < 32) {
-        // every lane reads chi before the shuffles, lane 0 writes it after them
-        const double x = lane < len ? M(1 + lane, 0) : 0.0;
-        double chi = M(0, 0), tau, u = x;
-        double s = x * x;
-        for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
-        const double nrm = sqrt(s);
-        if (nrm == 0.0) {
-            chi = -chi;
-            tau = 0.5;
-        } else {
-            const double alpha = hypot(chi, nrm);
-            const double rho = -copysign(alpha, chi);
-            const double miu = chi - rho;
-            chi = rho;
-            u = x * (1.0 / miu);
-            const double sc = nrm / fabs(miu);
-            tau = (1.0 + sc * sc) / 2.0;
-        }
-        if (lane < len) {
-            s_u[lane] = u;
-            t[1 + lane] = u;
-            M(1 + lane, 0) = 0.0;
-        }
-        if (lane == 0) {
-            M(0, 0) = chi;
-            t[0] = tau;
-            s_tau = tau;
-        }
+// Geometry of reflector t of a cycle with `rows` rows left (Bd2Bi_StepCycle,
+// Bidiagonaling.cs:489-516): the StepSide view sub(cycle, r0, nr, c0, nc),
+// transposed for a reflector from the right (stored in TV2) and plain for one
+// from the left (TU2); toff is its offset in the cycle's row of TU2 / TV2.
+struct StepGeom {
+    i64 r0, nr, c0, nc, toff;
+    bool trans;
+};
+
+__device__ inline StepGeom step_geom(i64 rows, int bs, int t, int steps) {
+    if (rows <= 1 + bs) {
+        if (t == 0) return {0, rows, 1, rows - 1, 1, true};
+        return {1, rows - 1, 1, rows - 1, 1, false};
     }
-    __syncthreads();
-    // w_j = a1_j + sum_l A2(l, j) u_l, w_j /= tau, a1_j -= w_j, A2(:, j) -= u w_j
-    const double rt = 1.0 / s_tau;
-    for (i64 j = 1 + tid; j < Cc; j += blockDim.x) {
-        double w = M(0, j);
-        for (int l = 0; l < len; l++) w = fma(M(1 + l, j), s_u[l], w);
-        w *= rt;
-        M(0, j) -= w;
-        for (int l = 0; l < len; l++) M(1 + l, j) = fma(-s_u[l], w, M(1 + l, j));
+    const int K = (steps - 4) / 2;   // passes of the StepCycle loop
+    if (t == 0) return {0, 1 + bs, 1, bs, 1, true};
+    if (t <= 2 * K) {
+        const i64 is = 1 + (i64)((t - 1) / 2) * bs, ie = is + bs;
+        if ((t - 1) % 2 == 0) return {is, bs, is, 2 * (i64)bs, is, false};
+        return {is, 2 * (i64)bs, ie, bs, ie, true};
     }
-    __syncthreads();
+    const i64 is = 1 + (i64)K * bs, ie = is + bs;
+    if (t == 2 * K + 1) return {is, bs, is, rows - is, is, false};
+    if (t == 2 * K + 2) return {is, rows - is, ie, rows - ie, ie, true};
+    return {ie, rows - ie, ie, rows - ie, ie, false};
 }
 
-// The bulge chase: CTA b runs cycles b, b + gridDim.x, ... in order.
+// StepSide (Bidiagonaling.cs:539-551) on M = the view of g (R <= 32 rows,
+// Cc <= 64 columns): the reflector of M's first column
+// (HouseHolder.BuildHouseHolder, HouseHolder.cs:34-58) applied from the left
+// to M's other columns (ApplyHouseHolder, HouseHolder.cs:95-115); tau and the
+// vector go to t, the column's tail is cleared.  Every warp builds the
+// reflector from column 0 (no barrier between build and apply); four
+// threads per column split its dot product, with the column's entries loaded
+// before the reflector is known.  Column 0 is written after the closing
+// barrier, by warp 0.
+__device__ void step_side(const ChaseArgs &a, i64 s, const StepGeom &g, double *t) {
+    __shared__ double s_u[BD2_THREADS / 32][BD2_BLOCK];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    double *p = a.W + (s + g.r0) * a.rs + (s + g.c0) * a.cs;
+    const i64 ers = g.trans ? a.cs : a.rs, ecs = g.trans ? a.rs : a.cs;   // M(r, c) = p[r ers + c ecs]
+    const int R = (int)(g.trans ? g.nc : g.nr), Cc = (int)(g.trans ? g.nr : g.nc);
+    const int len = R - 1;
+    const int j = 1 + (tid >> 2), sub = tid & 3;
+    const bool colv = j < Cc;
+    double v[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        const int l = sub + 4 * i;
+        v[i] = colv && l < len ? p[(1 + l) * ers + j * ecs] : 0.0;
+    }
+    const double a1 = colv ? p[j * ecs] : 0.0;
+    const double x = lane < len ? p[(1 + lane) * ers] : 0.0;
+    double chi = p[0], tau, u = x;
+    double ss = x * x;
+    for (int off = 16; off > 0; off >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, off);
+    const double nrm = sqrt(ss);
+    if (nrm == 0.0) {
+        chi = -chi;
+        tau = 0.5;
+    } else {
+        const double alpha = hypot(chi, nrm);
+        const double rho = -copysign(alpha, chi);
+        const double miu = chi - rho;
+        chi = rho;
+        u = x * (1.0 / miu);
+        const double sc = nrm / fabs(miu);
+        tau = (1.0 + sc * sc) / 2.0;
+    }
+    s_u[warp][lane] = u;
+    __syncwarp();
+    double part = 0.0;
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        const int l = sub + 4 * i;
+        if (l < len) part = fma(v[i], s_u[warp][l], part);
+    }
+    part += __shfl_xor_sync(0xffffffffu, part, 1);
+    part += __shfl_xor_sync(0xffffffffu, part, 2);
+    const double w = (a1 + part) * (1.0 / tau);
+    if (colv) {
+        if (sub == 0) p[j * ecs] = a1 - w;
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            const int l = sub + 4 * i;
+            if (l < len) p[(1 + l) * ers + j * ecs] = fma(-s_u[warp][l], w, v[i]);
+        }
+    }
+    __syncthreads();   // every warp has read column 0
+    if (warp == 0) {
+        if (lane < len) {
+            t[1 + lane] = u;
+            p[(1 + lane) * ers] = 0.0;
+        }
+        if (lane == 0) {
+            p[0] = chi;
+            t[0] = tau;
+        }
+        __syncwarp();
+    }
+}
+
+// The bulge chase: CTA b runs cycles b, b + gridDim.x, ... in order; reflector
+// t of cycle s waits until cycle s - 1 has finished min(t + LAG, all).
 __global__ void __launch_bounds__(BD2_THREADS) k_bd_chase(ChaseArgs a) {
     __shared__ int s_abort;
     const int tid = threadIdx.x;
     for (i64 s = blockIdx.x; s + 1 < a.n; s += gridDim.x) {
-        const int bs = a.bs;
         const i64 rows = a.n - s;
-        const int before = s > 0 ? cycle_steps(a.n, s - 1, bs) : 0;
-        double *tu = a.tu2 + s * a.n + s, *tv = a.tv2 + s * a.n + s;
-        int step = 0;
-        bool abort = false;
-        // one reflector of this cycle on sub(cycle view, r0, nr, c0, nc)
-        auto side = [&](i64 r0, i64 nr, i64 c0, i64 nc, bool trans, double *t) {
-            if (abort) return;
-            if (s > 0) {
-                const int want = step + BD2_LAG < before ? step + BD2_LAG : before;
-                if (tid == 0) {
-                    int ok = 0;
+        const int steps = cycle_steps(a.n, s, a.bs);
+        const int before = s > 0 ? cycle_steps(a.n, s - 1, a.bs) : 0;
+        for (int t = 0; t < steps; t++) {
+            if (tid == 0) {
+                int ok = 1;
+                if (s > 0) {
+                    const int want = t + BD2_LAG < before ? t + BD2_LAG : before;
+                    ok = 0;
                     for (long long it = 0; it < BD2_SPIN; it++) {
                         if (*(volatile int *)&a.prog[s - 1] >= want) { ok = 1; break; }
                         if (*(volatile int *)a.err) break;   // another cycle gave up
                     }
                     __threadfence();
-                    s_abort = !ok;
                     if (!ok) atomicExch(a.err, 1);
                 }
-                __syncthreads();
-                abort = s_abort != 0;
-                __syncthreads();
-                if (abort) return;
+                s_abort = !ok;
             }
-            step_side(a, s + r0, nr, s + c0, nc, trans, t);
-            step++;
+            __syncthreads();   // the wait, and this CTA's previous reflector, are complete
+            if (s_abort) return;
+            const StepGeom g = step_geom(rows, a.bs, t, steps);
+            step_side(a, s, g, (g.trans ? a.tv2 : a.tu2) + s * a.n + s + g.toff);
             if (tid == 0) {
                 __threadfence();
-                atomicExch(&a.prog[s], step);
+                atomicExch(&a.prog[s], t + 1);
             }
-        };
-        const i64 is0 = 1, ie0 = 1 + bs;
-        if (rows <= ie0) {
-            side(0, rows, is0, rows - is0, true, tv + is0);
-            side(is0, rows - is0, is0, rows - is0, false, tu + is0);
-        } else {
-            i64 is = is0, ie = ie0, ie2 = ie0 + bs;
-            side(0, ie, is, ie - is, true, tv + is);
-            while (ie2 < rows) {
-                side(is, ie - is, is, ie2 - is, false, tu + is);
-                side(is, ie2 - is, ie, ie2 - ie, true, tv + ie);
-                is += bs;
-                ie += bs;
-                ie2 += bs;
-            }
-            side(is, ie - is, is, rows - is, false, tu + is);
-            side(is, rows - is, ie, rows - ie, true, tv + ie);
-            side(ie, rows - ie, ie, rows - ie, false, tu + ie);
         }
-        if (abort) return;
     }
 }
 
-// BackCycle of cycle i (Bidiagonaling.cs:518-537): Q <- Q H_k for every
-// reflector k of the cycle, H_k = I - u u^T / tau on columns i + is_k ..
-// i + ie_k of Q (ApplyHouseHolder on Q^T from the left).  A warp per
-// (row of Q, reflector): lane l holds column c0 + l.
-__global__ void k_bd_back(double *Q, i64 rows, i64 rs, i64 cs, const double *t2, i64 n, i64 i, int bs, int nref) {
-    const int lane = threadIdx.x & 31;
-    const i64 wid = (blockIdx.x * (i64)blockDim.x + threadIdx.x) >> 5;
-    if (wid >= rows * nref) return;
-    const i64 r = wid / nref;
-    const int k = (int)(wid % nref);
-    const i64 cyc = n - i;
-    const i64 is = 1 + (i64)k * bs, ie = is + bs < cyc ? is + bs : cyc;
-    const int len = (int)(ie - is);
-    const double *t = t2 + i * n + i + is;
-    const double tau = t[0];
-    if (tau == 0.0) return;
-    const i64 c0 = i + is;
-    const double q = lane < len ? Q[r * rs + (c0 + lane) * cs] : 0.0;
-    const double u = lane == 0 ? 1.0 : (lane < len ? t[lane] : 0.0);
-    double w = lane == 0 ? 0.0 : q * u;
-    for (int off = 16; off > 0; off >>= 1) w += __shfl_xor_sync(0xffffffffu, w, off);
-    w = (__shfl_sync(0xffffffffu, q, 0) + w) * (1.0 / tau);
-    if (lane == 0) Q[r * rs + c0 * cs] = q - w;
-    else if (lane < len) Q[r * rs + (c0 + lane) * cs] = fma(-u, w, q);
+// BackCycle (Bidiagonaling.cs:518-537) of the cycles i0 .. i0 + G - 1 (G =
+// the block width bs): Q <- Q H for every reflector H = I - u u^T / tau of
+// those cycles, on U (TU2's reflectors) and V (TV2's) in one launch.
+// Reflector k of cycle i0 + g acts on columns base_k + g .. + len, base_k =
+// i0 + 1 + bs k.  Running k from the last down and, for each k, g upward
+// keeps DDLA's order wherever two reflectors overlap: (g, k) overlaps only
+// (g', k) and (g', k + 1) with g' < g, which it must follow, and (g', k) and
+// (g', k - 1) with g' > g, which must follow it.  So a row of Q needs only a
+// window of 2 bs - 1 columns per k: a CTA (one warp) keeps the window of
+// its rows in shared memory, writes back the bs columns that no later k
+// touches, shifts and loads the next bs; every element of U and V is read
+// and written once per group of cycles.  P threads per row split each dot
+// product (32 / P rows per CTA); the window pitch 64 + P puts the P threads
+// of the 16 / P rows of a half-warp on distinct banks.
+template <int P>
+__global__ void __launch_bounds__(32) k_bd_back(double *U, i64 m, i64 rsu, i64 csu, double *V, i64 rsv, i64 csv,
+                                                 const double *tu2, const double *tv2, i64 n, int bs, i64 i0,
+                                                 int ublocks) {
+    constexpr int RB = 32 / P, WP = 64 + P;
+    __shared__ double sQ[RB * WP];
+    __shared__ double sU[BD2_BLOCK * BD2_BLOCK];
+    __shared__ double sRt[BD2_BLOCK];
+    __shared__ int sLen[BD2_BLOCK];
+    const int lane = threadIdx.x, r = lane / P, p = lane % P;
+    const bool isu = (int)blockIdx.x < ublocks;
+    const i64 rb = isu ? blockIdx.x : blockIdx.x - ublocks;
+    const i64 rows = isu ? m : n, rs = isu ? rsu : rsv, cs = isu ? csu : csv;
+    const double *T = isu ? tu2 : tv2;
+    const i64 row = rb * RB + r;
+    const bool live = row < rows;
+    double *qrow = (isu ? U : V) + (live ? row : 0) * rs;
+    double *sq = sQ + r * WP;
+    const int G = (int)(n - 1 - i0 < bs ? n - 1 - i0 : bs), WW = 2 * bs - 1;
+    const int kmax = (int)((n - i0 - 2) / bs);
+    i64 base = i0 + 1 + (i64)bs * kmax;
+    for (int j = p; j < WW; j += P) sq[j] = live && base + j < n ? qrow[(base + j) * cs] : 0.0;
+    for (int k = kmax; k >= 0; k--) {
+        base = i0 + 1 + (i64)bs * k;
+        for (int e = lane; e < G * bs; e += 32) {
+            const int g = e / bs, l = e % bs;
+            const i64 i = i0 + g;
+            const bool has = k < (int)((n - i - 2) / bs + 1);
+            const i64 is = 1 + (i64)bs * k, ie = is + bs < n - i ? is + bs : n - i;
+            if (has && l < ie - is) {
+                const double *t = T + i * n + i + is;
+                sU[g * BD2_BLOCK + l] = t[l];
+                if (l == 0) sRt[g] = 1.0 / t[0];
+            }
+            if (l == 0) sLen[g] = has ? (int)(ie - is) : 0;
+        }
+        __syncwarp();
+        for (int g = 0; g < G; g++) {
+            const int len = sLen[g];
+            if (len == 0) continue;
+            double *q = sq + g;
+            const double *u = sU + g * BD2_BLOCK;
+            const double q0 = q[0];
+            double qv[32 / P], part0 = 0.0, part1 = 0.0;
+#pragma unroll
+            for (int i = 0; i < 32 / P; i++) {
+                const int l = 1 + p + P * i;
+                qv[i] = l < len ? q[l] : 0.0;
+                const double ul = l < len ? u[l] : 0.0;
+                if (i & 1) part1 = fma(qv[i], ul, part1);
+                else part0 = fma(qv[i], ul, part0);
+            }
+            double part = part0 + part1;
+#pragma unroll
+            for (int o = 1; o < P; o <<= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+            const double w = (q0 + part) * sRt[g];
+            if (p == 0) q[0] = q0 - w;
+#pragma unroll
+            for (int i = 0; i < 32 / P; i++) {
+                const int l = 1 + p + P * i;
+                if (l < len) q[l] = fma(-u[l], w, qv[i]);
+            }
+            __syncwarp();
+        }
+        // columns base + bs - 1 .. base + WW are final for this group
+        for (int j = (k == 0 ? 0 : bs - 1) + p; j < WW; j += P)
+            if (live && base + j < n) qrow[(base + j) * cs] = sq[j];
+        if (k == 0) break;
+        __syncwarp();
+        for (int j = p; j < bs - 1; j += P) sq[bs + j] = sq[j];
+        __syncwarp();
+        for (int j = p; j < bs; j += P) sq[j] = live && base - bs + j < n ? qrow[(base - bs + j) * cs] : 0.0;
+        __syncwarp();
+    }
 }
 
 }  // namespace
@@ -232,16 +325,22 @@ int bidiag2s(ddla_handle h, i64 m, i64 n, View<double> A, View<double> U, View<d
     const i64 bs = n < BD2_BLOCK ? n : BD2_BLOCK;
     const i64 tvc = n - bs;
     // workspace: TU (bs x n), TV (bs x tvc), TU2, TV2 (n x n), progress, error
+    // U and V are formed from block reflectors of up to FB columns
+    const i64 FB = std::max<i64>(bs, std::min<i64>(256, tune_get("bidiag2s.form_nb", 128)));
     const size_t nd = (size_t)bs * n + (size_t)bs * (tvc > 0 ? tvc : 1) + 2 * (size_t)n * n;
+    const size_t nf = (size_t)FB * FB + 2 * (size_t)n + (size_t)FB * m;
     void *ws;
-    DDLA_TRY(workspace(h, WS_BD2, sizeof(double) * nd + sizeof(int) * ((size_t)n + 8), &ws));
+    DDLA_TRY(workspace(h, WS_BD2, sizeof(double) * (nd + nf) + sizeof(int) * ((size_t)n + 8), &ws));
     double *TU = (double *)ws, *TV = TU + (size_t)bs * n, *TU2 = TV + (size_t)bs * (tvc > 0 ? tvc : 1),
            *TV2 = TU2 + (size_t)n * n;
-    int *prog = (int *)(TV2 + (size_t)n * n), *err = prog + n;
+    double *Sf = TV2 + (size_t)n * n, *tauf = Sf + (size_t)FB * FB, *Wf = tauf + 2 * (size_t)n;
+    int *prog = (int *)(Wf + (size_t)FB * m), *err = prog + n;
     DDLA_CUDA(cudaMemsetAsync(TU, 0, sizeof(double) * nd, s));
     DDLA_CUDA(cudaMemsetAsync(prog, 0, sizeof(int) * ((size_t)n + 8), s));
     auto grid_of = [](i64 tot) { return (unsigned)std::max<i64>(1, std::min<i64>((tot + 255) / 256, 8192)); };
     // ---- stage 1: Ge2Bd
+    {
+    Timed tm(s, TC_BD_BAND, 4.0 * m * n * n - 4.0 * n * n * n / 3.0 + 4.0 * m * m * n - 2.0 * m * n * n, 0.0);
     for (i64 i0 = 0; i0 < n;) {
         const i64 b = n - i0 < BD2_BLOCK ? n - i0 : BD2_BLOCK;
         View<double> AB1 = A.sub(i0, m - i0, i0, b);
@@ -250,7 +349,8 @@ int bidiag2s(ddla_handle h, i64 m, i64 n, View<double> A, View<double> U, View<d
         const i64 c22 = n - i0 - b;
         if (c22 > 0) {
             DDLA_TRY(ormqr(h, true, m - i0, b, View<const double>{AB1.p, AB1.rows, AB1.cols, AB1.rs, AB1.cs},
-                           View<const double>{TUb.p, b, b, TUb.rs, TUb.cs}, b, A.sub(i0, m - i0, i0 + b, c22), prec));
+                           View<const double>{TUb.p, b, b, TUb.rs, TUb.cs}, b, A.sub(i0, m - i0, i0 + b, c22), prec,
+                           BD2_BLOCK));
             // the block row right of it (the ragged last one takes all the remaining columns' width)
             const i64 b2 = c22 < BD2_BLOCK ? c22 : b;
             View<double> R = A.sub(i0, b2, i0 + b, c22).t();          // c22 x b2
@@ -258,25 +358,39 @@ int bidiag2s(ddla_handle h, i64 m, i64 n, View<double> A, View<double> U, View<d
             View<double> TVb{TV + i0, b2, b2, tvc, 1};
             DDLA_TRY(geqrf(h, c22, b2, R, TVb, b2, prec));
             DDLA_TRY(ormqr(h, true, c22, b2, View<const double>{R.p, R.rows, R.cols, R.rs, R.cs},
-                           View<const double>{TVb.p, b2, b2, TVb.rs, TVb.cs}, b2, below, prec));
+                           View<const double>{TVb.p, b2, b2, TVb.rs, TVb.cs}, b2, below, prec, BD2_BLOCK));
         }
         i0 += b;
     }
-    // U and V from the block reflectors (ApplyQlnfc); A keeps the band
+    // U and V from the block reflectors (ApplyQlnfc); A keeps the band.  The
+    // blocks of bs reflectors are joined into blocks of FB (their factor is
+    // the same triu(U^T U) with the taus on the diagonal) and applied last
+    // first to the identity, each only to the columns it can change.
+    auto form = [&](View<const double> R, i64 rows, i64 k, const double *T, i64 ldt, View<double> Q) -> int {
+        k_taus<<<grid_of(k), 256, 0, s>>>(T, ldt, k, (int)bs, tauf);
+        DDLA_LAUNCHED();
+        for (i64 j0 = ((k - 1) / FB) * FB; j0 >= 0; j0 -= FB) {
+            const i64 b = k - j0 < FB ? k - j0 : FB;
+            View<const double> Ub = R.sub(j0, rows - j0, j0, b);
+            DDLA_TRY(qr_tfactor(h, Ub, b, tauf + j0, View<double>{Sf, b, b, FB, 1}));
+            DDLA_TRY(qr_apply_block(h, false, Ub, b, View<const double>{Sf, b, b, FB, 1},
+                                    Q.sub(j0, rows - j0, j0, rows - j0), Wf, prec));
+        }
+        return 0;
+    };
     k_eye2<<<grid_of(m * m), 256, 0, s>>>(U.p, m, U.rs, U.cs);
     DDLA_LAUNCHED();
-    DDLA_TRY(ormqr(h, false, m, n, View<const double>{A.p, m, n, A.rs, A.cs}, View<const double>{TU, bs, n, n, 1}, bs,
-                   U, prec));
+    DDLA_TRY(form(View<const double>{A.p, m, n, A.rs, A.cs}, m, n, TU, n, U));
     k_zero_lower<<<grid_of(m * n), 256, 0, s>>>(A.p, A.rs, A.cs, m, n);
     DDLA_LAUNCHED();
     k_eye2<<<grid_of(n * n), 256, 0, s>>>(V.p, n, V.rs, V.cs);
     DDLA_LAUNCHED();
     if (tvc > 0) {
         View<double> Al = A.sub(0, tvc, bs, tvc).t();
-        DDLA_TRY(ormqr(h, false, tvc, tvc, View<const double>{Al.p, tvc, tvc, Al.rs, Al.cs},
-                       View<const double>{TV, bs, tvc, tvc, 1}, bs, V.sub(bs, tvc, bs, tvc), prec));
+        DDLA_TRY(form(View<const double>{Al.p, tvc, tvc, Al.rs, Al.cs}, tvc, tvc, TV, tvc, V.sub(bs, tvc, bs, tvc)));
         k_zero_lower<<<grid_of(tvc * tvc), 256, 0, s>>>(Al.p, Al.rs, Al.cs, tvc, tvc);
         DDLA_LAUNCHED();
+    }
     }
     // ---- stage 2: Bd2Bi
     if (n > 1) {
@@ -286,14 +400,26 @@ int bidiag2s(ddla_handle h, i64 m, i64 n, View<double> A, View<double> U, View<d
         const i64 cyc = n - 1;
         const int grid = (int)std::max<i64>(1, std::min<i64>(cyc, (i64)h->sm_count * std::max(per_sm, 1)));
         void *args[] = {&ca};
-        DDLA_CUDA(cudaLaunchCooperativeKernel((const void *)k_bd_chase, dim3(grid), dim3(BD2_THREADS), args, 0, s));
-        DDLA_LAUNCHED();
-        for (i64 i = 0; i + 1 < n; i++) {
-            const int nref = (int)((n - i - 2) / bs + 1);
-            const i64 wv = n * nref, wu = m * nref;
-            k_bd_back<<<(unsigned)((wv * 32 + 255) / 256), 256, 0, s>>>(V.p, n, V.rs, V.cs, TV2, n, i, (int)bs, nref);
+        {
+            Timed tm(s, TC_BD_CHASE, 0.0, 0.0);
+            DDLA_CUDA(cudaLaunchCooperativeKernel((const void *)k_bd_chase, dim3(grid), dim3(BD2_THREADS), args, 0,
+                                                  s));
             DDLA_LAUNCHED();
-            k_bd_back<<<(unsigned)((wu * 32 + 255) / 256), 256, 0, s>>>(U.p, m, U.rs, U.cs, TU2, n, i, (int)bs, nref);
+        }
+        // every group of bs cycles reads and writes columns i0 + 1 .. n of U and V once
+        Timed tm(s, TC_BD_BACK, 2.0 * n * n * (double)(m + n), 8.0 * n * n * (double)(m + n) / bs);
+        const int P = (int)tune_get("bidiag2s.back_p", 4), rb = 32 / (P == 2 || P == 8 ? P : 4);
+        const int ublocks = (int)((m + rb - 1) / rb), vblocks = (int)((n + rb - 1) / rb);
+        for (i64 i0 = 0; i0 + 1 < n; i0 += bs) {
+            if (P == 2)
+                k_bd_back<2><<<ublocks + vblocks, 32, 0, s>>>(U.p, m, U.rs, U.cs, V.p, V.rs, V.cs, TU2, TV2, n,
+                                                             (int)bs, i0, ublocks);
+            else if (P == 8)
+                k_bd_back<8><<<ublocks + vblocks, 32, 0, s>>>(U.p, m, U.rs, U.cs, V.p, V.rs, V.cs, TU2, TV2, n,
+                                                             (int)bs, i0, ublocks);
+            else
+                k_bd_back<4><<<ublocks + vblocks, 32, 0, s>>>(U.p, m, U.rs, U.cs, V.p, V.rs, V.cs, TU2, TV2, n,
+                                                             (int)bs, i0, ublocks);
             DDLA_LAUNCHED();
         }
     }

@@ -204,12 +204,20 @@ int ldlts(ddla_handle h, int uplo, i64 n, i64 nrhs, View<const T> A, View<T> B);
 // split-precision tensor-core GEMM; wcap caps the panel width (0 = automatic).
 int geqrf(ddla_handle h, i64 m, i64 n, View<double> A, View<double> T, i64 tb, int prec = DDLA_PREC_FP64,
           int wcap = 0);
+// oz_min_b: smallest block that takes the split-precision products (0 = 64).
 int ormqr(ddla_handle h, bool trans, i64 m, i64 n, View<const double> A, View<const double> T, i64 tb,
-          View<double> B, int prec = DDLA_PREC_FP64);
+          View<double> B, int prec = DDLA_PREC_FP64, int oz_min_b = 0);
 int geqrs(ddla_handle h, i64 m, i64 n, View<const double> A, View<const double> T, i64 tb, View<const double> B,
           View<double> Y, View<double> X);
 int orgqr(ddla_handle h, i64 m, i64 n, View<const double> A, View<const double> T, i64 tb, View<double> Q,
           int prec = DDLA_PREC_FP64);
+// One block reflector of those factors (qr.cu): S (b x b) = triu(U^T U) with
+// tau on the diagonal for the unit-lower m x b U stored below Ub's diagonal,
+// and C = (I - U S^-1 U^T)^T C (trans) or (I - U S^-1 U^T) C with W a
+// b x C.cols scratch.
+int qr_tfactor(ddla_handle h, View<const double> Ub, i64 b, const double *tau, View<double> S);
+int qr_apply_block(ddla_handle h, bool trans, View<const double> Ub, i64 b, View<const double> S, View<double> Cm,
+                   double *W, int prec = DDLA_PREC_FP64, int oz_min_b = 0);
 // Tridiagonaling.Tridiag on device data (tridiag.cu): A (lower triangle read)
 // becomes Q, d (n) and e (n - 1) the tridiagonal, T (tb rows) the factors.
 int sytrd(ddla_handle h, i64 n, View<double> A, View<double> T, i64 tb, double *d, double *e,

@@ -333,8 +333,11 @@ int qr_panel(ddla_handle h, View<double> P, int w, double *tau, double *S, i64 l
     return 0;
 }
 
+}  // namespace
+
 // S = upper(U^T U) with tau on the diagonal, U = the m x b unit-lower
-// trapezoid stored below the diagonal of Ub.
+// trapezoid stored below the diagonal of Ub.  The factor of several
+// consecutive blocks is the same formula over their joined columns.
 int qr_tfactor(ddla_handle h, View<const double> Ub, i64 b, const double *tau, View<double> S) {
     const i64 m = Ub.rows;
     Timed tm(h->stream, TC_QR_T, (double)m * b * b, 8.0 * (double)m * b);
@@ -349,12 +352,12 @@ int qr_tfactor(ddla_handle h, View<const double> Ub, i64 b, const double *tau, V
 // C = (I - U S^-1 U^T)^T C (trans) or (I - U S^-1 U^T) C, U m x b unit-lower
 // trapezoid in Ub, W a b x C.cols scratch.
 int qr_apply_block(ddla_handle h, bool trans, View<const double> Ub, i64 b, View<const double> S, View<double> Cm,
-                   double *W, int prec = DDLA_PREC_FP64) {
+                   double *W, int prec, int oz_min_b) {
     const i64 m = Ub.rows, nc = Cm.cols;
     if (nc <= 0 || m <= 0) return 0;
     View<const double> U{Ub.p, m, b, Ub.rs, Ub.cs};
     View<double> Wv{W, b, nc, nc, 1};
-    if (prec == DDLA_PREC_OZAKI && b >= 64 && m >= 256 && nc >= 64) {
+    if (prec == DDLA_PREC_OZAKI && b >= (oz_min_b > 0 ? oz_min_b : 64) && m >= 256 && nc >= 64) {
         // split-precision tensor-core products on an explicit copy of U
         void *ud;
         DDLA_TRY(workspace(h, WS_QRU, sizeof(double) * (size_t)(m * b), &ud));
@@ -388,8 +391,6 @@ int qr_apply_block(ddla_handle h, bool trans, View<const double> Ub, i64 b, View
     return gemm_f64_struct_h(h, m, nc, b, -1.0, U, OP_TRI | OP_LOWER | OP_UNIT, View<const double>{W, b, nc, nc, 1},
                              OP_DENSE, 1.0, Cm);
 }
-
-}  // namespace
 
 // QR of the m x n A in place; T (tb rows x n) receives the block factors.
 // Two levels: panels of w <= 32 columns (one cluster kernel each, which also
@@ -437,7 +438,7 @@ int geqrf(ddla_handle h, i64 m, i64 n, View<double> A, View<double> T, i64 tb, i
 
 // B (m x nrhs) = Q^T B (trans) or Q B with the factors of geqrf.
 int ormqr(ddla_handle h, bool trans, i64 m, i64 n, View<const double> A, View<const double> T, i64 tb,
-          View<double> B, int prec) {
+          View<double> B, int prec, int oz_min_b) {
     const i64 k = m < n ? m : n, nrhs = B.cols;
     if (k == 0 || nrhs == 0) return 0;
     void *ws;
@@ -450,7 +451,7 @@ int ormqr(ddla_handle h, bool trans, i64 m, i64 n, View<const double> A, View<co
         View<const double> Ub{A.p + j0 * A.rs + j0 * A.cs, m - j0, b, A.rs, A.cs};
         View<const double> S{T.p + j0 * T.cs, b, b, T.rs, T.cs};
         View<double> Cm{B.p + j0 * B.rs, m - j0, nrhs, B.rs, B.cs};
-        DDLA_TRY(qr_apply_block(h, trans, Ub, b, S, Cm, W, prec));
+        DDLA_TRY(qr_apply_block(h, trans, Ub, b, S, Cm, W, prec, oz_min_b));
     }
     return 0;
 }

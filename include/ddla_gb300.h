@@ -134,7 +134,9 @@ int ddla_measure_peaks(double *fp64_tflops, double *fp32_tflops);
 /* Per-launch device timing of kernel classes (0 trailing-matrix GEMM update,
  * 1 LU panel, 2 TRSM, 3 row interchanges, 4 refinement FP64 residual,
  * 5 batched, 6 einsum GEMM, 7 QR T factor, 8 refinement correction solves with
- * the low-precision factors).  ddla_timing_enable(1) clears the records and brackets every later
+ * the low-precision factors, 9 two-stage bidiagonal: band reduction with U and
+ * V of stage 1, 10 its band chase, 11 its back-transformation of U and V).
+ * ddla_timing_enable(1) clears the records and brackets every later
  * launch of those classes with CUDA events on its stream; ddla_timing_read
  * sums one class: total device ms, launches, algorithmic flops and bytes. */
 int ddla_timing_enable(int on);

@@ -56,7 +56,8 @@ def test_bidiag2s_leaves_input_and_layouts(ddla, orc):
 
 def test_bidiag2s_device_sizes_and_ozaki(ddla, orc):
     """Device entry point at a larger size: properties for FP64 and for the
-    split-precision block-reflector products, and the oracle's d and e."""
+    split-precision block-reflector products; the oracle's d and e (FP64),
+    LAPACK's singular values (split precision)."""
     torch = pytest.importorskip("torch")
     from ddla_gb300.device import Handle
     m, n = 1500, 1100
@@ -73,9 +74,17 @@ def test_bidiag2s_device_sizes_and_ozaki(ddla, orc):
             h.bidiag_twostage(dA, dd, de, dU, dV, precision=prec)
             h.sync()
             U, V, d, e = dU.cpu().numpy(), dV.cpu().numpy(), dd.cpu().numpy(), de.cpu().numpy()
-            assert np.max(np.abs(U.T @ A0 @ V - _bd(m, n, d, e))) <= 1e-13 * m
-            assert np.max(np.abs(U.T @ U - np.eye(m))) <= 1e-13
-            assert np.max(np.abs(V.T @ V - np.eye(n))) <= 1e-13
-            assert np.max(np.abs(d - do)) <= 1e-9 and np.max(np.abs(e - eo)) <= 1e-9
+            # split-precision products carry errors near 1e-14 relative per product
+            bar = 1e-13 if prec == 0 else 1e-11
+            assert np.max(np.abs(U.T @ A0 @ V - _bd(m, n, d, e))) <= bar * (m if prec == 0 else 1)
+            assert np.max(np.abs(U.T @ U - np.eye(m))) <= bar
+            assert np.max(np.abs(V.T @ V - np.eye(n))) <= bar
+            if prec == 0:
+                assert np.max(np.abs(d - do)) <= 1e-9 and np.max(np.abs(e - eo)) <= 1e-9
+            else:
+                # the bidiagonal entries move with the products' rounding through
+                # the chase; the singular values do not
+                sv = np.sort(np.linalg.svd(_bd(n, n, d, e), compute_uv=False))
+                assert np.max(np.abs(sv - np.sort(np.linalg.svd(A0, compute_uv=False)))) <= 1e-11 * sv.max()
     finally:
         h.close()
