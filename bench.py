@@ -33,6 +33,7 @@ is the headline LU solve):
   batched   20,000 LU / Cholesky solves, n ~ U{8..256}  (--precision fp32 | fp64)
   einsum-a  'bik,bkj->bij', b = 512, 256^3, U[-1,1]  (--precision fp64 | ozaki)
   einsum-b  'abcd,cdef->abef', all lengths 64        (--precision fp64 | ozaki)
+  bidiag2s  two-stage bidiagonal reduction + U, V, 4096^2 U[-1,1]  (--precision fp64 | ozaki)
 """
 import argparse
 import ctypes as C
@@ -353,6 +354,30 @@ def secondary(args):
             h.sync()
             B = torch.diag(dw) + torch.diag(ew, 1)
             return float((Uw.T @ A0 @ Vw - B).abs().max() / A0.abs().max())
+    elif wl == "bidiag2s":
+        n = args.n if args.n != N_DEFAULT else 4096
+        A0 = U(n, n)
+        Aw = torch.empty_like(A0)
+        Uw = torch.empty_like(A0)
+        Vw = torch.empty_like(A0)
+        dw = torch.zeros(n, dtype=torch.float64, device="cuda")
+        ew = torch.zeros(n - 1, dtype=torch.float64, device="cuda")
+        bprec = D.PREC_OZAKI if prec == D.PREC_OZAKI else 0
+        # band reduction 8/3 n^3, U and V 4/3 n^3 each, back-transformation of
+        # U and V by the chase's reflectors 2 n^2 (m + n) = 4 n^3 (the chase
+        # itself is O(n^2) and not credited)
+        flops = 8.0 * n ** 3 / 3.0 + 8.0 * n ** 3 / 3.0 + 4.0 * n ** 3
+        desc = f"two-stage bidiagonal reduction (band 32, bulge chase) + U, V, {n}x{n} FP64 U[-1,1], {pname}"
+
+        def step():
+            Aw.copy_(A0)
+            h.bidiag_twostage(Aw, dw, ew, Uw, Vw, precision=bprec)
+
+        def check_err():
+            step()
+            h.sync()
+            B = torch.diag(dw) + torch.diag(ew, 1)
+            return float((Uw.T @ A0 @ Vw - B).abs().max() / A0.abs().max())
     elif wl == "einsum-chain":
         n = args.n if args.n != N_DEFAULT else 4096
         expr = "ab,bc,cd,de->ae"
@@ -516,14 +541,15 @@ def secondary(args):
     ms = statistics.median(times)
     value = flops / (ms * 1e-3) / 1e9
     classes = None
-    if wl in ("qr", "tridiag", "bidiag"):
+    if wl in ("qr", "tridiag", "bidiag", "bidiag2s"):
         # one more step with per-class CUDA-event brackets (outside the timed steps)
         L.ddla_timing_enable(1)
         step()
         torch.cuda.synchronize()
         classes = {}
         names = {1: "qr_panel", 7: "qr_t_factor", 0: "block_reflector_gemm", 2: "trsm"} if wl == "qr" else \
-            {1: "reduction", 0: "form_q"}
+            {9: "band_reduction_and_uv", 10: "bulge_chase", 11: "back_transformation",
+             0: "block_reflector_gemm"} if wl == "bidiag2s" else {1: "reduction", 0: "form_q"}
         for cls, name in names.items():
             t_ms, cnt, fl, by = C.c_double(), C.c_int64(), C.c_double(), C.c_double()
             L.ddla_timing_read(cls, C.byref(t_ms), C.byref(cnt), C.byref(fl), C.byref(by))
@@ -640,7 +666,7 @@ def main():
                     help="library tuning key (ddla_tune_set) applied before the run; repeatable")
     ap.add_argument("--workload", default="lu", choices=["lu", "gemm", "chol", "batched", "einsum-a", "einsum-b",
                                                          "symm", "trmm", "syr2k", "qr", "einsum-chain",
-                                                         "tridiag", "bidiag"])
+                                                         "tridiag", "bidiag", "bidiag2s"])
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the oracle (CPU baseline and its checks)")
     ap.add_argument("--no-e2e", action="store_true")

@@ -23,7 +23,8 @@
 // tests/test_bd_chase_schedule.py enumerates the regions and checks it).  The
 // reflectors are stored in TU2 / TV2 (row i for cycle i) and applied to U and
 // V afterwards (BackCycle, :518-537), 32 cycles per launch with the rows of U
-// and V streamed through shared memory once per launch (k_bd_back).
+// and V streamed through shared memory once per launch and the reflectors
+// applied four at a time in compact WY form (k_bd_back).
 //
 // Every wait is bounded: on timeout the kernel sets an error word and
 // returns; the host reports DDLA_ERR_TIMEOUT.
@@ -230,84 +231,145 @@ __global__ void __launch_bounds__(BD2_THREADS) k_bd_chase(ChaseArgs a) {
 // keeps DDLA's order wherever two reflectors overlap: (g, k) overlaps only
 // (g', k) and (g', k + 1) with g' < g, which it must follow, and (g', k) and
 // (g', k - 1) with g' > g, which must follow it.  So a row of Q needs only a
-// window of 2 bs - 1 columns per k: a CTA (one warp) keeps the window of
-// its rows in shared memory, writes back the bs columns that no later k
-// touches, shifts and loads the next bs; every element of U and V is read
-// and written once per group of cycles.  P threads per row split each dot
-// product (32 / P rows per CTA); the window pitch 64 + P puts the P threads
-// of the 16 / P rows of a half-warp on distinct banks.
-template <int P>
+// window of 2 bs - 1 columns per k: a CTA (one warp, 8 rows) keeps the
+// window of its rows in shared memory, writes back the bs columns that no
+// later k touches, shifts and loads the next bs; every element of U and V is
+// read and written once per group of cycles.
+//
+// The reflectors of one k are applied four at a time in compact WY form: for
+// a row q and reflectors a = 0..3 (in order), d_a = q . u_a, w S = d with S
+// upper triangular, S_aa = tau_a, S_ab = u_a . u_b (a < b), and q -= sum_a
+// w_a u_a -- the same product as applying them one by one.  Z = S^-1 comes
+// from k_bd_back_prep.  Four threads per row: thread p sums the terms
+// l = p mod 4 of the four dot products and updates the columns = p mod 4.
+constexpr int BK_RB = 8;    // rows of Q per CTA
+constexpr int BK_WP = 68;   // window pitch (63 columns used): 8 r + 2 p distinct banks
+constexpr int BK_Q = 4;     // reflectors per WY block
+
+__host__ __device__ inline int refl_len(i64 n, i64 i, int bs, int k) {
+    // length of reflector k of cycle i, 0 if the cycle has no k-th reflector
+    const i64 rem = n - i - 1 - (i64)bs * k;
+    return rem <= 0 ? 0 : (int)(rem < bs ? rem : bs);
+}
+
+// Z = S^-1 of every WY block: grid (k, U/V), thread j = block j of the k.
+__global__ void k_bd_back_prep(const double *tu2, const double *tv2, i64 n, int bs, i64 i0, int G, int kcount,
+                               double *Zq) {
+    const int k = blockIdx.x, which = blockIdx.y, j = threadIdx.x;
+    if (j >= BD2_BLOCK / BK_Q) return;
+    const double *T = which == 0 ? tu2 : tv2;
+    int len[BK_Q];
+    const double *t[BK_Q];
+    double S[BK_Q][BK_Q], Z[BK_Q][BK_Q];
+    for (int a = 0; a < BK_Q; a++) {
+        const int g = BK_Q * j + a;
+        const i64 i = i0 + g;
+        len[a] = g < G ? refl_len(n, i, bs, k) : 0;
+        t[a] = T + i * n + i + 1 + (i64)bs * k;
+    }
+    for (int a = 0; a < BK_Q; a++)
+        for (int b = 0; b < BK_Q; b++) {
+            double v = 0.0;
+            if (a == b) v = len[a] ? t[a][0] : 1.0;
+            else if (a < b && len[a] && len[b])
+                for (int c = b; c < a + len[a] && c - b < len[b]; c++)
+                    v = fma(c == a ? 1.0 : t[a][c - a], c == b ? 1.0 : t[b][c - b], v);
+            S[a][b] = v;
+            Z[a][b] = 0.0;
+        }
+    for (int c = 0; c < BK_Q; c++) {
+        Z[c][c] = 1.0 / S[c][c];
+        for (int r = c - 1; r >= 0; r--) {
+            double v = 0.0;
+            for (int l = r + 1; l <= c; l++) v = fma(S[r][l], Z[l][c], v);
+            Z[r][c] = -v / S[r][r];
+        }
+    }
+    double *out = Zq + (((i64)which * kcount + k) * (BD2_BLOCK / BK_Q) + j) * BK_Q * BK_Q;
+    for (int a = 0; a < BK_Q; a++)
+        for (int b = 0; b < BK_Q; b++) out[a * BK_Q + b] = Z[a][b];
+}
+
 __global__ void __launch_bounds__(32) k_bd_back(double *U, i64 m, i64 rsu, i64 csu, double *V, i64 rsv, i64 csv,
-                                                 const double *tu2, const double *tv2, i64 n, int bs, i64 i0,
-                                                 int ublocks) {
-    constexpr int RB = 32 / P, WP = 64 + P;
-    __shared__ double sQ[RB * WP];
+                                                 const double *tu2, const double *tv2, const double *Zq, i64 n,
+                                                 int bs, i64 i0, int ublocks) {
+    __shared__ double sQ[BK_RB * BK_WP];
     __shared__ double sU[BD2_BLOCK * BD2_BLOCK];
-    __shared__ double sRt[BD2_BLOCK];
-    __shared__ int sLen[BD2_BLOCK];
-    const int lane = threadIdx.x, r = lane / P, p = lane % P;
+    __shared__ double sZ[BD2_BLOCK * BK_Q];
+    const int lane = threadIdx.x, r = lane >> 2, p = lane & 3;
     const bool isu = (int)blockIdx.x < ublocks;
     const i64 rb = isu ? blockIdx.x : blockIdx.x - ublocks;
     const i64 rows = isu ? m : n, rs = isu ? rsu : rsv, cs = isu ? csu : csv;
     const double *T = isu ? tu2 : tv2;
-    const i64 row = rb * RB + r;
+    const i64 row = rb * BK_RB + r;
     const bool live = row < rows;
     double *qrow = (isu ? U : V) + (live ? row : 0) * rs;
-    double *sq = sQ + r * WP;
+    double *sq = sQ + r * BK_WP;
     const int G = (int)(n - 1 - i0 < bs ? n - 1 - i0 : bs), WW = 2 * bs - 1;
-    const int kmax = (int)((n - i0 - 2) / bs);
+    const int kmax = (int)((n - i0 - 2) / bs), kcount = kmax + 1;
     i64 base = i0 + 1 + (i64)bs * kmax;
-    for (int j = p; j < WW; j += P) sq[j] = live && base + j < n ? qrow[(base + j) * cs] : 0.0;
+    for (int j = p; j < BK_WP; j += 4) sq[j] = j < WW && live && base + j < n ? qrow[(base + j) * cs] : 0.0;
     for (int k = kmax; k >= 0; k--) {
         base = i0 + 1 + (i64)bs * k;
-        for (int e = lane; e < G * bs; e += 32) {
-            const int g = e / bs, l = e % bs;
-            const i64 i = i0 + g;
-            const bool has = k < (int)((n - i - 2) / bs + 1);
-            const i64 is = 1 + (i64)bs * k, ie = is + bs < n - i ? is + bs : n - i;
-            if (has && l < ie - is) {
-                const double *t = T + i * n + i + is;
-                sU[g * BD2_BLOCK + l] = t[l];
-                if (l == 0) sRt[g] = 1.0 / t[0];
-            }
-            if (l == 0) sLen[g] = has ? (int)(ie - is) : 0;
+        // the reflectors of this k, u(0) = 1, zero past their length
+        int gk = 0;
+        for (int e = lane; e < BD2_BLOCK * BD2_BLOCK; e += 32) {
+            const int g = e >> 5, l = e & 31;
+            const int len = g < G ? refl_len(n, i0 + g, bs, k) : 0;
+            const double *t = T + (i0 + g) * n + i0 + g + 1 + (i64)bs * k;
+            sU[e] = l < len ? (l == 0 ? 1.0 : t[l]) : 0.0;
+            if (len) gk = g + 1;
         }
+        for (int o = 16; o > 0; o >>= 1) gk = max(gk, __shfl_xor_sync(0xffffffffu, gk, o));
+        const double *zk = Zq + ((isu ? 0 : 1) * (i64)kcount + k) * BD2_BLOCK * BK_Q;
+        for (int e = lane; e < BD2_BLOCK * BK_Q; e += 32) sZ[e] = zk[e];
         __syncwarp();
-        for (int g = 0; g < G; g++) {
-            const int len = sLen[g];
-            if (len == 0) continue;
-            double *q = sq + g;
-            const double *u = sU + g * BD2_BLOCK;
-            const double q0 = q[0];
-            double qv[32 / P], part0 = 0.0, part1 = 0.0;
+        for (int g0 = 0; g0 < gk; g0 += BK_Q) {
+            const double *u = sU + g0 * BD2_BLOCK;
+            double d[BK_Q] = {0.0, 0.0, 0.0, 0.0};
 #pragma unroll
-            for (int i = 0; i < 32 / P; i++) {
-                const int l = 1 + p + P * i;
-                qv[i] = l < len ? q[l] : 0.0;
-                const double ul = l < len ? u[l] : 0.0;
-                if (i & 1) part1 = fma(qv[i], ul, part1);
-                else part0 = fma(qv[i], ul, part0);
+            for (int i = 0; i < 8; i++) {
+                const int l = p + 4 * i;
+#pragma unroll
+                for (int a = 0; a < BK_Q; a++) d[a] = fma(sq[g0 + a + l], u[a * BD2_BLOCK + l], d[a]);
             }
-            double part = part0 + part1;
 #pragma unroll
-            for (int o = 1; o < P; o <<= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-            const double w = (q0 + part) * sRt[g];
-            if (p == 0) q[0] = q0 - w;
+            for (int a = 0; a < BK_Q; a++) {
+                d[a] += __shfl_xor_sync(0xffffffffu, d[a], 1);
+                d[a] += __shfl_xor_sync(0xffffffffu, d[a], 2);
+            }
+            const double *z = sZ + (g0 / BK_Q) * BK_Q * BK_Q;
+            double w[BK_Q];
 #pragma unroll
-            for (int i = 0; i < 32 / P; i++) {
-                const int l = 1 + p + P * i;
-                if (l < len) q[l] = fma(-u[l], w, qv[i]);
+            for (int a = 0; a < BK_Q; a++) {
+                w[a] = 0.0;
+#pragma unroll
+                for (int b = 0; b <= a; b++) w[a] = fma(d[b], z[b * BK_Q + a], w[a]);
+            }
+            // columns g0 + t, t = p mod 4, t < 32 + BK_Q - 1
+#pragma unroll
+            for (int s2 = 0; s2 < 9; s2++) {
+                const int t = p + 4 * s2;
+                if (t < BD2_BLOCK + BK_Q - 1) {
+                    double acc = sq[g0 + t];
+#pragma unroll
+                    for (int a = 0; a < BK_Q; a++) {
+                        const int l = t - a;
+                        if (l >= 0 && l < BD2_BLOCK) acc = fma(-w[a], u[a * BD2_BLOCK + l], acc);
+                    }
+                    sq[g0 + t] = acc;
+                }
             }
             __syncwarp();
         }
         // columns base + bs - 1 .. base + WW are final for this group
-        for (int j = (k == 0 ? 0 : bs - 1) + p; j < WW; j += P)
+        for (int j = (k == 0 ? 0 : bs - 1) + p; j < WW; j += 4)
             if (live && base + j < n) qrow[(base + j) * cs] = sq[j];
         if (k == 0) break;
         __syncwarp();
-        for (int j = p; j < bs - 1; j += P) sq[bs + j] = sq[j];
+        for (int j = p; j < bs - 1; j += 4) sq[bs + j] = sq[j];
         __syncwarp();
-        for (int j = p; j < bs; j += P) sq[j] = live && base - bs + j < n ? qrow[(base - bs + j) * cs] : 0.0;
+        for (int j = p; j < bs; j += 4) sq[j] = live && base - bs + j < n ? qrow[(base - bs + j) * cs] : 0.0;
         __syncwarp();
     }
 }
@@ -329,12 +391,14 @@ int bidiag2s(ddla_handle h, i64 m, i64 n, View<double> A, View<double> U, View<d
     const i64 FB = std::max<i64>(bs, std::min<i64>(256, tune_get("bidiag2s.form_nb", 128)));
     const size_t nd = (size_t)bs * n + (size_t)bs * (tvc > 0 ? tvc : 1) + 2 * (size_t)n * n;
     const size_t nf = (size_t)FB * FB + 2 * (size_t)n + (size_t)FB * m;
+    const size_t nz = 2 * (size_t)(n / bs + 2) * BD2_BLOCK * BK_Q;
     void *ws;
-    DDLA_TRY(workspace(h, WS_BD2, sizeof(double) * (nd + nf) + sizeof(int) * ((size_t)n + 8), &ws));
+    DDLA_TRY(workspace(h, WS_BD2, sizeof(double) * (nd + nf + nz) + sizeof(int) * ((size_t)n + 8), &ws));
     double *TU = (double *)ws, *TV = TU + (size_t)bs * n, *TU2 = TV + (size_t)bs * (tvc > 0 ? tvc : 1),
            *TV2 = TU2 + (size_t)n * n;
     double *Sf = TV2 + (size_t)n * n, *tauf = Sf + (size_t)FB * FB, *Wf = tauf + 2 * (size_t)n;
-    int *prog = (int *)(Wf + (size_t)FB * m), *err = prog + n;
+    double *Zq = Wf + (size_t)FB * m;
+    int *prog = (int *)(Zq + nz), *err = prog + n;
     DDLA_CUDA(cudaMemsetAsync(TU, 0, sizeof(double) * nd, s));
     DDLA_CUDA(cudaMemsetAsync(prog, 0, sizeof(int) * ((size_t)n + 8), s));
     auto grid_of = [](i64 tot) { return (unsigned)std::max<i64>(1, std::min<i64>((tot + 255) / 256, 8192)); };
@@ -408,18 +472,13 @@ int bidiag2s(ddla_handle h, i64 m, i64 n, View<double> A, View<double> U, View<d
         }
         // every group of bs cycles reads and writes columns i0 + 1 .. n of U and V once
         Timed tm(s, TC_BD_BACK, 2.0 * n * n * (double)(m + n), 8.0 * n * n * (double)(m + n) / bs);
-        const int P = (int)tune_get("bidiag2s.back_p", 4), rb = 32 / (P == 2 || P == 8 ? P : 4);
-        const int ublocks = (int)((m + rb - 1) / rb), vblocks = (int)((n + rb - 1) / rb);
+        const int ublocks = (int)((m + BK_RB - 1) / BK_RB), vblocks = (int)((n + BK_RB - 1) / BK_RB);
         for (i64 i0 = 0; i0 + 1 < n; i0 += bs) {
-            if (P == 2)
-                k_bd_back<2><<<ublocks + vblocks, 32, 0, s>>>(U.p, m, U.rs, U.cs, V.p, V.rs, V.cs, TU2, TV2, n,
-                                                             (int)bs, i0, ublocks);
-            else if (P == 8)
-                k_bd_back<8><<<ublocks + vblocks, 32, 0, s>>>(U.p, m, U.rs, U.cs, V.p, V.rs, V.cs, TU2, TV2, n,
-                                                             (int)bs, i0, ublocks);
-            else
-                k_bd_back<4><<<ublocks + vblocks, 32, 0, s>>>(U.p, m, U.rs, U.cs, V.p, V.rs, V.cs, TU2, TV2, n,
-                                                             (int)bs, i0, ublocks);
+            const int G = (int)(n - 1 - i0 < bs ? n - 1 - i0 : bs), kcount = (int)((n - i0 - 2) / bs) + 1;
+            k_bd_back_prep<<<dim3(kcount, 2), 32, 0, s>>>(TU2, TV2, n, (int)bs, i0, G, kcount, Zq);
+            DDLA_LAUNCHED();
+            k_bd_back<<<ublocks + vblocks, 32, 0, s>>>(U.p, m, U.rs, U.cs, V.p, V.rs, V.cs, TU2, TV2, Zq, n, (int)bs,
+                                                      i0, ublocks);
             DDLA_LAUNCHED();
         }
     }
