@@ -82,7 +82,7 @@ struct ddla_handle_s {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     // Growable device scratch areas (indexed by purpose).
-    ddla::Workspace ws[22];
+    ddla::Workspace ws[23];
     // Pinned host staging for host-pointer calls.
     void *pinned = nullptr;
     size_t pinned_bytes = 0;
@@ -114,14 +114,27 @@ namespace ddla {
 //   WS_TRDQ    tridiagonal reduction: Q of the trailing block before its copy
 //   WS_RHS     mixed solves: a block of right-hand sides
 //   WS_BD2     two-stage bidiagonal reduction: block factors, chase reflectors
+//   WS_NEXT    LU look-ahead: the next panel's columns after the previous step
 enum WsSlot {
     WS_A = 0, WS_B = 1, WS_C = 2, WS_TMP = 3, WS_PIV = 4, WS_F32 = 5, WS_X = 6, WS_MISC = 7,
     WS_TRI = 8, WS_Y = 9, WS_PERM = 10, WS_TC = 11, WS_TC2 = 12, WS_INV = 13, WS_PINV = 14, WS_QR = 15,
-    WS_SPLIT = 16, WS_QRU = 17, WS_TRD = 18, WS_TRDQ = 19, WS_RHS = 20, WS_BD2 = 21
+    WS_SPLIT = 16, WS_QRU = 17, WS_TRD = 18, WS_TRDQ = 19, WS_RHS = 20, WS_BD2 = 21, WS_NEXT = 22
 };
 
 // Order of the diagonal blocks that the triangular solves invert.
 constexpr int TRI_TB = 64;
+
+// Where an LU panel loads its rows from when the work of the previous step
+// was done out of place (panel.cu next_prep): rows from ld, and U12 rows to
+// copy to u12_dst (strides of the panel's own view) before factoring.
+template <typename T>
+struct PanelLoad {
+    const T *ld;
+    i64 ld_rs, ld_cs;
+    const T *u12_src;
+    T *u12_dst;
+    int u12_rows;
+};
 
 // Raises the kernel's dynamic shared-memory limit to everything the device
 // allows beside its static shared memory; returns that limit in *avail.

@@ -21,7 +21,11 @@ template <typename T>
 int panel_width_for(ddla_handle h, i64 m);
 template <typename T>
 int panel_factor(ddla_handle h, cudaStream_t s, View<T> X, i64 pc, int w, int32_t *d_piv, i64 row_base, int *d_info,
-                 T *inv, int slot);
+                 T *inv, int slot, const PanelLoad<T> *pl = nullptr);
+template <typename T>
+bool panel_fused_ok(ddla_handle h, i64 m, int w);
+int next_prep(ddla_handle h, cudaStream_t s, View<const float> F, i64 w0, i64 w1, int slot, const float *inv,
+              float *Tb);
 template <typename T>
 int panel_swap_cols(ddla_handle h, View<T> X, i64 ncols, i64 skip0, i64 skipw, int *perm, int slot);
 template <typename T>
@@ -354,11 +358,18 @@ int getrf(ddla_handle h, i64 n, View<T> A, int32_t *d_piv, int prec, int nb, int
     T *pinv;
     DDLA_TRY(workspace(h, WS_PINV, sizeof(T) * 2 * TRI_TB * TRI_TB, (void **)&pinv));
     auto inv_of = [&](i64 j0) { return pinv + ((j0 / w) & 1) * TRI_TB * TRI_TB; };
-    auto panel = [&](cudaStream_t st, i64 j0, int b) -> int {
+    auto panel = [&](cudaStream_t st, i64 j0, int b, const PanelLoad<T> *pl = nullptr) -> int {
         Timed t(st, TC_PANEL, 2.0 * b * b * ((n - j0) - b / 3.0), 2.0 * sizeof(T) * (n - j0) * (double)b);
         return panel_factor<T>(h, st, A.sub(j0, n - j0, 0, n), j0, b, d_piv + j0, j0, h->d_info + INFO_PIVOT,
-                               inv_of(j0), (int)((j0 / w) & 1));
+                               inv_of(j0), (int)((j0 / w) & 1), pl);
     };
+    // FP32: the work between two panels (the next panel's interchanges, U12
+    // and update) runs as one out-of-place launch (next_prep) instead of
+    // three, and the next panel loads its rows from that launch's output
+    const bool fused = ahead && sizeof(T) == 4 && tune_get("lu.nextprep", 1) != 0 &&
+                       panel_fused_ok<T>(h, n - (i64)w, w);
+    T *tb = nullptr;
+    if (fused) DDLA_TRY(workspace(h, WS_NEXT, sizeof(T) * (size_t)n * w, (void **)&tb));
     // U12 columns [c, c + nc) of the row block of panel j0: inv(L11) times a
     // copy of them (the same blocked inverse the general TRSM applies)
     const int tprec = sizeof(T) == 8 ? DDLA_PREC_FP64 : DDLA_PREC_FP32;
@@ -388,7 +399,7 @@ int getrf(ddla_handle h, i64 n, View<T> A, int32_t *d_piv, int prec, int nb, int
         const int b1n = (int)(r < w ? r : w);
         if (!ahead || r <= 0) {
             DDLA_TRY(panel_swap_rest<T>(h, A.sub(j0, n - j0, 0, n), j0, b, d_perm ? d_perm + j0 : nullptr, slot));
-        } else {
+        } else if (!fused) {
             // the next panel's columns now; the rest after the next panel started
             DDLA_TRY(panel_swap_cols<T>(h, A.sub(j0, n - j0, j0 + b, b1n), b1n, b1n, 0, nullptr, slot));
         }
@@ -397,7 +408,35 @@ int getrf(ddla_handle h, i64 n, View<T> A, int32_t *d_piv, int prec, int nb, int
         View<const T> A21{A.p + (j0 + b) * A.rs + j0 * A.cs, r, b, A.rs, A.cs};
         const i64 j1 = j0 + b;
         const int b1 = (int)(r < w ? r : w);
-        if (ahead) {
+        if (fused) {
+            // the next panel's columns (interchanges, U12, update) into tb in
+            // one launch, then the next panel from tb on the side stream,
+            // launched before this step's big update so that its cluster
+            // finds free SMs
+            {
+                Timed t(s, TC_UPDATE, 2.0 * r * b1 * b + (double)b * b * b1,
+                        sizeof(T) * (2.0 * (r + b) * b1 + r * b + b * b));
+                if constexpr (sizeof(T) == 4)
+                    DDLA_TRY(next_prep(h, s, View<const float>{A.p + j0 * A.rs + j0 * A.cs, n - j0, b + b1, A.rs, A.cs},
+                                       b, b1, slot, inv_of(j0), tb));
+            }
+            DDLA_CUDA(cudaEventRecord(h->ev_ready, s));
+            DDLA_CUDA(cudaStreamWaitEvent(h->side, h->ev_ready, 0));
+            const PanelLoad<T> pl{tb + (i64)b * b1, b1, 1, tb, A.p + j0 * A.rs + j1 * A.cs, b};
+            DDLA_TRY(panel(h->side, j1, b1, &pl));
+            DDLA_CUDA(cudaEventRecord(h->ev_panel, h->side));
+            DDLA_TRY(panel_swap_cols<T>(h, A.sub(j0, n - j0, 0, n), n - b - b1, j0, (i64)b + b1,
+                                        d_perm ? d_perm + j0 : nullptr, slot));
+            const i64 rest = r - b1;
+            if (rest > 0) {
+                DDLA_TRY(u12(j0, b, j1 + b1, rest));
+                Timed t(s, TC_UPDATE, 2.0 * r * rest * b, sizeof(T) * (2.0 * r * rest + r * b + b * rest));
+                DDLA_TRY(gemm_any<T>(h, prec, r, rest, b, T(-1), A21,
+                                     View<const T>{A12.p + b1 * A12.cs, b, rest, A12.rs, A12.cs}, T(1),
+                                     A.sub(j1, r, j1 + b1, rest)));
+            }
+            DDLA_CUDA(cudaStreamWaitEvent(s, h->ev_panel, 0));
+        } else if (ahead) {
             // next panel's columns first: their U12 part, then their update
             DDLA_TRY(u12(j0, b, j1, b1));
             {

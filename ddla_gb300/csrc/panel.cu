@@ -52,6 +52,14 @@ struct PanelArgs {
     T *inv;   // optional: inverse of the unit-lower w x w block L11 (row-major, ld TRI_TB)
     int *calu;   // tournament-pivoting scratch (k_panel_calu)
     int *err;    // set to 1 when a bounded wait of the cluster panel gives up
+    // optional (k_panel_lu): load the panel from ld (strides ld_rs, ld_cs)
+    // instead of P, and copy u12_rows x w finished U12 rows from u12_src
+    // (ld w) to u12_dst before the first exchange
+    const T *ld;
+    i64 ld_rs, ld_cs;
+    const T *u12_src;
+    T *u12_dst;
+    int u12_rows;
 };
 
 // Pivot search keys: |x| as an unsigned integer bit pattern plus one, NaN as
@@ -229,10 +237,17 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) k_panel_lu(PanelArgs<T> a) {
     const unsigned col_bytes = (unsigned)((CS + 1) * PKG);   // every CTA's candidate + row j
 
     if (rank == 0 && tid == 0) *a.touch_count = 0;
-    for (int e = tid; e < nloc * w; e += PANEL_THREADS) {
-        int l = e / w, c = e % w;
-        rows[l * WP + c] = a.P[(i64)(base + l) * a.rs + (i64)c * a.cs];
+    {
+        const T *src = a.ld ? a.ld : a.P;
+        const i64 srs = a.ld ? a.ld_rs : a.rs, scs = a.ld ? a.ld_cs : a.cs;
+        for (int e = tid; e < nloc * w; e += PANEL_THREADS) {
+            int l = e / w, c = e % w;
+            rows[l * WP + c] = src[(i64)(base + l) * srs + (i64)c * scs];
+        }
     }
+    if (a.u12_dst && rank == 0)
+        for (int e = tid; e < a.u12_rows * w; e += PANEL_THREADS)
+            a.u12_dst[(i64)(e / w) * a.rs + (i64)(e % w) * a.cs] = a.u12_src[e];
     for (int l = tid; l < nloc; l += PANEL_THREADS) origin[l] = base + l;
     if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32p(&full[0])) : "memory");
@@ -938,9 +953,130 @@ int tri_inverse_on(cudaStream_t s, bool lower, bool unit, View<const T> A, i64 n
 // panel k+1 is being factored; then the origin scratch of the fallback kernel.
 constexpr int TOUCH_INTS = 1 + 2 * LASWP_MAXT;
 
+// The work between two panels of the look-ahead LU, for the columns of
+// panel k+1, in one launch: panel k's row interchanges (its touched-row
+// list), U12 = inv(L11) A12 and the rank-w0 update A22 -= L21 U12
+// (LU.cs:334-360 for this block column).  F is panel k's top-left corner;
+// its frame rows [0, m0) and frame columns [w0, w0 + w1) are the next
+// panel's columns.  Nothing is written to F: the result (U12 in rows
+// [0, w0), the updated rows below) goes to Tb (m0 x w1, row-major), from
+// which panel k+1 loads its rows and copies U12 back.  So CTAs may gather
+// any source row without racing each other's writes.  Every CTA forms U12
+// itself (64^3 FMA) and updates 64 rows.
+constexpr int NP_ROWS = 64, NP_LD = 68;   // 16-byte rows for float4 operand loads
+
+// C (4 x 4 per thread, rows 4 ty.., columns 4 tx..) = sum_k AT[k][rows] B[k][cols]
+__device__ __forceinline__ void np_tile(const float *AT, const float *B, int kn, int ty, int tx, float acc[4][4]) {
+#pragma unroll 4
+    for (int k = 0; k < kn; k++) {
+        const float4 a = *reinterpret_cast<const float4 *>(AT + k * NP_LD + 4 * ty);
+        const float4 b = *reinterpret_cast<const float4 *>(B + k * NP_LD + 4 * tx);
+        const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_next_prep(const float *F, i64 rs, i64 cs, i64 m0, int w0, int w1,
+                                                   const int *tcount, const int *trows, const int *tsrc,
+                                                   const float *inv, float *Tb) {
+    extern __shared__ __align__(16) unsigned char np_smem[];
+    // A12[k][c], IvT[k][i] = inv(L11)[i][k], U12[k][c], L21T[k][l]; all ld NP_LD
+    float *A12 = (float *)np_smem, *IvT = A12 + PANEL_WMAX * NP_LD, *U12 = IvT + PANEL_WMAX * NP_LD,
+          *L21T = U12 + PANEL_WMAX * NP_LD;
+    __shared__ i64 srcA[PANEL_WMAX], srcOwn[NP_ROWS];
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    const i64 r0 = w0 + (i64)blockIdx.x * NP_ROWS;
+    const int nr = (int)(m0 - r0 < NP_ROWS ? (m0 - r0 > 0 ? m0 - r0 : 0) : NP_ROWS);
+    if (tid < PANEL_WMAX) srcA[tid] = tid;
+    if (tid >= 64 && tid < 64 + NP_ROWS) srcOwn[tid - 64] = r0 + (tid - 64);
+    __syncthreads();
+    const int cnt = *tcount;
+    for (int t = tid; t < cnt; t += 256) {
+        const i64 r = trows[t];
+        if (r < w0) srcA[r] = tsrc[t];
+        if (r >= r0 && r < r0 + NP_ROWS) srcOwn[r - r0] = tsrc[t];
+    }
+    __syncthreads();
+    // operands; entries outside w0 / w1 / nr are zero
+    for (int e = tid; e < PANEL_WMAX * PANEL_WMAX; e += 256) {
+        const int k = e >> 6, c = e & 63;
+        A12[k * NP_LD + c] = k < w0 && c < w1 ? F[srcA[k] * rs + (i64)(w0 + c) * cs] : 0.f;
+        IvT[c * NP_LD + k] = k < w0 && c < w0 ? inv[k * TRI_TB + c] : 0.f;   // IvT[c][k] = inv[k][c]
+        L21T[c * NP_LD + k] = k < nr && c < w0 ? F[(r0 + k) * rs + (i64)c * cs] : 0.f;   // L21T[c][l=k]
+    }
+    __syncthreads();
+    float acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) acc[i][j] = 0.f;
+    np_tile(IvT, A12, w0, ty, tx, acc);   // U12 = inv(L11) A12
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+        *reinterpret_cast<float4 *>(U12 + (4 * ty + i) * NP_LD + 4 * tx) =
+            make_float4(acc[i][0], acc[i][1], acc[i][2], acc[i][3]);
+    __syncthreads();
+    if (blockIdx.x == 0)
+        for (int e = tid; e < w0 * w1; e += 256) Tb[e] = U12[(e / w1) * NP_LD + e % w1];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) acc[i][j] = 0.f;
+    np_tile(L21T, U12, w0, ty, tx, acc);   // L21 U12 for this CTA's rows
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const int l = 4 * ty + i;
+        if (l >= nr) continue;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const int c = 4 * tx + j;
+            if (c < w1) Tb[(r0 + l) * w1 + c] = F[srcOwn[l] * rs + (i64)(w0 + c) * cs] - acc[i][j];
+        }
+    }
+}
+
+int next_prep(ddla_handle h, cudaStream_t s, View<const float> F, i64 w0, i64 w1, int slot, const float *inv,
+              float *Tb) {
+    const i64 m0 = F.rows;
+    int *tbuf;
+    DDLA_TRY(workspace(h, WS_PIV, sizeof(int) * (size_t)(2 * TOUCH_INTS + m0 + CALU_INTS), (void **)&tbuf));
+    tbuf += slot * TOUCH_INTS;
+    const size_t smem = sizeof(float) * 4 * PANEL_WMAX * NP_LD;
+    static bool attr = false;
+    if (!attr) {
+        DDLA_CUDA(cudaFuncSetAttribute(k_next_prep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        attr = true;
+    }
+    const i64 blocks = (m0 - w0 + NP_ROWS - 1) / NP_ROWS;
+    k_next_prep<<<(unsigned)(blocks > 0 ? blocks : 1), 256, smem, s>>>(F.p, F.rs, F.cs, m0, (int)w0, (int)w1,
+                                                                          tbuf, tbuf + 1, tbuf + 1 + LASWP_MAXT,
+                                                                          inv, Tb);
+    DDLA_LAUNCHED();
+    return 0;
+}
+
+// True when an m-row panel of width w runs on the cluster kernel k_panel_lu
+// (the only panel kernel that takes a PanelLoad).
+template <typename T>
+bool panel_fused_ok(ddla_handle h, i64 m, int w) {
+    int cs = max_cluster<T>(h);
+    if (cs <= 0 || w > PANEL_WMAX) return false;
+    if (sizeof(T) == 4 && tune_get("panel.calu", 0) != 0) return false;
+    const int64_t want = tune_get("panel.cluster", 0);
+    if (want > 0 && want < cs) cs = (int)want;
+    const size_t avail = panel_smem_avail<T>();
+    int use = 1;
+    while (use < cs && ((m + use - 1) / use > 512 || panel_smem_layout<T>((int)((m + use - 1) / use), w).total > avail))
+        use *= 2;
+    return panel_smem_layout<T>((int)((m + use - 1) / use), w).total <= avail;
+}
+
 template <typename T>
 int panel_factor(ddla_handle h, cudaStream_t s, View<T> X, i64 pc, int w, int32_t *d_piv, i64 row_base,
-                 int *d_info, T *inv, int slot) {
+                 int *d_info, T *inv, int slot, const PanelLoad<T> *pl) {
     const i64 m = X.rows;
     int *tbuf;
     DDLA_TRY(workspace(h, WS_PIV, sizeof(int) * (size_t)(2 * TOUCH_INTS + m + CALU_INTS), (void **)&tbuf));
@@ -963,6 +1099,16 @@ int panel_factor(ddla_handle h, cudaStream_t s, View<T> X, i64 pc, int w, int32_
     a.inv = inv;
     a.calu = calu;
     a.err = h->d_info + INFO_TIMEOUT;
+    a.ld = pl ? pl->ld : nullptr;
+    a.ld_rs = pl ? pl->ld_rs : 0;
+    a.ld_cs = pl ? pl->ld_cs : 0;
+    a.u12_src = pl ? pl->u12_src : nullptr;
+    a.u12_dst = pl ? pl->u12_dst : nullptr;
+    a.u12_rows = pl ? pl->u12_rows : 0;
+    if (pl && !panel_fused_ok<T>(h, m, w)) {
+        set_error("panel_lu: an out-of-place panel load needs the cluster panel");
+        return DDLA_ERR_UNSUPPORTED;
+    }
     int cs = max_cluster<T>(h);
     if (cs <= 0) return cs < 0 ? cs : DDLA_ERR_UNSUPPORTED;
     const int64_t want = tune_get("panel.cluster", 0);
@@ -1110,9 +1256,11 @@ int apply_perm(ddla_handle h, View<T> B, const int32_t *d_piv, i64 n, bool forwa
 template int panel_width_for<double>(ddla_handle, i64);
 template int panel_width_for<float>(ddla_handle, i64);
 template int panel_factor<double>(ddla_handle, cudaStream_t, View<double>, i64, int, int32_t *, i64, int *,
-                                  double *, int);
+                                  double *, int, const PanelLoad<double> *);
 template int panel_factor<float>(ddla_handle, cudaStream_t, View<float>, i64, int, int32_t *, i64, int *, float *,
-                                 int);
+                                 int, const PanelLoad<float> *);
+template bool panel_fused_ok<float>(ddla_handle, i64, int);
+template bool panel_fused_ok<double>(ddla_handle, i64, int);
 template int panel_swap_rest<double>(ddla_handle, View<double>, i64, int, int *, int);
 template int panel_swap_rest<float>(ddla_handle, View<float>, i64, int, int *, int);
 template int panel_swap_cols<double>(ddla_handle, View<double>, i64, i64, i64, int *, int);
