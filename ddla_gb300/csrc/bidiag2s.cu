@@ -83,6 +83,7 @@ struct ChaseArgs {
     double *tu2, *tv2;   // n x n, row i = cycle i's reflectors (tau, then the vector)
     int *prog;           // reflectors finished per cycle
     int *err;
+    int build_solo;      // 1: warp 0 alone builds each reflector
 };
 
 // Geometry of reflector t of a cycle with `rows` rows left (Bd2Bi_StepCycle,
@@ -116,13 +117,16 @@ __device__ inline StepGeom step_geom(i64 rows, int bs, int t, int steps) {
 // Cc <= 64 columns): the reflector of M's first column
 // (HouseHolder.BuildHouseHolder, HouseHolder.cs:34-58) applied from the left
 // to M's other columns (ApplyHouseHolder, HouseHolder.cs:95-115); tau and the
-// vector go to t, the column's tail is cleared.  Every warp builds the
-// reflector from column 0 (no barrier between build and apply); four
-// threads per column split its dot product, with the column's entries loaded
-// before the reflector is known.  Column 0 is written after the closing
-// barrier, by warp 0.
+// vector go to t, the column's tail is cleared.  Warp 0 builds the
+// reflector and shares it through one barrier (on GB300 the FP64 square
+// roots and divisions cost more than the barrier: 94 against 125 ms of chase
+// at n = 4096); with the tuning key bidiag2s.build_solo = 0 every warp builds
+// it and no barrier is taken.  1 / tau is formed once in the build.  Four threads per column split its
+// dot product, with the column's entries loaded before the reflector is
+// known.  Column 0 is written after the closing barrier, by warp 0.
 __device__ void step_side(const ChaseArgs &a, i64 s, const StepGeom &g, double *t) {
     __shared__ double s_u[BD2_THREADS / 32][BD2_BLOCK];
+    __shared__ double s_rt;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     double *p = a.W + (s + g.r0) * a.rs + (s + g.c0) * a.cs;
     const i64 ers = g.trans ? a.cs : a.rs, ecs = g.trans ? a.rs : a.cs;   // M(r, c) = p[r ers + c ecs]
@@ -137,40 +141,50 @@ __device__ void step_side(const ChaseArgs &a, i64 s, const StepGeom &g, double *
         v[i] = colv && l < len ? p[(1 + l) * ers + j * ecs] : 0.0;
     }
     const double a1 = colv ? p[j * ecs] : 0.0;
-    const double x = lane < len ? p[(1 + lane) * ers] : 0.0;
-    double chi = p[0], tau, u = x;
-    double ss = x * x;
-    for (int off = 16; off > 0; off >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, off);
-    const double nrm = sqrt(ss);
-    if (nrm == 0.0) {
-        chi = -chi;
-        tau = 0.5;
-    } else {
-        const double alpha = hypot(chi, nrm);
-        const double rho = -copysign(alpha, chi);
-        const double miu = chi - rho;
-        chi = rho;
-        u = x * (1.0 / miu);
-        const double sc = nrm / fabs(miu);
-        tau = (1.0 + sc * sc) / 2.0;
+    // the reflector: by every warp (no barrier), or by warp 0 alone with one
+    // barrier (the FP64 square roots and divisions then run once per CTA)
+    const bool solo = a.build_solo != 0;
+    double chi = 0.0, tau = 0.5, rtau = 2.0, u = 0.0;
+    if (!solo || warp == 0) {
+        const double x = lane < len ? p[(1 + lane) * ers] : 0.0;
+        chi = p[0];
+        u = x;
+        double ss = x * x;
+        for (int off = 16; off > 0; off >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, off);
+        if (ss == 0.0) {
+            chi = -chi;
+        } else {
+            const double alpha = hypot(chi, sqrt(ss));
+            const double rho = -copysign(alpha, chi);
+            const double miu = chi - rho;
+            const double rmiu = 1.0 / miu;
+            chi = rho;
+            u = x * rmiu;
+            tau = (1.0 + ss * rmiu * rmiu) / 2.0;   // (1 + (|x| / |miu|)^2) / 2
+            rtau = 1.0 / tau;
+        }
+        s_u[warp][lane] = u;
+        if (solo && lane == 0) s_rt = rtau;
     }
-    s_u[warp][lane] = u;
-    __syncwarp();
+    if (solo) __syncthreads();
+    else __syncwarp();
+    const double *su = s_u[solo ? 0 : warp];
+    const double rt = solo ? s_rt : rtau;
     double part = 0.0;
 #pragma unroll
     for (int i = 0; i < 8; i++) {
         const int l = sub + 4 * i;
-        if (l < len) part = fma(v[i], s_u[warp][l], part);
+        if (l < len) part = fma(v[i], su[l], part);
     }
     part += __shfl_xor_sync(0xffffffffu, part, 1);
     part += __shfl_xor_sync(0xffffffffu, part, 2);
-    const double w = (a1 + part) * (1.0 / tau);
+    const double w = (a1 + part) * rt;
     if (colv) {
         if (sub == 0) p[j * ecs] = a1 - w;
 #pragma unroll
         for (int i = 0; i < 8; i++) {
             const int l = sub + 4 * i;
-            if (l < len) p[(1 + l) * ers + j * ecs] = fma(-s_u[warp][l], w, v[i]);
+            if (l < len) p[(1 + l) * ers + j * ecs] = fma(-su[l], w, v[i]);
         }
     }
     __syncthreads();   // every warp has read column 0
@@ -458,7 +472,7 @@ int bidiag2s(ddla_handle h, i64 m, i64 n, View<double> A, View<double> U, View<d
     }
     // ---- stage 2: Bd2Bi
     if (n > 1) {
-        ChaseArgs ca{A.p, A.rs, A.cs, n, (int)bs, TU2, TV2, prog, err};
+        ChaseArgs ca{A.p, A.rs, A.cs, n, (int)bs, TU2, TV2, prog, err, (int)tune_get("bidiag2s.build_solo", 1)};
         int per_sm = 0;
         DDLA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bd_chase, BD2_THREADS, 0));
         const i64 cyc = n - 1;

@@ -981,7 +981,7 @@ __device__ __forceinline__ void np_tile(const float *AT, const float *B, int kn,
 
 __global__ void __launch_bounds__(256) k_next_prep(const float *F, i64 rs, i64 cs, i64 m0, int w0, int w1,
                                                    const int *tcount, const int *trows, const int *tsrc,
-                                                   const float *inv, float *Tb) {
+                                                   const float *inv, float *Tb, int vec) {
     extern __shared__ __align__(16) unsigned char np_smem[];
     // A12[k][c], IvT[k][i] = inv(L11)[i][k], U12[k][c], L21T[k][l]; all ld NP_LD
     float *A12 = (float *)np_smem, *IvT = A12 + PANEL_WMAX * NP_LD, *U12 = IvT + PANEL_WMAX * NP_LD,
@@ -1000,12 +1000,47 @@ __global__ void __launch_bounds__(256) k_next_prep(const float *F, i64 rs, i64 c
         if (r >= r0 && r < r0 + NP_ROWS) srcOwn[r - r0] = tsrc[t];
     }
     __syncthreads();
-    // operands; entries outside w0 / w1 / nr are zero
-    for (int e = tid; e < PANEL_WMAX * PANEL_WMAX; e += 256) {
-        const int k = e >> 6, c = e & 63;
-        A12[k * NP_LD + c] = k < w0 && c < w1 ? F[srcA[k] * rs + (i64)(w0 + c) * cs] : 0.f;
-        IvT[c * NP_LD + k] = k < w0 && c < w0 ? inv[k * TRI_TB + c] : 0.f;   // IvT[c][k] = inv[k][c]
-        L21T[c * NP_LD + k] = k < nr && c < w0 ? F[(r0 + k) * rs + (i64)c * cs] : 0.f;   // L21T[c][l=k]
+    // operands (entries outside w0 / w1 / nr are zero), and the rows this
+    // thread's 4 x 4 result is subtracted from, all loaded before any use:
+    // with contiguous 16-byte aligned rows as float4 (4 chunks of each kind
+    // per thread), else element by element
+    float4 own[4];
+    if (vec) {
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int e = tid + 256 * q, k = e >> 4, c4 = (e & 15) * 4;   // row k, columns c4 .. c4 + 3
+            const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+            const float4 a12 = k < w0 && c4 < w1 ? *reinterpret_cast<const float4 *>(F + srcA[k] * rs + w0 + c4) : z;
+            const float4 iv = k < w0 ? *reinterpret_cast<const float4 *>(inv + k * TRI_TB + c4) : z;
+            const float4 l21 = k < nr ? *reinterpret_cast<const float4 *>(F + (r0 + k) * rs + c4) : z;
+            const int l = 4 * ty + q;
+            own[q] = l < nr && 4 * tx < w1 ? *reinterpret_cast<const float4 *>(F + srcOwn[l] * rs + w0 + 4 * tx) : z;
+            *reinterpret_cast<float4 *>(A12 + k * NP_LD + c4) = a12;
+            const float ivv[4] = {iv.x, iv.y, iv.z, iv.w}, lv[4] = {l21.x, l21.y, l21.z, l21.w};
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                IvT[(c4 + j) * NP_LD + k] = c4 + j < w0 ? ivv[j] : 0.f;   // IvT[c][k] = inv[k][c]
+                L21T[(c4 + j) * NP_LD + k] = c4 + j < w0 ? lv[j] : 0.f;   // L21T[c][l = k]
+            }
+        }
+    } else {
+        for (int e = tid; e < PANEL_WMAX * PANEL_WMAX; e += 256) {
+            const int k = e >> 6, c = e & 63;
+            A12[k * NP_LD + c] = k < w0 && c < w1 ? F[srcA[k] * rs + (i64)(w0 + c) * cs] : 0.f;
+            IvT[c * NP_LD + k] = k < w0 && c < w0 ? inv[k * TRI_TB + c] : 0.f;
+            L21T[c * NP_LD + k] = k < nr && c < w0 ? F[(r0 + k) * rs + (i64)c * cs] : 0.f;
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int l = 4 * ty + q;
+            float o[4];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const int c = 4 * tx + j;
+                o[j] = l < nr && c < w1 ? F[srcOwn[l] * rs + (i64)(w0 + c) * cs] : 0.f;
+            }
+            own[q] = make_float4(o[0], o[1], o[2], o[3]);
+        }
     }
     __syncthreads();
     float acc[4][4];
@@ -1030,10 +1065,11 @@ __global__ void __launch_bounds__(256) k_next_prep(const float *F, i64 rs, i64 c
     for (int i = 0; i < 4; i++) {
         const int l = 4 * ty + i;
         if (l >= nr) continue;
+        const float ov[4] = {own[i].x, own[i].y, own[i].z, own[i].w};
 #pragma unroll
         for (int j = 0; j < 4; j++) {
             const int c = 4 * tx + j;
-            if (c < w1) Tb[(r0 + l) * w1 + c] = F[srcOwn[l] * rs + (i64)(w0 + c) * cs] - acc[i][j];
+            if (c < w1) Tb[(r0 + l) * w1 + c] = ov[j] - acc[i][j];
         }
     }
 }
@@ -1045,6 +1081,10 @@ int next_prep(ddla_handle h, cudaStream_t s, View<const float> F, i64 w0, i64 w1
     DDLA_TRY(workspace(h, WS_PIV, sizeof(int) * (size_t)(2 * TOUCH_INTS + m0 + CALU_INTS), (void **)&tbuf));
     tbuf += slot * TOUCH_INTS;
     const size_t smem = sizeof(float) * 4 * PANEL_WMAX * NP_LD;
+    // float4 loads: unit column stride, 16-byte aligned rows (the next
+    // panel's first column w0 and the row stride multiples of 4 elements)
+    const bool vec = F.cs == 1 && F.rs % 4 == 0 && w0 % 4 == 0 && w1 % 4 == 0 && (((uintptr_t)F.p) & 15) == 0 &&
+                     (((uintptr_t)inv) & 15) == 0;
     static bool attr = false;
     if (!attr) {
         DDLA_CUDA(cudaFuncSetAttribute(k_next_prep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -1053,7 +1093,7 @@ int next_prep(ddla_handle h, cudaStream_t s, View<const float> F, i64 w0, i64 w1
     const i64 blocks = (m0 - w0 + NP_ROWS - 1) / NP_ROWS;
     k_next_prep<<<(unsigned)(blocks > 0 ? blocks : 1), 256, smem, s>>>(F.p, F.rs, F.cs, m0, (int)w0, (int)w1,
                                                                           tbuf, tbuf + 1, tbuf + 1 + LASWP_MAXT,
-                                                                          inv, Tb);
+                                                                          inv, Tb, vec ? 1 : 0);
     DDLA_LAUNCHED();
     return 0;
 }
