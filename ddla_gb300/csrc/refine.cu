@@ -71,6 +71,33 @@ __global__ void k_colmax_abs(const double *X, i64 n, int nr, unsigned long long 
     }
 }
 
+// The FP32 copy of A (row-major n x n) and, in the same pass over A,
+// ||A||_inf (out[0]) and max |a_ij| (out[1], NaN ignored), as bit patterns of
+// non-negative doubles.  One warp per row.
+__global__ void k_d2s_norms(i64 n, const double *A, i64 lda, float *A32, unsigned long long *out) {
+    const int lane = threadIdx.x & 31;
+    const i64 row = (blockIdx.x * (i64)blockDim.x + threadIdx.x) >> 5;
+    if (row >= n) return;
+    double s = 0.0, mx = 0.0;
+    const double *a = A + row * lda;
+    float *y = A32 + row * n;
+#pragma unroll 4
+    for (i64 j = lane; j < n; j += 32) {
+        const double v = a[j];
+        y[j] = (float)v;
+        s += fabs(v);
+        mx = fmax(mx, fabs(v));
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        s += __shfl_down_sync(0xffffffffu, s, off);
+        mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, off));
+    }
+    if (lane == 0) {
+        atomicMax(&out[0], (unsigned long long)__double_as_longlong(s));
+        if (mx == mx) atomicMax(&out[1], (unsigned long long)__double_as_longlong(mx));
+    }
+}
+
 // ||A||_inf = max_i sum_j |a_ij| (row-major), one warp per row.
 __global__ void k_norm_inf(i64 n, const double *A, i64 lda, unsigned long long *out) {
     const int lane = threadIdx.x & 31;
@@ -284,15 +311,19 @@ int gmres_cycle(ddla_handle h, i64 n, const double *A, const double *R, double *
 template <typename F>
 int refine(ddla_handle h, i64 n, int nr, const double *A, const double *B, double *X, const double *x_ref,
            const ddla_opts *opts, ddla_solve_report *rep, F solve32, float *d32, double *R,
-           unsigned long long *norms) {
+           unsigned long long *norms, const unsigned long long *anorm = nullptr) {
     cudaStream_t s = h->stream;
     const int max_iter = (opts && opts->max_iter) ? opts->max_iter : 30;
     const double tol = (opts && opts->tol > 0) ? opts->tol : 1e-14;
     const i64 tot = n * nr;
     // norms[0] = ||A||_inf, [1..nr] = ||b_j||, [1+nr .. 1+2nr) = ||x_j||, [1+2nr .. 1+3nr) = ||r_j||
     DDLA_CUDA(cudaMemsetAsync(norms, 0, sizeof(unsigned long long) * (1 + 3 * MAX_RHS + 2), s));
-    k_norm_inf<<<(unsigned)((n * 32 + 255) / 256), 256, 0, s>>>(n, A, n, norms);
-    DDLA_LAUNCHED();
+    if (anorm) {   // formed with the FP32 copy of A
+        DDLA_CUDA(cudaMemcpyAsync(norms, anorm, sizeof(unsigned long long), cudaMemcpyDeviceToDevice, s));
+    } else {
+        k_norm_inf<<<(unsigned)((n * 32 + 255) / 256), 256, 0, s>>>(n, A, n, norms);
+        DDLA_LAUNCHED();
+    }
     k_colmax_abs<<<grid1(tot), 256, 0, s>>>(B, n, nr, norms + 1);
     DDLA_LAUNCHED();
     // x0 = LU \ b
@@ -420,14 +451,6 @@ __global__ void k_growth(const float *F, i64 rs, i64 cs, i64 n, int kind, unsign
         }
     }
 }
-// max |a_ij| of the FP64 matrix
-__global__ void k_absmax(const double *A, i64 tot, unsigned long long *out) {
-    double v = 0.0;
-    for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < tot; e += (i64)gridDim.x * blockDim.x)
-        v = fmax(v, fabs(A[e]));
-    for (int off = 16; off > 0; off >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, off));
-    if ((threadIdx.x & 31) == 0 && v == v) atomicMax(out, (unsigned long long)__double_as_longlong(v));
-}
 // D z = y for the LDL^T correction solve: row i of Y (n x nr) divided by d_i
 __global__ void k_rows_by_diag(float *Y, i64 n, int nr, const float *F, i64 dstride) {
     for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < n * nr; e += (i64)gridDim.x * blockDim.x)
@@ -469,12 +492,15 @@ int mixed_solve(ddla_handle h, int kind, int uplo, i64 n, i64 nrhs, const double
     DDLA_TRY(workspace(h, WS_B, sizeof(float) * (size_t)n * nr0 + 256, (void **)&d32));
     DDLA_TRY(workspace(h, WS_C, sizeof(double) * (size_t)n * nr0, (void **)&R));
     // norms: [0] ||A||, [1 .. 3 MAX_RHS] column norms, then the forward-error
-    // pair, the pivot comparison and the four growth figures
-    constexpr int NORMS = 1 + 3 * MAX_RHS + 2 + 1 + 4;
+    // pair, the pivot comparison, the three growth figures of the factor,
+    // and ||A||_inf, max |a_ij| from the pass that forms the FP32 copy
+    constexpr int NORMS = 1 + 3 * MAX_RHS + 2 + 1 + 3 + 2;
     DDLA_TRY(workspace(h, WS_A, sizeof(unsigned long long) * NORMS, (void **)&norms));
+    unsigned long long *astat = norms + NORMS - 2;
     DDLA_TRY(reset_info(h));
     DDLA_CUDA(cudaEventRecord(h->ev0, s));
-    k_d2s<<<grid1(n * n), 256, 0, s>>>(A, n * n, A32);
+    DDLA_CUDA(cudaMemsetAsync(astat, 0, 2 * sizeof(unsigned long long), s));
+    k_d2s_norms<<<(unsigned)((n * 32 + 255) / 256), 256, 0, s>>>(n, A, n, A32, astat);
     DDLA_LAUNCHED();
     const View<float> F{A32, n, n, n, 1};
     if (kind == MIX_LU) DDLA_TRY(getrf<float>(h, n, F, piv, prec, nb, perm));
@@ -499,7 +525,7 @@ int mixed_solve(ddla_handle h, int kind, int uplo, i64 n, i64 nrhs, const double
             k_piv_cmp<<<grid1(n), 256, 0, s>>>(piv, piv_ref, n, cmp);
             DDLA_LAUNCHED();
         }
-        const unsigned long long ginit[4] = {0ull, 0ull, 0x7ff0000000000000ull, 0ull};
+        const unsigned long long ginit[3] = {0ull, 0ull, 0x7ff0000000000000ull};
         DDLA_CUDA(cudaMemcpyAsync(grow, ginit, sizeof(ginit), cudaMemcpyHostToDevice, s));
         if (!info) {
             // the factor as the lower triangle L (Cholesky / LDL^T upper: the transpose)
@@ -507,10 +533,9 @@ int mixed_solve(ddla_handle h, int kind, int uplo, i64 n, i64 nrhs, const double
                                                                                  : View<const float>{A32, n, n, n, 1};
             k_growth<<<(unsigned)((n * 32 + 255) / 256), 256, 0, s>>>(Fg.p, Fg.rs, Fg.cs, n, kind, grow);
             DDLA_LAUNCHED();
-            k_absmax<<<grid1(n * n), 256, 0, s>>>(A, n * n, grow + 3);
-            DDLA_LAUNCHED();
         }
-        unsigned long long got[5];
+        // pivot comparison, growth of the factor, ||A||_inf, max |a_ij|
+        unsigned long long got[6];
         DDLA_CUDA(cudaMemcpyAsync(got, norms + 1 + 3 * MAX_RHS + 2, sizeof(got), cudaMemcpyDeviceToHost, s));
         DDLA_CUDA(cudaStreamSynchronize(s));
         if (piv_ref && piv) {
@@ -519,7 +544,7 @@ int mixed_solve(ddla_handle h, int kind, int uplo, i64 n, i64 nrhs, const double
             rep->pivots_first_diff = cmp[1] == INT_MAX ? -1 : cmp[1];
         }
         if (!info) {
-            const double gmax = u64d(got[1]), dmax = u64d(got[2]), dmin = u64d(got[3]), amax = u64d(got[4]);
+            const double gmax = u64d(got[1]), dmax = u64d(got[2]), dmin = u64d(got[3]), amax = u64d(got[5]);
             rep->growth = amax > 0 ? gmax / amax : gmax;
             rep->diag_ratio = dmin > 0 ? dmax / dmin : INFINITY;
         }
@@ -552,7 +577,7 @@ int mixed_solve(ddla_handle h, int kind, int uplo, i64 n, i64 nrhs, const double
     DDLA_CUDA(cudaEventRecord(h->ev0, s));
     int rc = 0;
     if (nrhs <= MAX_RHS) {
-        rc = refine(h, n, nr, A, B, X, x_ref, opts, rep, solve32, d32, R, norms);
+        rc = refine(h, n, nr, A, B, X, x_ref, opts, rep, solve32, d32, R, norms, astat);
     } else {
         // blocks of MAX_RHS columns, copied into dense n x nr blocks and back
         double *blk;
@@ -570,7 +595,8 @@ int mixed_solve(ddla_handle h, int kind, int uplo, i64 n, i64 nrhs, const double
                 DDLA_LAUNCHED();
             }
             ddla_solve_report part = *rep;
-            const int prc = refine(h, n, nr, A, Bc, Xc, x_ref ? XRc : nullptr, opts, &part, solve32, d32, R, norms);
+            const int prc = refine(h, n, nr, A, Bc, Xc, x_ref ? XRc : nullptr, opts, &part, solve32, d32, R, norms,
+                                   astat);
             if (prc != 0 && prc != DDLA_ERR_NOT_CONVERGED) return prc;
             k_cols_copy<<<grid1(n * nr), 256, 0, s>>>(Xc, nr, X + c0, nrhs, n, nr);
             DDLA_LAUNCHED();
