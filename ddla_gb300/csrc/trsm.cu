@@ -576,10 +576,12 @@ __global__ void __launch_bounds__(CL_THREADS)
                         pend |= cl_pending(xv[i][c]);
                     }
                 if (!__any_sync(0xffffffffu, pend)) break;
-                if (++it > CL_SPIN || *(volatile int *)&s_abort) { bad = true; break; }
+                // give up together: the decision is made warp-wide
+                const bool stop = ++it > CL_SPIN || *(volatile int *)&s_abort;
+                if (__any_sync(0xffffffffu, stop)) { bad = true; break; }
                 if (it > 64) __nanosleep(20);
             }
-            if (__any_sync(0xffffffffu, bad)) { bad = true; break; }
+            if (bad) break;
             __syncwarp();
             const T *tile = ring + (size_t)(consumed % S) * TB * CL_TLD;
 #pragma unroll
