@@ -81,12 +81,24 @@ __global__ void k_d2s_norms(i64 n, const double *A, i64 lda, float *A32, unsigne
     double s = 0.0, mx = 0.0;
     const double *a = A + row * lda;
     float *y = A32 + row * n;
+    if ((n & 3) == 0 && (lda & 3) == 0 && ((((uintptr_t)A) | ((uintptr_t)A32)) & 31) == 0) {
+        // 4 consecutive entries per lane: two 16-byte loads, one 16-byte store
+#pragma unroll 2
+        for (i64 j = 4 * lane; j < n; j += 128) {
+            const double2 v0 = *reinterpret_cast<const double2 *>(a + j);
+            const double2 v1 = *reinterpret_cast<const double2 *>(a + j + 2);
+            *reinterpret_cast<float4 *>(y + j) = make_float4((float)v0.x, (float)v0.y, (float)v1.x, (float)v1.y);
+            s += (fabs(v0.x) + fabs(v0.y)) + (fabs(v1.x) + fabs(v1.y));
+            mx = fmax(fmax(mx, fmax(fabs(v0.x), fabs(v0.y))), fmax(fabs(v1.x), fabs(v1.y)));
+        }
+    } else {
 #pragma unroll 4
-    for (i64 j = lane; j < n; j += 32) {
-        const double v = a[j];
-        y[j] = (float)v;
-        s += fabs(v);
-        mx = fmax(mx, fabs(v));
+        for (i64 j = lane; j < n; j += 32) {
+            const double v = a[j];
+            y[j] = (float)v;
+            s += fabs(v);
+            mx = fmax(mx, fabs(v));
+        }
     }
     for (int off = 16; off > 0; off >>= 1) {
         s += __shfl_down_sync(0xffffffffu, s, off);
