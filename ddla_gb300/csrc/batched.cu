@@ -58,6 +58,19 @@ struct BScratch {
     int src[BMV];       // ... and the row each receives
 };
 
+// Calls f(r, c) for r in [0, rows), c in [0, cols) over the CTA: threads
+// take columns in groups of the smallest power of two >= cols (at most 32),
+// rows by the remaining thread index bits -- no division per element.
+template <typename F>
+__device__ __forceinline__ void for_rc(int rows, int cols, F f) {
+    if (rows <= 0 || cols <= 0) return;
+    int lg = 5;
+    while (lg > 0 && (1 << (lg - 1)) >= cols) lg--;
+    const int tid = threadIdx.x, tpr = 1 << lg, rpp = BT >> lg;
+    for (int c = tid & (tpr - 1); c < cols; c += tpr)
+        for (int r = tid >> lg; r < rows; r += rpp) f(r, c);
+}
+
 // Block-wide first-max over rows of column j of the panel.
 template <typename T>
 __device__ int panel_argmax(const T *Ps, int ld, int m, int j, BScratch &S) {
@@ -101,10 +114,7 @@ __device__ int factor_item(T *W, int n, int kind, int nb, int *piv, T *Ps, T *Us
     for (int j0 = 0; j0 < n; j0 += nb) {
         const int jb = min(nb, n - j0), m = n - j0, r2 = n - j0 - jb;
         // 1. panel rows j0..n, cols j0..j0+jb
-        for (int e = tid; e < m * jb; e += BT) {
-            int r = e / jb, c = e % jb;
-            Ps[r * LDP + c] = W[(i64)(j0 + r) * n + j0 + c];
-        }
+        for_rc(m, jb, [&](int r, int c) { Ps[r * LDP + c] = W[(i64)(j0 + r) * n + j0 + c]; });
         __syncthreads();
         // 2. unblocked factorization of the panel
         if (kind == 2) {
@@ -125,12 +135,11 @@ __device__ int factor_item(T *W, int n, int kind, int nb, int *piv, T *Ps, T *Us
                 const T rinv = T(1) / d;
                 for (int r = j + 1 + tid; r < m; r += BT) Ps[r * LDP + j] *= rinv;
                 __syncthreads();
-                const int nr = m - j - 1, nc = jb - j - 1;
-                for (int e = tid; e < nr * nc; e += BT) {
-                    int r = j + 1 + e / nc, c = j + 1 + e % nc;
-                    if (r < jb && c > r) continue;   // diagonal block: lower triangle only
+                for_rc(m - j - 1, jb - j - 1, [&](int rr, int cc) {
+                    const int r = j + 1 + rr, c = j + 1 + cc;
+                    if (r < jb && c > r) return;   // diagonal block: lower triangle only
                     Ps[r * LDP + c] = fma(Ps[c * LDP + j], -Ps[r * LDP + j], Ps[r * LDP + c]);
-                }
+                });
                 __syncthreads();
             }
         } else {
@@ -157,22 +166,20 @@ __device__ int factor_item(T *W, int n, int kind, int nb, int *piv, T *Ps, T *Us
                 const T rinv = T(1) / d;
                 for (int r = j + 1 + tid; r < m; r += BT) Ps[r * LDP + j] *= rinv;
                 __syncthreads();
-                const int nr = m - j - 1, nc = jb - j - 1;
-                for (int e = tid; e < nr * nc; e += BT) {
-                    int r = j + 1 + e / nc, c = j + 1 + e % nc;
+                for_rc(m - j - 1, jb - j - 1, [&](int rr, int cc) {
+                    const int r = j + 1 + rr, c = j + 1 + cc;
                     Ps[r * LDP + c] = fma(Ps[r * LDP + j], -Ps[j * LDP + c], Ps[r * LDP + c]);
-                }
+                });
                 __syncthreads();
             }
         }
         __syncthreads();
         if (S.fail) return S.fail;
         // 3. write the panel back (Cholesky: only the lower part of the diagonal block)
-        for (int e = tid; e < m * jb; e += BT) {
-            int r = e / jb, c = e % jb;
-            if (kind == 2 && r < jb && c > r) continue;
+        for_rc(m, jb, [&](int r, int c) {
+            if (kind == 2 && r < jb && c > r) return;
             W[(i64)(j0 + r) * n + j0 + c] = Ps[r * LDP + c];
-        }
+        });
         __syncthreads();
         if (kind == 0) {
             // 4. the panel's interchanges on the other columns of rows j0..n,
@@ -222,10 +229,7 @@ __device__ int factor_item(T *W, int n, int kind, int nb, int *piv, T *Ps, T *Us
         if (r2 == 0) break;
         // 5. U12 = L11^-1 A12 (LU) or Us = L21^T (Cholesky), into shared memory
         if (kind == 2) {
-            for (int e = tid; e < jb * r2; e += BT) {
-                int i = e / r2, c = e % r2;
-                Us[i * n + c] = Ps[(jb + c) * LDP + i];
-            }
+            for_rc(jb, r2, [&](int i, int c) { Us[i * n + c] = Ps[(jb + c) * LDP + i]; });
         } else {
             // one thread per column c of U12, which it builds in Us (its own
             // column only: no barrier), forward substitution with unit L11
