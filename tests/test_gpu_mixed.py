@@ -8,8 +8,10 @@ from helpers import berr, rng, spd
 pytestmark = pytest.mark.gpu
 
 
+# n = 1001 and 2050: rows not 16-byte aligned (the element-wise form of the
+# fused next-panel step) and a last panel narrower than 64
 @pytest.mark.parametrize("prec", ["fp32", "tf32x3", "bf16x3"])
-@pytest.mark.parametrize("n,nrhs", [(100, 1), (1024, 1), (2048, 4), (3000, 16)])
+@pytest.mark.parametrize("n,nrhs", [(100, 1), (1001, 1), (1024, 1), (2048, 4), (2050, 2), (3000, 16)])
 def test_mixed_lu_reaches_fp64(ddla, orc, n, nrhs, prec):
     r = rng(n)
     A = r.standard_normal((n, n))
