@@ -912,13 +912,21 @@ struct OzSlots {
     }
 };
 
+constexpr int OZ_GROUP = 8;   // row tiles per raster group
+
 __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_gemm(OzArgs g) {
     extern __shared__ __align__(1024) unsigned char smem[];
     __shared__ __align__(8) unsigned long long full[OZ_NS], mdone[OZ_NS], mready[OZ_RING], fdone[OZ_RING];
     __shared__ unsigned tmem_slot;
     __shared__ volatile int abort_flag;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int64_t mt = blockIdx.y, nt = blockIdx.x, bz = blockIdx.z;
+    // grouped raster: the CTAs launched together walk OZ_GROUP row tiles
+    // before moving to the next column tile, so a wave shares A's and B's
+    // slice panels in L2 instead of streaming all of B once per wave
+    const int64_t NT = gridDim.x, MT = gridDim.y, bz = blockIdx.z;
+    const int64_t lin = (int64_t)blockIdx.y * NT + blockIdx.x, span = (int64_t)OZ_GROUP * NT;
+    const int64_t first = (lin / span) * OZ_GROUP, gm = MT - first < OZ_GROUP ? MT - first : OZ_GROUP;
+    const int64_t mt = first + (lin % span) % gm, nt = (lin % span) / gm;
     const __nv_bfloat16 *Ap = g.Ap + bz * g.a_item, *Bp = g.Bp + bz * g.b_item;
     const double *sa = g.sa + bz * g.s_item_a, *sb = g.sb + bz * g.s_item_b;
     double *Cz = g.C + (g.offs ? g.offs[3 * bz + 2] : 0);
