@@ -76,6 +76,19 @@ __host__ __device__ inline int cycle_steps(i64 n, i64 i, int bs) {
     return 2 * k + 4;
 }
 
+// Progress counters between chase cycles: a release store after the CTA's
+// closing barrier publishes every thread's writes of the reflector (the
+// barrier orders them before it); an acquire load by the waiting CTA's
+// thread 0, followed by a barrier, makes them visible to all its threads.
+__device__ __forceinline__ int prog_acquire(const int *p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void prog_release(int *p, int v) {
+    asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
 struct ChaseArgs {
     double *W;
     i64 rs, cs, n;
@@ -123,7 +136,9 @@ __device__ inline StepGeom step_geom(i64 rows, int bs, int t, int steps) {
 // at n = 4096); with the tuning key bidiag2s.build_solo = 0 every warp builds
 // it and no barrier is taken.  1 / tau is formed once in the build.  Four threads per column split its
 // dot product, with the column's entries loaded before the reflector is
-// known.  Column 0 is written after the closing barrier, by warp 0.
+// known.  Warp 0 writes column 0 and the reflector: right after the build
+// when it builds alone (no other warp reads column 0), else after the
+// closing barrier.
 __device__ void step_side(const ChaseArgs &a, i64 s, const StepGeom &g, double *t) {
     __shared__ double s_u[BD2_THREADS / 32][BD2_BLOCK];
     __shared__ double s_rt;
@@ -164,7 +179,21 @@ __device__ void step_side(const ChaseArgs &a, i64 s, const StepGeom &g, double *
             rtau = 1.0 / tau;
         }
         s_u[warp][lane] = u;
-        if (solo && lane == 0) s_rt = rtau;
+        if (solo) {
+            // only warp 0 reads column 0 in this mode: it stores the reflector
+            // and the column now, so the closing barrier covers them (the
+            // warp barrier orders every lane's read of p[0] before lane 0's store)
+            if (lane == 0) s_rt = rtau;
+            __syncwarp();
+            if (lane < len) {
+                t[1 + lane] = u;
+                p[(1 + lane) * ers] = 0.0;
+            }
+            if (lane == 0) {
+                p[0] = chi;
+                t[0] = tau;
+            }
+        }
     }
     if (solo) __syncthreads();
     else __syncwarp();
@@ -188,7 +217,7 @@ __device__ void step_side(const ChaseArgs &a, i64 s, const StepGeom &g, double *
         }
     }
     __syncthreads();   // every warp has read column 0
-    if (warp == 0) {
+    if (!solo && warp == 0) {
         if (lane < len) {
             t[1 + lane] = u;
             p[(1 + lane) * ers] = 0.0;
@@ -217,10 +246,9 @@ __global__ void __launch_bounds__(BD2_THREADS) k_bd_chase(ChaseArgs a) {
                     const int want = t + BD2_LAG < before ? t + BD2_LAG : before;
                     ok = 0;
                     for (long long it = 0; it < BD2_SPIN; it++) {
-                        if (*(volatile int *)&a.prog[s - 1] >= want) { ok = 1; break; }
+                        if (prog_acquire(&a.prog[s - 1]) >= want) { ok = 1; break; }
                         if (*(volatile int *)a.err) break;   // another cycle gave up
                     }
-                    __threadfence();
                     if (!ok) atomicExch(a.err, 1);
                 }
                 s_abort = !ok;
@@ -229,10 +257,7 @@ __global__ void __launch_bounds__(BD2_THREADS) k_bd_chase(ChaseArgs a) {
             if (s_abort) return;
             const StepGeom g = step_geom(rows, a.bs, t, steps);
             step_side(a, s, g, (g.trans ? a.tv2 : a.tu2) + s * a.n + s + g.toff);
-            if (tid == 0) {
-                __threadfence();
-                atomicExch(&a.prog[s], t + 1);
-            }
+            if (tid == 0) prog_release(&a.prog[s], t + 1);
         }
     }
 }
