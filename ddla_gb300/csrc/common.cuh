@@ -82,7 +82,7 @@ struct ddla_handle_s {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     // Growable device scratch areas (indexed by purpose).
-    ddla::Workspace ws[23];
+    ddla::Workspace ws[24];
     // Pinned host staging for host-pointer calls.
     void *pinned = nullptr;
     size_t pinned_bytes = 0;
@@ -115,10 +115,12 @@ namespace ddla {
 //   WS_RHS     mixed solves: a block of right-hand sides
 //   WS_BD2     two-stage bidiagonal reduction: block factors, chase reflectors
 //   WS_NEXT    LU look-ahead: the next panel's columns after the previous step
+//   WS_TRSV    split triangular solve: block flags, row states, far sums
 enum WsSlot {
     WS_A = 0, WS_B = 1, WS_C = 2, WS_TMP = 3, WS_PIV = 4, WS_F32 = 5, WS_X = 6, WS_MISC = 7,
     WS_TRI = 8, WS_Y = 9, WS_PERM = 10, WS_TC = 11, WS_TC2 = 12, WS_INV = 13, WS_PINV = 14, WS_QR = 15,
-    WS_SPLIT = 16, WS_QRU = 17, WS_TRD = 18, WS_TRDQ = 19, WS_RHS = 20, WS_BD2 = 21, WS_NEXT = 22
+    WS_SPLIT = 16, WS_QRU = 17, WS_TRD = 18, WS_TRDQ = 19, WS_RHS = 20, WS_BD2 = 21, WS_NEXT = 22,
+    WS_TRSV = 23
 };
 
 // Order of the diagonal blocks that the triangular solves invert.

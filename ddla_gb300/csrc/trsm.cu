@@ -438,10 +438,196 @@ __global__ void __launch_bounds__(CH16_THREADS)
     }
 }
 
+// Split mode (a grid of several clusters, W > 0).  The first cluster to start
+// runs the chain above over the NEAR tiles of each block row only: for l > W,
+// the W tiles A_lj with l - W <= j < l.  The other CTAs are helpers: each
+// takes block rows l > W in increasing order (a counter) and forms the far
+// sum F_l = sum_{j < l - W} A_lj x_j as the chain publishes each x_j (x_j in
+// X, then a flag per block), streaming the tiles ahead of the flags.  The
+// chain subtracts F_l from block l's right-hand side at its near tile
+// j = l - PW, by when the helper has normally released it.  A row that no
+// helper has taken when the chain reaches it is claimed by the chain and
+// summed there, so no wait depends on a CTA that has not started: the roles
+// and the rows are taken with atomics by whichever CTAs run first.  One
+// right-hand side.
+template <typename T>
+struct SplitArgs {
+    int *xflag;   // [nblk] logical block j's x is in X
+    int *rowst;   // [nblk] 0 free, 1 chain-owned, 2 helper-owned, 3 far sum in part
+    int *next;    // helpers' row counter
+    int *role;    // id + 1 of the chain cluster
+    T *part;      // [nblk][TB] far sums
+    int W, PW;    // near tiles per block row (0: one cluster, no split); where F_l is added
+};
+
+// Helper shared memory: per warp, ClStages stages of its 8 tile rows and x_j.
+template <typename T> __host__ __device__ constexpr int sp_stage() { return CL_WROWS * CL_TLD + TB; }
+template <typename T> __host__ __device__ constexpr size_t sp_smem() {
+    return sizeof(T) * (size_t)CL_WARPS * ClStages<T>::value * sp_stage<T>();
+}
+
+// Wait until at most k of this thread's cp.async groups are pending (k <= 7).
+__device__ __forceinline__ void cp_async_wait_n(int k) {
+    switch (k) {
+        case 0: cp_async_wait<0>(); break;
+        case 1: cp_async_wait<1>(); break;
+        case 2: cp_async_wait<2>(); break;
+        case 3: cp_async_wait<3>(); break;
+        case 4: cp_async_wait<4>(); break;
+        case 5: cp_async_wait<5>(); break;
+        case 6: cp_async_wait<6>(); break;
+        default: cp_async_wait<7>(); break;
+    }
+}
+
+// A helper CTA: far sums of the block rows it takes.  Each warp owns 8 rows of
+// the block row and streams its rows of the tiles A_lj (they do not depend on
+// the chain) up to S - 1 ahead; x_j is read once its flag is seen, for every
+// tile whose x has been published since the last look, so a helper that is
+// level with the chain pays one flag round trip per batch, not per tile.
+template <typename T>
+__device__ void split_helper(i64 n, int nblk, const T *__restrict__ A, i64 rs, i64 cs, int lower, int vec,
+                             const T *X, i64 ldx, int xvec, const SplitArgs<T> &sp, int *err, T *ring, int &s_row,
+                             int &s_abort) {
+    constexpr int S = ClStages<T>::value;
+    constexpr int HS = sp_stage<T>();
+    constexpr int CPR = TB * (int)sizeof(T) / 16, EPC = 16 / (int)sizeof(T);
+    constexpr int CPL = CL_WROWS * CPR / 32;   // 16-byte chunks per lane of a warp's tile rows
+    constexpr int XCH = TB / EPC;              // 16-byte chunks of x_j (<= 32)
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5, rr = lane >> 2, q = lane & 3;
+    T *wring = ring + (size_t)warp * S * HS;
+    auto phys = [&](int l) { return lower ? l : nblk - 1 - l; };
+    int c_row[CPL], c_col[CPL];
+#pragma unroll
+    for (int i = 0; i < CPL; i++) {
+        const int e = lane + 32 * i;
+        c_row[i] = e / CPR;
+        c_col[i] = (e % CPR) * EPC;
+    }
+    int ready = 0;   // x_0 .. x_{ready-1} are known to be published (warp-uniform)
+    for (;;) {
+        if (t == 0) {
+            const int row = atomicAdd(sp.next, 1) + sp.W + 1;
+            s_row = row >= nblk ? -2 : (atomicCAS(sp.rowst + row, 0, 2) == 0 ? row : -1);
+        }
+        __syncthreads();
+        const int row = s_row;
+        const bool quit = s_abort != 0;
+        __syncthreads();   // s_row and s_abort are read before thread 0 writes them again
+        if (row == -2 || quit) break;
+        if (row < 0) continue;
+        const int J = row - sp.W;   // far tiles j = 0 .. J - 1
+        const i64 g0 = (i64)phys(row) * TB + warp * CL_WROWS;   // first row of this warp
+        int produced = 0;
+        auto issue = [&](int j) {
+            T *dst = wring + (size_t)(j % S) * HS;
+            const i64 c0 = (i64)phys(j) * TB;
+            if (vec) {
+#pragma unroll
+                for (int i = 0; i < CPL; i++) {
+                    const i64 gr = g0 + c_row[i], gc = c0 + c_col[i];
+                    int bytes = 0;
+                    const T *src = A;
+                    if (gr < n && gc < n) {
+                        const i64 left = n - gc;
+                        bytes = (int)(left >= EPC ? 16 : left * (i64)sizeof(T));
+                        src = A + gr * rs + gc;
+                    }
+                    cp_async16(dst + c_row[i] * CL_TLD + c_col[i], src, bytes);
+                }
+            } else {
+                for (int e = lane; e < CL_WROWS * TB; e += 32) {
+                    const int row_ = e / TB, col = e % TB;
+                    const i64 gr = g0 + row_, gc = c0 + col;
+                    const bool in = gr < n && gc < n;
+                    cp_async_small<sizeof(T)>(dst + row_ * CL_TLD + col, in ? A + gr * rs + gc * cs : A,
+                                              in ? (int)sizeof(T) : 0);
+                }
+            }
+            cp_async_commit();
+        };
+        auto top_up = [&](int lim) {
+            while (produced < lim) issue(produced++);
+        };
+        T f = T(0);
+        bool bad = false;
+        int j = 0;
+        top_up(J < S ? J : S);
+        while (j < J) {
+            if (ready <= j) {
+                long long it = 0;
+                for (;;) {
+                    const int idx = ready + lane;
+                    const int v = idx < J ? ld_acquire(sp.xflag + idx) : 0;
+                    const unsigned b = __ballot_sync(0xffffffffu, v != 0);
+                    ready += b == 0xffffffffu ? 32 : __ffs(~b) - 1;
+                    if (ready > j) break;
+                    const bool stop = ++it > CL_SPIN || *(volatile int *)err != 0;
+                    if (__any_sync(0xffffffffu, stop)) {
+                        bad = true;
+                        break;
+                    }
+                    if (it > 16) __nanosleep(64);
+                }
+                if (bad) break;
+            }
+            // the lanes' flag loads above come before every lane's reads of x
+            __syncwarp();
+            const int jend = (ready < J ? ready : J) < j + S ? (ready < J ? ready : J) : j + S;
+            top_up(J < j + S ? J : j + S);
+            for (int b = j; b < jend; b++) {
+                T *xs = wring + (size_t)(b % S) * HS + CL_WROWS * CL_TLD;
+                const i64 c0 = (i64)phys(b) * TB;
+                if (xvec) {
+                    if (lane < XCH) {
+                        const i64 gc = c0 + lane * EPC;
+                        if (gc + EPC <= n) {
+                            *(uint4 *)(xs + lane * EPC) = __ldcg((const uint4 *)(X + gc));
+                        } else {
+#pragma unroll
+                            for (int e = 0; e < EPC; e++) xs[lane * EPC + e] = gc + e < n ? __ldcg(X + gc + e) : T(0);
+                        }
+                    }
+                } else {
+                    for (int e = lane; e < TB; e += 32) xs[e] = c0 + e < n ? __ldcg(X + (c0 + e) * ldx) : T(0);
+                }
+            }
+            cp_async_wait_n(produced - jend);   // the tiles of j .. jend - 1 have landed
+            __syncwarp();
+            for (int b = j; b < jend; b++) {
+                const T *st = wring + (size_t)(b % S) * HS;
+                const T *xs = st + CL_WROWS * CL_TLD;
+#pragma unroll
+                for (int i = 0; i < TB / 4; i++) f += st[rr * CL_TLD + q + 4 * i] * xs[q + 4 * i];
+            }
+            __syncwarp();   // stages j .. jend - 1 are free again
+            j = jend;
+            top_up(J < j + S ? J : j + S);
+        }
+        f += __shfl_xor_sync(0xffffffffu, f, 1);
+        f += __shfl_xor_sync(0xffffffffu, f, 2);
+        if (bad) {
+            if (lane == 0) {
+                atomicExch(err, 1);
+                s_abort = 1;
+            }
+        } else if (q == 0) {
+            sp.part[(size_t)row * TB + warp * CL_WROWS + rr] = f;
+        }
+        cp_async_wait<0>();
+        __syncthreads();   // every warp's far sums are stored
+        if (t == 0 && !s_abort) {
+            __threadfence();
+            st_release(sp.rowst + row, 3);
+        }
+    }
+    cp_async_wait<0>();
+}
+
 template <typename T, int NR>
 __global__ void __launch_bounds__(CL_THREADS)
     k_trsv_cluster(i64 n, int nblk, const T *__restrict__ A, i64 rs, i64 cs, int lower, int vec,
-                   const T *__restrict__ inv, T *X, i64 ldx, int nr, int *err) {
+                   const T *__restrict__ inv, T *X, i64 ldx, int nr, int *err, SplitArgs<T> sp, int xvec) {
     namespace cg = cooperative_groups;
     cg::cluster_group cluster = cg::this_cluster();
     constexpr int S = ClStages<T>::value;
@@ -452,8 +638,25 @@ __global__ void __launch_bounds__(CL_THREADS)
     T *ring = (T *)(smem + Ly.ring);
     T *xall = (T *)(smem + Ly.xall);
     T *acc = (T *)(smem + Ly.acc);
-    __shared__ int s_abort;
+    __shared__ int s_abort, s_role, s_own, s_row;
+    const int W = sp.W;
+    const int cid = (int)(blockIdx.x / (unsigned)CS) + 1;
     auto phys = [&](int l) { return lower ? l : nblk - 1 - l; };
+    // first tile of block row l that this chain streams
+    auto jlo = [&](int l) { return W > 0 && l > W ? l - W : 0; };
+    if (W > 0 && rank == 0 && t == 0) atomicCAS(sp.role, 0, cid);
+    for (int e = t; e < nblk * TB * NR; e += CL_THREADS) xall[e] = cl_marker<T>();
+    if (t == 0) s_abort = 0;
+    cluster.sync();   // every CTA's copy holds markers before anyone writes x into it
+    if (W > 0) {
+        if (t == 0) s_role = ld_acquire(sp.role);
+        __syncthreads();
+        if (s_role != cid) {   // a helper cluster: no DSMEM from here on
+            if constexpr (NR == 1)
+                split_helper<T>(n, nblk, A, rs, cs, lower, vec, X, ldx, xvec, sp, err, ring, s_row, s_abort);
+            return;
+        }
+    }
     // ring item (l, j): this warp's rows of tile A_lj (j < l) or of the
     // inverted diagonal block (j == l).  Each lane copies the same chunks
     // (row, 16-byte column chunk) of every item: their offsets are formed once.
@@ -507,15 +710,13 @@ __global__ void __launch_bounds__(CL_THREADS)
         }
     };
     // producer state: item (pl, pj) in consumption order
-    int pl = rank, pj = 0;
+    int pl = rank, pj = jlo(rank);
     auto advance = [&]() {
         if (++pj > pl) {
             pl += CS;
-            pj = 0;
+            pj = jlo(pl);
         }
     };
-    for (int e = t; e < nblk * TB * NR; e += CL_THREADS) xall[e] = cl_marker<T>();
-    if (t == 0) s_abort = 0;
     int produced = 0, consumed = 0;
     for (int i = 0; i < S - 1; i++) {
         if (pl < nblk) {
@@ -525,7 +726,6 @@ __global__ void __launch_bounds__(CL_THREADS)
         produced++;
         cp_async_commit();
     }
-    cluster.sync();   // every CTA's copy holds markers before anyone writes x into it
     // this warp's row r of a tile times x (sum over the 4 lanes of the row)
     auto rowdot = [&](const T *tile, const T *xv, T *p) {
 #pragma unroll
@@ -552,36 +752,71 @@ __global__ void __launch_bounds__(CL_THREADS)
         produced++;
         cp_async_commit();
     };
+    // this lane's entries of x_j (rows k = q + 4i) once none is the marker
+    // (bounded; the decision to give up is warp-wide)
+    auto wait_x = [&](int j, T (&xv)[TB / 4][NR]) -> bool {
+        const T *xj = xall + (size_t)phys(j) * TB * NR;
+        long long it = 0;
+        for (;;) {
+            bool pend = false;
+#pragma unroll
+            for (int i = 0; i < TB / 4; i++)
+#pragma unroll
+                for (int c = 0; c < NR; c++) {
+                    xv[i][c] = ld_volatile(xj + (q + 4 * i) * NR + c);
+                    pend |= cl_pending(xv[i][c]);
+                }
+            if (!__any_sync(0xffffffffu, pend)) return true;
+            const bool stop = ++it > CL_SPIN || *(volatile int *)&s_abort;
+            if (__any_sync(0xffffffffu, stop)) return false;
+            if (it > 64) __nanosleep(20);
+        }
+    };
     for (int l = rank; l < nblk; l += CS) {
         const i64 r0 = (i64)phys(l) * TB;
+        const bool helped = l > W && W > 0;
+        bool own = false;
+        if (helped) {
+            if (t == 0) s_own = atomicCAS(sp.rowst + l, 0, 1) == 0;
+            __syncthreads();
+            own = s_own != 0;
+        }
         if (q == 0)
 #pragma unroll
             for (int c = 0; c < NR; c++) acc[r * NR + c] = (r0 + r < n && c < nr) ? X[(r0 + r) * ldx + c] : T(0);
-        T p[NR];
+        T p[NR], pr[NR];   // pr: far sum of row r, subtracted at the next acc update
+#pragma unroll
+        for (int c = 0; c < NR; c++) pr[c] = T(0);
         bool bad = false;
-        for (int j = 0; j < l; j++) {
-            cp_async_wait<S - 2>();
-            // this lane's entries of x_j (rows k = q + 4i): wait until none is
-            // the marker any more (bounded)
-            const T *xj = xall + (size_t)phys(j) * TB * NR;
-            T xv[TB / 4][NR];
-            long long it = 0;
-            for (;;) {
-                bool pend = false;
+        if (helped && own) {   // no helper took this row: its far tiles, straight from A
+            for (int j = 0; j < l - W; j++) {
+                T xv[TB / 4][NR];
+                if (!wait_x(j, xv)) {
+                    bad = true;
+                    break;
+                }
+                const i64 c0 = (i64)phys(j) * TB, gr = r0 + r;
 #pragma unroll
-                for (int i = 0; i < TB / 4; i++)
+                for (int i = 0; i < TB / 4; i++) {
+                    const i64 gc = c0 + q + 4 * i;
+                    const T v = gr < n && gc < n ? A[gr * rs + gc * cs] : T(0);
 #pragma unroll
-                    for (int c = 0; c < NR; c++) {
-                        xv[i][c] = ld_volatile(xj + (q + 4 * i) * NR + c);
-                        pend |= cl_pending(xv[i][c]);
-                    }
-                if (!__any_sync(0xffffffffu, pend)) break;
-                // give up together: the decision is made warp-wide
-                const bool stop = ++it > CL_SPIN || *(volatile int *)&s_abort;
-                if (__any_sync(0xffffffffu, stop)) { bad = true; break; }
-                if (it > 64) __nanosleep(20);
+                    for (int c = 0; c < NR; c++) pr[c] += v * xv[i][c];
+                }
             }
-            if (bad) break;
+#pragma unroll
+            for (int c = 0; c < NR; c++) {
+                pr[c] += __shfl_xor_sync(0xffffffffu, pr[c], 1);
+                pr[c] += __shfl_xor_sync(0xffffffffu, pr[c], 2);
+            }
+        }
+        for (int j = jlo(l); j < l && !bad; j++) {
+            cp_async_wait<S - 2>();
+            T xv[TB / 4][NR];
+            if (!wait_x(j, xv)) {
+                bad = true;
+                break;
+            }
             __syncwarp();
             const T *tile = ring + (size_t)(consumed % S) * TB * CL_TLD;
 #pragma unroll
@@ -597,10 +832,34 @@ __global__ void __launch_bounds__(CL_THREADS)
                 p[c] += __shfl_xor_sync(0xffffffffu, p[c], 1);
                 p[c] += __shfl_xor_sync(0xffffffffu, p[c], 2);
             }
+            if (helped && !own && j == l - sp.PW) {
+                // this warp's rows of F_l, once the helper has released them
+                bool stop = false;
+                if (lane == 0) {
+                    long long it = 0;
+                    while (ld_acquire(sp.rowst + l) != 3) {
+                        if (++it > CL_SPIN || *(volatile int *)err != 0) {
+                            stop = true;
+                            break;
+                        }
+                        if (it > 16) __nanosleep(32);
+                    }
+                }
+                if (__shfl_sync(0xffffffffu, stop, 0)) {
+                    bad = true;
+                    break;
+                }
+                __syncwarp();
+                if (q == 0)
+#pragma unroll
+                    for (int c = 0; c < NR; c++) pr[c] += __ldcg(sp.part + ((size_t)l * TB + r) * NR + c);
+            }
             next_item();
             if (q == 0)
 #pragma unroll
-                for (int c = 0; c < NR; c++) acc[r * NR + c] -= p[c];
+                for (int c = 0; c < NR; c++) acc[r * NR + c] -= p[c] + pr[c];
+#pragma unroll
+            for (int c = 0; c < NR; c++) pr[c] = T(0);
         }
         if (bad && lane == 0) {
             atomicExch(err, 1);
@@ -623,6 +882,10 @@ __global__ void __launch_bounds__(CL_THREADS)
         if (q == 0 && r0 + r < n)
             for (int c = 0; c < nr; c++) X[(r0 + r) * ldx + c] = p[c];
         __syncthreads();   // acc is read above before the next block overwrites it
+        if (W > 0 && t == 0) {   // x_l is in X for the helpers
+            __threadfence();
+            st_release(sp.xflag + l, 1);
+        }
     }
     cp_async_wait<0>();
     __syncthreads();
@@ -678,14 +941,74 @@ int cluster_size(ddla_handle h, int nblk) {
     return c;
 }
 
+// Clusters of cs CTAs with `smem` bytes each that fit on the GPU at once.
+template <typename T, int NR>
+int active_clusters(int cs, size_t smem) {
+    static size_t last_smem = 0;
+    static int last_cs = 0, last_nc = 0;
+    if (smem == last_smem && cs == last_cs) return last_nc;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(cs);
+    cfg.blockDim = dim3(CL_THREADS);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = cs;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int nc = 0;
+    if (cudaOccupancyMaxActiveClusters(&nc, (const void *)k_trsv_cluster<T, NR>, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        nc = 0;
+    }
+    last_smem = smem;
+    last_cs = cs;
+    last_nc = nc;
+    return nc;
+}
+
+// One cluster, or (one right-hand side, a full cluster, far tiles to share)
+// the split solve: the chain cluster plus helper clusters, as many as run at
+// once and have block rows to take.  Tuning keys: trsv.split.w (near tiles
+// per block row, 0 = no split), trsv.split.pw (where the chain adds a row's
+// far sum), trsv.split.clusters (a cap on the clusters).
 template <typename T, int NR>
 int cluster_solve(ddla_handle h, int cs, i64 n, int nblk, View<const T> A, bool lower, const T *inv, T *X, i64 ldx,
                   int nr) {
     const bool vec = A.cs == 1 && (A.rs * (i64)sizeof(T)) % 16 == 0 && (((uintptr_t)A.p) & 15) == 0;
+    const int xvec = ldx == 1 && (((uintptr_t)X) & 15) == 0;
+    size_t smem = cl_layout<T, NR>(nblk).total;
+    SplitArgs<T> sp{};
+    int G = 1;
+    int W = NR == 1 && cs == CL_MAXCS ? (int)tune_get("trsv.split.w", 16) : 0;
+    if (W < 2 || nblk <= W + 1) W = 0;
+    if (W > 0) {
+        const size_t need = smem > sp_smem<T>() ? smem : sp_smem<T>();
+        const int rows = nblk - W - 1;   // block rows with far tiles
+        const int nc = need <= ClusterCfg<T, NR>::avail ? active_clusters<T, NR>(cs, need) : 0;
+        G = 1 + std::min(nc - 1, (rows + cs - 1) / cs);
+        const int cap = (int)tune_get("trsv.split.clusters", 0);
+        if (cap >= 1 && cap < G) G = cap;
+        if (G >= 2) {
+            int PW = (int)tune_get("trsv.split.pw", 6);
+            PW = PW < 1 ? 1 : (PW > W ? W : PW);
+            const size_t ib = (sizeof(int) * (2 * (size_t)nblk + 2) + 15) & ~(size_t)15;
+            char *w;
+            DDLA_TRY(workspace(h, WS_TRSV, ib + sizeof(T) * (size_t)nblk * TB, (void **)&w));
+            DDLA_CUDA(cudaMemsetAsync(w, 0, sizeof(int) * (2 * (size_t)nblk + 2), h->stream));
+            int *ints = (int *)w;
+            sp = SplitArgs<T>{ints, ints + nblk, ints + 2 * nblk, ints + 2 * nblk + 1, (T *)(w + ib), W, PW};
+            smem = need;
+        } else {
+            G = 1;
+        }
+    }
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(cs);
+    cfg.gridDim = dim3(cs * G);
     cfg.blockDim = dim3(CL_THREADS);
-    cfg.dynamicSmemBytes = cl_layout<T, NR>(nblk).total;
+    cfg.dynamicSmemBytes = smem;
     cfg.stream = h->stream;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -695,7 +1018,7 @@ int cluster_solve(ddla_handle h, int cs, i64 n, int nblk, View<const T> A, bool 
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     DDLA_CUDA(cudaLaunchKernelEx(&cfg, k_trsv_cluster<T, NR>, n, nblk, A.p, A.rs, A.cs, lower ? 1 : 0, vec ? 1 : 0,
-                                 inv, X, ldx, nr, h->d_info + INFO_TIMEOUT));
+                                 inv, X, ldx, nr, h->d_info + INFO_TIMEOUT, sp, xvec));
     count_launch();
     return 0;
 }
@@ -766,16 +1089,16 @@ int tri_inverse(ddla_handle h, bool lower, bool unit, View<const T> A, i64 n, T 
 template <typename T>
 int trsv_apply(ddla_handle h, bool lower, View<const T> A, i64 n, const T *inv, T *X, i64 ldx, int nr) {
     int nblk = (int)((n + TB - 1) / TB);
-    int *flags;
-    DDLA_TRY(workspace(h, WS_MISC, sizeof(int) * (size_t)(nblk + 1), (void **)&flags));
-    DDLA_CUDA(cudaMemsetAsync(flags, 0, sizeof(int) * (size_t)(nblk + 1), h->stream));
     if (nr <= 1) {
         // FP64 on 16 SMs is bounded by their FP64 units: past ~96 blocks the
         // chained solve over one CTA per block is faster
         const int cs = (sizeof(T) == 8 && nblk > 96) ? 0 : cluster_size<T, 1>(h, nblk);
         if (cs > 1 && nblk > 1) return cluster_solve<T, 1>(h, cs, n, nblk, A, lower, inv, X, ldx, nr);
-        return chain<T, 1>(h, n, nblk, A, lower, inv, X, ldx, nr, flags);
     }
+    int *flags;
+    DDLA_TRY(workspace(h, WS_MISC, sizeof(int) * (size_t)(nblk + 1), (void **)&flags));
+    DDLA_CUDA(cudaMemsetAsync(flags, 0, sizeof(int) * (size_t)(nblk + 1), h->stream));
+    if (nr <= 1) return chain<T, 1>(h, n, nblk, A, lower, inv, X, ldx, nr, flags);
     if (nr <= 2) return chain<T, 2>(h, n, nblk, A, lower, inv, X, ldx, nr, flags);
     if (nr <= 4) return chain<T, 4>(h, n, nblk, A, lower, inv, X, ldx, nr, flags);
     if (nr <= 8) return chain<T, 8>(h, n, nblk, A, lower, inv, X, ldx, nr, flags);

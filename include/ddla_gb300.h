@@ -150,7 +150,11 @@ int ddla_timing_read(int cls, double *total_ms, int64_t *launches, double *flops
  * pivoting FP32 panels), "trsv.cluster" (0 uses
  * the chained per-block triangular solve instead of the cluster solve),
  * "trsv.chain16" (0 keeps the 4-group chained solve for 9-16 right-hand sides),
- * "trsv.cluster.size", "refine.gmres" (0 = classical refinement for one
+ * "trsv.cluster.size", "trsv.split.w" (near tiles per block row that the
+ * one-right-hand-side cluster solve keeps on its chain while helper clusters
+ * sum the far tiles; 0 = one cluster), "trsv.split.pw" (the near tile at
+ * which the chain adds a row's far sum), "trsv.split.clusters" (cap on the
+ * clusters of the split solve), "refine.gmres" (0 = classical refinement for one
  * right-hand side), "refine.gmres.m" (GMRES restart length),
  * "refine.gmres.relax" (factor on GMRES's 2-norm stopping target; 0 =
  * min(16, sqrt(n) / 4)),

@@ -82,3 +82,67 @@ def test_chain16_vs_chain_vs_oracle(ddla, orc, n, nrhs):
                     autotune.tune_set("trsv.chain16", 1)
                 assert rel_max(x16, xo) <= 1e-12
                 assert rel_max(x4, xo) <= 1e-12
+
+
+_SPLIT_DEFAULTS = {"trsv.split.w": 16, "trsv.split.pw": 6, "trsv.split.clusters": 0}
+
+
+def _with_tune(setting, fn):
+    from ddla_gb300 import autotune
+    try:
+        for k, v in setting.items():
+            autotune.tune_set(k, v)
+        return fn()
+    finally:
+        for k in setting:
+            autotune.tune_set(k, _SPLIT_DEFAULTS[k])
+
+
+@pytest.mark.parametrize("n", [1500, 2051, 4096])
+@pytest.mark.parametrize("setting", [{}, {"trsv.split.w": 4, "trsv.split.pw": 2}, {"trsv.split.clusters": 2},
+                                     {"trsv.split.w": 24, "trsv.split.pw": 24}])
+def test_split_solve_vs_oracle(ddla, orc, n, setting):
+    """One right-hand side through the split solve: the chain cluster on the
+    tiles near the diagonal, helper clusters summing the far tiles.  Narrow
+    and wide near windows; with one helper cluster (clusters = 2) the chain
+    finds most rows untaken and sums them itself.  Against the oracle and the
+    one-cluster solve (trsv.split.w = 0); n = 2051 has unaligned rows (element
+    copies), n = 1500 few far rows."""
+    r = rng(n * 7 + len(setting))
+    for lower in (True, False):
+        for trans in (ddla.NO_TRANSPOSE, ddla.TRANSPOSE):
+            unit = trans == ddla.TRANSPOSE
+            A = _tri(r, n, lower, unit)
+            b = r.standard_normal((n, 1))
+            u = ddla.LOWER if lower else ddla.UPPER
+            d = ddla.UNIT if unit else ddla.NONUNIT
+            xo = b.copy()
+            orc.dtrsm(orc.LEFT, u, trans, d, 1.0, A, xo)
+
+            def run():
+                x = b.copy()
+                ddla.BlasProvider.TrSM(ddla.LEFT, u, trans, d, 1.0, A, x)
+                return x
+            xs = _with_tune(setting, run)
+            x1 = _with_tune({"trsv.split.w": 0}, run)
+            assert rel_max(xs, xo) <= 1e-12
+            assert rel_max(xs, x1) <= 1e-12
+
+
+@pytest.mark.parametrize("n", [3001, 4096])
+def test_split_solve_in_mixed_refinement(ddla, n):
+    """The FP32 correction solves of the mixed LU solve through the split
+    solve: the same solution and the same number of preconditioner
+    applications (within one) as with the one-cluster solve."""
+    from helpers import berr
+    r = rng(n + 11)
+    A = r.standard_normal((n, n))
+    b = r.standard_normal((n, 1))
+    xs, reps = _with_tune({}, lambda: ddla.solve_mixed(A, b))
+    x1, rep1 = _with_tune({"trsv.split.w": 0}, lambda: ddla.solve_mixed(A, b))
+    xc, repc = _with_tune({"trsv.split.clusters": 2}, lambda: ddla.solve_mixed(A, b))
+    for x, rep in ((xs, reps), (x1, rep1), (xc, repc)):
+        assert rep["converged"] and berr(A, x, b) <= 1e-14
+    assert abs(reps["iterations"] - rep1["iterations"]) <= 1
+    assert abs(repc["iterations"] - rep1["iterations"]) <= 1
+    assert rel_max(xs, x1) <= 1e-12
