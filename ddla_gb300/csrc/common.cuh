@@ -82,7 +82,7 @@ struct ddla_handle_s {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     // Growable device scratch areas (indexed by purpose).
-    ddla::Workspace ws[24];
+    ddla::Workspace ws[25];
     // Pinned host staging for host-pointer calls.
     void *pinned = nullptr;
     size_t pinned_bytes = 0;
@@ -116,11 +116,12 @@ namespace ddla {
 //   WS_BD2     two-stage bidiagonal reduction: block factors, chase reflectors
 //   WS_NEXT    LU look-ahead: the next panel's columns after the previous step
 //   WS_TRSV    split triangular solve: block flags, row states, far sums
+//   WS_TRSVM   cluster triangular solve: diagonal-block inverses times the last tiles
 enum WsSlot {
     WS_A = 0, WS_B = 1, WS_C = 2, WS_TMP = 3, WS_PIV = 4, WS_F32 = 5, WS_X = 6, WS_MISC = 7,
     WS_TRI = 8, WS_Y = 9, WS_PERM = 10, WS_TC = 11, WS_TC2 = 12, WS_INV = 13, WS_PINV = 14, WS_QR = 15,
     WS_SPLIT = 16, WS_QRU = 17, WS_TRD = 18, WS_TRDQ = 19, WS_RHS = 20, WS_BD2 = 21, WS_NEXT = 22,
-    WS_TRSV = 23
+    WS_TRSV = 23, WS_TRSVM = 24
 };
 
 // Order of the diagonal blocks that the triangular solves invert.
@@ -253,7 +254,12 @@ int bidiag2s(ddla_handle h, i64 m, i64 n, View<double> A, View<double> U, View<d
 template <typename T>
 int tri_inverse(ddla_handle h, bool lower, bool unit, View<const T> A, i64 n, T *inv);
 template <typename T>
-int trsv_apply(ddla_handle h, bool lower, View<const T> A, i64 n, const T *inv, T *X, i64 ldx, int nr);
+int trsv_apply(ddla_handle h, bool lower, View<const T> A, i64 n, const T *inv, T *X, i64 ldx, int nr,
+               const T *mlast = nullptr);
+// M_p = inv(A_pp) A_{p,p-1} (lower) or inv(A_pp) A_{p,p+1} (upper), TB x TB per
+// block row, for trsv_apply's one-right-hand-side cluster solve.
+template <typename T>
+int tri_mlast(ddla_handle h, bool lower, View<const T> A, i64 n, const T *inv, T *M);
 // Y = X element by element (any strides; trsm.cu).
 template <typename T>
 int copy2d_on(cudaStream_t s, View<const T> X, View<T> Y);

@@ -569,22 +569,29 @@ int mixed_solve(ddla_handle h, int kind, int uplo, i64 n, i64 nrhs, const double
     const View<const float> Uv = kind == MIX_LU ? Fc : Lv.t();
     const bool unit_l = kind != MIX_CHOL, unit_u = kind == MIX_LDLT;
     const i64 nblk = (n + TRI_TB - 1) / TRI_TB;
-    float *invL, *invU;
-    DDLA_TRY(workspace(h, WS_INV, sizeof(float) * 2 * (size_t)nblk * TRI_TB * TRI_TB, (void **)&invL));
-    invU = invL + (size_t)nblk * TRI_TB * TRI_TB;
+    float *invL, *invU, *mL = nullptr, *mU = nullptr;
+    const size_t blk = (size_t)nblk * TRI_TB * TRI_TB;
+    DDLA_TRY(workspace(h, WS_INV, sizeof(float) * (nr0 <= 1 ? 4 : 2) * blk, (void **)&invL));
+    invU = invL + blk;
     DDLA_TRY(tri_inverse<float>(h, true, unit_l, Lv, n, invL));
     DDLA_TRY(tri_inverse<float>(h, false, unit_u, Uv, n, invU));
+    if (nr0 <= 1) {   // one right-hand side: the cluster solves' last-tile products, formed once
+        mL = invU + blk;
+        mU = mL + blk;
+        DDLA_TRY(tri_mlast<float>(h, true, Lv, n, invL, mL));
+        DDLA_TRY(tri_mlast<float>(h, false, Uv, n, invU, mU));
+    }
     int nr = nr0;
     // d <- U^-1 (D^-1) L^-1 (P) d with the FP32 factors, nr columns
     auto solve32 = [&](float *d) -> int {
         Timed t(s, TC_SOLVE, 2.0 * n * n * nr, 4.0 * n * n);
         if (kind == MIX_LU) DDLA_TRY(permute_rows<float>(h, View<float>{d, n, nr, nr, 1}, perm, n, true));
-        DDLA_TRY(trsv_apply<float>(h, true, Lv, n, invL, d, nr, nr));
+        DDLA_TRY(trsv_apply<float>(h, true, Lv, n, invL, d, nr, nr, nr <= 1 ? mL : nullptr));
         if (kind == MIX_LDLT) {
             k_rows_by_diag<<<grid1(n * nr), 256, 0, s>>>(d, n, nr, A32, n + 1);
             DDLA_LAUNCHED();
         }
-        return trsv_apply<float>(h, false, Uv, n, invU, d, nr, nr);
+        return trsv_apply<float>(h, false, Uv, n, invU, d, nr, nr, nr <= 1 ? mU : nullptr);
     };
     DDLA_CUDA(cudaEventRecord(h->ev0, s));
     int rc = 0;

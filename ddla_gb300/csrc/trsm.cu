@@ -627,7 +627,8 @@ __device__ void split_helper(i64 n, int nblk, const T *__restrict__ A, i64 rs, i
 template <typename T, int NR>
 __global__ void __launch_bounds__(CL_THREADS)
     k_trsv_cluster(i64 n, int nblk, const T *__restrict__ A, i64 rs, i64 cs, int lower, int vec,
-                   const T *__restrict__ inv, T *X, i64 ldx, int nr, int *err, SplitArgs<T> sp, int xvec) {
+                   const T *__restrict__ inv, const T *__restrict__ mlast, T *X, i64 ldx, int nr, int *err,
+                   SplitArgs<T> sp, int xvec) {
     namespace cg = cooperative_groups;
     cg::cluster_group cluster = cg::this_cluster();
     constexpr int S = ClStages<T>::value;
@@ -640,6 +641,7 @@ __global__ void __launch_bounds__(CL_THREADS)
     T *acc = (T *)(smem + Ly.acc);
     __shared__ int s_abort, s_role, s_own, s_row;
     const int W = sp.W;
+    const bool fused = mlast != nullptr;
     const int cid = (int)(blockIdx.x / (unsigned)CS) + 1;
     auto phys = [&](int l) { return lower ? l : nblk - 1 - l; };
     // first tile of block row l that this chain streams
@@ -672,10 +674,13 @@ __global__ void __launch_bounds__(CL_THREADS)
         c_col[i] = (e % CPR) * EPC;
         c_goff[i] = (i64)c_row[i] * rs + c_col[i];
     }
+    // item j of block row l: a tile (j below the last), the inverted diagonal
+    // block, then (fused) M_l; contiguous TB x TB blocks are 16-byte aligned
     auto issue = [&](int l, int j, int stage) {
         T *dst = ring + (size_t)stage * TB * CL_TLD;
-        if (j == l) {   // inverse block: contiguous TB x TB, 16-byte aligned
-            const T *src = inv + (i64)phys(l) * TB * TB;
+        const bool is_inv = fused && l > 0 ? j == l - 1 : j == l;
+        if (is_inv || (fused && j == l)) {
+            const T *src = (is_inv ? inv : mlast) + (i64)phys(l) * TB * TB;
 #pragma unroll
             for (int i = 0; i < CPL; i++)
                 cp_async16(dst + c_row[i] * CL_TLD + c_col[i], src + c_row[i] * TB + c_col[i], 16);
@@ -810,7 +815,9 @@ __global__ void __launch_bounds__(CL_THREADS)
                 pr[c] += __shfl_xor_sync(0xffffffffu, pr[c], 2);
             }
         }
-        for (int j = jlo(l); j < l && !bad; j++) {
+        // tiles: all before the diagonal, or (fused) all but the last
+        const int jend = fused && l > 0 ? l - 1 : l;
+        for (int j = jlo(l); j < jend && !bad; j++) {
             cp_async_wait<S - 2>();
             T xv[TB / 4][NR];
             if (!wait_x(j, xv)) {
@@ -871,17 +878,53 @@ __global__ void __launch_bounds__(CL_THREADS)
         __syncwarp();
         rowdot(ring + (size_t)(consumed % S) * TB * CL_TLD, acc, p);   // x_l = inv(A_ll) acc
         next_item();
+        bool fail = false;
+        if (fused && l > 0) {
+            // x_l = inv(A_ll) acc - M_l x_{l-1}: each warp finishes its own rows
+            // as soon as x_{l-1} is in, with no CTA barrier on the chain
+            cp_async_wait<S - 2>();
+            T xv[TB / 4][NR];
+            if (!wait_x(l - 1, xv)) {
+                fail = true;
+                if (lane == 0) {
+                    atomicExch(err, 1);
+                    s_abort = 1;
+                }
+            } else {
+                __syncwarp();
+                const T *mt = ring + (size_t)(consumed % S) * TB * CL_TLD;
+                T d[NR];
+#pragma unroll
+                for (int c = 0; c < NR; c++) d[c] = T(0);
+#pragma unroll
+                for (int i = 0; i < TB / 4; i++) {
+                    const T v = mt[r * CL_TLD + q + 4 * i];
+#pragma unroll
+                    for (int c = 0; c < NR; c++) d[c] += v * xv[i][c];
+                }
+#pragma unroll
+                for (int c = 0; c < NR; c++) {
+                    d[c] += __shfl_xor_sync(0xffffffffu, d[c], 1);
+                    d[c] += __shfl_xor_sync(0xffffffffu, d[c], 2);
+                    p[c] -= d[c];
+                }
+            }
+            next_item();
+        }
         // publish x_l: the 4 lanes of row r each store it into a quarter of
         // the CTAs' copies (plain DSMEM stores; the values mark themselves)
         const int pb = phys(l);
-        for (int dst = q; dst < CS; dst += 4) {
-            T *xd = cluster.map_shared_rank(xall, dst) + (size_t)pb * TB * NR + r * NR;
+        if (!fail) {
+            for (int dst = q; dst < CS; dst += 4) {
+                T *xd = cluster.map_shared_rank(xall, dst) + (size_t)pb * TB * NR + r * NR;
 #pragma unroll
-            for (int c = 0; c < NR; c++) xd[c] = p[c];
+                for (int c = 0; c < NR; c++) xd[c] = p[c];
+            }
+            if (q == 0 && r0 + r < n)
+                for (int c = 0; c < nr; c++) X[(r0 + r) * ldx + c] = p[c];
         }
-        if (q == 0 && r0 + r < n)
-            for (int c = 0; c < nr; c++) X[(r0 + r) * ldx + c] = p[c];
         __syncthreads();   // acc is read above before the next block overwrites it
+        if (s_abort) break;
         if (W > 0 && t == 0) {   // x_l is in X for the helpers
             __threadfence();
             st_release(sp.xflag + l, 1);
@@ -975,8 +1018,8 @@ int active_clusters(int cs, size_t smem) {
 // per block row, 0 = no split), trsv.split.pw (where the chain adds a row's
 // far sum), trsv.split.clusters (a cap on the clusters).
 template <typename T, int NR>
-int cluster_solve(ddla_handle h, int cs, i64 n, int nblk, View<const T> A, bool lower, const T *inv, T *X, i64 ldx,
-                  int nr) {
+int cluster_solve(ddla_handle h, int cs, i64 n, int nblk, View<const T> A, bool lower, const T *inv, const T *mlast,
+                  T *X, i64 ldx, int nr) {
     const bool vec = A.cs == 1 && (A.rs * (i64)sizeof(T)) % 16 == 0 && (((uintptr_t)A.p) & 15) == 0;
     const int xvec = ldx == 1 && (((uintptr_t)X) & 15) == 0;
     size_t smem = cl_layout<T, NR>(nblk).total;
@@ -993,7 +1036,8 @@ int cluster_solve(ddla_handle h, int cs, i64 n, int nblk, View<const T> A, bool 
         if (cap >= 1 && cap < G) G = cap;
         if (G >= 2) {
             int PW = (int)tune_get("trsv.split.pw", 6);
-            PW = PW < 1 ? 1 : (PW > W ? W : PW);
+            const int pmin = mlast ? 2 : 1;   // fused: the last tile is not a tile step
+            PW = PW < pmin ? pmin : (PW > W ? W : PW);
             const size_t ib = (sizeof(int) * (2 * (size_t)nblk + 2) + 15) & ~(size_t)15;
             char *w;
             DDLA_TRY(workspace(h, WS_TRSV, ib + sizeof(T) * (size_t)nblk * TB, (void **)&w));
@@ -1018,7 +1062,7 @@ int cluster_solve(ddla_handle h, int cs, i64 n, int nblk, View<const T> A, bool 
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     DDLA_CUDA(cudaLaunchKernelEx(&cfg, k_trsv_cluster<T, NR>, n, nblk, A.p, A.rs, A.cs, lower ? 1 : 0, vec ? 1 : 0,
-                                 inv, X, ldx, nr, h->d_info + INFO_TIMEOUT, sp, xvec));
+                                 inv, mlast, X, ldx, nr, h->d_info + INFO_TIMEOUT, sp, xvec));
     count_launch();
     return 0;
 }
@@ -1084,16 +1128,74 @@ int tri_inverse(ddla_handle h, bool lower, bool unit, View<const T> A, i64 n, T 
     return tri_inverse_on<T>(h->stream, lower, unit, A, n, inv);
 }
 
-// Solve tri(A) X = X in place for X row-major (n x nr, leading dim ldx),
-// nr <= 16, with the precomputed diagonal-block inverses.
+namespace {
+// M_p = inv(A_pp) A_{p,p-1} (lower) or inv(A_pp) A_{p,p+1} (upper) for every
+// block row p with that neighbour, TB x TB row-major at M + p TB^2: the last
+// tile before a block's diagonal premultiplied by the block's inverse, so the
+// cluster solve ends each block with one product once the previous block's x
+// is in (x_l = inv(A_ll) acc - M_l x_{l-1}).  One CTA per block row; thread t
+// forms row t / 4, columns t % 4 + 4 c.
 template <typename T>
-int trsv_apply(ddla_handle h, bool lower, View<const T> A, i64 n, const T *inv, T *X, i64 ldx, int nr) {
+__global__ void __launch_bounds__(256) k_tri_mlast(const T *A, i64 rs, i64 cs, i64 n, int lower, const T *inv, T *M) {
+    __shared__ T sA[TB][TB];
+    const int p = lower ? blockIdx.x + 1 : blockIdx.x;
+    const i64 r0 = (i64)p * TB, c0 = (i64)(lower ? p - 1 : p + 1) * TB;
+    for (int e = threadIdx.x; e < TB * TB; e += 256) {
+        const int i = e / TB, k = e % TB;
+        const i64 gr = r0 + i, gc = c0 + k;
+        sA[i][k] = gr < n && gc < n ? A[gr * rs + gc * cs] : T(0);
+    }
+    __syncthreads();
+    const int i = threadIdx.x >> 2, k0 = threadIdx.x & 3;
+    const T *iv = inv + (i64)p * TB * TB + (i64)i * TB;
+    T out[TB / 4];
+#pragma unroll
+    for (int c = 0; c < TB / 4; c++) out[c] = T(0);
+    for (int m = 0; m < TB; m++) {
+        const T a = __ldg(iv + m);
+#pragma unroll
+        for (int c = 0; c < TB / 4; c++) out[c] += a * sA[m][k0 + 4 * c];
+    }
+    T *dst = M + (i64)p * TB * TB + (i64)i * TB;
+#pragma unroll
+    for (int c = 0; c < TB / 4; c++) dst[k0 + 4 * c] = out[c];
+}
+}  // namespace
+
+template <typename T>
+int tri_mlast(ddla_handle h, bool lower, View<const T> A, i64 n, const T *inv, T *M) {
+    const int nblk = (int)((n + TB - 1) / TB);
+    if (nblk < 2) return 0;
+    k_tri_mlast<T><<<nblk - 1, 256, 0, h->stream>>>(A.p, A.rs, A.cs, n, lower ? 1 : 0, inv, M);
+    DDLA_LAUNCHED();
+    return 0;
+}
+template int tri_mlast<double>(ddla_handle, bool, View<const double>, i64, const double *, double *);
+template int tri_mlast<float>(ddla_handle, bool, View<const float>, i64, const float *, float *);
+
+// Solve tri(A) X = X in place for X row-major (n x nr, leading dim ldx),
+// nr <= 16, with the precomputed diagonal-block inverses (and, for one
+// right-hand side, the products tri_mlast forms: made here when not given;
+// tuning key trsv.fused = 0 solves without them).
+template <typename T>
+int trsv_apply(ddla_handle h, bool lower, View<const T> A, i64 n, const T *inv, T *X, i64 ldx, int nr,
+               const T *mlast) {
     int nblk = (int)((n + TB - 1) / TB);
     if (nr <= 1) {
         // FP64 on 16 SMs is bounded by their FP64 units: past ~96 blocks the
         // chained solve over one CTA per block is faster
         const int cs = (sizeof(T) == 8 && nblk > 96) ? 0 : cluster_size<T, 1>(h, nblk);
-        if (cs > 1 && nblk > 1) return cluster_solve<T, 1>(h, cs, n, nblk, A, lower, inv, X, ldx, nr);
+        if (cs > 1 && nblk > 1) {
+            if (tune_get("trsv.fused", 1) == 0) {
+                mlast = nullptr;
+            } else if (!mlast) {
+                T *m;
+                DDLA_TRY(workspace(h, WS_TRSVM, sizeof(T) * (size_t)nblk * TB * TB, (void **)&m));
+                DDLA_TRY(tri_mlast<T>(h, lower, A, n, inv, m));
+                mlast = m;
+            }
+            return cluster_solve<T, 1>(h, cs, n, nblk, A, lower, inv, mlast, X, ldx, nr);
+        }
     }
     int *flags;
     DDLA_TRY(workspace(h, WS_MISC, sizeof(int) * (size_t)(nblk + 1), (void **)&flags));
@@ -1171,8 +1273,10 @@ template int trsm<double>(ddla_handle, int, int, int, int, i64, i64, double, Vie
 template int trsm<float>(ddla_handle, int, int, int, int, i64, i64, float, View<const float>, View<float>);
 template int tri_inverse<double>(ddla_handle, bool, bool, View<const double>, i64, double *);
 template int tri_inverse<float>(ddla_handle, bool, bool, View<const float>, i64, float *);
-template int trsv_apply<double>(ddla_handle, bool, View<const double>, i64, const double *, double *, i64, int);
-template int trsv_apply<float>(ddla_handle, bool, View<const float>, i64, const float *, float *, i64, int);
+template int trsv_apply<double>(ddla_handle, bool, View<const double>, i64, const double *, double *, i64, int,
+                                const double *);
+template int trsv_apply<float>(ddla_handle, bool, View<const float>, i64, const float *, float *, i64, int,
+                               const float *);
 
 }  // namespace ddla
 

@@ -84,7 +84,7 @@ def test_chain16_vs_chain_vs_oracle(ddla, orc, n, nrhs):
                 assert rel_max(x4, xo) <= 1e-12
 
 
-_SPLIT_DEFAULTS = {"trsv.split.w": 16, "trsv.split.pw": 6, "trsv.split.clusters": 0}
+_SPLIT_DEFAULTS = {"trsv.split.w": 16, "trsv.split.pw": 6, "trsv.split.clusters": 0, "trsv.fused": 1}
 
 
 def _with_tune(setting, fn):
@@ -100,14 +100,17 @@ def _with_tune(setting, fn):
 
 @pytest.mark.parametrize("n", [1500, 2051, 4096])
 @pytest.mark.parametrize("setting", [{}, {"trsv.split.w": 4, "trsv.split.pw": 2}, {"trsv.split.clusters": 2},
-                                     {"trsv.split.w": 24, "trsv.split.pw": 24}])
+                                     {"trsv.split.w": 24, "trsv.split.pw": 24}, {"trsv.fused": 0},
+                                     {"trsv.fused": 0, "trsv.split.pw": 1}])
 def test_split_solve_vs_oracle(ddla, orc, n, setting):
     """One right-hand side through the split solve: the chain cluster on the
     tiles near the diagonal, helper clusters summing the far tiles.  Narrow
     and wide near windows; with one helper cluster (clusters = 2) the chain
-    finds most rows untaken and sums them itself.  Against the oracle and the
-    one-cluster solve (trsv.split.w = 0); n = 2051 has unaligned rows (element
-    copies), n = 1500 few far rows."""
+    finds most rows untaken and sums them itself; without the last-tile
+    products (trsv.fused = 0) every block takes its last tile and its inverse
+    after the previous x.  Against the oracle and the one-cluster solve
+    (trsv.split.w = 0); n = 2051 has unaligned rows (element copies), n = 1500
+    few far rows."""
     r = rng(n * 7 + len(setting))
     for lower in (True, False):
         for trans in (ddla.NO_TRANSPOSE, ddla.TRANSPOSE):
@@ -132,8 +135,9 @@ def test_split_solve_vs_oracle(ddla, orc, n, setting):
 @pytest.mark.parametrize("n", [3001, 4096])
 def test_split_solve_in_mixed_refinement(ddla, n):
     """The FP32 correction solves of the mixed LU solve through the split
-    solve: the same solution and the same number of preconditioner
-    applications (within one) as with the one-cluster solve."""
+    solve (with and without the last-tile products, with few helpers): the
+    same solution and the same number of preconditioner applications (within
+    one) as with the one-cluster solve."""
     from helpers import berr
     r = rng(n + 11)
     A = r.standard_normal((n, n))
@@ -141,8 +145,9 @@ def test_split_solve_in_mixed_refinement(ddla, n):
     xs, reps = _with_tune({}, lambda: ddla.solve_mixed(A, b))
     x1, rep1 = _with_tune({"trsv.split.w": 0}, lambda: ddla.solve_mixed(A, b))
     xc, repc = _with_tune({"trsv.split.clusters": 2}, lambda: ddla.solve_mixed(A, b))
-    for x, rep in ((xs, reps), (x1, rep1), (xc, repc)):
+    xf, repf = _with_tune({"trsv.fused": 0}, lambda: ddla.solve_mixed(A, b))
+    for x, rep in ((xs, reps), (x1, rep1), (xc, repc), (xf, repf)):
         assert rep["converged"] and berr(A, x, b) <= 1e-14
-    assert abs(reps["iterations"] - rep1["iterations"]) <= 1
-    assert abs(repc["iterations"] - rep1["iterations"]) <= 1
+    for rep in (reps, repc, repf):
+        assert abs(rep["iterations"] - rep1["iterations"]) <= 1
     assert rel_max(xs, x1) <= 1e-12
