@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "convert.cuh"
 #include "timing.cuh"
 
 namespace ddla {
@@ -73,40 +74,72 @@ __global__ void k_colmax_abs(const double *X, i64 n, int nr, unsigned long long 
 
 // The FP32 copy of A (row-major n x n) and, in the same pass over A,
 // ||A||_inf (out[0]) and max |a_ij| (out[1], NaN ignored), as bit patterns of
-// non-negative doubles.  One warp per row.
+// non-negative doubles.  One warp per row.  No FP64 arithmetic per entry (it
+// runs at 1/64 of the FP32 rate on GB300): the copy is rounded on the integer
+// pipes (d2f_bits), max |a_ij| is an integer max of the FP64 bit patterns
+// (exact), and the row sums add FP32 partial sums of 16 magnitudes of the
+// FP32 copy into FP64 (relative error below 1e-6).  A row with an entry beyond
+// the FP32 range (an infinite copy) is summed again in FP64.
 __global__ void k_d2s_norms(i64 n, const double *A, i64 lda, float *A32, unsigned long long *out) {
     const int lane = threadIdx.x & 31;
     const i64 row = (blockIdx.x * (i64)blockDim.x + threadIdx.x) >> 5;
     if (row >= n) return;
-    double s = 0.0, mx = 0.0;
+    double s = 0.0;
+    float fs = 0.f;   // partial sum of up to 16 magnitudes
+    int cnt = 0;
+    unsigned long long mx = 0;
+    bool wide = false;
     const double *a = A + row * lda;
     float *y = A32 + row * n;
+    // the FP32 copy of one entry; its magnitude goes to the partial sum
+    auto conv = [&](double v) -> float {
+        const unsigned long long b = (unsigned long long)__double_as_longlong(v), ab = b & 0x7FFFFFFFFFFFFFFFull;
+        const unsigned f = d2f_bits(b);
+        if (ab <= 0x7FF0000000000000ull) mx = ab > mx ? ab : mx;
+        wide |= ab < 0x7FF0000000000000ull && (f & 0x7FFFFFFFu) == 0x7F800000u;
+        return __uint_as_float(f);
+    };
     if ((n & 3) == 0 && (lda & 3) == 0 && ((((uintptr_t)A) | ((uintptr_t)A32)) & 31) == 0) {
         // 4 consecutive entries per lane: two 16-byte loads, one 16-byte store
 #pragma unroll 2
         for (i64 j = 4 * lane; j < n; j += 128) {
             const double2 v0 = *reinterpret_cast<const double2 *>(a + j);
             const double2 v1 = *reinterpret_cast<const double2 *>(a + j + 2);
-            *reinterpret_cast<float4 *>(y + j) = make_float4((float)v0.x, (float)v0.y, (float)v1.x, (float)v1.y);
-            s += (fabs(v0.x) + fabs(v0.y)) + (fabs(v1.x) + fabs(v1.y));
-            mx = fmax(fmax(mx, fmax(fabs(v0.x), fabs(v0.y))), fmax(fabs(v1.x), fabs(v1.y)));
+            const float f0 = conv(v0.x), f1 = conv(v0.y), f2 = conv(v1.x), f3 = conv(v1.y);
+            *reinterpret_cast<float4 *>(y + j) = make_float4(f0, f1, f2, f3);
+            fs += (fabsf(f0) + fabsf(f1)) + (fabsf(f2) + fabsf(f3));
+            if (++cnt == 4) {
+                s += (double)fs;
+                fs = 0.f;
+                cnt = 0;
+            }
         }
     } else {
 #pragma unroll 4
         for (i64 j = lane; j < n; j += 32) {
-            const double v = a[j];
-            y[j] = (float)v;
-            s += fabs(v);
-            mx = fmax(mx, fabs(v));
+            const float f = conv(a[j]);
+            y[j] = f;
+            fs += fabsf(f);
+            if (++cnt == 16) {
+                s += (double)fs;
+                fs = 0.f;
+                cnt = 0;
+            }
         }
+    }
+    s += (double)fs;
+    if (__any_sync(0xffffffffu, wide)) {
+        s = 0.0;
+        for (i64 j = lane; j < n; j += 32) s += fabs(a[j]);
     }
     for (int off = 16; off > 0; off >>= 1) {
         s += __shfl_down_sync(0xffffffffu, s, off);
-        mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, off));
+        const unsigned long long o = __shfl_down_sync(0xffffffffu, mx, off);
+        mx = o > mx ? o : mx;
     }
     if (lane == 0) {
         atomicMax(&out[0], (unsigned long long)__double_as_longlong(s));
-        if (mx == mx) atomicMax(&out[1], (unsigned long long)__double_as_longlong(mx));
+        atomicMax(&out[1], mx);
     }
 }
 
@@ -442,8 +475,26 @@ __global__ void k_growth(const float *F, i64 rs, i64 cs, i64 n, int kind, unsign
     if (i >= n) return;
     double v = 0.0;
     if (kind == 0) {
-        for (i64 j = i + lane; j < n; j += 32) v = fmax(v, fabs((double)F[i * rs + j * cs]));
-        for (int off = 16; off > 0; off >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, off));
+        // the largest magnitude of FP32 values, taken in FP32: exact
+        float w = 0.f;
+        const float *fr = F + i * rs;
+        i64 j = i + lane;
+        if (cs == 1 && ((((uintptr_t)fr) & 15) == 0)) {
+            const i64 j4 = (i + 3) & ~(i64)3;   // first 16-byte-aligned column at or after i
+            if (j < j4 && j < n) w = fabsf(fr[j]);
+            for (i64 q = j4 + 4 * lane; q < n; q += 128) {
+                if (q + 4 <= n) {
+                    const float4 u = *reinterpret_cast<const float4 *>(fr + q);
+                    w = fmaxf(fmaxf(w, fmaxf(fabsf(u.x), fabsf(u.y))), fmaxf(fabsf(u.z), fabsf(u.w)));
+                } else {
+                    for (i64 t = q; t < n; t++) w = fmaxf(w, fabsf(fr[t]));
+                }
+            }
+        } else {
+            for (; j < n; j += 32) w = fmaxf(w, fabsf(fr[j * cs]));
+        }
+        for (int off = 16; off > 0; off >>= 1) w = fmaxf(w, __shfl_down_sync(0xffffffffu, w, off));
+        v = (double)w;
     } else {
         const i64 kend = kind == 1 ? i + 1 : i;
         for (i64 k = lane; k < kend; k += 32) {
