@@ -58,7 +58,7 @@ enum {
     DDLA_ERR_NOMEM = -1002,         /* device or pinned allocation failed */
     DDLA_ERR_TIMEOUT = -1003,       /* a bounded device-side wait gave up */
     DDLA_ERR_NOT_CONVERGED = -1004, /* iterative refinement hit max_iter */
-    DDLA_ERR_UNSUPPORTED = -1005,   /* valid request this build does not cover */
+    DDLA_ERR_UNSUPPORTED = -1005,   /* valid request the library does not cover */
     DDLA_ERR_NO_DEVICE = -1006      /* no usable sm_103 device */
 };
 
